@@ -1,0 +1,210 @@
+/*
+ * sgmev.h — C ABI of the GB300 (sm_103a) multi-evaluation library libsgpp_gb300.so.
+ *
+ * The library computes SG++'s OperationMultipleEval products for the piecewise-linear hat
+ * basis on Linear (no-boundary) sparse grids, on the GPU:
+ *
+ *   mult           result_j = sum_i alpha_i  prod_t max(1 - |2^{l_it} x_jt - i_it|, 0)
+ *   multTranspose  result_i = sum_j source_j prod_t max(1 - |2^{l_it} x_jt - i_it|, 0)
+ *
+ * All entry points take plain host pointers (or, for the *_device variants, device pointers)
+ * and sizes; none uses C++ or torch types. Every function returns SGMEV_OK (0) or a negative
+ * status; sgmev_last_error() then returns a message for the calling thread. No entry point
+ * calls exit() or aborts.
+ *
+ * Threading: one op handle per host thread at a time (like the reference operators, which are
+ * driven by single-threaded callers). Each handle owns a CUDA stream unless one is set with
+ * sgmev_set_stream().
+ *
+ * Layouts are the reference's own, so a maintainer passes SG++ buffers unchanged:
+ *   level_pow2, index : [n_grid x dim] row-major doubles, 2^l and i
+ *                       (HashGridStorage::getLevelIndexArraysForEval,
+ *                        base/src/sgpp/base/grid/storage/hashmap/HashGridStorage.cpp:433-450)
+ *   data              : [n_data x dim] row-major doubles (base::DataMatrix, DataMatrix.hpp:28)
+ *   vectors           : contiguous doubles (base::DataVector)
+ */
+#ifndef SGMEV_H_
+#define SGMEV_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SGMEV_API __attribute__((visibility("default")))
+#else
+#define SGMEV_API
+#endif
+
+/* ---- status codes -------------------------------------------------------------------- */
+#define SGMEV_OK 0
+#define SGMEV_ERR_INVALID (-1)     /* bad argument (null pointer, size, layout) */
+#define SGMEV_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define SGMEV_ERR_NO_DEVICE (-3)   /* no CUDA device visible */
+#define SGMEV_ERR_UNSUPPORTED (-4) /* combination not supported (e.g. non-hat grid type) */
+#define SGMEV_ERR_NOT_CONVERGED (-5)
+#define SGMEV_ERR_OOM (-6)         /* device allocation failed */
+
+/* ---- precision of the evaluation kernels ---------------------------------------------- */
+#define SGMEV_FP64 0 /* native double: the plain FP64 path (parity 1e-12 vs the reference) */
+#define SGMEV_FP32 1 /* single-precision hat products and tile sums; FP64 cross-tile sums */
+
+typedef struct sgmev_op sgmev_op;
+
+/* Message of the last failing call on this thread ("" if none). Never NULL. */
+SGMEV_API const char* sgmev_last_error(void);
+
+/* Library/ABI version, e.g. 10000 for 1.0.0. */
+SGMEV_API int sgmev_version(void);
+
+/* Number of visible CUDA devices (0 if none); never fails. */
+SGMEV_API int sgmev_device_count(void);
+
+/*
+ * Create an operator for one grid and one data set; replaces
+ *   sgpp::op_factory::createOperationMultipleEval(Grid&, DataMatrix&, OperationMultipleEvalConfiguration&)
+ *   datadriven/src/sgpp/datadriven/DatadrivenOpFactory.cpp:409-552 (new branch: Linear grid,
+ *   STREAMING type, CUDA subtype) and the operator constructor
+ *   datadriven/.../OperationMultiEvalStreaming/OperationMultiEvalStreaming.cpp:13-25.
+ * The data are copied to the device once (dim-major, padded), as the reference operator copies
+ * and transposes its dataset; the caller's buffers may be freed afterwards.
+ * bb_left/bb_right: optional bounding box ([dim] each, both NULL for the unit cube); data are
+ * mapped by (x - left) / (right - left) as BoundingBox::transformPointToUnitCube
+ * (base/src/sgpp/base/grid/common/BoundingBox.hpp:223-227).
+ * precision: SGMEV_FP64 or SGMEV_FP32. params_json: optional tuning knobs (may be NULL).
+ */
+SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double* level_pow2,
+                           const double* index, int64_t n_data, const double* data,
+                           const double* bb_left, const double* bb_right, int precision,
+                           const char* params_json);
+
+/* Destroy the operator and free its device memory. NULL is accepted. */
+SGMEV_API int sgmev_destroy(sgmev_op* op);
+
+/*
+ * Re-stage the grid after it changed (refinement appends points); replaces
+ *   OperationMultipleEval::prepare()  base/src/sgpp/base/operation/hash/OperationMultipleEval.hpp:118
+ *   (STREAMING: recalculateLevelAndIndex, OperationMultiEvalStreaming.cpp:145-156,181).
+ */
+SGMEV_API int sgmev_prepare(sgmev_op* op, int64_t n_grid, const double* level_pow2,
+                            const double* index);
+
+/* Sizes of the staged problem. */
+SGMEV_API int sgmev_get_sizes(const sgmev_op* op, int* dim, int64_t* n_grid, int64_t* n_data);
+
+/*
+ * result[n_data] = B alpha[n_grid]; replaces OperationMultipleEval::mult(alpha, result)
+ *   OperationMultipleEval.hpp:55. Host buffers; blocks until the result is in `result`.
+ */
+SGMEV_API int sgmev_mult(sgmev_op* op, const double* alpha, double* result);
+
+/*
+ * result[n_grid] = B^T source[n_data]; replaces OperationMultipleEval::multTranspose
+ *   OperationMultipleEval.hpp:81. Host buffers; blocks until done.
+ */
+SGMEV_API int sgmev_mult_transpose(sgmev_op* op, const double* source, double* result);
+
+/*
+ * Ranged variants; replace OperationMultipleEval.hpp:70-73 (data range of mult) and :97-100
+ * (grid range of multTranspose). result is the full-length vector; only
+ * result[start..end) is written.
+ */
+SGMEV_API int sgmev_mult_range(sgmev_op* op, const double* alpha, double* result,
+                               int64_t start_data, int64_t end_data);
+SGMEV_API int sgmev_mult_transpose_range(sgmev_op* op, const double* source, double* result,
+                                         int64_t start_grid, int64_t end_grid);
+
+/*
+ * Device-resident variants: the same products on device pointers (doubles), enqueued on the
+ * op's stream; they return without synchronising. For callers that keep vectors on the GPU.
+ */
+SGMEV_API int sgmev_mult_device(sgmev_op* op, const double* d_alpha, double* d_result);
+SGMEV_API int sgmev_mult_transpose_device(sgmev_op* op, const double* d_source,
+                                          double* d_result);
+
+/*
+ * System matrix of the least-squares regression, applied on the device:
+ *   result = B^T (B alpha) + lambda_times_m * alpha
+ * replaces SystemMatrixLeastSquaresIdentity::mult
+ *   datadriven/src/sgpp/datadriven/algorithm/SystemMatrixLeastSquaresIdentity.cpp:32-47
+ * (the reference passes lambda * number_of_instances). Host buffers; blocks.
+ */
+SGMEV_API int sgmev_system_apply(sgmev_op* op, const double* alpha, double* result,
+                                 double lambda_times_m);
+SGMEV_API int sgmev_system_apply_device(sgmev_op* op, const double* d_alpha, double* d_result,
+                                        double lambda_times_m);
+
+/*
+ * Regression fit on the device: b = B^T y, then conjugate gradients on
+ * (B^T B + lambda*M*I) alpha = b, all vectors resident on the GPU; replaces
+ *   SystemMatrixLeastSquaresIdentity::generateb (SystemMatrixLeastSquaresIdentity.cpp:49-56) +
+ *   solver::ConjugateGradients::solve (solver/src/sgpp/solver/sle/ConjugateGradients.cpp:22-151):
+ *   same relative stopping test delta_new <= epsilon^2 * delta_0, same true-residual refresh
+ *   every 50 iterations, same warm start (reuse != 0 keeps alpha as the start vector).
+ * mode:
+ *   SGMEV_SOLVE_PLAIN  — CG with the op's own precision kernels (FP64 op: the plain FP64 path).
+ *   SGMEV_SOLVE_MIXED  — FP32 kernels inside CG, FP64 residual b - A alpha for the outer
+ *                        iterative-refinement correction (the op must have been created with
+ *                        SGMEV_FP64; the FP32 copies are staged on first use).
+ * y: [n_data] host; alpha: [n_grid] host in/out. iterations: total inner CG iterations;
+ * residual: final delta_new (plain) or ||b - A alpha||^2 in FP64 (mixed).
+ */
+#define SGMEV_SOLVE_PLAIN 0
+#define SGMEV_SOLVE_MIXED 1
+SGMEV_API int sgmev_fit(sgmev_op* op, int mode, const double* y, double lambda,
+                        int64_t max_iterations, double epsilon, int reuse, double* alpha,
+                        int64_t* iterations, double* residual);
+
+/*
+ * Duration in seconds of the device work of the last mult / multTranspose / system apply /
+ * fit call (CUDA events on the op's stream); replaces OperationMultipleEval::getDuration
+ *   OperationMultipleEval.hpp:120. -1 before the first call.
+ */
+SGMEV_API double sgmev_get_duration(sgmev_op* op);
+
+/* Use `stream` (a cudaStream_t) for all following work of this op; NULL restores the op's own. */
+SGMEV_API int sgmev_set_stream(sgmev_op* op, void* stream);
+
+/* Block until all work enqueued by this op has finished. */
+SGMEV_API int sgmev_synchronize(sgmev_op* op);
+
+/* Number of kernels this op launched so far (instrumentation for benchmarks). */
+SGMEV_API int64_t sgmev_kernel_launches(const sgmev_op* op);
+
+/* ---- sparse-grid construction on the host (native C++) --------------------------------- */
+/*
+ * Regular Linear sparse grid without boundary in the reference's storage order; replaces
+ *   Grid::createLinearGrid(d)->getGenerator().regular(level)
+ *   base/src/sgpp/base/grid/Grid.cpp:73, HashGenerator.hpp:282-347.
+ * Call with level/index NULL to get the size in *n_grid; then with arrays of [n_grid x dim]
+ * int32 raw levels and indices.
+ */
+SGMEV_API int sggrid_regular(int dim, int level, int64_t* n_grid, int32_t* level_out,
+                             int32_t* index_out);
+
+/*
+ * One round of surplus refinement (largest |alpha| first); replaces
+ *   GridGenerator::refine(SurplusRefinementFunctor(alpha, n_points, threshold))
+ *   base/.../StandardGridGenerator.cpp:64-68, HashRefinement.cpp:124-147,
+ *   SurplusRefinementFunctor.cpp:23-28.
+ * level/index: [cap x dim] int32, first n_grid rows filled on entry; on return *n_out rows.
+ * New points are appended (existing rows keep their positions, as in the reference).
+ * Points are refined by descending |alpha|, ties by position; the set of created points
+ * equals the reference's (whose order follows its hash-map iteration).
+ */
+SGMEV_API int sggrid_refine_surplus(int dim, int64_t n_grid, int64_t cap, int32_t* level,
+                                    int32_t* index, const double* alpha, int64_t n_points,
+                                    double threshold, int64_t* n_out);
+
+/* (2^l, i) as doubles in the reference's eval layout (HashGridStorage.cpp:433-450). */
+SGMEV_API int sggrid_level_index_for_eval(int dim, int64_t n_grid, const int32_t* level,
+                                          const int32_t* index, double* level_pow2,
+                                          double* index_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SGMEV_H_ */

@@ -1,0 +1,327 @@
+// Test infrastructure only: a thin extern "C" harness around the SG++ reference library
+// (compiled from the reference's own sources by oracle/ref.mk into oracle/_ref/).
+// Nothing in the shipped product links or loads this file; tests and the golden-fixture
+// generator use it to pin the oracle restatement (oracle/oracle.c) and the CUDA path.
+//
+// What it drives, all unmodified reference code:
+//   grid      sgpp::base::Grid::createLinearGrid        base/src/sgpp/base/grid/Grid.cpp:73
+//             GridGenerator::regular                    base/.../StandardGridGenerator.cpp:27-30
+//             GridGenerator::refine(SurplusRefinementFunctor)
+//                                                       base/.../StandardGridGenerator.cpp:64-68
+//             HashGridStorage::getLevelIndexArraysForEval
+//                                                       base/.../HashGridStorage.cpp:433-450
+//   DEFAULT   op_factory::createOperationMultipleEval(grid, data)
+//             -> OperationMultipleEvalLinear            base/.../BaseOpFactory.cpp:595-598
+//   NAIVE     OperationMultipleEvalLinearNaive          base/.../OperationMultipleEvalLinearNaive.cpp
+//   STREAMING OperationMultiEvalStreaming               datadriven/.../OperationMultiEvalStreaming.cpp
+//   CG fit    SystemMatrixLeastSquaresIdentity + solver::ConjugateGradients
+//                                                       datadriven/.../SystemMatrixLeastSquaresIdentity.cpp
+//                                                       solver/src/sgpp/solver/sle/ConjugateGradients.cpp
+//
+// SystemMatrixLeastSquaresIdentity obtains its operator through the datadriven factory
+// (datadriven/src/sgpp/datadriven/DatadrivenOpFactory.cpp:409). That factory's translation
+// unit pulls in every datadriven operator, so this harness defines the one factory overload
+// itself and routes (DEFAULT) and (STREAMING, DEFAULT) exactly as the reference factory does
+// for Linear grids (DatadrivenOpFactory.cpp:439-452).
+
+#include <sgpp/base/datatypes/DataMatrix.hpp>
+#include <sgpp/base/datatypes/DataVector.hpp>
+#include <sgpp/base/exception/factory_exception.hpp>
+#include <sgpp/base/grid/Grid.hpp>
+#include <sgpp/base/grid/generation/functors/SurplusRefinementFunctor.hpp>
+#include <sgpp/base/grid/storage/hashmap/HashGridStorage.hpp>
+#include <sgpp/base/operation/BaseOpFactory.hpp>
+#include <sgpp/base/operation/hash/OperationMultipleEval.hpp>
+#include <sgpp/base/operation/hash/OperationMultipleEvalLinearNaive.hpp>
+#include <sgpp/base/tools/GaussLegendreQuadRule1D.hpp>
+#include <sgpp/datadriven/algorithm/SystemMatrixLeastSquaresIdentity.hpp>
+#include <sgpp/datadriven/operation/hash/DatadrivenOperationCommon.hpp>
+#include <sgpp/datadriven/operation/hash/OperationMultiEvalStreaming/OperationMultiEvalStreaming.hpp>
+#include <sgpp/solver/sle/ConjugateGradients.hpp>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include <cstdint>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+
+// The reference snapshot ships GaussLegendreQuadRule1D.hpp without its .cpp. Linear-grid code
+// never calls it, but other base/ translation units reference the symbols, so they are defined
+// here as inert stand-ins (they are never reached on the multi-evaluation path).
+namespace sgpp {
+namespace base {
+GaussLegendreQuadRule1D::GaussLegendreQuadRule1D() {}
+GaussLegendreQuadRule1D::~GaussLegendreQuadRule1D() {}
+void GaussLegendreQuadRule1D::getLevelPointsAndWeightsNormalized(size_t, DataVector&,
+                                                                 DataVector&) {
+  throw factory_exception("GaussLegendreQuadRule1D is not part of the multi-evaluation oracle");
+}
+GaussLegendreQuadRule1D& GaussLegendreQuadRule1D::getInstance() {
+  static GaussLegendreQuadRule1D instance;
+  return instance;
+}
+}  // namespace base
+
+namespace op_factory {
+// Routing for Linear grids as in DatadrivenOpFactory.cpp:439-452 (DEFAULT -> base factory,
+// STREAMING/DEFAULT -> OperationMultiEvalStreaming); every other combination throws, like
+// the reference's final `throw factory_exception` (DatadrivenOpFactory.cpp:551).
+base::OperationMultipleEval* createOperationMultipleEval(
+    base::Grid& grid, base::DataMatrix& dataset,
+    datadriven::OperationMultipleEvalConfiguration& configuration) {
+  using datadriven::OperationMultipleEvalSubType;
+  using datadriven::OperationMultipleEvalType;
+  if (configuration.getType() == OperationMultipleEvalType::DEFAULT) {
+    return createOperationMultipleEval(grid, dataset);
+  }
+  if (grid.getType() == base::GridType::Linear &&
+      configuration.getType() == OperationMultipleEvalType::STREAMING &&
+      configuration.getSubType() == OperationMultipleEvalSubType::DEFAULT) {
+    return new datadriven::OperationMultiEvalStreaming(grid, dataset);
+  }
+  throw base::factory_exception("oracle harness: unsupported multi-eval configuration");
+}
+}  // namespace op_factory
+}  // namespace sgpp
+
+namespace {
+
+thread_local std::string g_err;
+
+struct RefGrid {
+  std::unique_ptr<sgpp::base::Grid> grid;
+};
+
+enum RefKind { REF_DEFAULT = 0, REF_STREAMING = 1, REF_NAIVE = 2 };
+
+sgpp::base::DataMatrix make_matrix(const double* rows, int64_t m, int dim) {
+  sgpp::base::DataMatrix mat(static_cast<size_t>(m), static_cast<size_t>(dim));
+  std::memcpy(mat.getPointer(), rows, sizeof(double) * static_cast<size_t>(m) * dim);
+  return mat;
+}
+
+std::unique_ptr<sgpp::base::OperationMultipleEval> make_op(RefGrid* g,
+                                                           sgpp::base::DataMatrix& data,
+                                                           int kind) {
+  switch (kind) {
+    case REF_DEFAULT:
+      return std::unique_ptr<sgpp::base::OperationMultipleEval>(
+          sgpp::op_factory::createOperationMultipleEval(*g->grid, data));
+    case REF_STREAMING:
+      return std::make_unique<sgpp::datadriven::OperationMultiEvalStreaming>(*g->grid, data);
+    case REF_NAIVE:
+      return std::make_unique<sgpp::base::OperationMultipleEvalLinearNaive>(*g->grid, data);
+    default:
+      throw sgpp::base::factory_exception("unknown reference kind");
+  }
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    f();
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return 1;
+  } catch (...) {
+    g_err = "unknown exception";
+    return 1;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ref_last_error() { return g_err.c_str(); }
+
+void ref_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+int ref_max_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void* ref_grid_create_linear(int dim) {
+  RefGrid* g = new RefGrid;
+  g->grid.reset(sgpp::base::Grid::createLinearGrid(static_cast<size_t>(dim)));
+  return g;
+}
+
+void ref_grid_destroy(void* h) { delete static_cast<RefGrid*>(h); }
+
+int ref_grid_regular(void* h, int level) {
+  return guarded([&] { static_cast<RefGrid*>(h)->grid->getGenerator().regular(level); });
+}
+
+int64_t ref_grid_size(void* h) {
+  return static_cast<int64_t>(static_cast<RefGrid*>(h)->grid->getSize());
+}
+
+int ref_grid_dim(void* h) {
+  return static_cast<int>(static_cast<RefGrid*>(h)->grid->getDimension());
+}
+
+// level/index in the reference's eval layout: two [N x d] row-major arrays, 2^l and i as doubles.
+int ref_grid_level_index(void* h, double* level_pow2, double* index) {
+  return guarded([&] {
+    RefGrid* g = static_cast<RefGrid*>(h);
+    auto& st = g->grid->getStorage();
+    sgpp::base::DataMatrix lv(st.getSize(), st.getDimension());
+    sgpp::base::DataMatrix ix(st.getSize(), st.getDimension());
+    st.getLevelIndexArraysForEval(lv, ix);
+    std::memcpy(level_pow2, lv.getPointer(), sizeof(double) * lv.getSize());
+    std::memcpy(index, ix.getPointer(), sizeof(double) * ix.getSize());
+  });
+}
+
+// Raw (level, index, leaf) per grid point in storage sequence order.
+int ref_grid_points(void* h, int32_t* level, int32_t* index, int32_t* leaf) {
+  return guarded([&] {
+    auto& st = static_cast<RefGrid*>(h)->grid->getStorage();
+    const size_t d = st.getDimension();
+    for (size_t s = 0; s < st.getSize(); ++s) {
+      auto& p = st.getPoint(s);
+      for (size_t t = 0; t < d; ++t) {
+        level[s * d + t] = static_cast<int32_t>(p.getLevel(t));
+        index[s * d + t] = static_cast<int32_t>(p.getIndex(t));
+      }
+      if (leaf) leaf[s] = p.isLeaf() ? 1 : 0;
+    }
+  });
+}
+
+int ref_grid_set_bounding_box(void* h, const double* left, const double* right) {
+  return guarded([&] {
+    auto& bb = static_cast<RefGrid*>(h)->grid->getBoundingBox();
+    for (size_t t = 0; t < bb.getDimension(); ++t) {
+      bb.setBoundary(t, sgpp::base::BoundingBox1D(left[t], right[t]));
+    }
+  });
+}
+
+// One round of surplus refinement on |alpha| (SurplusRefinementFunctor.cpp:23-28).
+int ref_grid_refine_surplus(void* h, const double* alpha, int64_t n_alpha, int64_t n_points,
+                            double threshold) {
+  return guarded([&] {
+    RefGrid* g = static_cast<RefGrid*>(h);
+    sgpp::base::DataVector a(static_cast<size_t>(n_alpha));
+    std::memcpy(a.getPointer(), alpha, sizeof(double) * static_cast<size_t>(n_alpha));
+    sgpp::base::SurplusRefinementFunctor f(a, static_cast<size_t>(n_points), threshold);
+    g->grid->getGenerator().refine(f);
+  });
+}
+
+// Serialized grid text (Grid::serialize), for fixtures that want the reference's own format.
+int ref_grid_serialize(void* h, char* buf, int64_t cap, int64_t* needed) {
+  return guarded([&] {
+    std::string s;
+    static_cast<RefGrid*>(h)->grid->serialize(s);
+    *needed = static_cast<int64_t>(s.size()) + 1;
+    if (buf && cap >= *needed) std::memcpy(buf, s.c_str(), s.size() + 1);
+  });
+}
+
+// result[m] = sum_i alpha_i phi_i(x_m)  through the chosen reference implementation.
+int ref_mult(void* h, int kind, const double* data, int64_t m, const double* alpha,
+             double* result, double* seconds) {
+  return guarded([&] {
+    RefGrid* g = static_cast<RefGrid*>(h);
+    const int dim = static_cast<int>(g->grid->getDimension());
+    sgpp::base::DataMatrix x = make_matrix(data, m, dim);
+    auto op = make_op(g, x, kind);
+    sgpp::base::DataVector a(g->grid->getSize());
+    std::memcpy(a.getPointer(), alpha, sizeof(double) * a.getSize());
+    sgpp::base::DataVector r(static_cast<size_t>(m));
+    op->mult(a, r);
+    std::memcpy(result, r.getPointer(), sizeof(double) * r.getSize());
+    if (seconds) *seconds = kind == REF_STREAMING ? op->getDuration() : -1.0;
+  });
+}
+
+// result[i] = sum_m source_m phi_i(x_m)
+int ref_mult_transpose(void* h, int kind, const double* data, int64_t m, const double* source,
+                       double* result, double* seconds) {
+  return guarded([&] {
+    RefGrid* g = static_cast<RefGrid*>(h);
+    const int dim = static_cast<int>(g->grid->getDimension());
+    sgpp::base::DataMatrix x = make_matrix(data, m, dim);
+    auto op = make_op(g, x, kind);
+    sgpp::base::DataVector s(static_cast<size_t>(m));
+    std::memcpy(s.getPointer(), source, sizeof(double) * s.getSize());
+    sgpp::base::DataVector r(g->grid->getSize());
+    op->multTranspose(s, r);
+    std::memcpy(result, r.getPointer(), sizeof(double) * r.getSize());
+    if (seconds) *seconds = kind == REF_STREAMING ? op->getDuration() : -1.0;
+  });
+}
+
+// Repeated STREAMING mult/multTranspose on one prepared operator (CPU baseline timing): the
+// operator is built once, then `reps` calls run back to back; per-call durations are returned.
+int ref_streaming_time(void* h, const double* data, int64_t m, const double* alpha,
+                       const double* source, int reps, double* mult_seconds,
+                       double* multt_seconds) {
+  return guarded([&] {
+    RefGrid* g = static_cast<RefGrid*>(h);
+    const int dim = static_cast<int>(g->grid->getDimension());
+    sgpp::base::DataMatrix x = make_matrix(data, m, dim);
+    sgpp::datadriven::OperationMultiEvalStreaming op(*g->grid, x);
+    sgpp::base::DataVector a(g->grid->getSize());
+    std::memcpy(a.getPointer(), alpha, sizeof(double) * a.getSize());
+    sgpp::base::DataVector s(static_cast<size_t>(m));
+    std::memcpy(s.getPointer(), source, sizeof(double) * s.getSize());
+    sgpp::base::DataVector r1(static_cast<size_t>(m));
+    sgpp::base::DataVector r2(g->grid->getSize());
+    for (int k = 0; k < reps; ++k) {
+      op.mult(a, r1);
+      mult_seconds[k] = op.getDuration();
+      op.multTranspose(s, r2);
+      multt_seconds[k] = op.getDuration();
+    }
+  });
+}
+
+// Regression fit exactly as the reference learner does it: b = B^T y, then CG on
+// (B^T B + lambda*M*I) alpha = b with SystemMatrixLeastSquaresIdentity.
+int ref_cg_fit(void* h, int kind, const double* data, int64_t m, const double* y, double lambda,
+               int64_t imax, double epsilon, int reuse, double* alpha_io, int64_t* iterations,
+               double* residual) {
+  return guarded([&] {
+    RefGrid* g = static_cast<RefGrid*>(h);
+    const int dim = static_cast<int>(g->grid->getDimension());
+    sgpp::base::DataMatrix x = make_matrix(data, m, dim);
+    sgpp::datadriven::SystemMatrixLeastSquaresIdentity A(*g->grid, x, lambda);
+    sgpp::datadriven::OperationMultipleEvalConfiguration cfg(
+        kind == REF_STREAMING ? sgpp::datadriven::OperationMultipleEvalType::STREAMING
+                              : sgpp::datadriven::OperationMultipleEvalType::DEFAULT,
+        sgpp::datadriven::OperationMultipleEvalSubType::DEFAULT);
+    A.setImplementation(cfg);
+    sgpp::base::DataVector yv(static_cast<size_t>(m));
+    std::memcpy(yv.getPointer(), y, sizeof(double) * yv.getSize());
+    sgpp::base::DataVector b(g->grid->getSize());
+    A.generateb(yv, b);
+    sgpp::base::DataVector alpha(g->grid->getSize());
+    std::memcpy(alpha.getPointer(), alpha_io, sizeof(double) * alpha.getSize());
+    sgpp::solver::ConjugateGradients cg(static_cast<size_t>(imax), epsilon);
+    cg.solve(A, alpha, b, reuse != 0, false, 0.0);
+    std::memcpy(alpha_io, alpha.getPointer(), sizeof(double) * alpha.getSize());
+    *iterations = static_cast<int64_t>(cg.getNumberIterations());
+    *residual = cg.getResiduum();
+  });
+}
+
+}  // extern "C"

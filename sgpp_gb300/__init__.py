@@ -1,0 +1,646 @@
+"""sgpp_gb300 — GB300 (sm_103a) multi-evaluation for SG++'s hat-basis sparse grids.
+
+Host-side mirror of the reference interface for this path, over the C ABI of
+``libsgpp_gb300.so`` (``include/sgmev.h``). Names, argument meaning and error behaviour follow
+the reference (pysgpp) so that callers and tests read like the reference's own:
+
+  Grid.createLinearGrid(d); grid.getGenerator().regular(l); .refine(SurplusRefinementFunctor)
+      base/src/sgpp/base/grid/Grid.cpp:73, StandardGridGenerator.cpp:27-30,64-68
+  createOperationMultipleEval(grid, dataset, OperationMultipleEvalConfiguration(...))
+      datadriven/src/sgpp/datadriven/DatadrivenOpFactory.cpp:409-552 — the (Linear, STREAMING,
+      CUDA) branch returns OperationMultiEvalCuda; other combinations raise FactoryException
+  op.mult(alpha, result) / op.multTranspose(source, result) / ranged variants / prepare() /
+      getDuration() / getImplementationName()
+      base/src/sgpp/base/operation/hash/OperationMultipleEval.hpp:27-130
+  SystemMatrixLeastSquaresIdentity(grid, data, lambda)
+      datadriven/src/sgpp/datadriven/algorithm/SystemMatrixLeastSquaresIdentity.cpp:18-65
+  ConjugateGradients(imax, epsilon).solve(A, alpha, b, reuse, verbose, max_threshold)
+      solver/src/sgpp/solver/sle/ConjugateGradients.cpp:22-151
+
+DataVector / DataMatrix are numpy float64 arrays (1-D, and 2-D row-major [rows x dim]); result
+arrays are written in place, as the reference writes into its DataVector arguments.
+
+The compute path is the CUDA library only: importing works without a GPU, but creating an
+operator raises OperationException when the library or a CUDA device is missing. There is no
+CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBRARY_PATH = os.path.join(_HERE, "libsgpp_gb300.so")
+
+SGMEV_OK = 0
+SGMEV_ERR_INVALID = -1
+SGMEV_ERR_CUDA = -2
+SGMEV_ERR_NO_DEVICE = -3
+SGMEV_ERR_UNSUPPORTED = -4
+SGMEV_ERR_NOT_CONVERGED = -5
+SGMEV_ERR_OOM = -6
+
+SGMEV_FP64 = 0
+SGMEV_FP32 = 1
+SGMEV_SOLVE_PLAIN = 0
+SGMEV_SOLVE_MIXED = 1
+
+# every entry point declared in include/sgmev.h
+EXPORTED_SYMBOLS = (
+    "sgmev_last_error", "sgmev_version", "sgmev_device_count", "sgmev_create", "sgmev_destroy",
+    "sgmev_prepare", "sgmev_get_sizes", "sgmev_mult", "sgmev_mult_transpose", "sgmev_mult_range",
+    "sgmev_mult_transpose_range", "sgmev_mult_device", "sgmev_mult_transpose_device",
+    "sgmev_system_apply", "sgmev_system_apply_device", "sgmev_fit", "sgmev_get_duration",
+    "sgmev_set_stream", "sgmev_synchronize", "sgmev_kernel_launches", "sggrid_regular",
+    "sggrid_refine_surplus", "sggrid_level_index_for_eval", "sgmev_fma_peak",
+)
+
+
+# ---- exceptions (base/src/sgpp/base/exception/) --------------------------------------------
+class SGppException(RuntimeError):
+    pass
+
+
+class OperationException(SGppException):
+    """operation_exception"""
+
+
+class FactoryException(SGppException):
+    """factory_exception"""
+
+
+class NotImplementedException(SGppException):
+    """not_implemented_exception"""
+
+
+class GenerationException(SGppException):
+    """generation_exception"""
+
+
+# ---- library loading ----------------------------------------------------------------------
+_lib = None
+
+
+def _vp(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def load_library(path: str = LIBRARY_PATH):
+    """Load libsgpp_gb300.so (built by sgpp_gb300.build). Raises OperationException if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OperationException(
+            f"{path} is missing: build it with `python -m sgpp_gb300.build` (no CPU fallback)")
+    L = ctypes.CDLL(path)
+    i64, c_int, dbl, vp = ctypes.c_int64, ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+    pi64, pdbl = ctypes.POINTER(i64), ctypes.POINTER(dbl)
+    sig = {
+        "sgmev_last_error": (ctypes.c_char_p, []),
+        "sgmev_version": (c_int, []),
+        "sgmev_device_count": (c_int, []),
+        "sgmev_create": (c_int, [ctypes.POINTER(vp), c_int, i64, vp, vp, i64, vp, vp, vp, c_int,
+                                 ctypes.c_char_p]),
+        "sgmev_destroy": (c_int, [vp]),
+        "sgmev_prepare": (c_int, [vp, i64, vp, vp]),
+        "sgmev_get_sizes": (c_int, [vp, ctypes.POINTER(c_int), pi64, pi64]),
+        "sgmev_mult": (c_int, [vp, vp, vp]),
+        "sgmev_mult_transpose": (c_int, [vp, vp, vp]),
+        "sgmev_mult_range": (c_int, [vp, vp, vp, i64, i64]),
+        "sgmev_mult_transpose_range": (c_int, [vp, vp, vp, i64, i64]),
+        "sgmev_mult_device": (c_int, [vp, vp, vp]),
+        "sgmev_mult_transpose_device": (c_int, [vp, vp, vp]),
+        "sgmev_system_apply": (c_int, [vp, vp, vp, dbl]),
+        "sgmev_system_apply_device": (c_int, [vp, vp, vp, dbl]),
+        "sgmev_fit": (c_int, [vp, c_int, vp, dbl, i64, dbl, c_int, vp, pi64, pdbl]),
+        "sgmev_get_duration": (dbl, [vp]),
+        "sgmev_set_stream": (c_int, [vp, vp]),
+        "sgmev_synchronize": (c_int, [vp]),
+        "sgmev_kernel_launches": (i64, [vp]),
+        "sggrid_regular": (c_int, [c_int, c_int, pi64, vp, vp]),
+        "sggrid_refine_surplus": (c_int, [c_int, i64, i64, vp, vp, vp, i64, dbl, pi64]),
+        "sggrid_level_index_for_eval": (c_int, [c_int, i64, vp, vp, vp, vp]),
+        "sgmev_fma_peak": (c_int, [c_int, pdbl, ctypes.POINTER(c_int)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int, exc=OperationException):
+    if rc != SGMEV_OK:
+        msg = load_library().sgmev_last_error().decode(errors="replace")
+        raise exc(f"libsgpp_gb300 error {rc}: {msg}")
+
+
+def device_count() -> int:
+    return int(load_library().sgmev_device_count())
+
+
+def fma_peak(precision: int = SGMEV_FP32):
+    """Measured vector FMA throughput (FLOP/s, FMA = 2) and the reported SM clock (kHz)."""
+    f = ctypes.c_double(0.0)
+    k = ctypes.c_int(0)
+    _check(load_library().sgmev_fma_peak(int(precision), ctypes.byref(f), ctypes.byref(k)))
+    return float(f.value), int(k.value)
+
+
+# ---- grids --------------------------------------------------------------------------------
+class GridType(enum.IntEnum):
+    Linear = 0
+
+
+class BoundingBox1D:
+    def __init__(self, leftBoundary: float = 0.0, rightBoundary: float = 1.0):
+        self.leftBoundary = float(leftBoundary)
+        self.rightBoundary = float(rightBoundary)
+
+
+class BoundingBox:
+    """base/src/sgpp/base/grid/common/BoundingBox.hpp — per-dimension [left, right]."""
+
+    def __init__(self, dim: int):
+        self._b = [BoundingBox1D() for _ in range(dim)]
+
+    def setBoundary(self, d: int, bb: BoundingBox1D) -> None:
+        self._b[d] = BoundingBox1D(bb.leftBoundary, bb.rightBoundary)
+
+    def getBoundary(self, d: int) -> BoundingBox1D:
+        return self._b[d]
+
+    def getDimension(self) -> int:
+        return len(self._b)
+
+    def isUnitCube(self) -> bool:
+        return all(b.leftBoundary == 0.0 and b.rightBoundary == 1.0 for b in self._b)
+
+    def arrays(self):
+        return (np.array([b.leftBoundary for b in self._b]),
+                np.array([b.rightBoundary for b in self._b]))
+
+
+class GridStorage:
+    """Hash-grid storage view: raw (level, index) rows in sequence order."""
+
+    def __init__(self, dim: int):
+        self.dim = dim
+        self.level = np.zeros((0, dim), np.int32)
+        self.index = np.zeros((0, dim), np.int32)
+        self.boundingBox = BoundingBox(dim)
+
+    def getSize(self) -> int:
+        return int(self.level.shape[0])
+
+    def getDimension(self) -> int:
+        return self.dim
+
+    def getBoundingBox(self) -> BoundingBox:
+        return self.boundingBox
+
+    def setBoundingBox(self, bb: BoundingBox) -> None:
+        self.boundingBox = bb
+
+    def getLevelIndexArraysForEval(self, level: Optional[np.ndarray] = None,
+                                   index: Optional[np.ndarray] = None):
+        """(2^l, i) as [N x d] doubles (HashGridStorage.cpp:433-450)."""
+        n = self.getSize()
+        lp = np.empty((n, self.dim)) if level is None else level
+        ix = np.empty((n, self.dim)) if index is None else index
+        if n:
+            L = np.ascontiguousarray(self.level)
+            I = np.ascontiguousarray(self.index)
+            _check(load_library().sggrid_level_index_for_eval(self.dim, n, _vp(L), _vp(I),
+                                                               _vp(lp), _vp(ix)))
+        return lp, ix
+
+
+class SurplusRefinementFunctor:
+    """base/src/sgpp/base/grid/generation/functors/SurplusRefinementFunctor.cpp:14-44"""
+
+    def __init__(self, alpha, refinements_num: int = 1, threshold: float = 0.0):
+        self.alpha = np.ascontiguousarray(alpha, np.float64)
+        self.refinements_num = int(refinements_num)
+        self.threshold = float(threshold)
+
+    def getRefinementsNum(self) -> int:
+        return self.refinements_num
+
+    def getRefinementThreshold(self) -> float:
+        return self.threshold
+
+
+class GridGenerator:
+    def __init__(self, grid: "Grid"):
+        self.grid = grid
+
+    def regular(self, level: int) -> None:
+        """HashGenerator::regular (HashGenerator.hpp:53-58): storage must be empty."""
+        st = self.grid.getStorage()
+        if st.getSize() > 0:
+            raise GenerationException("storage not empty")
+        L = load_library()
+        n = ctypes.c_int64(0)
+        _check(L.sggrid_regular(st.dim, int(level), ctypes.byref(n), None, None),
+               GenerationException)
+        lev = np.zeros((n.value, st.dim), np.int32)
+        idx = np.zeros((n.value, st.dim), np.int32)
+        _check(L.sggrid_regular(st.dim, int(level), ctypes.byref(n), _vp(lev), _vp(idx)),
+               GenerationException)
+        st.level, st.index = lev, idx
+
+    def refine(self, functor: SurplusRefinementFunctor, addedPoints: Optional[list] = None) -> None:
+        """HashRefinement::free_refine (HashRefinement.cpp:124-147); new points are appended."""
+        st = self.grid.getStorage()
+        n = st.getSize()
+        if n == 0:
+            raise GenerationException("storage empty")
+        if functor.alpha.size < n:
+            raise GenerationException("alpha shorter than the grid")
+        k = functor.getRefinementsNum()
+        cap = n + max(k, 0) * 2 * st.dim * (2 + int(st.level.max(initial=1))) * st.dim + 16
+        lev = np.zeros((cap, st.dim), np.int32)
+        idx = np.zeros((cap, st.dim), np.int32)
+        lev[:n] = st.level
+        idx[:n] = st.index
+        out = ctypes.c_int64(0)
+        _check(load_library().sggrid_refine_surplus(st.dim, n, cap, _vp(lev), _vp(idx),
+                                                    _vp(functor.alpha), k,
+                                                    functor.getRefinementThreshold(),
+                                                    ctypes.byref(out)), GenerationException)
+        st.level, st.index = lev[:out.value].copy(), idx[:out.value].copy()
+        if addedPoints is not None:
+            addedPoints.extend(range(n, out.value))
+
+
+class Grid:
+    """A Linear (hat basis, no boundary) sparse grid (Grid::createLinearGrid, Grid.cpp:73)."""
+
+    def __init__(self, dim: int):
+        self._storage = GridStorage(dim)
+        self._generator = GridGenerator(self)
+
+    @staticmethod
+    def createLinearGrid(dim: int) -> "Grid":
+        if dim < 1:
+            raise GenerationException("dimension must be >= 1")
+        return Grid(int(dim))
+
+    @staticmethod
+    def fromArrays(level, index) -> "Grid":
+        """A grid from raw [N x d] level / index rows (e.g. exported from an SG++ storage)."""
+        level = np.ascontiguousarray(level, np.int32)
+        g = Grid(level.shape[1])
+        g._storage.level = level.copy()
+        g._storage.index = np.ascontiguousarray(index, np.int32).copy()
+        return g
+
+    def getStorage(self) -> GridStorage:
+        return self._storage
+
+    def getGenerator(self) -> GridGenerator:
+        return self._generator
+
+    def getBoundingBox(self) -> BoundingBox:
+        return self._storage.getBoundingBox()
+
+    def getSize(self) -> int:
+        return self._storage.getSize()
+
+    def getDimension(self) -> int:
+        return self._storage.getDimension()
+
+    def getType(self) -> GridType:
+        return GridType.Linear
+
+
+# ---- operator configuration (DatadrivenOperationCommon.hpp:17-95) ---------------------------
+class OperationMultipleEvalType(enum.IntEnum):
+    DEFAULT = 0
+    STREAMING = 1
+    SUBSPACELINEAR = 2
+    ADAPTIVE = 3
+    MORTONORDER = 4
+    SCALAPACK = 5
+
+
+class OperationMultipleEvalSubType(enum.IntEnum):
+    DEFAULT = 0
+    SIMPLE = 1
+    COMBINED = 2
+    OCL = 3
+    OCLFASTMP = 4
+    OCLMP = 5
+    OCLMASKMP = 6
+    OCLOPT = 7
+    OCLUNIFIED = 8
+    CUDA = 9
+
+
+class OperationMultipleEvalMPIType(enum.IntEnum):
+    NONE = 0
+    MASTERSLAVE = 1
+    HPX = 2
+
+
+class OperationMultipleEvalConfiguration:
+    """Operator selection plus a parameters tree. Parameters understood by the CUDA operator:
+    ``precision``: "double" (default) or "float"."""
+
+    def __init__(self, type=OperationMultipleEvalType.DEFAULT,
+                 subType=OperationMultipleEvalSubType.DEFAULT,
+                 mpiType=OperationMultipleEvalMPIType.NONE, parameters: Optional[dict] = None,
+                 name: str = "unnamed"):
+        self.type = OperationMultipleEvalType(type)
+        self.subType = OperationMultipleEvalSubType(subType)
+        self.mpiType = OperationMultipleEvalMPIType(mpiType)
+        self.parameters = dict(parameters or {})
+        self.name = name
+
+    def getType(self):
+        return self.type
+
+    def getSubType(self):
+        return self.subType
+
+    def getMPIType(self):
+        return self.mpiType
+
+    def getParameters(self):
+        return self.parameters
+
+    def getName(self):
+        return self.name
+
+
+def _as_matrix(data) -> np.ndarray:
+    a = np.ascontiguousarray(data, np.float64)
+    if a.ndim == 1:
+        a = a.reshape(-1, 1)
+    if a.ndim != 2:
+        raise OperationException("dataset must be a [rows x dim] matrix")
+    return a
+
+
+def _precision_of(params: dict) -> int:
+    p = str(params.get("precision", "double")).lower()
+    if p in ("double", "fp64", "f64"):
+        return SGMEV_FP64
+    if p in ("float", "fp32", "f32", "single"):
+        return SGMEV_FP32
+    raise OperationException(f"unknown precision {p!r}")
+
+
+class OperationMultiEvalCuda:
+    """B / B^T on the GPU for a Linear grid (OperationMultipleEval interface)."""
+
+    def __init__(self, grid: Grid, dataset, precision: int = SGMEV_FP64):
+        self.grid = grid
+        self.dataset = _as_matrix(dataset)
+        self.precision = precision
+        st = grid.getStorage()
+        if self.dataset.shape[1] != st.getDimension() and self.dataset.shape[0] > 0:
+            raise OperationException("dataset dimension does not match the grid")
+        L = load_library()
+        lp, ix = st.getLevelIndexArraysForEval()
+        bb = st.getBoundingBox()
+        left = right = None
+        if not bb.isUnitCube():
+            left, right = bb.arrays()
+        h = ctypes.c_void_p(None)
+        _check(L.sgmev_create(ctypes.byref(h), st.getDimension(), st.getSize(), _vp(lp), _vp(ix),
+                              self.dataset.shape[0], _vp(self.dataset), _vp(left), _vp(right),
+                              precision, None))
+        self._h = h
+        self._n = st.getSize()
+        self._m = self.dataset.shape[0]
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load_library().sgmev_destroy(self._h)
+            self._h = ctypes.c_void_p(None)
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def _vec(self, v, n: int, what: str) -> np.ndarray:
+        a = np.ascontiguousarray(v, np.float64)
+        if a.ndim != 1 or a.size < n:
+            raise OperationException(f"{what} has size {a.size}, expected {n}")
+        return a
+
+    @staticmethod
+    def _out(v, n: int, what: str) -> np.ndarray:
+        if not isinstance(v, np.ndarray) or v.dtype != np.float64 or not v.flags.c_contiguous:
+            raise OperationException(f"{what} must be a contiguous float64 numpy array")
+        if v.ndim != 1 or v.size < n:
+            raise OperationException(f"{what} has size {v.size}, expected {n}")
+        return v
+
+    def mult(self, alpha, result, startIndexData: Optional[int] = None,
+             endIndexData: Optional[int] = None) -> None:
+        a = self._vec(alpha, self._n, "alpha")
+        r = self._out(result, self._m, "result")
+        L = load_library()
+        if startIndexData is None:
+            _check(L.sgmev_mult(self._h, _vp(a), _vp(r)))
+        else:
+            _check(L.sgmev_mult_range(self._h, _vp(a), _vp(r), int(startIndexData),
+                                      int(endIndexData)))
+
+    def eval(self, alpha, result) -> None:
+        self.mult(alpha, result)
+
+    def multTranspose(self, source, result, startIndexGrid: Optional[int] = None,
+                      endIndexGrid: Optional[int] = None) -> None:
+        s = self._vec(source, self._m, "source")
+        r = self._out(result, self._n, "result")
+        L = load_library()
+        if startIndexGrid is None:
+            _check(L.sgmev_mult_transpose(self._h, _vp(s), _vp(r)))
+        else:
+            _check(L.sgmev_mult_transpose_range(self._h, _vp(s), _vp(r), int(startIndexGrid),
+                                                int(endIndexGrid)))
+
+    def prepare(self) -> None:
+        """Re-stage the (refined) grid (OperationMultipleEval::prepare)."""
+        st = self.grid.getStorage()
+        lp, ix = st.getLevelIndexArraysForEval()
+        _check(load_library().sgmev_prepare(self._h, st.getSize(), _vp(lp), _vp(ix)))
+        self._n = st.getSize()
+
+    def getDuration(self) -> float:
+        return float(load_library().sgmev_get_duration(self._h))
+
+    def getImplementationName(self) -> str:
+        return "CUDA_LINEAR_FP64" if self.precision == SGMEV_FP64 else "CUDA_LINEAR_FP32"
+
+    def kernelLaunches(self) -> int:
+        return int(load_library().sgmev_kernel_launches(self._h))
+
+    def systemApply(self, alpha, result, lambda_times_m: float) -> None:
+        a = self._vec(alpha, self._n, "alpha")
+        r = self._out(result, self._n, "result")
+        _check(load_library().sgmev_system_apply(self._h, _vp(a), _vp(r), float(lambda_times_m)))
+
+    def fit(self, y, lam: float, imax: int, epsilon: float, alpha=None, mode: int = SGMEV_SOLVE_PLAIN):
+        """Device-resident regression fit; returns (alpha, iterations, residual)."""
+        yv = self._vec(y, self._m, "y")
+        alpha_out = (np.zeros(self._n) if alpha is None
+                     else np.array(alpha, np.float64, copy=True))
+        it = ctypes.c_int64(0)
+        res = ctypes.c_double(0.0)
+        _check(load_library().sgmev_fit(self._h, int(mode), _vp(yv), float(lam), int(imax),
+                                        float(epsilon), 0 if alpha is None else 1,
+                                        _vp(alpha_out), ctypes.byref(it), ctypes.byref(res)))
+        return alpha_out, int(it.value), float(res.value)
+
+
+def createOperationMultipleEval(grid: Grid, dataset,
+                                configuration: Optional[OperationMultipleEvalConfiguration] = None):
+    """op_factory::createOperationMultipleEval with the new CUDA branch for Linear grids.
+
+    (Linear, STREAMING, CUDA) and, when no configuration is given, the default route both give
+    the GPU operator; every other combination raises FactoryException, as the reference does for
+    combinations it was not built with (DatadrivenOpFactory.cpp:551)."""
+    if configuration is None:
+        configuration = OperationMultipleEvalConfiguration(
+            OperationMultipleEvalType.STREAMING, OperationMultipleEvalSubType.CUDA)
+    if grid.getType() != GridType.Linear:
+        raise FactoryException("OperationMultipleEval is not implemented for this grid type.")
+    if (configuration.getType() == OperationMultipleEvalType.STREAMING
+            and configuration.getSubType() == OperationMultipleEvalSubType.CUDA
+            and configuration.getMPIType() == OperationMultipleEvalMPIType.NONE):
+        return OperationMultiEvalCuda(grid, dataset, _precision_of(configuration.getParameters()))
+    raise FactoryException("OperationMultipleEval is not implemented for this combination of "
+                           "type, subtype and MPI type in this build.")
+
+
+# ---- least-squares system and CG (the callers that drive the operator unchanged) -----------
+class SystemMatrixLeastSquaresIdentity:
+    """(B^T B + lambda*M*I) alpha, b = B^T y  (SystemMatrixLeastSquaresIdentity.cpp:18-65)."""
+
+    def __init__(self, grid: Grid, trainData, lambdaRegression: float):
+        self.grid = grid
+        self.dataset = _as_matrix(trainData)
+        self.lambda_ = float(lambdaRegression)
+        self.instances = self.dataset.shape[0]
+        self.implementationConfiguration = OperationMultipleEvalConfiguration(
+            OperationMultipleEvalType.STREAMING, OperationMultipleEvalSubType.CUDA)
+        self.B = createOperationMultipleEval(grid, self.dataset, self.implementationConfiguration)
+        self.completeTimeMult = 0.0
+        self.computeTimeMult = 0.0
+        self.completeTimeMultTrans = 0.0
+        self.computeTimeMultTrans = 0.0
+
+    def mult(self, alpha, result) -> None:
+        temp = np.zeros(self.instances)
+        self.B.mult(alpha, temp)
+        self.computeTimeMult += self.B.getDuration()
+        self.B.multTranspose(temp, result)
+        self.computeTimeMultTrans += self.B.getDuration()
+        result += float(self.instances) * self.lambda_ * np.asarray(alpha, np.float64)
+
+    def generateb(self, classes, b) -> None:
+        self.B.multTranspose(np.array(classes, np.float64, copy=True), b)
+        self.computeTimeMultTrans += self.B.getDuration()
+
+    def prepareGrid(self) -> None:
+        self.B.prepare()
+
+    def setImplementation(self, operationConfiguration: OperationMultipleEvalConfiguration) -> None:
+        self.implementationConfiguration = operationConfiguration
+        if hasattr(self.B, "close"):
+            self.B.close()
+        self.B = createOperationMultipleEval(self.grid, self.dataset, operationConfiguration)
+
+    def getLambda(self) -> float:
+        return self.lambda_
+
+
+class ConjugateGradients:
+    """FP64 CG on the host driving any OperationMatrix-like `mult` (ConjugateGradients.cpp:22-151)."""
+
+    def __init__(self, imax: int, epsilon: float):
+        self.nMaxIterations = int(imax)
+        self.myEpsilon = float(epsilon)
+        self.nIterations = 0
+        self.residuum = 0.0
+
+    def solve(self, SystemMatrix, alpha: np.ndarray, b, reuse: bool = False,
+              verbose: bool = False, max_threshold: float = 0.0) -> None:
+        eps2 = self.myEpsilon * self.myEpsilon
+        self.nIterations = 0
+        n = alpha.size
+        temp = np.zeros(n)
+        q = np.zeros(n)
+        r = np.array(b, np.float64, copy=True)
+        delta_0 = 0.0
+        if reuse:
+            q[:] = 0.0
+            SystemMatrix.mult(q, temp)
+            r -= temp
+            delta_0 = float(r @ r) * eps2
+        else:
+            alpha[:] = 0.0
+        SystemMatrix.mult(alpha, temp)
+        r -= temp
+        d = r.copy()
+        delta_new = float(r @ r)
+        if not reuse:
+            delta_0 = delta_new * eps2
+        self.residuum = delta_0 / eps2 if eps2 > 0 else delta_new
+        while (self.nIterations < self.nMaxIterations and delta_new > delta_0
+               and delta_new > max_threshold):
+            SystemMatrix.mult(d, q)
+            dq = float(d @ q)
+            if dq == 0.0:
+                break
+            a = delta_new / dq
+            alpha += a * d
+            if self.nIterations % 50 == 0 and self.nIterations > 0:
+                SystemMatrix.mult(alpha, temp)
+                r[:] = np.asarray(b, np.float64) - temp
+            else:
+                r -= a * q
+            delta_old = delta_new
+            delta_new = float(r @ r)
+            beta = delta_new / delta_old
+            self.residuum = delta_new
+            if verbose:
+                print(f"delta: {delta_new}")
+            d *= beta
+            d += r
+            self.nIterations += 1
+        self.residuum = delta_new
+
+    def getNumberIterations(self) -> int:
+        return self.nIterations
+
+    def getResiduum(self) -> float:
+        return self.residuum
+
+
+__all__ = [
+    "Grid", "GridStorage", "GridGenerator", "GridType", "BoundingBox", "BoundingBox1D",
+    "SurplusRefinementFunctor", "OperationMultipleEvalType", "OperationMultipleEvalSubType",
+    "OperationMultipleEvalMPIType", "OperationMultipleEvalConfiguration",
+    "createOperationMultipleEval", "OperationMultiEvalCuda", "SystemMatrixLeastSquaresIdentity",
+    "ConjugateGradients", "OperationException", "FactoryException", "NotImplementedException",
+    "GenerationException", "load_library", "device_count", "EXPORTED_SYMBOLS", "SGMEV_FP64",
+    "SGMEV_FP32", "SGMEV_SOLVE_PLAIN", "SGMEV_SOLVE_MIXED",
+]

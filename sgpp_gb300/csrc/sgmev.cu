@@ -1,0 +1,1035 @@
+// libsgpp_gb300: GB300 multi-evaluation operator behind the C ABI declared in include/sgmev.h.
+//
+// Host-side structure (one op = one grid + one data set, as the reference operator):
+//   staging   data rows -> dim-major FP64 and FP32 copies, grid (2^l, i) -> interleaved pairs
+//   plans     per precision: CTA tile shapes and the 2-D split (tiles x chunks) sized so that
+//             every launch has at least `target_ctas` CTAs on the 152 SMs
+//   products  mult / multT = one tile kernel writing partials + one fixed-order reduce kernel
+//   system    B^T(B a) + lambda*M*a: mult, reduce into the M-vector, multT, reduce (+ lambda term)
+//   fit       conjugate gradients with every vector on the device; scalars come back to the
+//             host once per dot product to drive the loop exactly like
+//             solver/src/sgpp/solver/sle/ConjugateGradients.cpp:22-151
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sgmev.h"
+#include "kernels.cuh"
+
+namespace sgmev {
+
+thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define SGMEV_CUDA(call)                                                                 \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      return fail(e_ == cudaErrorMemoryAllocation ? SGMEV_ERR_OOM : SGMEV_ERR_CUDA,      \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+    }                                                                                    \
+  } while (0)
+
+#define SGMEV_TRY(expr)   \
+  do {                    \
+    int rc_ = (expr);     \
+    if (rc_ != SGMEV_OK) return rc_; \
+  } while (0)
+
+constexpr int kBlock = 128;
+constexpr int kGT = 32;       // grid points per shared-memory tile (mult)
+constexpr int kDT = 64;       // data points per shared-memory tile (multT)
+constexpr int64_t kMPadTo = 1024;
+constexpr int64_t kNPadTo = 512;
+constexpr int kMaxTemplDim = 16;
+constexpr int kReduceBlocks = 1216;  // 8 x 152 SMs
+constexpr int kDotBlocks = 304;
+constexpr int kDotThreads = 256;
+
+static inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+static inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
+
+// Register blocking per precision and dimension (data points per thread for mult, grid points
+// per thread for multT).
+template <typename T>
+struct Blocking;
+template <>
+struct Blocking<float> {
+  static constexpr int mult_r(int dim) { return dim <= 12 ? 8 : 4; }
+  static constexpr int multt_r(int) { return 4; }
+};
+template <>
+struct Blocking<double> {
+  static constexpr int mult_r(int) { return 4; }
+  static constexpr int multt_r(int) { return 2; }
+};
+
+struct Plan {
+  int64_t tiles = 0;   // CTAs along the tiled axis
+  int64_t nsplit = 1;  // CTAs along the split axis
+  int64_t chunk = 0;   // elements of the split axis per CTA
+  bool generic = false;
+};
+
+}  // namespace sgmev
+
+using namespace sgmev;
+
+struct sgmev_op {
+  int dim = 0;
+  int64_t n = 0, m = 0, npad = 0, mpad = 0;
+  int precision = SGMEV_FP64;
+  int device = 0;
+  int num_sms = 152;
+  int64_t target_ctas = 4 * 152;
+
+  double* xt64 = nullptr;
+  float* xt32 = nullptr;
+  double2* li64 = nullptr;
+  float2* li32 = nullptr;
+  int64_t npad_cap = 0;
+
+  // work vectors
+  double* a64 = nullptr;   // [npad] converted input (mult) / padded grid vector
+  float* a32 = nullptr;    // [npad]
+  double* v64 = nullptr;   // [mpad] data-side vector (mult output / multT input)
+  float* v32 = nullptr;    // [mpad]
+  double* out64 = nullptr; // [max(npad, mpad)]
+  void* part = nullptr;
+  size_t part_bytes = 0;
+  int64_t part_elems = 0;  // capacity of `part` in doubles
+
+  // CG vectors (FP64, npad each)
+  double* cg = nullptr;  // 8 vectors: b, alpha, r, d, q, t, delta, spare
+  double* dot_part = nullptr;
+  double* dot_out = nullptr;
+  double* host_scalar = nullptr;  // pinned
+
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+  double last_seconds = -1.0;
+  int64_t launches = 0;
+
+  std::vector<double> bb_left, bb_width;
+};
+
+namespace sgmev {
+
+// ---------------------------------------------------------------------------------------
+// staging kernels
+// ---------------------------------------------------------------------------------------
+__global__ void stage_data_kernel(const double* __restrict__ rows, int64_t m, int dim,
+                                  int64_t mpad, const double* __restrict__ bb_left,
+                                  const double* __restrict__ bb_width, double* __restrict__ xt64,
+                                  float* __restrict__ xt32) {
+  const int64_t total = mpad * dim;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int t = static_cast<int>(k / mpad);
+    const int64_t j = k - static_cast<int64_t>(t) * mpad;
+    double x = 0.0;
+    if (j < m) {
+      x = rows[j * dim + t];
+      if (bb_left) x = (x - bb_left[t]) / bb_width[t];
+    }
+    xt64[k] = x;
+    xt32[k] = static_cast<float>(x);
+  }
+}
+
+__global__ void stage_grid_kernel(const double* __restrict__ level_pow2,
+                                  const double* __restrict__ index, int64_t n, int dim,
+                                  int64_t npad, double2* __restrict__ li64,
+                                  float2* __restrict__ li32) {
+  const int64_t total = npad * dim;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double L = 0.0, I = 2.0;  // padded row: t = -2, hat = 0
+    if (k < n * dim) {
+      L = level_pow2[k];
+      I = index[k];
+    }
+    li64[k] = make_double2(L, I);
+    li32[k] = make_float2(static_cast<float>(L), static_cast<float>(I));
+  }
+}
+
+__global__ void convert_pad_kernel(const double* __restrict__ in, int64_t n, int64_t npad,
+                                   double* __restrict__ out64, float* __restrict__ out32) {
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < npad;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const double v = k < n ? in[k] : 0.0;
+    if (out64) out64[k] = v;
+    if (out32) out32[k] = static_cast<float>(v);
+  }
+}
+
+// deterministic dot product: fixed grid, fixed tree
+__global__ void dot_partial_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                                   int64_t n, double* __restrict__ part) {
+  __shared__ double s[kDotThreads];
+  double acc = 0.0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    acc = fma(a[i], b[i], acc);
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = kDotThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = s[0];
+}
+
+__global__ void dot_final_kernel(const double* __restrict__ part, int np, double* __restrict__ out) {
+  __shared__ double s[kDotThreads];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < np; i += kDotThreads) acc += part[i];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = kDotThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = s[0];
+}
+
+// y = a*x + y
+__global__ void axpy_kernel(int64_t n, double a, const double* __restrict__ x,
+                            double* __restrict__ y) {
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    y[i] = fma(a, x[i], y[i]);
+}
+
+// d = beta*d + r
+__global__ void xpby_kernel(int64_t n, const double* __restrict__ r, double beta,
+                            double* __restrict__ d) {
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    d[i] = fma(beta, d[i], r[i]);
+}
+
+// z = x - y
+__global__ void sub_kernel(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
+                           double* __restrict__ z) {
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    z[i] = x[i] - y[i];
+}
+
+// ---------------------------------------------------------------------------------------
+// launch planning and dispatch
+// ---------------------------------------------------------------------------------------
+template <typename T>
+static Plan plan_mult(const sgmev_op* op, int64_t tiles_total) {
+  Plan p;
+  p.generic = op->dim > kMaxTemplDim;
+  p.tiles = tiles_total;
+  // splits along the grid axis: at most one per grid tile and at most what the partial buffer
+  // holds at a stride of mpad
+  const int64_t max_split = std::max<int64_t>(
+      1, std::min<int64_t>(op->npad / kGT, op->part_elems / op->mpad));
+  int64_t want = ceil_div(op->target_ctas, std::max<int64_t>(p.tiles, 1));
+  want = std::max<int64_t>(1, std::min(want, max_split));
+  p.chunk = round_up(ceil_div(op->npad, want), kGT);
+  p.nsplit = ceil_div(op->npad, p.chunk);
+  return p;
+}
+
+template <typename T>
+static Plan plan_multt(const sgmev_op* op, int64_t tiles_total) {
+  Plan p;
+  p.generic = op->dim > kMaxTemplDim;
+  p.tiles = tiles_total;
+  const int64_t max_split = std::max<int64_t>(
+      1, std::min<int64_t>(op->mpad / kDT, op->part_elems / op->npad));
+  int64_t want = ceil_div(op->target_ctas, std::max<int64_t>(p.tiles, 1));
+  want = std::max<int64_t>(1, std::min(want, max_split));
+  p.chunk = round_up(ceil_div(op->mpad, want), kDT);
+  p.nsplit = ceil_div(op->mpad, p.chunk);
+  return p;
+}
+
+template <typename T, int DIM>
+static void launch_mult_dim(sgmev_op* op, const T* xt, const typename Pair<T>::type* li,
+                            const T* alpha, const Plan& p, int64_t tile_offset, T* part) {
+  constexpr int R = Blocking<T>::mult_r(DIM);
+  dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+  mult_kernel<T, DIM, R, kBlock, kGT><<<grid, kBlock, 0, op->stream>>>(
+      xt, op->mpad, li, alpha, op->npad, p.chunk, tile_offset, part);
+}
+
+template <typename T, int DIM>
+static void launch_multt_dim(sgmev_op* op, const T* xt, const T* v,
+                             const typename Pair<T>::type* li, const Plan& p, int64_t tile_offset,
+                             T* part) {
+  constexpr int RG = Blocking<T>::multt_r(DIM);
+  dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+  mult_transpose_kernel<T, DIM, RG, kBlock, kDT><<<grid, kBlock, 0, op->stream>>>(
+      xt, v, op->mpad, li, op->npad, p.chunk, tile_offset, part);
+}
+
+#define SGMEV_DIM_CASES(F) \
+  F(1) F(2) F(3) F(4) F(5) F(6) F(7) F(8) F(9) F(10) F(11) F(12) F(13) F(14) F(15) F(16)
+
+// mult over data range [j_begin, j_end): partial sums into op->part, returns the plan used.
+template <typename T>
+static int run_mult(sgmev_op* op, const T* xt, const typename Pair<T>::type* li, const T* alpha,
+                    int64_t j_begin, int64_t j_end, Plan* used) {
+  T* part = static_cast<T*>(op->part);
+  if (op->dim <= kMaxTemplDim) {
+    const int64_t tile_pts = kBlock * Blocking<T>::mult_r(op->dim);
+    const int64_t t0 = j_begin / tile_pts;
+    const int64_t t1 = ceil_div(j_end, tile_pts);
+    Plan p = plan_mult<T>(op, t1 - t0);
+    switch (op->dim) {
+#define F(D)                                                         \
+  case D:                                                            \
+    launch_mult_dim<T, D>(op, xt, li, alpha, p, t0, part);           \
+    break;
+      SGMEV_DIM_CASES(F)
+#undef F
+      default:
+        break;
+    }
+    *used = p;
+  } else {
+    const int64_t count = j_end - j_begin;
+    Plan p = plan_mult<T>(op, ceil_div(count, kBlock));
+    dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+    mult_generic_kernel<T><<<grid, kBlock, 0, op->stream>>>(xt, op->mpad, op->dim, li, alpha,
+                                                            op->npad, p.chunk, j_begin, count,
+                                                            part);
+    *used = p;
+  }
+  op->launches += 1;
+  SGMEV_CUDA(cudaGetLastError());
+  return SGMEV_OK;
+}
+
+template <typename T>
+static int run_multt(sgmev_op* op, const T* xt, const T* v, const typename Pair<T>::type* li,
+                     int64_t g_begin, int64_t g_end, Plan* used) {
+  T* part = static_cast<T*>(op->part);
+  if (op->dim <= kMaxTemplDim) {
+    const int64_t tile_pts = kBlock * Blocking<T>::multt_r(op->dim);
+    const int64_t t0 = g_begin / tile_pts;
+    const int64_t t1 = ceil_div(g_end, tile_pts);
+    Plan p = plan_multt<T>(op, t1 - t0);
+    switch (op->dim) {
+#define F(D)                                                      \
+  case D:                                                         \
+    launch_multt_dim<T, D>(op, xt, v, li, p, t0, part);           \
+    break;
+      SGMEV_DIM_CASES(F)
+#undef F
+      default:
+        break;
+    }
+    *used = p;
+  } else {
+    const int64_t count = g_end - g_begin;
+    Plan p = plan_multt<T>(op, ceil_div(count, kBlock));
+    dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+    mult_transpose_generic_kernel<T><<<grid, kBlock, 0, op->stream>>>(
+        xt, v, op->mpad, op->dim, li, op->npad, p.chunk, g_begin, count, part);
+    *used = p;
+  }
+  op->launches += 1;
+  SGMEV_CUDA(cudaGetLastError());
+  return SGMEV_OK;
+}
+
+template <typename TP, typename TO>
+static int run_reduce(sgmev_op* op, int nsplit, int64_t stride, int64_t begin, int64_t n_valid,
+                      int64_t n_total, TO* out, const double* add, double scale) {
+  const int64_t work = std::max<int64_t>(n_total - begin, 1);
+  const unsigned blocks =
+      static_cast<unsigned>(std::min<int64_t>(kReduceBlocks, ceil_div(work, 256)));
+  reduce_splits_kernel<TP, TO><<<blocks, 256, 0, op->stream>>>(
+      static_cast<const TP*>(op->part), nsplit, stride, begin, n_valid, n_total, out, add, scale);
+  op->launches += 1;
+  SGMEV_CUDA(cudaGetLastError());
+  return SGMEV_OK;
+}
+
+static unsigned vec_blocks(int64_t n) {
+  return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(kReduceBlocks, ceil_div(n, 256))));
+}
+
+// ---------------------------------------------------------------------------------------
+// device-side products on padded device vectors
+// ---------------------------------------------------------------------------------------
+// v_out[mpad] (zero beyond m) = B * a_in[npad]   in precision `prec`; a_in must be padded.
+static int dev_mult(sgmev_op* op, int prec, const double* a_in64, const float* a_in32,
+                    double* out64, float* out32, int64_t j_begin, int64_t j_end) {
+  if (j_end <= j_begin) return SGMEV_OK;
+  Plan p;
+  if (prec == SGMEV_FP64) {
+    SGMEV_TRY(run_mult<double>(op, op->xt64, op->li64, a_in64, j_begin, j_end, &p));
+  } else {
+    SGMEV_TRY(run_mult<float>(op, op->xt32, op->li32, a_in32, j_begin, j_end, &p));
+  }
+  const int64_t total = j_end;
+  if (prec == SGMEV_FP64) {
+    if (out64) SGMEV_TRY((run_reduce<double, double>(op, (int)p.nsplit, op->mpad, j_begin, std::min(op->m, total), total, out64, nullptr, 0.0)));
+    if (out32) SGMEV_TRY((run_reduce<double, float>(op, (int)p.nsplit, op->mpad, j_begin, std::min(op->m, total), total, out32, nullptr, 0.0)));
+  } else {
+    if (out64) SGMEV_TRY((run_reduce<float, double>(op, (int)p.nsplit, op->mpad, j_begin, std::min(op->m, total), total, out64, nullptr, 0.0)));
+    if (out32) SGMEV_TRY((run_reduce<float, float>(op, (int)p.nsplit, op->mpad, j_begin, std::min(op->m, total), total, out32, nullptr, 0.0)));
+  }
+  return SGMEV_OK;
+}
+
+// out64[g_begin..g_end) = B^T v_in[mpad] (+ scale * add)
+static int dev_multt(sgmev_op* op, int prec, const double* v_in64, const float* v_in32,
+                     double* out64, int64_t g_begin, int64_t g_end, const double* add,
+                     double scale) {
+  if (g_end <= g_begin) return SGMEV_OK;
+  Plan p;
+  if (prec == SGMEV_FP64) {
+    SGMEV_TRY(run_multt<double>(op, op->xt64, v_in64, op->li64, g_begin, g_end, &p));
+    SGMEV_TRY((run_reduce<double, double>(op, (int)p.nsplit, op->npad, g_begin, std::min(op->n, g_end), g_end, out64, add, scale)));
+  } else {
+    SGMEV_TRY(run_multt<float>(op, op->xt32, v_in32, op->li32, g_begin, g_end, &p));
+    SGMEV_TRY((run_reduce<float, double>(op, (int)p.nsplit, op->npad, g_begin, std::min(op->n, g_end), g_end, out64, add, scale)));
+  }
+  return SGMEV_OK;
+}
+
+// out64[npad] = B^T (B a) + lm * a, a given as padded FP64 device vector [npad]
+static int dev_system(sgmev_op* op, int prec, const double* a64, double* out64, double lm) {
+  if (prec == SGMEV_FP32) {
+    convert_pad_kernel<<<vec_blocks(op->npad), 256, 0, op->stream>>>(a64, op->npad, op->npad,
+                                                                      nullptr, op->a32);
+    op->launches += 1;
+    SGMEV_TRY(dev_mult(op, prec, nullptr, op->a32, nullptr, op->v32, 0, op->mpad));
+    SGMEV_TRY(dev_multt(op, prec, nullptr, op->v32, out64, 0, op->npad, a64, lm));
+  } else {
+    SGMEV_TRY(dev_mult(op, prec, a64, nullptr, op->v64, nullptr, 0, op->mpad));
+    SGMEV_TRY(dev_multt(op, prec, op->v64, nullptr, out64, 0, op->npad, a64, lm));
+  }
+  return SGMEV_OK;
+}
+
+static int dev_dot(sgmev_op* op, const double* a, const double* b, int64_t n, double* host_out) {
+  dot_partial_kernel<<<kDotBlocks, kDotThreads, 0, op->stream>>>(a, b, n, op->dot_part);
+  dot_final_kernel<<<1, kDotThreads, 0, op->stream>>>(op->dot_part, kDotBlocks, op->dot_out);
+  op->launches += 2;
+  SGMEV_CUDA(cudaGetLastError());
+  SGMEV_CUDA(cudaMemcpyAsync(op->host_scalar, op->dot_out, sizeof(double),
+                             cudaMemcpyDeviceToHost, op->stream));
+  SGMEV_CUDA(cudaStreamSynchronize(op->stream));
+  *host_out = *op->host_scalar;
+  return SGMEV_OK;
+}
+
+static int dev_axpy(sgmev_op* op, int64_t n, double a, const double* x, double* y) {
+  axpy_kernel<<<vec_blocks(n), 256, 0, op->stream>>>(n, a, x, y);
+  op->launches += 1;
+  SGMEV_CUDA(cudaGetLastError());
+  return SGMEV_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// allocation helpers
+// ---------------------------------------------------------------------------------------
+template <typename T>
+static int dalloc(T** p, size_t count) {
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  if (count == 0) count = 1;
+  SGMEV_CUDA(cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T)));
+  return SGMEV_OK;
+}
+
+// Partial-sum capacity: enough for the full-range plans of both products (the split count
+// a full-range launch wants is ceil(target_ctas / tiles)), and at least 8 strides of each axis.
+// Ranged launches clamp their split count to this capacity.
+static int64_t part_need_elems(const sgmev_op* op) {
+  int64_t need = 8 * std::max(op->mpad, op->npad);
+  const int rm[2] = {Blocking<float>::mult_r(op->dim), Blocking<double>::mult_r(op->dim)};
+  const int rt[2] = {Blocking<float>::multt_r(op->dim), Blocking<double>::multt_r(op->dim)};
+  for (int k = 0; k < 2; ++k) {
+    const int64_t mt = op->dim > kMaxTemplDim ? ceil_div(op->mpad, kBlock) : op->mpad / (kBlock * rm[k]);
+    const int64_t nt = op->dim > kMaxTemplDim ? ceil_div(op->npad, kBlock) : op->npad / (kBlock * rt[k]);
+    const int64_t sm = std::min<int64_t>(op->npad / kGT, ceil_div(op->target_ctas, std::max<int64_t>(mt, 1)));
+    const int64_t st = std::min<int64_t>(op->mpad / kDT, ceil_div(op->target_ctas, std::max<int64_t>(nt, 1)));
+    need = std::max(need, std::max(sm * op->mpad, st * op->npad));
+  }
+  return need;
+}
+
+static int check_grid(int dim, int64_t n, const double* level_pow2, const double* index) {
+  for (int64_t k = 0; k < n * dim; ++k) {
+    const double L = level_pow2[k], I = index[k];
+    if (!(L >= 2.0) || L > 1099511627776.0 || std::floor(L) != L) {
+      return fail(SGMEV_ERR_UNSUPPORTED,
+                  "level entry " + std::to_string(k) + " is not 2^l with l >= 1 (hat basis "
+                  "without boundary only)");
+    }
+    const double lg = std::log2(L);
+    if (std::floor(lg) != lg) {
+      return fail(SGMEV_ERR_UNSUPPORTED, "level entry " + std::to_string(k) + " is not a power of two");
+    }
+    if (!(I >= 1.0) || !(I < L) || std::floor(I) != I || std::fmod(I, 2.0) != 1.0) {
+      return fail(SGMEV_ERR_UNSUPPORTED,
+                  "index entry " + std::to_string(k) + " is not an odd integer in (0, 2^l)");
+    }
+  }
+  return SGMEV_OK;
+}
+
+static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const double* index) {
+  const int64_t npad = std::max<int64_t>(round_up(std::max<int64_t>(n, 1), kNPadTo), kNPadTo);
+  if (npad > op->npad_cap) {
+    SGMEV_TRY(dalloc(&op->li64, static_cast<size_t>(npad * op->dim)));
+    SGMEV_TRY(dalloc(&op->li32, static_cast<size_t>(npad * op->dim)));
+    SGMEV_TRY(dalloc(&op->a64, static_cast<size_t>(npad)));
+    SGMEV_TRY(dalloc(&op->a32, static_cast<size_t>(npad)));
+    SGMEV_TRY(dalloc(&op->cg, static_cast<size_t>(npad) * 8));
+    op->npad_cap = npad;
+  }
+  op->n = n;
+  op->npad = npad;
+  double* d_l = nullptr;
+  double* d_i = nullptr;
+  const size_t bytes = sizeof(double) * static_cast<size_t>(std::max<int64_t>(n * op->dim, 1));
+  SGMEV_CUDA(cudaMalloc(&d_l, bytes));
+  cudaError_t e = cudaMalloc(&d_i, bytes);
+  if (e != cudaSuccess) {
+    cudaFree(d_l);
+    return fail(SGMEV_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  if (n > 0) {
+    cudaMemcpyAsync(d_l, level_pow2, bytes, cudaMemcpyHostToDevice, op->stream);
+    cudaMemcpyAsync(d_i, index, bytes, cudaMemcpyHostToDevice, op->stream);
+  }
+  stage_grid_kernel<<<vec_blocks(npad * op->dim), 256, 0, op->stream>>>(d_l, d_i, n, op->dim,
+                                                                         npad, op->li64, op->li32);
+  op->launches += 1;
+  e = cudaStreamSynchronize(op->stream);
+  cudaFree(d_l);
+  cudaFree(d_i);
+  if (e != cudaSuccess) return fail(SGMEV_ERR_CUDA, std::string("stage grid: ") + cudaGetErrorString(e));
+  // output vector and split partials depend on npad
+  SGMEV_TRY(dalloc(&op->out64, static_cast<size_t>(std::max(op->npad, op->mpad))));
+  const int64_t elems = part_need_elems(op);
+  const size_t need = static_cast<size_t>(elems) * sizeof(double);
+  if (need > op->part_bytes) {
+    if (op->part) cudaFree(op->part);
+    op->part = nullptr;
+    op->part_bytes = 0;
+    op->part_elems = 0;
+    SGMEV_CUDA(cudaMalloc(&op->part, need));
+    op->part_bytes = need;
+  }
+  op->part_elems = static_cast<int64_t>(op->part_bytes / sizeof(double));
+  return SGMEV_OK;
+}
+
+static void release(sgmev_op* op) {
+  void* ptrs[] = {op->xt64, op->xt32, op->li64, op->li32, op->a64, op->a32, op->v64,
+                  op->v32,  op->out64, op->part, op->cg,   op->dot_part, op->dot_out};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (op->host_scalar) cudaFreeHost(op->host_scalar);
+  if (op->ev_start) cudaEventDestroy(op->ev_start);
+  if (op->ev_stop) cudaEventDestroy(op->ev_stop);
+  if (op->own_stream) cudaStreamDestroy(op->own_stream);
+}
+
+static int begin_timed(sgmev_op* op) {
+  SGMEV_CUDA(cudaEventRecord(op->ev_start, op->stream));
+  return SGMEV_OK;
+}
+
+static int end_timed(sgmev_op* op, bool sync) {
+  SGMEV_CUDA(cudaEventRecord(op->ev_stop, op->stream));
+  if (sync) {
+    SGMEV_CUDA(cudaEventSynchronize(op->ev_stop));
+    float ms = 0.f;
+    SGMEV_CUDA(cudaEventElapsedTime(&ms, op->ev_start, op->ev_stop));
+    op->last_seconds = ms * 1e-3;
+  }
+  return SGMEV_OK;
+}
+
+static int check_op(const sgmev_op* op) {
+  if (!op) return fail(SGMEV_ERR_INVALID, "op is NULL");
+  return SGMEV_OK;
+}
+
+}  // namespace sgmev
+
+// =========================================================================================
+// C ABI
+// =========================================================================================
+extern "C" {
+
+SGMEV_API const char* sgmev_last_error(void) { return sgmev::g_last_error.c_str(); }
+
+SGMEV_API int sgmev_version(void) { return 10000; }
+
+SGMEV_API int sgmev_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double* level_pow2,
+                           const double* index, int64_t n_data, const double* data,
+                           const double* bb_left, const double* bb_right, int precision,
+                           const char* params_json) {
+  using namespace sgmev;
+  g_last_error.clear();
+  if (!out) return fail(SGMEV_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (dim < 1) return fail(SGMEV_ERR_INVALID, "dim must be >= 1");
+  if (n_grid < 0 || n_data < 0) return fail(SGMEV_ERR_INVALID, "negative size");
+  if (n_grid > 0 && (!level_pow2 || !index)) return fail(SGMEV_ERR_INVALID, "level/index is NULL");
+  if (n_data > 0 && !data) return fail(SGMEV_ERR_INVALID, "data is NULL");
+  if ((bb_left == nullptr) != (bb_right == nullptr))
+    return fail(SGMEV_ERR_INVALID, "bounding box needs both left and right");
+  if (precision != SGMEV_FP64 && precision != SGMEV_FP32)
+    return fail(SGMEV_ERR_INVALID, "precision must be SGMEV_FP64 or SGMEV_FP32");
+  if (n_data > (int64_t(1) << 40) || n_grid > (int64_t(1) << 34))
+    return fail(SGMEV_ERR_INVALID, "problem too large");
+  SGMEV_TRY(check_grid(dim, n_grid, level_pow2, index));
+  if (bb_left) {
+    for (int t = 0; t < dim; ++t)
+      if (!(bb_right[t] > bb_left[t]))
+        return fail(SGMEV_ERR_INVALID, "bounding box interval " + std::to_string(t) + " is empty");
+  }
+  (void)params_json;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(SGMEV_ERR_NO_DEVICE, "no CUDA device is visible");
+  }
+
+  sgmev_op* op = new sgmev_op;
+  op->dim = dim;
+  op->precision = precision;
+  op->m = n_data;
+  op->mpad = std::max<int64_t>(round_up(std::max<int64_t>(n_data, 1), kMPadTo), kMPadTo);
+  auto bail = [&](int rc) {
+    release(op);
+    delete op;
+    return rc;
+  };
+#define CREATE_CUDA(call)                                                               \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return bail(fail(e_ == cudaErrorMemoryAllocation ? SGMEV_ERR_OOM : SGMEV_ERR_CUDA, \
+                       std::string(#call) + ": " + cudaGetErrorString(e_)));            \
+  } while (0)
+#define CREATE_TRY(expr)               \
+  do {                                 \
+    int rc_ = (expr);                  \
+    if (rc_ != SGMEV_OK) return bail(rc_); \
+  } while (0)
+
+  CREATE_CUDA(cudaGetDevice(&op->device));
+  CREATE_CUDA(cudaDeviceGetAttribute(&op->num_sms, cudaDevAttrMultiProcessorCount, op->device));
+  op->target_ctas = static_cast<int64_t>(op->num_sms) * 4;
+  CREATE_CUDA(cudaStreamCreateWithFlags(&op->own_stream, cudaStreamNonBlocking));
+  op->stream = op->own_stream;
+  CREATE_CUDA(cudaEventCreate(&op->ev_start));
+  CREATE_CUDA(cudaEventCreate(&op->ev_stop));
+  CREATE_CUDA(cudaMallocHost(&op->host_scalar, sizeof(double) * 8));
+  CREATE_TRY(dalloc(&op->dot_part, kDotBlocks));
+  CREATE_TRY(dalloc(&op->dot_out, 8));
+
+  // data
+  CREATE_TRY(dalloc(&op->xt64, static_cast<size_t>(op->mpad * dim)));
+  CREATE_TRY(dalloc(&op->xt32, static_cast<size_t>(op->mpad * dim)));
+  CREATE_TRY(dalloc(&op->v64, static_cast<size_t>(op->mpad)));
+  CREATE_TRY(dalloc(&op->v32, static_cast<size_t>(op->mpad)));
+  {
+    double* d_rows = nullptr;
+    double* d_bb = nullptr;
+    const size_t rbytes = sizeof(double) * static_cast<size_t>(std::max<int64_t>(n_data * dim, 1));
+    CREATE_CUDA(cudaMalloc(&d_rows, rbytes));
+    if (n_data > 0) cudaMemcpyAsync(d_rows, data, rbytes, cudaMemcpyHostToDevice, op->stream);
+    if (bb_left) {
+      op->bb_left.assign(bb_left, bb_left + dim);
+      op->bb_width.resize(dim);
+      std::vector<double> hb(2 * dim);
+      for (int t = 0; t < dim; ++t) {
+        op->bb_width[t] = bb_right[t] - bb_left[t];
+        hb[t] = bb_left[t];
+        hb[dim + t] = op->bb_width[t];
+      }
+      cudaError_t e = cudaMalloc(&d_bb, sizeof(double) * 2 * dim);
+      if (e != cudaSuccess) {
+        cudaFree(d_rows);
+        return bail(fail(SGMEV_ERR_OOM, "cudaMalloc bounding box"));
+      }
+      cudaMemcpyAsync(d_bb, hb.data(), sizeof(double) * 2 * dim, cudaMemcpyHostToDevice, op->stream);
+    }
+    stage_data_kernel<<<vec_blocks(op->mpad * dim), 256, 0, op->stream>>>(
+        d_rows, n_data, dim, op->mpad, d_bb, d_bb ? d_bb + dim : nullptr, op->xt64, op->xt32);
+    op->launches += 1;
+    cudaError_t e = cudaStreamSynchronize(op->stream);
+    cudaFree(d_rows);
+    if (d_bb) cudaFree(d_bb);
+    if (e != cudaSuccess) return bail(fail(SGMEV_ERR_CUDA, std::string("stage data: ") + cudaGetErrorString(e)));
+  }
+  CREATE_TRY(stage_grid(op, n_grid, level_pow2, index));
+#undef CREATE_CUDA
+#undef CREATE_TRY
+  *out = op;
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_destroy(sgmev_op* op) {
+  if (!op) return SGMEV_OK;
+  if (op->stream) cudaStreamSynchronize(op->stream);
+  sgmev::release(op);
+  delete op;
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_prepare(sgmev_op* op, int64_t n_grid, const double* level_pow2,
+                            const double* index) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if (n_grid < 0) return fail(SGMEV_ERR_INVALID, "negative size");
+  if (n_grid > 0 && (!level_pow2 || !index)) return fail(SGMEV_ERR_INVALID, "level/index is NULL");
+  SGMEV_TRY(check_grid(op->dim, n_grid, level_pow2, index));
+  SGMEV_CUDA(cudaStreamSynchronize(op->stream));
+  return stage_grid(op, n_grid, level_pow2, index);
+}
+
+SGMEV_API int sgmev_get_sizes(const sgmev_op* op, int* dim, int64_t* n_grid, int64_t* n_data) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if (dim) *dim = op->dim;
+  if (n_grid) *n_grid = op->n;
+  if (n_data) *n_data = op->m;
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_set_stream(sgmev_op* op, void* stream) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  op->stream = stream ? static_cast<cudaStream_t>(stream) : op->own_stream;
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_synchronize(sgmev_op* op) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  SGMEV_CUDA(cudaStreamSynchronize(op->stream));
+  return SGMEV_OK;
+}
+
+SGMEV_API int64_t sgmev_kernel_launches(const sgmev_op* op) { return op ? op->launches : 0; }
+
+SGMEV_API double sgmev_get_duration(sgmev_op* op) { return op ? op->last_seconds : -1.0; }
+
+static int mult_common(sgmev_op* op, const double* alpha_dev_or_null, const double* alpha_host,
+                       double* result_dev, double* result_host, int64_t start, int64_t end) {
+  using namespace sgmev;
+  const int prec = op->precision;
+  SGMEV_TRY(begin_timed(op));
+  const double* src = alpha_dev_or_null;
+  if (alpha_host) {
+    if (op->n > 0)
+      SGMEV_CUDA(cudaMemcpyAsync(op->out64, alpha_host, sizeof(double) * op->n,
+                                 cudaMemcpyHostToDevice, op->stream));
+    src = op->out64;
+  }
+  convert_pad_kernel<<<vec_blocks(op->npad), 256, 0, op->stream>>>(
+      src, op->n, op->npad, prec == SGMEV_FP64 ? op->a64 : nullptr,
+      prec == SGMEV_FP32 ? op->a32 : nullptr);
+  op->launches += 1;
+  // tile-aligned data range covering [start, end)
+  const int64_t tile_pts = kBlock * (prec == SGMEV_FP64 ? Blocking<double>::mult_r(op->dim)
+                                                        : Blocking<float>::mult_r(op->dim));
+  const int64_t jb = op->dim <= kMaxTemplDim ? (start / tile_pts) * tile_pts : start;
+  const int64_t je = op->dim <= kMaxTemplDim ? std::min(op->mpad, round_up(end, tile_pts)) : end;
+  SGMEV_TRY(dev_mult(op, prec, op->a64, op->a32, op->v64, nullptr, jb, je));
+  if (result_host) {
+    if (end > start)
+      SGMEV_CUDA(cudaMemcpyAsync(result_host + start, op->v64 + start,
+                                 sizeof(double) * (end - start), cudaMemcpyDeviceToHost,
+                                 op->stream));
+  } else if (result_dev && end > start) {
+    SGMEV_CUDA(cudaMemcpyAsync(result_dev + start, op->v64 + start, sizeof(double) * (end - start),
+                               cudaMemcpyDeviceToDevice, op->stream));
+  }
+  SGMEV_TRY(end_timed(op, result_host != nullptr));
+  return SGMEV_OK;
+}
+
+static int multt_common(sgmev_op* op, const double* src_dev, const double* src_host,
+                        double* result_dev, double* result_host, int64_t start, int64_t end) {
+  using namespace sgmev;
+  const int prec = op->precision;
+  SGMEV_TRY(begin_timed(op));
+  const double* src = src_dev;
+  if (src_host) {
+    if (op->m > 0)
+      SGMEV_CUDA(cudaMemcpyAsync(op->out64, src_host, sizeof(double) * op->m,
+                                 cudaMemcpyHostToDevice, op->stream));
+    src = op->out64;
+  }
+  convert_pad_kernel<<<vec_blocks(op->mpad), 256, 0, op->stream>>>(
+      src, op->m, op->mpad, prec == SGMEV_FP64 ? op->v64 : nullptr,
+      prec == SGMEV_FP32 ? op->v32 : nullptr);
+  op->launches += 1;
+  const int64_t tile_pts = kBlock * (prec == SGMEV_FP64 ? Blocking<double>::multt_r(op->dim)
+                                                        : Blocking<float>::multt_r(op->dim));
+  const int64_t gb = op->dim <= kMaxTemplDim ? (start / tile_pts) * tile_pts : start;
+  const int64_t ge = op->dim <= kMaxTemplDim ? std::min(op->npad, round_up(end, tile_pts)) : end;
+  double* tmp = op->cg + 7 * op->npad;  // spare CG slot as result staging
+  SGMEV_TRY(dev_multt(op, prec, op->v64, op->v32, tmp, gb, ge, nullptr, 0.0));
+  if (result_host) {
+    if (end > start)
+      SGMEV_CUDA(cudaMemcpyAsync(result_host + start, tmp + start, sizeof(double) * (end - start),
+                                 cudaMemcpyDeviceToHost, op->stream));
+  } else if (result_dev && end > start) {
+    SGMEV_CUDA(cudaMemcpyAsync(result_dev + start, tmp + start, sizeof(double) * (end - start),
+                               cudaMemcpyDeviceToDevice, op->stream));
+  }
+  SGMEV_TRY(end_timed(op, result_host != nullptr));
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_mult(sgmev_op* op, const double* alpha, double* result) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if ((op->n > 0 && !alpha) || (op->m > 0 && !result)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  return mult_common(op, nullptr, alpha, nullptr, result, 0, op->m);
+}
+
+SGMEV_API int sgmev_mult_transpose(sgmev_op* op, const double* source, double* result) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if ((op->m > 0 && !source) || (op->n > 0 && !result)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  return multt_common(op, nullptr, source, nullptr, result, 0, op->n);
+}
+
+SGMEV_API int sgmev_mult_range(sgmev_op* op, const double* alpha, double* result,
+                               int64_t start_data, int64_t end_data) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if (start_data < 0 || end_data > op->m || start_data > end_data)
+    return fail(SGMEV_ERR_INVALID, "data range out of bounds");
+  if ((op->n > 0 && !alpha) || (end_data > start_data && !result)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  return mult_common(op, nullptr, alpha, nullptr, result, start_data, end_data);
+}
+
+SGMEV_API int sgmev_mult_transpose_range(sgmev_op* op, const double* source, double* result,
+                                         int64_t start_grid, int64_t end_grid) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if (start_grid < 0 || end_grid > op->n || start_grid > end_grid)
+    return fail(SGMEV_ERR_INVALID, "grid range out of bounds");
+  if ((op->m > 0 && !source) || (end_grid > start_grid && !result)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  return multt_common(op, nullptr, source, nullptr, result, start_grid, end_grid);
+}
+
+SGMEV_API int sgmev_mult_device(sgmev_op* op, const double* d_alpha, double* d_result) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if ((op->n > 0 && !d_alpha) || (op->m > 0 && !d_result)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  return mult_common(op, d_alpha, nullptr, d_result, nullptr, 0, op->m);
+}
+
+SGMEV_API int sgmev_mult_transpose_device(sgmev_op* op, const double* d_source,
+                                          double* d_result) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if ((op->m > 0 && !d_source) || (op->n > 0 && !d_result)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  return multt_common(op, d_source, nullptr, d_result, nullptr, 0, op->n);
+}
+
+static int system_common(sgmev_op* op, const double* a_dev, const double* a_host, double* r_dev,
+                         double* r_host, double lm) {
+  using namespace sgmev;
+  SGMEV_TRY(begin_timed(op));
+  double* a = op->cg + 6 * op->npad;  // padded copy of the input
+  double* r = op->cg + 7 * op->npad;
+  const double* src = a_dev;
+  if (a_host) {
+    if (op->n > 0)
+      SGMEV_CUDA(cudaMemcpyAsync(op->out64, a_host, sizeof(double) * op->n,
+                                 cudaMemcpyHostToDevice, op->stream));
+    src = op->out64;
+  }
+  convert_pad_kernel<<<vec_blocks(op->npad), 256, 0, op->stream>>>(src, op->n, op->npad, a, nullptr);
+  op->launches += 1;
+  SGMEV_TRY(dev_system(op, op->precision, a, r, lm));
+  if (r_host) {
+    if (op->n > 0)
+      SGMEV_CUDA(cudaMemcpyAsync(r_host, r, sizeof(double) * op->n, cudaMemcpyDeviceToHost, op->stream));
+  } else if (op->n > 0) {
+    SGMEV_CUDA(cudaMemcpyAsync(r_dev, r, sizeof(double) * op->n, cudaMemcpyDeviceToDevice, op->stream));
+  }
+  SGMEV_TRY(end_timed(op, r_host != nullptr));
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_system_apply(sgmev_op* op, const double* alpha, double* result,
+                                 double lambda_times_m) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if (op->n > 0 && (!alpha || !result)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  return system_common(op, nullptr, alpha, nullptr, result, lambda_times_m);
+}
+
+SGMEV_API int sgmev_system_apply_device(sgmev_op* op, const double* d_alpha, double* d_result,
+                                        double lambda_times_m) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if (op->n > 0 && (!d_alpha || !d_result)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  return system_common(op, d_alpha, nullptr, d_result, nullptr, lambda_times_m);
+}
+
+// CG on (B^T B + lm I) x = rhs with operator precision `prec`; all vectors padded device FP64.
+// Mirrors ConjugateGradients::solve (ConjugateGradients.cpp:22-151). x is the start vector
+// when reuse, otherwise zeroed. delta0_scale multiplies the starting delta (epsilon^2).
+static int cg_core(sgmev_op* op, int prec, const double* rhs, double* x, double lm,
+                   int64_t imax, double eps, bool reuse, int64_t* iters, double* delta_final) {
+  using namespace sgmev;
+  const int64_t np = op->npad;
+  double* r = op->cg + 2 * np;
+  double* d = op->cg + 3 * np;
+  double* q = op->cg + 4 * np;
+  double* t = op->cg + 5 * np;
+  const double eps2 = eps * eps;
+  double delta_0 = 0.0;
+  SGMEV_CUDA(cudaMemcpyAsync(r, rhs, sizeof(double) * np, cudaMemcpyDeviceToDevice, op->stream));
+  if (reuse) {
+    // A * 0 = 0, so r = rhs (ConjugateGradients.cpp:58-62)
+    SGMEV_TRY(dev_dot(op, r, r, np, &delta_0));
+    delta_0 *= eps2;
+  } else {
+    SGMEV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * np, op->stream));
+  }
+  if (reuse) {
+    // r = rhs - A x (ConjugateGradients.cpp:68-70); for x = 0 this product is exactly zero
+    // (0 * hat = 0, sums of zeros, lambda * 0), so the cold start skips it.
+    SGMEV_TRY(dev_system(op, prec, x, t, lm));
+    sub_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, r, t, r);
+    op->launches += 1;
+  }
+  SGMEV_CUDA(cudaMemcpyAsync(d, r, sizeof(double) * np, cudaMemcpyDeviceToDevice, op->stream));
+  double delta_new = 0.0;
+  SGMEV_TRY(dev_dot(op, r, r, np, &delta_new));
+  if (!reuse) delta_0 = delta_new * eps2;
+  int64_t it = 0;
+  while (it < imax && delta_new > delta_0 && delta_new > 0.0) {
+    SGMEV_TRY(dev_system(op, prec, d, q, lm));
+    double dq = 0.0;
+    SGMEV_TRY(dev_dot(op, d, q, np, &dq));
+    if (dq == 0.0) break;
+    const double a = delta_new / dq;
+    SGMEV_TRY(dev_axpy(op, np, a, d, x));
+    if (it % 50 == 0 && it > 0) {
+      SGMEV_TRY(dev_system(op, prec, x, t, lm));
+      sub_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, rhs, t, r);
+      op->launches += 1;
+    } else {
+      SGMEV_TRY(dev_axpy(op, np, -a, q, r));
+    }
+    const double delta_old = delta_new;
+    SGMEV_TRY(dev_dot(op, r, r, np, &delta_new));
+    const double beta = delta_new / delta_old;
+    xpby_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, r, beta, d);
+    op->launches += 1;
+    ++it;
+  }
+  SGMEV_CUDA(cudaGetLastError());
+  *iters = it;
+  *delta_final = delta_new;
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_fit(sgmev_op* op, int mode, const double* y, double lambda,
+                        int64_t max_iterations, double epsilon, int reuse, double* alpha,
+                        int64_t* iterations, double* residual) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if ((op->m > 0 && !y) || (op->n > 0 && !alpha)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  if (mode != SGMEV_SOLVE_PLAIN && mode != SGMEV_SOLVE_MIXED)
+    return fail(SGMEV_ERR_INVALID, "mode must be SGMEV_SOLVE_PLAIN or SGMEV_SOLVE_MIXED");
+  if (mode == SGMEV_SOLVE_MIXED && op->precision != SGMEV_FP64)
+    return fail(SGMEV_ERR_INVALID, "mixed mode needs an op created with SGMEV_FP64");
+  if (!(epsilon > 0.0) || max_iterations < 0) return fail(SGMEV_ERR_INVALID, "bad epsilon/max_iterations");
+  const int64_t np = op->npad;
+  double* b = op->cg;
+  double* x = op->cg + np;
+  const double lm = static_cast<double>(op->m) * lambda;
+  SGMEV_TRY(begin_timed(op));
+  // b = B^T y in FP64 (generateb)
+  if (op->m > 0)
+    SGMEV_CUDA(cudaMemcpyAsync(op->out64, y, sizeof(double) * op->m, cudaMemcpyHostToDevice, op->stream));
+  convert_pad_kernel<<<vec_blocks(op->mpad), 256, 0, op->stream>>>(op->out64, op->m, op->mpad, op->v64, op->v32);
+  op->launches += 1;
+  SGMEV_TRY(dev_multt(op, mode == SGMEV_SOLVE_MIXED ? SGMEV_FP64 : op->precision, op->v64, op->v32,
+                      b, 0, np, nullptr, 0.0));
+  if (reuse) {
+    double* tmp = op->cg + 7 * np;
+    if (op->n > 0)
+      SGMEV_CUDA(cudaMemcpyAsync(tmp, alpha, sizeof(double) * op->n, cudaMemcpyHostToDevice, op->stream));
+    convert_pad_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(tmp, op->n, np, x, nullptr);
+    op->launches += 1;
+  }
+  int64_t total_it = 0;
+  double res = 0.0;
+  if (mode == SGMEV_SOLVE_PLAIN) {
+    SGMEV_TRY(cg_core(op, op->precision, b, x, lm, max_iterations, epsilon, reuse != 0, &total_it, &res));
+  } else {
+    // iterative refinement: r = b - A64 x (FP64), solve A32 dx = r by CG, x += dx
+    double* rr = op->cg + 6 * np;  // outer residual (cg_core uses slots 2..5)
+    double* dx = op->cg + 7 * np;
+    if (!reuse) SGMEV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * np, op->stream));
+    double rnorm2 = 0.0, r0 = 0.0;
+    const double eps_inner = 1e-3;
+    for (int outer = 0; outer < 64; ++outer) {
+      SGMEV_TRY(dev_system(op, SGMEV_FP64, x, rr, lm));
+      sub_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, b, rr, rr);
+      op->launches += 1;
+      SGMEV_TRY(dev_dot(op, rr, rr, np, &rnorm2));
+      if (outer == 0) r0 = rnorm2;
+      res = rnorm2;
+      if (rnorm2 <= epsilon * epsilon * r0 || rnorm2 == 0.0 || total_it >= max_iterations) break;
+      int64_t it = 0;
+      double dres = 0.0;
+      const double want = std::max(eps_inner, epsilon * std::sqrt(r0 / rnorm2) * 0.5);
+      SGMEV_TRY(cg_core(op, SGMEV_FP32, rr, dx, lm, max_iterations - total_it, std::min(want, 0.5), false, &it, &dres));
+      total_it += it;
+      SGMEV_TRY(dev_axpy(op, np, 1.0, dx, x));
+    }
+  }
+  if (op->n > 0)
+    SGMEV_CUDA(cudaMemcpyAsync(alpha, x, sizeof(double) * op->n, cudaMemcpyDeviceToHost, op->stream));
+  SGMEV_TRY(end_timed(op, true));
+  if (iterations) *iterations = total_it;
+  if (residual) *residual = res;
+  return SGMEV_OK;
+}
+
+}  // extern "C"

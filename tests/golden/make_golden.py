@@ -1,0 +1,239 @@
+"""Generate the golden fixtures in this folder from the reference's own compiled code.
+
+Run where the reference sources exist (they are read only by oracle/ref.mk at build time):
+
+    make -f oracle/ref.mk -j8 && make -C oracle && python tests/golden/make_golden.py
+
+Every fixture comes from SG++'s own FP64 implementation (oracle/_ref/libsgpp_ref.so, built
+from the unmodified reference sources plus oracle/ref_harness.cpp), on seeded inputs:
+
+  grids.npz     regular Linear grids (HashGenerator::regular_iter order) — full arrays for
+                small grids, SHA-256 of the int32 level/index arrays for large ones
+  refine.npz    surplus-refinement sequences (SurplusRefinementFunctor + HashRefinement::free_refine)
+  multeval.npz  mult / multTranspose outputs of the DEFAULT (OperationMultipleEvalLinear) and
+                STREAMING (OperationMultiEvalStreaming) operators, with their inputs
+  cgfit.npz     regression fits through SystemMatrixLeastSquaresIdentity + ConjugateGradients
+  bt_linear.npz the reference's golden B^T matrices for the hat basis
+                (datadriven/datasets/BT_BBT/BT_phi_li_hut_*), reduced to the row sums and sorted
+                column sums that datadriven/tests/testBT.cpp compares, plus their data points
+"""
+from __future__ import annotations
+
+import gzip
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import REF_DEFAULT, REF_STREAMING, Reference  # noqa: E402
+
+REF_SRC = os.environ.get("SGPP_REFERENCE_SRC", "/root/reference")
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, np.int32).tobytes()).hexdigest()
+
+
+def edge_points(rng, m, d):
+    """Uniform points with a share of exact hat nodes / support edges / cube faces mixed in."""
+    x = rng.random((m, d))
+    k = max(1, m // 8)
+    nodes = rng.integers(0, 65, size=(k, d)) / 64.0  # exact dyadic grid nodes incl. 0 and 1
+    x[:k] = nodes
+    return x
+
+
+def make_grids(ref: Reference):
+    out = {}
+    cases = [(1, 3), (2, 2), (2, 5), (3, 4), (4, 3), (5, 6), (8, 4), (10, 3), (10, 5), (12, 3)]
+    for d, l in cases:
+        g = ref.grid(d, l)
+        lev, idx, leaf = g.points()
+        key = f"d{d}_l{l}"
+        out[key + "_n"] = np.int64(lev.shape[0])
+        out[key + "_sha_level"] = np.array(sha(lev))
+        out[key + "_sha_index"] = np.array(sha(idx))
+        if lev.shape[0] <= 400:
+            out[key + "_level"] = lev.astype(np.int8)
+            out[key + "_index"] = idx.astype(np.int16)
+            out[key + "_leaf"] = leaf.astype(np.int8)
+    np.savez_compressed(os.path.join(HERE, "grids.npz"), **out)
+
+
+def make_refine(ref: Reference):
+    out = {}
+    seqs = [("small", 4, 3, 3, 10, 11), ("cfg3", 8, 4, 6, 40, 12)]
+    for name, d, l, rounds, npts, seed in seqs:
+        rng = np.random.default_rng(seed)
+        g = ref.grid(d, l)
+        out[f"{name}_dim"] = np.int64(d)
+        out[f"{name}_level"] = np.int64(l)
+        out[f"{name}_rounds"] = np.int64(rounds)
+        out[f"{name}_npoints"] = np.int64(npts)
+        for r in range(rounds):
+            lev, idx, _ = g.points()
+            out[f"{name}_r{r}_pre_level"] = lev.astype(np.int8)
+            out[f"{name}_r{r}_pre_index"] = idx.astype(np.int16)
+            alpha = rng.standard_normal(g.size)
+            out[f"{name}_r{r}_alpha"] = alpha
+            g.refine_surplus(alpha, npts, 0.0)
+            lev, idx, _ = g.points()
+            out[f"{name}_r{r}_post_level"] = lev.astype(np.int8)
+            out[f"{name}_r{r}_post_index"] = idx.astype(np.int16)
+    np.savez_compressed(os.path.join(HERE, "refine.npz"), **out)
+
+
+def make_multeval(ref: Reference):
+    out = {}
+    cases = [
+        ("d1_l3_m8", 1, 3, 8, 0),
+        ("d2_l5_m300", 2, 5, 300, 0),
+        ("d3_l4_m512", 3, 4, 512, 0),
+        ("d5_l4_m1000", 5, 4, 1000, 0),
+        ("d5_l6_m2000", 5, 6, 2000, 0),       # the plain FP64 d=5 level 6 grid, fewer points
+        ("d10_l3_m777", 10, 3, 777, 0),       # ragged M (not a multiple of any chunk)
+        ("d10_l5_m300", 10, 5, 300, 0),       # the regression-fit grid
+        ("d8_l4_ad2_m1000", 8, 4, 1000, 2),   # adaptive: 2 surplus-refinement rounds of 40
+        ("d12_l3_m257", 12, 3, 257, 0),
+        ("d4_l3_m1", 4, 3, 1, 0),             # single data point
+    ]
+    rng = np.random.default_rng(20261203)
+    names = []
+    for name, d, l, m, rounds in cases:
+        g = ref.grid(d, l)
+        for _ in range(rounds):
+            g.refine_surplus(rng.standard_normal(g.size), 40, 0.0)
+        lev, idx, _ = g.points()
+        x = edge_points(rng, m, d)
+        alpha = rng.standard_normal(g.size)
+        v = rng.standard_normal(m)
+        out[name + "_level"] = lev.astype(np.int8)
+        out[name + "_index"] = idx.astype(np.int16)
+        out[name + "_x"] = x
+        out[name + "_alpha"] = alpha
+        out[name + "_v"] = v
+        out[name + "_mult_default"] = g.mult(REF_DEFAULT, x, alpha)
+        out[name + "_mult_streaming"] = g.mult(REF_STREAMING, x, alpha)
+        out[name + "_multt_default"] = g.mult_transpose(REF_DEFAULT, x, v)
+        out[name + "_multt_streaming"] = g.mult_transpose(REF_STREAMING, x, v)
+        names.append(name)
+    # bounding box: reference KAT layout (base/tests/test_OperationMultipleEval.cpp:24-79) and a
+    # random box, both through the DEFAULT operator which applies BoundingBox::transformPointToUnitCube
+    for name, d, l, m, left, right in [
+        ("bb_kat", 2, 2, 3, [3.0, -2.0], [5.0, 2.0]),
+        ("bb_rand", 3, 4, 400, [-1.0, 0.5, 2.0], [1.0, 2.5, 2.25]),
+    ]:
+        g = ref.grid(d, l)
+        g.set_bounding_box(left, right)
+        lev, idx, _ = g.points()
+        if name == "bb_kat":
+            x = np.array([[4.0, 2.0], [3.6, -0.4], [4.8, 0.8]])
+            alpha = np.arange(1, g.size + 1, dtype=np.float64)
+        else:
+            lo, hi = np.array(left), np.array(right)
+            x = lo + (hi - lo) * (rng.random((m, d)) * 1.2 - 0.1)  # some points outside the box
+            alpha = rng.standard_normal(g.size)
+        v = rng.standard_normal(x.shape[0])
+        out[name + "_level"] = lev.astype(np.int8)
+        out[name + "_index"] = idx.astype(np.int16)
+        out[name + "_x"] = x
+        out[name + "_alpha"] = alpha
+        out[name + "_v"] = v
+        out[name + "_bb_left"] = np.array(left)
+        out[name + "_bb_right"] = np.array(right)
+        out[name + "_mult_default"] = g.mult(REF_DEFAULT, x, alpha)
+        out[name + "_multt_default"] = g.mult_transpose(REF_DEFAULT, x, v)
+    out["cases"] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, "multeval.npz"), **out)
+
+
+def make_cgfit(ref: Reference):
+    out = {}
+    rng = np.random.default_rng(7)
+    cases = [("d4_l4", 4, 4, 3000, 1e-3), ("d6_l3", 6, 3, 2500, 1e-4)]
+    for name, d, l, m, lam in cases:
+        g = ref.grid(d, l)
+        x = rng.random((m, d))
+        y = (10 * np.sin(np.pi * x[:, 0] * x[:, 1]) + 20 * (x[:, 2] - 0.5) ** 2 + 10 * x[:, 3]
+             + 0.1 * rng.standard_normal(m))
+        lev, idx, _ = g.points()
+        alpha, it, res = g.cg_fit(REF_STREAMING, x, y, lam, 1000, 1e-12)
+        out[name + "_level"] = lev.astype(np.int8)
+        out[name + "_index"] = idx.astype(np.int16)
+        out[name + "_x"] = x
+        out[name + "_y"] = y
+        out[name + "_lambda"] = np.float64(lam)
+        out[name + "_alpha"] = alpha
+        out[name + "_iterations"] = np.int64(it)
+        out[name + "_residual"] = np.float64(res)
+    np.savez_compressed(os.path.join(HERE, "cgfit.npz"), **out)
+
+
+def read_arff(path):
+    rows = []
+    with gzip.open(path, "rt") as f:
+        data = False
+        for line in f:
+            s = line.strip()
+            if not s:
+                continue
+            if data:
+                rows.append([float(v) for v in s.split(",")])
+            elif s.upper().startswith("@DATA"):
+                data = True
+    return np.array(rows)
+
+
+def read_matrix(path):
+    rows = []
+    with gzip.open(path, "rt") as f:
+        for line in f:
+            s = line.strip()
+            if not s:
+                break
+            rows.append([float(v) for v in s.split()])
+    return np.array(rows)
+
+
+def make_bt(ref: Reference):
+    """datadriven/tests/testBT.cpp, suite TestOperationBTLinear: regular Linear grid, B built
+    column by column with mult(e_i); row sums compared in order, column sums sorted, 1e-5 %."""
+    base = os.path.join(REF_SRC, "datadriven", "datasets", "BT_BBT")
+    cases = [("d1_l3", 1, 3, "data_dim_1_nops_8_float.arff.gz", "BT_phi_li_hut_dim_1_nopsgrid_7_float.dat.gz"),
+             ("d1_l5", 1, 5, "data_dim_1_nops_8_float.arff.gz", "BT_phi_li_hut_dim_1_nopsgrid_31_float.dat.gz"),
+             ("d3_l3", 3, 3, "data_dim_3_nops_512_float.arff.gz", "BT_phi_li_hut_dim_3_nopsgrid_31_float.dat.gz"),
+             ("d3_l4", 3, 4, "data_dim_3_nops_512_float.arff.gz", "BT_phi_li_hut_dim_3_nopsgrid_111_float.dat.gz")]
+    out = {}
+    for name, d, l, data_file, mat_file in cases:
+        x = read_arff(os.path.join(base, data_file))
+        mat = read_matrix(os.path.join(base, mat_file))
+        g = ref.grid(d, l)
+        assert mat.shape == (x.shape[0], g.size), (name, mat.shape, x.shape, g.size)
+        out[name + "_x"] = x
+        out[name + "_row_sums"] = mat.sum(axis=1)
+        out[name + "_col_sums_sorted"] = np.sort(mat.sum(axis=0))
+        out[name + "_dim"] = np.int64(d)
+        out[name + "_level"] = np.int64(l)
+    np.savez_compressed(os.path.join(HERE, "bt_linear.npz"), **out)
+
+
+def main():
+    ref = Reference()
+    ref.set_threads(os.cpu_count() or 1)
+    make_grids(ref)
+    make_refine(ref)
+    make_multeval(ref)
+    make_cgfit(ref)
+    make_bt(ref)
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,292 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's own FP64 outputs
+(tests/golden, produced by the reference's compiled code) and against the oracle.
+
+Tolerances (max abs error / max abs reference value):
+  FP64 kernels   1e-12   (the reference's STREAMING-vs-DEFAULT agreement is ~1e-14)
+  FP32 kernels   1e-4    (x is rounded to float: |dt| <= 2^l * 2^-24 per dimension)
+  fits           1e-9 in alpha for the plain FP64 CG, 1e-6 for the mixed-precision fit
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_err
+
+import sgpp_gb300 as sg
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu(lib):
+    if lib.sgmev_device_count() < 1:
+        pytest.fail("no CUDA device visible to libsgpp_gb300 (the GPU tests need one)")
+
+
+def _grid_from(g, name):
+    return sg.Grid.fromArrays(g[name + "_level"].astype(np.int32),
+                              g[name + "_index"].astype(np.int32))
+
+
+def _op(grid, x, precision="double"):
+    cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                sg.OperationMultipleEvalSubType.CUDA,
+                                                parameters={"precision": precision})
+    return sg.createOperationMultipleEval(grid, x, cfg)
+
+
+MULTEVAL = [str(c) for c in load_golden("multeval.npz")["cases"]]
+
+
+@pytest.mark.parametrize("precision,tol", [("double", FP64_TOL), ("float", FP32_TOL)])
+@pytest.mark.parametrize("name", MULTEVAL)
+def test_mult_and_transpose_match_reference(name, precision, tol):
+    g = load_golden("multeval.npz")
+    grid = _grid_from(g, name)
+    x = g[name + "_x"]
+    op = _op(grid, x, precision)
+    out = np.zeros(x.shape[0])
+    op.mult(g[name + "_alpha"], out)
+    assert rel_err(out, g[name + "_mult_default"]) < tol
+    outt = np.zeros(grid.getSize())
+    op.multTranspose(g[name + "_v"], outt)
+    assert rel_err(outt, g[name + "_multt_default"]) < tol
+    assert op.getDuration() > 0.0
+
+
+@pytest.mark.parametrize("name", ["bb_kat", "bb_rand"])
+def test_bounding_box_matches_reference(name):
+    g = load_golden("multeval.npz")
+    grid = _grid_from(g, name)
+    bb = sg.BoundingBox(grid.getDimension())
+    for t, (lo, hi) in enumerate(zip(g[name + "_bb_left"], g[name + "_bb_right"])):
+        bb.setBoundary(t, sg.BoundingBox1D(lo, hi))
+    grid.getStorage().setBoundingBox(bb)
+    x = g[name + "_x"]
+    op = _op(grid, x)
+    out = np.zeros(x.shape[0])
+    op.mult(g[name + "_alpha"], out)
+    assert rel_err(out, g[name + "_mult_default"]) < FP64_TOL
+    outt = np.zeros(grid.getSize())
+    op.multTranspose(g[name + "_v"], outt)
+    assert rel_err(outt, g[name + "_multt_default"]) < FP64_TOL
+    if name == "bb_kat":
+        # base/tests/test_OperationMultipleEval.cpp:71-78
+        np.testing.assert_allclose(out, [0.0, 2.72, 1.64], rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["d1_l3", "d1_l5", "d3_l3", "d3_l4"])
+def test_bt_golden_matrices(name):
+    """datadriven/tests/testBT.cpp (TestOperationBTLinear) through the CUDA operator."""
+    g = load_golden("bt_linear.npz")
+    d, l = int(g[name + "_dim"]), int(g[name + "_level"])
+    grid = sg.Grid.createLinearGrid(d)
+    grid.getGenerator().regular(l)
+    x = g[name + "_x"]
+    op = _op(grid, x)
+    n = grid.getSize()
+    B = np.zeros((x.shape[0], n))
+    col = np.zeros(x.shape[0])
+    for i in range(n):
+        e = np.zeros(n)
+        e[i] = 1.0
+        op.mult(e, col)
+        B[:, i] = col
+    np.testing.assert_allclose(B.sum(axis=1), g[name + "_row_sums"], rtol=1e-7, atol=1e-9)
+    np.testing.assert_allclose(np.sort(B.sum(axis=0)), g[name + "_col_sums_sorted"], rtol=1e-7,
+                               atol=1e-9)
+
+
+def test_results_are_bitwise_reproducible():
+    g = load_golden("multeval.npz")
+    name = "d5_l6_m2000"
+    grid = _grid_from(g, name)
+    x = g[name + "_x"]
+    for prec in ("double", "float"):
+        op = _op(grid, x, prec)
+        a = np.zeros(x.shape[0])
+        b = np.zeros(x.shape[0])
+        op.mult(g[name + "_alpha"], a)
+        op.mult(g[name + "_alpha"], b)
+        assert np.array_equal(a, b)
+        ta = np.zeros(grid.getSize())
+        tb = np.zeros(grid.getSize())
+        op.multTranspose(g[name + "_v"], ta)
+        op.multTranspose(g[name + "_v"], tb)
+        assert np.array_equal(ta, tb)
+
+
+def test_ranged_variants(oracle):
+    rng = np.random.default_rng(5)
+    grid = sg.Grid.createLinearGrid(4)
+    grid.getGenerator().regular(5)
+    x = rng.random((5000, 4))
+    a = rng.standard_normal(grid.getSize())
+    v = rng.standard_normal(5000)
+    op = _op(grid, x)
+    full = np.zeros(5000)
+    op.mult(a, full)
+    fullt = np.zeros(grid.getSize())
+    op.multTranspose(v, fullt)
+    for s, e in [(0, 5000), (0, 1), (123, 4321), (4999, 5000), (2048, 2048)]:
+        part = np.full(5000, np.nan)
+        op.mult(a, part, s, e)
+        assert rel_err(part[s:e], full[s:e]) < FP64_TOL if e > s else True
+        assert np.isnan(part[:s]).all() and np.isnan(part[e:]).all()
+    n = grid.getSize()
+    for s, e in [(0, n), (0, 1), (17, n - 5), (n - 1, n)]:
+        part = np.full(n, np.nan)
+        op.multTranspose(v, part, s, e)
+        assert rel_err(part[s:e], fullt[s:e]) < FP64_TOL
+        assert np.isnan(part[:s]).all() and np.isnan(part[e:]).all()
+
+
+def test_edge_sizes(oracle):
+    rng = np.random.default_rng(9)
+    # single grid point, d = 1
+    grid = sg.Grid.createLinearGrid(1)
+    grid.getGenerator().regular(1)
+    x = np.array([[0.0], [0.25], [0.5], [1.0], [0.75]])
+    op = _op(grid, x)
+    out = np.zeros(5)
+    op.mult(np.array([2.0]), out)
+    np.testing.assert_allclose(out, [0.0, 1.0, 2.0, 0.0, 1.0], rtol=0, atol=1e-15)
+    # empty data set: mult writes nothing, multTranspose gives zeros
+    grid = sg.Grid.createLinearGrid(3)
+    grid.getGenerator().regular(3)
+    op = _op(grid, np.zeros((0, 3)))
+    op.mult(np.ones(grid.getSize()), np.zeros(0))
+    outt = np.full(grid.getSize(), 7.0)
+    op.multTranspose(np.zeros(0), outt)
+    assert not outt.any()
+    # high dimension goes through the generic (non-templated) kernels
+    d = 20
+    grid = sg.Grid.createLinearGrid(d)
+    grid.getGenerator().regular(2)
+    x = rng.random((333, d))
+    a = rng.standard_normal(grid.getSize())
+    v = rng.standard_normal(333)
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    for prec, tol in (("double", FP64_TOL), ("float", FP32_TOL)):
+        op = _op(grid, x, prec)
+        out = np.zeros(333)
+        op.mult(a, out)
+        assert rel_err(out, oracle.mult_naive(lp, ix, x, a)) < tol
+        outt = np.zeros(grid.getSize())
+        op.multTranspose(v, outt)
+        assert rel_err(outt, oracle.mult_transpose_naive(lp, ix, x, v)) < tol
+
+
+def test_wrong_sizes_raise():
+    grid = sg.Grid.createLinearGrid(2)
+    grid.getGenerator().regular(3)
+    op = _op(grid, np.random.default_rng(0).random((10, 2)))
+    with pytest.raises(sg.OperationException):
+        op.mult(np.ones(grid.getSize() - 1), np.zeros(10))
+    with pytest.raises(sg.OperationException):
+        op.multTranspose(np.ones(10), np.zeros(grid.getSize() - 1))
+    with pytest.raises(sg.OperationException):
+        op.mult(np.ones(grid.getSize()), np.zeros(10), 5, 11)
+
+
+def test_prepare_after_refinement(oracle):
+    rng = np.random.default_rng(11)
+    grid = sg.Grid.createLinearGrid(6)
+    grid.getGenerator().regular(3)
+    x = rng.random((3000, 6))
+    op = _op(grid, x)
+    for _ in range(3):
+        grid.getGenerator().refine(sg.SurplusRefinementFunctor(rng.standard_normal(grid.getSize()), 25))
+        op.prepare()
+        a = rng.standard_normal(grid.getSize())
+        out = np.zeros(3000)
+        op.mult(a, out)
+        lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+        assert rel_err(out, oracle.mult_naive(lp, ix, x, a)) < FP64_TOL
+        v = rng.standard_normal(3000)
+        outt = np.zeros(grid.getSize())
+        op.multTranspose(v, outt)
+        assert rel_err(outt, oracle.stream(x).mult_transpose(lp, ix, v)) < FP64_TOL
+
+
+def test_system_apply_matches_oracle(oracle):
+    rng = np.random.default_rng(13)
+    grid = sg.Grid.createLinearGrid(5)
+    grid.getGenerator().regular(4)
+    x = rng.random((4000, 5))
+    a = rng.standard_normal(grid.getSize())
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    st = oracle.stream(x)
+    lam_m = 4000 * 1e-3
+    ref = st.mult_transpose(lp, ix, st.mult(lp, ix, a)) + lam_m * a
+    op = _op(grid, x)
+    out = np.zeros(grid.getSize())
+    op.systemApply(a, out, lam_m)
+    assert rel_err(out, ref) < FP64_TOL
+    op32 = _op(grid, x, "float")
+    op32.systemApply(a, out, lam_m)
+    assert rel_err(out, ref) < FP32_TOL
+
+
+@pytest.mark.parametrize("name", ["d4_l4", "d6_l3"])
+def test_device_cg_fit_matches_reference(name):
+    g = load_golden("cgfit.npz")
+    grid = _grid_from(g, name)
+    op = _op(grid, g[name + "_x"])
+    alpha, it, res = op.fit(g[name + "_y"], float(g[name + "_lambda"]), 1000, 1e-12)
+    assert rel_err(alpha, g[name + "_alpha"]) < 1e-9
+    assert abs(it - int(g[name + "_iterations"])) <= 2
+
+
+@pytest.mark.parametrize("name", ["d4_l4", "d6_l3"])
+def test_mixed_precision_fit_within_1e6(name):
+    g = load_golden("cgfit.npz")
+    grid = _grid_from(g, name)
+    op = _op(grid, g[name + "_x"])
+    alpha, it, res = op.fit(g[name + "_y"], float(g[name + "_lambda"]), 5000, 1e-10,
+                            mode=sg.SGMEV_SOLVE_MIXED)
+    assert rel_err(alpha, g[name + "_alpha"]) < 1e-6
+
+
+def test_reference_callers_drive_the_operator_unchanged():
+    """SystemMatrixLeastSquaresIdentity + ConjugateGradients on the host, CUDA op inside."""
+    g = load_golden("cgfit.npz")
+    name = "d4_l4"
+    grid = _grid_from(g, name)
+    A = sg.SystemMatrixLeastSquaresIdentity(grid, g[name + "_x"], float(g[name + "_lambda"]))
+    b = np.zeros(grid.getSize())
+    A.generateb(g[name + "_y"], b)
+    alpha = np.zeros(grid.getSize())
+    cg = sg.ConjugateGradients(1000, 1e-12)
+    cg.solve(A, alpha, b, False, False, 0.0)
+    assert rel_err(alpha, g[name + "_alpha"]) < 1e-9
+    assert abs(cg.getNumberIterations() - int(g[name + "_iterations"])) <= 2
+
+
+def test_adjoint_and_linearity_at_full_size():
+    """Size-independent properties at the regression-fit workload size (d=10, level 5,
+    2^20 points): <B a, v> = <a, B^T v>, and B is linear."""
+    rng = np.random.default_rng(21)
+    grid = sg.Grid.createLinearGrid(10)
+    grid.getGenerator().regular(5)
+    m = 1 << 20
+    x = rng.random((m, 10))
+    n = grid.getSize()
+    a = rng.standard_normal(n)
+    b = rng.standard_normal(n)
+    v = rng.standard_normal(m)
+    op = _op(grid, x, "float")
+    Ba = np.zeros(m)
+    Bb = np.zeros(m)
+    Bab = np.zeros(m)
+    op.mult(a, Ba)
+    op.mult(b, Bb)
+    op.mult(2.0 * a - 3.0 * b, Bab)
+    assert rel_err(Bab, 2.0 * Ba - 3.0 * Bb) < 1e-5
+    Btv = np.zeros(n)
+    op.multTranspose(v, Btv)
+    lhs = float(Ba @ v)
+    rhs = float(a @ Btv)
+    assert abs(lhs - rhs) <= 1e-5 * (np.abs(Ba).sum() * np.abs(v).max())
