@@ -1,0 +1,408 @@
+#!/usr/bin/env python3
+"""Headline benchmark: regression fits per second on the GB300.
+
+Workload (the regression-fit configuration): regular Linear sparse grid d=10, level 5
+(N = 13,441 grid points); M = 2^20 data points from an 8-component Gaussian mixture (means
+uniform in [0.2, 0.8]^10, diagonal sigma 0.08, equal weights) clipped to [0, 1]^10;
+y = 10 sin(pi x1 x2) + 20 (x3 - 0.5)^2 + 10 x4 + 5 x5 + N(0, 0.1^2); lambda = 1e-4.
+Synthetic, seeded data of that shape (no dataset files are read).
+
+One step = one regression fit: b = B^T y, then CG on (B^T B + lambda M I) alpha = b to the
+relative FP64 residual `epsilon`, mixed precision (FP32 hat kernels inside CG, FP64-accurate
+residual for the outer iterative-refinement correction), all state resident on the GPU.
+Each fit's alpha is checked against an FP64 solution computed once before timing.
+
+value   fits/s with the data resident in HBM (device pointers for y and alpha)
+e2e     fits/s through the public API from pinned host buffers: create the operator from the
+        host data matrix (H2D copy inside the timed region), fit with host y, read alpha back
+roofline  dominant tile kernel (FP32 mult / multTranspose): achieved = 6 N M d FLOP per
+        launch (the reference's count, LearnerVectorizedPerformanceCalculator.cpp:91-93) over
+        its CUDA-event duration, against the FP32 FMA peak measured in the same run
+cpu_baseline  the oracle port of the reference's STREAMING FP64 path on the host cores
+        (bounded sample: one B^T B application on 2^16 of the points, scaled to M and to the
+        CG operation count of one fit)
+
+--impl reference prints the same line for the reference's CPU implementation of the path
+(the oracle port: the compiled reference needs its sources, which do not travel).
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+DIM, LEVEL, M_POINTS, LAMBDA = 10, 5, 1 << 20, 1e-4
+FLOP_PER_PAIR_DIM = 6.0  # reference's count per (grid point, data point, dimension)
+CPU_SAMPLE_POINTS = 1 << 16
+
+
+def make_workload(seed: int, m: int = M_POINTS, d: int = DIM):
+    """Seeded Gaussian-mixture data and the benchmark's target function."""
+    rng = np.random.default_rng(seed)
+    means = rng.uniform(0.2, 0.8, size=(8, d))
+    comp = rng.integers(0, 8, size=m)
+    x = np.clip(means[comp] + 0.08 * rng.standard_normal((m, d)), 0.0, 1.0)
+    y = (10.0 * np.sin(np.pi * x[:, 0] * x[:, 1]) + 20.0 * (x[:, 2] - 0.5) ** 2 + 10.0 * x[:, 3]
+         + 5.0 * x[:, 4] + 0.1 * rng.standard_normal(m))
+    return x, y
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.gpu_index), "-lms", "200"], stdout=self.file,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        rows = list(csv.reader(io.StringIO(self.file.read())))
+        self.file.close()
+        os.unlink(self.file.name)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                power.append(float(r[3]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_fit_seconds(x, grid_lp, grid_ix, cg_ops: float, threads: int):
+    """Oracle port of the reference's STREAMING FP64 path on the host cores: time one
+    B^T (B a) on CPU_SAMPLE_POINTS points, scale linearly to all points and to the number of
+    operator applications one CG fit performs. Returns (seconds per fit, sample description)."""
+    from oracle import Oracle
+
+    orc = Oracle()
+    orc.set_threads(threads)
+    ms = min(CPU_SAMPLE_POINTS, x.shape[0])
+    st = orc.stream(x[:ms])
+    a = np.random.default_rng(0).standard_normal(grid_lp.shape[0])
+    st.mult_transpose(grid_lp, grid_ix, st.mult(grid_lp, grid_ix, a))  # warm-up
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        st.mult_transpose(grid_lp, grid_ix, st.mult(grid_lp, grid_ix, a))
+        ts.append(time.perf_counter() - t0)
+    st.close()
+    t_apply = statistics.median(ts) * (x.shape[0] / ms)
+    sample = (f"one B^T(B a) (mult + multTranspose, FP64) on {ms} of the {x.shape[0]} points, "
+              f"median of 3 after 1 warm-up, {threads} OpenMP threads, scaled x{x.shape[0] / ms:g} "
+              f"to all points and x{cg_ops:g} operator applications per fit")
+    return t_apply * cg_ops, sample
+
+
+def cg_operator_applications(iterations: int) -> float:
+    """B^T B applications of one fit as ConjugateGradients.cpp:22-151 performs them: one per
+    iteration, one extra every 50 iterations (true residual), plus b = B^T y (half)."""
+    return iterations + iterations // 50 + 0.5
+
+
+def grid_arrays():
+    import sgpp_gb300 as sg
+
+    grid = sg.Grid.createLinearGrid(DIM)
+    grid.getGenerator().regular(LEVEL)
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    return grid, lp, ix
+
+
+# Iterations of the plain FP64 CG on this workload to relative residual 1e-8; used only to scale
+# per-iteration CPU timings of the reference path to one fit. Measured with the plain FP64 CUDA
+# CG (sgmev_fit, SGMEV_SOLVE_PLAIN) on this exact seeded workload; bench.py re-measures the FP32
+# CG count live and reports both.
+PLAIN_FP64_CG_ITERATIONS = None
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    x, y = make_workload(args.seed)
+    _, lp, ix = grid_arrays()
+    iters = args.reference_iterations
+    cg_ops = cg_operator_applications(iters)
+    times = []
+    sample = ""
+    for k in range(args.warmup + args.steps):
+        t_fit, sample = cpu_fit_seconds(x, lp, ix, cg_ops, threads)
+        if k >= args.warmup:
+            times.append(t_fit)
+    sec = statistics.median(times)
+    value = 1.0 / sec
+    line = {
+        "impl": "reference", "metric": "fits_per_sec", "value": value, "unit": "fits/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"regression fit, regular Linear grid d={DIM} level {LEVEL} "
+                               f"(N=13441), M={M_POINTS} Gaussian-mixture points, lambda={LAMBDA}",
+                   "cg_iterations_per_fit": iters, "l2_policy": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": "fits/s", "cores": threads, "kind": "port",
+                         "sample": sample, "host": os.uname().machine},
+        "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    import sgpp_gb300 as sg
+
+    rank, world, local_rank = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist = dist_mod
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    if sg.device_count() < 1:
+        raise RuntimeError("bench.py needs a CUDA device")
+
+    x, y = make_workload(args.seed + rank)
+    grid, lp, ix = grid_arrays()
+    n, m = grid.getSize(), x.shape[0]
+    work_per_op = FLOP_PER_PAIR_DIM * n * m * DIM
+
+    stream = torch.cuda.Stream()
+    op = sg.createOperationMultipleEval(grid, x)  # FP64 op; mixed mode stages FP32 copies too
+    op.setStream(stream.cuda_stream)
+    d_y = torch.from_numpy(y).to(f"cuda:{local_rank}")
+    d_alpha = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local_rank}")
+    d_ref = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local_rank}")
+
+    # FP64 solution for the error check (untimed): refinement to a tight FP64 residual
+    it_ref, _ = op.fitDevice(d_y.data_ptr(), d_ref.data_ptr(), LAMBDA, 20000, args.ref_epsilon,
+                             mode=sg.SGMEV_SOLVE_MIXED)
+    alpha_ref = d_ref.cpu().numpy()
+
+    def one_fit():
+        return op.fitDevice(d_y.data_ptr(), d_alpha.data_ptr(), LAMBDA, 20000, args.epsilon,
+                            mode=sg.SGMEV_SOLVE_MIXED)
+
+    for _ in range(args.warmup):
+        one_fit()
+    peak32, clock_khz = sg.fma_peak(sg.SGMEV_FP32)
+    peak64, _ = sg.fma_peak(sg.SGMEV_FP64)
+
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[local_rank]) \
+        if os.environ.get("CUDA_VISIBLE_DEVICES") else local_rank
+    sampler = ClockSampler(gpu_index)
+    launches0 = op.kernelLaunches()
+    op.profile(True)
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+    iters = []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    for k in range(args.steps):
+        events[k][0].record(stream)
+        it, _ = one_fit()
+        events[k][1].record(stream)
+        iters.append(it)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    if dist:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in events]
+    total_s = sum(step_ms) * 1e-3
+    launches = op.kernelLaunches() - launches0
+    kstats = {name: op.profileRead(kind) for name, kind in
+              (("mult_fp32", sg.SGMEV_KERNEL_MULT_FP32), ("multT_fp32", sg.SGMEV_KERNEL_MULTT_FP32),
+               ("mult_fp64", sg.SGMEV_KERNEL_MULT_FP64), ("multT_fp64", sg.SGMEV_KERNEL_MULTT_FP64))}
+    op.profile(False)
+    alpha = d_alpha.cpu().numpy()
+    err = float(np.abs(alpha - alpha_ref).max() / np.abs(alpha_ref).max())
+
+    if dist:
+        t = torch.tensor([total_s], device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = args.steps * world / total_s
+
+    # roofline of the dominant tile kernel
+    dom = max(kstats, key=lambda k: kstats[k][1])
+    cnt, sec = kstats[dom]
+    avg = sec / max(cnt, 1)
+    achieved = work_per_op / avg / 1e12
+    is64 = dom.endswith("fp64")
+    peak = (peak64 if is64 else peak32) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(dom)
+    roofline = {"bound": "fp64-vector" if is64 else "fp32-vector", "kernel": dom,
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": traffic, "launches_timed": cnt, "avg_launch_ms": avg * 1e3,
+                "peak_source": "measured in this run: FMA chains on every SM (sgmev_fma_peak); "
+                               "MEASURED_PEAKS.json holds no FP32/FP64 vector peak",
+                "peaks_measured_tflops": {"fp32": peak32 / 1e12, "fp64": peak64 / 1e12},
+                "flop_per_launch": work_per_op}
+
+    # mult GFLOP/s (reference count) of the FP32 mult kernel
+    mc, msec = kstats["mult_fp32"]
+    mult_tflops = work_per_op / (msec / max(mc, 1)) / 1e12 if mc else None
+
+    # end to end through the public API from pinned host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        x_pin = torch.from_numpy(x).pin_memory()
+        y_pin = torch.from_numpy(y).pin_memory()
+        xs = x_pin.numpy()
+        ys = y_pin.numpy()
+        e2e_times = []
+        for k in range(args.e2e_steps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            op2 = sg.createOperationMultipleEval(grid, xs)
+            a_host, _, _ = op2.fit(ys, LAMBDA, 20000, args.epsilon, mode=sg.SGMEV_SOLVE_MIXED)
+            op2.close()
+            torch.cuda.synchronize()
+            if k > 0:  # first call is a warm-up
+                e2e_times.append(time.perf_counter() - t0)
+        h2d = x.nbytes + y.nbytes + lp.nbytes + ix.nbytes
+        e2e = {"value": len(e2e_times) / sum(e2e_times), "unit": "fits/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(n * 8),
+               "steps": len(e2e_times),
+               "what": "createOperationMultipleEval(host X) + fit(host y) + alpha to host + close"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        iters_fit = args.reference_iterations
+        t_fit, sample = cpu_fit_seconds(x, lp, ix, cg_operator_applications(iters_fit), threads)
+        cpu = {"value": 1.0 / t_fit, "unit": "fits/s", "cores": threads, "kind": "port",
+               "sample": sample, "cg_iterations_per_fit": iters_fit,
+               "host": os.uname().machine}
+
+    # plain FP64 path (same CG, native FP64 kernels): one timed B^T B application, scaled
+    t_fp64 = None
+    if args.plain_fp64_probe:
+        d_t = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local_rank}")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        op.systemApplyDevice(d_alpha.data_ptr(), d_t.data_ptr(), LAMBDA * m)
+        e0.record(stream)
+        op.systemApplyDevice(d_alpha.data_ptr(), d_t.data_ptr(), LAMBDA * m)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_fp64 = e0.elapsed_time(e1) * 1e-3
+    plain = None
+    if t_fp64:
+        t_plain_fit = t_fp64 * cg_operator_applications(args.reference_iterations)
+        plain = {"fits_per_sec": 1.0 / t_plain_fit, "system_apply_ms": t_fp64 * 1e3,
+                 "cg_iterations_per_fit": args.reference_iterations,
+                 "speedup_mixed_vs_plain_fp64": value / world * t_plain_fit}
+
+    if rank == 0:
+        lat = sorted(step_ms)
+        p = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
+        line = {
+            "metric": "fits_per_sec", "value": value, "unit": "fits/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": f"regression fit, regular Linear grid d={DIM} level {LEVEL} "
+                                   f"(N={n}), M={m} Gaussian-mixture points, lambda={LAMBDA}, "
+                                   f"mixed-precision CG to relative FP64 residual {args.epsilon}",
+                       "l2_policy": "inputs larger than L2 (84 MB FP64 + 42 MB FP32 data, "
+                                    "re-read every operator application)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "latency_ms": {"p50": p(0.5), "p99": p(0.99)},
+            "alpha_rel_err_vs_fp64": err, "cg_iterations": iters,
+            "fp64_solution_iterations": it_ref,
+            "mult_tflops_ref_count": mult_tflops,
+            "mult_frac_of_fp32_peak": (mult_tflops / (peak32 / 1e12)) if mult_tflops else None,
+            "kernel_stats": {k: {"launches": c, "ms_total": s * 1e3} for k, (c, s) in kstats.items()},
+            "roofline": roofline, "clocks": clocks, "gpu_launches": int(launches),
+            "e2e": e2e, "cpu_baseline": cpu, "plain_fp64_path": plain,
+        }
+        print(json.dumps(line), flush=True)
+    op.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--epsilon", type=float, default=1e-8)
+    ap.add_argument("--ref-epsilon", type=float, default=1e-12)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--reference-iterations", type=int, default=110)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-fp64-probe", type=int, default=1)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -157,6 +157,11 @@ SGMEV_API int sgmev_fit(sgmev_op* op, int mode, const double* y, double lambda,
                         int64_t max_iterations, double epsilon, int reuse, double* alpha,
                         int64_t* iterations, double* residual);
 
+/* sgmev_fit with y [n_data] and alpha [n_grid] as device pointers (doubles). Blocks. */
+SGMEV_API int sgmev_fit_device(sgmev_op* op, int mode, const double* d_y, double lambda,
+                               int64_t max_iterations, double epsilon, int reuse, double* d_alpha,
+                               int64_t* iterations, double* residual);
+
 /*
  * Duration in seconds of the device work of the last mult / multTranspose / system apply /
  * fit call (CUDA events on the op's stream); replaces OperationMultipleEval::getDuration

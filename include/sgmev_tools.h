@@ -21,6 +21,19 @@ extern "C" {
  */
 SGMEV_API int sgmev_fma_peak(int precision, double* flops_per_second, int* sm_clock_khz);
 
+/*
+ * Per-kernel timing of an op's tile kernels. sgmev_profile(op, 1) resets the counters and
+ * records a CUDA event pair around every following mult / multTranspose tile-kernel launch on
+ * the op's stream; sgmev_profile_read() synchronises the stream and returns, for one kernel
+ * kind, the number of launches and their summed device time since the reset.
+ */
+#define SGMEV_KERNEL_MULT_FP32 0
+#define SGMEV_KERNEL_MULTT_FP32 1
+#define SGMEV_KERNEL_MULT_FP64 2
+#define SGMEV_KERNEL_MULTT_FP64 3
+SGMEV_API int sgmev_profile(sgmev_op* op, int enable);
+SGMEV_API int sgmev_profile_read(sgmev_op* op, int kind, int64_t* launches, double* seconds);
+
 #ifdef __cplusplus
 }
 #endif

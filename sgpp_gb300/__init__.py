@@ -56,8 +56,14 @@ EXPORTED_SYMBOLS = (
     "sgmev_mult_transpose_range", "sgmev_mult_device", "sgmev_mult_transpose_device",
     "sgmev_system_apply", "sgmev_system_apply_device", "sgmev_fit", "sgmev_get_duration",
     "sgmev_set_stream", "sgmev_synchronize", "sgmev_kernel_launches", "sggrid_regular",
-    "sggrid_refine_surplus", "sggrid_level_index_for_eval", "sgmev_fma_peak",
+    "sggrid_refine_surplus", "sggrid_level_index_for_eval", "sgmev_fma_peak", "sgmev_profile",
+    "sgmev_profile_read", "sgmev_fit_device",
 )
+
+SGMEV_KERNEL_MULT_FP32 = 0
+SGMEV_KERNEL_MULTT_FP32 = 1
+SGMEV_KERNEL_MULT_FP64 = 2
+SGMEV_KERNEL_MULTT_FP64 = 3
 
 
 # ---- exceptions (base/src/sgpp/base/exception/) --------------------------------------------
@@ -126,6 +132,9 @@ def load_library(path: str = LIBRARY_PATH):
         "sggrid_refine_surplus": (c_int, [c_int, i64, i64, vp, vp, vp, i64, dbl, pi64]),
         "sggrid_level_index_for_eval": (c_int, [c_int, i64, vp, vp, vp, vp]),
         "sgmev_fma_peak": (c_int, [c_int, pdbl, ctypes.POINTER(c_int)]),
+        "sgmev_fit_device": (c_int, [vp, c_int, vp, dbl, i64, dbl, c_int, vp, pi64, pdbl]),
+        "sgmev_profile": (c_int, [vp, c_int]),
+        "sgmev_profile_read": (c_int, [vp, c_int, pi64, pdbl]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -491,6 +500,50 @@ class OperationMultiEvalCuda:
 
     def kernelLaunches(self) -> int:
         return int(load_library().sgmev_kernel_launches(self._h))
+
+    def setStream(self, stream_ptr: int) -> None:
+        """Run this op's work on an external cudaStream_t (0 restores the op's own stream)."""
+        _check(load_library().sgmev_set_stream(self._h, ctypes.c_void_p(int(stream_ptr) or None)))
+
+    def synchronize(self) -> None:
+        _check(load_library().sgmev_synchronize(self._h))
+
+    def profile(self, enable: bool = True) -> None:
+        """Reset and enable (or disable) per-kernel event timing of the tile kernels."""
+        _check(load_library().sgmev_profile(self._h, 1 if enable else 0))
+
+    def profileRead(self, kind: int):
+        """(launches, seconds) of one tile-kernel kind since the last profile() call."""
+        n = ctypes.c_int64(0)
+        t = ctypes.c_double(0.0)
+        _check(load_library().sgmev_profile_read(self._h, int(kind), ctypes.byref(n),
+                                                 ctypes.byref(t)))
+        return int(n.value), float(t.value)
+
+    def fitDevice(self, d_y: int, d_alpha: int, lam: float, imax: int, epsilon: float,
+                  reuse: bool = False, mode: int = SGMEV_SOLVE_PLAIN):
+        """fit() on device pointers (y [n_data], alpha [n_grid] float64); (iterations, residual)."""
+        it = ctypes.c_int64(0)
+        res = ctypes.c_double(0.0)
+        _check(load_library().sgmev_fit_device(self._h, int(mode), ctypes.c_void_p(d_y),
+                                               float(lam), int(imax), float(epsilon),
+                                               1 if reuse else 0, ctypes.c_void_p(d_alpha),
+                                               ctypes.byref(it), ctypes.byref(res)))
+        return int(it.value), float(res.value)
+
+    def multDevice(self, d_alpha: int, d_result: int) -> None:
+        """mult on device pointers (float64, n_grid / n_data), enqueued on the op's stream."""
+        _check(load_library().sgmev_mult_device(self._h, ctypes.c_void_p(d_alpha),
+                                                ctypes.c_void_p(d_result)))
+
+    def multTransposeDevice(self, d_source: int, d_result: int) -> None:
+        _check(load_library().sgmev_mult_transpose_device(self._h, ctypes.c_void_p(d_source),
+                                                          ctypes.c_void_p(d_result)))
+
+    def systemApplyDevice(self, d_alpha: int, d_result: int, lambda_times_m: float) -> None:
+        _check(load_library().sgmev_system_apply_device(self._h, ctypes.c_void_p(d_alpha),
+                                                        ctypes.c_void_p(d_result),
+                                                        float(lambda_times_m)))
 
     def systemApply(self, alpha, result, lambda_times_m: float) -> None:
         a = self._vec(alpha, self._n, "alpha")

@@ -122,9 +122,47 @@ struct sgmev_op {
   int64_t launches = 0;
 
   std::vector<double> bb_left, bb_width;
+
+  // optional per-kernel timing (sgmev_profile): one event pair per tile-kernel launch,
+  // resolved when read
+  bool profile = false;
+  std::vector<cudaEvent_t> prof_events;  // pool, 2 per launch
+  std::vector<int> prof_kind;            // kind of launch i
+  size_t prof_used = 0;                  // launches recorded since the last reset
+  int64_t prof_count[8] = {0};
+  double prof_seconds[8] = {0.0};
 };
 
 namespace sgmev {
+
+// kinds of timed tile kernels (sgmev_tools.h SGMEV_KERNEL_*)
+enum { KIND_MULT_FP32 = 0, KIND_MULTT_FP32 = 1, KIND_MULT_FP64 = 2, KIND_MULTT_FP64 = 3 };
+
+template <typename T>
+static int kind_mult() { return sizeof(T) == 4 ? KIND_MULT_FP32 : KIND_MULT_FP64; }
+template <typename T>
+static int kind_multt() { return sizeof(T) == 4 ? KIND_MULTT_FP32 : KIND_MULTT_FP64; }
+
+static long prof_begin(sgmev_op* op, int kind) {
+  if (!op->profile) return -1;
+  if (op->prof_events.size() < 2 * (op->prof_used + 1)) {
+    const size_t grow = std::max<size_t>(64, op->prof_events.size());
+    for (size_t k = 0; k < grow; ++k) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return -1;
+      op->prof_events.push_back(e);
+    }
+  }
+  if (op->prof_kind.size() < op->prof_used + 1) op->prof_kind.resize(op->prof_used + 1);
+  const long i = static_cast<long>(op->prof_used++);
+  op->prof_kind[i] = kind;
+  cudaEventRecord(op->prof_events[2 * i], op->stream);
+  return i;
+}
+
+static void prof_end(sgmev_op* op, long i) {
+  if (i >= 0) cudaEventRecord(op->prof_events[2 * i + 1], op->stream);
+}
 
 // ---------------------------------------------------------------------------------------
 // staging kernels
@@ -294,6 +332,7 @@ static int run_mult(sgmev_op* op, const T* xt, const typename Pair<T>::type* li,
     const int64_t t0 = j_begin / tile_pts;
     const int64_t t1 = ceil_div(j_end, tile_pts);
     Plan p = plan_mult<T>(op, t1 - t0);
+    const long ev = prof_begin(op, kind_mult<T>());
     switch (op->dim) {
 #define F(D)                                                         \
   case D:                                                            \
@@ -304,14 +343,17 @@ static int run_mult(sgmev_op* op, const T* xt, const typename Pair<T>::type* li,
       default:
         break;
     }
+    prof_end(op, ev);
     *used = p;
   } else {
     const int64_t count = j_end - j_begin;
     Plan p = plan_mult<T>(op, ceil_div(count, kBlock));
     dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+    const long ev = prof_begin(op, kind_mult<T>());
     mult_generic_kernel<T><<<grid, kBlock, 0, op->stream>>>(xt, op->mpad, op->dim, li, alpha,
                                                             op->npad, p.chunk, j_begin, count,
                                                             part);
+    prof_end(op, ev);
     *used = p;
   }
   op->launches += 1;
@@ -328,6 +370,7 @@ static int run_multt(sgmev_op* op, const T* xt, const T* v, const typename Pair<
     const int64_t t0 = g_begin / tile_pts;
     const int64_t t1 = ceil_div(g_end, tile_pts);
     Plan p = plan_multt<T>(op, t1 - t0);
+    const long ev = prof_begin(op, kind_multt<T>());
     switch (op->dim) {
 #define F(D)                                                      \
   case D:                                                         \
@@ -338,13 +381,16 @@ static int run_multt(sgmev_op* op, const T* xt, const T* v, const typename Pair<
       default:
         break;
     }
+    prof_end(op, ev);
     *used = p;
   } else {
     const int64_t count = g_end - g_begin;
     Plan p = plan_multt<T>(op, ceil_div(count, kBlock));
     dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+    const long ev = prof_begin(op, kind_multt<T>());
     mult_transpose_generic_kernel<T><<<grid, kBlock, 0, op->stream>>>(
         xt, v, op->mpad, op->dim, li, op->npad, p.chunk, g_begin, count, part);
+    prof_end(op, ev);
     *used = p;
   }
   op->launches += 1;
@@ -548,6 +594,7 @@ static void release(sgmev_op* op) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (op->host_scalar) cudaFreeHost(op->host_scalar);
+  for (cudaEvent_t e : op->prof_events) cudaEventDestroy(e);
   if (op->ev_start) cudaEventDestroy(op->ev_start);
   if (op->ev_stop) cudaEventDestroy(op->ev_stop);
   if (op->own_stream) cudaStreamDestroy(op->own_stream);
@@ -571,6 +618,18 @@ static int end_timed(sgmev_op* op, bool sync) {
 
 static int check_op(const sgmev_op* op) {
   if (!op) return fail(SGMEV_ERR_INVALID, "op is NULL");
+  return SGMEV_OK;
+}
+
+// resolve recorded launch timings into the per-kind totals (needs the stream idle)
+static int prof_resolve(sgmev_op* op) {
+  for (size_t i = 0; i < op->prof_used; ++i) {
+    float ms = 0.f;
+    SGMEV_CUDA(cudaEventElapsedTime(&ms, op->prof_events[2 * i], op->prof_events[2 * i + 1]));
+    op->prof_count[op->prof_kind[i]] += 1;
+    op->prof_seconds[op->prof_kind[i]] += ms * 1e-3;
+  }
+  op->prof_used = 0;
   return SGMEV_OK;
 }
 
@@ -967,9 +1026,27 @@ static int cg_core(sgmev_op* op, int prec, const double* rhs, double* x, double 
   return SGMEV_OK;
 }
 
+static int fit_common(sgmev_op* op, int mode, const double* y, bool y_on_device, double lambda,
+                      int64_t max_iterations, double epsilon, int reuse, double* alpha,
+                      bool alpha_on_device, int64_t* iterations, double* residual);
+
 SGMEV_API int sgmev_fit(sgmev_op* op, int mode, const double* y, double lambda,
                         int64_t max_iterations, double epsilon, int reuse, double* alpha,
                         int64_t* iterations, double* residual) {
+  return fit_common(op, mode, y, false, lambda, max_iterations, epsilon, reuse, alpha, false,
+                    iterations, residual);
+}
+
+SGMEV_API int sgmev_fit_device(sgmev_op* op, int mode, const double* d_y, double lambda,
+                               int64_t max_iterations, double epsilon, int reuse, double* d_alpha,
+                               int64_t* iterations, double* residual) {
+  return fit_common(op, mode, d_y, true, lambda, max_iterations, epsilon, reuse, d_alpha, true,
+                    iterations, residual);
+}
+
+static int fit_common(sgmev_op* op, int mode, const double* y, bool y_on_device, double lambda,
+                      int64_t max_iterations, double epsilon, int reuse, double* alpha,
+                      bool alpha_on_device, int64_t* iterations, double* residual) {
   using namespace sgmev;
   SGMEV_TRY(check_op(op));
   if ((op->m > 0 && !y) || (op->n > 0 && !alpha)) return fail(SGMEV_ERR_INVALID, "NULL vector");
@@ -985,7 +1062,9 @@ SGMEV_API int sgmev_fit(sgmev_op* op, int mode, const double* y, double lambda,
   SGMEV_TRY(begin_timed(op));
   // b = B^T y in FP64 (generateb)
   if (op->m > 0)
-    SGMEV_CUDA(cudaMemcpyAsync(op->out64, y, sizeof(double) * op->m, cudaMemcpyHostToDevice, op->stream));
+    SGMEV_CUDA(cudaMemcpyAsync(op->out64, y, sizeof(double) * op->m,
+                               y_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               op->stream));
   convert_pad_kernel<<<vec_blocks(op->mpad), 256, 0, op->stream>>>(op->out64, op->m, op->mpad, op->v64, op->v32);
   op->launches += 1;
   SGMEV_TRY(dev_multt(op, mode == SGMEV_SOLVE_MIXED ? SGMEV_FP64 : op->precision, op->v64, op->v32,
@@ -993,7 +1072,9 @@ SGMEV_API int sgmev_fit(sgmev_op* op, int mode, const double* y, double lambda,
   if (reuse) {
     double* tmp = op->cg + 7 * np;
     if (op->n > 0)
-      SGMEV_CUDA(cudaMemcpyAsync(tmp, alpha, sizeof(double) * op->n, cudaMemcpyHostToDevice, op->stream));
+      SGMEV_CUDA(cudaMemcpyAsync(tmp, alpha, sizeof(double) * op->n,
+                                 alpha_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                 op->stream));
     convert_pad_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(tmp, op->n, np, x, nullptr);
     op->launches += 1;
   }
@@ -1025,10 +1106,36 @@ SGMEV_API int sgmev_fit(sgmev_op* op, int mode, const double* y, double lambda,
     }
   }
   if (op->n > 0)
-    SGMEV_CUDA(cudaMemcpyAsync(alpha, x, sizeof(double) * op->n, cudaMemcpyDeviceToHost, op->stream));
+    SGMEV_CUDA(cudaMemcpyAsync(alpha, x, sizeof(double) * op->n,
+                               alpha_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               op->stream));
   SGMEV_TRY(end_timed(op, true));
   if (iterations) *iterations = total_it;
   if (residual) *residual = res;
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_profile(sgmev_op* op, int enable) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  SGMEV_CUDA(cudaStreamSynchronize(op->stream));
+  op->profile = enable != 0;
+  op->prof_used = 0;
+  for (int k = 0; k < 8; ++k) {
+    op->prof_count[k] = 0;
+    op->prof_seconds[k] = 0.0;
+  }
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_profile_read(sgmev_op* op, int kind, int64_t* launches, double* seconds) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if (kind < 0 || kind >= 8) return fail(SGMEV_ERR_INVALID, "unknown kernel kind");
+  SGMEV_CUDA(cudaStreamSynchronize(op->stream));
+  SGMEV_TRY(prof_resolve(op));
+  if (launches) *launches = op->prof_count[kind];
+  if (seconds) *seconds = op->prof_seconds[kind];
   return SGMEV_OK;
 }
 
