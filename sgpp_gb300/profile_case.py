@@ -1,0 +1,76 @@
+"""Run a few launches of one tile kernel on a synthetic case, for profilers (ncu) and timing.
+
+    python -m sgpp_gb300.profile_case --kernel mult --precision float --dim 10 --level 5 \
+        --points 4194304 --launches 3
+
+Data are uniform on [0, 1]^d (seeded); the grid is the regular Linear grid of the given level.
+Prints one JSON line with the per-launch CUDA-event times of the tile kernel (sgmev_profile).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import sgpp_gb300 as sg  # noqa: E402
+
+KINDS = {("mult", "float"): sg.SGMEV_KERNEL_MULT_FP32, ("multT", "float"): sg.SGMEV_KERNEL_MULTT_FP32,
+         ("mult", "double"): sg.SGMEV_KERNEL_MULT_FP64, ("multT", "double"): sg.SGMEV_KERNEL_MULTT_FP64}
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--kernel", choices=["mult", "multT"], default="mult")
+    ap.add_argument("--precision", choices=["float", "double"], default="float")
+    ap.add_argument("--dim", type=int, default=10)
+    ap.add_argument("--level", type=int, default=5)
+    ap.add_argument("--points", type=int, default=1 << 22)
+    ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=1)
+    args = ap.parse_args()
+
+    rng = np.random.default_rng(7)
+    grid = sg.Grid.createLinearGrid(args.dim)
+    grid.getGenerator().regular(args.level)
+    n = grid.getSize()
+    x = rng.random((args.points, args.dim))
+    cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                sg.OperationMultipleEvalSubType.CUDA,
+                                                parameters={"precision": args.precision})
+    op = sg.createOperationMultipleEval(grid, x, cfg)
+    a = rng.standard_normal(n)
+    v = rng.standard_normal(args.points)
+    out_m = np.zeros(args.points)
+    out_t = np.zeros(n)
+
+    def run():
+        if args.kernel == "mult":
+            op.mult(a, out_m)
+        else:
+            op.multTranspose(v, out_t)
+
+    for _ in range(args.warmup):
+        run()
+    op.profile(True)
+    for _ in range(args.launches):
+        run()
+    cnt, sec = op.profileRead(KINDS[(args.kernel, args.precision)])
+    op.profile(False)
+    flop = 6.0 * n * args.points * args.dim
+    avg = sec / max(cnt, 1)
+    print(json.dumps({"kernel": args.kernel, "precision": args.precision, "dim": args.dim,
+                      "level": args.level, "n_grid": n, "points": args.points, "launches": cnt,
+                      "avg_ms": avg * 1e3, "tflops_ref_count": flop / avg / 1e12}))
+    op.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
