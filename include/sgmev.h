@@ -125,6 +125,22 @@ SGMEV_API int sgmev_mult_transpose_device(sgmev_op* op, const double* d_source,
                                           double* d_result);
 
 /*
+ * result[n_grid] = B^T source[n_data] (FP64) for callers that cannot allocate GPU memory.
+ * No counterpart in the reference. Everything is a device pointer the caller owns, in the
+ * reference's layouts (level_pow2/index [n_grid x dim], data [n_data x dim] row-major, already in
+ * the unit cube); work is enqueued on `stream` (NULL = the legacy default stream) and the call
+ * returns without synchronising. It allocates nothing: the split partial sums live in a fixed
+ * 16 MiB array inside the library (2^21 doubles), so n_grid is limited to 2,097,152
+ * (SGMEV_ERR_INVALID beyond that) and dim to 64. The first call on each device looks up that
+ * array's device address; make that first call before any stream capture. Calls share the array:
+ * calls whose work overlaps on the GPU race and must be serialised by the caller.
+ */
+SGMEV_API int sgmev_mult_transpose_noalloc(int dim, int64_t n_grid, const double* d_level_pow2,
+                                           const double* d_index, int64_t n_data,
+                                           const double* d_data, const double* d_source,
+                                           double* d_result, void* stream);
+
+/*
  * System matrix of the least-squares regression, applied on the device:
  *   result = B^T (B alpha) + lambda_times_m * alpha
  * replaces SystemMatrixLeastSquaresIdentity::mult

@@ -57,7 +57,7 @@ EXPORTED_SYMBOLS = (
     "sgmev_system_apply", "sgmev_system_apply_device", "sgmev_fit", "sgmev_get_duration",
     "sgmev_set_stream", "sgmev_synchronize", "sgmev_kernel_launches", "sggrid_regular",
     "sggrid_refine_surplus", "sggrid_level_index_for_eval", "sgmev_fma_peak", "sgmev_profile",
-    "sgmev_profile_read", "sgmev_fit_device",
+    "sgmev_profile_read", "sgmev_fit_device", "sgmev_mult_transpose_noalloc",
 )
 
 SGMEV_KERNEL_MULT_FP32 = 0
@@ -133,6 +133,7 @@ def load_library(path: str = LIBRARY_PATH):
         "sggrid_level_index_for_eval": (c_int, [c_int, i64, vp, vp, vp, vp]),
         "sgmev_fma_peak": (c_int, [c_int, pdbl, ctypes.POINTER(c_int)]),
         "sgmev_fit_device": (c_int, [vp, c_int, vp, dbl, i64, dbl, c_int, vp, pi64, pdbl]),
+        "sgmev_mult_transpose_noalloc": (c_int, [c_int, i64, vp, vp, i64, vp, vp, vp, vp]),
         "sgmev_profile": (c_int, [vp, c_int]),
         "sgmev_profile_read": (c_int, [vp, c_int, pi64, pdbl]),
     }
