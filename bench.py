@@ -8,8 +8,9 @@ y = 10 sin(pi x1 x2) + 20 (x3 - 0.5)^2 + 10 x4 + 5 x5 + N(0, 0.1^2); lambda = 1e
 Synthetic, seeded data of that shape (no dataset files are read).
 
 One step = one regression fit: b = B^T y, then CG on (B^T B + lambda M I) alpha = b to the
-relative FP64 residual `epsilon`, mixed precision (FP32 hat kernels inside CG, FP64-accurate
-residual for the outer iterative-refinement correction), all state resident on the GPU.
+relative FP64 residual `epsilon`, mixed precision (FP32 hat kernels inside CG; the outer
+iterative-refinement residual b - A alpha with the FP64-accurate float-float "df64" kernels),
+all state resident on the GPU.
 Each fit's alpha is checked against an FP64 solution computed once before timing.
 
 value   fits/s with the data resident in HBM (device pointers for y and alpha)
@@ -269,7 +270,8 @@ def run_ours(args):
     launches = op.kernelLaunches() - launches0
     kstats = {name: op.profileRead(kind) for name, kind in
               (("mult_fp32", sg.SGMEV_KERNEL_MULT_FP32), ("multT_fp32", sg.SGMEV_KERNEL_MULTT_FP32),
-               ("mult_fp64", sg.SGMEV_KERNEL_MULT_FP64), ("multT_fp64", sg.SGMEV_KERNEL_MULTT_FP64))}
+               ("mult_fp64", sg.SGMEV_KERNEL_MULT_FP64), ("multT_fp64", sg.SGMEV_KERNEL_MULTT_FP64),
+               ("mult_df64", sg.SGMEV_KERNEL_MULT_DF64), ("multT_df64", sg.SGMEV_KERNEL_MULTT_DF64))}
     op.profile(False)
     alpha = d_alpha.cpu().numpy()
     err = float(np.abs(alpha - alpha_ref).max() / np.abs(alpha_ref).max())

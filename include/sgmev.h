@@ -50,6 +50,9 @@ extern "C" {
 /* ---- precision of the evaluation kernels ---------------------------------------------- */
 #define SGMEV_FP64 0 /* native double: the plain FP64 path (parity 1e-12 vs the reference) */
 #define SGMEV_FP32 1 /* single-precision hat products and tile sums; FP64 cross-tile sums */
+#define SGMEV_DF64 2 /* FP64-accurate float-float ("df64") arithmetic on the FP32 pipes: every
+                        1-D hat exact, products and sums with ~2^-47 relative rounding; parity
+                        1e-12 like SGMEV_FP64, at a fraction of native FP64's cost on GB300 */
 
 typedef struct sgmev_op sgmev_op;
 
@@ -161,14 +164,18 @@ SGMEV_API int sgmev_system_apply_device(sgmev_op* op, const double* d_alpha, dou
  *   every 50 iterations, same warm start (reuse != 0 keeps alpha as the start vector).
  * mode:
  *   SGMEV_SOLVE_PLAIN  — CG with the op's own precision kernels (FP64 op: the plain FP64 path).
- *   SGMEV_SOLVE_MIXED  — FP32 kernels inside CG, FP64 residual b - A alpha for the outer
- *                        iterative-refinement correction (the op must have been created with
- *                        SGMEV_FP64; the FP32 copies are staged on first use).
+ *   SGMEV_SOLVE_MIXED  — iterative refinement: the outer residual b - A alpha (and b) with the
+ *                        FP64-accurate df64 kernels, the inner correction solves by CG with
+ *                        FP32 kernels and FP64 vectors; stops when ||b - A alpha||^2 <=
+ *                        epsilon^2 * ||b - A alpha_0||^2.
+ *   SGMEV_SOLVE_MIXED_NATIVE64 — the same with native FP64 kernels for the residual.
+ * Every op stages the FP64, FP32 and df64 copies of its data, so any mode works on any op.
  * y: [n_data] host; alpha: [n_grid] host in/out. iterations: total inner CG iterations;
  * residual: final delta_new (plain) or ||b - A alpha||^2 in FP64 (mixed).
  */
 #define SGMEV_SOLVE_PLAIN 0
 #define SGMEV_SOLVE_MIXED 1
+#define SGMEV_SOLVE_MIXED_NATIVE64 2
 SGMEV_API int sgmev_fit(sgmev_op* op, int mode, const double* y, double lambda,
                         int64_t max_iterations, double epsilon, int reuse, double* alpha,
                         int64_t* iterations, double* residual);

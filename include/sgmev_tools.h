@@ -31,6 +31,8 @@ SGMEV_API int sgmev_fma_peak(int precision, double* flops_per_second, int* sm_cl
 #define SGMEV_KERNEL_MULTT_FP32 1
 #define SGMEV_KERNEL_MULT_FP64 2
 #define SGMEV_KERNEL_MULTT_FP64 3
+#define SGMEV_KERNEL_MULT_DF64 4
+#define SGMEV_KERNEL_MULTT_DF64 5
 SGMEV_API int sgmev_profile(sgmev_op* op, int enable);
 SGMEV_API int sgmev_profile_read(sgmev_op* op, int kind, int64_t* launches, double* seconds);
 

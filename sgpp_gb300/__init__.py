@@ -46,8 +46,10 @@ SGMEV_ERR_OOM = -6
 
 SGMEV_FP64 = 0
 SGMEV_FP32 = 1
+SGMEV_DF64 = 2
 SGMEV_SOLVE_PLAIN = 0
 SGMEV_SOLVE_MIXED = 1
+SGMEV_SOLVE_MIXED_NATIVE64 = 2
 
 # every entry point declared in include/sgmev.h
 EXPORTED_SYMBOLS = (
@@ -64,6 +66,8 @@ SGMEV_KERNEL_MULT_FP32 = 0
 SGMEV_KERNEL_MULTT_FP32 = 1
 SGMEV_KERNEL_MULT_FP64 = 2
 SGMEV_KERNEL_MULTT_FP64 = 3
+SGMEV_KERNEL_MULT_DF64 = 4
+SGMEV_KERNEL_MULTT_DF64 = 5
 
 
 # ---- exceptions (base/src/sgpp/base/exception/) --------------------------------------------
@@ -362,7 +366,8 @@ class OperationMultipleEvalMPIType(enum.IntEnum):
 
 class OperationMultipleEvalConfiguration:
     """Operator selection plus a parameters tree. Parameters understood by the CUDA operator:
-    ``precision``: "double" (default) or "float"."""
+    ``precision``: "double" (default, native FP64), "df64" (FP64-accurate float-float on the
+    FP32 pipes) or "float"."""
 
     def __init__(self, type=OperationMultipleEvalType.DEFAULT,
                  subType=OperationMultipleEvalSubType.DEFAULT,
@@ -405,6 +410,8 @@ def _precision_of(params: dict) -> int:
         return SGMEV_FP64
     if p in ("float", "fp32", "f32", "single"):
         return SGMEV_FP32
+    if p in ("df64", "float-float", "double-float"):
+        return SGMEV_DF64
     raise OperationException(f"unknown precision {p!r}")
 
 
@@ -497,7 +504,8 @@ class OperationMultiEvalCuda:
         return float(load_library().sgmev_get_duration(self._h))
 
     def getImplementationName(self) -> str:
-        return "CUDA_LINEAR_FP64" if self.precision == SGMEV_FP64 else "CUDA_LINEAR_FP32"
+        return {SGMEV_FP64: "CUDA_LINEAR_FP64", SGMEV_FP32: "CUDA_LINEAR_FP32",
+                SGMEV_DF64: "CUDA_LINEAR_DF64"}[self.precision]
 
     def kernelLaunches(self) -> int:
         return int(load_library().sgmev_kernel_launches(self._h))
@@ -696,5 +704,6 @@ __all__ = [
     "createOperationMultipleEval", "OperationMultiEvalCuda", "SystemMatrixLeastSquaresIdentity",
     "ConjugateGradients", "OperationException", "FactoryException", "NotImplementedException",
     "GenerationException", "load_library", "device_count", "EXPORTED_SYMBOLS", "SGMEV_FP64",
-    "SGMEV_FP32", "SGMEV_SOLVE_PLAIN", "SGMEV_SOLVE_MIXED",
+    "SGMEV_FP32", "SGMEV_DF64", "SGMEV_SOLVE_PLAIN", "SGMEV_SOLVE_MIXED",
+    "SGMEV_SOLVE_MIXED_NATIVE64",
 ]

@@ -213,9 +213,208 @@ __global__ void mult_transpose_generic_kernel(const T* __restrict__ xt, const T*
 }
 
 // ---------------------------------------------------------------------------------------
+// df64: FP64-accurate products on the FP32 pipes (float-float arithmetic).
+//
+// A data coordinate is the pair x = xh + xl (xh = float(x), xl = float(x - xh)); a grid point
+// per dimension is the float4 (L, A, B, 0) = (2^l, 1 - i, 1 + i, 0), all exact in FP32 for
+// l, log2(i) < 24. The hat is
+//     h(x) = max(0, min(L x + A, B - L x))
+// and within the support both branch values at xh, a = fma(xh, L, A) and b = fma(xh, -L, B),
+// are exact FP32 numbers (Sterbenz's lemma: L xh lies within a factor two of i - 1, i or i + 1,
+// and L xh itself is exact because L is a power of two). The low part of x moves the rising
+// branch by +L xl and the falling one by -L xl, again exactly. The branch is chosen on the
+// sign of (a - b) + 2 L xl (a - b is exact near the kink) and the clamp on the sign of the pair
+// sum, so every one-dimensional hat is an exact float-float pair (hh, hl). Products use
+// Dekker's two-product via FMA (Dekker 1971: p = a*b, e = fma(a, b, -p)); sums use Knuth's
+// two-sum (Knuth, TAOCP vol. 2, 4.2.2). The relative error of one pair-product is ~2^-47, far
+// below the 1e-12 parity bound.
+// ---------------------------------------------------------------------------------------
+struct ff {
+  float h, l;
+};
+
+__device__ __forceinline__ ff hat_ff(float xh, float xl, float4 g) {
+  const float a = fmaf(xh, g.x, g.y);
+  const float b = fmaf(xh, -g.x, g.z);
+  const float s = g.x * xl;
+  const float c = fmaf(2.0f, s, a - b);
+  const bool rise = c <= 0.0f;
+  const float h = rise ? a : b;
+  const float lo = rise ? s : -s;
+  const bool pos = (h + lo) > 0.0f;
+  return ff{pos ? h : 0.0f, pos ? lo : 0.0f};
+}
+
+// (p.h + p.l) * (q.h + q.l), unnormalised; the l*l term is below the working precision
+__device__ __forceinline__ ff mul_ff(ff p, ff q) {
+  const float nh = p.h * q.h;
+  const float e = fmaf(p.h, q.h, -nh);
+  return ff{nh, fmaf(p.h, q.l, fmaf(p.l, q.h, e))};
+}
+
+// acc += q (two-sum on the high parts, low parts added)
+__device__ __forceinline__ void add_ff(ff& acc, ff q) {
+  const float s = acc.h + q.h;
+  const float bb = s - acc.h;
+  const float err = (acc.h - (s - bb)) + (q.h - bb);
+  acc.l = acc.l + (q.l + err);
+  acc.h = s;
+}
+
+// fast two-sum renormalisation (|acc.h| >= |acc.l| or acc.h == 0)
+__device__ __forceinline__ void renorm_ff(ff& acc) {
+  const float t = acc.h + acc.l;
+  acc.l = acc.l - (t - acc.h);
+  acc.h = t;
+}
+
+// mult in df64: part[split][j] = (hi, lo) of sum_{g in chunk} alpha_g prod_t hat(x_jt)
+template <int DIM, int R, int BLOCK, int GT>
+__global__ void __launch_bounds__(BLOCK) mult_df_kernel(
+    const float* __restrict__ xh_t, const float* __restrict__ xl_t, int64_t mpad,
+    const float4* __restrict__ gq, const float* __restrict__ ah_v, const float* __restrict__ al_v,
+    int64_t npad, int64_t chunk_len, int64_t tile_offset, float2* __restrict__ part) {
+  __shared__ float4 s_g[GT * DIM];
+  __shared__ float2 s_a[GT];
+  const int64_t tile = static_cast<int64_t>(blockIdx.x) + tile_offset;
+  const int64_t j0 = tile * (BLOCK * R) + threadIdx.x;
+  float xh[R][DIM], xl[R][DIM];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+#pragma unroll
+    for (int t = 0; t < DIM; ++t) {
+      xh[r][t] = xh_t[static_cast<int64_t>(t) * mpad + j0 + r * BLOCK];
+      xl[r][t] = xl_t[static_cast<int64_t>(t) * mpad + j0 + r * BLOCK];
+    }
+  }
+  ff acc[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) acc[r] = ff{0.0f, 0.0f};
+  const int64_t g_begin = static_cast<int64_t>(blockIdx.y) * chunk_len;
+  int64_t g_end = g_begin + chunk_len;
+  if (g_end > npad) g_end = npad;
+  for (int64_t g0 = g_begin; g0 < g_end; g0 += GT) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < GT * DIM; k += BLOCK) s_g[k] = gq[g0 * DIM + k];
+    for (int k = threadIdx.x; k < GT; k += BLOCK) s_a[k] = make_float2(ah_v[g0 + k], al_v[g0 + k]);
+    __syncthreads();
+    for (int g = 0; g < GT; ++g) {
+      ff p[R];
+      const float4 q0 = s_g[g * DIM];
+#pragma unroll
+      for (int r = 0; r < R; ++r) p[r] = hat_ff(xh[r][0], xl[r][0], q0);
+#pragma unroll
+      for (int t = 1; t < DIM; ++t) {
+        const float4 qt = s_g[g * DIM + t];
+#pragma unroll
+        for (int r = 0; r < R; ++r) p[r] = mul_ff(p[r], hat_ff(xh[r][t], xl[r][t], qt));
+      }
+      const float2 a = s_a[g];
+#pragma unroll
+      for (int r = 0; r < R; ++r) add_ff(acc[r], mul_ff(p[r], ff{a.x, a.y}));
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) renorm_ff(acc[r]);
+  }
+  float2* out = part + static_cast<int64_t>(blockIdx.y) * mpad;
+#pragma unroll
+  for (int r = 0; r < R; ++r) out[j0 + r * BLOCK] = make_float2(acc[r].h, acc[r].l);
+}
+
+// multT in df64: part[split][g] = (hi, lo) of sum_{j in chunk} v_j prod_t hat(x_jt)
+template <int DIM, int RG, int BLOCK, int DT>
+__global__ void __launch_bounds__(BLOCK) mult_transpose_df_kernel(
+    const float* __restrict__ xh_t, const float* __restrict__ xl_t, const float* __restrict__ vh,
+    const float* __restrict__ vl, int64_t mpad, const float4* __restrict__ gq, int64_t npad,
+    int64_t chunk_len, int64_t tile_offset, float2* __restrict__ part) {
+  __shared__ float2 s_x[DIM * DT];
+  __shared__ float2 s_v[DT];
+  const int64_t tile = static_cast<int64_t>(blockIdx.x) + tile_offset;
+  const int64_t g0 = tile * (BLOCK * RG) + threadIdx.x;
+  float4 q[RG][DIM];
+#pragma unroll
+  for (int k = 0; k < RG; ++k) {
+#pragma unroll
+    for (int t = 0; t < DIM; ++t) q[k][t] = gq[(g0 + k * BLOCK) * DIM + t];
+  }
+  ff acc[RG];
+#pragma unroll
+  for (int k = 0; k < RG; ++k) acc[k] = ff{0.0f, 0.0f};
+  const int64_t j_begin = static_cast<int64_t>(blockIdx.y) * chunk_len;
+  int64_t j_end = j_begin + chunk_len;
+  if (j_end > mpad) j_end = mpad;
+  for (int64_t jt = j_begin; jt < j_end; jt += DT) {
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < DIM; ++t) {
+      for (int k = threadIdx.x; k < DT; k += BLOCK) {
+        const int64_t src = static_cast<int64_t>(t) * mpad + jt + k;
+        s_x[t * DT + k] = make_float2(xh_t[src], xl_t[src]);
+      }
+    }
+    for (int k = threadIdx.x; k < DT; k += BLOCK) s_v[k] = make_float2(vh[jt + k], vl[jt + k]);
+    __syncthreads();
+    for (int j = 0; j < DT; ++j) {
+      ff p[RG];
+      const float2 x0 = s_x[j];
+#pragma unroll
+      for (int k = 0; k < RG; ++k) p[k] = hat_ff(x0.x, x0.y, q[k][0]);
+#pragma unroll
+      for (int t = 1; t < DIM; ++t) {
+        const float2 xv = s_x[t * DT + j];
+#pragma unroll
+        for (int k = 0; k < RG; ++k) p[k] = mul_ff(p[k], hat_ff(xv.x, xv.y, q[k][t]));
+      }
+      const float2 vj = s_v[j];
+#pragma unroll
+      for (int k = 0; k < RG; ++k) add_ff(acc[k], mul_ff(p[k], ff{vj.x, vj.y}));
+    }
+#pragma unroll
+    for (int k = 0; k < RG; ++k) renorm_ff(acc[k]);
+  }
+  float2* out = part + static_cast<int64_t>(blockIdx.y) * npad;
+#pragma unroll
+  for (int k = 0; k < RG; ++k) out[g0 + k * BLOCK] = make_float2(acc[k].h, acc[k].l);
+}
+
+// generic-dimension df64 fallbacks (one point per thread, coordinates from global/L1)
+__global__ void mult_df_generic_kernel(const float* __restrict__ xh_t, const float* __restrict__ xl_t,
+                                       int64_t mpad, int dim, const float4* __restrict__ gq,
+                                       const float* __restrict__ ah_v, const float* __restrict__ al_v,
+                                       int64_t npad, int64_t chunk_len, int64_t j_offset,
+                                       int64_t j_count, float2* __restrict__ part);
+__global__ void mult_transpose_df_generic_kernel(const float* __restrict__ xh_t,
+                                                 const float* __restrict__ xl_t,
+                                                 const float* __restrict__ vh,
+                                                 const float* __restrict__ vl, int64_t mpad, int dim,
+                                                 const float4* __restrict__ gq, int64_t npad,
+                                                 int64_t chunk_len, int64_t g_offset,
+                                                 int64_t g_count, float2* __restrict__ part);
+
+// ---------------------------------------------------------------------------------------
 // Fixed-order reduction over splits: out[i] = sum_s part[s*stride + i] (+ scale * add[i]),
 // accumulated in double. Indices in [n_valid, n_total) are written as zero (padding).
 // ---------------------------------------------------------------------------------------
+// float-float partials: value = hi + lo, accumulated in double
+template <typename TP>
+__device__ __forceinline__ double part_value(TP v) {
+  return static_cast<double>(v);
+}
+template <>
+__device__ __forceinline__ double part_value<float2>(float2 v) {
+  return static_cast<double>(v.x) + static_cast<double>(v.y);
+}
+
+template <typename TO>
+__device__ __forceinline__ void store_out(TO* out, int64_t i, double s) {
+  out[i] = static_cast<TO>(s);
+}
+template <>
+__device__ __forceinline__ void store_out<float2>(float2* out, int64_t i, double s) {
+  const float h = static_cast<float>(s);
+  out[i] = make_float2(h, static_cast<float>(s - static_cast<double>(h)));
+}
+
 template <typename TP, typename TO>
 __global__ void reduce_splits_kernel(const TP* __restrict__ part, int nsplit, int64_t stride,
                                      int64_t begin, int64_t n_valid, int64_t n_total,
@@ -225,10 +424,10 @@ __global__ void reduce_splits_kernel(const TP* __restrict__ part, int nsplit, in
        i < n_total; i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     double s = 0.0;
     if (i < n_valid) {
-      for (int k = 0; k < nsplit; ++k) s += static_cast<double>(part[k * stride + i]);
+      for (int k = 0; k < nsplit; ++k) s += part_value(part[k * stride + i]);
       if (add) s = fma(scale, add[i], s);
     }
-    out[i] = static_cast<TO>(s);
+    store_out(out, i, s);
   }
 }
 

@@ -94,16 +94,20 @@ struct sgmev_op {
   int64_t target_ctas = 4 * 152;
 
   double* xt64 = nullptr;
-  float* xt32 = nullptr;
+  float* xt32 = nullptr;    // float(x)
+  float* xt32lo = nullptr;  // float(x - float(x)): the df64 low part
   double2* li64 = nullptr;
   float2* li32 = nullptr;
+  float4* gq = nullptr;     // df64 grid constants (2^l, 1 - i, 1 + i, 0)
   int64_t npad_cap = 0;
 
   // work vectors
   double* a64 = nullptr;   // [npad] converted input (mult) / padded grid vector
   float* a32 = nullptr;    // [npad]
+  float* a32lo = nullptr;  // [npad] df64 low part
   double* v64 = nullptr;   // [mpad] data-side vector (mult output / multT input)
   float* v32 = nullptr;    // [mpad]
+  float* v32lo = nullptr;  // [mpad] df64 low part
   double* out64 = nullptr; // [max(npad, mpad)]
   void* part = nullptr;
   size_t part_bytes = 0;
@@ -136,7 +140,14 @@ struct sgmev_op {
 namespace sgmev {
 
 // kinds of timed tile kernels (sgmev_tools.h SGMEV_KERNEL_*)
-enum { KIND_MULT_FP32 = 0, KIND_MULTT_FP32 = 1, KIND_MULT_FP64 = 2, KIND_MULTT_FP64 = 3 };
+enum {
+  KIND_MULT_FP32 = 0,
+  KIND_MULTT_FP32 = 1,
+  KIND_MULT_FP64 = 2,
+  KIND_MULTT_FP64 = 3,
+  KIND_MULT_DF64 = 4,
+  KIND_MULTT_DF64 = 5
+};
 
 template <typename T>
 static int kind_mult() { return sizeof(T) == 4 ? KIND_MULT_FP32 : KIND_MULT_FP64; }
@@ -170,7 +181,7 @@ static void prof_end(sgmev_op* op, long i) {
 __global__ void stage_data_kernel(const double* __restrict__ rows, int64_t m, int dim,
                                   int64_t mpad, const double* __restrict__ bb_left,
                                   const double* __restrict__ bb_width, double* __restrict__ xt64,
-                                  float* __restrict__ xt32) {
+                                  float* __restrict__ xt32, float* __restrict__ xt32lo) {
   const int64_t total = mpad * dim;
   for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
        k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -182,14 +193,16 @@ __global__ void stage_data_kernel(const double* __restrict__ rows, int64_t m, in
       if (bb_left) x = (x - bb_left[t]) / bb_width[t];
     }
     xt64[k] = x;
-    xt32[k] = static_cast<float>(x);
+    const float h = static_cast<float>(x);
+    xt32[k] = h;
+    xt32lo[k] = static_cast<float>(x - static_cast<double>(h));
   }
 }
 
 __global__ void stage_grid_kernel(const double* __restrict__ level_pow2,
                                   const double* __restrict__ index, int64_t n, int dim,
                                   int64_t npad, double2* __restrict__ li64,
-                                  float2* __restrict__ li32) {
+                                  float2* __restrict__ li32, float4* __restrict__ gq) {
   const int64_t total = npad * dim;
   for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
        k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -200,17 +213,74 @@ __global__ void stage_grid_kernel(const double* __restrict__ level_pow2,
     }
     li64[k] = make_double2(L, I);
     li32[k] = make_float2(static_cast<float>(L), static_cast<float>(I));
+    // padded rows (L = 0): a = 1 - 2 = -1, b = 1 + 2 = 3, so min(a, b) < 0 and the hat is 0
+    gq[k] = make_float4(static_cast<float>(L), static_cast<float>(1.0 - I),
+                        static_cast<float>(1.0 + I), 0.0f);
   }
 }
 
 __global__ void convert_pad_kernel(const double* __restrict__ in, int64_t n, int64_t npad,
-                                   double* __restrict__ out64, float* __restrict__ out32) {
+                                   double* __restrict__ out64, float* __restrict__ out32,
+                                   float* __restrict__ out32lo) {
   for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < npad;
        k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const double v = k < n ? in[k] : 0.0;
     if (out64) out64[k] = v;
-    if (out32) out32[k] = static_cast<float>(v);
+    const float h = static_cast<float>(v);
+    if (out32) out32[k] = h;
+    if (out32lo) out32lo[k] = static_cast<float>(v - static_cast<double>(h));
   }
+}
+
+// generic-dimension df64 kernels
+__global__ void mult_df_generic_kernel(const float* __restrict__ xh_t, const float* __restrict__ xl_t,
+                                       int64_t mpad, int dim, const float4* __restrict__ gq,
+                                       const float* __restrict__ ah_v, const float* __restrict__ al_v,
+                                       int64_t npad, int64_t chunk_len, int64_t j_offset,
+                                       int64_t j_count, float2* __restrict__ part) {
+  const int64_t j = j_offset + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= j_offset + j_count) return;
+  const int64_t g_begin = static_cast<int64_t>(blockIdx.y) * chunk_len;
+  int64_t g_end = g_begin + chunk_len;
+  if (g_end > npad) g_end = npad;
+  ff acc{0.0f, 0.0f};
+  for (int64_t g = g_begin; g < g_end; ++g) {
+    ff p = hat_ff(xh_t[j], xl_t[j], gq[g * dim]);
+    for (int t = 1; t < dim; ++t) {
+      const int64_t src = static_cast<int64_t>(t) * mpad + j;
+      p = mul_ff(p, hat_ff(xh_t[src], xl_t[src], gq[g * dim + t]));
+    }
+    add_ff(acc, mul_ff(p, ff{ah_v[g], al_v[g]}));
+    if ((g & 31) == 31) renorm_ff(acc);
+  }
+  renorm_ff(acc);
+  part[static_cast<int64_t>(blockIdx.y) * mpad + j] = make_float2(acc.h, acc.l);
+}
+
+__global__ void mult_transpose_df_generic_kernel(const float* __restrict__ xh_t,
+                                                 const float* __restrict__ xl_t,
+                                                 const float* __restrict__ vh,
+                                                 const float* __restrict__ vl, int64_t mpad, int dim,
+                                                 const float4* __restrict__ gq, int64_t npad,
+                                                 int64_t chunk_len, int64_t g_offset,
+                                                 int64_t g_count, float2* __restrict__ part) {
+  const int64_t g = g_offset + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (g >= g_offset + g_count) return;
+  const int64_t j_begin = static_cast<int64_t>(blockIdx.y) * chunk_len;
+  int64_t j_end = j_begin + chunk_len;
+  if (j_end > mpad) j_end = mpad;
+  ff acc{0.0f, 0.0f};
+  for (int64_t j = j_begin; j < j_end; ++j) {
+    ff p = hat_ff(xh_t[j], xl_t[j], gq[g * dim]);
+    for (int t = 1; t < dim; ++t) {
+      const int64_t src = static_cast<int64_t>(t) * mpad + j;
+      p = mul_ff(p, hat_ff(xh_t[src], xl_t[src], gq[g * dim + t]));
+    }
+    add_ff(acc, mul_ff(p, ff{vh[j], vl[j]}));
+    if ((j & 31) == 31) renorm_ff(acc);
+  }
+  renorm_ff(acc);
+  part[static_cast<int64_t>(blockIdx.y) * npad + g] = make_float2(acc.h, acc.l);
 }
 
 // deterministic dot product: fixed grid, fixed tree
@@ -415,57 +485,185 @@ static unsigned vec_blocks(int64_t n) {
   return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(kReduceBlocks, ceil_div(n, 256))));
 }
 
+// df64 tile kernels (float-float), R = 4 data points / RG = 2 grid points per thread
+constexpr int kDfMultR = 4;
+constexpr int kDfMulttRG = 2;
+
+template <int DIM>
+static void launch_mult_df_dim(sgmev_op* op, const float* ah, const float* al, const Plan& p,
+                               int64_t tile_offset, float2* part) {
+  dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+  mult_df_kernel<DIM, kDfMultR, kBlock, kGT><<<grid, kBlock, 0, op->stream>>>(
+      op->xt32, op->xt32lo, op->mpad, op->gq, ah, al, op->npad, p.chunk, tile_offset, part);
+}
+
+template <int DIM>
+static void launch_multt_df_dim(sgmev_op* op, const float* vh, const float* vl, const Plan& p,
+                                int64_t tile_offset, float2* part) {
+  dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+  mult_transpose_df_kernel<DIM, kDfMulttRG, kBlock, kDT><<<grid, kBlock, 0, op->stream>>>(
+      op->xt32, op->xt32lo, vh, vl, op->mpad, op->gq, op->npad, p.chunk, tile_offset, part);
+}
+
+static int run_mult_df(sgmev_op* op, const float* ah, const float* al, int64_t j_begin,
+                       int64_t j_end, Plan* used) {
+  float2* part = static_cast<float2*>(op->part);
+  if (op->dim <= kMaxTemplDim) {
+    const int64_t tile_pts = kBlock * kDfMultR;
+    const int64_t t0 = j_begin / tile_pts;
+    const int64_t t1 = ceil_div(j_end, tile_pts);
+    Plan p = plan_mult<float>(op, t1 - t0);
+    const long ev = prof_begin(op, KIND_MULT_DF64);
+    switch (op->dim) {
+#define F(D)                                               \
+  case D:                                                  \
+    launch_mult_df_dim<D>(op, ah, al, p, t0, part);        \
+    break;
+      SGMEV_DIM_CASES(F)
+#undef F
+      default:
+        break;
+    }
+    prof_end(op, ev);
+    *used = p;
+  } else {
+    const int64_t count = j_end - j_begin;
+    Plan p = plan_mult<float>(op, ceil_div(count, kBlock));
+    dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+    const long ev = prof_begin(op, KIND_MULT_DF64);
+    mult_df_generic_kernel<<<grid, kBlock, 0, op->stream>>>(op->xt32, op->xt32lo, op->mpad, op->dim,
+                                                            op->gq, ah, al, op->npad, p.chunk,
+                                                            j_begin, count, part);
+    prof_end(op, ev);
+    *used = p;
+  }
+  op->launches += 1;
+  SGMEV_CUDA(cudaGetLastError());
+  return SGMEV_OK;
+}
+
+static int run_multt_df(sgmev_op* op, const float* vh, const float* vl, int64_t g_begin,
+                        int64_t g_end, Plan* used) {
+  float2* part = static_cast<float2*>(op->part);
+  if (op->dim <= kMaxTemplDim) {
+    const int64_t tile_pts = kBlock * kDfMulttRG;
+    const int64_t t0 = g_begin / tile_pts;
+    const int64_t t1 = ceil_div(g_end, tile_pts);
+    Plan p = plan_multt<float>(op, t1 - t0);
+    const long ev = prof_begin(op, KIND_MULTT_DF64);
+    switch (op->dim) {
+#define F(D)                                                \
+  case D:                                                   \
+    launch_multt_df_dim<D>(op, vh, vl, p, t0, part);        \
+    break;
+      SGMEV_DIM_CASES(F)
+#undef F
+      default:
+        break;
+    }
+    prof_end(op, ev);
+    *used = p;
+  } else {
+    const int64_t count = g_end - g_begin;
+    Plan p = plan_multt<float>(op, ceil_div(count, kBlock));
+    dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+    const long ev = prof_begin(op, KIND_MULTT_DF64);
+    mult_transpose_df_generic_kernel<<<grid, kBlock, 0, op->stream>>>(
+        op->xt32, op->xt32lo, vh, vl, op->mpad, op->dim, op->gq, op->npad, p.chunk, g_begin,
+        count, part);
+    prof_end(op, ev);
+    *used = p;
+  }
+  op->launches += 1;
+  SGMEV_CUDA(cudaGetLastError());
+  return SGMEV_OK;
+}
+
+// data points per mult tile / grid points per multT tile for a precision (tile-aligned ranges)
+static int64_t mult_tile_pts(const sgmev_op* op, int prec) {
+  if (op->dim > kMaxTemplDim) return 1;
+  if (prec == SGMEV_FP64) return kBlock * Blocking<double>::mult_r(op->dim);
+  if (prec == SGMEV_DF64) return kBlock * kDfMultR;
+  return kBlock * Blocking<float>::mult_r(op->dim);
+}
+
+static int64_t multt_tile_pts(const sgmev_op* op, int prec) {
+  if (op->dim > kMaxTemplDim) return 1;
+  if (prec == SGMEV_FP64) return kBlock * Blocking<double>::multt_r(op->dim);
+  if (prec == SGMEV_DF64) return kBlock * kDfMulttRG;
+  return kBlock * Blocking<float>::multt_r(op->dim);
+}
+
 // ---------------------------------------------------------------------------------------
 // device-side products on padded device vectors
 // ---------------------------------------------------------------------------------------
-// v_out[mpad] (zero beyond m) = B * a_in[npad]   in precision `prec`; a_in must be padded.
-static int dev_mult(sgmev_op* op, int prec, const double* a_in64, const float* a_in32,
-                    double* out64, float* out32, int64_t j_begin, int64_t j_end) {
+// Inputs per precision: FP64 a64; FP32 a32; DF64 (a32, a32lo) — all padded to npad.
+// out64 / out32 [mpad] (zero beyond m) = B a over data range [j_begin, j_end).
+static int dev_mult(sgmev_op* op, int prec, const double* a64, const float* a32,
+                    const float* a32lo, double* out64, float* out32, int64_t j_begin,
+                    int64_t j_end) {
   if (j_end <= j_begin) return SGMEV_OK;
   Plan p;
-  if (prec == SGMEV_FP64) {
-    SGMEV_TRY(run_mult<double>(op, op->xt64, op->li64, a_in64, j_begin, j_end, &p));
-  } else {
-    SGMEV_TRY(run_mult<float>(op, op->xt32, op->li32, a_in32, j_begin, j_end, &p));
-  }
   const int64_t total = j_end;
+  const int64_t valid = std::min(op->m, total);
   if (prec == SGMEV_FP64) {
-    if (out64) SGMEV_TRY((run_reduce<double, double>(op, (int)p.nsplit, op->mpad, j_begin, std::min(op->m, total), total, out64, nullptr, 0.0)));
-    if (out32) SGMEV_TRY((run_reduce<double, float>(op, (int)p.nsplit, op->mpad, j_begin, std::min(op->m, total), total, out32, nullptr, 0.0)));
+    SGMEV_TRY(run_mult<double>(op, op->xt64, op->li64, a64, j_begin, j_end, &p));
+    if (out64) SGMEV_TRY((run_reduce<double, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
+    if (out32) SGMEV_TRY((run_reduce<double, float>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out32, nullptr, 0.0)));
+  } else if (prec == SGMEV_DF64) {
+    SGMEV_TRY(run_mult_df(op, a32, a32lo, j_begin, j_end, &p));
+    if (out64) SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
+    if (out32) SGMEV_TRY((run_reduce<float2, float>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out32, nullptr, 0.0)));
   } else {
-    if (out64) SGMEV_TRY((run_reduce<float, double>(op, (int)p.nsplit, op->mpad, j_begin, std::min(op->m, total), total, out64, nullptr, 0.0)));
-    if (out32) SGMEV_TRY((run_reduce<float, float>(op, (int)p.nsplit, op->mpad, j_begin, std::min(op->m, total), total, out32, nullptr, 0.0)));
+    SGMEV_TRY(run_mult<float>(op, op->xt32, op->li32, a32, j_begin, j_end, &p));
+    if (out64) SGMEV_TRY((run_reduce<float, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
+    if (out32) SGMEV_TRY((run_reduce<float, float>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out32, nullptr, 0.0)));
   }
   return SGMEV_OK;
 }
 
-// out64[g_begin..g_end) = B^T v_in[mpad] (+ scale * add)
-static int dev_multt(sgmev_op* op, int prec, const double* v_in64, const float* v_in32,
-                     double* out64, int64_t g_begin, int64_t g_end, const double* add,
-                     double scale) {
+// out64[g_begin..g_end) = B^T v (+ scale * add); inputs FP64 v64, FP32 v32, DF64 (v32, v32lo)
+static int dev_multt(sgmev_op* op, int prec, const double* v64, const float* v32,
+                     const float* v32lo, double* out64, int64_t g_begin, int64_t g_end,
+                     const double* add, double scale) {
   if (g_end <= g_begin) return SGMEV_OK;
   Plan p;
+  const int64_t valid = std::min(op->n, g_end);
   if (prec == SGMEV_FP64) {
-    SGMEV_TRY(run_multt<double>(op, op->xt64, v_in64, op->li64, g_begin, g_end, &p));
-    SGMEV_TRY((run_reduce<double, double>(op, (int)p.nsplit, op->npad, g_begin, std::min(op->n, g_end), g_end, out64, add, scale)));
+    SGMEV_TRY(run_multt<double>(op, op->xt64, v64, op->li64, g_begin, g_end, &p));
+    SGMEV_TRY((run_reduce<double, double>(op, (int)p.nsplit, op->npad, g_begin, valid, g_end, out64, add, scale)));
+  } else if (prec == SGMEV_DF64) {
+    SGMEV_TRY(run_multt_df(op, v32, v32lo, g_begin, g_end, &p));
+    SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->npad, g_begin, valid, g_end, out64, add, scale)));
   } else {
-    SGMEV_TRY(run_multt<float>(op, op->xt32, v_in32, op->li32, g_begin, g_end, &p));
-    SGMEV_TRY((run_reduce<float, double>(op, (int)p.nsplit, op->npad, g_begin, std::min(op->n, g_end), g_end, out64, add, scale)));
+    SGMEV_TRY(run_multt<float>(op, op->xt32, v32, op->li32, g_begin, g_end, &p));
+    SGMEV_TRY((run_reduce<float, double>(op, (int)p.nsplit, op->npad, g_begin, valid, g_end, out64, add, scale)));
   }
+  return SGMEV_OK;
+}
+
+static int dev_convert(sgmev_op* op, const double* in, int64_t n, int64_t npad, double* o64,
+                       float* o32, float* o32lo) {
+  convert_pad_kernel<<<vec_blocks(npad), 256, 0, op->stream>>>(in, n, npad, o64, o32, o32lo);
+  op->launches += 1;
+  SGMEV_CUDA(cudaGetLastError());
   return SGMEV_OK;
 }
 
 // out64[npad] = B^T (B a) + lm * a, a given as padded FP64 device vector [npad]
 static int dev_system(sgmev_op* op, int prec, const double* a64, double* out64, double lm) {
   if (prec == SGMEV_FP32) {
-    convert_pad_kernel<<<vec_blocks(op->npad), 256, 0, op->stream>>>(a64, op->npad, op->npad,
-                                                                      nullptr, op->a32);
-    op->launches += 1;
-    SGMEV_TRY(dev_mult(op, prec, nullptr, op->a32, nullptr, op->v32, 0, op->mpad));
-    SGMEV_TRY(dev_multt(op, prec, nullptr, op->v32, out64, 0, op->npad, a64, lm));
+    SGMEV_TRY(dev_convert(op, a64, op->npad, op->npad, nullptr, op->a32, nullptr));
+    SGMEV_TRY(dev_mult(op, prec, nullptr, op->a32, nullptr, nullptr, op->v32, 0, op->mpad));
+    SGMEV_TRY(dev_multt(op, prec, nullptr, op->v32, nullptr, out64, 0, op->npad, a64, lm));
+  } else if (prec == SGMEV_DF64) {
+    SGMEV_TRY(dev_convert(op, a64, op->npad, op->npad, nullptr, op->a32, op->a32lo));
+    SGMEV_TRY(dev_mult(op, prec, nullptr, op->a32, op->a32lo, op->v64, nullptr, 0, op->mpad));
+    SGMEV_TRY(dev_convert(op, op->v64, op->mpad, op->mpad, nullptr, op->v32, op->v32lo));
+    SGMEV_TRY(dev_multt(op, prec, nullptr, op->v32, op->v32lo, out64, 0, op->npad, a64, lm));
   } else {
-    SGMEV_TRY(dev_mult(op, prec, a64, nullptr, op->v64, nullptr, 0, op->mpad));
-    SGMEV_TRY(dev_multt(op, prec, op->v64, nullptr, out64, 0, op->npad, a64, lm));
+    SGMEV_TRY(dev_mult(op, prec, a64, nullptr, nullptr, op->v64, nullptr, 0, op->mpad));
+    SGMEV_TRY(dev_multt(op, prec, op->v64, nullptr, nullptr, out64, 0, op->npad, a64, lm));
   }
   return SGMEV_OK;
 }
@@ -545,8 +743,10 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
   if (npad > op->npad_cap) {
     SGMEV_TRY(dalloc(&op->li64, static_cast<size_t>(npad * op->dim)));
     SGMEV_TRY(dalloc(&op->li32, static_cast<size_t>(npad * op->dim)));
+    SGMEV_TRY(dalloc(&op->gq, static_cast<size_t>(npad * op->dim)));
     SGMEV_TRY(dalloc(&op->a64, static_cast<size_t>(npad)));
     SGMEV_TRY(dalloc(&op->a32, static_cast<size_t>(npad)));
+    SGMEV_TRY(dalloc(&op->a32lo, static_cast<size_t>(npad)));
     SGMEV_TRY(dalloc(&op->cg, static_cast<size_t>(npad) * 8));
     op->npad_cap = npad;
   }
@@ -565,8 +765,8 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
     cudaMemcpyAsync(d_l, level_pow2, bytes, cudaMemcpyHostToDevice, op->stream);
     cudaMemcpyAsync(d_i, index, bytes, cudaMemcpyHostToDevice, op->stream);
   }
-  stage_grid_kernel<<<vec_blocks(npad * op->dim), 256, 0, op->stream>>>(d_l, d_i, n, op->dim,
-                                                                         npad, op->li64, op->li32);
+  stage_grid_kernel<<<vec_blocks(npad * op->dim), 256, 0, op->stream>>>(
+      d_l, d_i, n, op->dim, npad, op->li64, op->li32, op->gq);
   op->launches += 1;
   e = cudaStreamSynchronize(op->stream);
   cudaFree(d_l);
@@ -589,8 +789,9 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
 }
 
 static void release(sgmev_op* op) {
-  void* ptrs[] = {op->xt64, op->xt32, op->li64, op->li32, op->a64, op->a32, op->v64,
-                  op->v32,  op->out64, op->part, op->cg,   op->dot_part, op->dot_out};
+  void* ptrs[] = {op->xt64, op->xt32, op->xt32lo, op->li64, op->li32, op->gq, op->a64,
+                  op->a32,  op->a32lo, op->v64,   op->v32,  op->v32lo, op->out64, op->part,
+                  op->cg,   op->dot_part, op->dot_out};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (op->host_scalar) cudaFreeHost(op->host_scalar);
@@ -667,8 +868,8 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   if (n_data > 0 && !data) return fail(SGMEV_ERR_INVALID, "data is NULL");
   if ((bb_left == nullptr) != (bb_right == nullptr))
     return fail(SGMEV_ERR_INVALID, "bounding box needs both left and right");
-  if (precision != SGMEV_FP64 && precision != SGMEV_FP32)
-    return fail(SGMEV_ERR_INVALID, "precision must be SGMEV_FP64 or SGMEV_FP32");
+  if (precision != SGMEV_FP64 && precision != SGMEV_FP32 && precision != SGMEV_DF64)
+    return fail(SGMEV_ERR_INVALID, "precision must be SGMEV_FP64, SGMEV_FP32 or SGMEV_DF64");
   if (n_data > (int64_t(1) << 40) || n_grid > (int64_t(1) << 34))
     return fail(SGMEV_ERR_INVALID, "problem too large");
   SGMEV_TRY(check_grid(dim, n_grid, level_pow2, index));
@@ -721,8 +922,10 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   // data
   CREATE_TRY(dalloc(&op->xt64, static_cast<size_t>(op->mpad * dim)));
   CREATE_TRY(dalloc(&op->xt32, static_cast<size_t>(op->mpad * dim)));
+  CREATE_TRY(dalloc(&op->xt32lo, static_cast<size_t>(op->mpad * dim)));
   CREATE_TRY(dalloc(&op->v64, static_cast<size_t>(op->mpad)));
   CREATE_TRY(dalloc(&op->v32, static_cast<size_t>(op->mpad)));
+  CREATE_TRY(dalloc(&op->v32lo, static_cast<size_t>(op->mpad)));
   {
     double* d_rows = nullptr;
     double* d_bb = nullptr;
@@ -746,7 +949,8 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
       cudaMemcpyAsync(d_bb, hb.data(), sizeof(double) * 2 * dim, cudaMemcpyHostToDevice, op->stream);
     }
     stage_data_kernel<<<vec_blocks(op->mpad * dim), 256, 0, op->stream>>>(
-        d_rows, n_data, dim, op->mpad, d_bb, d_bb ? d_bb + dim : nullptr, op->xt64, op->xt32);
+        d_rows, n_data, dim, op->mpad, d_bb, d_bb ? d_bb + dim : nullptr, op->xt64, op->xt32,
+        op->xt32lo);
     op->launches += 1;
     cudaError_t e = cudaStreamSynchronize(op->stream);
     cudaFree(d_rows);
@@ -818,16 +1022,14 @@ static int mult_common(sgmev_op* op, const double* alpha_dev_or_null, const doub
                                  cudaMemcpyHostToDevice, op->stream));
     src = op->out64;
   }
-  convert_pad_kernel<<<vec_blocks(op->npad), 256, 0, op->stream>>>(
-      src, op->n, op->npad, prec == SGMEV_FP64 ? op->a64 : nullptr,
-      prec == SGMEV_FP32 ? op->a32 : nullptr);
-  op->launches += 1;
+  SGMEV_TRY(dev_convert(op, src, op->n, op->npad, prec == SGMEV_FP64 ? op->a64 : nullptr,
+                        prec == SGMEV_FP64 ? nullptr : op->a32,
+                        prec == SGMEV_DF64 ? op->a32lo : nullptr));
   // tile-aligned data range covering [start, end)
-  const int64_t tile_pts = kBlock * (prec == SGMEV_FP64 ? Blocking<double>::mult_r(op->dim)
-                                                        : Blocking<float>::mult_r(op->dim));
-  const int64_t jb = op->dim <= kMaxTemplDim ? (start / tile_pts) * tile_pts : start;
-  const int64_t je = op->dim <= kMaxTemplDim ? std::min(op->mpad, round_up(end, tile_pts)) : end;
-  SGMEV_TRY(dev_mult(op, prec, op->a64, op->a32, op->v64, nullptr, jb, je));
+  const int64_t tile_pts = mult_tile_pts(op, prec);
+  const int64_t jb = (start / tile_pts) * tile_pts;
+  const int64_t je = std::min(op->mpad, round_up(end, tile_pts));
+  SGMEV_TRY(dev_mult(op, prec, op->a64, op->a32, op->a32lo, op->v64, nullptr, jb, je));
   if (result_host) {
     if (end > start)
       SGMEV_CUDA(cudaMemcpyAsync(result_host + start, op->v64 + start,
@@ -853,16 +1055,14 @@ static int multt_common(sgmev_op* op, const double* src_dev, const double* src_h
                                  cudaMemcpyHostToDevice, op->stream));
     src = op->out64;
   }
-  convert_pad_kernel<<<vec_blocks(op->mpad), 256, 0, op->stream>>>(
-      src, op->m, op->mpad, prec == SGMEV_FP64 ? op->v64 : nullptr,
-      prec == SGMEV_FP32 ? op->v32 : nullptr);
-  op->launches += 1;
-  const int64_t tile_pts = kBlock * (prec == SGMEV_FP64 ? Blocking<double>::multt_r(op->dim)
-                                                        : Blocking<float>::multt_r(op->dim));
-  const int64_t gb = op->dim <= kMaxTemplDim ? (start / tile_pts) * tile_pts : start;
-  const int64_t ge = op->dim <= kMaxTemplDim ? std::min(op->npad, round_up(end, tile_pts)) : end;
+  SGMEV_TRY(dev_convert(op, src, op->m, op->mpad, prec == SGMEV_FP64 ? op->v64 : nullptr,
+                        prec == SGMEV_FP64 ? nullptr : op->v32,
+                        prec == SGMEV_DF64 ? op->v32lo : nullptr));
+  const int64_t tile_pts = multt_tile_pts(op, prec);
+  const int64_t gb = (start / tile_pts) * tile_pts;
+  const int64_t ge = std::min(op->npad, round_up(end, tile_pts));
   double* tmp = op->cg + 7 * op->npad;  // spare CG slot as result staging
-  SGMEV_TRY(dev_multt(op, prec, op->v64, op->v32, tmp, gb, ge, nullptr, 0.0));
+  SGMEV_TRY(dev_multt(op, prec, op->v64, op->v32, op->v32lo, tmp, gb, ge, nullptr, 0.0));
   if (result_host) {
     if (end > start)
       SGMEV_CUDA(cudaMemcpyAsync(result_host + start, tmp + start, sizeof(double) * (end - start),
@@ -937,8 +1137,7 @@ static int system_common(sgmev_op* op, const double* a_dev, const double* a_host
                                  cudaMemcpyHostToDevice, op->stream));
     src = op->out64;
   }
-  convert_pad_kernel<<<vec_blocks(op->npad), 256, 0, op->stream>>>(src, op->n, op->npad, a, nullptr);
-  op->launches += 1;
+  SGMEV_TRY(dev_convert(op, src, op->n, op->npad, a, nullptr, nullptr));
   SGMEV_TRY(dev_system(op, op->precision, a, r, lm));
   if (r_host) {
     if (op->n > 0)
@@ -1050,10 +1249,12 @@ static int fit_common(sgmev_op* op, int mode, const double* y, bool y_on_device,
   using namespace sgmev;
   SGMEV_TRY(check_op(op));
   if ((op->m > 0 && !y) || (op->n > 0 && !alpha)) return fail(SGMEV_ERR_INVALID, "NULL vector");
-  if (mode != SGMEV_SOLVE_PLAIN && mode != SGMEV_SOLVE_MIXED)
-    return fail(SGMEV_ERR_INVALID, "mode must be SGMEV_SOLVE_PLAIN or SGMEV_SOLVE_MIXED");
-  if (mode == SGMEV_SOLVE_MIXED && op->precision != SGMEV_FP64)
-    return fail(SGMEV_ERR_INVALID, "mixed mode needs an op created with SGMEV_FP64");
+  if (mode != SGMEV_SOLVE_PLAIN && mode != SGMEV_SOLVE_MIXED && mode != SGMEV_SOLVE_MIXED_NATIVE64)
+    return fail(SGMEV_ERR_INVALID, "mode must be SGMEV_SOLVE_PLAIN, _MIXED or _MIXED_NATIVE64");
+  // precision of b = B^T y and of the outer residual
+  const int res_prec = mode == SGMEV_SOLVE_MIXED            ? SGMEV_DF64
+                       : mode == SGMEV_SOLVE_MIXED_NATIVE64 ? SGMEV_FP64
+                                                            : op->precision;
   if (!(epsilon > 0.0) || max_iterations < 0) return fail(SGMEV_ERR_INVALID, "bad epsilon/max_iterations");
   const int64_t np = op->npad;
   double* b = op->cg;
@@ -1065,32 +1266,30 @@ static int fit_common(sgmev_op* op, int mode, const double* y, bool y_on_device,
     SGMEV_CUDA(cudaMemcpyAsync(op->out64, y, sizeof(double) * op->m,
                                y_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                op->stream));
-  convert_pad_kernel<<<vec_blocks(op->mpad), 256, 0, op->stream>>>(op->out64, op->m, op->mpad, op->v64, op->v32);
-  op->launches += 1;
-  SGMEV_TRY(dev_multt(op, mode == SGMEV_SOLVE_MIXED ? SGMEV_FP64 : op->precision, op->v64, op->v32,
-                      b, 0, np, nullptr, 0.0));
+  SGMEV_TRY(dev_convert(op, op->out64, op->m, op->mpad, op->v64, op->v32, op->v32lo));
+  SGMEV_TRY(dev_multt(op, res_prec, op->v64, op->v32, op->v32lo, b, 0, np, nullptr, 0.0));
   if (reuse) {
     double* tmp = op->cg + 7 * np;
     if (op->n > 0)
       SGMEV_CUDA(cudaMemcpyAsync(tmp, alpha, sizeof(double) * op->n,
                                  alpha_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                  op->stream));
-    convert_pad_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(tmp, op->n, np, x, nullptr);
-    op->launches += 1;
+    SGMEV_TRY(dev_convert(op, tmp, op->n, np, x, nullptr, nullptr));
   }
   int64_t total_it = 0;
   double res = 0.0;
   if (mode == SGMEV_SOLVE_PLAIN) {
     SGMEV_TRY(cg_core(op, op->precision, b, x, lm, max_iterations, epsilon, reuse != 0, &total_it, &res));
   } else {
-    // iterative refinement: r = b - A64 x (FP64), solve A32 dx = r by CG, x += dx
+    // iterative refinement: r = b - A x with the FP64-accurate operator (df64 or native FP64),
+    // solve A32 dx = r by CG with FP32 kernels and FP64 vectors, x += dx
     double* rr = op->cg + 6 * np;  // outer residual (cg_core uses slots 2..5)
     double* dx = op->cg + 7 * np;
     if (!reuse) SGMEV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * np, op->stream));
     double rnorm2 = 0.0, r0 = 0.0;
     const double eps_inner = 1e-3;
     for (int outer = 0; outer < 64; ++outer) {
-      SGMEV_TRY(dev_system(op, SGMEV_FP64, x, rr, lm));
+      SGMEV_TRY(dev_system(op, res_prec, x, rr, lm));
       sub_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, b, rr, rr);
       op->launches += 1;
       SGMEV_TRY(dev_dot(op, rr, rr, np, &rnorm2));

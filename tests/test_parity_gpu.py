@@ -2,7 +2,8 @@
 (tests/golden, produced by the reference's compiled code) and against the oracle.
 
 Tolerances (max abs error / max abs reference value):
-  FP64 kernels   1e-12   (the reference's STREAMING-vs-DEFAULT agreement is ~1e-14)
+  FP64 kernels   1e-12   (the reference's STREAMING-vs-DEFAULT agreement is ~1e-14), both the
+                 native-FP64 ("double") and the float-float ("df64") kernels
   FP32 kernels   1e-4    (x is rounded to float: |dt| <= 2^l * 2^-24 per dimension)
   fits           1e-9 in alpha for the plain FP64 CG, 1e-6 for the mixed-precision fit
 """
@@ -40,7 +41,8 @@ def _op(grid, x, precision="double"):
 MULTEVAL = [str(c) for c in load_golden("multeval.npz")["cases"]]
 
 
-@pytest.mark.parametrize("precision,tol", [("double", FP64_TOL), ("float", FP32_TOL)])
+@pytest.mark.parametrize("precision,tol", [("double", FP64_TOL), ("df64", FP64_TOL),
+                                           ("float", FP32_TOL)])
 @pytest.mark.parametrize("name", MULTEVAL)
 def test_mult_and_transpose_match_reference(name, precision, tol):
     g = load_golden("multeval.npz")
@@ -56,8 +58,9 @@ def test_mult_and_transpose_match_reference(name, precision, tol):
     assert op.getDuration() > 0.0
 
 
+@pytest.mark.parametrize("precision", ["double", "df64"])
 @pytest.mark.parametrize("name", ["bb_kat", "bb_rand"])
-def test_bounding_box_matches_reference(name):
+def test_bounding_box_matches_reference(name, precision):
     g = load_golden("multeval.npz")
     grid = _grid_from(g, name)
     bb = sg.BoundingBox(grid.getDimension())
@@ -65,7 +68,7 @@ def test_bounding_box_matches_reference(name):
         bb.setBoundary(t, sg.BoundingBox1D(lo, hi))
     grid.getStorage().setBoundingBox(bb)
     x = g[name + "_x"]
-    op = _op(grid, x)
+    op = _op(grid, x, precision)
     out = np.zeros(x.shape[0])
     op.mult(g[name + "_alpha"], out)
     assert rel_err(out, g[name + "_mult_default"]) < FP64_TOL
@@ -104,7 +107,7 @@ def test_results_are_bitwise_reproducible():
     name = "d5_l6_m2000"
     grid = _grid_from(g, name)
     x = g[name + "_x"]
-    for prec in ("double", "float"):
+    for prec in ("double", "df64", "float"):
         op = _op(grid, x, prec)
         a = np.zeros(x.shape[0])
         b = np.zeros(x.shape[0])
@@ -118,14 +121,15 @@ def test_results_are_bitwise_reproducible():
         assert np.array_equal(ta, tb)
 
 
-def test_ranged_variants(oracle):
+@pytest.mark.parametrize("precision", ["double", "df64"])
+def test_ranged_variants(oracle, precision):
     rng = np.random.default_rng(5)
     grid = sg.Grid.createLinearGrid(4)
     grid.getGenerator().regular(5)
     x = rng.random((5000, 4))
     a = rng.standard_normal(grid.getSize())
     v = rng.standard_normal(5000)
-    op = _op(grid, x)
+    op = _op(grid, x, precision)
     full = np.zeros(5000)
     op.mult(a, full)
     fullt = np.zeros(grid.getSize())
@@ -169,7 +173,7 @@ def test_edge_sizes(oracle):
     a = rng.standard_normal(grid.getSize())
     v = rng.standard_normal(333)
     lp, ix = grid.getStorage().getLevelIndexArraysForEval()
-    for prec, tol in (("double", FP64_TOL), ("float", FP32_TOL)):
+    for prec, tol in (("double", FP64_TOL), ("df64", FP64_TOL), ("float", FP32_TOL)):
         op = _op(grid, x, prec)
         out = np.zeros(333)
         op.mult(a, out)
@@ -225,28 +229,32 @@ def test_system_apply_matches_oracle(oracle):
     out = np.zeros(grid.getSize())
     op.systemApply(a, out, lam_m)
     assert rel_err(out, ref) < FP64_TOL
+    opdf = _op(grid, x, "df64")
+    opdf.systemApply(a, out, lam_m)
+    assert rel_err(out, ref) < FP64_TOL
     op32 = _op(grid, x, "float")
     op32.systemApply(a, out, lam_m)
     assert rel_err(out, ref) < FP32_TOL
 
 
+@pytest.mark.parametrize("precision", ["double", "df64"])
 @pytest.mark.parametrize("name", ["d4_l4", "d6_l3"])
-def test_device_cg_fit_matches_reference(name):
+def test_device_cg_fit_matches_reference(name, precision):
     g = load_golden("cgfit.npz")
     grid = _grid_from(g, name)
-    op = _op(grid, g[name + "_x"])
+    op = _op(grid, g[name + "_x"], precision)
     alpha, it, res = op.fit(g[name + "_y"], float(g[name + "_lambda"]), 1000, 1e-12)
     assert rel_err(alpha, g[name + "_alpha"]) < 1e-9
     assert abs(it - int(g[name + "_iterations"])) <= 2
 
 
+@pytest.mark.parametrize("mode", [sg.SGMEV_SOLVE_MIXED, sg.SGMEV_SOLVE_MIXED_NATIVE64])
 @pytest.mark.parametrize("name", ["d4_l4", "d6_l3"])
-def test_mixed_precision_fit_within_1e6(name):
+def test_mixed_precision_fit_within_1e6(name, mode):
     g = load_golden("cgfit.npz")
     grid = _grid_from(g, name)
     op = _op(grid, g[name + "_x"])
-    alpha, it, res = op.fit(g[name + "_y"], float(g[name + "_lambda"]), 5000, 1e-10,
-                            mode=sg.SGMEV_SOLVE_MIXED)
+    alpha, it, res = op.fit(g[name + "_y"], float(g[name + "_lambda"]), 5000, 1e-10, mode=mode)
     assert rel_err(alpha, g[name + "_alpha"]) < 1e-6
 
 
@@ -263,6 +271,28 @@ def test_reference_callers_drive_the_operator_unchanged():
     cg.solve(A, alpha, b, False, False, 0.0)
     assert rel_err(alpha, g[name + "_alpha"]) < 1e-9
     assert abs(cg.getNumberIterations() - int(g[name + "_iterations"])) <= 2
+
+
+def test_df64_matches_native_fp64_at_full_size():
+    """FP64-accurate float-float kernels against the native FP64 kernels at the regression-fit
+    workload size (d=10, level 5, 2^20 points)."""
+    rng = np.random.default_rng(22)
+    grid = sg.Grid.createLinearGrid(10)
+    grid.getGenerator().regular(5)
+    m = 1 << 20
+    x = rng.random((m, 10))
+    a = rng.standard_normal(grid.getSize())
+    v = rng.standard_normal(m)
+    out64, outdf = np.zeros(m), np.zeros(m)
+    op64 = _op(grid, x, "double")
+    opdf = _op(grid, x, "df64")
+    op64.mult(a, out64)
+    opdf.mult(a, outdf)
+    assert rel_err(outdf, out64) < FP64_TOL
+    t64, tdf = np.zeros(grid.getSize()), np.zeros(grid.getSize())
+    op64.multTranspose(v, t64)
+    opdf.multTranspose(v, tdf)
+    assert rel_err(tdf, t64) < FP64_TOL
 
 
 def test_adjoint_and_linearity_at_full_size():
