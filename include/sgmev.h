@@ -76,7 +76,11 @@ SGMEV_API int sgmev_device_count(void);
  * bb_left/bb_right: optional bounding box ([dim] each, both NULL for the unit cube); data are
  * mapped by (x - left) / (right - left) as BoundingBox::transformPointToUnitCube
  * (base/src/sgpp/base/grid/common/BoundingBox.hpp:223-227).
- * precision: SGMEV_FP64 or SGMEV_FP32. params_json: optional tuning knobs (may be NULL).
+ * precision: SGMEV_FP64, SGMEV_FP32 or SGMEV_DF64. params_json: optional flat JSON object of
+ * string knobs (may be NULL): "precond": "none" (default) or "jacobi" — the preconditioner of the
+ * inner correction solves of SGMEV_SOLVE_MIXED* fits (SGMEV_SOLVE_PLAIN is never preconditioned).
+ * Jacobi (diag(B^T B) + lambda*M) doubled the iteration count on clustered (Gaussian-mixture) data,
+ * where fine-level hats see few points, so it is off unless asked for.
  */
 SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double* level_pow2,
                            const double* index, int64_t n_data, const double* data,
@@ -166,8 +170,9 @@ SGMEV_API int sgmev_system_apply_device(sgmev_op* op, const double* d_alpha, dou
  *   SGMEV_SOLVE_PLAIN  — CG with the op's own precision kernels (FP64 op: the plain FP64 path).
  *   SGMEV_SOLVE_MIXED  — iterative refinement: the outer residual b - A alpha (and b) with the
  *                        FP64-accurate df64 kernels, the inner correction solves by CG with
- *                        FP32 kernels and FP64 vectors; stops when ||b - A alpha||^2 <=
- *                        epsilon^2 * ||b - A alpha_0||^2.
+ *                        FP32 kernels and FP64 vectors (Jacobi-preconditioned with
+ *                        diag(B^T B) + lambda*M if params say "precond": "jacobi"); stops when
+ *                        ||b - A alpha||^2 <= epsilon^2 * ||b - A alpha_0||^2 (true residual).
  *   SGMEV_SOLVE_MIXED_NATIVE64 — the same with native FP64 kernels for the residual.
  * Every op stages the FP64, FP32 and df64 copies of its data, so any mode works on any op.
  * y: [n_data] host; alpha: [n_grid] host in/out. iterations: total inner CG iterations;

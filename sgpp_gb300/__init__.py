@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import ctypes
 import enum
+import json
 import os
 from typing import Optional
 
@@ -367,7 +368,8 @@ class OperationMultipleEvalMPIType(enum.IntEnum):
 class OperationMultipleEvalConfiguration:
     """Operator selection plus a parameters tree. Parameters understood by the CUDA operator:
     ``precision``: "double" (default, native FP64), "df64" (FP64-accurate float-float on the
-    FP32 pipes) or "float"."""
+    FP32 pipes) or "float"; ``precond``: "none" (default) or "jacobi" for the inner solves of
+    mixed-precision fits."""
 
     def __init__(self, type=OperationMultipleEvalType.DEFAULT,
                  subType=OperationMultipleEvalSubType.DEFAULT,
@@ -418,7 +420,8 @@ def _precision_of(params: dict) -> int:
 class OperationMultiEvalCuda:
     """B / B^T on the GPU for a Linear grid (OperationMultipleEval interface)."""
 
-    def __init__(self, grid: Grid, dataset, precision: int = SGMEV_FP64):
+    def __init__(self, grid: Grid, dataset, precision: int = SGMEV_FP64,
+                 params: Optional[dict] = None):
         self.grid = grid
         self.dataset = _as_matrix(dataset)
         self.precision = precision
@@ -432,9 +435,11 @@ class OperationMultiEvalCuda:
         if not bb.isUnitCube():
             left, right = bb.arrays()
         h = ctypes.c_void_p(None)
+        knobs = {k: str(v) for k, v in (params or {}).items() if k in ("precond",)}
+        pj = json.dumps(knobs).encode() if knobs else None
         _check(L.sgmev_create(ctypes.byref(h), st.getDimension(), st.getSize(), _vp(lp), _vp(ix),
                               self.dataset.shape[0], _vp(self.dataset), _vp(left), _vp(right),
-                              precision, None))
+                              precision, pj))
         self._h = h
         self._n = st.getSize()
         self._m = self.dataset.shape[0]
@@ -587,7 +592,8 @@ def createOperationMultipleEval(grid: Grid, dataset,
     if (configuration.getType() == OperationMultipleEvalType.STREAMING
             and configuration.getSubType() == OperationMultipleEvalSubType.CUDA
             and configuration.getMPIType() == OperationMultipleEvalMPIType.NONE):
-        return OperationMultiEvalCuda(grid, dataset, _precision_of(configuration.getParameters()))
+        return OperationMultiEvalCuda(grid, dataset, _precision_of(configuration.getParameters()),
+                                      configuration.getParameters())
     raise FactoryException("OperationMultipleEval is not implemented for this combination of "
                            "type, subtype and MPI type in this build.")
 

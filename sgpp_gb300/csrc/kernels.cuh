@@ -42,6 +42,15 @@ __device__ __forceinline__ float hat_first(float x, float2 li) {
 __device__ __forceinline__ float hat_next(float p, float x, float2 li) {
   return p * __saturatef(1.0f - fabsf(fmaf(x, li.x, -li.y)));
 }
+// squared hats (diagonal of B^T B): p = prod_t hat_t^2
+__device__ __forceinline__ float hat_first_sq(float x, float2 li) {
+  const float h = hat_first(x, li);
+  return h * h;
+}
+__device__ __forceinline__ float hat_next_sq(float p, float x, float2 li) {
+  const float h = __saturatef(1.0f - fabsf(fmaf(x, li.x, -li.y)));
+  return p * (h * h);
+}
 __device__ __forceinline__ double hat_first(double x, double2 li) {
   return fmax(1.0 - fabs(fma(x, li.x, -li.y)), 0.0);
 }
@@ -112,7 +121,7 @@ __global__ void __launch_bounds__(BLOCK) mult_kernel(const T* __restrict__ xt, i
 // multT: part[split][g] = sum_{j in chunk(split)} v_j prod_t hat(x_jt; l_gt, i_gt)
 // grid: (grid tiles of BLOCK*RG points) x (data chunks). chunk_len is a multiple of DT.
 // ---------------------------------------------------------------------------------------
-template <typename T, int DIM, int RG, int BLOCK, int DT>
+template <typename T, int DIM, int RG, int BLOCK, int DT, bool SQ = false>
 __global__ void __launch_bounds__(BLOCK) mult_transpose_kernel(
     const T* __restrict__ xt, const T* __restrict__ v, int64_t mpad,
     const typename Pair<T>::type* __restrict__ li, int64_t npad, int64_t chunk_len,
@@ -152,12 +161,18 @@ __global__ void __launch_bounds__(BLOCK) mult_transpose_kernel(
       T p[RG];
       const T x0 = s_x[j];
 #pragma unroll
-      for (int k = 0; k < RG; ++k) p[k] = hat_first(x0, l[k][0]);
+      for (int k = 0; k < RG; ++k) {
+        if constexpr (SQ) p[k] = hat_first_sq(x0, l[k][0]);
+        else p[k] = hat_first(x0, l[k][0]);
+      }
 #pragma unroll
       for (int t = 1; t < DIM; ++t) {
         const T xv = s_x[t * DT + j];
 #pragma unroll
-        for (int k = 0; k < RG; ++k) p[k] = hat_next(p[k], xv, l[k][t]);
+        for (int k = 0; k < RG; ++k) {
+          if constexpr (SQ) p[k] = hat_next_sq(p[k], xv, l[k][t]);
+          else p[k] = hat_next(p[k], xv, l[k][t]);
+        }
       }
       const T vj = s_v[j];
 #pragma unroll
@@ -192,7 +207,7 @@ __global__ void mult_generic_kernel(const T* __restrict__ xt, int64_t mpad, int 
   part[static_cast<int64_t>(blockIdx.y) * mpad + j] = acc;
 }
 
-template <typename T>
+template <typename T, bool SQ = false>
 __global__ void mult_transpose_generic_kernel(const T* __restrict__ xt, const T* __restrict__ v,
                                               int64_t mpad, int dim,
                                               const typename Pair<T>::type* __restrict__ li,
@@ -206,7 +221,11 @@ __global__ void mult_transpose_generic_kernel(const T* __restrict__ xt, const T*
   T acc = T(0);
   for (int64_t j = j_begin; j < j_end; ++j) {
     T p = hat_first(xt[j], li[g * dim]);
-    for (int t = 1; t < dim; ++t) p = hat_next(p, xt[static_cast<int64_t>(t) * mpad + j], li[g * dim + t]);
+    if (SQ) p = p * p;
+    for (int t = 1; t < dim; ++t) {
+      const T h = hat_first(xt[static_cast<int64_t>(t) * mpad + j], li[g * dim + t]);
+      p = p * (SQ ? h * h : h);
+    }
     acc = fma(v[j], p, acc);
   }
   part[static_cast<int64_t>(blockIdx.y) * npad + g] = acc;

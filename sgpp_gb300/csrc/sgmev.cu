@@ -55,6 +55,7 @@ constexpr int kMaxTemplDim = 16;
 constexpr int kReduceBlocks = 1216;  // 8 x 152 SMs
 constexpr int kDotBlocks = 304;
 constexpr int kDotThreads = 256;
+constexpr int kCgSlots = 10;
 
 static inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
@@ -114,7 +115,9 @@ struct sgmev_op {
   int64_t part_elems = 0;  // capacity of `part` in doubles
 
   // CG vectors (FP64, npad each)
-  double* cg = nullptr;  // 8 vectors: b, alpha, r, d, q, t, delta, spare
+  double* cg = nullptr;  // kCgSlots vectors: b, x, r, d, q, t, outer residual, dx, z, 1/diag
+  bool pc_valid = false;  // 1/diag(B^T B + lm I) in slot 9 is current
+  double pc_lm = 0.0;
   double* dot_part = nullptr;
   double* dot_out = nullptr;
   double* host_scalar = nullptr;  // pinned
@@ -124,6 +127,7 @@ struct sgmev_op {
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
   double last_seconds = -1.0;
   int64_t launches = 0;
+  bool precond = false;  // Jacobi-preconditioned inner CG in the mixed fits (params "precond")
 
   std::vector<double> bb_left, bb_width;
 
@@ -327,6 +331,31 @@ __global__ void xpby_kernel(int64_t n, const double* __restrict__ r, double beta
   for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x)
     d[i] = fma(beta, d[i], r[i]);
+}
+
+// z = a * b (elementwise)
+__global__ void mul_kernel(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                           double* __restrict__ z) {
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    z[i] = a[i] * b[i];
+}
+
+// inv[i] = 1 / (diag[i] + lm) for i < n, 0 in the padding
+__global__ void inv_diag_kernel(int64_t n, int64_t npad, const double* __restrict__ diag,
+                                double lm, double* __restrict__ inv) {
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < npad;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const double dv = diag[i] + lm;
+    inv[i] = (i < n && dv > 0.0) ? 1.0 / dv : 0.0;
+  }
+}
+
+// v[j] = 1 for j < m, 0 in the padding (FP32)
+__global__ void ones_kernel(int64_t m, int64_t mpad, float* __restrict__ v) {
+  for (int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; j < mpad;
+       j += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    v[j] = j < m ? 1.0f : 0.0f;
 }
 
 // z = x - y
@@ -747,11 +776,12 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
     SGMEV_TRY(dalloc(&op->a64, static_cast<size_t>(npad)));
     SGMEV_TRY(dalloc(&op->a32, static_cast<size_t>(npad)));
     SGMEV_TRY(dalloc(&op->a32lo, static_cast<size_t>(npad)));
-    SGMEV_TRY(dalloc(&op->cg, static_cast<size_t>(npad) * 8));
+    SGMEV_TRY(dalloc(&op->cg, static_cast<size_t>(npad) * kCgSlots));
     op->npad_cap = npad;
   }
   op->n = n;
   op->npad = npad;
+  op->pc_valid = false;
   double* d_l = nullptr;
   double* d_i = nullptr;
   const size_t bytes = sizeof(double) * static_cast<size_t>(std::max<int64_t>(n * op->dim, 1));
@@ -817,6 +847,23 @@ static int end_timed(sgmev_op* op, bool sync) {
   return SGMEV_OK;
 }
 
+// Value of a string entry "key": "value" in a flat JSON object (the operator's parameters);
+// empty if absent. Only what the parameters here need: no nesting, no escapes.
+static std::string json_string(const char* json, const char* key) {
+  if (!json) return "";
+  const std::string s(json);
+  const std::string k = std::string("\"") + key + "\"";
+  size_t p = s.find(k);
+  if (p == std::string::npos) return "";
+  p = s.find(':', p + k.size());
+  if (p == std::string::npos) return "";
+  p = s.find('"', p + 1);
+  if (p == std::string::npos) return "";
+  const size_t e = s.find('"', p + 1);
+  if (e == std::string::npos) return "";
+  return s.substr(p + 1, e - p - 1);
+}
+
 static int check_op(const sgmev_op* op) {
   if (!op) return fail(SGMEV_ERR_INVALID, "op is NULL");
   return SGMEV_OK;
@@ -878,7 +925,9 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
       if (!(bb_right[t] > bb_left[t]))
         return fail(SGMEV_ERR_INVALID, "bounding box interval " + std::to_string(t) + " is empty");
   }
-  (void)params_json;
+  const std::string precond = json_string(params_json, "precond");
+  if (!precond.empty() && precond != "jacobi" && precond != "none")
+    return fail(SGMEV_ERR_INVALID, "params: precond must be \"jacobi\" or \"none\"");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
@@ -890,6 +939,7 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   op->precision = precision;
   op->m = n_data;
   op->mpad = std::max<int64_t>(round_up(std::max<int64_t>(n_data, 1), kMPadTo), kMPadTo);
+  op->precond = precond == "jacobi";
   auto bail = [&](int rc) {
     release(op);
     delete op;
@@ -1225,6 +1275,93 @@ static int cg_core(sgmev_op* op, int prec, const double* rhs, double* x, double 
   return SGMEV_OK;
 }
 
+// 1/diag(B^T B + lm I) into CG slot 9 (Jacobi preconditioner), from one FP32 squared-hat
+// multTranspose with v = 1: diag_i = sum_j prod_t hat_t(x_j)^2. Cached until the grid or lm changes.
+static int dev_precond(sgmev_op* op, double lm) {
+  using namespace sgmev;
+  const int64_t np = op->npad;
+  double* inv = op->cg + 9 * np;
+  if (op->pc_valid && op->pc_lm == lm) return SGMEV_OK;
+  ones_kernel<<<vec_blocks(op->mpad), 256, 0, op->stream>>>(op->m, op->mpad, op->v32);
+  op->launches += 1;
+  Plan p;
+  float* part = static_cast<float*>(op->part);
+  if (op->dim <= kMaxTemplDim) {
+    const int64_t tiles = np / (kBlock * Blocking<float>::multt_r(op->dim));
+    p = plan_multt<float>(op, tiles);
+    dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+    switch (op->dim) {
+#define F(D)                                                                                     \
+  case D:                                                                                        \
+    mult_transpose_kernel<float, D, Blocking<float>::multt_r(D), kBlock, kDT, true>              \
+        <<<grid, kBlock, 0, op->stream>>>(op->xt32, op->v32, op->mpad, op->li32, np, p.chunk, 0, \
+                                          part);                                                 \
+    break;
+      SGMEV_DIM_CASES(F)
+#undef F
+      default:
+        break;
+    }
+  } else {
+    p = plan_multt<float>(op, ceil_div(np, kBlock));
+    dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+    mult_transpose_generic_kernel<float, true><<<grid, kBlock, 0, op->stream>>>(
+        op->xt32, op->v32, op->mpad, op->dim, op->li32, np, p.chunk, 0, np, part);
+  }
+  op->launches += 1;
+  SGMEV_CUDA(cudaGetLastError());
+  double* diag = op->cg + 8 * np;
+  SGMEV_TRY((run_reduce<float, double>(op, (int)p.nsplit, np, 0, op->n, np, diag, nullptr, 0.0)));
+  inv_diag_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(op->n, np, diag, lm, inv);
+  op->launches += 1;
+  SGMEV_CUDA(cudaGetLastError());
+  op->pc_valid = true;
+  op->pc_lm = lm;
+  return SGMEV_OK;
+}
+
+// Jacobi-preconditioned CG from x = 0 on (B^T B + lm I) x = rhs with operator precision `prec`
+// (the inner correction solve of the mixed fit). Stops when the preconditioned residual norm
+// r.z falls below eps^2 times its start value, or after imax iterations.
+static int pcg_core(sgmev_op* op, int prec, const double* rhs, double* x, double lm,
+                    int64_t imax, double eps, int64_t* iters) {
+  using namespace sgmev;
+  const int64_t np = op->npad;
+  double* r = op->cg + 2 * np;
+  double* d = op->cg + 3 * np;
+  double* q = op->cg + 4 * np;
+  double* z = op->cg + 8 * np;
+  const double* inv = op->cg + 9 * np;
+  SGMEV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * np, op->stream));
+  SGMEV_CUDA(cudaMemcpyAsync(r, rhs, sizeof(double) * np, cudaMemcpyDeviceToDevice, op->stream));
+  mul_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, inv, r, z);
+  op->launches += 1;
+  SGMEV_CUDA(cudaMemcpyAsync(d, z, sizeof(double) * np, cudaMemcpyDeviceToDevice, op->stream));
+  double delta_new = 0.0;
+  SGMEV_TRY(dev_dot(op, r, z, np, &delta_new));
+  const double delta_0 = delta_new * eps * eps;
+  int64_t it = 0;
+  while (it < imax && delta_new > delta_0 && delta_new > 0.0) {
+    SGMEV_TRY(dev_system(op, prec, d, q, lm));
+    double dq = 0.0;
+    SGMEV_TRY(dev_dot(op, d, q, np, &dq));
+    if (dq == 0.0) break;
+    const double a = delta_new / dq;
+    SGMEV_TRY(dev_axpy(op, np, a, d, x));
+    SGMEV_TRY(dev_axpy(op, np, -a, q, r));
+    mul_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, inv, r, z);
+    op->launches += 1;
+    const double delta_old = delta_new;
+    SGMEV_TRY(dev_dot(op, r, z, np, &delta_new));
+    xpby_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, z, delta_new / delta_old, d);
+    op->launches += 1;
+    ++it;
+  }
+  SGMEV_CUDA(cudaGetLastError());
+  *iters = it;
+  return SGMEV_OK;
+}
+
 static int fit_common(sgmev_op* op, int mode, const double* y, bool y_on_device, double lambda,
                       int64_t max_iterations, double epsilon, int reuse, double* alpha,
                       bool alpha_on_device, int64_t* iterations, double* residual);
@@ -1288,6 +1425,7 @@ static int fit_common(sgmev_op* op, int mode, const double* y, bool y_on_device,
     if (!reuse) SGMEV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * np, op->stream));
     double rnorm2 = 0.0, r0 = 0.0;
     const double eps_inner = 1e-3;
+    if (op->precond) SGMEV_TRY(dev_precond(op, lm));
     for (int outer = 0; outer < 64; ++outer) {
       SGMEV_TRY(dev_system(op, res_prec, x, rr, lm));
       sub_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, b, rr, rr);
@@ -1299,7 +1437,13 @@ static int fit_common(sgmev_op* op, int mode, const double* y, bool y_on_device,
       int64_t it = 0;
       double dres = 0.0;
       const double want = std::max(eps_inner, epsilon * std::sqrt(r0 / rnorm2) * 0.5);
-      SGMEV_TRY(cg_core(op, SGMEV_FP32, rr, dx, lm, max_iterations - total_it, std::min(want, 0.5), false, &it, &dres));
+      if (op->precond) {
+        SGMEV_TRY(pcg_core(op, SGMEV_FP32, rr, dx, lm, max_iterations - total_it,
+                           std::min(want, 0.5), &it));
+      } else {
+        SGMEV_TRY(cg_core(op, SGMEV_FP32, rr, dx, lm, max_iterations - total_it,
+                          std::min(want, 0.5), false, &it, &dres));
+      }
       total_it += it;
       SGMEV_TRY(dev_axpy(op, np, 1.0, dx, x));
     }

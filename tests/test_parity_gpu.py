@@ -248,14 +248,36 @@ def test_device_cg_fit_matches_reference(name, precision):
     assert abs(it - int(g[name + "_iterations"])) <= 2
 
 
+@pytest.mark.parametrize("precond", ["jacobi", "none"])
 @pytest.mark.parametrize("mode", [sg.SGMEV_SOLVE_MIXED, sg.SGMEV_SOLVE_MIXED_NATIVE64])
 @pytest.mark.parametrize("name", ["d4_l4", "d6_l3"])
-def test_mixed_precision_fit_within_1e6(name, mode):
+def test_mixed_precision_fit_within_1e6(name, mode, precond):
     g = load_golden("cgfit.npz")
     grid = _grid_from(g, name)
-    op = _op(grid, g[name + "_x"])
+    cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                sg.OperationMultipleEvalSubType.CUDA,
+                                                parameters={"precond": precond})
+    op = sg.createOperationMultipleEval(grid, g[name + "_x"], cfg)
     alpha, it, res = op.fit(g[name + "_y"], float(g[name + "_lambda"]), 5000, 1e-10, mode=mode)
     assert rel_err(alpha, g[name + "_alpha"]) < 1e-6
+
+
+def test_mixed_fit_after_refinement_uses_fresh_preconditioner(oracle):
+    """prepare() after refinement invalidates the cached diagonal: the next mixed fit must still
+    reach the FP64 solution (checked against the oracle's FP64 CG)."""
+    rng = np.random.default_rng(31)
+    grid = sg.Grid.createLinearGrid(4)
+    grid.getGenerator().regular(3)
+    x = rng.random((3000, 4))
+    y = np.sin(4 * x[:, 0]) * x[:, 1] + x[:, 2] ** 2
+    op = _op(grid, x)
+    a0, _, _ = op.fit(y, 1e-3, 5000, 1e-10, mode=sg.SGMEV_SOLVE_MIXED)
+    grid.getGenerator().refine(sg.SurplusRefinementFunctor(a0, 10))
+    op.prepare()
+    a1, _, _ = op.fit(y, 1e-3, 5000, 1e-10, mode=sg.SGMEV_SOLVE_MIXED)
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    ref, _, _ = oracle.stream(x).cg_fit(lp, ix, y, 1e-3, 5000, 1e-12)
+    assert rel_err(a1, ref) < 1e-6
 
 
 def test_reference_callers_drive_the_operator_unchanged():
