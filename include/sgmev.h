@@ -206,6 +206,49 @@ SGMEV_API int sgmev_synchronize(sgmev_op* op);
 /* Number of kernels this op launched so far (instrumentation for benchmarks). */
 SGMEV_API int64_t sgmev_kernel_launches(const sgmev_op* op);
 
+/* ---- batched fits: many independent problems, continuous batching ----------------------- */
+/*
+ * A batch engine fits many independent regression problems of uneven dimension, grid size and
+ * data size at once: every problem runs the mixed-precision fit of sgmev_fit (SGMEV_SOLVE_MIXED:
+ * FP32 CG inside, df64 residual outside) as a state machine on the device, and one step advances
+ * every unfinished problem by one inner CG iteration or one outer residual, with one launch per
+ * phase for all problems (persistent CTAs pulling per-problem tiles from a device work list) and
+ * the step's launches captured into one CUDA graph. Problems can be added while others run
+ * (continuous batching); each result is the same alone and in any mix. Each problem carries
+ * `rhs` right-hand sides (1 or 16) that share its operator B.
+ * Replaces, per problem, SystemMatrixLeastSquaresIdentity::generateb + ConjugateGradients::solve
+ * (datadriven/.../SystemMatrixLeastSquaresIdentity.cpp:49-56, solver/.../ConjugateGradients.cpp:22-151)
+ * run for many problems; the reference has no batched counterpart.
+ *   grid_capacity: total grid rows x dim over all resident problems (padded to 512 rows each);
+ *   data_capacity: total data points x dim (padded to 1024 points each).
+ */
+typedef struct sgmev_batch sgmev_batch;
+SGMEV_API int sgmev_batch_create(sgmev_batch** out, int max_slots, int rhs, int64_t grid_capacity,
+                                 int64_t data_capacity, const char* params_json);
+SGMEV_API int sgmev_batch_destroy(sgmev_batch* b);
+/* Pool elements one problem occupies (admission by device-memory footprint). */
+SGMEV_API int sgmev_batch_footprint(int dim, int64_t n_grid, int64_t n_data, int rhs,
+                                    int64_t* grid_elems, int64_t* data_elems);
+/* Stage one problem (host buffers: eval arrays [n_grid x dim], data [n_data x dim],
+ * y [n_data x rhs] row-major) and compute b = B^T y; returns its slot. SGMEV_ERR_OOM when no slot
+ * or pool space is free (the caller retries after sgmev_batch_remove). */
+SGMEV_API int sgmev_batch_add(sgmev_batch* b, int dim, int64_t n_grid, const double* level_pow2,
+                              const double* index, int64_t n_data, const double* data,
+                              const double* y, double lambda, double epsilon,
+                              int64_t max_iterations, int* slot_out);
+SGMEV_API int sgmev_batch_remove(sgmev_batch* b, int slot);
+/* Advance all unfinished problems by `steps` steps; phases[max_slots] receives each slot's phase
+ * (0 empty, 1 outer residual pending, 2 inner CG, 3 done). */
+SGMEV_API int sgmev_batch_step(sgmev_batch* b, int steps, int* phases);
+/* Step until no problem is running (or max_steps); *steps_taken = steps run. */
+SGMEV_API int sgmev_batch_solve(sgmev_batch* b, int64_t max_steps, int64_t* steps_taken);
+/* alpha [n_grid x rhs] row-major; iterations = inner CG iterations; residual = worst column's
+ * ||b - A alpha||^2 / ||b||^2 at the last outer step; phase as above. */
+SGMEV_API int sgmev_batch_result(sgmev_batch* b, int slot, double* alpha, int64_t* iterations,
+                                 double* residual, int* phase);
+SGMEV_API int sgmev_batch_info(sgmev_batch* b, int64_t* steps, int64_t* launches,
+                               int* free_slots);
+
 /* ---- sparse-grid construction on the host (native C++) --------------------------------- */
 /*
  * Regular Linear sparse grid without boundary in the reference's storage order; replaces

@@ -61,6 +61,9 @@ EXPORTED_SYMBOLS = (
     "sgmev_set_stream", "sgmev_synchronize", "sgmev_kernel_launches", "sggrid_regular",
     "sggrid_refine_surplus", "sggrid_level_index_for_eval", "sgmev_fma_peak", "sgmev_profile",
     "sgmev_profile_read", "sgmev_fit_device", "sgmev_mult_transpose_noalloc",
+    "sgmev_batch_create", "sgmev_batch_destroy", "sgmev_batch_footprint", "sgmev_batch_add",
+    "sgmev_batch_remove", "sgmev_batch_step", "sgmev_batch_solve", "sgmev_batch_result",
+    "sgmev_batch_info",
 )
 
 SGMEV_KERNEL_MULT_FP32 = 0
@@ -139,6 +142,16 @@ def load_library(path: str = LIBRARY_PATH):
         "sgmev_fma_peak": (c_int, [c_int, pdbl, ctypes.POINTER(c_int)]),
         "sgmev_fit_device": (c_int, [vp, c_int, vp, dbl, i64, dbl, c_int, vp, pi64, pdbl]),
         "sgmev_mult_transpose_noalloc": (c_int, [c_int, i64, vp, vp, i64, vp, vp, vp, vp]),
+        "sgmev_batch_create": (c_int, [ctypes.POINTER(vp), c_int, c_int, i64, i64, ctypes.c_char_p]),
+        "sgmev_batch_destroy": (c_int, [vp]),
+        "sgmev_batch_footprint": (c_int, [c_int, i64, i64, c_int, pi64, pi64]),
+        "sgmev_batch_add": (c_int, [vp, c_int, i64, vp, vp, i64, vp, vp, dbl, dbl, i64,
+                                    ctypes.POINTER(c_int)]),
+        "sgmev_batch_remove": (c_int, [vp, c_int]),
+        "sgmev_batch_step": (c_int, [vp, c_int, vp]),
+        "sgmev_batch_solve": (c_int, [vp, i64, pi64]),
+        "sgmev_batch_result": (c_int, [vp, c_int, vp, pi64, pdbl, ctypes.POINTER(c_int)]),
+        "sgmev_batch_info": (c_int, [vp, pi64, pi64, ctypes.POINTER(c_int)]),
         "sgmev_profile": (c_int, [vp, c_int]),
         "sgmev_profile_read": (c_int, [vp, c_int, pi64, pdbl]),
     }
@@ -577,6 +590,102 @@ class OperationMultiEvalCuda:
         return alpha_out, int(it.value), float(res.value)
 
 
+class BatchEngine:
+    """Many independent regression fits advanced together on the GPU (sgmev_batch_*).
+
+    Every problem is a (grid, data X [M x d], Y [M x rhs], lambda) fit; add() stages it and
+    computes b = B^T Y, step()/solve() advance all unfinished problems (continuous batching:
+    problems may be added while others run), result() returns alpha [N x rhs]."""
+
+    PHASE_EMPTY, PHASE_OUTER, PHASE_INNER, PHASE_DONE = 0, 1, 2, 3
+
+    def __init__(self, max_slots: int, rhs: int = 1, grid_capacity: int = 1 << 24,
+                 data_capacity: int = 1 << 26):
+        L = load_library()
+        h = ctypes.c_void_p(None)
+        _check(L.sgmev_batch_create(ctypes.byref(h), int(max_slots), int(rhs), int(grid_capacity),
+                                    int(data_capacity), None))
+        self._h = h
+        self.max_slots = int(max_slots)
+        self.rhs = int(rhs)
+        self.sizes = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load_library().sgmev_batch_destroy(self._h)
+            self._h = ctypes.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def footprint(dim: int, n_grid: int, n_data: int, rhs: int = 1):
+        g = ctypes.c_int64(0)
+        d = ctypes.c_int64(0)
+        _check(load_library().sgmev_batch_footprint(int(dim), int(n_grid), int(n_data), int(rhs),
+                                                    ctypes.byref(g), ctypes.byref(d)))
+        return int(g.value), int(d.value)
+
+    def add(self, grid: Grid, X, Y, lam: float, epsilon: float = 1e-8,
+            max_iterations: int = 100000) -> int:
+        st = grid.getStorage()
+        lp, ix = st.getLevelIndexArraysForEval()
+        X = _as_matrix(X)
+        Y = np.ascontiguousarray(np.asarray(Y, np.float64).reshape(X.shape[0], self.rhs))
+        slot = ctypes.c_int(-1)
+        _check(load_library().sgmev_batch_add(self._h, st.getDimension(), st.getSize(), _vp(lp),
+                                              _vp(ix), X.shape[0], _vp(X), _vp(Y), float(lam),
+                                              float(epsilon), int(max_iterations),
+                                              ctypes.byref(slot)))
+        self.sizes[slot.value] = st.getSize()
+        return int(slot.value)
+
+    def tryAdd(self, grid: Grid, X, Y, lam: float, epsilon: float = 1e-8,
+               max_iterations: int = 100000):
+        """add() that returns None instead of raising when no slot or pool space is free."""
+        try:
+            return self.add(grid, X, Y, lam, epsilon, max_iterations)
+        except OperationException as e:
+            if f"error {SGMEV_ERR_OOM}" in str(e):
+                return None
+            raise
+
+    def remove(self, slot: int) -> None:
+        _check(load_library().sgmev_batch_remove(self._h, int(slot)))
+        self.sizes.pop(slot, None)
+
+    def step(self, steps: int = 1) -> np.ndarray:
+        ph = np.zeros(self.max_slots, np.int32)
+        _check(load_library().sgmev_batch_step(self._h, int(steps), _vp(ph)))
+        return ph
+
+    def solve(self, max_steps: int = 1000000) -> int:
+        n = ctypes.c_int64(0)
+        _check(load_library().sgmev_batch_solve(self._h, int(max_steps), ctypes.byref(n)))
+        return int(n.value)
+
+    def result(self, slot: int):
+        n = self.sizes[slot]
+        a = np.zeros((n, self.rhs))
+        it = ctypes.c_int64(0)
+        res = ctypes.c_double(0.0)
+        ph = ctypes.c_int(0)
+        _check(load_library().sgmev_batch_result(self._h, int(slot), _vp(a), ctypes.byref(it),
+                                                 ctypes.byref(res), ctypes.byref(ph)))
+        return a, int(it.value), float(res.value), int(ph.value)
+
+    def info(self):
+        s = ctypes.c_int64(0)
+        l = ctypes.c_int64(0)
+        f = ctypes.c_int(0)
+        _check(load_library().sgmev_batch_info(self._h, ctypes.byref(s), ctypes.byref(l),
+                                               ctypes.byref(f)))
+        return {"steps": int(s.value), "launches": int(l.value), "free_slots": int(f.value)}
+
+
 def createOperationMultipleEval(grid: Grid, dataset,
                                 configuration: Optional[OperationMultipleEvalConfiguration] = None):
     """op_factory::createOperationMultipleEval with the new CUDA branch for Linear grids.
@@ -708,7 +817,7 @@ __all__ = [
     "SurplusRefinementFunctor", "OperationMultipleEvalType", "OperationMultipleEvalSubType",
     "OperationMultipleEvalMPIType", "OperationMultipleEvalConfiguration",
     "createOperationMultipleEval", "OperationMultiEvalCuda", "SystemMatrixLeastSquaresIdentity",
-    "ConjugateGradients", "OperationException", "FactoryException", "NotImplementedException",
+    "ConjugateGradients", "BatchEngine", "OperationException", "FactoryException", "NotImplementedException",
     "GenerationException", "load_library", "device_count", "EXPORTED_SYMBOLS", "SGMEV_FP64",
     "SGMEV_FP32", "SGMEV_DF64", "SGMEV_SOLVE_PLAIN", "SGMEV_SOLVE_MIXED",
     "SGMEV_SOLVE_MIXED_NATIVE64",
