@@ -322,6 +322,14 @@ class Grid:
         return Grid(int(dim))
 
     @staticmethod
+    def regularSize(dim: int, level: int) -> int:
+        """Number of points of the regular Linear grid of this dimension and level."""
+        n = ctypes.c_int64(0)
+        _check(load_library().sggrid_regular(int(dim), int(level), ctypes.byref(n), None, None),
+               GenerationException)
+        return int(n.value)
+
+    @staticmethod
     def fromArrays(level, index) -> "Grid":
         """A grid from raw [N x d] level / index rows (e.g. exported from an SG++ storage)."""
         level = np.ascontiguousarray(level, np.int32)

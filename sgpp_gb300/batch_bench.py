@@ -1,0 +1,108 @@
+"""Batched multi-problem, multi-right-hand-side fits: solves/s of the batch engine against
+sequential per-problem fits.
+
+    python -m sgpp_gb300.batch_bench --problems 96 --rhs 16 --max-work 2e9
+
+Problems follow the batched-fit size mix (d uniform in 2..12, level in 3..7, data size
+log-uniform in [1e3, 2^20], uniform data, Y ~ N(0,1) with `rhs` columns), truncated to
+N*M*d <= --max-work so that the run ends in minutes with the dense kernels. One "solve" is one
+right-hand side of one problem fitted to the relative FP64 residual --epsilon.
+
+Reported: batched solves/s (all problems resident, one engine), the error of a subset's alpha
+against FP64 solutions (single-problem df64-refined fits to 1e-12), and sequential solves/s of
+the plain FP64 CUDA path (native FP64 kernels, CG per right-hand side) and of the single-problem
+mixed path, both timed on the first --sequential problems (one right-hand side each).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import sgpp_gb300 as sg  # noqa: E402
+from sgpp_gb300.serving import MixGenerator  # noqa: E402
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--problems", type=int, default=96)
+    ap.add_argument("--rhs", type=int, default=16)
+    ap.add_argument("--max-work", type=float, default=2e9)
+    ap.add_argument("--epsilon", type=float, default=1e-8)
+    ap.add_argument("--lam", type=float, default=1e-4)
+    ap.add_argument("--check", type=int, default=4, help="problems checked against FP64 fits")
+    ap.add_argument("--sequential", type=int, default=4, help="problems timed sequentially")
+    ap.add_argument("--seed", type=int, default=11)
+    args = ap.parse_args()
+
+    gen = MixGenerator(args.seed, args.max_work, pool=4)
+    probs = [gen.draw(args.rhs) for _ in range(args.problems)]
+    grid_elems = sum(sg.BatchEngine.footprint(g.getDimension(), g.getSize(), X.shape[0], args.rhs)[0]
+                     for g, X, _ in probs)
+    data_elems = sum(sg.BatchEngine.footprint(g.getDimension(), g.getSize(), X.shape[0], args.rhs)[1]
+                     for g, X, _ in probs)
+    eng = sg.BatchEngine(max_slots=args.problems, rhs=args.rhs, grid_capacity=grid_elems + 4096,
+                         data_capacity=data_elems + 4096)
+    slots = [eng.add(g, X, Y, args.lam, args.epsilon) for g, X, Y in probs]
+    # the first step captures the graph; time from there on
+    eng.step(1)
+    t0 = time.perf_counter()
+    steps = eng.solve()
+    t_batch = time.perf_counter() - t0
+    solves = args.problems * args.rhs
+    iters = [eng.result(s)[1] for s in slots]
+
+    errs = []
+    for k in range(min(args.check, args.problems)):
+        g, X, Y = probs[k]
+        alpha = eng.result(slots[k])[0]
+        op = sg.createOperationMultipleEval(g, X)
+        for c in range(args.rhs):
+            ref, _, _ = op.fit(Y[:, c], args.lam, 100000, 1e-12, mode=sg.SGMEV_SOLVE_MIXED)
+            errs.append(float(np.abs(alpha[:, c] - ref).max() / np.abs(ref).max()))
+        op.close()
+    eng.close()
+
+    seq_plain, seq_mixed = [], []
+    for k in range(min(args.sequential, args.problems)):
+        g, X, Y = probs[k]
+        op = sg.createOperationMultipleEval(g, X)
+        t1 = time.perf_counter()
+        op.fit(Y[:, 0], args.lam, 100000, args.epsilon, mode=sg.SGMEV_SOLVE_PLAIN)
+        seq_plain.append(time.perf_counter() - t1)
+        t1 = time.perf_counter()
+        op.fit(Y[:, 0], args.lam, 100000, args.epsilon, mode=sg.SGMEV_SOLVE_MIXED)
+        seq_mixed.append(time.perf_counter() - t1)
+        op.close()
+    # the sequential subset's share of the batch work, to put both on the same footing
+    work = np.array([g.getSize() * X.shape[0] * g.getDimension() for g, X, _ in probs], float)
+    share = work[: len(seq_plain)].sum() / work.sum()
+    line = {
+        "metric": "batched_solves_per_sec", "value": solves / t_batch, "unit": "solves/s",
+        "problems": args.problems, "rhs": args.rhs, "steps": steps, "seconds": t_batch,
+        "inner_iterations": {"min": int(min(iters)), "max": int(max(iters))},
+        "alpha_rel_err_vs_fp64": {"max": max(errs) if errs else None, "checked_solves": len(errs)},
+        # all problems x all right-hand sides sequentially: sum(subset times) / share per column
+        "sequential_plain_fp64_solves_per_sec_est": (
+            args.problems * share / sum(seq_plain) if seq_plain else None),
+        "sequential_mixed_solves_per_sec_est": (
+            args.problems * share / sum(seq_mixed) if seq_mixed else None),
+        "sequential_note": (f"timed on the first {len(seq_plain)} problems x 1 right-hand side, "
+                            "rescaled by their share of the batch's N*M*d work"),
+        "config": {"mix": "d 2..12, level 3..7, M log-uniform [1e3, 2^20], uniform data",
+                   "max_work_NMd": args.max_work, "epsilon": args.epsilon, "lambda": args.lam},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

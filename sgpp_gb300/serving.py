@@ -1,0 +1,198 @@
+"""Continuous-batching regression-fit server over the batch engine (sgmev_batch_*).
+
+Requests (grid, X, Y, lambda, epsilon) arrive over time. The loop admits waiting requests in
+arrival order while a slot and pool space are free (admission by device-memory footprint: the
+engine's pools are sized once and a problem is admitted only if its padded grid, data and vector
+blocks fit), advances every resident problem by a few steps, hands finished results back and
+frees their slots. Grids, data and CG state stay on the device for a request's whole life; work of
+requests that arrive while others run overlaps with theirs in the same launches.
+
+    python -m sgpp_gb300.serving --rate 200 --duration 20 --max-work 2e10
+
+prints one JSON line: completed fits/s, offered load, p50/p99 latency, queue depth.
+Synthetic requests follow the batched-fit size mix (d uniform in 2..12, level in 3..7, data size
+log-uniform in [1e3, 2^20], uniform data), optionally truncated to N*M*d <= --max-work.
+"""
+from __future__ import annotations
+
+import argparse
+import dataclasses
+import json
+import os
+import sys
+import time
+from typing import Callable, Dict, List, Optional
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import sgpp_gb300 as sg  # noqa: E402
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    arrival: float          # seconds after the start of the run
+    grid: "sg.Grid"
+    X: np.ndarray
+    Y: np.ndarray
+    lam: float
+    epsilon: float = 1e-8
+    # filled in by the server
+    admitted: Optional[float] = None
+    finished: Optional[float] = None
+    alpha: Optional[np.ndarray] = None
+    iterations: int = 0
+    residual: float = 0.0
+
+
+class FitServer:
+    def __init__(self, max_slots: int = 64, rhs: int = 1, grid_capacity: int = 1 << 24,
+                 data_capacity: int = 1 << 26, steps_per_poll: int = 4):
+        self.engine = sg.BatchEngine(max_slots, rhs, grid_capacity, data_capacity)
+        self.steps_per_poll = steps_per_poll
+        self.queue_depths: List[int] = []
+
+    def close(self) -> None:
+        self.engine.close()
+
+    def run(self, requests: List[Request], clock: Callable[[], float] = time.perf_counter,
+            keep_alpha: bool = True, max_seconds: float = 1e9) -> List[Request]:
+        """Serve `requests` (sorted by arrival) in real time; returns the completed ones."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        waiting: List[Request] = []
+        resident: Dict[int, Request] = {}
+        done: List[Request] = []
+        t0 = clock()
+        k = 0
+        while (k < len(pending) or waiting or resident) and clock() - t0 < max_seconds:
+            now = clock() - t0
+            while k < len(pending) and pending[k].arrival <= now:
+                waiting.append(pending[k])
+                k += 1
+            # FIFO admission while a slot and pool space are free
+            while waiting:
+                r = waiting[0]
+                slot = self.engine.tryAdd(r.grid, r.X, r.Y, r.lam, r.epsilon)
+                if slot is None:
+                    if not resident:
+                        raise sg.OperationException(
+                            f"request {r.rid} does not fit into an empty engine")
+                    break
+                r.admitted = clock() - t0
+                resident[slot] = r
+                waiting.pop(0)
+            self.queue_depths.append(len(waiting))
+            if not resident:
+                # idle until the next arrival
+                if k < len(pending):
+                    time.sleep(max(0.0, min(0.001, pending[k].arrival - (clock() - t0))))
+                continue
+            phases = self.engine.step(self.steps_per_poll)
+            for slot in list(resident):
+                if phases[slot] == sg.BatchEngine.PHASE_DONE:
+                    r = resident.pop(slot)
+                    alpha, r.iterations, r.residual, _ = self.engine.result(slot)
+                    r.alpha = alpha if keep_alpha else None
+                    r.finished = clock() - t0
+                    self.engine.remove(slot)
+                    done.append(r)
+        return done
+
+
+def percentile(values: List[float], q: float) -> float:
+    if not values:
+        return float("nan")
+    v = sorted(values)
+    return v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
+
+
+class MixGenerator:
+    """Synthetic requests of the batched-fit size mix; grids are cached per (d, level) and the
+    data of a request is drawn from a pool of pre-generated matrices (per dimension)."""
+
+    def __init__(self, seed: int = 0, max_work: float = float("inf"), pool: int = 8,
+                 max_points: int = 1 << 20):
+        self.rng = np.random.default_rng(seed)
+        self.max_work = max_work
+        self.max_points = max_points
+        self.grids: Dict[tuple, sg.Grid] = {}
+        self.pool = pool
+        self.data: Dict[int, List[np.ndarray]] = {}
+
+    def grid(self, d: int, level: int) -> "sg.Grid":
+        key = (d, level)
+        if key not in self.grids:
+            g = sg.Grid.createLinearGrid(d)
+            g.getGenerator().regular(level)
+            self.grids[key] = g
+        return self.grids[key]
+
+    def _x(self, d: int, m: int) -> np.ndarray:
+        lst = self.data.setdefault(d, [])
+        if len(lst) < self.pool:
+            lst.append(self.rng.random((self.max_points, d)))
+        base = lst[int(self.rng.integers(0, len(lst)))]
+        off = int(self.rng.integers(0, self.max_points - m + 1))
+        return base[off:off + m]
+
+    def draw(self, rhs: int = 1):
+        for _ in range(1000):
+            d = int(self.rng.integers(2, 13))
+            level = int(self.rng.integers(3, 8))
+            m = int(np.exp(self.rng.uniform(np.log(1e3), np.log(self.max_points))))
+            n = sg.Grid.regularSize(d, level)
+            if n * m * d <= self.max_work:
+                break
+        X = self._x(d, m)
+        Y = self.rng.standard_normal((m, rhs))
+        return self.grid(d, level), X, Y
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rate", type=float, default=200.0, help="mean arrivals per second")
+    ap.add_argument("--duration", type=float, default=20.0, help="arrival window in seconds")
+    ap.add_argument("--max-work", type=float, default=2e10, help="cap on N*M*d per request")
+    ap.add_argument("--max-slots", type=int, default=64)
+    ap.add_argument("--epsilon", type=float, default=1e-8)
+    ap.add_argument("--lam", type=float, default=1e-4)
+    ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--drain-seconds", type=float, default=60.0)
+    args = ap.parse_args()
+
+    gen = MixGenerator(args.seed, args.max_work)
+    rng = np.random.default_rng(args.seed + 1)
+    t, reqs = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / args.rate)
+        if t > args.duration:
+            break
+        g, X, Y = gen.draw()
+        reqs.append(Request(len(reqs), t, g, X, Y, args.lam, args.epsilon))
+    server = FitServer(max_slots=args.max_slots, grid_capacity=1 << 25, data_capacity=1 << 27)
+    t0 = time.perf_counter()
+    done = server.run(reqs, keep_alpha=False, max_seconds=args.duration + args.drain_seconds)
+    wall = time.perf_counter() - t0
+    lat = [r.finished - r.arrival for r in done]
+    line = {
+        "metric": "served_fits_per_sec", "value": len(done) / wall, "unit": "fits/s",
+        "offered_rate": args.rate, "requests": len(reqs), "completed": len(done),
+        "wall_s": wall, "latency_ms": {"p50": 1e3 * percentile(lat, 0.5),
+                                        "p99": 1e3 * percentile(lat, 0.99)},
+        "queue_depth": {"max": max(server.queue_depths or [0]),
+                        "mean": float(np.mean(server.queue_depths or [0]))},
+        "config": {"mix": "d in 2..12, level 3..7, M log-uniform [1e3, 2^20], uniform data",
+                   "max_work_NMd": args.max_work, "epsilon": args.epsilon, "lambda": args.lam,
+                   "slots": args.max_slots, "engine_steps": server.engine.info()["steps"]},
+    }
+    print(json.dumps(line))
+    server.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
