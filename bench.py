@@ -271,7 +271,9 @@ def run_ours(args):
     kstats = {name: op.profileRead(kind) for name, kind in
               (("mult_fp32", sg.SGMEV_KERNEL_MULT_FP32), ("multT_fp32", sg.SGMEV_KERNEL_MULTT_FP32),
                ("mult_fp64", sg.SGMEV_KERNEL_MULT_FP64), ("multT_fp64", sg.SGMEV_KERNEL_MULTT_FP64),
-               ("mult_df64", sg.SGMEV_KERNEL_MULT_DF64), ("multT_df64", sg.SGMEV_KERNEL_MULTT_DF64))}
+               ("mult_df64", sg.SGMEV_KERNEL_MULT_DF64), ("multT_df64", sg.SGMEV_KERNEL_MULTT_DF64),
+               ("mult_sub32", sg.SGMEV_KERNEL_MULT_SUB32),
+               ("multT_sub32", sg.SGMEV_KERNEL_MULTT_SUB32))}
     op.profile(False)
     alpha = d_alpha.cpu().numpy()
     err = float(np.abs(alpha - alpha_ref).max() / np.abs(alpha_ref).max())
@@ -287,7 +289,7 @@ def run_ours(args):
     cnt, sec = kstats[dom]
     avg = sec / max(cnt, 1)
     achieved = work_per_op / avg / 1e12
-    is64 = dom.endswith("fp64")
+    is64 = dom.endswith("fp64") or dom.endswith("df64")
     peak = (peak64 if is64 else peak32) / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")

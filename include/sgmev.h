@@ -81,6 +81,10 @@ SGMEV_API int sgmev_device_count(void);
  * inner correction solves of SGMEV_SOLVE_MIXED* fits (SGMEV_SOLVE_PLAIN is never preconditioned).
  * Jacobi (diag(B^T B) + lambda*M) doubled the iteration count on clustered (Gaussian-mixture) data,
  * where fine-level hats see few points, so it is off unless asked for.
+ * "algo": "auto" (default), "dense" or "subspace" — how the FP32 products are evaluated: dense
+ * (every grid point for every data point, the STREAMING algorithm) or subspace-skipping (one basis
+ * function per subspace and data point, as the reference's DEFAULT operator; grids of dim <= 16
+ * with at most 24,576 subspace positions); "auto" takes subspace when it needs fewer instructions.
  */
 SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double* level_pow2,
                            const double* index, int64_t n_data, const double* data,

@@ -72,6 +72,8 @@ SGMEV_KERNEL_MULT_FP64 = 2
 SGMEV_KERNEL_MULTT_FP64 = 3
 SGMEV_KERNEL_MULT_DF64 = 4
 SGMEV_KERNEL_MULTT_DF64 = 5
+SGMEV_KERNEL_MULT_SUB32 = 6
+SGMEV_KERNEL_MULTT_SUB32 = 7
 
 
 # ---- exceptions (base/src/sgpp/base/exception/) --------------------------------------------
@@ -390,7 +392,8 @@ class OperationMultipleEvalConfiguration:
     """Operator selection plus a parameters tree. Parameters understood by the CUDA operator:
     ``precision``: "double" (default, native FP64), "df64" (FP64-accurate float-float on the
     FP32 pipes) or "float"; ``precond``: "none" (default) or "jacobi" for the inner solves of
-    mixed-precision fits."""
+    mixed-precision fits; ``algo``: "auto" (default), "dense" or "subspace" for the FP32 products
+    (subspace = one basis function per subspace and data point)."""
 
     def __init__(self, type=OperationMultipleEvalType.DEFAULT,
                  subType=OperationMultipleEvalSubType.DEFAULT,
@@ -456,7 +459,7 @@ class OperationMultiEvalCuda:
         if not bb.isUnitCube():
             left, right = bb.arrays()
         h = ctypes.c_void_p(None)
-        knobs = {k: str(v) for k, v in (params or {}).items() if k in ("precond",)}
+        knobs = {k: str(v) for k, v in (params or {}).items() if k in ("precond", "algo")}
         pj = json.dumps(knobs).encode() if knobs else None
         _check(L.sgmev_create(ctypes.byref(h), st.getDimension(), st.getSize(), _vp(lp), _vp(ix),
                               self.dataset.shape[0], _vp(self.dataset), _vp(left), _vp(right),

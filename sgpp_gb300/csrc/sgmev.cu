@@ -21,6 +21,7 @@
 
 #include "../../include/sgmev.h"
 #include "kernels.cuh"
+#include "subspace.h"
 
 namespace sgmev {
 
@@ -128,6 +129,9 @@ struct sgmev_op {
   double last_seconds = -1.0;
   int64_t launches = 0;
   bool precond = false;  // Jacobi-preconditioned inner CG in the mixed fits (params "precond")
+  int algo = 2;          // FP32 products: 0 dense, 1 subspace, 2 auto (params "algo")
+  SubPlan sub;           // subspace tables of the current grid
+  bool sub_ok = false;   // sub is built and chosen for the FP32 products
 
   std::vector<double> bb_left, bb_width;
 
@@ -150,7 +154,9 @@ enum {
   KIND_MULT_FP64 = 2,
   KIND_MULTT_FP64 = 3,
   KIND_MULT_DF64 = 4,
-  KIND_MULTT_DF64 = 5
+  KIND_MULTT_DF64 = 5,
+  KIND_MULT_SUB32 = 6,
+  KIND_MULTT_SUB32 = 7
 };
 
 template <typename T>
@@ -643,6 +649,12 @@ static int dev_mult(sgmev_op* op, int prec, const double* a64, const float* a32,
     SGMEV_TRY(run_mult_df(op, a32, a32lo, j_begin, j_end, &p));
     if (out64) SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
     if (out32) SGMEV_TRY((run_reduce<float2, float>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out32, nullptr, 0.0)));
+  } else if (op->sub_ok) {
+    const long ev = prof_begin(op, KIND_MULT_SUB32);
+    SGMEV_CUDA(subspace_mult(op->sub, op->stream, op->xt32, op->mpad, op->m, a32, out32, out64,
+                             j_begin, j_end, op->num_sms));
+    prof_end(op, ev);
+    op->launches += 2;
   } else {
     SGMEV_TRY(run_mult<float>(op, op->xt32, op->li32, a32, j_begin, j_end, &p));
     if (out64) SGMEV_TRY((run_reduce<float, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
@@ -664,6 +676,13 @@ static int dev_multt(sgmev_op* op, int prec, const double* v64, const float* v32
   } else if (prec == SGMEV_DF64) {
     SGMEV_TRY(run_multt_df(op, v32, v32lo, g_begin, g_end, &p));
     SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->npad, g_begin, valid, g_end, out64, add, scale)));
+  } else if (op->sub_ok) {
+    // the subspace scatter produces every grid entry at once (the range is a subset of it)
+    const long ev = prof_begin(op, KIND_MULTT_SUB32);
+    SGMEV_CUDA(subspace_multt(op->sub, op->stream, op->xt32, op->mpad, op->m, v32, op->npad,
+                              out64, add, scale, op->num_sms));
+    prof_end(op, ev);
+    op->launches += 3;
   } else {
     SGMEV_TRY(run_multt<float>(op, op->xt32, v32, op->li32, g_begin, g_end, &p));
     SGMEV_TRY((run_reduce<float, double>(op, (int)p.nsplit, op->npad, g_begin, valid, g_end, out64, add, scale)));
@@ -802,6 +821,22 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
   cudaFree(d_l);
   cudaFree(d_i);
   if (e != cudaSuccess) return fail(SGMEV_ERR_CUDA, std::string("stage grid: ") + cudaGetErrorString(e));
+  // subspace tables for the FP32 products: used when chosen ("algo") and cheaper by the
+  // instruction count per data point (one basis function per subspace, ~7 per dimension,
+  // against 3 per dimension for every grid point)
+  op->sub_ok = false;
+  subspace_free(&op->sub);
+  if (op->algo != 0 && n > 0) {
+    std::string why;
+    if (subspace_build(&op->sub, op->dim, n, level_pow2, index, &why)) {
+      const double dense_cost = 3.0 * op->dim * static_cast<double>(n);
+      const double sub_cost = (7.0 * op->dim + 3.0) * op->sub.n_sub;
+      op->sub_ok = op->algo == 1 || sub_cost * 1.5 < dense_cost;
+      if (!op->sub_ok) subspace_free(&op->sub);
+    } else if (op->algo == 1) {
+      return fail(SGMEV_ERR_UNSUPPORTED, "algo \"subspace\": " + why);
+    }
+  }
   // output vector and split partials depend on npad
   SGMEV_TRY(dalloc(&op->out64, static_cast<size_t>(std::max(op->npad, op->mpad))));
   const int64_t elems = part_need_elems(op);
@@ -829,6 +864,7 @@ static void release(sgmev_op* op) {
   if (op->ev_start) cudaEventDestroy(op->ev_start);
   if (op->ev_stop) cudaEventDestroy(op->ev_stop);
   if (op->own_stream) cudaStreamDestroy(op->own_stream);
+  subspace_free(&op->sub);
 }
 
 static int begin_timed(sgmev_op* op) {
@@ -926,6 +962,9 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
         return fail(SGMEV_ERR_INVALID, "bounding box interval " + std::to_string(t) + " is empty");
   }
   const std::string precond = json_string(params_json, "precond");
+  const std::string algo = json_string(params_json, "algo");
+  if (!algo.empty() && algo != "dense" && algo != "subspace" && algo != "auto")
+    return fail(SGMEV_ERR_INVALID, "params: algo must be \"dense\", \"subspace\" or \"auto\"");
   if (!precond.empty() && precond != "jacobi" && precond != "none")
     return fail(SGMEV_ERR_INVALID, "params: precond must be \"jacobi\" or \"none\"");
   int ndev = 0;
@@ -940,6 +979,7 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   op->m = n_data;
   op->mpad = std::max<int64_t>(round_up(std::max<int64_t>(n_data, 1), kMPadTo), kMPadTo);
   op->precond = precond == "jacobi";
+  op->algo = algo == "dense" ? 0 : (algo == "subspace" ? 1 : 2);
   auto bail = [&](int rc) {
     release(op);
     delete op;

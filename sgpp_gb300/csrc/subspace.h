@@ -1,0 +1,50 @@
+// Subspace-skipping evaluation of the hat basis (FP32): one basis function per subspace and
+// data point instead of every grid point (internal interface of libsgpp_gb300).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+namespace sgmev {
+
+// A grid regrouped by subspace (level vector). Positions: each subspace owns the contiguous range
+// [offset, offset + prod_t 2^{l_t - 1}) in subspace order; a grid point's position is
+// offset + sum_t ((i_t - 1) / 2) * stride_t. Positions without a grid point (adaptive grids)
+// carry alpha = 0 and are ignored on output.
+struct SubPlan {
+  int dim = 0;
+  int n_sub = 0;
+  int64_t total = 0;      // positions
+  int64_t n = 0;          // grid points
+  int4* desc = nullptr;   // [n_sub * dim] (bits(2^{l-1}), bits(2^l), stride, 0)
+  uint32_t* base = nullptr;  // [n_sub] offset - sum_t bits(1.5*2^23) * stride_t (mod 2^32)
+  int* pos = nullptr;     // [n] grid point -> position
+  float* asub = nullptr;  // [total] alpha in subspace order
+  unsigned long long* acc = nullptr;  // [total] fixed-point accumulators (multTranspose)
+  unsigned int* maxbits = nullptr;    // max |v| as float bits
+};
+
+// largest position count the shared-memory kernels handle (two 4-byte accumulators per position in
+// 192 KB)
+constexpr int64_t kSubMaxPositions = 24 * 1024;
+
+// Build the plan from the eval arrays (host, [n x dim] 2^l and i). Returns false (and leaves
+// the plan empty) when the grid does not fit the shared-memory kernels or dim is not templated.
+bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2,
+                    const double* index, std::string* err);
+void subspace_free(SubPlan* p);
+
+// out[j] (FP32 and/or FP64, zero beyond m) = sum_g alpha_g phi_g(x_j) for j in [j_begin, j_end)
+// (tile-aligned to 512); alpha32 [n] FP32.
+cudaError_t subspace_mult(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
+                          int64_t m, const float* alpha32, float* out32, double* out64,
+                          int64_t j_begin, int64_t j_end, int num_sms);
+
+// out64[g] (g < n; zero in [n, npad)) = sum_j v_j phi_g(x_j) (+ scale_add * add[g]); v32 [mpad]
+cudaError_t subspace_multt(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
+                           int64_t m, const float* v32, int64_t npad, double* out64,
+                           const double* add, double scale_add, int num_sms);
+
+}  // namespace sgmev

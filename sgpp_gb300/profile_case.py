@@ -21,14 +21,21 @@ if ROOT not in sys.path:
 
 import sgpp_gb300 as sg  # noqa: E402
 
-KINDS = {("mult", "float"): sg.SGMEV_KERNEL_MULT_FP32, ("multT", "float"): sg.SGMEV_KERNEL_MULTT_FP32,
-         ("mult", "double"): sg.SGMEV_KERNEL_MULT_FP64, ("multT", "double"): sg.SGMEV_KERNEL_MULTT_FP64}
+KINDS = {("mult", "float", "dense"): sg.SGMEV_KERNEL_MULT_FP32,
+         ("multT", "float", "dense"): sg.SGMEV_KERNEL_MULTT_FP32,
+         ("mult", "float", "subspace"): sg.SGMEV_KERNEL_MULT_SUB32,
+         ("multT", "float", "subspace"): sg.SGMEV_KERNEL_MULTT_SUB32,
+         ("mult", "double", "dense"): sg.SGMEV_KERNEL_MULT_FP64,
+         ("multT", "double", "dense"): sg.SGMEV_KERNEL_MULTT_FP64,
+         ("mult", "df64", "dense"): sg.SGMEV_KERNEL_MULT_DF64,
+         ("multT", "df64", "dense"): sg.SGMEV_KERNEL_MULTT_DF64}
 
 
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel", choices=["mult", "multT"], default="mult")
-    ap.add_argument("--precision", choices=["float", "double"], default="float")
+    ap.add_argument("--precision", choices=["float", "double", "df64"], default="float")
+    ap.add_argument("--algo", choices=["dense", "subspace"], default="dense")
     ap.add_argument("--dim", type=int, default=10)
     ap.add_argument("--level", type=int, default=5)
     ap.add_argument("--points", type=int, default=1 << 22)
@@ -43,7 +50,8 @@ def main() -> int:
     x = rng.random((args.points, args.dim))
     cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
                                                 sg.OperationMultipleEvalSubType.CUDA,
-                                                parameters={"precision": args.precision})
+                                                parameters={"precision": args.precision,
+                                                            "algo": args.algo})
     op = sg.createOperationMultipleEval(grid, x, cfg)
     a = rng.standard_normal(n)
     v = rng.standard_normal(args.points)
@@ -61,11 +69,13 @@ def main() -> int:
     op.profile(True)
     for _ in range(args.launches):
         run()
-    cnt, sec = op.profileRead(KINDS[(args.kernel, args.precision)])
+    algo = args.algo if args.precision == "float" else "dense"
+    cnt, sec = op.profileRead(KINDS[(args.kernel, args.precision, algo)])
     op.profile(False)
     flop = 6.0 * n * args.points * args.dim
     avg = sec / max(cnt, 1)
-    print(json.dumps({"kernel": args.kernel, "precision": args.precision, "dim": args.dim,
+    print(json.dumps({"kernel": args.kernel, "precision": args.precision, "algo": algo,
+                      "dim": args.dim,
                       "level": args.level, "n_grid": n, "points": args.points, "launches": cnt,
                       "avg_ms": avg * 1e3, "tflops_ref_count": flop / avg / 1e12}))
     op.close()

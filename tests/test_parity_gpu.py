@@ -31,24 +31,26 @@ def _grid_from(g, name):
                               g[name + "_index"].astype(np.int32))
 
 
-def _op(grid, x, precision="double"):
+def _op(grid, x, precision="double", algo="auto"):
     cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
                                                 sg.OperationMultipleEvalSubType.CUDA,
-                                                parameters={"precision": precision})
+                                                parameters={"precision": precision, "algo": algo})
     return sg.createOperationMultipleEval(grid, x, cfg)
 
 
 MULTEVAL = [str(c) for c in load_golden("multeval.npz")["cases"]]
 
 
-@pytest.mark.parametrize("precision,tol", [("double", FP64_TOL), ("df64", FP64_TOL),
-                                           ("float", FP32_TOL)])
+@pytest.mark.parametrize("precision,tol,algo", [("double", FP64_TOL, "auto"),
+                                                ("df64", FP64_TOL, "auto"),
+                                                ("float", FP32_TOL, "dense"),
+                                                ("float", FP32_TOL, "subspace")])
 @pytest.mark.parametrize("name", MULTEVAL)
-def test_mult_and_transpose_match_reference(name, precision, tol):
+def test_mult_and_transpose_match_reference(name, precision, tol, algo):
     g = load_golden("multeval.npz")
     grid = _grid_from(g, name)
     x = g[name + "_x"]
-    op = _op(grid, x, precision)
+    op = _op(grid, x, precision, algo)
     out = np.zeros(x.shape[0])
     op.mult(g[name + "_alpha"], out)
     assert rel_err(out, g[name + "_mult_default"]) < tol
@@ -107,8 +109,9 @@ def test_results_are_bitwise_reproducible():
     name = "d5_l6_m2000"
     grid = _grid_from(g, name)
     x = g[name + "_x"]
-    for prec in ("double", "df64", "float"):
-        op = _op(grid, x, prec)
+    for prec, algo in (("double", "auto"), ("df64", "auto"), ("float", "dense"),
+                       ("float", "subspace")):
+        op = _op(grid, x, prec, algo)
         a = np.zeros(x.shape[0])
         b = np.zeros(x.shape[0])
         op.mult(g[name + "_alpha"], a)
@@ -232,9 +235,10 @@ def test_system_apply_matches_oracle(oracle):
     opdf = _op(grid, x, "df64")
     opdf.systemApply(a, out, lam_m)
     assert rel_err(out, ref) < FP64_TOL
-    op32 = _op(grid, x, "float")
-    op32.systemApply(a, out, lam_m)
-    assert rel_err(out, ref) < FP32_TOL
+    for algo in ("dense", "subspace"):
+        op32 = _op(grid, x, "float", algo)
+        op32.systemApply(a, out, lam_m)
+        assert rel_err(out, ref) < FP32_TOL
 
 
 @pytest.mark.parametrize("precision", ["double", "df64"])
@@ -317,9 +321,10 @@ def test_df64_matches_native_fp64_at_full_size():
     assert rel_err(tdf, t64) < FP64_TOL
 
 
-def test_adjoint_and_linearity_at_full_size():
+@pytest.mark.parametrize("algo", ["dense", "subspace"])
+def test_adjoint_and_linearity_at_full_size(algo):
     """Size-independent properties at the regression-fit workload size (d=10, level 5,
-    2^20 points): <B a, v> = <a, B^T v>, and B is linear."""
+    2^20 points): <B a, v> = <a, B^T v>, B is linear, and the FP32 algorithms agree."""
     rng = np.random.default_rng(21)
     grid = sg.Grid.createLinearGrid(10)
     grid.getGenerator().regular(5)
@@ -329,7 +334,7 @@ def test_adjoint_and_linearity_at_full_size():
     a = rng.standard_normal(n)
     b = rng.standard_normal(n)
     v = rng.standard_normal(m)
-    op = _op(grid, x, "float")
+    op = _op(grid, x, "float", algo)
     Ba = np.zeros(m)
     Bb = np.zeros(m)
     Bab = np.zeros(m)
@@ -342,3 +347,11 @@ def test_adjoint_and_linearity_at_full_size():
     lhs = float(Ba @ v)
     rhs = float(a @ Btv)
     assert abs(lhs - rhs) <= 1e-5 * (np.abs(Ba).sum() * np.abs(v).max())
+    # against the FP64-accurate kernels at full size
+    ref = _op(grid, x, "df64")
+    Ba64 = np.zeros(m)
+    ref.mult(a, Ba64)
+    assert rel_err(Ba, Ba64) < FP32_TOL
+    Btv64 = np.zeros(n)
+    ref.multTranspose(v, Btv64)
+    assert rel_err(Btv, Btv64) < FP32_TOL
