@@ -202,6 +202,18 @@ def run_reference(args):
     return 0
 
 
+def op_config(args):
+    """Operator configuration: the CUDA subtype with its default knobs, plus --inner-tol."""
+    import sgpp_gb300 as sg
+
+    params = {}
+    if args.inner_tol is not None:
+        params["inner_tol"] = repr(args.inner_tol)
+    return sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                 sg.OperationMultipleEvalSubType.CUDA,
+                                                 parameters=params)
+
+
 def run_ours(args):
     import torch
 
@@ -224,7 +236,7 @@ def run_ours(args):
     work_per_op = FLOP_PER_PAIR_DIM * n * m * DIM
 
     stream = torch.cuda.Stream()
-    op = sg.createOperationMultipleEval(grid, x)  # FP64 op; mixed mode stages FP32 copies too
+    op = sg.createOperationMultipleEval(grid, x, op_config(args))  # FP64 op + FP32 copies
     op.setStream(stream.cuda_stream)
     d_y = torch.from_numpy(y).to(f"cuda:{local_rank}")
     d_alpha = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local_rank}")
@@ -273,7 +285,9 @@ def run_ours(args):
                ("mult_fp64", sg.SGMEV_KERNEL_MULT_FP64), ("multT_fp64", sg.SGMEV_KERNEL_MULTT_FP64),
                ("mult_df64", sg.SGMEV_KERNEL_MULT_DF64), ("multT_df64", sg.SGMEV_KERNEL_MULTT_DF64),
                ("mult_sub32", sg.SGMEV_KERNEL_MULT_SUB32),
-               ("multT_sub32", sg.SGMEV_KERNEL_MULTT_SUB32))}
+               ("multT_sub32", sg.SGMEV_KERNEL_MULTT_SUB32),
+               ("mult_subdf64", sg.SGMEV_KERNEL_MULT_SUBDF),
+               ("multT_subdf64", sg.SGMEV_KERNEL_MULTT_SUBDF))}
     op.profile(False)
     alpha = d_alpha.cpu().numpy()
     err = float(np.abs(alpha - alpha_ref).max() / np.abs(alpha_ref).max())
@@ -289,7 +303,7 @@ def run_ours(args):
     cnt, sec = kstats[dom]
     avg = sec / max(cnt, 1)
     achieved = work_per_op / avg / 1e12
-    is64 = dom.endswith("fp64") or dom.endswith("df64")
+    is64 = dom.endswith("fp64")
     peak = (peak64 if is64 else peak32) / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
@@ -318,7 +332,7 @@ def run_ours(args):
         for k in range(args.e2e_steps + 1):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            op2 = sg.createOperationMultipleEval(grid, xs)
+            op2 = sg.createOperationMultipleEval(grid, xs, op_config(args))
             a_host, _, _ = op2.fit(ys, LAMBDA, 20000, args.epsilon, mode=sg.SGMEV_SOLVE_MIXED)
             op2.close()
             torch.cuda.synchronize()
@@ -400,6 +414,8 @@ def main():
     ap.add_argument("--reference-iterations", type=int, default=110)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-fp64-probe", type=int, default=1)
+    ap.add_argument("--inner-tol", type=float, default=None,
+                    help="inner tolerance of the mixed fits (library default when omitted)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -81,6 +81,7 @@ SGMEV_API int sgmev_device_count(void);
  * inner correction solves of SGMEV_SOLVE_MIXED* fits (SGMEV_SOLVE_PLAIN is never preconditioned).
  * Jacobi (diag(B^T B) + lambda*M) doubled the iteration count on clustered (Gaussian-mixture) data,
  * where fine-level hats see few points, so it is off unless asked for.
+ * "inner_tol": relative tolerance of the inner correction solves of mixed fits (default "1e-4").
  * "algo": "auto" (default), "dense" or "subspace" — how the FP32 products are evaluated: dense
  * (every grid point for every data point, the STREAMING algorithm) or subspace-skipping (one basis
  * function per subspace and data point, as the reference's DEFAULT operator; grids of dim <= 16

@@ -129,6 +129,7 @@ struct sgmev_op {
   double last_seconds = -1.0;
   int64_t launches = 0;
   bool precond = false;  // Jacobi-preconditioned inner CG in the mixed fits (params "precond")
+  double inner_tol = 1e-4;  // relative tolerance of the inner solves of mixed fits ("inner_tol")
   int algo = 2;          // FP32 products: 0 dense, 1 subspace, 2 auto (params "algo")
   SubPlan sub;           // subspace tables of the current grid
   bool sub_ok = false;   // sub is built and chosen for the FP32 products
@@ -141,8 +142,8 @@ struct sgmev_op {
   std::vector<cudaEvent_t> prof_events;  // pool, 2 per launch
   std::vector<int> prof_kind;            // kind of launch i
   size_t prof_used = 0;                  // launches recorded since the last reset
-  int64_t prof_count[8] = {0};
-  double prof_seconds[8] = {0.0};
+  int64_t prof_count[10] = {0};
+  double prof_seconds[10] = {0.0};
 };
 
 namespace sgmev {
@@ -156,8 +157,11 @@ enum {
   KIND_MULT_DF64 = 4,
   KIND_MULTT_DF64 = 5,
   KIND_MULT_SUB32 = 6,
-  KIND_MULTT_SUB32 = 7
+  KIND_MULTT_SUB32 = 7,
+  KIND_MULT_SUBDF = 8,
+  KIND_MULTT_SUBDF = 9
 };
+constexpr int kKinds = 10;
 
 template <typename T>
 static int kind_mult() { return sizeof(T) == 4 ? KIND_MULT_FP32 : KIND_MULT_FP64; }
@@ -645,6 +649,12 @@ static int dev_mult(sgmev_op* op, int prec, const double* a64, const float* a32,
     SGMEV_TRY(run_mult<double>(op, op->xt64, op->li64, a64, j_begin, j_end, &p));
     if (out64) SGMEV_TRY((run_reduce<double, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
     if (out32) SGMEV_TRY((run_reduce<double, float>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out32, nullptr, 0.0)));
+  } else if (prec == SGMEV_DF64 && op->sub_ok && out64 && !out32) {
+    const long ev = prof_begin(op, KIND_MULT_SUBDF);
+    SGMEV_CUDA(subspace_mult_df(op->sub, op->stream, op->xt32, op->xt32lo, op->mpad, op->m, a32,
+                                a32lo, out64, j_begin, j_end, op->num_sms));
+    prof_end(op, ev);
+    op->launches += 2;
   } else if (prec == SGMEV_DF64) {
     SGMEV_TRY(run_mult_df(op, a32, a32lo, j_begin, j_end, &p));
     if (out64) SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
@@ -673,6 +683,13 @@ static int dev_multt(sgmev_op* op, int prec, const double* v64, const float* v32
   if (prec == SGMEV_FP64) {
     SGMEV_TRY(run_multt<double>(op, op->xt64, v64, op->li64, g_begin, g_end, &p));
     SGMEV_TRY((run_reduce<double, double>(op, (int)p.nsplit, op->npad, g_begin, valid, g_end, out64, add, scale)));
+  } else if (prec == SGMEV_DF64 && op->sub_ok && subspace_owner_fits(op->sub, true)) {
+    // the subspace sums produce every grid entry at once (the range is a subset of them)
+    const long ev = prof_begin(op, KIND_MULTT_SUBDF);
+    SGMEV_CUDA(subspace_multt_df(op->sub, op->stream, op->xt32, op->xt32lo, op->mpad, op->m, v32,
+                                 v32lo, op->npad, out64, add, scale, op->num_sms));
+    prof_end(op, ev);
+    op->launches += 3;
   } else if (prec == SGMEV_DF64) {
     SGMEV_TRY(run_multt_df(op, v32, v32lo, g_begin, g_end, &p));
     SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->npad, g_begin, valid, g_end, out64, add, scale)));
@@ -822,15 +839,15 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
   cudaFree(d_i);
   if (e != cudaSuccess) return fail(SGMEV_ERR_CUDA, std::string("stage grid: ") + cudaGetErrorString(e));
   // subspace tables for the FP32 products: used when chosen ("algo") and cheaper by the
-  // instruction count per data point (one basis function per subspace, ~7 per dimension,
-  // against 3 per dimension for every grid point)
+  // instruction count per data point (one basis function per subspace, ~8 per active dimension
+  // and ~10 per subspace, against 3 per dimension for every grid point)
   op->sub_ok = false;
   subspace_free(&op->sub);
   if (op->algo != 0 && n > 0) {
     std::string why;
     if (subspace_build(&op->sub, op->dim, n, level_pow2, index, &why)) {
       const double dense_cost = 3.0 * op->dim * static_cast<double>(n);
-      const double sub_cost = (7.0 * op->dim + 3.0) * op->sub.n_sub;
+      const double sub_cost = 8.0 * static_cast<double>(op->sub.act_work) + 10.0 * op->sub.n_sub;
       op->sub_ok = op->algo == 1 || sub_cost * 1.5 < dense_cost;
       if (!op->sub_ok) subspace_free(&op->sub);
     } else if (op->algo == 1) {
@@ -979,6 +996,19 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   op->m = n_data;
   op->mpad = std::max<int64_t>(round_up(std::max<int64_t>(n_data, 1), kMPadTo), kMPadTo);
   op->precond = precond == "jacobi";
+  {
+    const std::string it = json_string(params_json, "inner_tol");
+    if (!it.empty()) {
+      char* end = nullptr;
+      const double v = std::strtod(it.c_str(), &end);
+      if (!end || *end != '\0' || !(v > 0.0) || !(v < 1.0)) {
+        release(op);
+        delete op;
+        return fail(SGMEV_ERR_INVALID, "params: inner_tol must be a number in (0, 1)");
+      }
+      op->inner_tol = v;
+    }
+  }
   op->algo = algo == "dense" ? 0 : (algo == "subspace" ? 1 : 2);
   auto bail = [&](int rc) {
     release(op);
@@ -1464,12 +1494,17 @@ static int fit_common(sgmev_op* op, int mode, const double* y, bool y_on_device,
     double* dx = op->cg + 7 * np;
     if (!reuse) SGMEV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * np, op->stream));
     double rnorm2 = 0.0, r0 = 0.0;
-    const double eps_inner = 1e-3;
+    const double eps_inner = op->inner_tol;
     if (op->precond) SGMEV_TRY(dev_precond(op, lm));
     for (int outer = 0; outer < 64; ++outer) {
-      SGMEV_TRY(dev_system(op, res_prec, x, rr, lm));
-      sub_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, b, rr, rr);
-      op->launches += 1;
+      if (outer == 0 && !reuse) {
+        // cold start: A * 0 is exactly zero, so the first residual is b itself
+        SGMEV_CUDA(cudaMemcpyAsync(rr, b, sizeof(double) * np, cudaMemcpyDeviceToDevice, op->stream));
+      } else {
+        SGMEV_TRY(dev_system(op, res_prec, x, rr, lm));
+        sub_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, b, rr, rr);
+        op->launches += 1;
+      }
       SGMEV_TRY(dev_dot(op, rr, rr, np, &rnorm2));
       if (outer == 0) r0 = rnorm2;
       res = rnorm2;
@@ -1504,7 +1539,7 @@ SGMEV_API int sgmev_profile(sgmev_op* op, int enable) {
   SGMEV_CUDA(cudaStreamSynchronize(op->stream));
   op->profile = enable != 0;
   op->prof_used = 0;
-  for (int k = 0; k < 8; ++k) {
+  for (int k = 0; k < kKinds; ++k) {
     op->prof_count[k] = 0;
     op->prof_seconds[k] = 0.0;
   }
@@ -1514,7 +1549,7 @@ SGMEV_API int sgmev_profile(sgmev_op* op, int enable) {
 SGMEV_API int sgmev_profile_read(sgmev_op* op, int kind, int64_t* launches, double* seconds) {
   using namespace sgmev;
   SGMEV_TRY(check_op(op));
-  if (kind < 0 || kind >= 8) return fail(SGMEV_ERR_INVALID, "unknown kernel kind");
+  if (kind < 0 || kind >= kKinds) return fail(SGMEV_ERR_INVALID, "unknown kernel kind");
   SGMEV_CUDA(cudaStreamSynchronize(op->stream));
   SGMEV_TRY(prof_resolve(op));
   if (launches) *launches = op->prof_count[kind];

@@ -6,14 +6,12 @@
 // non-zero: in dimension t its index is i_t = 2 k_t + 1 with k_t = floor(x_t 2^{l_t - 1}). So a
 // product costs one evaluation per subspace instead of one per grid point. The kernels are
 // branch-free per dimension: with S = 2^{l-1}, L = 2^l and xc = x clamped into [0, 1),
-//     y5 = fma(xc, S, -0.5)               exact when xc S >= 0.5 (xc S is exact: S = 2^k)
-//     r  = y5 + 1.5*2^23                  rounds to the integer k; r = 1.5*2^23 + k exactly
-//     t  = fma(x, L, -(2 (r - 1.5*2^23) + 1)),  h = sat(1 - |t|),  p *= h
-//     flat += bits(r) * stride            (the offset term is folded into the subspace base)
-// Rounding xc S - 0.5 to the nearest integer gives floor(xc S) except at exact cell boundaries,
-// where both neighbouring hats are 0, so the choice there does not matter; xc S < S - 0.5 keeps k
-// at most S - 1, and x outside [0, 1) selects an edge cell whose hat is 0. (The constant
-// 1.5*2^23 - 0.5 is not an FP32 number, so the 0.5 is subtracted in its own exact step.)
+//     r  = fma_rd(xc, S, 2^23)            = 2^23 + floor(xc S) exactly (xc S is exact: S = 2^k,
+//                                           and [2^23, 2^24) has spacing 1; rounded downwards)
+//     t  = fma(x, L, fma(r, -2, 2^24 - 1)) = x L - (2k + 1),  h = sat(1 - |t|),  p *= h
+//     flat += bits(r) * stride            (bits(2^23 + k) = bits(2^23) + k; the offset term is
+//                                           folded into the subspace base)
+// xc < 1 keeps k at most S - 1, and x outside [0, 1) selects an edge cell whose hat is 0.
 //
 //   mult        gather: result_j = sum_s asub[pos_s(x_j)] * prod_t h_t; asub in shared memory
 //   multT       scatter: contributions v_j * prod_t h_t are rounded to 43-bit fixed point (one
@@ -28,8 +26,10 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <type_traits>
 #include <vector>
 
+#include "kernels.cuh"
 #include "subspace.h"
 
 namespace sgmev {
@@ -37,11 +37,11 @@ namespace sgmev {
 namespace {
 
 constexpr int kSDT = 64;                  // subspaces per shared-memory descriptor tile
-constexpr unsigned kMagicBits = 0x4B400000u;  // bits of 1.5 * 2^23
-constexpr float kMagic = 12582912.0f;         // 1.5 * 2^23
+constexpr unsigned kMagicBits = 0x4B000000u;  // bits of 2^23
+constexpr float kMagic = 8388608.0f;          // 2^23
+constexpr float kTwoMagic = 16777216.0f;      // 2^24
 constexpr float kBelowOne = 0.99999994f;      // largest float < 1
 
-constexpr int kMultThreads = 128, kMultR = 4;
 constexpr int kMulttThreads = 256, kMulttR = 2;
 
 template <int DIM, int R>
@@ -82,8 +82,8 @@ __device__ __forceinline__ void eval_subspace(const Pt<DIM, R>& pt, const int4* 
     const uint32_t st = static_cast<uint32_t>(q.z);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const float rr = fmaf(pt.xc[r][t], S, -0.5f) + kMagic;
-      const float nI = fmaf(rr - kMagic, -2.0f, -1.0f);
+      const float rr = __fmaf_rd(pt.xc[r][t], S, kMagic);
+      const float nI = fmaf(rr, -2.0f, kTwoMagic - 1.0f);
       const float tt = fmaf(pt.x[r][t], L, nI);
       p[r] *= __saturatef(1.0f - fabsf(tt));
       flat[r] += __float_as_uint(rr) * st;
@@ -95,47 +95,252 @@ __device__ __forceinline__ void eval_subspace(const Pt<DIM, R>& pt, const int4* 
   for (int r = 0; r < R; ++r) flat[r] = min(flat[r], last);
 }
 
+// Active-dimension evaluation (FP32). Most subspaces have level 1 in most dimensions, and the
+// level-1 hat h1(x) = min(2x, 2 - 2x) (exact, and > 0 inside (0, 1)) does not depend on the
+// subspace. So a point carries H1 = prod_t h1(x_t) and r_t = 1 / h1(x_t), and a subspace with
+// active dimensions A = {t : l_t > 1} costs |A| one-dimensional evaluations:
+//     p = H1 * prod_{t in A} h_{l_t}(x_t) * r_t,      flat = base_A + sum_{t in A} bits(r) * stride_t
+// (the h1 factors cancel to rounding). A point with a coordinate outside (2^-100, 1) gets H1 = 0
+// (its hats are 0, or below 2^-90 next to the origin) and coordinates 0.5, so every cell index
+// stays inside its subspace.
+constexpr int kActThreads = 256, kActR = 2;  // the mult kernel: tiles of 512 points, 2 per thread
+constexpr int kActUnrolled = 6;              // active-dimension counts with unrolled evaluation
+constexpr float kActLow = 7.88860905e-31f;   // 2^-100
+
+// whether a coordinate lies in the evaluated domain
+__device__ __forceinline__ bool act_inside(float x) { return x > kActLow && x < 1.0f; }
+
+// p_r *= prod_{a < na} h(x_{r, t_a}) / h1(x_{r, t_a}), flat_r += sum_a bits(cell) * stride_a, for the
+// kActR points of this thread; xr points at the thread's (x, 1 / h1) pairs, dimension t at
+// xr[t * kActR * kActThreads + r * kActThreads]
+template <int NA>
+__device__ __forceinline__ void act_eval(const int4* __restrict__ d, const float2* __restrict__ xr,
+                                         int na, float (&p)[kActR], uint32_t (&flat)[kActR]) {
+#pragma unroll
+  for (int a = 0; a < (NA < 0 ? 1 : NA); ++a) {
+    if (NA < 0 && a >= na) break;
+    const int4 q = d[a];
+    const float S = __int_as_float(q.y), L = __int_as_float(q.z);
+    const uint32_t st = static_cast<uint32_t>(q.w);
+    const float2* xt = xr + q.x * (kActR * kActThreads);
+#pragma unroll
+    for (int r = 0; r < kActR; ++r) {
+      const float2 v = xt[r * kActThreads];
+      const float rr = __fmaf_rd(v.x, S, kMagic);
+      const float nI = fmaf(rr, -2.0f, kTwoMagic - 1.0f);
+      const float h = __saturatef(1.0f - fabsf(fmaf(v.x, L, nI)));
+      p[r] = (p[r] * h) * v.y;
+      flat[r] += __float_as_uint(rr) * st;
+    }
+  }
+  if (NA < 0) {  // more active dimensions than the unrolled cases: plain loop
+    for (int a = 1; a < na; ++a) {
+      const int4 q = d[a];
+      const float S = __int_as_float(q.y), L = __int_as_float(q.z);
+      const uint32_t st = static_cast<uint32_t>(q.w);
+      const float2* xt = xr + q.x * (kActR * kActThreads);
+#pragma unroll
+      for (int r = 0; r < kActR; ++r) {
+        const float2 v = xt[r * kActThreads];
+        const float rr = __fmaf_rd(v.x, S, kMagic);
+        const float nI = fmaf(rr, -2.0f, kTwoMagic - 1.0f);
+        const float h = __saturatef(1.0f - fabsf(fmaf(v.x, L, nI)));
+        p[r] = (p[r] * h) * v.y;
+        flat[r] += __float_as_uint(rr) * st;
+      }
+    }
+  }
+}
+
 template <int DIM>
-__global__ void __launch_bounds__(kMultThreads) sub_mult_kernel(
-    const int4* __restrict__ desc, const uint32_t* __restrict__ base, int n_sub,
+__global__ void __launch_bounds__(kActThreads, 2) sub_mult_act_kernel(
+    const int4* __restrict__ act, const int4* __restrict__ sact, int n_sub,
     const float* __restrict__ asub, int total, const float* __restrict__ xt, int64_t mpad,
     int64_t m, int64_t tile_begin, int64_t n_tiles, float* __restrict__ out32,
     double* __restrict__ out64) {
   extern __shared__ __align__(16) unsigned char smem[];
-  int4* s_desc = reinterpret_cast<int4*>(smem);
-  uint32_t* s_base = reinterpret_cast<uint32_t*>(s_desc + kSDT * DIM);
-  float* s_a = reinterpret_cast<float*>(s_base + kSDT);
-  for (int k = threadIdx.x; k < total; k += kMultThreads) s_a[k] = asub[k];
+  int4* s_act = reinterpret_cast<int4*>(smem);             // [kSDT * DIM] (t, S, L, stride)
+  int4* s_info = s_act + kSDT * DIM;                        // [kSDT] (base, cells, -, n_active)
+  float2* s_xr = reinterpret_cast<float2*>(s_info + kSDT);  // [DIM][kActR][kActThreads]
+  float* s_a = reinterpret_cast<float*>(s_xr + DIM * kActR * kActThreads);  // [total]
+  const int tid = threadIdx.x;
+  const float2* xr = s_xr + tid;
+  for (int k = tid; k < total; k += kActThreads) s_a[k] = asub[k];
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    const int64_t j0 = (tile_begin + tile) * (kMultThreads * kMultR) + threadIdx.x;
-    Pt<DIM, kMultR> pt;
-    load_points(pt, xt, mpad, j0, kMultThreads);
-    float acc[kMultR];
+    const int64_t j0 = (tile_begin + tile) * (kActR * kActThreads) + tid;
+    float h1p[kActR];
 #pragma unroll
-    for (int r = 0; r < kMultR; ++r) acc[r] = 0.0f;
+    for (int r = 0; r < kActR; ++r) {
+      const int64_t j = j0 + r * kActThreads;
+      float xv[DIM];
+      bool inside = j < m;
+#pragma unroll
+      for (int t = 0; t < DIM; ++t) {
+        xv[t] = xt[static_cast<int64_t>(t) * mpad + j];
+        inside = inside && act_inside(xv[t]);
+      }
+      h1p[r] = inside ? 1.0f : 0.0f;
+#pragma unroll
+      for (int t = 0; t < DIM; ++t) {
+        const float x = inside ? xv[t] : 0.5f;
+        const float h1 = fminf(2.0f * x, 2.0f - 2.0f * x);
+        h1p[r] *= h1;
+        // thread-private slots: read back only by this thread
+        s_xr[(t * kActR + r) * kActThreads + tid] = make_float2(x, 1.0f / h1);
+      }
+    }
+    float acc[kActR];
+#pragma unroll
+    for (int r = 0; r < kActR; ++r) acc[r] = 0.0f;
     for (int s0 = 0; s0 < n_sub; s0 += kSDT) {
       const int cnt = min(kSDT, n_sub - s0);
       __syncthreads();
-      for (int k = threadIdx.x; k < cnt * DIM; k += kMultThreads) s_desc[k] = desc[s0 * DIM + k];
-      for (int k = threadIdx.x; k < cnt; k += kMultThreads) s_base[k] = base[s0 + k];
+      for (int k = tid; k < cnt * DIM; k += kActThreads) s_act[k] = act[s0 * DIM + k];
+      for (int k = tid; k < cnt; k += kActThreads) s_info[k] = sact[s0 + k];
       __syncthreads();
       for (int s = 0; s < cnt; ++s) {
-        uint32_t flat[kMultR];
-        float p[kMultR];
-        eval_subspace<DIM, kMultR>(pt, s_desc + s * DIM, s_base[s], static_cast<uint32_t>(total - 1),
-                                   flat, p);
+        const int4 si = s_info[s];
+        const int4* d = s_act + s * DIM;
+        float p[kActR];
+        uint32_t flat[kActR];
 #pragma unroll
-        for (int r = 0; r < kMultR; ++r) acc[r] = fmaf(s_a[flat[r]], p[r], acc[r]);
+        for (int r = 0; r < kActR; ++r) {
+          p[r] = h1p[r];
+          flat[r] = static_cast<uint32_t>(si.x);
+        }
+        switch (si.w) {  // warp-uniform: every thread walks the same subspace
+          case 0: break;
+          case 1: act_eval<1>(d, xr, 1, p, flat); break;
+          case 2: act_eval<2>(d, xr, 2, p, flat); break;
+          case 3: act_eval<(DIM < 3 ? DIM : 3)>(d, xr, 3, p, flat); break;
+          case 4: act_eval<(DIM < 4 ? DIM : 4)>(d, xr, 4, p, flat); break;
+          case 5: act_eval<(DIM < 5 ? DIM : 5)>(d, xr, 5, p, flat); break;
+          case kActUnrolled: act_eval<(DIM < kActUnrolled ? DIM : kActUnrolled)>(d, xr, kActUnrolled, p, flat); break;
+          default: act_eval<-1>(d, xr, si.w, p, flat); break;
+        }
+#pragma unroll
+        for (int r = 0; r < kActR; ++r)
+          acc[r] = fmaf(s_a[min(flat[r], static_cast<uint32_t>(total - 1))], p[r], acc[r]);
       }
     }
 #pragma unroll
-    for (int r = 0; r < kMultR; ++r) {
-      const int64_t j = j0 + r * kMultThreads;
+    for (int r = 0; r < kActR; ++r) {
+      const int64_t j = j0 + r * kActThreads;
       const float v = j < m ? acc[r] : 0.0f;
       if (out32) out32[j] = v;
       if (out64) out64[j] = static_cast<double>(v);
     }
   }
+}
+
+// df64 (FP64-accurate) subspace mult. A point is the float-float value x = x_hi + x_lo
+// (|x_lo| <= ulp(x_hi) / 2). Points with a coordinate outside the open interval (0, 1) see only zero
+// hats (every Linear-grid hat vanishes there), so their result is 0 and their coordinates are
+// replaced by 0.5 before the loop. For x in (0, 1) the cell and hat per dimension are
+//     sl = L x_lo                          exact (L = 2^l)
+//     t2 = fma_rd(x_hi, L, sl)             = the largest float <= x L (one rounding, downwards)
+//     r  = fma_rd(t2, 0.5, 2^23)           = 2^23 + k, k = floor(x S) in [0, S - 1]
+//     m  = fma(r, -2, 2^24)                = -2k exactly
+//     a  = fma(x_hi, L, m), b = fma(x_hi, -L, 2 - m)
+// floor(t2 / 2) = floor(x L / 2) because every even integer is a float, so rounding downwards
+// cannot cross one. x lies in the closed cell [k/S, (k+1)/S], where the hat is
+// min(x L - 2k, 2k + 2 - x L) >= 0; the smaller side is (a, sl) (rising) or (b, -sl) (falling), and
+// its high part is exact (Sterbenz: x_hi L lies within a factor 2 of 2k resp. 2k + 2), as is
+// a - b near the middle, so the sign test picks the side exactly and the float-float hat is exact.
+// alpha is a float-float pair per position in shared memory.
+constexpr int kDfThreads = 512, kDfR = 1;
+
+template <int DIM>
+__global__ void __launch_bounds__(kDfThreads, 1) sub_mult_df_kernel(
+    const int4* __restrict__ desc, const uint32_t* __restrict__ base, int n_sub,
+    const float2* __restrict__ asub2, int total, const float* __restrict__ xh_t,
+    const float* __restrict__ xl_t, int64_t mpad, int64_t m, int64_t tile_begin,
+    int64_t n_tiles, double* __restrict__ out64) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  int4* s_desc = reinterpret_cast<int4*>(smem);
+  uint32_t* s_base = reinterpret_cast<uint32_t*>(s_desc + kSDT * DIM);
+  float2* s_a = reinterpret_cast<float2*>(s_base + kSDT);
+  for (int k = threadIdx.x; k < total; k += kDfThreads) s_a[k] = asub2[k];
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t j0 = (tile_begin + tile) * (kDfThreads * kDfR) + threadIdx.x;
+    float xh[kDfR][DIM], xl[kDfR][DIM];
+    bool inside[kDfR];
+#pragma unroll
+    for (int r = 0; r < kDfR; ++r) {
+      inside[r] = true;
+#pragma unroll
+      for (int t = 0; t < DIM; ++t) {
+        const int64_t src = static_cast<int64_t>(t) * mpad + j0 + r * kDfThreads;
+        const float h = xh_t[src], l = xl_t[src];
+        inside[r] = inside[r] && (h > 0.0f || (h == 0.0f && l > 0.0f)) &&
+                    (h < 1.0f || (h == 1.0f && l < 0.0f));
+        xh[r][t] = h;
+        xl[r][t] = l;
+      }
+#pragma unroll
+      for (int t = 0; t < DIM; ++t) {
+        xh[r][t] = inside[r] ? xh[r][t] : 0.5f;
+        xl[r][t] = inside[r] ? xl[r][t] : 0.0f;
+      }
+    }
+    ff acc[kDfR];
+#pragma unroll
+    for (int r = 0; r < kDfR; ++r) acc[r] = ff{0.0f, 0.0f};
+    for (int s0 = 0; s0 < n_sub; s0 += kSDT) {
+      const int cnt = min(kSDT, n_sub - s0);
+      __syncthreads();
+      for (int k = threadIdx.x; k < cnt * DIM; k += kDfThreads) s_desc[k] = desc[s0 * DIM + k];
+      for (int k = threadIdx.x; k < cnt; k += kDfThreads) s_base[k] = base[s0 + k];
+      __syncthreads();
+      for (int s = 0; s < cnt; ++s) {
+        const int4* d = s_desc + s * DIM;
+        uint32_t flat[kDfR];
+        ff p[kDfR];
+#pragma unroll
+        for (int r = 0; r < kDfR; ++r) flat[r] = s_base[s];
+#pragma unroll
+        for (int t = 0; t < DIM; ++t) {
+          const int4 q = d[t];
+          const float L = __int_as_float(q.y);
+          const uint32_t st = static_cast<uint32_t>(q.z);
+#pragma unroll
+          for (int r = 0; r < kDfR; ++r) {
+            const float sl = L * xl[r][t];
+            const float t2 = __fmaf_rd(xh[r][t], L, sl);
+            const float rr = __fmaf_rd(t2, 0.5f, kMagic);
+            const float m2k = fmaf(rr, -2.0f, kTwoMagic);
+            const float a = fmaf(xh[r][t], L, m2k);
+            const float b = fmaf(xh[r][t], -L, 2.0f - m2k);
+            const bool rise = fmaf(2.0f, sl, a - b) <= 0.0f;
+            const ff h{rise ? a : b, rise ? sl : -sl};
+            p[r] = t == 0 ? h : mul_ff(p[r], h);
+            flat[r] += __float_as_uint(rr) * st;
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < kDfR; ++r) {
+          const float2 a = s_a[min(flat[r], static_cast<uint32_t>(total - 1))];
+          add_ff(acc[r], mul_ff(p[r], ff{a.x, a.y}));
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kDfR; ++r) renorm_ff(acc[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < kDfR; ++r) {
+      const int64_t j = j0 + r * kDfThreads;
+      out64[j] = (j < m && inside[r]) ? static_cast<double>(acc[r].h) + static_cast<double>(acc[r].l)
+                                      : 0.0;
+    }
+  }
+}
+
+__global__ void scatter_alpha_df_kernel(const float* __restrict__ ah, const float* __restrict__ al,
+                                        const int* __restrict__ pos, int64_t n,
+                                        float2* __restrict__ asub2) {
+  for (int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; g < n;
+       g += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    asub2[pos[g]] = make_float2(ah[g], al[g]);
 }
 
 // fixed-point scale 2^k for contributions |v_j| * prod h <= max|v|: one contribution stays below
@@ -209,6 +414,339 @@ __global__ void __launch_bounds__(kMulttThreads) sub_multt_kernel(
   }
 }
 
+// Owner-computes multTranspose. Thread k of a pass owns subspace s = pass * blockDim + k and sums
+// v_j * prod_t h_t(x_j) over the CTA's points into per-cell accumulators in shared memory, laid out
+// [cell][thread] so that a warp's 32 updates hit 32 different banks. The points of a tile are
+// staged in shared memory as rows (x_0 .. x_{d-1}, v) and read by all threads at once (broadcast).
+// After each tile a thread adds its cells into the CTA's FP64 row of the partial matrix (its cells
+// belong to it alone, so the update order is fixed); sum_rows_kernel adds the rows in CTA order.
+// Every step has a fixed order, so the result is the same bit for bit from run to run.
+// Points with a coordinate outside the open interval (0, 1) see only zero hats; the staging step
+// gives them v = 0 and coordinates 0.5, which keeps the cell arithmetic inside the subspace with no
+// clamp. FP32: the per-dimension product is the one of the mult kernel. DF: as sub_mult_df_kernel,
+// with float-float per-tile sums.
+constexpr int kOwnMaxThreads = 512, kOwnTile = 256;
+
+template <int DIM, bool DF>
+struct OwnLayout {
+  static constexpr int W = DF ? (2 * DIM + 2 + 3) / 4 * 4 : (DIM + 1 + 3) / 4 * 4;  // floats per row
+  static constexpr int V = DF ? 2 * DIM : DIM;                                       // v column
+  using Acc = typename std::conditional<DF, float2, float>::type;
+};
+
+template <int DIM, bool DF>
+__device__ __forceinline__ void own_stage_tile(float* s_pt, int64_t tile,
+                                               const float* __restrict__ xh_t,
+                                               const float* __restrict__ xl_t, int64_t mpad,
+                                               int64_t m, const float* __restrict__ vh,
+                                               const float* __restrict__ vl) {
+  using Lay = OwnLayout<DIM, DF>;
+  const int64_t j0 = tile * kOwnTile;
+  for (int k = threadIdx.x; k < kOwnTile * DIM; k += blockDim.x) {
+    const int t = k / kOwnTile, jj = k - t * kOwnTile;
+    const int64_t src = static_cast<int64_t>(t) * mpad + j0 + jj;
+    s_pt[jj * Lay::W + t] = xh_t[src];
+    if constexpr (DF) s_pt[jj * Lay::W + DIM + t] = xl_t[src];
+  }
+  __syncthreads();
+  for (int jj = threadIdx.x; jj < kOwnTile; jj += blockDim.x) {
+    float* row = s_pt + jj * Lay::W;
+    const int64_t j = j0 + jj;
+    bool inside = j < m;
+#pragma unroll
+    for (int t = 0; t < DIM; ++t) {
+      const float h = row[t];
+      if constexpr (DF) {
+        const float l = row[DIM + t];
+        inside = inside && (h > 0.0f || (h == 0.0f && l > 0.0f)) &&
+                 (h < 1.0f || (h == 1.0f && l < 0.0f));
+      } else {
+        inside = inside && h > 0.0f && h < 1.0f;
+      }
+    }
+    if (!inside) {
+#pragma unroll
+      for (int t = 0; t < DIM; ++t) {
+        row[t] = 0.5f;
+        if constexpr (DF) row[DIM + t] = 0.0f;
+      }
+    }
+    row[Lay::V] = inside ? vh[j] : 0.0f;
+    if constexpr (DF) row[Lay::V + 1] = inside ? vl[j] : 0.0f;
+  }
+  __syncthreads();
+}
+
+template <int DIM, bool DF>
+__global__ void __launch_bounds__(kOwnMaxThreads, DF ? 1 : 2) sub_multt_own_kernel(
+    const int4* __restrict__ desc, const int4* __restrict__ sinfo, int n_sub, int cmax,
+    int total, const float* __restrict__ xh_t, const float* __restrict__ xl_t, int64_t mpad,
+    int64_t m, const float* __restrict__ vh, const float* __restrict__ vl, int64_t n_tiles,
+    double* __restrict__ rows) {
+  using Lay = OwnLayout<DIM, DF>;
+  using Acc = typename Lay::Acc;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* s_pt = reinterpret_cast<float*>(smem);                // [kOwnTile][W]
+  Acc* s_acc = reinterpret_cast<Acc*>(s_pt + kOwnTile * Lay::W);  // [cmax][blockDim]
+  double* row = rows + static_cast<int64_t>(blockIdx.x) * total;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int s0 = 0; s0 < n_sub; s0 += nth) {
+    const int sid = s0 + tid;
+    const bool active = sid < n_sub;
+    const int4 info = active ? sinfo[sid] : make_int4(0, 0, 0, 0);  // (offset, cells, cbase, 0)
+    float S[DIM], L[DIM];
+    uint32_t st[DIM];
+#pragma unroll
+    for (int t = 0; t < DIM; ++t) {
+      const int4 q = active ? desc[static_cast<int64_t>(sid) * DIM + t]
+                            : make_int4(__float_as_int(1.0f), __float_as_int(2.0f), 0, 0);
+      S[t] = __int_as_float(q.x);
+      L[t] = __int_as_float(q.y);
+      st[t] = static_cast<uint32_t>(q.z);
+    }
+    for (int c = 0; c < info.y; ++c) s_acc[c * nth + tid] = Acc{};
+    bool first = true;
+    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+      __syncthreads();  // the previous tile's rows are no longer read
+      own_stage_tile<DIM, DF>(s_pt, tile, xh_t, xl_t, mpad, m, vh, vl);
+      if (active) {
+        for (int jj = 0; jj < kOwnTile; ++jj) {
+          const float4* r4 = reinterpret_cast<const float4*>(s_pt + jj * Lay::W);
+          float rw[Lay::W];
+#pragma unroll
+          for (int k = 0; k < Lay::W / 4; ++k) {
+            const float4 f = r4[k];
+            rw[4 * k] = f.x;
+            rw[4 * k + 1] = f.y;
+            rw[4 * k + 2] = f.z;
+            rw[4 * k + 3] = f.w;
+          }
+          uint32_t c = static_cast<uint32_t>(info.z);
+          if constexpr (DF) {
+            ff p{1.0f, 0.0f};
+#pragma unroll
+            for (int t = 0; t < DIM; ++t) {
+              const float xh = rw[t], xl = rw[DIM + t];
+              const float sl = L[t] * xl;
+              const float t2 = __fmaf_rd(xh, L[t], sl);
+              const float rr = __fmaf_rd(t2, 0.5f, kMagic);
+              const float m2k = fmaf(rr, -2.0f, kTwoMagic);
+              const float a = fmaf(xh, L[t], m2k);
+              const float b = fmaf(xh, -L[t], 2.0f - m2k);
+              const bool rise = fmaf(2.0f, sl, a - b) <= 0.0f;
+              const ff h{rise ? a : b, rise ? sl : -sl};
+              p = t == 0 ? h : mul_ff(p, h);
+              c += __float_as_uint(rr) * st[t];
+            }
+            const ff q = mul_ff(p, ff{rw[Lay::V], rw[Lay::V + 1]});
+            float2* slot = reinterpret_cast<float2*>(s_acc) + min(c, static_cast<uint32_t>(cmax - 1)) * nth + tid;
+            ff a{slot->x, slot->y};
+            add_ff(a, q);
+            *slot = make_float2(a.h, a.l);
+          } else {
+            float p = 1.0f;
+#pragma unroll
+            for (int t = 0; t < DIM; ++t) {
+              const float rr = __fmaf_rd(rw[t], S[t], kMagic);
+              const float nI = fmaf(rr, -2.0f, kTwoMagic - 1.0f);
+              const float h = __saturatef(1.0f - fabsf(fmaf(rw[t], L[t], nI)));
+              p = t == 0 ? h : p * h;
+              c += __float_as_uint(rr) * st[t];
+            }
+            float* slot = reinterpret_cast<float*>(s_acc) + min(c, static_cast<uint32_t>(cmax - 1)) * nth + tid;
+            *slot = fmaf(rw[Lay::V], p, *slot);
+          }
+        }
+        // this tile's sums into the CTA's FP64 row (cells of this subspace are this thread's)
+        for (int c = 0; c < info.y; ++c) {
+          Acc& a = s_acc[c * nth + tid];
+          double v;
+          if constexpr (DF) {
+            v = static_cast<double>(a.x) + static_cast<double>(a.y);
+          } else {
+            v = static_cast<double>(a);
+          }
+          double* dst = row + info.x + c;
+          *dst = first ? v : *dst + v;
+          a = Acc{};
+        }
+      }
+      first = false;
+    }
+    if (active && first)  // no tile for this CTA: its row holds zeros
+      for (int c = 0; c < info.y; ++c) row[info.x + c] = 0.0;
+  }
+}
+
+// Owner-computes multTranspose with active-dimension evaluation (FP32): as sub_multt_own_kernel,
+// with rows (H1 * v, 0, (x_0, 1 / h1(x_0)), ..., (x_{d-1}, 1 / h1(x_{d-1}))); a thread's active
+// dimensions are held in registers for up to 4 of them (unrolled per count), else looped over.
+template <int DIM>
+struct ActRow {
+  static constexpr int W = (2 + 2 * DIM + 3) / 4 * 4;
+};
+
+template <int DIM>
+__device__ __forceinline__ void act_stage_tile(float* s_pt, int64_t tile,
+                                               const float* __restrict__ xt, int64_t mpad,
+                                               int64_t m, const float* __restrict__ v) {
+  constexpr int W = ActRow<DIM>::W;
+  const int64_t j0 = tile * kOwnTile;
+  for (int k = threadIdx.x; k < kOwnTile * DIM; k += blockDim.x) {
+    const int t = k / kOwnTile, jj = k - t * kOwnTile;
+    s_pt[jj * W + 2 + 2 * t] = xt[static_cast<int64_t>(t) * mpad + j0 + jj];
+  }
+  __syncthreads();
+  for (int jj = threadIdx.x; jj < kOwnTile; jj += blockDim.x) {
+    float* row = s_pt + jj * W;
+    const int64_t j = j0 + jj;
+    bool inside = j < m;
+#pragma unroll
+    for (int t = 0; t < DIM; ++t) inside = inside && act_inside(row[2 + 2 * t]);
+    float h1p = 1.0f;
+#pragma unroll
+    for (int t = 0; t < DIM; ++t) {
+      const float x = inside ? row[2 + 2 * t] : 0.5f;
+      const float h1 = fminf(2.0f * x, 2.0f - 2.0f * x);
+      h1p *= h1;
+      row[2 + 2 * t] = x;
+      row[3 + 2 * t] = 1.0f / h1;
+    }
+    row[0] = inside ? h1p * v[j] : 0.0f;
+    row[1] = 0.0f;
+  }
+  __syncthreads();
+}
+
+// one tile of points for a subspace with NA active dimensions: s_acc[c * nth + tid] += p_j
+template <int NA>
+__device__ __forceinline__ void act_own_tile(const float* __restrict__ s_pt, int w,
+                                             const int4* __restrict__ q, uint32_t cbase,
+                                             int cmax, float* __restrict__ s_acc, int nth, int tid) {
+  int toff[NA > 0 ? NA : 1];
+  float S[NA > 0 ? NA : 1], L[NA > 0 ? NA : 1];
+  uint32_t st[NA > 0 ? NA : 1];
+#pragma unroll
+  for (int a = 0; a < NA; ++a) {
+    toff[a] = 2 + 2 * q[a].x;
+    S[a] = __int_as_float(q[a].y);
+    L[a] = __int_as_float(q[a].z);
+    st[a] = static_cast<uint32_t>(q[a].w);
+  }
+  float* acc = s_acc + tid;
+  for (int jj = 0; jj < kOwnTile; ++jj) {
+    const float* r = s_pt + jj * w;
+    float p = r[0];
+    uint32_t c = cbase;
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+      const float2 xr = *reinterpret_cast<const float2*>(r + toff[a]);
+      const float rr = __fmaf_rd(xr.x, S[a], kMagic);
+      const float nI = fmaf(rr, -2.0f, kTwoMagic - 1.0f);
+      const float h = __saturatef(1.0f - fabsf(fmaf(xr.x, L[a], nI)));
+      p = (p * h) * xr.y;
+      c += __float_as_uint(rr) * st[a];
+    }
+    acc[min(c, static_cast<uint32_t>(cmax - 1)) * nth] += p;
+  }
+}
+
+// more active dimensions than the unrolled cases: a loop over them
+__device__ __forceinline__ void act_own_tile_dyn(const float* __restrict__ s_pt, int w,
+                                                 const int4* __restrict__ q, int na,
+                                                 uint32_t cbase, int cmax,
+                                                 float* __restrict__ s_acc, int nth, int tid) {
+  float* acc = s_acc + tid;
+  for (int jj = 0; jj < kOwnTile; ++jj) {
+    const float* r = s_pt + jj * w;
+    float p = r[0];
+    uint32_t c = cbase;
+    for (int a = 0; a < na; ++a) {
+      const int4 d = q[a];
+      const float2 xr = *reinterpret_cast<const float2*>(r + 2 + 2 * d.x);
+      const float rr = __fmaf_rd(xr.x, __int_as_float(d.y), kMagic);
+      const float nI = fmaf(rr, -2.0f, kTwoMagic - 1.0f);
+      const float h = __saturatef(1.0f - fabsf(fmaf(xr.x, __int_as_float(d.z), nI)));
+      p = (p * h) * xr.y;
+      c += __float_as_uint(rr) * static_cast<uint32_t>(d.w);
+    }
+    acc[min(c, static_cast<uint32_t>(cmax - 1)) * nth] += p;
+  }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kOwnMaxThreads, 2) sub_multt_act_kernel(
+    const int4* __restrict__ act, const int4* __restrict__ sact, int n_sub, int cmax, int total,
+    const float* __restrict__ xt, int64_t mpad, int64_t m, const float* __restrict__ v,
+    int64_t n_tiles, double* __restrict__ rows) {
+  constexpr int W = ActRow<DIM>::W;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* s_pt = reinterpret_cast<float*>(smem);   // [kOwnTile][W]
+  float* s_acc = s_pt + kOwnTile * W;             // [cmax][blockDim]
+  double* row = rows + static_cast<int64_t>(blockIdx.x) * total;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int s0 = 0; s0 < n_sub; s0 += nth) {
+    const int sid = s0 + tid;
+    const bool active = sid < n_sub;
+    const int4 info = active ? sact[sid] : make_int4(0, 0, 0, 0);  // (base, cells, cbase, n_active)
+    const uint32_t offset = static_cast<uint32_t>(info.x) - static_cast<uint32_t>(info.z);
+    const uint32_t cbase = static_cast<uint32_t>(info.z);
+    const int4* q = act + static_cast<int64_t>(active ? sid : 0) * DIM;
+    for (int c = 0; c < info.y; ++c) s_acc[c * nth + tid] = 0.0f;
+    bool first = true;
+    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+      __syncthreads();  // the previous tile's rows are no longer read
+      act_stage_tile<DIM>(s_pt, tile, xt, mpad, m, v);
+      if (active) {
+        // subspaces are sorted by their active-dimension count, so a warp mostly takes one case
+        switch (info.w) {
+          case 0: act_own_tile<0>(s_pt, W, q, cbase, cmax, s_acc, nth, tid); break;
+          case 1: act_own_tile<1>(s_pt, W, q, cbase, cmax, s_acc, nth, tid); break;
+          case 2: act_own_tile<(DIM < 2 ? DIM : 2)>(s_pt, W, q, cbase, cmax, s_acc, nth, tid); break;
+          case 3: act_own_tile<(DIM < 3 ? DIM : 3)>(s_pt, W, q, cbase, cmax, s_acc, nth, tid); break;
+          case 4: act_own_tile<(DIM < 4 ? DIM : 4)>(s_pt, W, q, cbase, cmax, s_acc, nth, tid); break;
+          default: act_own_tile_dyn(s_pt, W, q, info.w, cbase, cmax, s_acc, nth, tid); break;
+        }
+        for (int c = 0; c < info.y; ++c) {
+          float& a = s_acc[c * nth + tid];
+          double* dst = row + offset + c;
+          *dst = first ? static_cast<double>(a) : *dst + static_cast<double>(a);
+          a = 0.0f;
+        }
+      }
+      first = false;
+    }
+    if (active && first)
+      for (int c = 0; c < info.y; ++c) row[offset + c] = 0.0;
+  }
+}
+
+// sums[k] = sum over rows b in order of rows[b][k] (k < total)
+__global__ void sum_rows_kernel(const double* __restrict__ rows, int nrows, int64_t total,
+                                double* __restrict__ sums) {
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double a = 0.0;
+    for (int b = 0; b < nrows; ++b) a += rows[static_cast<int64_t>(b) * total + k];
+    sums[k] = a;
+  }
+}
+
+// out[g] (g < n; zero in [n, npad)) = sums[pos[g]] (+ scale_add * add[g])
+__global__ void gather_sums_kernel(const double* __restrict__ sums, const int* __restrict__ pos,
+                                   int64_t n, int64_t npad, const double* __restrict__ add,
+                                   double scale_add, double* __restrict__ out) {
+  for (int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; g < npad;
+       g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double r = 0.0;
+    if (g < n) {
+      r = sums[pos[g]];
+      if (add) r = fma(scale_add, add[g], r);
+    }
+    out[g] = r;
+  }
+}
+
 __global__ void maxabs_kernel(const float* __restrict__ v, int64_t m, unsigned int* __restrict__ out) {
   __shared__ float s[256];
   float mx = 0.0f;
@@ -248,9 +786,6 @@ __global__ void gather_result_kernel(const unsigned long long* __restrict__ acc,
   }
 }
 
-size_t mult_smem(int dim, int64_t total) {
-  return sizeof(int4) * kSDT * dim + sizeof(uint32_t) * kSDT + sizeof(float) * total;
-}
 size_t multt_smem(int dim, int64_t total) {
   return sizeof(int4) * kSDT * dim + sizeof(uint32_t) * kSDT + 2 * sizeof(int) * total;
 }
@@ -264,13 +799,28 @@ template <int DIM>
 cudaError_t launch_mult(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
                         int64_t m, float* out32, double* out64, int64_t t0, int64_t nt,
                         int num_sms) {
-  const size_t sm = mult_smem(DIM, p.total);
-  cudaError_t e = cudaFuncSetAttribute(sub_mult_kernel<DIM>,
+  const size_t sm = sizeof(int4) * (kSDT * DIM + kSDT) +
+                    sizeof(float2) * DIM * kActR * kActThreads + sizeof(float) * p.total;
+  cudaError_t e = cudaFuncSetAttribute(sub_mult_act_kernel<DIM>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
   if (e != cudaSuccess) return e;
   const int64_t blocks = std::min<int64_t>(nt, static_cast<int64_t>(num_sms) * 8);
-  sub_mult_kernel<DIM><<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kMultThreads, sm, s>>>(
-      p.desc, p.base, p.n_sub, p.asub, static_cast<int>(p.total), xt, mpad, m, t0, nt, out32, out64);
+  sub_mult_act_kernel<DIM><<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kActThreads, sm, s>>>(
+      p.act, p.sact, p.n_sub, p.asub, static_cast<int>(p.total), xt, mpad, m, t0, nt, out32, out64);
+  return cudaGetLastError();
+}
+
+template <int DIM>
+cudaError_t launch_mult_df(const SubPlan& p, cudaStream_t s, const float* xh, const float* xl,
+                           int64_t mpad, int64_t m, double* out64, int64_t t0, int64_t nt,
+                           int num_sms) {
+  const size_t sm = sizeof(int4) * kSDT * DIM + sizeof(uint32_t) * kSDT + sizeof(float2) * p.total;
+  cudaError_t e = cudaFuncSetAttribute(sub_mult_df_kernel<DIM>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = std::min<int64_t>(nt, static_cast<int64_t>(num_sms) * 8);
+  sub_mult_df_kernel<DIM><<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kDfThreads, sm, s>>>(
+      p.desc, p.base, p.n_sub, p.asub2, static_cast<int>(p.total), xh, xl, mpad, m, t0, nt, out64);
   return cudaGetLastError();
 }
 
@@ -286,6 +836,72 @@ cudaError_t launch_multt(const SubPlan& p, cudaStream_t s, const float* xt, int6
   sub_multt_kernel<DIM><<<static_cast<unsigned>(blocks), kMulttThreads, sm, s>>>(
       p.desc, p.base, p.n_sub, static_cast<int>(p.total), xt, mpad, m, nt, v, p.maxbits,
       static_cast<float>(std::max<int64_t>(m, 1)), p.acc);
+  return cudaGetLastError();
+}
+
+int own_threads(const SubPlan& p) {
+  return static_cast<int>(std::min<int64_t>(kOwnMaxThreads, (p.n_sub + 31) / 32 * 32));
+}
+
+size_t own_smem(const SubPlan& p, int dim, bool df) {
+  const int w = df ? (2 * dim + 2 + 3) / 4 * 4 : (dim + 1 + 3) / 4 * 4;
+  return sizeof(float) * kOwnTile * w +
+         (df ? sizeof(float2) : sizeof(float)) * static_cast<size_t>(p.cmax) * own_threads(p);
+}
+
+template <int DIM, bool DF>
+cudaError_t launch_multt_own(const SubPlan& p, cudaStream_t s, const float* xh, const float* xl,
+                             int64_t mpad, int64_t m, const float* vh, const float* vl,
+                             int num_sms) {
+  auto kern = sub_multt_own_kernel<DIM, DF>;
+  const size_t sm = own_smem(p, DIM, DF);
+  const int nth = own_threads(p);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
+  if (e != cudaSuccess) return e;
+  const int64_t nt = mpad / kOwnTile;
+  // a fixed grid for a given device and plan: the row count, and with it the summation order,
+  // does not change between calls
+  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), p.row_cap);
+  kern<<<static_cast<unsigned>(rows), nth, sm, s>>>(p.desc, p.sinfo, p.n_sub, p.cmax,
+                                                    static_cast<int>(p.total), xh, xl, mpad, m, vh,
+                                                    vl, nt, p.rows);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  sum_rows_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.total + 255) / 256)), 256, 0, s>>>(
+      p.rows, static_cast<int>(rows), p.total, reinterpret_cast<double*>(p.acc));
+  return cudaGetLastError();
+}
+
+size_t act_own_smem(const SubPlan& p, int dim) {
+  return sizeof(float) * kOwnTile * ((2 + 2 * dim + 3) / 4 * 4) +
+         sizeof(float) * static_cast<size_t>(p.cmax) * own_threads(p);
+}
+
+template <int DIM>
+cudaError_t launch_multt_act(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
+                             int64_t m, const float* v, int num_sms) {
+  auto kern = sub_multt_act_kernel<DIM>;
+  const size_t sm = act_own_smem(p, DIM);
+  const int nth = own_threads(p);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
+  if (e != cudaSuccess) return e;
+  const int64_t nt = mpad / kOwnTile;
+  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), p.row_cap);
+  kern<<<static_cast<unsigned>(rows), nth, sm, s>>>(p.act, p.sact, p.n_sub, p.cmax,
+                                                    static_cast<int>(p.total), xt, mpad, m, v, nt,
+                                                    p.rows);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  sum_rows_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.total + 255) / 256)), 256, 0, s>>>(
+      p.rows, static_cast<int>(rows), p.total, reinterpret_cast<double*>(p.acc));
   return cudaGetLastError();
 }
 
@@ -313,11 +929,25 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
     }
     groups[lv].push_back(g);
   }
-  std::vector<int4> desc;
+  std::vector<int4> desc, sinfo, act, sact;
   std::vector<uint32_t> base;
+  int64_t cmax = 0;
+  int na_max = 0;
+  int64_t act_work = 0;
+  // subspaces in order of their number of active (level > 1) dimensions, so that neighbouring
+  // threads of the owner-computes kernels run the same number of evaluations
+  std::vector<const std::pair<const std::vector<int>, std::vector<int64_t>>*> order;
+  for (const auto& kv : groups) order.push_back(&kv);
+  auto n_active = [](const std::vector<int>& l) {
+    return static_cast<int>(std::count_if(l.begin(), l.end(), [](int v) { return v > 1; }));
+  };
+  std::stable_sort(order.begin(), order.end(), [&](const auto* a, const auto* b) {
+    return n_active(a->first) < n_active(b->first);
+  });
   std::vector<int> pos(static_cast<size_t>(n));
   int64_t offset = 0;
-  for (const auto& kv : groups) {
+  for (const auto* kvp : order) {
+    const auto& kv = *kvp;
     const std::vector<int>& l = kv.first;
     std::vector<int64_t> stride(dim);
     int64_t size = 1;
@@ -342,6 +972,30 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
       b -= kMagicBits * static_cast<uint32_t>(stride[t]);  // mod 2^32
     }
     base.push_back(b);
+    sinfo.push_back(make_int4(static_cast<int>(offset), static_cast<int>(size),
+                              static_cast<int>(b - static_cast<uint32_t>(offset)), 0));
+    cmax = std::max(cmax, size);
+    // active dimensions: (t, S bits, L bits, stride); the base counts only their magic offsets
+    uint32_t cb = 0;
+    int na = 0;
+    for (int t = 0; t < dim; ++t) {
+      if (l[t] <= 1) continue;
+      const float S = std::ldexp(1.0f, l[t] - 1);
+      const float L = std::ldexp(1.0f, l[t]);
+      int4 q;
+      q.x = t;
+      std::memcpy(&q.y, &S, 4);
+      std::memcpy(&q.z, &L, 4);
+      q.w = static_cast<int>(stride[t]);
+      act.push_back(q);
+      cb -= kMagicBits * static_cast<uint32_t>(stride[t]);
+      ++na;
+    }
+    for (int t = na; t < dim; ++t) act.push_back(make_int4(0, 0, 0, 0));
+    na_max = std::max(na_max, na);
+    act_work += na;
+    sact.push_back(make_int4(static_cast<int>(static_cast<uint32_t>(offset) + cb),
+                             static_cast<int>(size), static_cast<int>(cb), na));
     for (int64_t g : kv.second) {
       int64_t f = offset;
       for (int t = 0; t < dim; ++t) f += ((static_cast<int64_t>(index[g * dim + t]) - 1) / 2) * stride[t];
@@ -353,13 +1007,35 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
   p->n_sub = static_cast<int>(groups.size());
   p->total = offset;
   p->n = n;
+  p->cmax = static_cast<int>(cmax);
+  p->na_max = na_max;
+  p->act_work = act_work;
+  // partial rows of the owner-computes multTranspose: up to 16 CTAs per SM (fewer for wide CTAs),
+  // at most 256 MB
+  int dev = 0, sms = 1;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    *err = "subspace plan: device query failed";
+    return false;
+  }
+  const int nth = own_threads(*p);
+  p->row_cap = std::min<int64_t>(static_cast<int64_t>(sms) * std::min(16, std::max(2, 1024 / nth)),
+                                 std::max<int64_t>(1, (int64_t(256) << 20) / (8 * offset)));
   bool ok = cudaMalloc(&p->desc, sizeof(int4) * desc.size()) == cudaSuccess &&
+            cudaMalloc(&p->sinfo, sizeof(int4) * sinfo.size()) == cudaSuccess &&
+            cudaMalloc(&p->act, sizeof(int4) * act.size()) == cudaSuccess &&
+            cudaMalloc(&p->sact, sizeof(int4) * sact.size()) == cudaSuccess &&
+            cudaMalloc(&p->rows, sizeof(double) * p->row_cap * offset) == cudaSuccess &&
             cudaMalloc(&p->base, sizeof(uint32_t) * base.size()) == cudaSuccess &&
             cudaMalloc(&p->pos, sizeof(int) * pos.size()) == cudaSuccess &&
             cudaMalloc(&p->asub, sizeof(float) * offset) == cudaSuccess &&
+            cudaMalloc(&p->asub2, sizeof(float2) * offset) == cudaSuccess &&
             cudaMalloc(&p->acc, sizeof(unsigned long long) * offset) == cudaSuccess &&
             cudaMalloc(&p->maxbits, sizeof(unsigned int)) == cudaSuccess;
   ok = ok && cudaMemcpy(p->desc, desc.data(), sizeof(int4) * desc.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(p->sinfo, sinfo.data(), sizeof(int4) * sinfo.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(p->act, act.data(), sizeof(int4) * act.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(p->sact, sact.data(), sizeof(int4) * sact.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemcpy(p->base, base.data(), sizeof(uint32_t) * base.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemcpy(p->pos, pos.data(), sizeof(int) * pos.size(), cudaMemcpyHostToDevice) == cudaSuccess;
   if (!ok) {
@@ -372,9 +1048,14 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
 
 void subspace_free(SubPlan* p) {
   cudaFree(p->desc);
+  cudaFree(p->sinfo);
+  cudaFree(p->act);
+  cudaFree(p->sact);
+  cudaFree(p->rows);
   cudaFree(p->base);
   cudaFree(p->pos);
   cudaFree(p->asub);
+  cudaFree(p->asub2);
   cudaFree(p->acc);
   cudaFree(p->maxbits);
   *p = SubPlan{};
@@ -389,7 +1070,7 @@ cudaError_t subspace_mult(const SubPlan& p, cudaStream_t s, const float* xt, int
   if (e != cudaSuccess) return e;
   scatter_alpha_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.n + 255) / 256)), 256, 0, s>>>(
       alpha32, p.pos, p.n, p.asub);
-  const int64_t tile = kMultThreads * kMultR;
+  const int64_t tile = kActR * kActThreads;
   const int64_t t0 = j_begin / tile;
   const int64_t nt = (j_end + tile - 1) / tile - t0;
   if (nt <= 0) return cudaGetLastError();
@@ -404,10 +1085,63 @@ cudaError_t subspace_mult(const SubPlan& p, cudaStream_t s, const float* xt, int
   }
 }
 
+cudaError_t subspace_mult_df(const SubPlan& p, cudaStream_t s, const float* xh, const float* xl,
+                             int64_t mpad, int64_t m, const float* ah, const float* al,
+                             double* out64, int64_t j_begin, int64_t j_end, int num_sms) {
+  cudaError_t e = cudaMemsetAsync(p.asub2, 0, sizeof(float2) * p.total, s);
+  if (e != cudaSuccess) return e;
+  scatter_alpha_df_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.n + 255) / 256)), 256, 0, s>>>(
+      ah, al, p.pos, p.n, p.asub2);
+  const int64_t tile = kDfThreads * kDfR;
+  const int64_t t0 = j_begin / tile;
+  const int64_t nt = (j_end + tile - 1) / tile - t0;
+  if (nt <= 0) return cudaGetLastError();
+  switch (p.dim) {
+#define F(D) \
+  case D:    \
+    return launch_mult_df<D>(p, s, xh, xl, mpad, m, out64, t0, nt, num_sms);
+    SUB_DIMS(F)
+#undef F
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+namespace {
+constexpr size_t kOwnSmemBudget = 200 * 1024;
+
+cudaError_t own_finish(const SubPlan& p, cudaStream_t s, int64_t npad, double* out64,
+                       const double* add, double scale_add) {
+  gather_sums_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (npad + 255) / 256)), 256, 0, s>>>(
+      reinterpret_cast<const double*>(p.acc), p.pos, p.n, npad, add, scale_add, out64);
+  return cudaGetLastError();
+}
+}  // namespace
+
+bool subspace_owner_fits(const SubPlan& p, bool df) {
+  const size_t sm = df ? own_smem(p, p.dim, true) : act_own_smem(p, p.dim);
+  return p.n_sub > 0 && p.cmax > 0 && p.rows != nullptr && sm <= kOwnSmemBudget;
+}
+
 cudaError_t subspace_multt(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
                            int64_t m, const float* v32, int64_t npad, double* out64,
                            const double* add, double scale_add, int num_sms) {
-  cudaError_t e = cudaMemsetAsync(p.maxbits, 0, sizeof(unsigned int), s);
+  cudaError_t e = cudaSuccess;
+  if (subspace_owner_fits(p, false)) {
+    switch (p.dim) {
+#define F(D)                                                                                 \
+  case D:                                                                                    \
+    e = launch_multt_act<D>(p, s, xt, mpad, m, v32, num_sms);                                \
+    break;
+      SUB_DIMS(F)
+#undef F
+      default:
+        return cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
+    return own_finish(p, s, npad, out64, add, scale_add);
+  }
+  e = cudaMemsetAsync(p.maxbits, 0, sizeof(unsigned int), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(p.acc, 0, sizeof(unsigned long long) * p.total, s);
   if (e != cudaSuccess) return e;
   maxabs_kernel<<<static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(608, (m + 255) / 256))), 256, 0, s>>>(
@@ -427,6 +1161,26 @@ cudaError_t subspace_multt(const SubPlan& p, cudaStream_t s, const float* xt, in
       p.acc, p.pos, p.n, npad, p.maxbits, static_cast<float>(std::max<int64_t>(m, 1)), add,
       scale_add, out64);
   return cudaGetLastError();
+}
+
+cudaError_t subspace_multt_df(const SubPlan& p, cudaStream_t s, const float* xh, const float* xl,
+                              int64_t mpad, int64_t m, const float* vh, const float* vl,
+                              int64_t npad, double* out64, const double* add, double scale_add,
+                              int num_sms) {
+  if (!subspace_owner_fits(p, true)) return cudaErrorInvalidValue;
+  cudaError_t e = cudaSuccess;
+  switch (p.dim) {
+#define F(D)                                                                   \
+  case D:                                                                      \
+    e = launch_multt_own<D, true>(p, s, xh, xl, mpad, m, vh, vl, num_sms);     \
+    break;
+    SUB_DIMS(F)
+#undef F
+    default:
+      return cudaErrorInvalidValue;
+  }
+  if (e != cudaSuccess) return e;
+  return own_finish(p, s, npad, out64, add, scale_add);
 }
 
 }  // namespace sgmev

@@ -22,8 +22,17 @@ struct SubPlan {
   uint32_t* base = nullptr;  // [n_sub] offset - sum_t bits(1.5*2^23) * stride_t (mod 2^32)
   int* pos = nullptr;     // [n] grid point -> position
   float* asub = nullptr;  // [total] alpha in subspace order
-  unsigned long long* acc = nullptr;  // [total] fixed-point accumulators (multTranspose)
+  float2* asub2 = nullptr;  // [total] alpha as float-float pairs (df64 mult)
+  unsigned long long* acc = nullptr;  // [total] fixed-point accumulators / FP64 sums (multT)
   unsigned int* maxbits = nullptr;    // max |v| as float bits
+  int4* sinfo = nullptr;  // [n_sub] (offset, cells, offset-free base, 0)
+  int4* act = nullptr;    // [n_sub * dim] active dimensions (t, bits(S), bits(L), stride), padded
+  int4* sact = nullptr;   // [n_sub] (base over active dimensions, cells, its offset-free part, count)
+  int na_max = 0;         // most active dimensions of a subspace
+  int64_t act_work = 0;   // active dimensions summed over subspaces
+  int cmax = 0;           // largest cell count of a subspace
+  double* rows = nullptr;  // [row_cap * total] per-CTA partial sums (owner-computes multT)
+  int64_t row_cap = 0;
 };
 
 // largest position count the shared-memory kernels handle (two 4-byte accumulators per position in
@@ -42,9 +51,26 @@ cudaError_t subspace_mult(const SubPlan& p, cudaStream_t s, const float* xt, int
                           int64_t m, const float* alpha32, float* out32, double* out64,
                           int64_t j_begin, int64_t j_end, int num_sms);
 
+// FP64-accurate (float-float) mult: out64[j] for j in [j_begin, j_end) (tile-aligned to 512),
+// x as (xh, xl) dim-major pairs, alpha as (ah, al) [n]
+cudaError_t subspace_mult_df(const SubPlan& p, cudaStream_t s, const float* xh, const float* xl,
+                             int64_t mpad, int64_t m, const float* ah, const float* al,
+                             double* out64, int64_t j_begin, int64_t j_end, int num_sms);
+
+// true when the owner-computes multTranspose holds its per-cell sums in shared memory (FP32 or
+// float-float); otherwise subspace_multt falls back to the fixed-point scatter and
+// subspace_multt_df must not be called
+bool subspace_owner_fits(const SubPlan& p, bool df);
+
 // out64[g] (g < n; zero in [n, npad)) = sum_j v_j phi_g(x_j) (+ scale_add * add[g]); v32 [mpad]
 cudaError_t subspace_multt(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
                            int64_t m, const float* v32, int64_t npad, double* out64,
                            const double* add, double scale_add, int num_sms);
+
+// FP64-accurate (float-float) multTranspose: x as (xh, xl), v as (vh, vl) [mpad]
+cudaError_t subspace_multt_df(const SubPlan& p, cudaStream_t s, const float* xh, const float* xl,
+                              int64_t mpad, int64_t m, const float* vh, const float* vl,
+                              int64_t npad, double* out64, const double* add, double scale_add,
+                              int num_sms);
 
 }  // namespace sgmev

@@ -28,7 +28,9 @@ KINDS = {("mult", "float", "dense"): sg.SGMEV_KERNEL_MULT_FP32,
          ("mult", "double", "dense"): sg.SGMEV_KERNEL_MULT_FP64,
          ("multT", "double", "dense"): sg.SGMEV_KERNEL_MULTT_FP64,
          ("mult", "df64", "dense"): sg.SGMEV_KERNEL_MULT_DF64,
-         ("multT", "df64", "dense"): sg.SGMEV_KERNEL_MULTT_DF64}
+         ("multT", "df64", "dense"): sg.SGMEV_KERNEL_MULTT_DF64,
+         ("mult", "df64", "subspace"): sg.SGMEV_KERNEL_MULT_SUBDF,
+         ("multT", "df64", "subspace"): sg.SGMEV_KERNEL_MULTT_SUBDF}
 
 
 def main() -> int:
@@ -69,7 +71,7 @@ def main() -> int:
     op.profile(True)
     for _ in range(args.launches):
         run()
-    algo = args.algo if args.precision == "float" else "dense"
+    algo = "dense" if args.precision == "double" else args.algo
     cnt, sec = op.profileRead(KINDS[(args.kernel, args.precision, algo)])
     op.profile(False)
     flop = 6.0 * n * args.points * args.dim

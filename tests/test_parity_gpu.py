@@ -42,7 +42,8 @@ MULTEVAL = [str(c) for c in load_golden("multeval.npz")["cases"]]
 
 
 @pytest.mark.parametrize("precision,tol,algo", [("double", FP64_TOL, "auto"),
-                                                ("df64", FP64_TOL, "auto"),
+                                                ("df64", FP64_TOL, "dense"),
+                                                ("df64", FP64_TOL, "subspace"),
                                                 ("float", FP32_TOL, "dense"),
                                                 ("float", FP32_TOL, "subspace")])
 @pytest.mark.parametrize("name", MULTEVAL)
@@ -299,6 +300,85 @@ def test_reference_callers_drive_the_operator_unchanged():
     assert abs(cg.getNumberIterations() - int(g[name + "_iterations"])) <= 2
 
 
+@pytest.mark.parametrize("algo", ["dense", "subspace"])
+def test_df64_at_cell_boundaries_and_outside_the_cube(oracle, algo):
+    """Coordinates on dyadic cell boundaries, one double ulp and 1e-9 either side of them, on the
+    cube faces and outside [0, 1]: the float-float kernels follow the FP64 value, not its float
+    high part, in the choice of cell (checked against the oracle's FP64 evaluation)."""
+    rng = np.random.default_rng(41)
+    dim, level = 5, 5
+    grid = sg.Grid.createLinearGrid(dim)
+    grid.getGenerator().regular(level)
+    m = 20000
+    nodes = rng.integers(0, 2 ** level + 1, (m, dim)) / 2.0 ** level
+    shift = rng.choice([0.0, 1e-9, -1e-9, 3e-8, -3e-8, 1e-12], (m, dim))
+    x = nodes + shift
+    ulp = rng.integers(0, 3, (m, dim))  # 0: as is, 1: next double up, 2: next double down
+    x = np.where(ulp == 1, np.nextafter(x, 2.0), np.where(ulp == 2, np.nextafter(x, -1.0), x))
+    x[:50, 0] = -1e-9
+    x[50:100, 1] = 1.0 + 1e-9
+    x[100:200] = rng.random((100, dim))
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    a = rng.standard_normal(grid.getSize())
+    ref = oracle.stream(x).mult(lp, ix, a)
+    op = _op(grid, x, "df64", algo)
+    out = np.zeros(m)
+    op.mult(a, out)
+    assert rel_err(out, ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("dim,level", [(1, 14), (2, 9), (3, 6), (12, 3)])
+@pytest.mark.parametrize("precision,tol", [("float", FP32_TOL), ("df64", FP64_TOL)])
+def test_subspace_shapes_match_oracle(oracle, dim, level, precision, tol):
+    """Subspace kernels on grids with few wide subspaces (d=1 level 14: 8192 cells in one
+    subspace, beyond the shared-memory sums of the owner-computes multTranspose, so FP32 takes the
+    fixed-point scatter and df64 the dense kernel) and with many narrow ones (d=12 level 3)."""
+    rng = np.random.default_rng(dim * 100 + level)
+    grid = sg.Grid.createLinearGrid(dim)
+    grid.getGenerator().regular(level)
+    m = 30000
+    x = rng.random((m, dim))
+    x[:20] = np.round(x[:20] * 2 ** level) / 2 ** level  # on cell boundaries
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    a = rng.standard_normal(grid.getSize())
+    v = rng.standard_normal(m)
+    if precision == "float":
+        # FP32 inputs: rounding x moves 2^l x by up to 2^(l-25), and the hats with it
+        tol = max(tol, 2.0 ** (level - 23))
+    else:
+        # float-float inputs hold 48 of x's 53 bits: 2^l x moves by up to 2^(l-49)
+        tol = max(tol, 2.0 ** (level - 47))
+    st = oracle.stream(x)
+    op = _op(grid, x, precision, "subspace")
+    out, outt = np.zeros(m), np.zeros(grid.getSize())
+    op.mult(a, out)
+    op.multTranspose(v, outt)
+    assert rel_err(out, st.mult(lp, ix, a)) < tol
+    assert rel_err(outt, st.mult_transpose(lp, ix, v)) < tol
+
+
+def test_inner_tolerance_knob():
+    """params "inner_tol": any value in (0, 1) reaches the same FP64 solution; others raise."""
+    g = load_golden("cgfit.npz")
+    name = "d4_l4"
+    grid = _grid_from(g, name)
+    for tol in ("1e-2", "1e-5"):
+        cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                    sg.OperationMultipleEvalSubType.CUDA,
+                                                    parameters={"inner_tol": tol})
+        op = sg.createOperationMultipleEval(grid, g[name + "_x"], cfg)
+        alpha, _, _ = op.fit(g[name + "_y"], float(g[name + "_lambda"]), 5000, 1e-10,
+                             mode=sg.SGMEV_SOLVE_MIXED)
+        assert rel_err(alpha, g[name + "_alpha"]) < 1e-6
+        op.close()
+    for bad in ("0", "1.5", "x"):
+        cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                    sg.OperationMultipleEvalSubType.CUDA,
+                                                    parameters={"inner_tol": bad})
+        with pytest.raises(Exception):
+            sg.createOperationMultipleEval(grid, g[name + "_x"], cfg)
+
+
 def test_df64_matches_native_fp64_at_full_size():
     """FP64-accurate float-float kernels against the native FP64 kernels at the regression-fit
     workload size (d=10, level 5, 2^20 points)."""
@@ -311,7 +391,12 @@ def test_df64_matches_native_fp64_at_full_size():
     v = rng.standard_normal(m)
     out64, outdf = np.zeros(m), np.zeros(m)
     op64 = _op(grid, x, "double")
-    opdf = _op(grid, x, "df64")
+    opdf = _op(grid, x, "df64", "dense")
+    opsub = _op(grid, x, "df64", "subspace")
+    outsub = np.zeros(m)
+    opsub.mult(a, outsub)
+    op64.mult(a, out64)
+    assert rel_err(outsub, out64) < FP64_TOL
     op64.mult(a, out64)
     opdf.mult(a, outdf)
     assert rel_err(outdf, out64) < FP64_TOL
@@ -348,7 +433,7 @@ def test_adjoint_and_linearity_at_full_size(algo):
     rhs = float(a @ Btv)
     assert abs(lhs - rhs) <= 1e-5 * (np.abs(Ba).sum() * np.abs(v).max())
     # against the FP64-accurate kernels at full size
-    ref = _op(grid, x, "df64")
+    ref = _op(grid, x, "df64", "dense")
     Ba64 = np.zeros(m)
     ref.mult(a, Ba64)
     assert rel_err(Ba, Ba64) < FP32_TOL

@@ -1,27 +1,31 @@
 """The FP32 index arithmetic of the subspace-skipping kernels (sgpp_gb300/csrc/subspace.cu),
-emulated with numpy float32 operations: for every level 1..20 the cell index stays inside
-[0, 2^{l-1} - 1] and the hat of the chosen cell equals the exact hat of x's cell, for random
-points, the cube faces, dyadic nodes, their float neighbours and points outside [0, 1]."""
+emulated exactly on the CPU: for every level 1..20 the cell index stays inside [0, 2^{l-1} - 1]
+and the hat of the chosen cell equals the hat of the point's cell, for random points, the cube
+faces, dyadic nodes, their float neighbours and points outside [0, 1]; for the float-float
+(df64) kernel the hat pair is the exact hat of x_hi + x_lo."""
+import math
+from fractions import Fraction
+
 import numpy as np
 
 F = np.float32
-M = F(12582912.0)          # 1.5 * 2^23
-M_BITS = np.uint32(0x4B400000)
+MAGIC = 2.0 ** 23
 
 
 def kernel_arith(x, S, L):
+    """FP32 kernel: r = fma_rd(xc, S, 2^23), t = fma(x, L, fma(r, -2, 2^24 - 1))."""
     xc = np.minimum(np.maximum(x, F(0)), F(0.99999994))
-    y5 = (np.float64(xc) * np.float64(S) - 0.5).astype(np.float32)  # fma: one rounding
-    r = (y5 + M).astype(np.float32)
-    k = (r.view(np.uint32) - M_BITS).astype(np.int64)
-    n_i = ((r - M).astype(np.float32) * F(-2) - F(1)).astype(np.float32)
-    t = (np.float64(x) * np.float64(L) + np.float64(n_i)).astype(np.float32)
-    return k, np.clip(F(1) - np.abs(t), 0, 1)
+    k = np.floor(np.float64(xc) * float(S))          # xc S is exact; rounding down gives floor
+    r = MAGIC + k                                    # in [2^23, 2^24): spacing 1, exact
+    n_i = r * -2.0 + (2.0 ** 24 - 1.0)               # -(2k + 1), exact
+    t = (np.float64(x) * float(L) + n_i).astype(np.float32)  # exact in FP64, one FP32 rounding
+    return k.astype(np.int64), np.clip(F(1) - np.abs(t), 0, 1)
 
 
-def test_magic_constant_with_half_is_not_fp32():
-    # the reason the kernels subtract 0.5 in a separate step
-    assert float(np.float32(12582911.5)) != 12582911.5
+def test_round_down_magic_gives_floor():
+    # 2^23 + k for k in [0, 2^23) are consecutive floats: the round-down addend yields floor
+    assert np.float32(MAGIC + 1) - np.float32(MAGIC) == 1.0
+    assert float(np.float32(2.0 ** 24 - 1)) == 2.0 ** 24 - 1
 
 
 def test_cell_index_in_range_and_hat_exact():
@@ -40,3 +44,62 @@ def test_cell_index_in_range_and_hat_exact():
         exact = np.maximum(1 - np.abs(xd * float(L) - (2 * kt + 1)), 0)
         worst = max(worst, float(np.abs(np.float64(h) - exact).max()))
     assert worst < 1e-7
+
+
+def _f32_down(q: Fraction) -> np.float32:
+    """Largest float32 <= q."""
+    f = np.float32(float(q))
+    while Fraction(float(f)) > q:
+        f = np.nextafter(f, F(-np.inf))
+    while Fraction(float(np.nextafter(f, F(np.inf)))) <= q:
+        f = np.nextafter(f, F(np.inf))
+    return f
+
+
+def _f32_near(q: Fraction) -> np.float32:
+    """float32 nearest to q (ties to even)."""
+    f = _f32_down(q)
+    up = np.nextafter(f, F(np.inf))
+    d0, d1 = q - Fraction(float(f)), Fraction(float(up)) - q
+    if d1 < d0 or (d1 == d0 and (int(up.view(np.uint32)) & 1) == 0):
+        return up
+    return f
+
+
+def df_kernel_arith(xh, xl, L):
+    """df64 kernel per dimension for a point inside (0, 1): returns (k, hat_hi, hat_lo)."""
+    Lq = Fraction(float(L))
+    sl = F(L) * xl                                   # exact (power of two)
+    t2 = _f32_down(Fraction(float(xh)) * Lq + Fraction(float(sl)))
+    rr = _f32_down(Fraction(float(t2)) / 2 + Fraction(MAGIC))
+    m2k = _f32_near(Fraction(float(rr)) * -2 + Fraction(2 ** 24))
+    a = _f32_near(Fraction(float(xh)) * Lq + Fraction(float(m2k)))
+    b = _f32_near(-Fraction(float(xh)) * Lq + Fraction(float(F(2) - m2k)))
+    c = F(F(2) * sl) + F(a - b)                      # fma(2, sl, a - b): 2 sl is exact
+    rise = c <= 0
+    k = int(float(rr) - MAGIC)
+    return k, (a if rise else b), (sl if rise else -sl)
+
+
+def test_float_float_cell_and_hat_exact():
+    """df64 subspace kernel: the cell of x_hi + x_lo (not of x_hi alone) and an exact hat pair,
+    for points within a float ulp of cell boundaries, random points and the (0, 1) filter."""
+    rng = np.random.default_rng(1)
+    for level in range(1, 21):
+        S, L = 2.0 ** (level - 1), 2.0 ** level
+        b = rng.integers(0, int(S) + 1, 150) / S
+        x = np.concatenate([b + rng.normal(0, 1e-8, b.size) * rng.choice([0, 0.1, 1], b.size),
+                            rng.random(100), np.array([0, 1, 1 - 1e-17, 1e-17, -1e-17, 1 - 2e-8])])
+        xh = x.astype(np.float32)
+        xl = (x - xh.astype(np.float64)).astype(np.float32)
+        for h, lo in zip(xh, xl):
+            xq = Fraction(float(h)) + Fraction(float(lo))
+            inside = (h > 0 or (h == 0 and lo > 0)) and (h < 1 or (h == 1 and lo < 0))
+            assert inside == (0 < xq < 1)
+            if not inside:
+                continue  # every Linear-grid hat is 0 outside (0, 1): the kernel writes 0
+            k, hh, hl = df_kernel_arith(h, lo, L)
+            kt = math.floor(xq * int(S))
+            assert 0 <= k <= S - 1 and k == kt, (level, h, lo)
+            exact = max(1 - abs(xq * int(L) - (2 * kt + 1)), 0)
+            assert Fraction(float(hh)) + Fraction(float(hl)) == exact, (level, h, lo)
