@@ -426,6 +426,7 @@ __global__ void __launch_bounds__(kMulttThreads) sub_multt_kernel(
 // clamp. FP32: the per-dimension product is the one of the mult kernel. DF: as sub_mult_df_kernel,
 // with float-float per-tile sums.
 constexpr int kOwnMaxThreads = 512, kOwnTile = 256;
+constexpr int kActOwnThreads = 512;  // FP32 owner kernel (128-thread CTAs measured slower)
 
 template <int DIM, bool DF>
 struct OwnLayout {
@@ -478,7 +479,7 @@ __device__ __forceinline__ void own_stage_tile(float* s_pt, int64_t tile,
 }
 
 template <int DIM, bool DF>
-__global__ void __launch_bounds__(kOwnMaxThreads, DF ? 1 : 2) sub_multt_own_kernel(
+__global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_multt_own_kernel(
     const int4* __restrict__ desc, const int4* __restrict__ sinfo, int n_sub, int cmax,
     int total, const float* __restrict__ xh_t, const float* __restrict__ xl_t, int64_t mpad,
     int64_t m, const float* __restrict__ vh, const float* __restrict__ vl, int64_t n_tiles,
@@ -675,7 +676,7 @@ __device__ __forceinline__ void act_own_tile_dyn(const float* __restrict__ s_pt,
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(kOwnMaxThreads, 2) sub_multt_act_kernel(
+__global__ void __launch_bounds__(kActOwnThreads, 2) sub_multt_act_kernel(
     const int4* __restrict__ act, const int4* __restrict__ sact, int n_sub, int cmax, int total,
     const float* __restrict__ xt, int64_t mpad, int64_t m, const float* __restrict__ v,
     int64_t n_tiles, double* __restrict__ rows) {
@@ -839,14 +840,15 @@ cudaError_t launch_multt(const SubPlan& p, cudaStream_t s, const float* xt, int6
   return cudaGetLastError();
 }
 
-int own_threads(const SubPlan& p) {
-  return static_cast<int>(std::min<int64_t>(kOwnMaxThreads, (p.n_sub + 31) / 32 * 32));
+int own_threads(const SubPlan& p, bool df) {
+  return static_cast<int>(std::min<int64_t>(df ? kOwnMaxThreads : kActOwnThreads,
+                                            (p.n_sub + 31) / 32 * 32));
 }
 
 size_t own_smem(const SubPlan& p, int dim, bool df) {
   const int w = df ? (2 * dim + 2 + 3) / 4 * 4 : (dim + 1 + 3) / 4 * 4;
   return sizeof(float) * kOwnTile * w +
-         (df ? sizeof(float2) : sizeof(float)) * static_cast<size_t>(p.cmax) * own_threads(p);
+         (df ? sizeof(float2) : sizeof(float)) * static_cast<size_t>(p.cmax) * own_threads(p, df);
 }
 
 template <int DIM, bool DF>
@@ -855,7 +857,7 @@ cudaError_t launch_multt_own(const SubPlan& p, cudaStream_t s, const float* xh, 
                              int num_sms) {
   auto kern = sub_multt_own_kernel<DIM, DF>;
   const size_t sm = own_smem(p, DIM, DF);
-  const int nth = own_threads(p);
+  const int nth = own_threads(p, DF);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(sm));
   if (e != cudaSuccess) return e;
@@ -878,7 +880,7 @@ cudaError_t launch_multt_own(const SubPlan& p, cudaStream_t s, const float* xh, 
 
 size_t act_own_smem(const SubPlan& p, int dim) {
   return sizeof(float) * kOwnTile * ((2 + 2 * dim + 3) / 4 * 4) +
-         sizeof(float) * static_cast<size_t>(p.cmax) * own_threads(p);
+         sizeof(float) * static_cast<size_t>(p.cmax) * own_threads(p, false);
 }
 
 template <int DIM>
@@ -886,7 +888,7 @@ cudaError_t launch_multt_act(const SubPlan& p, cudaStream_t s, const float* xt, 
                              int64_t m, const float* v, int num_sms) {
   auto kern = sub_multt_act_kernel<DIM>;
   const size_t sm = act_own_smem(p, DIM);
-  const int nth = own_threads(p);
+  const int nth = own_threads(p, false);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(sm));
   if (e != cudaSuccess) return e;
@@ -1018,7 +1020,7 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
     *err = "subspace plan: device query failed";
     return false;
   }
-  const int nth = own_threads(*p);
+  const int nth = own_threads(*p, false);
   p->row_cap = std::min<int64_t>(static_cast<int64_t>(sms) * std::min(16, std::max(2, 1024 / nth)),
                                  std::max<int64_t>(1, (int64_t(256) << 20) / (8 * offset)));
   bool ok = cudaMalloc(&p->desc, sizeof(int4) * desc.size()) == cudaSuccess &&
