@@ -287,7 +287,9 @@ def run_ours(args):
                ("mult_sub32", sg.SGMEV_KERNEL_MULT_SUB32),
                ("multT_sub32", sg.SGMEV_KERNEL_MULTT_SUB32),
                ("mult_subdf64", sg.SGMEV_KERNEL_MULT_SUBDF),
-               ("multT_subdf64", sg.SGMEV_KERNEL_MULTT_SUBDF))}
+               ("multT_subdf64", sg.SGMEV_KERNEL_MULTT_SUBDF),
+               ("mult_mat32", sg.SGMEV_KERNEL_MULT_MAT32),
+               ("multT_mat32", sg.SGMEV_KERNEL_MULTT_MAT32))}
     op.profile(False)
     alpha = d_alpha.cpu().numpy()
     err = float(np.abs(alpha - alpha_ref).max() / np.abs(alpha_ref).max())

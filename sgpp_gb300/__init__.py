@@ -76,6 +76,8 @@ SGMEV_KERNEL_MULT_SUB32 = 6
 SGMEV_KERNEL_MULTT_SUB32 = 7
 SGMEV_KERNEL_MULT_SUBDF = 8
 SGMEV_KERNEL_MULTT_SUBDF = 9
+SGMEV_KERNEL_MULT_MAT32 = 10
+SGMEV_KERNEL_MULTT_MAT32 = 11
 
 
 # ---- exceptions (base/src/sgpp/base/exception/) --------------------------------------------
@@ -462,7 +464,7 @@ class OperationMultiEvalCuda:
             left, right = bb.arrays()
         h = ctypes.c_void_p(None)
         knobs = {k: str(v) for k, v in (params or {}).items()
-                 if k in ("precond", "algo", "inner_tol")}
+                 if k in ("precond", "algo", "inner_tol", "materialize", "materialize_multt")}
         pj = json.dumps(knobs).encode() if knobs else None
         _check(L.sgmev_create(ctypes.byref(h), st.getDimension(), st.getSize(), _vp(lp), _vp(ix),
                               self.dataset.shape[0], _vp(self.dataset), _vp(left), _vp(right),

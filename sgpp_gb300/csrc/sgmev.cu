@@ -130,6 +130,9 @@ struct sgmev_op {
   int64_t launches = 0;
   bool precond = false;  // Jacobi-preconditioned inner CG in the mixed fits (params "precond")
   double inner_tol = 1e-4;  // relative tolerance of the inner solves of mixed fits ("inner_tol")
+  int mat_mode = 1;         // materialised FP32 products: 0 off, 1 auto, 2 on ("materialize")
+  bool mat_multt = false;   // multTranspose streams them too ("materialize_multt")
+  bool mat_failed = false;  // a build was refused or failed for the current grid
   int algo = 2;          // FP32 products: 0 dense, 1 subspace, 2 auto (params "algo")
   SubPlan sub;           // subspace tables of the current grid
   bool sub_ok = false;   // sub is built and chosen for the FP32 products
@@ -142,8 +145,8 @@ struct sgmev_op {
   std::vector<cudaEvent_t> prof_events;  // pool, 2 per launch
   std::vector<int> prof_kind;            // kind of launch i
   size_t prof_used = 0;                  // launches recorded since the last reset
-  int64_t prof_count[10] = {0};
-  double prof_seconds[10] = {0.0};
+  int64_t prof_count[12] = {0};
+  double prof_seconds[12] = {0.0};
 };
 
 namespace sgmev {
@@ -159,9 +162,11 @@ enum {
   KIND_MULT_SUB32 = 6,
   KIND_MULTT_SUB32 = 7,
   KIND_MULT_SUBDF = 8,
-  KIND_MULTT_SUBDF = 9
+  KIND_MULTT_SUBDF = 9,
+  KIND_MULT_MAT32 = 10,
+  KIND_MULTT_MAT32 = 11
 };
-constexpr int kKinds = 10;
+constexpr int kKinds = 12;
 
 template <typename T>
 static int kind_mult() { return sizeof(T) == 4 ? KIND_MULT_FP32 : KIND_MULT_FP64; }
@@ -636,6 +641,37 @@ static int64_t multt_tile_pts(const sgmev_op* op, int prec) {
 // ---------------------------------------------------------------------------------------
 // device-side products on padded device vectors
 // ---------------------------------------------------------------------------------------
+// Materialised FP32 subspace products: built on the first FP32 product after the grid was
+// staged, when the "materialize" knob allows it and they fit (auto: at most half of the free
+// device memory and 64 GiB); a failed build falls back to the on-the-fly kernels for this grid.
+static bool mat_ready(sgmev_op* op) {
+  using namespace sgmev;
+  if (op->sub.pmat) return true;
+  if (op->mat_mode == 0 || op->mat_failed || !subspace_mat_fits(op->sub)) return false;
+  const int64_t bytes = subspace_mat_bytes(op->sub, op->mpad);
+  if (op->mat_mode == 1) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      (void)cudaGetLastError();
+      op->mat_failed = true;
+      return false;
+    }
+    if (static_cast<double>(bytes) > std::min(0.5 * static_cast<double>(free_b), 64.0 * (1ull << 30))) {
+      op->mat_failed = true;
+      return false;
+    }
+  }
+  if (subspace_materialize(&op->sub, op->stream, op->xt32, op->mpad, op->m, op->num_sms) != cudaSuccess) {
+    (void)cudaGetLastError();
+    cudaFree(op->sub.pmat);
+    op->sub.pmat = nullptr;
+    op->mat_failed = true;
+    return false;
+  }
+  op->launches += 1;
+  return true;
+}
+
 // Inputs per precision: FP64 a64; FP32 a32; DF64 (a32, a32lo) — all padded to npad.
 // out64 / out32 [mpad] (zero beyond m) = B a over data range [j_begin, j_end).
 static int dev_mult(sgmev_op* op, int prec, const double* a64, const float* a32,
@@ -659,6 +695,12 @@ static int dev_mult(sgmev_op* op, int prec, const double* a64, const float* a32,
     SGMEV_TRY(run_mult_df(op, a32, a32lo, j_begin, j_end, &p));
     if (out64) SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
     if (out32) SGMEV_TRY((run_reduce<float2, float>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out32, nullptr, 0.0)));
+  } else if (op->sub_ok && mat_ready(op)) {
+    const long ev = prof_begin(op, KIND_MULT_MAT32);
+    SGMEV_CUDA(subspace_mult_mat(op->sub, op->stream, op->xt32, op->mpad, op->m, a32, out32, out64,
+                                 j_begin, j_end, op->num_sms));
+    prof_end(op, ev);
+    op->launches += 2;
   } else if (op->sub_ok) {
     const long ev = prof_begin(op, KIND_MULT_SUB32);
     SGMEV_CUDA(subspace_mult(op->sub, op->stream, op->xt32, op->mpad, op->m, a32, out32, out64,
@@ -693,6 +735,13 @@ static int dev_multt(sgmev_op* op, int prec, const double* v64, const float* v32
   } else if (prec == SGMEV_DF64) {
     SGMEV_TRY(run_multt_df(op, v32, v32lo, g_begin, g_end, &p));
     SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->npad, g_begin, valid, g_end, out64, add, scale)));
+  } else if (op->sub_ok && op->mat_multt && mat_ready(op)) {
+    // the subspace sums produce every grid entry at once (the range is a subset of them)
+    const long ev = prof_begin(op, KIND_MULTT_MAT32);
+    SGMEV_CUDA(subspace_multt_mat(op->sub, op->stream, op->xt32, op->mpad, op->m, v32, op->npad,
+                                  out64, add, scale, op->num_sms));
+    prof_end(op, ev);
+    op->launches += 3;
   } else if (op->sub_ok) {
     // the subspace scatter produces every grid entry at once (the range is a subset of it)
     const long ev = prof_begin(op, KIND_MULTT_SUB32);
@@ -842,6 +891,7 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
   // instruction count per data point (one basis function per subspace, ~8 per active dimension
   // and ~10 per subspace, against 3 per dimension for every grid point)
   op->sub_ok = false;
+  op->mat_failed = false;
   subspace_free(&op->sub);
   if (op->algo != 0 && n > 0) {
     std::string why;
@@ -984,6 +1034,12 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
     return fail(SGMEV_ERR_INVALID, "params: algo must be \"dense\", \"subspace\" or \"auto\"");
   if (!precond.empty() && precond != "jacobi" && precond != "none")
     return fail(SGMEV_ERR_INVALID, "params: precond must be \"jacobi\" or \"none\"");
+  const std::string mat = json_string(params_json, "materialize");
+  if (!mat.empty() && mat != "auto" && mat != "on" && mat != "off")
+    return fail(SGMEV_ERR_INVALID, "params: materialize must be \"auto\", \"on\" or \"off\"");
+  const std::string mat_t = json_string(params_json, "materialize_multt");
+  if (!mat_t.empty() && mat_t != "on" && mat_t != "off")
+    return fail(SGMEV_ERR_INVALID, "params: materialize_multt must be \"on\" or \"off\"");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
@@ -996,6 +1052,8 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   op->m = n_data;
   op->mpad = std::max<int64_t>(round_up(std::max<int64_t>(n_data, 1), kMPadTo), kMPadTo);
   op->precond = precond == "jacobi";
+  op->mat_mode = mat == "off" ? 0 : (mat == "on" ? 2 : 1);
+  op->mat_multt = mat_t == "on";
   {
     const std::string it = json_string(params_json, "inner_tol");
     if (!it.empty()) {

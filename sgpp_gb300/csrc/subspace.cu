@@ -31,15 +31,15 @@
 
 #include "kernels.cuh"
 #include "subspace.h"
+#include "subspace_common.cuh"
 
 namespace sgmev {
 
 namespace {
 
+using namespace subk;
+
 constexpr int kSDT = 64;                  // subspaces per shared-memory descriptor tile
-constexpr unsigned kMagicBits = 0x4B000000u;  // bits of 2^23
-constexpr float kMagic = 8388608.0f;          // 2^23
-constexpr float kTwoMagic = 16777216.0f;      // 2^24
 constexpr float kBelowOne = 0.99999994f;      // largest float < 1
 
 constexpr int kMulttThreads = 256, kMulttR = 2;
@@ -105,10 +105,6 @@ __device__ __forceinline__ void eval_subspace(const Pt<DIM, R>& pt, const int4* 
 // stays inside its subspace.
 constexpr int kActThreads = 256, kActR = 2;  // the mult kernel: tiles of 512 points, 2 per thread
 constexpr int kActUnrolled = 6;              // active-dimension counts with unrolled evaluation
-constexpr float kActLow = 7.88860905e-31f;   // 2^-100
-
-// whether a coordinate lies in the evaluated domain
-__device__ __forceinline__ bool act_inside(float x) { return x > kActLow && x < 1.0f; }
 
 // p_r *= prod_{a < na} h(x_{r, t_a}) / h1(x_{r, t_a}), flat_r += sum_a bits(cell) * stride_a, for the
 // kActR points of this thread; xr points at the thread's (x, 1 / h1) pairs, dimension t at
@@ -425,8 +421,9 @@ __global__ void __launch_bounds__(kMulttThreads) sub_multt_kernel(
 // gives them v = 0 and coordinates 0.5, which keeps the cell arithmetic inside the subspace with no
 // clamp. FP32: the per-dimension product is the one of the mult kernel. DF: as sub_mult_df_kernel,
 // with float-float per-tile sums.
-constexpr int kOwnMaxThreads = 512, kOwnTile = 256;
+constexpr int kOwnMaxThreads = 512;
 constexpr int kActOwnThreads = 512;  // FP32 owner kernel (128-thread CTAs measured slower)
+constexpr int kActFlushTiles = 4;    // FP32 owner kernel: tiles summed in FP32 per flush
 
 template <int DIM, bool DF>
 struct OwnLayout {
@@ -582,43 +579,6 @@ __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_multt_own_kernel(
 // Owner-computes multTranspose with active-dimension evaluation (FP32): as sub_multt_own_kernel,
 // with rows (H1 * v, 0, (x_0, 1 / h1(x_0)), ..., (x_{d-1}, 1 / h1(x_{d-1}))); a thread's active
 // dimensions are held in registers for up to 4 of them (unrolled per count), else looped over.
-template <int DIM>
-struct ActRow {
-  static constexpr int W = (2 + 2 * DIM + 3) / 4 * 4;
-};
-
-template <int DIM>
-__device__ __forceinline__ void act_stage_tile(float* s_pt, int64_t tile,
-                                               const float* __restrict__ xt, int64_t mpad,
-                                               int64_t m, const float* __restrict__ v) {
-  constexpr int W = ActRow<DIM>::W;
-  const int64_t j0 = tile * kOwnTile;
-  for (int k = threadIdx.x; k < kOwnTile * DIM; k += blockDim.x) {
-    const int t = k / kOwnTile, jj = k - t * kOwnTile;
-    s_pt[jj * W + 2 + 2 * t] = xt[static_cast<int64_t>(t) * mpad + j0 + jj];
-  }
-  __syncthreads();
-  for (int jj = threadIdx.x; jj < kOwnTile; jj += blockDim.x) {
-    float* row = s_pt + jj * W;
-    const int64_t j = j0 + jj;
-    bool inside = j < m;
-#pragma unroll
-    for (int t = 0; t < DIM; ++t) inside = inside && act_inside(row[2 + 2 * t]);
-    float h1p = 1.0f;
-#pragma unroll
-    for (int t = 0; t < DIM; ++t) {
-      const float x = inside ? row[2 + 2 * t] : 0.5f;
-      const float h1 = fminf(2.0f * x, 2.0f - 2.0f * x);
-      h1p *= h1;
-      row[2 + 2 * t] = x;
-      row[3 + 2 * t] = 1.0f / h1;
-    }
-    row[0] = inside ? h1p * v[j] : 0.0f;
-    row[1] = 0.0f;
-  }
-  __syncthreads();
-}
-
 // one tile of points for a subspace with NA active dimensions: s_acc[c * nth + tid] += p_j
 template <int NA>
 __device__ __forceinline__ void act_own_tile(const float* __restrict__ s_pt, int w,
@@ -695,6 +655,7 @@ __global__ void __launch_bounds__(kActOwnThreads, 2) sub_multt_act_kernel(
     const int4* q = act + static_cast<int64_t>(active ? sid : 0) * DIM;
     for (int c = 0; c < info.y; ++c) s_acc[c * nth + tid] = 0.0f;
     bool first = true;
+    int since = 0;  // tiles summed in s_acc since the last flush
     for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
       __syncthreads();  // the previous tile's rows are no longer read
       act_stage_tile<DIM>(s_pt, tile, xt, mpad, m, v);
@@ -708,14 +669,21 @@ __global__ void __launch_bounds__(kActOwnThreads, 2) sub_multt_act_kernel(
           case 4: act_own_tile<(DIM < 4 ? DIM : 4)>(s_pt, W, q, cbase, cmax, s_acc, nth, tid); break;
           default: act_own_tile_dyn(s_pt, W, q, info.w, cbase, cmax, s_acc, nth, tid); break;
         }
-        for (int c = 0; c < info.y; ++c) {
-          float& a = s_acc[c * nth + tid];
-          double* dst = row + offset + c;
-          *dst = first ? static_cast<double>(a) : *dst + static_cast<double>(a);
-          a = 0.0f;
-        }
       }
-      first = false;
+      ++since;
+      // FP32 sums over kActFlushTiles tiles (1024 points), then into the FP64 row
+      if (since == kActFlushTiles || tile + gridDim.x >= n_tiles) {
+        if (active) {
+          for (int c = 0; c < info.y; ++c) {
+            float& a = s_acc[c * nth + tid];
+            double* dst = row + offset + c;
+            *dst = first ? static_cast<double>(a) : *dst + static_cast<double>(a);
+            a = 0.0f;
+          }
+        }
+        first = false;
+        since = 0;
+      }
     }
     if (active && first)
       for (int c = 0; c < info.y; ++c) row[offset + c] = 0.0;
@@ -1051,6 +1019,7 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
 void subspace_free(SubPlan* p) {
   cudaFree(p->desc);
   cudaFree(p->sinfo);
+  cudaFree(p->pmat);
   cudaFree(p->act);
   cudaFree(p->sact);
   cudaFree(p->rows);
@@ -1065,13 +1034,28 @@ void subspace_free(SubPlan* p) {
 
 #define SUB_DIMS(F) F(1) F(2) F(3) F(4) F(5) F(6) F(7) F(8) F(9) F(10) F(11) F(12) F(13) F(14) F(15) F(16)
 
-cudaError_t subspace_mult(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
-                          int64_t m, const float* alpha32, float* out32, double* out64,
-                          int64_t j_begin, int64_t j_end, int num_sms) {
+cudaError_t subspace_scatter_alpha(const SubPlan& p, cudaStream_t s, const float* alpha32) {
   cudaError_t e = cudaMemsetAsync(p.asub, 0, sizeof(float) * p.total, s);
   if (e != cudaSuccess) return e;
   scatter_alpha_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.n + 255) / 256)), 256, 0, s>>>(
       alpha32, p.pos, p.n, p.asub);
+  return cudaGetLastError();
+}
+
+cudaError_t subspace_finish_rows(const SubPlan& p, cudaStream_t s, int64_t nrows, int64_t npad,
+                                 double* out64, const double* add, double scale_add) {
+  sum_rows_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.total + 255) / 256)), 256, 0, s>>>(
+      p.rows, static_cast<int>(nrows), p.total, reinterpret_cast<double*>(p.acc));
+  gather_sums_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (npad + 255) / 256)), 256, 0, s>>>(
+      reinterpret_cast<const double*>(p.acc), p.pos, p.n, npad, add, scale_add, out64);
+  return cudaGetLastError();
+}
+
+cudaError_t subspace_mult(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
+                          int64_t m, const float* alpha32, float* out32, double* out64,
+                          int64_t j_begin, int64_t j_end, int num_sms) {
+  cudaError_t e = subspace_scatter_alpha(p, s, alpha32);
+  if (e != cudaSuccess) return e;
   const int64_t tile = kActR * kActThreads;
   const int64_t t0 = j_begin / tile;
   const int64_t nt = (j_end + tile - 1) / tile - t0;

@@ -33,6 +33,11 @@ struct SubPlan {
   int cmax = 0;           // largest cell count of a subspace
   double* rows = nullptr;  // [row_cap * total] per-CTA partial sums (owner-computes multT)
   int64_t row_cap = 0;
+  // materialised products P[j / 4][s][j % 4] (s padded to s_pad, a multiple of 32), for the data
+  // of mat_mpad padded points; nullptr when not built
+  float4* pmat = nullptr;
+  int64_t s_pad = 0;
+  int64_t mat_mpad = 0;
 };
 
 // largest position count the shared-memory kernels handle (two 4-byte accumulators per position in
@@ -66,6 +71,26 @@ bool subspace_owner_fits(const SubPlan& p, bool df);
 cudaError_t subspace_multt(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
                            int64_t m, const float* v32, int64_t npad, double* out64,
                            const double* add, double scale_add, int num_sms);
+
+// internal steps shared by the subspace sources: alpha (FP32, [n]) into asub in position order,
+// and out64 = gather of the sum of `nrows` partial rows (+ scale_add * add)
+cudaError_t subspace_scatter_alpha(const SubPlan& p, cudaStream_t s, const float* alpha32);
+cudaError_t subspace_finish_rows(const SubPlan& p, cudaStream_t s, int64_t nrows, int64_t npad,
+                                 double* out64, const double* add, double scale_add);
+
+// Materialised FP32 products: bytes they take for mpad points, whether the kernels' shared memory
+// fits the plan, building them (allocates; the data xt must not change afterwards), and the
+// products that stream them (same contracts as subspace_mult / subspace_multt).
+int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad);
+bool subspace_mat_fits(const SubPlan& p);
+cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xt, int64_t mpad,
+                                 int64_t m, int num_sms);
+cudaError_t subspace_mult_mat(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
+                              int64_t m, const float* alpha32, float* out32, double* out64,
+                              int64_t j_begin, int64_t j_end, int num_sms);
+cudaError_t subspace_multt_mat(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
+                               int64_t m, const float* v32, int64_t npad, double* out64,
+                               const double* add, double scale_add, int num_sms);
 
 // FP64-accurate (float-float) multTranspose: x as (xh, xl), v as (vh, vl) [mpad]
 cudaError_t subspace_multt_df(const SubPlan& p, cudaStream_t s, const float* xh, const float* xl,

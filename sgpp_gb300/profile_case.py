@@ -25,6 +25,8 @@ KINDS = {("mult", "float", "dense"): sg.SGMEV_KERNEL_MULT_FP32,
          ("multT", "float", "dense"): sg.SGMEV_KERNEL_MULTT_FP32,
          ("mult", "float", "subspace"): sg.SGMEV_KERNEL_MULT_SUB32,
          ("multT", "float", "subspace"): sg.SGMEV_KERNEL_MULTT_SUB32,
+         ("mult", "float", "materialized"): sg.SGMEV_KERNEL_MULT_MAT32,
+         ("multT", "float", "materialized"): sg.SGMEV_KERNEL_MULTT_MAT32,
          ("mult", "double", "dense"): sg.SGMEV_KERNEL_MULT_FP64,
          ("multT", "double", "dense"): sg.SGMEV_KERNEL_MULTT_FP64,
          ("mult", "df64", "dense"): sg.SGMEV_KERNEL_MULT_DF64,
@@ -37,7 +39,8 @@ def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel", choices=["mult", "multT"], default="mult")
     ap.add_argument("--precision", choices=["float", "double", "df64"], default="float")
-    ap.add_argument("--algo", choices=["dense", "subspace"], default="dense")
+    ap.add_argument("--algo", choices=["dense", "subspace", "materialized"], default="dense",
+                    help="materialized: subspace products kept in device memory (FP32)")
     ap.add_argument("--dim", type=int, default=10)
     ap.add_argument("--level", type=int, default=5)
     ap.add_argument("--points", type=int, default=1 << 22)
@@ -45,6 +48,7 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=1)
     args = ap.parse_args()
 
+    mat = args.algo == "materialized"
     rng = np.random.default_rng(7)
     grid = sg.Grid.createLinearGrid(args.dim)
     grid.getGenerator().regular(args.level)
@@ -52,8 +56,11 @@ def main() -> int:
     x = rng.random((args.points, args.dim))
     cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
                                                 sg.OperationMultipleEvalSubType.CUDA,
-                                                parameters={"precision": args.precision,
-                                                            "algo": args.algo})
+                                                parameters={
+                                                    "precision": args.precision,
+                                                    "algo": "subspace" if mat else args.algo,
+                                                    "materialize": "on" if mat else "off",
+                                                    "materialize_multt": "on" if mat else "off"})
     op = sg.createOperationMultipleEval(grid, x, cfg)
     a = rng.standard_normal(n)
     v = rng.standard_normal(args.points)

@@ -32,9 +32,15 @@ def _grid_from(g, name):
 
 
 def _op(grid, x, precision="double", algo="auto"):
+    """algo: "auto", "dense", "subspace" (hats evaluated on every call) or "materialized"
+    (subspace products kept in device memory, for mult and multTranspose)."""
+    params = {"precision": precision, "algo": "subspace" if algo == "materialized" else algo}
+    if algo in ("subspace", "materialized"):
+        params["materialize"] = "on" if algo == "materialized" else "off"
+        params["materialize_multt"] = "on" if algo == "materialized" else "off"
     cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
                                                 sg.OperationMultipleEvalSubType.CUDA,
-                                                parameters={"precision": precision, "algo": algo})
+                                                parameters=params)
     return sg.createOperationMultipleEval(grid, x, cfg)
 
 
@@ -45,7 +51,8 @@ MULTEVAL = [str(c) for c in load_golden("multeval.npz")["cases"]]
                                                 ("df64", FP64_TOL, "dense"),
                                                 ("df64", FP64_TOL, "subspace"),
                                                 ("float", FP32_TOL, "dense"),
-                                                ("float", FP32_TOL, "subspace")])
+                                                ("float", FP32_TOL, "subspace"),
+                                                ("float", FP32_TOL, "materialized")])
 @pytest.mark.parametrize("name", MULTEVAL)
 def test_mult_and_transpose_match_reference(name, precision, tol, algo):
     g = load_golden("multeval.npz")
@@ -111,7 +118,7 @@ def test_results_are_bitwise_reproducible():
     grid = _grid_from(g, name)
     x = g[name + "_x"]
     for prec, algo in (("double", "auto"), ("df64", "auto"), ("float", "dense"),
-                       ("float", "subspace")):
+                       ("float", "subspace"), ("float", "materialized")):
         op = _op(grid, x, prec, algo)
         a = np.zeros(x.shape[0])
         b = np.zeros(x.shape[0])
@@ -236,7 +243,7 @@ def test_system_apply_matches_oracle(oracle):
     opdf = _op(grid, x, "df64")
     opdf.systemApply(a, out, lam_m)
     assert rel_err(out, ref) < FP64_TOL
-    for algo in ("dense", "subspace"):
+    for algo in ("dense", "subspace", "materialized"):
         op32 = _op(grid, x, "float", algo)
         op32.systemApply(a, out, lam_m)
         assert rel_err(out, ref) < FP32_TOL
@@ -328,8 +335,10 @@ def test_df64_at_cell_boundaries_and_outside_the_cube(oracle, algo):
 
 
 @pytest.mark.parametrize("dim,level", [(1, 14), (2, 9), (3, 6), (12, 3)])
-@pytest.mark.parametrize("precision,tol", [("float", FP32_TOL), ("df64", FP64_TOL)])
-def test_subspace_shapes_match_oracle(oracle, dim, level, precision, tol):
+@pytest.mark.parametrize("precision,tol,algo", [("float", FP32_TOL, "subspace"),
+                                                ("float", FP32_TOL, "materialized"),
+                                                ("df64", FP64_TOL, "subspace")])
+def test_subspace_shapes_match_oracle(oracle, dim, level, precision, tol, algo):
     """Subspace kernels on grids with few wide subspaces (d=1 level 14: 8192 cells in one
     subspace, beyond the shared-memory sums of the owner-computes multTranspose, so FP32 takes the
     fixed-point scatter and df64 the dense kernel) and with many narrow ones (d=12 level 3)."""
@@ -349,7 +358,7 @@ def test_subspace_shapes_match_oracle(oracle, dim, level, precision, tol):
         # float-float inputs hold 48 of x's 53 bits: 2^l x moves by up to 2^(l-49)
         tol = max(tol, 2.0 ** (level - 47))
     st = oracle.stream(x)
-    op = _op(grid, x, precision, "subspace")
+    op = _op(grid, x, precision, algo)
     out, outt = np.zeros(m), np.zeros(grid.getSize())
     op.mult(a, out)
     op.multTranspose(v, outt)
@@ -406,7 +415,7 @@ def test_df64_matches_native_fp64_at_full_size():
     assert rel_err(tdf, t64) < FP64_TOL
 
 
-@pytest.mark.parametrize("algo", ["dense", "subspace"])
+@pytest.mark.parametrize("algo", ["dense", "subspace", "materialized"])
 def test_adjoint_and_linearity_at_full_size(algo):
     """Size-independent properties at the regression-fit workload size (d=10, level 5,
     2^20 points): <B a, v> = <a, B^T v>, B is linear, and the FP32 algorithms agree."""
