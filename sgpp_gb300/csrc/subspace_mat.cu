@@ -30,8 +30,10 @@ using namespace subk;
 constexpr int kMatThreads = 512;              // subspaces per pass
 constexpr int kGroups = kOwnTile / 4;         // point groups per tile
 constexpr int kMatWarps = kMatThreads / 32;
-// point groups loaded ahead of use (more in multT, which holds fewer other values in registers)
-constexpr int kMultAhead = 2, kMulttAhead = 4;
+// point groups in flight per thread: a ring of loads issued this many groups ahead of their use
+// (kGroups is a multiple of both)
+constexpr int kMultAhead = 4, kMulttAhead = 4;
+static_assert(kGroups % kMultAhead == 0 && kGroups % kMulttAhead == 0, "ring must divide a tile");
 // multT: FP32 sums over this many tiles (1024 points) before they go into the FP64 row
 constexpr int kFlushTiles = 4;
 
@@ -185,15 +187,17 @@ __device__ __forceinline__ void mult_tile(const float* __restrict__ s_pt, int w,
   MatDesc<(NA > 0 ? NA : 1)> desc;
   if (NA > 0) desc.load(q);
   const float* a_col = s_at + sid;
-  for (int g0 = 0; g0 < kGroups; g0 += kMultAhead) {
-    float4 pv[kMultAhead];
+  float4 ring[kMultAhead];
 #pragma unroll
-    for (int u = 0; u < kMultAhead; ++u) pv[u] = __ldcs(src + static_cast<int64_t>(g0 + u) * s_pad);
+  for (int u = 0; u < kMultAhead; ++u) ring[u] = __ldcs(src + static_cast<int64_t>(u) * s_pad);
+  for (int g0 = 0; g0 < kGroups; g0 += kMultAhead) {
 #pragma unroll
     for (int u = 0; u < kMultAhead; ++u) {
       const int g = g0 + u;
+      const float4 cur = ring[u];
+      if (g + kMultAhead < kGroups) ring[u] = __ldcs(src + static_cast<int64_t>(g + kMultAhead) * s_pad);
       float cv[4];
-      const float pp[4] = {pv[u].x, pv[u].y, pv[u].z, pv[u].w};
+      const float pp[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const float* row = s_pt + (4 * g + i) * w;
@@ -282,13 +286,16 @@ __device__ __forceinline__ void multt_tile(const float* __restrict__ s_pt, int w
                                            int64_t s_pad, float* __restrict__ acc, int nth) {
   MatDesc<(NA > 0 ? NA : 1)> desc;
   if (NA > 0) desc.load(q);
-  for (int g0 = 0; g0 < kGroups; g0 += kMulttAhead) {
-    float4 pv[kMulttAhead];
+  float4 ring[kMulttAhead];
 #pragma unroll
-    for (int u = 0; u < kMulttAhead; ++u) pv[u] = __ldcs(src + static_cast<int64_t>(g0 + u) * s_pad);
+  for (int u = 0; u < kMulttAhead; ++u) ring[u] = __ldcs(src + static_cast<int64_t>(u) * s_pad);
+  for (int g0 = 0; g0 < kGroups; g0 += kMulttAhead) {
 #pragma unroll
     for (int u = 0; u < kMulttAhead; ++u) {
-      const float pp[4] = {pv[u].x, pv[u].y, pv[u].z, pv[u].w};
+      const float4 cur = ring[u];
+      const int gn = g0 + u + kMulttAhead;
+      if (gn < kGroups) ring[u] = __ldcs(src + static_cast<int64_t>(gn) * s_pad);
+      const float pp[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const float* row = s_pt + (4 * (g0 + u) + i) * w;
