@@ -206,7 +206,7 @@ def op_config(args):
     """Operator configuration: the CUDA subtype with its default knobs, plus --inner-tol."""
     import sgpp_gb300 as sg
 
-    params = {}
+    params = dict(kv.split("=", 1) for kv in args.param)
     if args.inner_tol is not None:
         params["inner_tol"] = repr(args.inner_tol)
     return sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
@@ -418,6 +418,8 @@ def main():
     ap.add_argument("--plain-fp64-probe", type=int, default=1)
     ap.add_argument("--inner-tol", type=float, default=None,
                     help="inner tolerance of the mixed fits (library default when omitted)")
+    ap.add_argument("--param", action="append", default=[], metavar="KEY=VALUE",
+                    help="operator knob passed to createOperationMultipleEval (repeatable)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -86,11 +86,12 @@ SGMEV_API int sgmev_device_count(void);
  * (every grid point for every data point, the STREAMING algorithm) or subspace-skipping (one basis
  * function per subspace and data point, as the reference's DEFAULT operator; grids of dim <= 16
  * with at most 24,576 subspace positions); "auto" takes subspace when it needs fewer instructions.
- * "materialize": "auto" (default), "on" or "off" — whether the subspace FP32 mult keeps
+ * "materialize": "auto" (default), "on" or "off" — whether the subspace FP32 products keep
  * p_s(x_j) for every data point and subspace in device memory (4 bytes each, built on the first
  * FP32 product) and streams it, instead of evaluating the hats on every call; "auto" does so when
- * it takes at most half of the free device memory and 64 GiB. "materialize_multt": "off"
- * (default) or "on" — whether the FP32 multTranspose streams them too.
+ * it takes at most half of the free device memory and 64 GiB. With it, each product keeps its
+ * cell index too (1 byte; grids whose subspaces have at most 256 cells). "materialize_multt":
+ * "on" (default) or "off" — whether the FP32 multTranspose streams them too.
  */
 SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double* level_pow2,
                            const double* index, int64_t n_data, const double* data,

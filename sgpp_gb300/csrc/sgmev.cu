@@ -131,7 +131,7 @@ struct sgmev_op {
   bool precond = false;  // Jacobi-preconditioned inner CG in the mixed fits (params "precond")
   double inner_tol = 1e-4;  // relative tolerance of the inner solves of mixed fits ("inner_tol")
   int mat_mode = 1;         // materialised FP32 products: 0 off, 1 auto, 2 on ("materialize")
-  bool mat_multt = false;   // multTranspose streams them too ("materialize_multt")
+  bool mat_multt = true;    // multTranspose streams them too ("materialize_multt")
   bool mat_failed = false;  // a build was refused or failed for the current grid
   int algo = 2;          // FP32 products: 0 dense, 1 subspace, 2 auto (params "algo")
   SubPlan sub;           // subspace tables of the current grid
@@ -664,7 +664,9 @@ static bool mat_ready(sgmev_op* op) {
   if (subspace_materialize(&op->sub, op->stream, op->xt32, op->mpad, op->m, op->num_sms) != cudaSuccess) {
     (void)cudaGetLastError();
     cudaFree(op->sub.pmat);
+    cudaFree(op->sub.cmat);
     op->sub.pmat = nullptr;
+    op->sub.cmat = nullptr;
     op->mat_failed = true;
     return false;
   }
@@ -1053,7 +1055,7 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   op->mpad = std::max<int64_t>(round_up(std::max<int64_t>(n_data, 1), kMPadTo), kMPadTo);
   op->precond = precond == "jacobi";
   op->mat_mode = mat == "off" ? 0 : (mat == "on" ? 2 : 1);
-  op->mat_multt = mat_t == "on";
+  op->mat_multt = mat_t != "off";
   {
     const std::string it = json_string(params_json, "inner_tol");
     if (!it.empty()) {

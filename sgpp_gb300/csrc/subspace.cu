@@ -1020,6 +1020,7 @@ void subspace_free(SubPlan* p) {
   cudaFree(p->desc);
   cudaFree(p->sinfo);
   cudaFree(p->pmat);
+  cudaFree(p->cmat);
   cudaFree(p->act);
   cudaFree(p->sact);
   cudaFree(p->rows);

@@ -33,9 +33,11 @@ struct SubPlan {
   int cmax = 0;           // largest cell count of a subspace
   double* rows = nullptr;  // [row_cap * total] per-CTA partial sums (owner-computes multT)
   int64_t row_cap = 0;
-  // materialised products P[j / 4][s][j % 4] (s padded to s_pad, a multiple of 32), for the data
-  // of mat_mpad padded points; nullptr when not built
+  // materialised products P[j / 4][s][j % 4] (s padded to s_pad, a multiple of 32) and the cell
+  // index of each within its subspace, C[j / 4][s] (four bytes, point j % 4 in byte j % 4), for
+  // the data of mat_mpad padded points; nullptr when not built
   float4* pmat = nullptr;
+  uint32_t* cmat = nullptr;
   int64_t s_pad = 0;
   int64_t mat_mpad = 0;
 };
