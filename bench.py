@@ -289,7 +289,9 @@ def run_ours(args):
                ("mult_subdf64", sg.SGMEV_KERNEL_MULT_SUBDF),
                ("multT_subdf64", sg.SGMEV_KERNEL_MULTT_SUBDF),
                ("mult_mat32", sg.SGMEV_KERNEL_MULT_MAT32),
-               ("multT_mat32", sg.SGMEV_KERNEL_MULTT_MAT32))}
+               ("multT_mat32", sg.SGMEV_KERNEL_MULTT_MAT32),
+               ("mult_matdf64", sg.SGMEV_KERNEL_MULT_MATDF),
+               ("multT_matdf64", sg.SGMEV_KERNEL_MULTT_MATDF))}
     op.profile(False)
     alpha = d_alpha.cpu().numpy()
     err = float(np.abs(alpha - alpha_ref).max() / np.abs(alpha_ref).max())

@@ -89,9 +89,10 @@ SGMEV_API int sgmev_device_count(void);
  * "materialize": "auto" (default), "on" or "off" — whether the subspace FP32 products keep
  * p_s(x_j) for every data point and subspace in device memory (4 bytes each, built on the first
  * FP32 product) and streams it, instead of evaluating the hats on every call; "auto" does so when
- * it takes at most half of the free device memory and 64 GiB. With it, each product keeps its
- * cell index too (1 byte; grids whose subspaces have at most 256 cells). "materialize_multt":
- * "on" (default) or "off" — whether the FP32 multTranspose streams them too.
+ * it takes at most half of the free device memory and 64 GiB. The products are kept as
+ * float-float pairs with their cell index (9 bytes each; grids whose subspaces have at most 256
+ * cells), so the df64 (FP64-accurate) products stream them too. "materialize_multt": "on"
+ * (default) or "off" — whether multTranspose streams them as well as mult.
  */
 SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double* level_pow2,
                            const double* index, int64_t n_data, const double* data,

@@ -39,6 +39,8 @@ SGMEV_API int sgmev_fma_peak(int precision, double* flops_per_second, int* sm_cl
 #define SGMEV_KERNEL_MULTT_SUBDF 9 /* df64 subspace-skipping multTranspose */
 #define SGMEV_KERNEL_MULT_MAT32 10 /* FP32 mult streaming the materialised subspace products */
 #define SGMEV_KERNEL_MULTT_MAT32 11 /* FP32 multTranspose streaming them */
+#define SGMEV_KERNEL_MULT_MATDF 12 /* df64 mult streaming them */
+#define SGMEV_KERNEL_MULTT_MATDF 13 /* df64 multTranspose streaming them */
 SGMEV_API int sgmev_profile(sgmev_op* op, int enable);
 SGMEV_API int sgmev_profile_read(sgmev_op* op, int kind, int64_t* launches, double* seconds);
 

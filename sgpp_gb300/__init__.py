@@ -78,6 +78,8 @@ SGMEV_KERNEL_MULT_SUBDF = 8
 SGMEV_KERNEL_MULTT_SUBDF = 9
 SGMEV_KERNEL_MULT_MAT32 = 10
 SGMEV_KERNEL_MULTT_MAT32 = 11
+SGMEV_KERNEL_MULT_MATDF = 12
+SGMEV_KERNEL_MULTT_MATDF = 13
 
 
 # ---- exceptions (base/src/sgpp/base/exception/) --------------------------------------------

@@ -145,8 +145,8 @@ struct sgmev_op {
   std::vector<cudaEvent_t> prof_events;  // pool, 2 per launch
   std::vector<int> prof_kind;            // kind of launch i
   size_t prof_used = 0;                  // launches recorded since the last reset
-  int64_t prof_count[12] = {0};
-  double prof_seconds[12] = {0.0};
+  int64_t prof_count[14] = {0};
+  double prof_seconds[14] = {0.0};
 };
 
 namespace sgmev {
@@ -164,9 +164,11 @@ enum {
   KIND_MULT_SUBDF = 8,
   KIND_MULTT_SUBDF = 9,
   KIND_MULT_MAT32 = 10,
-  KIND_MULTT_MAT32 = 11
+  KIND_MULTT_MAT32 = 11,
+  KIND_MULT_MATDF = 12,
+  KIND_MULTT_MATDF = 13
 };
-constexpr int kKinds = 12;
+constexpr int kKinds = 14;
 
 template <typename T>
 static int kind_mult() { return sizeof(T) == 4 ? KIND_MULT_FP32 : KIND_MULT_FP64; }
@@ -647,7 +649,7 @@ static int64_t multt_tile_pts(const sgmev_op* op, int prec) {
 static bool mat_ready(sgmev_op* op) {
   using namespace sgmev;
   if (op->sub.pmat) return true;
-  if (op->mat_mode == 0 || op->mat_failed || !subspace_mat_fits(op->sub)) return false;
+  if (op->mat_mode == 0 || op->mat_failed || !subspace_mat_fits(op->sub, false)) return false;
   const int64_t bytes = subspace_mat_bytes(op->sub, op->mpad);
   if (op->mat_mode == 1) {
     size_t free_b = 0, total_b = 0;
@@ -661,11 +663,13 @@ static bool mat_ready(sgmev_op* op) {
       return false;
     }
   }
-  if (subspace_materialize(&op->sub, op->stream, op->xt32, op->mpad, op->m, op->num_sms) != cudaSuccess) {
+  if (subspace_materialize(&op->sub, op->stream, op->xt32, op->xt32lo, op->mpad, op->m,
+                           op->num_sms) != cudaSuccess) {
     (void)cudaGetLastError();
     cudaFree(op->sub.pmat);
+    cudaFree(op->sub.pmat_lo);
     cudaFree(op->sub.cmat);
-    op->sub.pmat = nullptr;
+    op->sub.pmat = op->sub.pmat_lo = nullptr;
     op->sub.cmat = nullptr;
     op->mat_failed = true;
     return false;
@@ -687,6 +691,13 @@ static int dev_mult(sgmev_op* op, int prec, const double* a64, const float* a32,
     SGMEV_TRY(run_mult<double>(op, op->xt64, op->li64, a64, j_begin, j_end, &p));
     if (out64) SGMEV_TRY((run_reduce<double, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
     if (out32) SGMEV_TRY((run_reduce<double, float>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out32, nullptr, 0.0)));
+  } else if (prec == SGMEV_DF64 && op->sub_ok && out64 && !out32 && mat_ready(op) &&
+             subspace_mat_fits(op->sub, true)) {
+    const long ev = prof_begin(op, KIND_MULT_MATDF);
+    SGMEV_CUDA(subspace_mult_mat_df(op->sub, op->stream, op->mpad, op->m, a32, a32lo, out64,
+                                    j_begin, j_end, op->num_sms));
+    prof_end(op, ev);
+    op->launches += 2;
   } else if (prec == SGMEV_DF64 && op->sub_ok && out64 && !out32) {
     const long ev = prof_begin(op, KIND_MULT_SUBDF);
     SGMEV_CUDA(subspace_mult_df(op->sub, op->stream, op->xt32, op->xt32lo, op->mpad, op->m, a32,
@@ -727,6 +738,14 @@ static int dev_multt(sgmev_op* op, int prec, const double* v64, const float* v32
   if (prec == SGMEV_FP64) {
     SGMEV_TRY(run_multt<double>(op, op->xt64, v64, op->li64, g_begin, g_end, &p));
     SGMEV_TRY((run_reduce<double, double>(op, (int)p.nsplit, op->npad, g_begin, valid, g_end, out64, add, scale)));
+  } else if (prec == SGMEV_DF64 && op->sub_ok && op->mat_multt && mat_ready(op) &&
+             subspace_mat_fits(op->sub, true)) {
+    // the subspace sums produce every grid entry at once (the range is a subset of them)
+    const long ev = prof_begin(op, KIND_MULTT_MATDF);
+    SGMEV_CUDA(subspace_multt_mat_df(op->sub, op->stream, op->mpad, v32, v32lo, op->npad, out64,
+                                     add, scale, op->num_sms));
+    prof_end(op, ev);
+    op->launches += 3;
   } else if (prec == SGMEV_DF64 && op->sub_ok && subspace_owner_fits(op->sub, true)) {
     // the subspace sums produce every grid entry at once (the range is a subset of them)
     const long ev = prof_begin(op, KIND_MULTT_SUBDF);

@@ -469,8 +469,9 @@ __device__ __forceinline__ void own_stage_tile(float* s_pt, int64_t tile,
         if constexpr (DF) row[DIM + t] = 0.0f;
       }
     }
-    row[Lay::V] = inside ? vh[j] : 0.0f;
-    if constexpr (DF) row[Lay::V + 1] = inside ? vl[j] : 0.0f;
+    // vh == nullptr: the v column holds the inside flag (1 or 0), vl's column 0
+    row[Lay::V] = inside ? (vh ? vh[j] : 1.0f) : 0.0f;
+    if constexpr (DF) row[Lay::V + 1] = (inside && vl) ? vl[j] : 0.0f;
   }
   __syncthreads();
 }
@@ -574,6 +575,101 @@ __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_multt_own_kernel(
     if (active && first)  // no tile for this CTA: its row holds zeros
       for (int c = 0; c < info.y; ++c) row[info.x + c] = 0.0;
   }
+}
+
+// Build of the materialised products (see subspace_mat.cu): thread k of a pass owns subspace
+// s = pass * blockDim + k and writes, for every point of the CTA's tiles, the float-float product
+// of its basis function (renormalised: hi = the FP32 rounding of the pair) and the cell index, in
+// the layout P_hi[g][s], P_lo[g][s] (float4: points 4g .. 4g+3) and C[g][s] (a byte per point).
+// The arithmetic is the one of the float-float kernels above, so the cells follow x_hi + x_lo.
+template <int DIM>
+__global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_mat_build_kernel(
+    const int4* __restrict__ desc, const int4* __restrict__ sinfo, int n_sub, int s_pad,
+    const float* __restrict__ xh_t, const float* __restrict__ xl_t, int64_t mpad, int64_t m,
+    int64_t n_tiles, float4* __restrict__ phi, float4* __restrict__ plo,
+    uint32_t* __restrict__ cm) {
+  using Lay = OwnLayout<DIM, true>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* s_pt = reinterpret_cast<float*>(smem);  // [kOwnTile][W]
+  const int tid = threadIdx.x;
+  constexpr int kGroupsPerTile = kOwnTile / 4;
+  for (int s0 = 0; s0 < s_pad; s0 += blockDim.x) {
+    const int sid = s0 + tid;
+    const bool real = sid < n_sub;
+    const int4 info = real ? sinfo[sid] : make_int4(0, 0, 0, 0);  // (offset, cells, cbase, 0)
+    float L[DIM];
+    uint32_t st[DIM];
+#pragma unroll
+    for (int t = 0; t < DIM; ++t) {
+      const int4 q = real ? desc[static_cast<int64_t>(sid) * DIM + t]
+                          : make_int4(__float_as_int(1.0f), __float_as_int(2.0f), 0, 0);
+      L[t] = __int_as_float(q.y);
+      st[t] = static_cast<uint32_t>(q.z);
+    }
+    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+      __syncthreads();  // the previous tile's rows are no longer read
+      own_stage_tile<DIM, true>(s_pt, tile, xh_t, xl_t, mpad, m, nullptr, nullptr);
+      if (sid >= s_pad) continue;
+      const int64_t at = tile * kGroupsPerTile * static_cast<int64_t>(s_pad) + sid;
+      for (int g = 0; g < kGroupsPerTile; ++g) {
+        float hv[4], lv[4];
+        uint32_t cells = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float* rw = s_pt + (4 * g + i) * Lay::W;
+          uint32_t c = static_cast<uint32_t>(info.z);
+          ff p{0.0f, 0.0f};
+          if (real) {
+            p = ff{1.0f, 0.0f};
+#pragma unroll
+            for (int t = 0; t < DIM; ++t) {
+              const float xh = rw[t], xl = rw[DIM + t];
+              const float sl = L[t] * xl;
+              const float t2 = __fmaf_rd(xh, L[t], sl);
+              const float rr = __fmaf_rd(t2, 0.5f, kMagic);
+              const float m2k = fmaf(rr, -2.0f, kTwoMagic);
+              const float a = fmaf(xh, L[t], m2k);
+              const float b = fmaf(xh, -L[t], 2.0f - m2k);
+              const bool rise = fmaf(2.0f, sl, a - b) <= 0.0f;
+              const ff h{rise ? a : b, rise ? sl : -sl};
+              p = t == 0 ? h : mul_ff(p, h);
+              c += __float_as_uint(rr) * st[t];
+            }
+            const float in = rw[Lay::V];  // 1 inside the domain, 0 outside
+            p = ff{p.h * in, p.l * in};
+            const float sh = p.h + p.l;
+            p = ff{sh, p.l - (sh - p.h)};
+          } else {
+            c = 0;
+          }
+          hv[i] = p.h;
+          lv[i] = p.l;
+          cells |= (c & 0xFFu) << (8 * i);
+        }
+        const int64_t k = at + static_cast<int64_t>(g) * s_pad;
+        phi[k] = make_float4(hv[0], hv[1], hv[2], hv[3]);
+        plo[k] = make_float4(lv[0], lv[1], lv[2], lv[3]);
+        cm[k] = cells;
+      }
+    }
+  }
+}
+
+template <int DIM>
+cudaError_t launch_mat_build(const SubPlan& p, cudaStream_t s, const float* xh, const float* xl,
+                             int64_t mpad, int64_t m, int num_sms) {
+  using Lay = OwnLayout<DIM, true>;
+  const size_t sm = sizeof(float) * kOwnTile * Lay::W;
+  auto kern = sub_mat_build_kernel<DIM>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  const int64_t nt = mpad / kOwnTile;
+  const int nth = static_cast<int>(std::min<int64_t>(kOwnMaxThreads, p.s_pad));
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, 2LL * num_sms));
+  kern<<<static_cast<unsigned>(blocks), nth, sm, s>>>(p.desc, p.sinfo, p.n_sub,
+                                                      static_cast<int>(p.s_pad), xh, xl, mpad, m,
+                                                      nt, p.pmat, p.pmat_lo, p.cmat);
+  return cudaGetLastError();
 }
 
 // Owner-computes multTranspose with active-dimension evaluation (FP32): as sub_multt_own_kernel,
@@ -1020,6 +1116,7 @@ void subspace_free(SubPlan* p) {
   cudaFree(p->desc);
   cudaFree(p->sinfo);
   cudaFree(p->pmat);
+  cudaFree(p->pmat_lo);
   cudaFree(p->cmat);
   cudaFree(p->act);
   cudaFree(p->sact);
@@ -1040,6 +1137,28 @@ cudaError_t subspace_scatter_alpha(const SubPlan& p, cudaStream_t s, const float
   if (e != cudaSuccess) return e;
   scatter_alpha_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.n + 255) / 256)), 256, 0, s>>>(
       alpha32, p.pos, p.n, p.asub);
+  return cudaGetLastError();
+}
+
+cudaError_t subspace_mat_build(const SubPlan& p, cudaStream_t s, const float* xh,
+                               const float* xl, int64_t mpad, int64_t m, int num_sms) {
+  switch (p.dim) {
+#define F(D) \
+  case D:    \
+    return launch_mat_build<D>(p, s, xh, xl, mpad, m, num_sms);
+    SUB_DIMS(F)
+#undef F
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t subspace_scatter_alpha_df(const SubPlan& p, cudaStream_t s, const float* ah,
+                                      const float* al) {
+  cudaError_t e = cudaMemsetAsync(p.asub2, 0, sizeof(float2) * p.total, s);
+  if (e != cudaSuccess) return e;
+  scatter_alpha_df_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.n + 255) / 256)), 256, 0, s>>>(
+      ah, al, p.pos, p.n, p.asub2);
   return cudaGetLastError();
 }
 

@@ -33,10 +33,12 @@ struct SubPlan {
   int cmax = 0;           // largest cell count of a subspace
   double* rows = nullptr;  // [row_cap * total] per-CTA partial sums (owner-computes multT)
   int64_t row_cap = 0;
-  // materialised products P[j / 4][s][j % 4] (s padded to s_pad, a multiple of 32) and the cell
-  // index of each within its subspace, C[j / 4][s] (four bytes, point j % 4 in byte j % 4), for
-  // the data of mat_mpad padded points; nullptr when not built
+  // materialised products as float-float pairs P_hi[j / 4][s][j % 4], P_lo[...] (s padded to
+  // s_pad, a multiple of 32) and the cell index of each within its subspace, C[j / 4][s] (four
+  // bytes, point j % 4 in byte j % 4), for the data of mat_mpad padded points; nullptr when not
+  // built
   float4* pmat = nullptr;
+  float4* pmat_lo = nullptr;
   uint32_t* cmat = nullptr;
   int64_t s_pad = 0;
   int64_t mat_mpad = 0;
@@ -79,14 +81,27 @@ cudaError_t subspace_multt(const SubPlan& p, cudaStream_t s, const float* xt, in
 cudaError_t subspace_scatter_alpha(const SubPlan& p, cudaStream_t s, const float* alpha32);
 cudaError_t subspace_finish_rows(const SubPlan& p, cudaStream_t s, int64_t nrows, int64_t npad,
                                  double* out64, const double* add, double scale_add);
+cudaError_t subspace_scatter_alpha_df(const SubPlan& p, cudaStream_t s, const float* ah,
+                                      const float* al);
+// fills pmat, pmat_lo and cmat (allocated, s_pad set) from the float-float data (xh, xl)
+cudaError_t subspace_mat_build(const SubPlan& p, cudaStream_t s, const float* xh,
+                               const float* xl, int64_t mpad, int64_t m, int num_sms);
 
-// Materialised FP32 products: bytes they take for mpad points, whether the kernels' shared memory
-// fits the plan, building them (allocates; the data xt must not change afterwards), and the
-// products that stream them (same contracts as subspace_mult / subspace_multt).
+// Materialised products: bytes they take for mpad points, whether the FP32 (df = false) or
+// float-float (df = true) kernels' shared memory fits the plan, building them from the
+// float-float data (allocates; the data must not change afterwards), and the products that
+// stream them (same contracts as subspace_mult / subspace_multt / subspace_mult_df /
+// subspace_multt_df).
 int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad);
-bool subspace_mat_fits(const SubPlan& p);
-cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xt, int64_t mpad,
-                                 int64_t m, int num_sms);
+bool subspace_mat_fits(const SubPlan& p, bool df);
+cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, const float* xl,
+                                 int64_t mpad, int64_t m, int num_sms);
+cudaError_t subspace_mult_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad, int64_t m,
+                                 const float* ah, const float* al, double* out64, int64_t j_begin,
+                                 int64_t j_end, int num_sms);
+cudaError_t subspace_multt_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad,
+                                  const float* vh, const float* vl, int64_t npad, double* out64,
+                                  const double* add, double scale_add, int num_sms);
 cudaError_t subspace_mult_mat(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
                               int64_t m, const float* alpha32, float* out32, double* out64,
                               int64_t j_begin, int64_t j_end, int num_sms);

@@ -1,13 +1,14 @@
-// Materialised subspace products (FP32). For a fixed data set and grid, the product
+// Materialised subspace products. For a fixed data set and grid, the product
 // p_s(x_j) = prod_t h_{l_t}(x_{j,t}) of the one possibly non-zero basis function of subspace s at
 // point j, and that function's cell index c_s(x_j) within its subspace, do not change between
-// calls. They are computed once (mat_build_kernel) and kept in HBM as
-//     P[g][s] : float4, the products of points 4g .. 4g+3        (4 bytes per point and subspace)
-//     C[g][s] : uint32, their cell indices, one byte each          (1 byte per point and subspace)
-// with s padded to a multiple of 32 (padded entries 0). mult and multTranspose then stream P and
-// C once per call and touch no coordinates: 5 bytes per (point, subspace) and a handful of
-// instructions, so they are bounded by HBM bandwidth rather than the hat arithmetic. Points
-// outside the domain have P = 0 (and cell 0), so they need no test.
+// calls. They are computed once, in float-float arithmetic (sub_mat_build_kernel in subspace.cu),
+// and kept in HBM as
+//     P_hi[g][s], P_lo[g][s] : float4, the products of points 4g .. 4g+3 as float-float pairs
+//     C[g][s]                : uint32, their cell indices, one byte each
+// with s padded to a multiple of 32 (padded entries 0). The FP32 mult and multTranspose stream
+// P_hi and C (5 bytes per point and subspace), the FP64-accurate ones all three (9 bytes); none
+// touches a coordinate, so they are bounded by HBM bandwidth rather than the hat arithmetic.
+// Points outside the domain have P = 0 (and cell 0), so they need no test.
 //
 // Both kernels are owner-computes: thread k of a pass owns subspace s = pass * blockDim + k and
 // walks the CTA's tiles of points; a warp reads P[g][32 consecutive s] as 512 contiguous bytes
@@ -18,11 +19,13 @@
 //   multT: lane s adds v_j * p into its cells ([cell][thread] in shared memory, conflict-free) and
 //          flushes them into the CTA's FP64 row every kFlushTiles tiles; rows are added in CTA
 //          order.
+// The float-float variants do the same with float-float products, sums and butterfly.
 // Every sum has a fixed order, so results are the same bit for bit from run to run.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 
+#include "kernels.cuh"
 #include "subspace.h"
 #include "subspace_common.cuh"
 
@@ -36,75 +39,11 @@ constexpr int kGroups = kOwnTile / 4;         // point groups per tile
 constexpr int kMatWarps = kMatThreads / 32;
 constexpr int kMatMaxCells = 256;             // cell indices are stored in one byte
 // point groups in flight per thread: a ring of loads issued this many groups ahead of their use
-constexpr int kAhead = 4;
-static_assert(kGroups % kAhead == 0, "the ring must divide a tile");
+// (fewer for the float-float kernels, whose arithmetic holds more registers)
+constexpr int kAhead = 4, kAheadDf = 2;
+static_assert(kGroups % kAhead == 0 && kGroups % kAheadDf == 0, "the ring must divide a tile");
 // multT: FP32 sums over this many tiles (1024 points) before they go into the FP64 row
 constexpr int kFlushTiles = 4;
-
-// ---- build -----------------------------------------------------------------------------
-template <int NA>
-__device__ __forceinline__ void build_tile(const float* __restrict__ s_pt, int w,
-                                           const int4* __restrict__ q, int na, uint32_t cbase,
-                                           float4* __restrict__ dst, uint32_t* __restrict__ cdst,
-                                           int64_t s_pad) {
-  ActDesc<(NA > 0 ? NA : 1)> desc;
-  if (NA > 0) desc.load(q);
-  for (int g = 0; g < kGroups; ++g) {
-    float pv[4];
-    uint32_t cells = 0;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float* row = s_pt + (4 * g + i) * w;
-      uint32_t c = cbase;
-      pv[i] = NA > 0 ? desc.eval(row, cbase, c)
-                     : (NA == 0 ? row[0] : act_eval_dyn(row, q, na, cbase, c));
-      cells |= (c & 0xFFu) << (8 * i);
-    }
-    dst[static_cast<int64_t>(g) * s_pad] = make_float4(pv[0], pv[1], pv[2], pv[3]);
-    cdst[static_cast<int64_t>(g) * s_pad] = cells;
-  }
-}
-
-template <int DIM>
-__global__ void __launch_bounds__(kMatThreads, 1) mat_build_kernel(
-    const int4* __restrict__ act, const int4* __restrict__ sact, int n_sub, int s_pad,
-    const float* __restrict__ xt, int64_t mpad, int64_t m, int64_t n_tiles,
-    float4* __restrict__ pm, uint32_t* __restrict__ cm) {
-  constexpr int W = ActRow<DIM>::W;
-  extern __shared__ __align__(16) unsigned char smem[];
-  float* s_pt = reinterpret_cast<float*>(smem);  // [kOwnTile][W]
-  const int tid = threadIdx.x;
-  for (int s0 = 0; s0 < s_pad; s0 += blockDim.x) {
-    const int sid = s0 + tid;
-    const bool real = sid < n_sub;
-    const int4 info = real ? sact[sid] : make_int4(0, 0, 0, 0);
-    const int4* q = act + static_cast<int64_t>(real ? sid : 0) * DIM;
-    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-      __syncthreads();
-      act_stage_tile<DIM>(s_pt, tile, xt, mpad, m, nullptr);
-      if (sid >= s_pad) continue;
-      const int64_t at = tile * kGroups * static_cast<int64_t>(s_pad) + sid;
-      if (!real) {
-        for (int g = 0; g < kGroups; ++g) {
-          pm[at + static_cast<int64_t>(g) * s_pad] = make_float4(0.f, 0.f, 0.f, 0.f);
-          cm[at + static_cast<int64_t>(g) * s_pad] = 0u;
-        }
-        continue;
-      }
-      const uint32_t cbase = static_cast<uint32_t>(info.z);
-      float4* dst = pm + at;
-      uint32_t* cdst = cm + at;
-      switch (info.w) {
-        case 0: build_tile<0>(s_pt, W, q, 0, cbase, dst, cdst, s_pad); break;
-        case 1: build_tile<1>(s_pt, W, q, 1, cbase, dst, cdst, s_pad); break;
-        case 2: build_tile<(DIM < 2 ? DIM : 2)>(s_pt, W, q, 2, cbase, dst, cdst, s_pad); break;
-        case 3: build_tile<(DIM < 3 ? DIM : 3)>(s_pt, W, q, 3, cbase, dst, cdst, s_pad); break;
-        case 4: build_tile<(DIM < 4 ? DIM : 4)>(s_pt, W, q, 4, cbase, dst, cdst, s_pad); break;
-        default: build_tile<-1>(s_pt, W, q, info.w, cbase, dst, cdst, s_pad); break;
-      }
-    }
-  }
-}
 
 // ---- mult --------------------------------------------------------------------------------
 // lane sums of 4 values -> the 32-lane sum of value (2 * bit4 + bit3) of the lane index
@@ -266,7 +205,181 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
   }
 }
 
-size_t build_smem(int dim) { return sizeof(float) * kOwnTile * ((2 + 2 * dim + 3) / 4 * 4); }
+// ---- float-float (FP64-accurate) variants -------------------------------------------------
+__device__ __forceinline__ ff shfl_ff(ff v, int mask) {
+  return ff{__shfl_xor_sync(0xffffffffu, v.h, mask), __shfl_xor_sync(0xffffffffu, v.l, mask)};
+}
+
+// reduce4 in float-float
+__device__ __forceinline__ ff reduce4_ff(ff v0, ff v1, ff v2, ff v3, int lane) {
+  const bool hi = lane & 16;
+  ff a0 = hi ? v2 : v0, a1 = hi ? v3 : v1;
+  const ff s0 = hi ? v0 : v2, s1 = hi ? v1 : v3;
+  add_ff(a0, shfl_ff(s0, 16));
+  add_ff(a1, shfl_ff(s1, 16));
+  const bool b3 = lane & 8;
+  ff b = b3 ? a1 : a0;
+  add_ff(b, shfl_ff(b3 ? a0 : a1, 8));
+  add_ff(b, shfl_ff(b, 4));
+  add_ff(b, shfl_ff(b, 2));
+  add_ff(b, shfl_ff(b, 1));
+  return b;
+}
+
+__global__ void __launch_bounds__(kMatThreads, 1) mat_mult_df_kernel(
+    const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
+    const float2* __restrict__ asub2, int64_t m, int64_t tile_begin, int64_t n_tiles,
+    const float4* __restrict__ phi, const float4* __restrict__ plo,
+    const uint32_t* __restrict__ cm, double* __restrict__ out64) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* s_part = reinterpret_cast<float2*>(smem);  // [warps][kOwnTile]
+  float2* s_at = s_part + kMatWarps * kOwnTile;      // [cmax][s_pad]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t cm1 = static_cast<uint32_t>(cmax - 1);
+  for (int k = tid; k < cmax * s_pad; k += blockDim.x) {
+    const int c = k / s_pad, sidx = k - c * s_pad;
+    float2 a = make_float2(0.0f, 0.0f);
+    if (sidx < n_sub) {
+      const int4 info = sact[sidx];
+      const int off = static_cast<int>(static_cast<uint32_t>(info.x) - static_cast<uint32_t>(info.z));
+      if (c < info.y) a = asub2[off + c];
+    }
+    s_at[k] = a;
+  }
+  __syncthreads();
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t gt = tile_begin + tile;
+    for (int s0 = 0; s0 < s_pad; s0 += blockDim.x) {
+      if (s0 + warp * 32 >= s_pad) continue;  // whole warps: s_pad is a multiple of 32
+      const int sid = s0 + tid;
+      const int64_t at = gt * kGroups * static_cast<int64_t>(s_pad) + sid;
+      const float2* a_col = s_at + sid;
+      float2* part = s_part + warp * kOwnTile;
+      const bool first = s0 == 0;
+      float4 rh[kAheadDf], rl[kAheadDf];
+      uint32_t rc[kAheadDf];
+#pragma unroll
+      for (int u = 0; u < kAheadDf; ++u) {
+        rh[u] = __ldcs(phi + at + static_cast<int64_t>(u) * s_pad);
+        rl[u] = __ldcs(plo + at + static_cast<int64_t>(u) * s_pad);
+        rc[u] = __ldcs(cm + at + static_cast<int64_t>(u) * s_pad);
+      }
+      for (int g0 = 0; g0 < kGroups; g0 += kAheadDf) {
+#pragma unroll
+        for (int u = 0; u < kAheadDf; ++u) {
+          const int g = g0 + u;
+          const float4 ph = rh[u], pl = rl[u];
+          const uint32_t cs = rc[u];
+          if (g + kAheadDf < kGroups) {
+            const int64_t k = at + static_cast<int64_t>(g + kAheadDf) * s_pad;
+            rh[u] = __ldcs(phi + k);
+            rl[u] = __ldcs(plo + k);
+            rc[u] = __ldcs(cm + k);
+          }
+          const float2 a0 = a_col[min(cs & 0xFFu, cm1) * s_pad];
+          const float2 a1 = a_col[min((cs >> 8) & 0xFFu, cm1) * s_pad];
+          const float2 a2 = a_col[min((cs >> 16) & 0xFFu, cm1) * s_pad];
+          const float2 a3 = a_col[min(cs >> 24, cm1) * s_pad];
+          const ff r = reduce4_ff(mul_ff(ff{ph.x, pl.x}, ff{a0.x, a0.y}),
+                                  mul_ff(ff{ph.y, pl.y}, ff{a1.x, a1.y}),
+                                  mul_ff(ff{ph.z, pl.z}, ff{a2.x, a2.y}),
+                                  mul_ff(ff{ph.w, pl.w}, ff{a3.x, a3.y}), lane);
+          if ((lane & 7) == 0) {
+            float2* dst = part + 4 * g + (lane >> 3);
+            ff acc = first ? ff{0.0f, 0.0f} : ff{dst->x, dst->y};
+            add_ff(acc, r);
+            *dst = make_float2(acc.h, acc.l);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const int wrote = min(kMatWarps, s_pad / 32);
+    for (int jj = tid; jj < kOwnTile; jj += blockDim.x) {
+      ff r{0.0f, 0.0f};
+      for (int w = 0; w < wrote; ++w) {
+        const float2 q = s_part[w * kOwnTile + jj];
+        add_ff(r, ff{q.x, q.y});
+      }
+      const int64_t j = gt * kOwnTile + jj;
+      out64[j] = j < m ? static_cast<double>(r.h) + static_cast<double>(r.l) : 0.0;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
+    const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
+    const float* __restrict__ vh, const float* __restrict__ vl, int64_t n_tiles,
+    const float4* __restrict__ phi, const float4* __restrict__ plo,
+    const uint32_t* __restrict__ cm, double* __restrict__ rows) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* s_acc = reinterpret_cast<float2*>(smem);  // [cmax][blockDim]
+  double* row = rows + static_cast<int64_t>(blockIdx.x) * total;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const uint32_t cm1 = static_cast<uint32_t>(cmax - 1);
+  const float4* vh4 = reinterpret_cast<const float4*>(vh);
+  const float4* vl4 = reinterpret_cast<const float4*>(vl);
+  for (int s0 = 0; s0 < n_sub; s0 += nth) {
+    const int sid = s0 + tid;
+    if (sid >= n_sub) continue;  // no barriers below: threads run independently
+    const int4 info = sact[sid];
+    const uint32_t offset = static_cast<uint32_t>(info.x) - static_cast<uint32_t>(info.z);
+    float2* acc = s_acc + tid;
+    for (int c = 0; c < info.y; ++c) acc[c * nth] = make_float2(0.0f, 0.0f);
+    bool first = true;
+    int since = 0;
+    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+      const int64_t at = tile * kGroups * static_cast<int64_t>(s_pad) + sid;
+      float4 rh[kAheadDf], rl[kAheadDf];
+      uint32_t rc[kAheadDf];
+#pragma unroll
+      for (int u = 0; u < kAheadDf; ++u) {
+        rh[u] = __ldcs(phi + at + static_cast<int64_t>(u) * s_pad);
+        rl[u] = __ldcs(plo + at + static_cast<int64_t>(u) * s_pad);
+        rc[u] = __ldcs(cm + at + static_cast<int64_t>(u) * s_pad);
+      }
+      for (int g0 = 0; g0 < kGroups; g0 += kAheadDf) {
+#pragma unroll
+        for (int u = 0; u < kAheadDf; ++u) {
+          const int g = g0 + u;
+          const float4 ph = rh[u], pl = rl[u];
+          const uint32_t cs = rc[u];
+          if (g + kAheadDf < kGroups) {
+            const int64_t k = at + static_cast<int64_t>(g + kAheadDf) * s_pad;
+            rh[u] = __ldcs(phi + k);
+            rl[u] = __ldcs(plo + k);
+            rc[u] = __ldcs(cm + k);
+          }
+          const float4 vvh = vh4[tile * kGroups + g], vvl = vl4[tile * kGroups + g];
+          const float ph_[4] = {ph.x, ph.y, ph.z, ph.w}, pl_[4] = {pl.x, pl.y, pl.z, pl.w};
+          const float vh_[4] = {vvh.x, vvh.y, vvh.z, vvh.w}, vl_[4] = {vvl.x, vvl.y, vvl.z, vvl.w};
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            float2* slot = acc + min((cs >> (8 * i)) & 0xFFu, cm1) * nth;
+            ff a{slot->x, slot->y};
+            add_ff(a, mul_ff(ff{ph_[i], pl_[i]}, ff{vh_[i], vl_[i]}));
+            *slot = make_float2(a.h, a.l);
+          }
+        }
+      }
+      ++since;
+      if (since == kFlushTiles || tile + gridDim.x >= n_tiles) {
+        for (int c = 0; c < info.y; ++c) {
+          const float2 a = acc[c * nth];
+          const double v = static_cast<double>(a.x) + static_cast<double>(a.y);
+          double* dst = row + offset + c;
+          *dst = first ? v : *dst + v;
+          acc[c * nth] = make_float2(0.0f, 0.0f);
+        }
+        first = false;
+        since = 0;
+      }
+    }
+    if (first)
+      for (int c = 0; c < info.y; ++c) row[offset + c] = 0.0;
+  }
+}
 
 int mat_threads(int64_t s_pad) { return static_cast<int>(std::min<int64_t>(kMatThreads, s_pad)); }
 
@@ -278,66 +391,97 @@ size_t mat_multt_smem(int cmax, int64_t s_pad) {
   return sizeof(float) * static_cast<size_t>(cmax) * mat_threads(s_pad);
 }
 
-template <int DIM>
-cudaError_t launch_build(SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad, int64_t m,
-                         int num_sms) {
-  const size_t sm = build_smem(DIM);
-  auto kern = mat_build_kernel<DIM>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
-  if (e != cudaSuccess) return e;
-  const int64_t nt = mpad / kOwnTile;
-  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, 2LL * num_sms));
-  kern<<<static_cast<unsigned>(blocks), mat_threads(p.s_pad), sm, s>>>(
-      p.act, p.sact, p.n_sub, static_cast<int>(p.s_pad), xt, mpad, m, nt, p.pmat, p.cmat);
-  return cudaGetLastError();
+size_t mat_mult_df_smem(int cmax, int64_t s_pad) {
+  return sizeof(float2) * kMatWarps * kOwnTile + sizeof(float2) * static_cast<size_t>(cmax) * s_pad;
 }
 
-#define MAT_DIMS(F) F(1) F(2) F(3) F(4) F(5) F(6) F(7) F(8) F(9) F(10) F(11) F(12) F(13) F(14) F(15) F(16)
+size_t mat_multt_df_smem(int cmax, int64_t s_pad) {
+  return sizeof(float2) * static_cast<size_t>(cmax) * mat_threads(s_pad);
+}
 
 constexpr size_t kMatSmemBudget = 200 * 1024;
 
 }  // namespace
 
-bool subspace_mat_fits(const SubPlan& p) {
+bool subspace_mat_fits(const SubPlan& p, bool df) {
   const int64_t s_pad = (p.n_sub + 31) / 32 * 32;
-  return p.n_sub > 0 && p.cmax > 0 && p.cmax <= kMatMaxCells && p.rows != nullptr &&
-         mat_mult_smem(p.cmax, s_pad) <= kMatSmemBudget &&
+  if (!(p.n_sub > 0 && p.cmax > 0 && p.cmax <= kMatMaxCells && p.rows != nullptr)) return false;
+  if (df)
+    return mat_mult_df_smem(p.cmax, s_pad) <= kMatSmemBudget &&
+           mat_multt_df_smem(p.cmax, s_pad) <= kMatSmemBudget;
+  return mat_mult_smem(p.cmax, s_pad) <= kMatSmemBudget &&
          mat_multt_smem(p.cmax, s_pad) <= kMatSmemBudget;
 }
 
 int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad) {
-  return mpad * ((p.n_sub + 31) / 32 * 32) * static_cast<int64_t>(sizeof(float) + 1);
+  return mpad * ((p.n_sub + 31) / 32 * 32) * static_cast<int64_t>(2 * sizeof(float) + 1);
 }
 
-cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xt, int64_t mpad,
-                                 int64_t m, int num_sms) {
+cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, const float* xl,
+                                 int64_t mpad, int64_t m, int num_sms) {
   cudaFree(p->pmat);
+  cudaFree(p->pmat_lo);
   cudaFree(p->cmat);
-  p->pmat = nullptr;
+  p->pmat = p->pmat_lo = nullptr;
   p->cmat = nullptr;
   p->s_pad = (p->n_sub + 31) / 32 * 32;
   p->mat_mpad = mpad;
   const size_t entries = static_cast<size_t>(mpad / 4) * static_cast<size_t>(p->s_pad);
   cudaError_t e = cudaMalloc(&p->pmat, entries * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMalloc(&p->pmat_lo, entries * sizeof(float4));
   if (e == cudaSuccess) e = cudaMalloc(&p->cmat, entries * sizeof(uint32_t));
   if (e != cudaSuccess) {
     cudaFree(p->pmat);
-    p->pmat = nullptr;
+    cudaFree(p->pmat_lo);
+    p->pmat = p->pmat_lo = nullptr;
     p->cmat = nullptr;
     (void)cudaGetLastError();
     return e;
   }
-  switch (p->dim) {
-#define F(D)                                                 \
-  case D:                                                    \
-    e = launch_build<D>(*p, s, xt, mpad, m, num_sms);        \
-    break;
-    MAT_DIMS(F)
-#undef F
-    default:
-      e = cudaErrorInvalidValue;
-  }
-  return e;
+  return subspace_mat_build(*p, s, xh, xl, mpad, m, num_sms);
+}
+
+cudaError_t subspace_mult_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad, int64_t m,
+                                 const float* ah, const float* al, double* out64, int64_t j_begin,
+                                 int64_t j_end, int num_sms) {
+  if (!p.pmat || !p.pmat_lo || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
+  cudaError_t e = subspace_scatter_alpha_df(p, s, ah, al);
+  if (e != cudaSuccess) return e;
+  const int64_t t0 = j_begin / kOwnTile;
+  const int64_t nt = (j_end + kOwnTile - 1) / kOwnTile - t0;
+  if (nt <= 0) return cudaSuccess;
+  const size_t sm = mat_mult_df_smem(p.cmax, p.s_pad);
+  e = cudaFuncSetAttribute(mat_mult_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mat_mult_df_kernel, kMatThreads, sm);
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
+  mat_mult_df_kernel<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
+      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub2, m, t0, nt, p.pmat, p.pmat_lo,
+      p.cmat, out64);
+  return cudaGetLastError();
+}
+
+cudaError_t subspace_multt_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad,
+                                  const float* vh, const float* vl, int64_t npad, double* out64,
+                                  const double* add, double scale_add, int num_sms) {
+  if (!p.pmat || !p.pmat_lo || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
+  const size_t sm = mat_multt_df_smem(p.cmax, p.s_pad);
+  const int nth = mat_threads(p.s_pad);
+  cudaError_t e = cudaFuncSetAttribute(mat_multt_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mat_multt_df_kernel, nth, sm);
+  if (e != cudaSuccess) return e;
+  const int64_t nt = mpad / kOwnTile;
+  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), p.row_cap);
+  mat_multt_df_kernel<<<static_cast<unsigned>(rows), nth, sm, s>>>(
+      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), vh, vl, nt,
+      p.pmat, p.pmat_lo, p.cmat, p.rows);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return subspace_finish_rows(p, s, rows, npad, out64, add, scale_add);
 }
 
 cudaError_t subspace_mult_mat(const SubPlan& p, cudaStream_t s, const float* /*xt*/, int64_t mpad,

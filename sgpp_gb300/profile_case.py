@@ -27,6 +27,8 @@ KINDS = {("mult", "float", "dense"): sg.SGMEV_KERNEL_MULT_FP32,
          ("multT", "float", "subspace"): sg.SGMEV_KERNEL_MULTT_SUB32,
          ("mult", "float", "materialized"): sg.SGMEV_KERNEL_MULT_MAT32,
          ("multT", "float", "materialized"): sg.SGMEV_KERNEL_MULTT_MAT32,
+         ("mult", "df64", "materialized"): sg.SGMEV_KERNEL_MULT_MATDF,
+         ("multT", "df64", "materialized"): sg.SGMEV_KERNEL_MULTT_MATDF,
          ("mult", "double", "dense"): sg.SGMEV_KERNEL_MULT_FP64,
          ("multT", "double", "dense"): sg.SGMEV_KERNEL_MULTT_FP64,
          ("mult", "df64", "dense"): sg.SGMEV_KERNEL_MULT_DF64,

@@ -50,6 +50,7 @@ MULTEVAL = [str(c) for c in load_golden("multeval.npz")["cases"]]
 @pytest.mark.parametrize("precision,tol,algo", [("double", FP64_TOL, "auto"),
                                                 ("df64", FP64_TOL, "dense"),
                                                 ("df64", FP64_TOL, "subspace"),
+                                                ("df64", FP64_TOL, "materialized"),
                                                 ("float", FP32_TOL, "dense"),
                                                 ("float", FP32_TOL, "subspace"),
                                                 ("float", FP32_TOL, "materialized")])
@@ -307,7 +308,7 @@ def test_reference_callers_drive_the_operator_unchanged():
     assert abs(cg.getNumberIterations() - int(g[name + "_iterations"])) <= 2
 
 
-@pytest.mark.parametrize("algo", ["dense", "subspace"])
+@pytest.mark.parametrize("algo", ["dense", "subspace", "materialized"])
 def test_df64_at_cell_boundaries_and_outside_the_cube(oracle, algo):
     """Coordinates on dyadic cell boundaries, one double ulp and 1e-9 either side of them, on the
     cube faces and outside [0, 1]: the float-float kernels follow the FP64 value, not its float
@@ -337,7 +338,8 @@ def test_df64_at_cell_boundaries_and_outside_the_cube(oracle, algo):
 @pytest.mark.parametrize("dim,level", [(1, 14), (2, 9), (3, 6), (12, 3)])
 @pytest.mark.parametrize("precision,tol,algo", [("float", FP32_TOL, "subspace"),
                                                 ("float", FP32_TOL, "materialized"),
-                                                ("df64", FP64_TOL, "subspace")])
+                                                ("df64", FP64_TOL, "subspace"),
+                                                ("df64", FP64_TOL, "materialized")])
 def test_subspace_shapes_match_oracle(oracle, dim, level, precision, tol, algo):
     """Subspace kernels on grids with few wide subspaces (d=1 level 14: 8192 cells in one
     subspace, beyond the shared-memory sums of the owner-computes multTranspose, so FP32 takes the
@@ -406,6 +408,12 @@ def test_df64_matches_native_fp64_at_full_size():
     opsub.mult(a, outsub)
     op64.mult(a, out64)
     assert rel_err(outsub, out64) < FP64_TOL
+    opmat = _op(grid, x, "df64", "materialized")
+    outmat = np.zeros(m)
+    opmat.mult(a, outmat)
+    assert rel_err(outmat, out64) < FP64_TOL
+    tmat = np.zeros(grid.getSize())
+    opmat.multTranspose(v, tmat)
     op64.mult(a, out64)
     opdf.mult(a, outdf)
     assert rel_err(outdf, out64) < FP64_TOL
@@ -413,6 +421,7 @@ def test_df64_matches_native_fp64_at_full_size():
     op64.multTranspose(v, t64)
     opdf.multTranspose(v, tdf)
     assert rel_err(tdf, t64) < FP64_TOL
+    assert rel_err(tmat, t64) < FP64_TOL
 
 
 @pytest.mark.parametrize("algo", ["dense", "subspace", "materialized"])
