@@ -16,9 +16,13 @@ Each fit's alpha is checked against an FP64 solution computed once before timing
 value   fits/s with the data resident in HBM (device pointers for y and alpha)
 e2e     fits/s through the public API from pinned host buffers: create the operator from the
         host data matrix (H2D copy inside the timed region), fit with host y, read alpha back
-roofline  dominant tile kernel (FP32 mult / multTranspose): achieved = 6 N M d FLOP per
-        launch (the reference's count, LearnerVectorizedPerformanceCalculator.cpp:91-93) over
-        its CUDA-event duration, against the FP32 FMA peak measured in the same run
+roofline  the kernel with the most device time in the fits. When it streams the materialised
+        subspace products (the default), it is HBM-bound: achieved = its algorithmic bytes per
+        launch (5 B per padded point and padded subspace in FP32, 9 B in df64, plus the vectors)
+        over its CUDA-event duration, against MEASURED_PEAKS.json's copy bandwidth. A kernel that
+        evaluates hats is reported against the FP32/FP64 FMA peak measured in the same run, with
+        the reference's count of 6 N M d FLOP per launch
+        (LearnerVectorizedPerformanceCalculator.cpp:91-93).
 cpu_baseline  the oracle port of the reference's STREAMING FP64 path on the host cores
         (bounded sample: one B^T B application on 2^16 of the points, scaled to M and to the
         CG operation count of one fit)
@@ -159,6 +163,30 @@ def grid_arrays():
     grid.getGenerator().regular(LEVEL)
     lp, ix = grid.getStorage().getLevelIndexArraysForEval()
     return grid, lp, ix
+
+
+def subspace_count(lp):
+    """Distinct level vectors of the grid (its subspaces), from the eval arrays (2^l)."""
+    return len({tuple(row) for row in np.asarray(lp, dtype=np.int64).tolist()})
+
+
+def mat_bytes_per_launch(kernel: str, lp, m: int, n: int) -> float:
+    """Algorithmic HBM bytes of one launch of a kernel streaming the materialised products."""
+    mpad = -(-m // 1024) * 1024
+    s_pad = -(-subspace_count(lp) // 32) * 32
+    per_entry = 9 if "df64" in kernel else 5
+    vec = (8 if "df64" in kernel else 4) * m + 8 * n
+    return float(mpad) * s_pad * per_entry + vec
+
+
+def hbm_peak_gbs():
+    """(GB/s, source): the measured HBM copy bandwidth of the GB300s (driver-written
+    MEASURED_PEAKS.json), else the 6.8 TB/s fallback of an earlier GB300 measurement."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s (of fallback)"
 
 
 # Iterations of the plain FP64 CG on this workload to relative residual 1e-8; used only to scale
@@ -302,24 +330,38 @@ def run_ours(args):
         total_s = float(t.item())
     value = args.steps * world / total_s
 
-    # roofline of the dominant tile kernel
+    # roofline of the dominant tile kernel: HBM-bound for the kernels that stream the
+    # materialised products, FMA-bound for the ones that evaluate the hats
     dom = max(kstats, key=lambda k: kstats[k][1])
     cnt, sec = kstats[dom]
     avg = sec / max(cnt, 1)
-    achieved = work_per_op / avg / 1e12
-    is64 = dom.endswith("fp64")
-    peak = (peak64 if is64 else peak32) / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         traffic = json.load(open(tpath)).get(dom)
-    roofline = {"bound": "fp64-vector" if is64 else "fp32-vector", "kernel": dom,
-                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": traffic, "launches_timed": cnt, "avg_launch_ms": avg * 1e3,
-                "peak_source": "measured in this run: FMA chains on every SM (sgmev_fma_peak); "
-                               "MEASURED_PEAKS.json holds no FP32/FP64 vector peak",
-                "peaks_measured_tflops": {"fp32": peak32 / 1e12, "fp64": peak64 / 1e12},
-                "flop_per_launch": work_per_op}
+    if "_mat" in dom:
+        by = mat_bytes_per_launch(dom, lp, m, n)
+        achieved = by / avg / 1e9
+        peak, peak_src = hbm_peak_gbs()
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                    "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                    "launches_timed": cnt, "avg_launch_ms": avg * 1e3,
+                    "peak_source": peak_src,
+                    "bytes_per_launch": by,
+                    "bytes_model": "materialised products read once per launch (FP32: 4 B product + "
+                                   "1 B cell; df64: 8 + 1 B) per padded point and padded subspace, "
+                                   "plus the input and output vectors"}
+    else:
+        achieved = work_per_op / avg / 1e12
+        is64 = dom.endswith("fp64") and not dom.endswith("df64")
+        peak = (peak64 if is64 else peak32) / 1e12
+        roofline = {"bound": "fp64-vector" if is64 else "fp32-vector", "kernel": dom,
+                    "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak, "traffic": traffic, "launches_timed": cnt,
+                    "avg_launch_ms": avg * 1e3,
+                    "peak_source": "measured in this run: FMA chains on every SM (sgmev_fma_peak)",
+                    "peaks_measured_tflops": {"fp32": peak32 / 1e12, "fp64": peak64 / 1e12},
+                    "flop_per_launch": work_per_op}
 
     # mult GFLOP/s (reference count) of the FP32 mult kernel
     mc, msec = kstats["mult_fp32"]

@@ -787,13 +787,37 @@ __global__ void __launch_bounds__(kActOwnThreads, 2) sub_multt_act_kernel(
 }
 
 // sums[k] = sum over rows b in order of rows[b][k] (k < total)
-__global__ void sum_rows_kernel(const double* __restrict__ rows, int nrows, int64_t total,
-                                double* __restrict__ sums) {
-  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
-       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    double a = 0.0;
-    for (int b = 0; b < nrows; ++b) a += rows[static_cast<int64_t>(b) * total + k];
-    sums[k] = a;
+// sums[k] = sum over rows b of rows[b][k] (k < total) in a fixed order: a block of 32 x 8 threads
+// takes 32 positions; thread (x, y) adds rows y, y + 8, y + 16, ... in order (four loads in
+// flight), and the 8 partial sums are then added in y order
+constexpr int kSumRowGroups = 8;
+
+__global__ void __launch_bounds__(32 * kSumRowGroups) sum_rows_kernel(
+    const double* __restrict__ rows, int nrows, int64_t total, double* __restrict__ sums) {
+  __shared__ double part[kSumRowGroups][32];
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * 32 + threadIdx.x;
+  const int y = threadIdx.y;
+  double a = 0.0;
+  if (k < total) {
+    int b = y;
+    for (; b + 3 * kSumRowGroups < nrows; b += 4 * kSumRowGroups) {
+      const double r0 = rows[static_cast<int64_t>(b) * total + k];
+      const double r1 = rows[static_cast<int64_t>(b + kSumRowGroups) * total + k];
+      const double r2 = rows[static_cast<int64_t>(b + 2 * kSumRowGroups) * total + k];
+      const double r3 = rows[static_cast<int64_t>(b + 3 * kSumRowGroups) * total + k];
+      a += r0;
+      a += r1;
+      a += r2;
+      a += r3;
+    }
+    for (; b < nrows; b += kSumRowGroups) a += rows[static_cast<int64_t>(b) * total + k];
+  }
+  part[y][threadIdx.x] = a;
+  __syncthreads();
+  if (y == 0 && k < total) {
+    double r = part[0][threadIdx.x];
+    for (int g = 1; g < kSumRowGroups; ++g) r += part[g][threadIdx.x];
+    sums[k] = r;
   }
 }
 
@@ -937,7 +961,7 @@ cudaError_t launch_multt_own(const SubPlan& p, cudaStream_t s, const float* xh, 
                                                     vl, nt, p.rows);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  sum_rows_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.total + 255) / 256)), 256, 0, s>>>(
+  sum_rows_kernel<<<static_cast<unsigned>((p.total + 31) / 32), dim3(32, kSumRowGroups), 0, s>>>(
       p.rows, static_cast<int>(rows), p.total, reinterpret_cast<double*>(p.acc));
   return cudaGetLastError();
 }
@@ -966,7 +990,7 @@ cudaError_t launch_multt_act(const SubPlan& p, cudaStream_t s, const float* xt, 
                                                     p.rows);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  sum_rows_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.total + 255) / 256)), 256, 0, s>>>(
+  sum_rows_kernel<<<static_cast<unsigned>((p.total + 31) / 32), dim3(32, kSumRowGroups), 0, s>>>(
       p.rows, static_cast<int>(rows), p.total, reinterpret_cast<double*>(p.acc));
   return cudaGetLastError();
 }
@@ -1164,7 +1188,7 @@ cudaError_t subspace_scatter_alpha_df(const SubPlan& p, cudaStream_t s, const fl
 
 cudaError_t subspace_finish_rows(const SubPlan& p, cudaStream_t s, int64_t nrows, int64_t npad,
                                  double* out64, const double* add, double scale_add) {
-  sum_rows_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (p.total + 255) / 256)), 256, 0, s>>>(
+  sum_rows_kernel<<<static_cast<unsigned>((p.total + 31) / 32), dim3(32, kSumRowGroups), 0, s>>>(
       p.rows, static_cast<int>(nrows), p.total, reinterpret_cast<double*>(p.acc));
   gather_sums_kernel<<<static_cast<unsigned>(std::min<int64_t>(1216, (npad + 255) / 256)), 256, 0, s>>>(
       reinterpret_cast<const double*>(p.acc), p.pos, p.n, npad, add, scale_add, out64);
