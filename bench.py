@@ -319,7 +319,8 @@ def run_ours(args):
                ("mult_mat32", sg.SGMEV_KERNEL_MULT_MAT32),
                ("multT_mat32", sg.SGMEV_KERNEL_MULTT_MAT32),
                ("mult_matdf64", sg.SGMEV_KERNEL_MULT_MATDF),
-               ("multT_matdf64", sg.SGMEV_KERNEL_MULTT_MATDF))}
+               ("multT_matdf64", sg.SGMEV_KERNEL_MULTT_MATDF),
+               ("system_mat32", sg.SGMEV_KERNEL_SYSTEM_MAT32))}
     op.profile(False)
     alpha = d_alpha.cpu().numpy()
     err = float(np.abs(alpha - alpha_ref).max() / np.abs(alpha_ref).max())

@@ -41,6 +41,7 @@ SGMEV_API int sgmev_fma_peak(int precision, double* flops_per_second, int* sm_cl
 #define SGMEV_KERNEL_MULTT_MAT32 11 /* FP32 multTranspose streaming them */
 #define SGMEV_KERNEL_MULT_MATDF 12 /* df64 mult streaming them */
 #define SGMEV_KERNEL_MULTT_MATDF 13 /* df64 multTranspose streaming them */
+#define SGMEV_KERNEL_SYSTEM_MAT32 14 /* FP32 B^T (B a) in one pass over them */
 SGMEV_API int sgmev_profile(sgmev_op* op, int enable);
 SGMEV_API int sgmev_profile_read(sgmev_op* op, int kind, int64_t* launches, double* seconds);
 

@@ -80,6 +80,7 @@ SGMEV_KERNEL_MULT_MAT32 = 10
 SGMEV_KERNEL_MULTT_MAT32 = 11
 SGMEV_KERNEL_MULT_MATDF = 12
 SGMEV_KERNEL_MULTT_MATDF = 13
+SGMEV_KERNEL_SYSTEM_MAT32 = 14
 
 
 # ---- exceptions (base/src/sgpp/base/exception/) --------------------------------------------

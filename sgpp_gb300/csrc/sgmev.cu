@@ -145,8 +145,8 @@ struct sgmev_op {
   std::vector<cudaEvent_t> prof_events;  // pool, 2 per launch
   std::vector<int> prof_kind;            // kind of launch i
   size_t prof_used = 0;                  // launches recorded since the last reset
-  int64_t prof_count[14] = {0};
-  double prof_seconds[14] = {0.0};
+  int64_t prof_count[15] = {0};
+  double prof_seconds[15] = {0.0};
 };
 
 namespace sgmev {
@@ -166,9 +166,10 @@ enum {
   KIND_MULT_MAT32 = 10,
   KIND_MULTT_MAT32 = 11,
   KIND_MULT_MATDF = 12,
-  KIND_MULTT_MATDF = 13
+  KIND_MULTT_MATDF = 13,
+  KIND_SYSTEM_MAT32 = 14
 };
-constexpr int kKinds = 14;
+constexpr int kKinds = 15;
 
 template <typename T>
 static int kind_mult() { return sizeof(T) == 4 ? KIND_MULT_FP32 : KIND_MULT_FP64; }
@@ -789,6 +790,15 @@ static int dev_convert(sgmev_op* op, const double* in, int64_t n, int64_t npad, 
 static int dev_system(sgmev_op* op, int prec, const double* a64, double* out64, double lm) {
   if (prec == SGMEV_FP32) {
     SGMEV_TRY(dev_convert(op, a64, op->npad, op->npad, nullptr, op->a32, nullptr));
+    if (op->sub_ok && op->mat_multt && mat_ready(op) && subspace_system_mat_fits(op->sub)) {
+      // one pass over the materialised products for B^T (B a)
+      const long ev = prof_begin(op, KIND_SYSTEM_MAT32);
+      SGMEV_CUDA(subspace_system_mat(op->sub, op->stream, op->mpad, op->a32, op->npad, out64, a64,
+                                     lm, op->num_sms));
+      prof_end(op, ev);
+      op->launches += 4;
+      return SGMEV_OK;
+    }
     SGMEV_TRY(dev_mult(op, prec, nullptr, op->a32, nullptr, nullptr, op->v32, 0, op->mpad));
     SGMEV_TRY(dev_multt(op, prec, nullptr, op->v32, nullptr, out64, 0, op->npad, a64, lm));
   } else if (prec == SGMEV_DF64) {

@@ -96,6 +96,12 @@ int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad);
 bool subspace_mat_fits(const SubPlan& p, bool df);
 cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, const float* xl,
                                  int64_t mpad, int64_t m, int num_sms);
+// fused FP32 system product out64 = B^T (B alpha) (+ scale_add * add), one pass over the
+// materialised products (grids of at most 1024 subspaces)
+bool subspace_system_mat_fits(const SubPlan& p);
+cudaError_t subspace_system_mat(const SubPlan& p, cudaStream_t s, int64_t mpad,
+                                const float* alpha32, int64_t npad, double* out64,
+                                const double* add, double scale_add, int num_sms);
 cudaError_t subspace_mult_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad, int64_t m,
                                  const float* ah, const float* al, double* out64, int64_t j_begin,
                                  int64_t j_end, int num_sms);

@@ -381,6 +381,159 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
   }
 }
 
+// ---- fused system product B^T (B a) --------------------------------------------------------
+// One CTA owns every subspace (s_pad <= kSysMaxSub, in passes of blockDim) and walks tiles of
+// kSysTile points: phase A streams the tile's P and C from HBM and forms (B a)_j exactly as
+// mat_mult_kernel (butterfly, per-warp partials, warp-order sum); phase B streams the same tile
+// again, now from L2 (a tile's slice is T * s_pad * 5 bytes, ~50 MB for all CTAs), and adds
+// (B a)_j * p into the owner's cells as mat_multt_kernel. So P and C leave HBM once per system
+// product instead of twice.
+constexpr int kSysTile = 64;                 // points per tile
+constexpr int kSysGroups = kSysTile / 4;
+constexpr int kSysAhead = 8;                 // ring depth (one CTA per SM: registers to spare)
+constexpr int kSysFlushTiles = 16;           // FP32 sums over 1024 points per flush
+constexpr int kSysMaxSub = 1024;
+static_assert(kSysGroups % kSysAhead == 0, "the ring must divide a tile");
+
+__global__ void __launch_bounds__(kMatThreads, 1) mat_system_kernel(
+    const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
+    const float* __restrict__ asub, int64_t n_tiles, const float4* __restrict__ pm,
+    const uint32_t* __restrict__ cm, double* __restrict__ rows) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* s_at = reinterpret_cast<float*>(smem);            // [cmax][s_pad] alpha by (cell, s)
+  float* s_acc = s_at + static_cast<size_t>(cmax) * s_pad;  // [cmax][s_pad] sums by (cell, s)
+  float* s_part = s_acc + static_cast<size_t>(cmax) * s_pad;  // [warps][kSysTile]
+  float* s_ba = s_part + kMatWarps * kSysTile;               // [kSysTile] (B a)_j
+  double* row = rows + static_cast<int64_t>(blockIdx.x) * total;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t cm1 = static_cast<uint32_t>(cmax - 1);
+  for (int k = tid; k < cmax * s_pad; k += blockDim.x) {
+    const int c = k / s_pad, sidx = k - c * s_pad;
+    float a = 0.0f;
+    if (sidx < n_sub) {
+      const int4 info = sact[sidx];
+      const int off = static_cast<int>(static_cast<uint32_t>(info.x) - static_cast<uint32_t>(info.z));
+      if (c < info.y) a = asub[off + c];
+    }
+    s_at[k] = a;
+    s_acc[k] = 0.0f;
+  }
+  __syncthreads();
+  int since = 0;
+  bool first = true;
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t g_base = tile * kSysGroups;  // first point group of the tile
+    // phase A: (B a)_j for the tile's points
+    for (int s0 = 0; s0 < s_pad; s0 += blockDim.x) {
+      if (s0 + warp * 32 >= s_pad) continue;
+      const int sid = s0 + tid;
+      const int64_t at = g_base * s_pad + sid;
+      const float* a_col = s_at + sid;
+      float* part = s_part + warp * kSysTile;
+      const bool pass0 = s0 == 0;
+      float4 ring[kSysAhead];
+      uint32_t cring[kSysAhead];
+#pragma unroll
+      for (int u = 0; u < kSysAhead; ++u) {
+        ring[u] = __ldcg(pm + at + static_cast<int64_t>(u) * s_pad);
+        cring[u] = __ldcg(cm + at + static_cast<int64_t>(u) * s_pad);
+      }
+      for (int g0 = 0; g0 < kSysGroups; g0 += kSysAhead) {
+#pragma unroll
+        for (int u = 0; u < kSysAhead; ++u) {
+          const int g = g0 + u;
+          const float4 p = ring[u];
+          const uint32_t cs = cring[u];
+          if (g + kSysAhead < kSysGroups) {
+            ring[u] = __ldcg(pm + at + static_cast<int64_t>(g + kSysAhead) * s_pad);
+            cring[u] = __ldcg(cm + at + static_cast<int64_t>(g + kSysAhead) * s_pad);
+          }
+          const float v0 = a_col[min(cs & 0xFFu, cm1) * s_pad] * p.x;
+          const float v1 = a_col[min((cs >> 8) & 0xFFu, cm1) * s_pad] * p.y;
+          const float v2 = a_col[min((cs >> 16) & 0xFFu, cm1) * s_pad] * p.z;
+          const float v3 = a_col[min(cs >> 24, cm1) * s_pad] * p.w;
+          const float r = reduce4(v0, v1, v2, v3, lane);
+          if ((lane & 7) == 0) {
+            float* dst = part + 4 * g + (lane >> 3);
+            *dst = pass0 ? r : *dst + r;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const int wrote = min(kMatWarps, s_pad / 32);
+    for (int jj = tid; jj < kSysTile; jj += blockDim.x) {
+      float r = 0.0f;
+      for (int w = 0; w < wrote; ++w) r += s_part[w * kSysTile + jj];
+      s_ba[jj] = r;  // points outside the data have P = 0, so their (B a)_j is 0
+    }
+    __syncthreads();
+    // phase B: the owner of subspace s adds (B a)_j * p_s(x_j) into its cells
+    for (int s0 = 0; s0 < s_pad; s0 += blockDim.x) {
+      const int sid = s0 + tid;
+      if (sid >= n_sub) continue;
+      const int64_t at = g_base * s_pad + sid;
+      float* acc = s_acc + sid;
+      float4 ring[kSysAhead];
+      uint32_t cring[kSysAhead];
+#pragma unroll
+      for (int u = 0; u < kSysAhead; ++u) {
+        ring[u] = __ldcs(pm + at + static_cast<int64_t>(u) * s_pad);
+        cring[u] = __ldcs(cm + at + static_cast<int64_t>(u) * s_pad);
+      }
+      for (int g0 = 0; g0 < kSysGroups; g0 += kSysAhead) {
+#pragma unroll
+        for (int u = 0; u < kSysAhead; ++u) {
+          const int g = g0 + u;
+          const float4 p = ring[u];
+          const uint32_t cs = cring[u];
+          if (g + kSysAhead < kSysGroups) {
+            ring[u] = __ldcs(pm + at + static_cast<int64_t>(g + kSysAhead) * s_pad);
+            cring[u] = __ldcs(cm + at + static_cast<int64_t>(g + kSysAhead) * s_pad);
+          }
+          const float4 ba = *reinterpret_cast<const float4*>(s_ba + 4 * g);
+          acc[min(cs & 0xFFu, cm1) * s_pad] += ba.x * p.x;
+          acc[min((cs >> 8) & 0xFFu, cm1) * s_pad] += ba.y * p.y;
+          acc[min((cs >> 16) & 0xFFu, cm1) * s_pad] += ba.z * p.z;
+          acc[min(cs >> 24, cm1) * s_pad] += ba.w * p.w;
+        }
+      }
+    }
+    ++since;
+    const bool last = tile + gridDim.x >= n_tiles;
+    if (since == kSysFlushTiles || last) {
+      for (int s0 = 0; s0 < n_sub; s0 += blockDim.x) {
+        const int sid = s0 + tid;
+        if (sid >= n_sub) continue;
+        const int4 info = sact[sid];
+        const uint32_t offset = static_cast<uint32_t>(info.x) - static_cast<uint32_t>(info.z);
+        for (int c = 0; c < info.y; ++c) {
+          float& a = s_acc[c * s_pad + sid];
+          double* dst = row + offset + c;
+          *dst = first ? static_cast<double>(a) : *dst + static_cast<double>(a);
+          a = 0.0f;
+        }
+      }
+      first = false;
+      since = 0;
+    }
+    __syncthreads();  // s_part and s_ba are rewritten by the next tile
+  }
+  if (first) {  // no tile for this CTA: its row holds zeros
+    for (int s0 = 0; s0 < n_sub; s0 += blockDim.x) {
+      const int sid = s0 + tid;
+      if (sid >= n_sub) continue;
+      const int4 info = sact[sid];
+      const uint32_t offset = static_cast<uint32_t>(info.x) - static_cast<uint32_t>(info.z);
+      for (int c = 0; c < info.y; ++c) row[offset + c] = 0.0;
+    }
+  }
+}
+
+size_t mat_system_smem(int cmax, int64_t s_pad) {
+  return sizeof(float) * (2 * static_cast<size_t>(cmax) * s_pad + kMatWarps * kSysTile + kSysTile);
+}
+
 int mat_threads(int64_t s_pad) { return static_cast<int>(std::min<int64_t>(kMatThreads, s_pad)); }
 
 size_t mat_mult_smem(int cmax, int64_t s_pad) {
@@ -439,6 +592,31 @@ cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, co
     return e;
   }
   return subspace_mat_build(*p, s, xh, xl, mpad, m, num_sms);
+}
+
+bool subspace_system_mat_fits(const SubPlan& p) {
+  const int64_t s_pad = (p.n_sub + 31) / 32 * 32;
+  return subspace_mat_fits(p, false) && s_pad <= kSysMaxSub &&
+         mat_system_smem(p.cmax, s_pad) <= kMatSmemBudget;
+}
+
+cudaError_t subspace_system_mat(const SubPlan& p, cudaStream_t s, int64_t mpad,
+                                const float* alpha32, int64_t npad, double* out64,
+                                const double* add, double scale_add, int num_sms) {
+  if (!p.pmat || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
+  cudaError_t e = subspace_scatter_alpha(p, s, alpha32);
+  if (e != cudaSuccess) return e;
+  const size_t sm = mat_system_smem(p.cmax, p.s_pad);
+  e = cudaFuncSetAttribute(mat_system_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  const int64_t nt = mpad / kSysTile;
+  const int64_t rows = std::min<int64_t>(num_sms, p.row_cap);
+  mat_system_kernel<<<static_cast<unsigned>(rows), kMatThreads, sm, s>>>(
+      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), p.asub, nt,
+      p.pmat, p.cmat, p.rows);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return subspace_finish_rows(p, s, rows, npad, out64, add, scale_add);
 }
 
 cudaError_t subspace_mult_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad, int64_t m,

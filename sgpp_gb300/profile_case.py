@@ -27,6 +27,7 @@ KINDS = {("mult", "float", "dense"): sg.SGMEV_KERNEL_MULT_FP32,
          ("multT", "float", "subspace"): sg.SGMEV_KERNEL_MULTT_SUB32,
          ("mult", "float", "materialized"): sg.SGMEV_KERNEL_MULT_MAT32,
          ("multT", "float", "materialized"): sg.SGMEV_KERNEL_MULTT_MAT32,
+         ("system", "float", "materialized"): sg.SGMEV_KERNEL_SYSTEM_MAT32,
          ("mult", "df64", "materialized"): sg.SGMEV_KERNEL_MULT_MATDF,
          ("multT", "df64", "materialized"): sg.SGMEV_KERNEL_MULTT_MATDF,
          ("mult", "double", "dense"): sg.SGMEV_KERNEL_MULT_FP64,
@@ -39,7 +40,8 @@ KINDS = {("mult", "float", "dense"): sg.SGMEV_KERNEL_MULT_FP32,
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["mult", "multT"], default="mult")
+    ap.add_argument("--kernel", choices=["mult", "multT", "system"], default="mult",
+                    help="system: B^T (B a) + lambda M a (systemApply)")
     ap.add_argument("--precision", choices=["float", "double", "df64"], default="float")
     ap.add_argument("--algo", choices=["dense", "subspace", "materialized"], default="dense",
                     help="materialized: subspace products kept in device memory (FP32)")
@@ -70,7 +72,9 @@ def main() -> int:
     out_t = np.zeros(n)
 
     def run():
-        if args.kernel == "mult":
+        if args.kernel == "system":
+            op.systemApply(a, out_t, 1e-4 * args.points)
+        elif args.kernel == "mult":
             op.mult(a, out_m)
         else:
             op.multTranspose(v, out_t)
