@@ -385,17 +385,21 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
 // One CTA owns every subspace (s_pad <= kSysMaxSub, in passes of blockDim) and walks tiles of
 // kSysTile points: phase A streams the tile's P and C from HBM and forms (B a)_j exactly as
 // mat_mult_kernel (butterfly, per-warp partials, warp-order sum); phase B streams the same tile
-// again, now from L2 (a tile's slice is T * s_pad * 5 bytes, ~50 MB for all CTAs), and adds
-// (B a)_j * p into the owner's cells as mat_multt_kernel. So P and C leave HBM once per system
-// product instead of twice.
-constexpr int kSysTile = 64;                 // points per tile
+// again, now from L2, and adds (B a)_j * p into the owner's cells as mat_multt_kernel. So P and
+// C leave HBM once per system product instead of twice. While a tile is processed, one thread asks
+// L2 for the CTA's next tile (two bulk prefetches, a hint with nothing to wait for), so that HBM
+// stays busy during phase B; a tile and its successor take 2 * T * s_pad * 5 bytes per CTA
+// (~50 MB of L2 for all CTAs at T = 32, s_pad = 1024).
+constexpr int kSysTile = 32;                 // points per tile
 constexpr int kSysGroups = kSysTile / 4;
-constexpr int kSysAhead = 8;                 // ring depth (one CTA per SM: registers to spare)
-constexpr int kSysFlushTiles = 16;           // FP32 sums over 1024 points per flush
+constexpr int kSysAhead = 4;                 // ring depth
+constexpr int kSysThreads = 1024;            // one CTA per SM, one subspace per thread
+constexpr int kSysWarps = kSysThreads / 32;
+constexpr int kSysFlushTiles = 32;           // FP32 sums over 1024 points per flush
 constexpr int kSysMaxSub = 1024;
 static_assert(kSysGroups % kSysAhead == 0, "the ring must divide a tile");
 
-__global__ void __launch_bounds__(kMatThreads, 1) mat_system_kernel(
+__global__ void __launch_bounds__(kSysThreads, 1) mat_system_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
     const float* __restrict__ asub, int64_t n_tiles, const float4* __restrict__ pm,
     const uint32_t* __restrict__ cm, double* __restrict__ rows) {
@@ -403,7 +407,7 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_system_kernel(
   float* s_at = reinterpret_cast<float*>(smem);            // [cmax][s_pad] alpha by (cell, s)
   float* s_acc = s_at + static_cast<size_t>(cmax) * s_pad;  // [cmax][s_pad] sums by (cell, s)
   float* s_part = s_acc + static_cast<size_t>(cmax) * s_pad;  // [warps][kSysTile]
-  float* s_ba = s_part + kMatWarps * kSysTile;               // [kSysTile] (B a)_j
+  float* s_ba = s_part + kSysWarps * kSysTile;               // [kSysTile] (B a)_j
   double* row = rows + static_cast<int64_t>(blockIdx.x) * total;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t cm1 = static_cast<uint32_t>(cmax - 1);
@@ -423,6 +427,13 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_system_kernel(
   bool first = true;
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t g_base = tile * kSysGroups;  // first point group of the tile
+    if (tid == 0 && tile + gridDim.x < n_tiles) {
+      const int64_t nb = (tile + gridDim.x) * kSysGroups * static_cast<int64_t>(s_pad);
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(pm + nb),
+                   "r"(static_cast<uint32_t>(sizeof(float4) * kSysGroups * s_pad)) : "memory");
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(cm + nb),
+                   "r"(static_cast<uint32_t>(sizeof(uint32_t) * kSysGroups * s_pad)) : "memory");
+    }
     // phase A: (B a)_j for the tile's points
     for (int s0 = 0; s0 < s_pad; s0 += blockDim.x) {
       if (s0 + warp * 32 >= s_pad) continue;
@@ -461,7 +472,7 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_system_kernel(
       }
     }
     __syncthreads();
-    const int wrote = min(kMatWarps, s_pad / 32);
+    const int wrote = min(kSysWarps, s_pad / 32);
     for (int jj = tid; jj < kSysTile; jj += blockDim.x) {
       float r = 0.0f;
       for (int w = 0; w < wrote; ++w) r += s_part[w * kSysTile + jj];
@@ -531,7 +542,7 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_system_kernel(
 }
 
 size_t mat_system_smem(int cmax, int64_t s_pad) {
-  return sizeof(float) * (2 * static_cast<size_t>(cmax) * s_pad + kMatWarps * kSysTile + kSysTile);
+  return sizeof(float) * (2 * static_cast<size_t>(cmax) * s_pad + kSysWarps * kSysTile + kSysTile);
 }
 
 int mat_threads(int64_t s_pad) { return static_cast<int>(std::min<int64_t>(kMatThreads, s_pad)); }
@@ -611,7 +622,7 @@ cudaError_t subspace_system_mat(const SubPlan& p, cudaStream_t s, int64_t mpad,
   if (e != cudaSuccess) return e;
   const int64_t nt = mpad / kSysTile;
   const int64_t rows = std::min<int64_t>(num_sms, p.row_cap);
-  mat_system_kernel<<<static_cast<unsigned>(rows), kMatThreads, sm, s>>>(
+  mat_system_kernel<<<static_cast<unsigned>(rows), kSysThreads, sm, s>>>(
       p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), p.asub, nt,
       p.pmat, p.cmat, p.rows);
   e = cudaGetLastError();
