@@ -429,8 +429,9 @@ def run_ours(args):
             "config": {"workload": f"regression fit, regular Linear grid d={DIM} level {LEVEL} "
                                    f"(N={n}), M={m} Gaussian-mixture points, lambda={LAMBDA}, "
                                    f"mixed-precision CG to relative FP64 residual {args.epsilon}",
-                       "l2_policy": "inputs larger than L2 (84 MB FP64 + 42 MB FP32 data, "
-                                    "re-read every operator application)",
+                       "l2_policy": "inputs larger than L2: every CG system product streams "
+                                    "the materialised subspace products (5.4 GB at M=2^20) from "
+                                    "HBM",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "latency_ms": {"p50": p(0.5), "p99": p(0.99)},
             "alpha_rel_err_vs_fp64": err, "cg_iterations": iters,
