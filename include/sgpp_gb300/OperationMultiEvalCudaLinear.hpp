@@ -37,8 +37,10 @@ namespace sgpp_gb300 {
 
 class OperationMultiEvalCudaLinear : public sgpp::base::OperationMultipleEval {
  public:
-  // precision: SGMEV_FP64 (default, parity with the reference) or SGMEV_FP32; read from the
-  // configuration's parameters ("precision": "float") when one is given.
+  // precision: SGMEV_FP64 (default, parity with the reference), SGMEV_FP32 or SGMEV_DF64; read
+  // from the configuration's parameters ("precision": "double" | "float" | "df64") when one is
+  // given, together with the library's other knobs ("algo", "materialize", "materialize_multt",
+  // "inner_tol", "precond"; see include/sgmev.h), which are passed through unchanged.
   OperationMultiEvalCudaLinear(sgpp::base::Grid& grid, sgpp::base::DataMatrix& dataset,
                                int precision = SGMEV_FP64)
       : OperationMultipleEval(grid, dataset), precision_(precision) {
@@ -49,9 +51,18 @@ class OperationMultiEvalCudaLinear : public sgpp::base::OperationMultipleEval {
                                sgpp::datadriven::OperationMultipleEvalConfiguration& config)
       : OperationMultipleEval(grid, dataset), precision_(SGMEV_FP64) {
     auto params = config.getParameters();
-    if (params && params->contains("precision") &&
-        (*params)["precision"].get() == std::string("float")) {
-      precision_ = SGMEV_FP32;
+    if (params && params->contains("precision")) {
+      const std::string p = (*params)["precision"].get();
+      if (p == "float") precision_ = SGMEV_FP32;
+      if (p == "df64") precision_ = SGMEV_DF64;
+    }
+    if (params) {
+      for (const char* key : {"algo", "materialize", "materialize_multt", "inner_tol", "precond"}) {
+        if (!params->contains(key)) continue;
+        knobs_ += knobs_.empty() ? "{" : ",";
+        knobs_ += std::string("\"") + key + "\":\"" + (*params)[key].get() + "\"";
+      }
+      if (!knobs_.empty()) knobs_ += "}";
     }
     create();
   }
@@ -100,7 +111,8 @@ class OperationMultiEvalCudaLinear : public sgpp::base::OperationMultipleEval {
   double getDuration() override { return sgmev_get_duration(op_); }
 
   std::string getImplementationName() override {
-    return precision_ == SGMEV_FP32 ? "CUDA_LINEAR_FP32" : "CUDA_LINEAR_FP64";
+    return precision_ == SGMEV_FP32 ? "CUDA_LINEAR_FP32"
+                                     : (precision_ == SGMEV_DF64 ? "CUDA_LINEAR_DF64" : "CUDA_LINEAR_FP64");
   }
 
  private:
@@ -124,7 +136,8 @@ class OperationMultiEvalCudaLinear : public sgpp::base::OperationMultipleEval {
     }
     check(sgmev_create(&op_, dim, n_grid_, level.data(), index.data(), n_data_,
                        dataset.getPointer(), unit ? nullptr : left.data(),
-                       unit ? nullptr : right.data(), precision_, nullptr));
+                       unit ? nullptr : right.data(), precision_,
+                       knobs_.empty() ? nullptr : knobs_.c_str()));
   }
 
   void export_grid(std::vector<double>& level, std::vector<double>& index) {
@@ -153,6 +166,7 @@ class OperationMultiEvalCudaLinear : public sgpp::base::OperationMultipleEval {
 
   sgmev_op* op_ = nullptr;
   int precision_;
+  std::string knobs_;  // flat JSON object of string knobs, or empty
   int64_t n_grid_ = 0;
   int64_t n_data_ = 0;
 };
