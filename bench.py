@@ -174,7 +174,7 @@ def mat_bytes_per_launch(kernel: str, lp, m: int, n: int) -> float:
     """Algorithmic HBM bytes of one launch of a kernel streaming the materialised products."""
     mpad = -(-m // 1024) * 1024
     s_pad = -(-subspace_count(lp) // 32) * 32
-    per_entry = 9 if "df64" in kernel else 5
+    per_entry = 9 if "df64" in kernel else (3 if "mat16" in kernel else 5)
     vec = (8 if "df64" in kernel else 4) * m + 8 * n
     return float(mpad) * s_pad * per_entry + vec
 
@@ -320,7 +320,9 @@ def run_ours(args):
                ("multT_mat32", sg.SGMEV_KERNEL_MULTT_MAT32),
                ("mult_matdf64", sg.SGMEV_KERNEL_MULT_MATDF),
                ("multT_matdf64", sg.SGMEV_KERNEL_MULTT_MATDF),
-               ("system_mat32", sg.SGMEV_KERNEL_SYSTEM_MAT32))}
+               ("system_mat32", sg.SGMEV_KERNEL_SYSTEM_MAT32),
+               ("mult_mat16", sg.SGMEV_KERNEL_MULT_MAT16),
+               ("multT_mat16", sg.SGMEV_KERNEL_MULTT_MAT16))}
     op.profile(False)
     alpha = d_alpha.cpu().numpy()
     err = float(np.abs(alpha - alpha_ref).max() / np.abs(alpha_ref).max())

@@ -92,7 +92,10 @@ SGMEV_API int sgmev_device_count(void);
  * it takes at most half of the free device memory and 64 GiB. The products are kept as
  * float-float pairs with their cell index (9 bytes each; grids whose subspaces have at most 256
  * cells), so the df64 (FP64-accurate) products stream them too. "materialize_multt": "on"
- * (default) or "off" — whether multTranspose streams them as well as mult.
+ * (default) or "off" — whether multTranspose streams them as well as mult. "inner_products":
+ * "half" (default) or "float" — the inner FP32 solves of mixed fits stream an FP16 copy of the
+ * products (3 bytes per entry instead of 5; the FP64-accurate outer residual keeps the result
+ * exact to the fit's tolerance).
  */
 SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double* level_pow2,
                            const double* index, int64_t n_data, const double* data,

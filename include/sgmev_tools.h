@@ -42,6 +42,8 @@ SGMEV_API int sgmev_fma_peak(int precision, double* flops_per_second, int* sm_cl
 #define SGMEV_KERNEL_MULT_MATDF 12 /* df64 mult streaming them */
 #define SGMEV_KERNEL_MULTT_MATDF 13 /* df64 multTranspose streaming them */
 #define SGMEV_KERNEL_SYSTEM_MAT32 14 /* FP32 B^T (B a) in one pass over them */
+#define SGMEV_KERNEL_MULT_MAT16 15 /* mult streaming their FP16 copy (inner solves of mixed fits) */
+#define SGMEV_KERNEL_MULTT_MAT16 16 /* multTranspose streaming it */
 SGMEV_API int sgmev_profile(sgmev_op* op, int enable);
 SGMEV_API int sgmev_profile_read(sgmev_op* op, int kind, int64_t* launches, double* seconds);
 

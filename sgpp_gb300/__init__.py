@@ -81,6 +81,8 @@ SGMEV_KERNEL_MULTT_MAT32 = 11
 SGMEV_KERNEL_MULT_MATDF = 12
 SGMEV_KERNEL_MULTT_MATDF = 13
 SGMEV_KERNEL_SYSTEM_MAT32 = 14
+SGMEV_KERNEL_MULT_MAT16 = 15
+SGMEV_KERNEL_MULTT_MAT16 = 16
 
 
 # ---- exceptions (base/src/sgpp/base/exception/) --------------------------------------------
@@ -467,7 +469,8 @@ class OperationMultiEvalCuda:
             left, right = bb.arrays()
         h = ctypes.c_void_p(None)
         knobs = {k: str(v) for k, v in (params or {}).items()
-                 if k in ("precond", "algo", "inner_tol", "materialize", "materialize_multt")}
+                 if k in ("precond", "algo", "inner_tol", "materialize", "materialize_multt",
+                          "inner_products")}
         pj = json.dumps(knobs).encode() if knobs else None
         _check(L.sgmev_create(ctypes.byref(h), st.getDimension(), st.getSize(), _vp(lp), _vp(ix),
                               self.dataset.shape[0], _vp(self.dataset), _vp(left), _vp(right),

@@ -133,6 +133,8 @@ struct sgmev_op {
   int mat_mode = 1;         // materialised FP32 products: 0 off, 1 auto, 2 on ("materialize")
   bool mat_multt = true;    // multTranspose streams them too ("materialize_multt")
   bool mat_failed = false;  // a build was refused or failed for the current grid
+  bool inner_half = true;   // inner solves of mixed fits use the FP16 products ("inner_products")
+  bool use_half = false;    // set while such an inner solve runs
   int algo = 2;          // FP32 products: 0 dense, 1 subspace, 2 auto (params "algo")
   SubPlan sub;           // subspace tables of the current grid
   bool sub_ok = false;   // sub is built and chosen for the FP32 products
@@ -145,8 +147,8 @@ struct sgmev_op {
   std::vector<cudaEvent_t> prof_events;  // pool, 2 per launch
   std::vector<int> prof_kind;            // kind of launch i
   size_t prof_used = 0;                  // launches recorded since the last reset
-  int64_t prof_count[15] = {0};
-  double prof_seconds[15] = {0.0};
+  int64_t prof_count[17] = {0};
+  double prof_seconds[17] = {0.0};
 };
 
 namespace sgmev {
@@ -167,9 +169,11 @@ enum {
   KIND_MULTT_MAT32 = 11,
   KIND_MULT_MATDF = 12,
   KIND_MULTT_MATDF = 13,
-  KIND_SYSTEM_MAT32 = 14
+  KIND_SYSTEM_MAT32 = 14,
+  KIND_MULT_MAT16 = 15,
+  KIND_MULTT_MAT16 = 16
 };
-constexpr int kKinds = 15;
+constexpr int kKinds = 17;
 
 template <typename T>
 static int kind_mult() { return sizeof(T) == 4 ? KIND_MULT_FP32 : KIND_MULT_FP64; }
@@ -710,9 +714,9 @@ static int dev_mult(sgmev_op* op, int prec, const double* a64, const float* a32,
     if (out64) SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
     if (out32) SGMEV_TRY((run_reduce<float2, float>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out32, nullptr, 0.0)));
   } else if (op->sub_ok && mat_ready(op)) {
-    const long ev = prof_begin(op, KIND_MULT_MAT32);
+    const long ev = prof_begin(op, op->use_half ? KIND_MULT_MAT16 : KIND_MULT_MAT32);
     SGMEV_CUDA(subspace_mult_mat(op->sub, op->stream, op->xt32, op->mpad, op->m, a32, out32, out64,
-                                 j_begin, j_end, op->num_sms));
+                                 j_begin, j_end, op->num_sms, op->use_half));
     prof_end(op, ev);
     op->launches += 2;
   } else if (op->sub_ok) {
@@ -759,9 +763,9 @@ static int dev_multt(sgmev_op* op, int prec, const double* v64, const float* v32
     SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->npad, g_begin, valid, g_end, out64, add, scale)));
   } else if (op->sub_ok && op->mat_multt && mat_ready(op)) {
     // the subspace sums produce every grid entry at once (the range is a subset of them)
-    const long ev = prof_begin(op, KIND_MULTT_MAT32);
+    const long ev = prof_begin(op, op->use_half ? KIND_MULTT_MAT16 : KIND_MULTT_MAT32);
     SGMEV_CUDA(subspace_multt_mat(op->sub, op->stream, op->xt32, op->mpad, op->m, v32, op->npad,
-                                  out64, add, scale, op->num_sms));
+                                  out64, add, scale, op->num_sms, op->use_half));
     prof_end(op, ev);
     op->launches += 3;
   } else if (op->sub_ok) {
@@ -790,7 +794,8 @@ static int dev_convert(sgmev_op* op, const double* in, int64_t n, int64_t npad, 
 static int dev_system(sgmev_op* op, int prec, const double* a64, double* out64, double lm) {
   if (prec == SGMEV_FP32) {
     SGMEV_TRY(dev_convert(op, a64, op->npad, op->npad, nullptr, op->a32, nullptr));
-    if (op->sub_ok && op->mat_multt && mat_ready(op) && subspace_system_mat_fits(op->sub)) {
+    if (!op->use_half && op->sub_ok && op->mat_multt && mat_ready(op) &&
+        subspace_system_mat_fits(op->sub)) {
       // one pass over the materialised products for B^T (B a)
       const long ev = prof_begin(op, KIND_SYSTEM_MAT32);
       SGMEV_CUDA(subspace_system_mat(op->sub, op->stream, op->mpad, op->a32, op->npad, out64, a64,
@@ -1068,6 +1073,9 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   const std::string mat = json_string(params_json, "materialize");
   if (!mat.empty() && mat != "auto" && mat != "on" && mat != "off")
     return fail(SGMEV_ERR_INVALID, "params: materialize must be \"auto\", \"on\" or \"off\"");
+  const std::string inner_p = json_string(params_json, "inner_products");
+  if (!inner_p.empty() && inner_p != "half" && inner_p != "float")
+    return fail(SGMEV_ERR_INVALID, "params: inner_products must be \"half\" or \"float\"");
   const std::string mat_t = json_string(params_json, "materialize_multt");
   if (!mat_t.empty() && mat_t != "on" && mat_t != "off")
     return fail(SGMEV_ERR_INVALID, "params: materialize_multt must be \"on\" or \"off\"");
@@ -1085,6 +1093,7 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   op->precond = precond == "jacobi";
   op->mat_mode = mat == "off" ? 0 : (mat == "on" ? 2 : 1);
   op->mat_multt = mat_t != "off";
+  op->inner_half = inner_p != "float";
   {
     const std::string it = json_string(params_json, "inner_tol");
     if (!it.empty()) {
@@ -1601,6 +1610,13 @@ static int fit_common(sgmev_op* op, int mode, const double* y, bool y_on_device,
       int64_t it = 0;
       double dres = 0.0;
       const double want = std::max(eps_inner, epsilon * std::sqrt(r0 / rnorm2) * 0.5);
+      // the inner solve may use the FP16 copy of the materialised products: the outer residual
+      // is FP64-accurate, so the refinement still converges to the FP64 solution
+      struct HalfScope {
+        sgmev_op* o;
+        explicit HalfScope(sgmev_op* op_) : o(op_) { o->use_half = o->inner_half; }
+        ~HalfScope() { o->use_half = false; }
+      } half_scope(op);
       if (op->precond) {
         SGMEV_TRY(pcg_core(op, SGMEV_FP32, rr, dx, lm, max_iterations - total_it,
                            std::min(want, 0.5), &it));

@@ -20,6 +20,7 @@
 //               int64 vector after every 512-point tile (so no word sum can overflow); integer
 //               addition is exact and associative, so the result is the same bit for bit
 //               whatever the order of the atomic updates
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -586,7 +587,7 @@ template <int DIM>
 __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_mat_build_kernel(
     const int4* __restrict__ desc, const int4* __restrict__ sinfo, int n_sub, int s_pad,
     const float* __restrict__ xh_t, const float* __restrict__ xl_t, int64_t mpad, int64_t m,
-    int64_t n_tiles, float4* __restrict__ phi, float4* __restrict__ plo,
+    int64_t n_tiles, float4* __restrict__ phi, float4* __restrict__ plo, uint2* __restrict__ p16,
     uint32_t* __restrict__ cm) {
   using Lay = OwnLayout<DIM, true>;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -649,6 +650,9 @@ __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_mat_build_kernel(
         const int64_t k = at + static_cast<int64_t>(g) * s_pad;
         phi[k] = make_float4(hv[0], hv[1], hv[2], hv[3]);
         plo[k] = make_float4(lv[0], lv[1], lv[2], lv[3]);
+        const __half2 h01 = __floats2half2_rn(hv[0], hv[1]), h23 = __floats2half2_rn(hv[2], hv[3]);
+        p16[k] = make_uint2(*reinterpret_cast<const uint32_t*>(&h01),
+                            *reinterpret_cast<const uint32_t*>(&h23));
         cm[k] = cells;
       }
     }
@@ -668,7 +672,7 @@ cudaError_t launch_mat_build(const SubPlan& p, cudaStream_t s, const float* xh, 
   const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, 2LL * num_sms));
   kern<<<static_cast<unsigned>(blocks), nth, sm, s>>>(p.desc, p.sinfo, p.n_sub,
                                                       static_cast<int>(p.s_pad), xh, xl, mpad, m,
-                                                      nt, p.pmat, p.pmat_lo, p.cmat);
+                                                      nt, p.pmat, p.pmat_lo, p.pmat16, p.cmat);
   return cudaGetLastError();
 }
 
@@ -1141,6 +1145,7 @@ void subspace_free(SubPlan* p) {
   cudaFree(p->sinfo);
   cudaFree(p->pmat);
   cudaFree(p->pmat_lo);
+  cudaFree(p->pmat16);
   cudaFree(p->cmat);
   cudaFree(p->act);
   cudaFree(p->sact);

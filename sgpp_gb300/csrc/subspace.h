@@ -39,6 +39,7 @@ struct SubPlan {
   // built
   float4* pmat = nullptr;
   float4* pmat_lo = nullptr;
+  uint2* pmat16 = nullptr;  // the same products rounded to FP16 (four halves per entry)
   uint32_t* cmat = nullptr;
   int64_t s_pad = 0;
   int64_t mat_mpad = 0;
@@ -83,7 +84,7 @@ cudaError_t subspace_finish_rows(const SubPlan& p, cudaStream_t s, int64_t nrows
                                  double* out64, const double* add, double scale_add);
 cudaError_t subspace_scatter_alpha_df(const SubPlan& p, cudaStream_t s, const float* ah,
                                       const float* al);
-// fills pmat, pmat_lo and cmat (allocated, s_pad set) from the float-float data (xh, xl)
+// fills pmat, pmat_lo, pmat16 and cmat (allocated, s_pad set) from the float-float data (xh, xl)
 cudaError_t subspace_mat_build(const SubPlan& p, cudaStream_t s, const float* xh,
                                const float* xl, int64_t mpad, int64_t m, int num_sms);
 
@@ -108,12 +109,15 @@ cudaError_t subspace_mult_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad,
 cudaError_t subspace_multt_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad,
                                   const float* vh, const float* vl, int64_t npad, double* out64,
                                   const double* add, double scale_add, int num_sms);
+// half: stream the FP16 copy of the products (3 bytes per entry instead of 5; products good to
+// 2^-11, for the inner solves of mixed fits)
 cudaError_t subspace_mult_mat(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
                               int64_t m, const float* alpha32, float* out32, double* out64,
-                              int64_t j_begin, int64_t j_end, int num_sms);
+                              int64_t j_begin, int64_t j_end, int num_sms, bool half = false);
 cudaError_t subspace_multt_mat(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
                                int64_t m, const float* v32, int64_t npad, double* out64,
-                               const double* add, double scale_add, int num_sms);
+                               const double* add, double scale_add, int num_sms,
+                               bool half = false);
 
 // FP64-accurate (float-float) multTranspose: x as (xh, xl), v as (vh, vl) [mpad]
 cudaError_t subspace_multt_df(const SubPlan& p, cudaStream_t s, const float* xh, const float* xl,

@@ -21,6 +21,7 @@
 //          order.
 // The float-float variants do the same with float-float products, sums and butterfly.
 // Every sum has a fixed order, so results are the same bit for bit from run to run.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -62,11 +63,29 @@ __device__ __forceinline__ float reduce4(float v0, float v1, float v2, float v3,
   return b;
 }
 
+// products of a point group as stored: FP32 (float4) or FP16 (four halves in a uint2)
+template <bool HALF>
+struct Prod {
+  using T = float4;
+  static __device__ __forceinline__ float4 get(float4 v) { return v; }
+};
+template <>
+struct Prod<true> {
+  using T = uint2;
+  static __device__ __forceinline__ float4 get(uint2 v) {
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&v.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&v.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+  }
+};
+
+template <bool HALF>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
     const float* __restrict__ asub, int64_t m, int64_t tile_begin, int64_t n_tiles,
-    const float4* __restrict__ pm, const uint32_t* __restrict__ cm,
+    const typename Prod<HALF>::T* __restrict__ pm, const uint32_t* __restrict__ cm,
     float* __restrict__ out32, double* __restrict__ out64) {
+  using PT = typename Prod<HALF>::T;
   extern __shared__ __align__(16) unsigned char smem[];
   float* s_part = reinterpret_cast<float*>(smem);   // [warps][kOwnTile]
   float* s_at = s_part + kMatWarps * kOwnTile;      // [cmax][s_pad] alpha by (cell, subspace)
@@ -90,12 +109,12 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
       if (s0 + warp * 32 >= s_pad) continue;  // whole warps: s_pad is a multiple of 32
       const int sid = s0 + tid;
       const int64_t at = gt * kGroups * static_cast<int64_t>(s_pad) + sid;
-      const float4* src = pm + at;
+      const PT* src = pm + at;
       const uint32_t* csrc = cm + at;
       const float* a_col = s_at + sid;
       float* part = s_part + warp * kOwnTile;
       const bool first = s0 == 0;
-      float4 ring[kAhead];
+      PT ring[kAhead];
       uint32_t cring[kAhead];
 #pragma unroll
       for (int u = 0; u < kAhead; ++u) {
@@ -106,7 +125,7 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
 #pragma unroll
         for (int u = 0; u < kAhead; ++u) {
           const int g = g0 + u;
-          const float4 p = ring[u];
+          const float4 p = Prod<HALF>::get(ring[u]);
           const uint32_t cs = cring[u];
           if (g + kAhead < kGroups) {
             ring[u] = __ldcs(src + static_cast<int64_t>(g + kAhead) * s_pad);
@@ -141,10 +160,12 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
 }
 
 // ---- multTranspose -------------------------------------------------------------------------
+template <bool HALF>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
-    const float* __restrict__ v, int64_t n_tiles, const float4* __restrict__ pm,
+    const float* __restrict__ v, int64_t n_tiles, const typename Prod<HALF>::T* __restrict__ pm,
     const uint32_t* __restrict__ cm, double* __restrict__ rows) {
+  using PT = typename Prod<HALF>::T;
   extern __shared__ __align__(16) unsigned char smem[];
   float* s_acc = reinterpret_cast<float*>(smem);  // [cmax][blockDim]
   double* row = rows + static_cast<int64_t>(blockIdx.x) * total;
@@ -162,10 +183,10 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
     int since = 0;  // tiles summed in s_acc since the last flush
     for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
       const int64_t at = tile * kGroups * static_cast<int64_t>(s_pad) + sid;
-      const float4* src = pm + at;
+      const PT* src = pm + at;
       const uint32_t* csrc = cm + at;
       const float4* vt = v4 + tile * kGroups;
-      float4 ring[kAhead];
+      PT ring[kAhead];
       uint32_t cring[kAhead];
 #pragma unroll
       for (int u = 0; u < kAhead; ++u) {
@@ -176,7 +197,7 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
 #pragma unroll
         for (int u = 0; u < kAhead; ++u) {
           const int g = g0 + u;
-          const float4 p = ring[u];
+          const float4 p = Prod<HALF>::get(ring[u]);
           const uint32_t cs = cring[u];
           if (g + kAhead < kGroups) {
             ring[u] = __ldcs(src + static_cast<int64_t>(g + kAhead) * s_pad);
@@ -578,26 +599,31 @@ bool subspace_mat_fits(const SubPlan& p, bool df) {
 }
 
 int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad) {
-  return mpad * ((p.n_sub + 31) / 32 * 32) * static_cast<int64_t>(2 * sizeof(float) + 1);
+  return mpad * ((p.n_sub + 31) / 32 * 32) * static_cast<int64_t>(2 * sizeof(float) + 2 + 1);
 }
 
 cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, const float* xl,
                                  int64_t mpad, int64_t m, int num_sms) {
   cudaFree(p->pmat);
   cudaFree(p->pmat_lo);
+  cudaFree(p->pmat16);
   cudaFree(p->cmat);
   p->pmat = p->pmat_lo = nullptr;
+  p->pmat16 = nullptr;
   p->cmat = nullptr;
   p->s_pad = (p->n_sub + 31) / 32 * 32;
   p->mat_mpad = mpad;
   const size_t entries = static_cast<size_t>(mpad / 4) * static_cast<size_t>(p->s_pad);
   cudaError_t e = cudaMalloc(&p->pmat, entries * sizeof(float4));
   if (e == cudaSuccess) e = cudaMalloc(&p->pmat_lo, entries * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMalloc(&p->pmat16, entries * sizeof(uint2));
   if (e == cudaSuccess) e = cudaMalloc(&p->cmat, entries * sizeof(uint32_t));
   if (e != cudaSuccess) {
     cudaFree(p->pmat);
     cudaFree(p->pmat_lo);
+    cudaFree(p->pmat16);
     p->pmat = p->pmat_lo = nullptr;
+    p->pmat16 = nullptr;
     p->cmat = nullptr;
     (void)cudaGetLastError();
     return e;
@@ -673,46 +699,65 @@ cudaError_t subspace_multt_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad
   return subspace_finish_rows(p, s, rows, npad, out64, add, scale_add);
 }
 
+namespace {
+template <bool HALF>
+cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, const typename Prod<HALF>::T* pm,
+                            int64_t m, float* out32, double* out64, int64_t t0, int64_t nt,
+                            int num_sms) {
+  auto kern = mat_mult_kernel<HALF>;
+  const size_t sm = mat_mult_smem(p.cmax, p.s_pad);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMatThreads, sm);
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
+  kern<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
+      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub, m, t0, nt, pm, p.cmat, out32,
+      out64);
+  return cudaGetLastError();
+}
+
+template <bool HALF>
+cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, const typename Prod<HALF>::T* pm,
+                             int64_t mpad, const float* v32, int num_sms, int64_t* rows) {
+  auto kern = mat_multt_kernel<HALF>;
+  const size_t sm = mat_multt_smem(p.cmax, p.s_pad);
+  const int nth = mat_threads(p.s_pad);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
+  if (e != cudaSuccess) return e;
+  const int64_t nt = mpad / kOwnTile;
+  *rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), p.row_cap);
+  kern<<<static_cast<unsigned>(*rows), nth, sm, s>>>(p.sact, p.n_sub, static_cast<int>(p.s_pad),
+                                                     p.cmax, static_cast<int>(p.total), v32, nt,
+                                                     pm, p.cmat, p.rows);
+  return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t subspace_mult_mat(const SubPlan& p, cudaStream_t s, const float* /*xt*/, int64_t mpad,
                               int64_t m, const float* alpha32, float* out32, double* out64,
-                              int64_t j_begin, int64_t j_end, int num_sms) {
-  if (!p.pmat || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
+                              int64_t j_begin, int64_t j_end, int num_sms, bool half) {
+  if (!p.pmat || !p.pmat16 || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
   cudaError_t e = subspace_scatter_alpha(p, s, alpha32);
   if (e != cudaSuccess) return e;
   const int64_t t0 = j_begin / kOwnTile;
   const int64_t nt = (j_end + kOwnTile - 1) / kOwnTile - t0;
   if (nt <= 0) return cudaSuccess;
-  const size_t sm = mat_mult_smem(p.cmax, p.s_pad);
-  e = cudaFuncSetAttribute(mat_mult_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mat_mult_kernel, kMatThreads, sm);
-  if (e != cudaSuccess) return e;
-  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
-  mat_mult_kernel<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
-      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub, m, t0, nt, p.pmat, p.cmat,
-      out32, out64);
-  return cudaGetLastError();
+  return half ? launch_mat_mult<true>(p, s, p.pmat16, m, out32, out64, t0, nt, num_sms)
+              : launch_mat_mult<false>(p, s, p.pmat, m, out32, out64, t0, nt, num_sms);
 }
 
 cudaError_t subspace_multt_mat(const SubPlan& p, cudaStream_t s, const float* /*xt*/, int64_t mpad,
-                               int64_t m, const float* v32, int64_t npad, double* out64,
-                               const double* add, double scale_add, int num_sms) {
-  (void)m;
-  if (!p.pmat || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
-  const size_t sm = mat_multt_smem(p.cmax, p.s_pad);
-  const int nth = mat_threads(p.s_pad);
-  cudaError_t e = cudaFuncSetAttribute(mat_multt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mat_multt_kernel, nth, sm);
-  if (e != cudaSuccess) return e;
-  const int64_t nt = mpad / kOwnTile;
-  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), p.row_cap);
-  mat_multt_kernel<<<static_cast<unsigned>(rows), nth, sm, s>>>(
-      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), v32, nt,
-      p.pmat, p.cmat, p.rows);
-  e = cudaGetLastError();
+                               int64_t /*m*/, const float* v32, int64_t npad, double* out64,
+                               const double* add, double scale_add, int num_sms, bool half) {
+  if (!p.pmat || !p.pmat16 || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
+  int64_t rows = 0;
+  cudaError_t e = half ? launch_mat_multt<true>(p, s, p.pmat16, mpad, v32, num_sms, &rows)
+                       : launch_mat_multt<false>(p, s, p.pmat, mpad, v32, num_sms, &rows);
   if (e != cudaSuccess) return e;
   return subspace_finish_rows(p, s, rows, npad, out64, add, scale_add);
 }

@@ -368,6 +368,30 @@ def test_subspace_shapes_match_oracle(oracle, dim, level, precision, tol, algo):
     assert rel_err(outt, st.mult_transpose(lp, ix, v)) < tol
 
 
+@pytest.mark.parametrize("products", ["half", "float"])
+def test_mixed_fit_inner_products(products):
+    """params "inner_products": the inner solves stream the FP16 or the FP32 copy of the
+    materialised products; either way the refinement reaches the FP64 solution."""
+    g = load_golden("cgfit.npz")
+    for name in ("d4_l4", "d6_l3"):
+        grid = _grid_from(g, name)
+        cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                    sg.OperationMultipleEvalSubType.CUDA,
+                                                    parameters={"inner_products": products,
+                                                                "algo": "subspace",
+                                                                "materialize": "on"})
+        op = sg.createOperationMultipleEval(grid, g[name + "_x"], cfg)
+        alpha, _, _ = op.fit(g[name + "_y"], float(g[name + "_lambda"]), 5000, 1e-10,
+                             mode=sg.SGMEV_SOLVE_MIXED)
+        assert rel_err(alpha, g[name + "_alpha"]) < 1e-6
+        op.close()
+    cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                sg.OperationMultipleEvalSubType.CUDA,
+                                                parameters={"inner_products": "bf16"})
+    with pytest.raises(Exception):
+        sg.createOperationMultipleEval(grid, g[name + "_x"], cfg)
+
+
 def test_inner_tolerance_knob():
     """params "inner_tol": any value in (0, 1) reaches the same FP64 solution; others raise."""
     g = load_golden("cgfit.npz")
