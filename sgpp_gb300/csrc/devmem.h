@@ -1,0 +1,27 @@
+// Device memory of the operators (internal to libsgpp_gb300): stream-ordered allocations, so
+// that creating and destroying operators in several host threads never synchronises the whole
+// device (cudaFree does), and small pinned host blocks recycled instead of freed.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace sgmev {
+
+// cudaMallocAsync on `s` from the device's default pool, which keeps freed memory for reuse
+// (its release threshold is raised once per device); *p is nullptr on failure
+cudaError_t dev_malloc(void** p, size_t bytes, cudaStream_t s);
+
+template <typename T>
+inline cudaError_t dev_malloc(T** p, size_t bytes, cudaStream_t s) {
+  return dev_malloc(reinterpret_cast<void**>(p), bytes, s);
+}
+
+// cudaFreeAsync on `s` (nullptr is accepted); the memory is reused once `s` reaches this point
+void dev_free(void* p, cudaStream_t s);
+
+// 64-byte pinned host blocks for scalars read back from the device
+void* pinned_block();
+void pinned_release(void* p);
+
+}  // namespace sgmev

@@ -21,6 +21,7 @@
 
 #include "../../include/sgmev.h"
 #include "kernels.cuh"
+#include "devmem.h"
 #include "subspace.h"
 
 namespace sgmev {
@@ -671,10 +672,12 @@ static bool mat_ready(sgmev_op* op) {
   if (subspace_materialize(&op->sub, op->stream, op->xt32, op->xt32lo, op->mpad, op->m,
                            op->num_sms) != cudaSuccess) {
     (void)cudaGetLastError();
-    cudaFree(op->sub.pmat);
-    cudaFree(op->sub.pmat_lo);
-    cudaFree(op->sub.cmat);
+    dev_free(op->sub.pmat, op->stream);
+    dev_free(op->sub.pmat_lo, op->stream);
+    dev_free(op->sub.pmat16, op->stream);
+    dev_free(op->sub.cmat, op->stream);
     op->sub.pmat = op->sub.pmat_lo = nullptr;
+    op->sub.pmat16 = nullptr;
     op->sub.cmat = nullptr;
     op->mat_failed = true;
     return false;
@@ -841,13 +844,13 @@ static int dev_axpy(sgmev_op* op, int64_t n, double a, const double* x, double* 
 // allocation helpers
 // ---------------------------------------------------------------------------------------
 template <typename T>
-static int dalloc(T** p, size_t count) {
+static int dalloc(cudaStream_t s, T** p, size_t count) {
   if (*p) {
-    cudaFree(*p);
+    dev_free(*p, s);
     *p = nullptr;
   }
   if (count == 0) count = 1;
-  SGMEV_CUDA(cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T)));
+  SGMEV_CUDA(dev_malloc(p, count * sizeof(T), s));
   return SGMEV_OK;
 }
 
@@ -891,13 +894,13 @@ static int check_grid(int dim, int64_t n, const double* level_pow2, const double
 static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const double* index) {
   const int64_t npad = std::max<int64_t>(round_up(std::max<int64_t>(n, 1), kNPadTo), kNPadTo);
   if (npad > op->npad_cap) {
-    SGMEV_TRY(dalloc(&op->li64, static_cast<size_t>(npad * op->dim)));
-    SGMEV_TRY(dalloc(&op->li32, static_cast<size_t>(npad * op->dim)));
-    SGMEV_TRY(dalloc(&op->gq, static_cast<size_t>(npad * op->dim)));
-    SGMEV_TRY(dalloc(&op->a64, static_cast<size_t>(npad)));
-    SGMEV_TRY(dalloc(&op->a32, static_cast<size_t>(npad)));
-    SGMEV_TRY(dalloc(&op->a32lo, static_cast<size_t>(npad)));
-    SGMEV_TRY(dalloc(&op->cg, static_cast<size_t>(npad) * kCgSlots));
+    SGMEV_TRY(dalloc(op->stream, &op->li64, static_cast<size_t>(npad * op->dim)));
+    SGMEV_TRY(dalloc(op->stream, &op->li32, static_cast<size_t>(npad * op->dim)));
+    SGMEV_TRY(dalloc(op->stream, &op->gq, static_cast<size_t>(npad * op->dim)));
+    SGMEV_TRY(dalloc(op->stream, &op->a64, static_cast<size_t>(npad)));
+    SGMEV_TRY(dalloc(op->stream, &op->a32, static_cast<size_t>(npad)));
+    SGMEV_TRY(dalloc(op->stream, &op->a32lo, static_cast<size_t>(npad)));
+    SGMEV_TRY(dalloc(op->stream, &op->cg, static_cast<size_t>(npad) * kCgSlots));
     op->npad_cap = npad;
   }
   op->n = n;
@@ -906,11 +909,11 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
   double* d_l = nullptr;
   double* d_i = nullptr;
   const size_t bytes = sizeof(double) * static_cast<size_t>(std::max<int64_t>(n * op->dim, 1));
-  SGMEV_CUDA(cudaMalloc(&d_l, bytes));
-  cudaError_t e = cudaMalloc(&d_i, bytes);
+  SGMEV_CUDA(dev_malloc(&d_l, bytes, op->stream));
+  cudaError_t e = dev_malloc(&d_i, bytes, op->stream);
   if (e != cudaSuccess) {
-    cudaFree(d_l);
-    return fail(SGMEV_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    dev_free(d_l, op->stream);
+    return fail(SGMEV_ERR_OOM, std::string("device allocation: ") + cudaGetErrorString(e));
   }
   if (n > 0) {
     cudaMemcpyAsync(d_l, level_pow2, bytes, cudaMemcpyHostToDevice, op->stream);
@@ -920,8 +923,8 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
       d_l, d_i, n, op->dim, npad, op->li64, op->li32, op->gq);
   op->launches += 1;
   e = cudaStreamSynchronize(op->stream);
-  cudaFree(d_l);
-  cudaFree(d_i);
+  dev_free(d_l, op->stream);
+  dev_free(d_i, op->stream);
   if (e != cudaSuccess) return fail(SGMEV_ERR_CUDA, std::string("stage grid: ") + cudaGetErrorString(e));
   // subspace tables for the FP32 products: used when chosen ("algo") and cheaper by the
   // instruction count per data point (one basis function per subspace, ~8 per active dimension
@@ -931,7 +934,7 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
   subspace_free(&op->sub);
   if (op->algo != 0 && n > 0) {
     std::string why;
-    if (subspace_build(&op->sub, op->dim, n, level_pow2, index, &why)) {
+    if (subspace_build(&op->sub, op->dim, n, level_pow2, index, op->stream, &why)) {
       const double dense_cost = 3.0 * op->dim * static_cast<double>(n);
       const double sub_cost = 8.0 * static_cast<double>(op->sub.act_work) + 10.0 * op->sub.n_sub;
       op->sub_ok = op->algo == 1 || sub_cost * 1.5 < dense_cost;
@@ -941,15 +944,15 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
     }
   }
   // output vector and split partials depend on npad
-  SGMEV_TRY(dalloc(&op->out64, static_cast<size_t>(std::max(op->npad, op->mpad))));
+  SGMEV_TRY(dalloc(op->stream, &op->out64, static_cast<size_t>(std::max(op->npad, op->mpad))));
   const int64_t elems = part_need_elems(op);
   const size_t need = static_cast<size_t>(elems) * sizeof(double);
   if (need > op->part_bytes) {
-    if (op->part) cudaFree(op->part);
+    dev_free(op->part, op->stream);
     op->part = nullptr;
     op->part_bytes = 0;
     op->part_elems = 0;
-    SGMEV_CUDA(cudaMalloc(&op->part, need));
+    SGMEV_CUDA(dev_malloc(&op->part, need, op->stream));
     op->part_bytes = need;
   }
   op->part_elems = static_cast<int64_t>(op->part_bytes / sizeof(double));
@@ -957,17 +960,21 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
 }
 
 static void release(sgmev_op* op) {
+  // the operator's own work is done before its memory is handed back (a wait on its stream
+  // only; frees are stream-ordered and never synchronise the device)
+  if (op->stream) cudaStreamSynchronize(op->stream);
+  subspace_free(&op->sub);
   void* ptrs[] = {op->xt64, op->xt32, op->xt32lo, op->li64, op->li32, op->gq, op->a64,
                   op->a32,  op->a32lo, op->v64,   op->v32,  op->v32lo, op->out64, op->part,
                   op->cg,   op->dot_part, op->dot_out};
-  for (void* p : ptrs)
-    if (p) cudaFree(p);
-  if (op->host_scalar) cudaFreeHost(op->host_scalar);
+  for (void* p : ptrs) dev_free(p, op->stream);
+  pinned_release(op->host_scalar);
+  op->host_scalar = nullptr;
   for (cudaEvent_t e : op->prof_events) cudaEventDestroy(e);
   if (op->ev_start) cudaEventDestroy(op->ev_start);
   if (op->ev_stop) cudaEventDestroy(op->ev_stop);
   if (op->own_stream) cudaStreamDestroy(op->own_stream);
-  subspace_free(&op->sub);
+  (void)cudaGetLastError();
 }
 
 static int begin_timed(sgmev_op* op) {
@@ -1133,22 +1140,23 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   op->stream = op->own_stream;
   CREATE_CUDA(cudaEventCreate(&op->ev_start));
   CREATE_CUDA(cudaEventCreate(&op->ev_stop));
-  CREATE_CUDA(cudaMallocHost(&op->host_scalar, sizeof(double) * 8));
-  CREATE_TRY(dalloc(&op->dot_part, kDotBlocks));
-  CREATE_TRY(dalloc(&op->dot_out, 8));
+  op->host_scalar = static_cast<double*>(pinned_block());
+  if (!op->host_scalar) return bail(fail(SGMEV_ERR_OOM, "pinned host block"));
+  CREATE_TRY(dalloc(op->stream, &op->dot_part, kDotBlocks));
+  CREATE_TRY(dalloc(op->stream, &op->dot_out, 8));
 
   // data
-  CREATE_TRY(dalloc(&op->xt64, static_cast<size_t>(op->mpad * dim)));
-  CREATE_TRY(dalloc(&op->xt32, static_cast<size_t>(op->mpad * dim)));
-  CREATE_TRY(dalloc(&op->xt32lo, static_cast<size_t>(op->mpad * dim)));
-  CREATE_TRY(dalloc(&op->v64, static_cast<size_t>(op->mpad)));
-  CREATE_TRY(dalloc(&op->v32, static_cast<size_t>(op->mpad)));
-  CREATE_TRY(dalloc(&op->v32lo, static_cast<size_t>(op->mpad)));
+  CREATE_TRY(dalloc(op->stream, &op->xt64, static_cast<size_t>(op->mpad * dim)));
+  CREATE_TRY(dalloc(op->stream, &op->xt32, static_cast<size_t>(op->mpad * dim)));
+  CREATE_TRY(dalloc(op->stream, &op->xt32lo, static_cast<size_t>(op->mpad * dim)));
+  CREATE_TRY(dalloc(op->stream, &op->v64, static_cast<size_t>(op->mpad)));
+  CREATE_TRY(dalloc(op->stream, &op->v32, static_cast<size_t>(op->mpad)));
+  CREATE_TRY(dalloc(op->stream, &op->v32lo, static_cast<size_t>(op->mpad)));
   {
     double* d_rows = nullptr;
     double* d_bb = nullptr;
     const size_t rbytes = sizeof(double) * static_cast<size_t>(std::max<int64_t>(n_data * dim, 1));
-    CREATE_CUDA(cudaMalloc(&d_rows, rbytes));
+    CREATE_CUDA(dev_malloc(&d_rows, rbytes, op->stream));
     if (n_data > 0) cudaMemcpyAsync(d_rows, data, rbytes, cudaMemcpyHostToDevice, op->stream);
     if (bb_left) {
       op->bb_left.assign(bb_left, bb_left + dim);
@@ -1159,10 +1167,10 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
         hb[t] = bb_left[t];
         hb[dim + t] = op->bb_width[t];
       }
-      cudaError_t e = cudaMalloc(&d_bb, sizeof(double) * 2 * dim);
+      cudaError_t e = dev_malloc(&d_bb, sizeof(double) * 2 * dim, op->stream);
       if (e != cudaSuccess) {
-        cudaFree(d_rows);
-        return bail(fail(SGMEV_ERR_OOM, "cudaMalloc bounding box"));
+        dev_free(d_rows, op->stream);
+        return bail(fail(SGMEV_ERR_OOM, "device allocation for the bounding box"));
       }
       cudaMemcpyAsync(d_bb, hb.data(), sizeof(double) * 2 * dim, cudaMemcpyHostToDevice, op->stream);
     }
@@ -1171,8 +1179,8 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
         op->xt32lo);
     op->launches += 1;
     cudaError_t e = cudaStreamSynchronize(op->stream);
-    cudaFree(d_rows);
-    if (d_bb) cudaFree(d_bb);
+    dev_free(d_rows, op->stream);
+    dev_free(d_bb, op->stream);
     if (e != cudaSuccess) return bail(fail(SGMEV_ERR_CUDA, std::string("stage data: ") + cudaGetErrorString(e)));
   }
   CREATE_TRY(stage_grid(op, n_grid, level_pow2, index));

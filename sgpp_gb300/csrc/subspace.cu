@@ -30,6 +30,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "devmem.h"
 #include "kernels.cuh"
 #include "subspace.h"
 #include "subspace_common.cuh"
@@ -665,7 +666,7 @@ cudaError_t launch_mat_build(const SubPlan& p, cudaStream_t s, const float* xh, 
   using Lay = OwnLayout<DIM, true>;
   const size_t sm = sizeof(float) * kOwnTile * Lay::W;
   auto kern = sub_mat_build_kernel<DIM>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  cudaError_t e = set_smem_cap(kern, sm);
   if (e != cudaSuccess) return e;
   const int64_t nt = mpad / kOwnTile;
   const int nth = static_cast<int>(std::min<int64_t>(kOwnMaxThreads, p.s_pad));
@@ -894,8 +895,7 @@ cudaError_t launch_mult(const SubPlan& p, cudaStream_t s, const float* xt, int64
                         int num_sms) {
   const size_t sm = sizeof(int4) * (kSDT * DIM + kSDT) +
                     sizeof(float2) * DIM * kActR * kActThreads + sizeof(float) * p.total;
-  cudaError_t e = cudaFuncSetAttribute(sub_mult_act_kernel<DIM>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  cudaError_t e = set_smem_cap(sub_mult_act_kernel<DIM>, sm);
   if (e != cudaSuccess) return e;
   const int64_t blocks = std::min<int64_t>(nt, static_cast<int64_t>(num_sms) * 8);
   sub_mult_act_kernel<DIM><<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kActThreads, sm, s>>>(
@@ -908,8 +908,7 @@ cudaError_t launch_mult_df(const SubPlan& p, cudaStream_t s, const float* xh, co
                            int64_t mpad, int64_t m, double* out64, int64_t t0, int64_t nt,
                            int num_sms) {
   const size_t sm = sizeof(int4) * kSDT * DIM + sizeof(uint32_t) * kSDT + sizeof(float2) * p.total;
-  cudaError_t e = cudaFuncSetAttribute(sub_mult_df_kernel<DIM>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  cudaError_t e = set_smem_cap(sub_mult_df_kernel<DIM>, sm);
   if (e != cudaSuccess) return e;
   const int64_t blocks = std::min<int64_t>(nt, static_cast<int64_t>(num_sms) * 8);
   sub_mult_df_kernel<DIM><<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kDfThreads, sm, s>>>(
@@ -921,8 +920,7 @@ template <int DIM>
 cudaError_t launch_multt(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
                          int64_t m, const float* v, int num_sms) {
   const size_t sm = multt_smem(DIM, p.total);
-  cudaError_t e = cudaFuncSetAttribute(sub_multt_kernel<DIM>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  cudaError_t e = set_smem_cap(sub_multt_kernel<DIM>, sm);
   if (e != cudaSuccess) return e;
   const int64_t nt = mpad / (kMulttThreads * kMulttR);
   const int64_t blocks = multt_blocks(mpad, num_sms);
@@ -950,8 +948,7 @@ cudaError_t launch_multt_own(const SubPlan& p, cudaStream_t s, const float* xh, 
   auto kern = sub_multt_own_kernel<DIM, DF>;
   const size_t sm = own_smem(p, DIM, DF);
   const int nth = own_threads(p, DF);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(sm));
+  cudaError_t e = set_smem_cap(kern, sm);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
@@ -981,8 +978,7 @@ cudaError_t launch_multt_act(const SubPlan& p, cudaStream_t s, const float* xt, 
   auto kern = sub_multt_act_kernel<DIM>;
   const size_t sm = act_own_smem(p, DIM);
   const int nth = own_threads(p, false);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(sm));
+  cudaError_t e = set_smem_cap(kern, sm);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
@@ -1002,8 +998,9 @@ cudaError_t launch_multt_act(const SubPlan& p, cudaStream_t s, const float* xt, 
 }  // namespace
 
 bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, const double* index,
-                    std::string* err) {
+                    cudaStream_t stream, std::string* err) {
   subspace_free(p);
+  p->stream = stream;
   if (dim < 1 || dim > 16 || n < 1) {
     *err = "subspace kernels need 1 <= dim <= 16 and a non-empty grid";
     return false;
@@ -1115,23 +1112,28 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
   const int nth = own_threads(*p, false);
   p->row_cap = std::min<int64_t>(static_cast<int64_t>(sms) * std::min(16, std::max(2, 1024 / nth)),
                                  std::max<int64_t>(1, (int64_t(256) << 20) / (8 * offset)));
-  bool ok = cudaMalloc(&p->desc, sizeof(int4) * desc.size()) == cudaSuccess &&
-            cudaMalloc(&p->sinfo, sizeof(int4) * sinfo.size()) == cudaSuccess &&
-            cudaMalloc(&p->act, sizeof(int4) * act.size()) == cudaSuccess &&
-            cudaMalloc(&p->sact, sizeof(int4) * sact.size()) == cudaSuccess &&
-            cudaMalloc(&p->rows, sizeof(double) * p->row_cap * offset) == cudaSuccess &&
-            cudaMalloc(&p->base, sizeof(uint32_t) * base.size()) == cudaSuccess &&
-            cudaMalloc(&p->pos, sizeof(int) * pos.size()) == cudaSuccess &&
-            cudaMalloc(&p->asub, sizeof(float) * offset) == cudaSuccess &&
-            cudaMalloc(&p->asub2, sizeof(float2) * offset) == cudaSuccess &&
-            cudaMalloc(&p->acc, sizeof(unsigned long long) * offset) == cudaSuccess &&
-            cudaMalloc(&p->maxbits, sizeof(unsigned int)) == cudaSuccess;
-  ok = ok && cudaMemcpy(p->desc, desc.data(), sizeof(int4) * desc.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-       cudaMemcpy(p->sinfo, sinfo.data(), sizeof(int4) * sinfo.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-       cudaMemcpy(p->act, act.data(), sizeof(int4) * act.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-       cudaMemcpy(p->sact, sact.data(), sizeof(int4) * sact.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-       cudaMemcpy(p->base, base.data(), sizeof(uint32_t) * base.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-       cudaMemcpy(p->pos, pos.data(), sizeof(int) * pos.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  auto alloc = [&](auto** q, size_t bytes) { return dev_malloc(q, bytes, stream) == cudaSuccess; };
+  auto put = [&](void* dst, const void* src, size_t bytes) {
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream) == cudaSuccess;
+  };
+  bool ok = alloc(&p->desc, sizeof(int4) * desc.size()) &&
+            alloc(&p->sinfo, sizeof(int4) * sinfo.size()) &&
+            alloc(&p->act, sizeof(int4) * act.size()) &&
+            alloc(&p->sact, sizeof(int4) * sact.size()) &&
+            alloc(&p->rows, sizeof(double) * p->row_cap * offset) &&
+            alloc(&p->base, sizeof(uint32_t) * base.size()) &&
+            alloc(&p->pos, sizeof(int) * pos.size()) &&
+            alloc(&p->asub, sizeof(float) * offset) &&
+            alloc(&p->asub2, sizeof(float2) * offset) &&
+            alloc(&p->acc, sizeof(unsigned long long) * offset) &&
+            alloc(&p->maxbits, sizeof(unsigned int));
+  // (pageable sources: each copy has taken the data when it returns)
+  ok = ok && put(p->desc, desc.data(), sizeof(int4) * desc.size()) &&
+       put(p->sinfo, sinfo.data(), sizeof(int4) * sinfo.size()) &&
+       put(p->act, act.data(), sizeof(int4) * act.size()) &&
+       put(p->sact, sact.data(), sizeof(int4) * sact.size()) &&
+       put(p->base, base.data(), sizeof(uint32_t) * base.size()) &&
+       put(p->pos, pos.data(), sizeof(int) * pos.size());
   if (!ok) {
     subspace_free(p);
     *err = "subspace plan allocation failed";
@@ -1141,21 +1143,11 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
 }
 
 void subspace_free(SubPlan* p) {
-  cudaFree(p->desc);
-  cudaFree(p->sinfo);
-  cudaFree(p->pmat);
-  cudaFree(p->pmat_lo);
-  cudaFree(p->pmat16);
-  cudaFree(p->cmat);
-  cudaFree(p->act);
-  cudaFree(p->sact);
-  cudaFree(p->rows);
-  cudaFree(p->base);
-  cudaFree(p->pos);
-  cudaFree(p->asub);
-  cudaFree(p->asub2);
-  cudaFree(p->acc);
-  cudaFree(p->maxbits);
+  const cudaStream_t st = p->stream;
+  void* ptrs[] = {p->desc, p->sinfo, p->act,  p->sact,    p->pmat,  p->pmat_lo, p->pmat16,
+                  p->cmat, p->rows,  p->base, p->pos,     p->asub,  p->asub2,   p->acc,
+                  p->maxbits};
+  for (void* q : ptrs) dev_free(q, st);
   *p = SubPlan{};
 }
 

@@ -9,6 +9,20 @@
 
 namespace sgmev {
 
+// Allow `kern` the device's largest dynamic shared memory, after checking that `need` fits. Every
+// caller sets the same value, so operators running in several host threads cannot undo one
+// another's setting between the call and their launch (the attribute belongs to the kernel, not
+// to the launch).
+template <typename Kernel>
+inline cudaError_t set_smem_cap(Kernel kern, size_t need) {
+  int dev = 0, cap = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  if (need > static_cast<size_t>(cap)) return cudaErrorInvalidValue;
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+}
+
 // A grid regrouped by subspace (level vector). Positions: each subspace owns the contiguous range
 // [offset, offset + prod_t 2^{l_t - 1}) in subspace order; a grid point's position is
 // offset + sum_t ((i_t - 1) / 2) * stride_t. Positions without a grid point (adaptive grids)
@@ -43,6 +57,7 @@ struct SubPlan {
   uint32_t* cmat = nullptr;
   int64_t s_pad = 0;
   int64_t mat_mpad = 0;
+  cudaStream_t stream = nullptr;  // device memory of the plan is allocated and freed on it
 };
 
 // largest position count the shared-memory kernels handle (two 4-byte accumulators per position in
@@ -52,7 +67,7 @@ constexpr int64_t kSubMaxPositions = 24 * 1024;
 // Build the plan from the eval arrays (host, [n x dim] 2^l and i). Returns false (and leaves
 // the plan empty) when the grid does not fit the shared-memory kernels or dim is not templated.
 bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2,
-                    const double* index, std::string* err);
+                    const double* index, cudaStream_t stream, std::string* err);
 void subspace_free(SubPlan* p);
 
 // out[j] (FP32 and/or FP64, zero beyond m) = sum_g alpha_g phi_g(x_j) for j in [j_begin, j_end)

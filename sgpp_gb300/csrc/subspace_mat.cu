@@ -26,6 +26,7 @@
 
 #include <algorithm>
 
+#include "devmem.h"
 #include "kernels.cuh"
 #include "subspace.h"
 #include "subspace_common.cuh"
@@ -604,24 +605,25 @@ int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad) {
 
 cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, const float* xl,
                                  int64_t mpad, int64_t m, int num_sms) {
-  cudaFree(p->pmat);
-  cudaFree(p->pmat_lo);
-  cudaFree(p->pmat16);
-  cudaFree(p->cmat);
+  dev_free(p->pmat, s);
+  dev_free(p->pmat_lo, s);
+  dev_free(p->pmat16, s);
+  dev_free(p->cmat, s);
   p->pmat = p->pmat_lo = nullptr;
   p->pmat16 = nullptr;
   p->cmat = nullptr;
   p->s_pad = (p->n_sub + 31) / 32 * 32;
   p->mat_mpad = mpad;
   const size_t entries = static_cast<size_t>(mpad / 4) * static_cast<size_t>(p->s_pad);
-  cudaError_t e = cudaMalloc(&p->pmat, entries * sizeof(float4));
-  if (e == cudaSuccess) e = cudaMalloc(&p->pmat_lo, entries * sizeof(float4));
-  if (e == cudaSuccess) e = cudaMalloc(&p->pmat16, entries * sizeof(uint2));
-  if (e == cudaSuccess) e = cudaMalloc(&p->cmat, entries * sizeof(uint32_t));
+  cudaError_t e = dev_malloc(&p->pmat, entries * sizeof(float4), s);
+  if (e == cudaSuccess) e = dev_malloc(&p->pmat_lo, entries * sizeof(float4), s);
+  if (e == cudaSuccess) e = dev_malloc(&p->pmat16, entries * sizeof(uint2), s);
+  if (e == cudaSuccess) e = dev_malloc(&p->cmat, entries * sizeof(uint32_t), s);
   if (e != cudaSuccess) {
-    cudaFree(p->pmat);
-    cudaFree(p->pmat_lo);
-    cudaFree(p->pmat16);
+    dev_free(p->pmat, s);
+    dev_free(p->pmat_lo, s);
+    dev_free(p->pmat16, s);
+    dev_free(p->cmat, s);
     p->pmat = p->pmat_lo = nullptr;
     p->pmat16 = nullptr;
     p->cmat = nullptr;
@@ -644,7 +646,7 @@ cudaError_t subspace_system_mat(const SubPlan& p, cudaStream_t s, int64_t mpad,
   cudaError_t e = subspace_scatter_alpha(p, s, alpha32);
   if (e != cudaSuccess) return e;
   const size_t sm = mat_system_smem(p.cmax, p.s_pad);
-  e = cudaFuncSetAttribute(mat_system_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  e = set_smem_cap(mat_system_kernel, sm);
   if (e != cudaSuccess) return e;
   const int64_t nt = mpad / kSysTile;
   const int64_t rows = std::min<int64_t>(num_sms, p.row_cap);
@@ -666,7 +668,7 @@ cudaError_t subspace_mult_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad,
   const int64_t nt = (j_end + kOwnTile - 1) / kOwnTile - t0;
   if (nt <= 0) return cudaSuccess;
   const size_t sm = mat_mult_df_smem(p.cmax, p.s_pad);
-  e = cudaFuncSetAttribute(mat_mult_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  e = set_smem_cap(mat_mult_df_kernel, sm);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mat_mult_df_kernel, kMatThreads, sm);
@@ -684,7 +686,7 @@ cudaError_t subspace_multt_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad
   if (!p.pmat || !p.pmat_lo || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
   const size_t sm = mat_multt_df_smem(p.cmax, p.s_pad);
   const int nth = mat_threads(p.s_pad);
-  cudaError_t e = cudaFuncSetAttribute(mat_multt_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  cudaError_t e = set_smem_cap(mat_multt_df_kernel, sm);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mat_multt_df_kernel, nth, sm);
@@ -706,7 +708,7 @@ cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, const typename Pro
                             int num_sms) {
   auto kern = mat_mult_kernel<HALF>;
   const size_t sm = mat_mult_smem(p.cmax, p.s_pad);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  cudaError_t e = set_smem_cap(kern, sm);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMatThreads, sm);
@@ -724,7 +726,7 @@ cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, const typename Pr
   auto kern = mat_multt_kernel<HALF>;
   const size_t sm = mat_multt_smem(p.cmax, p.s_pad);
   const int nth = mat_threads(p.s_pad);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  cudaError_t e = set_smem_cap(kern, sm);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);

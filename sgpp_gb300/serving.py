@@ -1,4 +1,6 @@
-"""Continuous-batching regression-fit server over the batch engine (sgmev_batch_*).
+"""Regression-fit servers: continuous batching over the batch engine (sgmev_batch_*), or a pool
+of worker threads that each fit one request at a time with its own operator (subspace and
+materialised products, own CUDA stream).
 
 Requests (grid, X, Y, lambda, epsilon) arrive over time. The loop admits waiting requests in
 arrival order while a slot and pool space are free (admission by device-memory footprint: the
@@ -7,7 +9,13 @@ blocks fit), advances every resident problem by a few steps, hands finished resu
 frees their slots. Grids, data and CG state stay on the device for a request's whole life; work of
 requests that arrive while others run overlaps with theirs in the same launches.
 
-    python -m sgpp_gb300.serving --rate 200 --duration 20 --max-work 2e10
+    python -m sgpp_gb300.serving --rate 200 --duration 20 --max-work 2e10 [--engine pool|batch]
+
+The pool server (default): a request is admitted when a worker is free (first come, first
+served); the worker creates the operator for the request's grid and data (algo and
+materialisation chosen by the library), runs the device-resident mixed-precision fit and frees
+the operator. Workers overlap on the GPU through their streams; the host waits of one fit (its
+CG scalars) are hidden by the other workers' launches. The library call releases the GIL.
 
 prints one JSON line: completed fits/s, offered load, p50/p99 latency, queue depth.
 Synthetic requests follow the batched-fit size mix (d uniform in 2..12, level in 3..7, data size
@@ -103,6 +111,79 @@ class FitServer:
         return done
 
 
+class PoolServer:
+    """Worker threads, each fitting one request at a time with its own operator."""
+
+    def __init__(self, workers: int = 8, params: Optional[dict] = None):
+        self.workers = workers
+        self.params = dict(params or {})
+        self.queue_depths: List[int] = []
+
+    def close(self) -> None:
+        pass
+
+    def _fit(self, r: Request, keep_alpha: bool) -> None:
+        cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                    sg.OperationMultipleEvalSubType.CUDA,
+                                                    parameters=self.params)
+        op = sg.createOperationMultipleEval(r.grid, r.X, cfg)
+        try:
+            alpha, r.iterations, r.residual = op.fit(np.ascontiguousarray(r.Y[:, 0]), r.lam,
+                                                     100000, r.epsilon,
+                                                     mode=sg.SGMEV_SOLVE_MIXED)
+        finally:
+            op.close()
+        r.alpha = alpha if keep_alpha else None
+
+    def run(self, requests: List[Request], clock: Callable[[], float] = time.perf_counter,
+            keep_alpha: bool = True, max_seconds: float = 1e9) -> List[Request]:
+        """Serve `requests` (sorted by arrival) in real time; returns the completed ones."""
+        import queue
+        import threading
+
+        pending = sorted(requests, key=lambda r: r.arrival)
+        work: "queue.Queue[Optional[Request]]" = queue.Queue()
+        done: List[Request] = []
+        lock = threading.Lock()
+        errors: List[BaseException] = []
+        t0 = clock()
+
+        def worker():
+            while True:
+                r = work.get()
+                if r is None:
+                    return
+                if clock() - t0 > max_seconds:
+                    continue  # past the deadline: drop the rest of the queue
+                r.admitted = clock() - t0
+                try:
+                    self._fit(r, keep_alpha)
+                except BaseException as e:  # reported after the run
+                    with lock:
+                        errors.append(e)
+                    continue
+                r.finished = clock() - t0
+                with lock:
+                    done.append(r)
+
+        threads = [threading.Thread(target=worker, daemon=True) for _ in range(self.workers)]
+        for t in threads:
+            t.start()
+        for r in pending:
+            wait = r.arrival - (clock() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            work.put(r)
+            self.queue_depths.append(work.qsize())
+        for _ in threads:
+            work.put(None)
+        for t in threads:
+            t.join()
+        if errors:
+            raise errors[0]
+        return done
+
+
 def percentile(values: List[float], q: float) -> float:
     if not values:
         return float("nan")
@@ -162,6 +243,8 @@ def main() -> int:
     ap.add_argument("--lam", type=float, default=1e-4)
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--drain-seconds", type=float, default=60.0)
+    ap.add_argument("--engine", choices=["pool", "batch"], default="pool")
+    ap.add_argument("--workers", type=int, default=8, help="pool server: concurrent fits")
     args = ap.parse_args()
 
     gen = MixGenerator(args.seed, args.max_work)
@@ -173,7 +256,11 @@ def main() -> int:
             break
         g, X, Y = gen.draw()
         reqs.append(Request(len(reqs), t, g, X, Y, args.lam, args.epsilon))
-    server = FitServer(max_slots=args.max_slots, grid_capacity=1 << 25, data_capacity=1 << 27)
+    if args.engine == "pool":
+        server = PoolServer(workers=args.workers)
+    else:
+        server = FitServer(max_slots=args.max_slots, grid_capacity=1 << 25,
+                           data_capacity=1 << 27)
     t0 = time.perf_counter()
     done = server.run(reqs, keep_alpha=False, max_seconds=args.duration + args.drain_seconds)
     wall = time.perf_counter() - t0
@@ -187,7 +274,9 @@ def main() -> int:
                         "mean": float(np.mean(server.queue_depths or [0]))},
         "config": {"mix": "d in 2..12, level 3..7, M log-uniform [1e3, 2^20], uniform data",
                    "max_work_NMd": args.max_work, "epsilon": args.epsilon, "lambda": args.lam,
-                   "slots": args.max_slots, "engine_steps": server.engine.info()["steps"]},
+                   "engine": args.engine,
+                   **({"workers": args.workers} if args.engine == "pool" else
+                      {"slots": args.max_slots, "engine_steps": server.engine.info()["steps"]})},
     }
     print(json.dumps(line))
     server.close()

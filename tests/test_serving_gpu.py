@@ -39,3 +39,29 @@ def test_server_results_equal_alone_results():
         assert phase == sg.BatchEngine.PHASE_DONE
         assert it == r.iterations
         assert np.array_equal(alone, r.alpha)
+
+
+def test_pool_server_results_equal_alone_fits():
+    """Worker-pool server: every request completes with the same alpha, bit for bit, as the same
+    fit run alone (the operator's results do not depend on what else runs on the GPU)."""
+    from sgpp_gb300.serving import PoolServer
+
+    gen = MixGenerator(seed=6, max_work=5e7, max_points=8192)
+    rng = np.random.default_rng(7)
+    reqs, t = [], 0.0
+    for rid in range(20):
+        t += rng.exponential(1.0 / 500.0)
+        g, X, Y = gen.draw()
+        reqs.append(Request(rid, t, g, X, Y, 1e-3, 1e-9))
+    server = PoolServer(workers=4)
+    done = server.run(reqs)
+    assert len(done) == len(reqs)
+    lat = [r.finished - r.arrival for r in done]
+    assert all(v > 0 for v in lat)
+    for r in done[:6]:
+        op = sg.createOperationMultipleEval(r.grid, r.X)
+        alone, it, _ = op.fit(np.ascontiguousarray(r.Y[:, 0]), r.lam, 100000, r.epsilon,
+                              mode=sg.SGMEV_SOLVE_MIXED)
+        op.close()
+        assert it == r.iterations
+        assert np.array_equal(alone, r.alpha)
