@@ -956,7 +956,7 @@ cudaError_t launch_multt_own(const SubPlan& p, cudaStream_t s, const float* xh, 
   const int64_t nt = mpad / kOwnTile;
   // a fixed grid for a given device and plan: the row count, and with it the summation order,
   // does not change between calls
-  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), p.row_cap);
+  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
   kern<<<static_cast<unsigned>(rows), nth, sm, s>>>(p.desc, p.sinfo, p.n_sub, p.cmax,
                                                     static_cast<int>(p.total), xh, xl, mpad, m, vh,
                                                     vl, nt, p.rows);
@@ -984,7 +984,7 @@ cudaError_t launch_multt_act(const SubPlan& p, cudaStream_t s, const float* xt, 
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
   if (e != cudaSuccess) return e;
   const int64_t nt = mpad / kOwnTile;
-  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), p.row_cap);
+  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
   kern<<<static_cast<unsigned>(rows), nth, sm, s>>>(p.act, p.sact, p.n_sub, p.cmax,
                                                     static_cast<int>(p.total), xt, mpad, m, v, nt,
                                                     p.rows);

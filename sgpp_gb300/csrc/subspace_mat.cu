@@ -649,7 +649,7 @@ cudaError_t subspace_system_mat(const SubPlan& p, cudaStream_t s, int64_t mpad,
   e = set_smem_cap(mat_system_kernel, sm);
   if (e != cudaSuccess) return e;
   const int64_t nt = mpad / kSysTile;
-  const int64_t rows = std::min<int64_t>(num_sms, p.row_cap);
+  const int64_t rows = std::min<int64_t>(num_sms, std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
   mat_system_kernel<<<static_cast<unsigned>(rows), kSysThreads, sm, s>>>(
       p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), p.asub, nt,
       p.pmat, p.cmat, p.rows);
@@ -692,7 +692,7 @@ cudaError_t subspace_multt_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mat_multt_df_kernel, nth, sm);
   if (e != cudaSuccess) return e;
   const int64_t nt = mpad / kOwnTile;
-  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), p.row_cap);
+  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
   mat_multt_df_kernel<<<static_cast<unsigned>(rows), nth, sm, s>>>(
       p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), vh, vl, nt,
       p.pmat, p.pmat_lo, p.cmat, p.rows);
@@ -732,7 +732,7 @@ cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, const typename Pr
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
   if (e != cudaSuccess) return e;
   const int64_t nt = mpad / kOwnTile;
-  *rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), p.row_cap);
+  *rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
   kern<<<static_cast<unsigned>(*rows), nth, sm, s>>>(p.sact, p.n_sub, static_cast<int>(p.s_pad),
                                                      p.cmax, static_cast<int>(p.total), v32, nt,
                                                      pm, p.cmat, p.rows);

@@ -118,6 +118,7 @@ class PoolServer:
         self.workers = workers
         self.params = dict(params or {})
         self.queue_depths: List[int] = []
+        self.phase_seconds = {"create": 0.0, "fit": 0.0, "close": 0.0}
 
     def close(self) -> None:
         pass
@@ -126,13 +127,20 @@ class PoolServer:
         cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
                                                     sg.OperationMultipleEvalSubType.CUDA,
                                                     parameters=self.params)
+        t0 = time.perf_counter()
         op = sg.createOperationMultipleEval(r.grid, r.X, cfg)
+        t1 = time.perf_counter()
         try:
             alpha, r.iterations, r.residual = op.fit(np.ascontiguousarray(r.Y[:, 0]), r.lam,
                                                      100000, r.epsilon,
                                                      mode=sg.SGMEV_SOLVE_MIXED)
         finally:
+            t2 = time.perf_counter()
             op.close()
+        t3 = time.perf_counter()
+        self.phase_seconds["create"] += t1 - t0  # (unsynchronised sums: a rough split)
+        self.phase_seconds["fit"] += t2 - t1
+        self.phase_seconds["close"] += t3 - t2
         r.alpha = alpha if keep_alpha else None
 
     def run(self, requests: List[Request], clock: Callable[[], float] = time.perf_counter,
@@ -196,7 +204,9 @@ class MixGenerator:
     data of a request is drawn from a pool of pre-generated matrices (per dimension)."""
 
     def __init__(self, seed: int = 0, max_work: float = float("inf"), pool: int = 8,
-                 max_points: int = 1 << 20):
+                 max_points: int = 1 << 20, pinned: bool = False):
+        self.pinned = pinned
+        self._keep = []  # pinned tensors backing the pooled matrices
         self.rng = np.random.default_rng(seed)
         self.max_work = max_work
         self.max_points = max_points
@@ -215,7 +225,14 @@ class MixGenerator:
     def _x(self, d: int, m: int) -> np.ndarray:
         lst = self.data.setdefault(d, [])
         if len(lst) < self.pool:
-            lst.append(self.rng.random((self.max_points, d)))
+            a = self.rng.random((self.max_points, d))
+            if self.pinned:  # request data in page-locked host memory, as a server's receive
+                import torch  # buffers would be; host-to-device copies then run at full speed
+
+                t = torch.from_numpy(a).pin_memory()
+                self._keep.append(t)
+                a = t.numpy()
+            lst.append(a)
         base = lst[int(self.rng.integers(0, len(lst)))]
         off = int(self.rng.integers(0, self.max_points - m + 1))
         return base[off:off + m]
@@ -245,9 +262,11 @@ def main() -> int:
     ap.add_argument("--drain-seconds", type=float, default=60.0)
     ap.add_argument("--engine", choices=["pool", "batch"], default="pool")
     ap.add_argument("--workers", type=int, default=8, help="pool server: concurrent fits")
+    ap.add_argument("--pinned", action="store_true",
+                    help="request data in page-locked host memory (receive buffers)")
     args = ap.parse_args()
 
-    gen = MixGenerator(args.seed, args.max_work)
+    gen = MixGenerator(args.seed, args.max_work, pinned=args.pinned)
     rng = np.random.default_rng(args.seed + 1)
     t, reqs = 0.0, []
     while True:
@@ -274,10 +293,12 @@ def main() -> int:
                         "mean": float(np.mean(server.queue_depths or [0]))},
         "config": {"mix": "d in 2..12, level 3..7, M log-uniform [1e3, 2^20], uniform data",
                    "max_work_NMd": args.max_work, "epsilon": args.epsilon, "lambda": args.lam,
-                   "engine": args.engine,
+                   "engine": args.engine, "pinned_request_data": args.pinned,
                    **({"workers": args.workers} if args.engine == "pool" else
                       {"slots": args.max_slots, "engine_steps": server.engine.info()["steps"]})},
     }
+    if args.engine == "pool":
+        line["worker_seconds"] = server.phase_seconds
     print(json.dumps(line))
     server.close()
     return 0
