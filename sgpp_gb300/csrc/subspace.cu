@@ -150,7 +150,9 @@ __device__ __forceinline__ void act_eval(const int4* __restrict__ d, const float
   }
 }
 
-template <int DIM>
+// GA: alpha is read from global memory (through L1/L2) instead of being staged in shared memory,
+// for grids with more positions than shared memory holds
+template <int DIM, bool GA>
 __global__ void __launch_bounds__(kActThreads, 2) sub_mult_act_kernel(
     const int4* __restrict__ act, const int4* __restrict__ sact, int n_sub,
     const float* __restrict__ asub, int total, const float* __restrict__ xt, int64_t mpad,
@@ -160,10 +162,12 @@ __global__ void __launch_bounds__(kActThreads, 2) sub_mult_act_kernel(
   int4* s_act = reinterpret_cast<int4*>(smem);             // [kSDT * DIM] (t, S, L, stride)
   int4* s_info = s_act + kSDT * DIM;                        // [kSDT] (base, cells, -, n_active)
   float2* s_xr = reinterpret_cast<float2*>(s_info + kSDT);  // [DIM][kActR][kActThreads]
-  float* s_a = reinterpret_cast<float*>(s_xr + DIM * kActR * kActThreads);  // [total]
+  float* s_stage = reinterpret_cast<float*>(s_xr + DIM * kActR * kActThreads);  // [total]
   const int tid = threadIdx.x;
   const float2* xr = s_xr + tid;
-  for (int k = tid; k < total; k += kActThreads) s_a[k] = asub[k];
+  if (!GA)
+    for (int k = tid; k < total; k += kActThreads) s_stage[k] = asub[k];
+  const float* s_a = GA ? asub : s_stage;
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t j0 = (tile_begin + tile) * (kActR * kActThreads) + tid;
     float h1p[kActR];
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(kActThreads, 2) sub_mult_act_kernel(
 // alpha is a float-float pair per position in shared memory.
 constexpr int kDfThreads = 512, kDfR = 1;
 
-template <int DIM>
+template <int DIM, bool GA>
 __global__ void __launch_bounds__(kDfThreads, 1) sub_mult_df_kernel(
     const int4* __restrict__ desc, const uint32_t* __restrict__ base, int n_sub,
     const float2* __restrict__ asub2, int total, const float* __restrict__ xh_t,
@@ -257,8 +261,10 @@ __global__ void __launch_bounds__(kDfThreads, 1) sub_mult_df_kernel(
   extern __shared__ __align__(16) unsigned char smem[];
   int4* s_desc = reinterpret_cast<int4*>(smem);
   uint32_t* s_base = reinterpret_cast<uint32_t*>(s_desc + kSDT * DIM);
-  float2* s_a = reinterpret_cast<float2*>(s_base + kSDT);
-  for (int k = threadIdx.x; k < total; k += kDfThreads) s_a[k] = asub2[k];
+  float2* s_stage = reinterpret_cast<float2*>(s_base + kSDT);
+  if (!GA)
+    for (int k = threadIdx.x; k < total; k += kDfThreads) s_stage[k] = asub2[k];
+  const float2* s_a = GA ? asub2 : s_stage;
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t j0 = (tile_begin + tile) * (kDfThreads * kDfR) + threadIdx.x;
     float xh[kDfR][DIM], xl[kDfR][DIM];
@@ -893,12 +899,14 @@ template <int DIM>
 cudaError_t launch_mult(const SubPlan& p, cudaStream_t s, const float* xt, int64_t mpad,
                         int64_t m, float* out32, double* out64, int64_t t0, int64_t nt,
                         int num_sms) {
+  const bool ga = p.total > kSubMaxPositions;
   const size_t sm = sizeof(int4) * (kSDT * DIM + kSDT) +
-                    sizeof(float2) * DIM * kActR * kActThreads + sizeof(float) * p.total;
-  cudaError_t e = set_smem_cap(sub_mult_act_kernel<DIM>, sm);
+                    sizeof(float2) * DIM * kActR * kActThreads + (ga ? 0 : sizeof(float) * p.total);
+  auto kern = ga ? sub_mult_act_kernel<DIM, true> : sub_mult_act_kernel<DIM, false>;
+  cudaError_t e = set_smem_cap(kern, sm);
   if (e != cudaSuccess) return e;
   const int64_t blocks = std::min<int64_t>(nt, static_cast<int64_t>(num_sms) * 8);
-  sub_mult_act_kernel<DIM><<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kActThreads, sm, s>>>(
+  kern<<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kActThreads, sm, s>>>(
       p.act, p.sact, p.n_sub, p.asub, static_cast<int>(p.total), xt, mpad, m, t0, nt, out32, out64);
   return cudaGetLastError();
 }
@@ -907,11 +915,13 @@ template <int DIM>
 cudaError_t launch_mult_df(const SubPlan& p, cudaStream_t s, const float* xh, const float* xl,
                            int64_t mpad, int64_t m, double* out64, int64_t t0, int64_t nt,
                            int num_sms) {
-  const size_t sm = sizeof(int4) * kSDT * DIM + sizeof(uint32_t) * kSDT + sizeof(float2) * p.total;
-  cudaError_t e = set_smem_cap(sub_mult_df_kernel<DIM>, sm);
+  const bool ga = p.total > kSubMaxPositions;
+  const size_t sm = sizeof(int4) * kSDT * DIM + sizeof(uint32_t) * kSDT + (ga ? 0 : sizeof(float2) * p.total);
+  auto kern = ga ? sub_mult_df_kernel<DIM, true> : sub_mult_df_kernel<DIM, false>;
+  cudaError_t e = set_smem_cap(kern, sm);
   if (e != cudaSuccess) return e;
   const int64_t blocks = std::min<int64_t>(nt, static_cast<int64_t>(num_sms) * 8);
-  sub_mult_df_kernel<DIM><<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kDfThreads, sm, s>>>(
+  kern<<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kDfThreads, sm, s>>>(
       p.desc, p.base, p.n_sub, p.asub2, static_cast<int>(p.total), xh, xl, mpad, m, t0, nt, out64);
   return cudaGetLastError();
 }
@@ -1046,8 +1056,8 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
       stride[t] = size;
       size *= int64_t(1) << (l[t] - 1);
     }
-    if (offset + size > kSubMaxPositions) {
-      *err = "grid has more subspace positions than the shared-memory kernels hold";
+    if (offset + size > kSubMaxTotal) {
+      *err = "grid has more subspace positions than the subspace kernels index";
       return false;
     }
     uint32_t b = static_cast<uint32_t>(offset);
@@ -1137,6 +1147,12 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
   if (!ok) {
     subspace_free(p);
     *err = "subspace plan allocation failed";
+    return false;
+  }
+  if (p->total > kSubMaxPositions && !subspace_owner_fits(*p, false)) {
+    subspace_free(p);
+    *err = "grid has too many positions for the fixed-point scatter and a subspace too wide for "
+           "the owner-computes multTranspose";
     return false;
   }
   return true;
@@ -1268,6 +1284,7 @@ cudaError_t subspace_multt(const SubPlan& p, cudaStream_t s, const float* xt, in
     if (e != cudaSuccess) return e;
     return own_finish(p, s, npad, out64, add, scale_add);
   }
+  if (p.total > kSubMaxPositions) return cudaErrorInvalidValue;  // (rejected at build)
   e = cudaMemsetAsync(p.maxbits, 0, sizeof(unsigned int), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(p.acc, 0, sizeof(unsigned long long) * p.total, s);
   if (e != cudaSuccess) return e;

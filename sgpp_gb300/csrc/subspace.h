@@ -60,12 +60,15 @@ struct SubPlan {
   cudaStream_t stream = nullptr;  // device memory of the plan is allocated and freed on it
 };
 
-// largest position count the shared-memory kernels handle (two 4-byte accumulators per position in
-// 192 KB)
+// position count up to which alpha is staged in shared memory (and the fixed-point scatter, two
+// 4-byte accumulators per position, can run); larger grids read alpha from global memory
 constexpr int64_t kSubMaxPositions = 24 * 1024;
+// largest position count of a plan (32-bit indices, per-CTA rows of FP64 sums)
+constexpr int64_t kSubMaxTotal = int64_t(1) << 27;
 
 // Build the plan from the eval arrays (host, [n x dim] 2^l and i). Returns false (and leaves
-// the plan empty) when the grid does not fit the shared-memory kernels or dim is not templated.
+// the plan empty) when the grid has more than kSubMaxTotal positions, a subspace that the
+// owner-computes multTranspose cannot hold (beyond kSubMaxPositions), or dim is not templated.
 bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2,
                     const double* index, cudaStream_t stream, std::string* err);
 void subspace_free(SubPlan* p);

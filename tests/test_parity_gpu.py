@@ -368,6 +368,30 @@ def test_subspace_shapes_match_oracle(oracle, dim, level, precision, tol, algo):
     assert rel_err(outt, st.mult_transpose(lp, ix, v)) < tol
 
 
+@pytest.mark.parametrize("dim,level", [(6, 7), (4, 9)])
+@pytest.mark.parametrize("precision,tol", [("float", FP32_TOL), ("df64", FP64_TOL)])
+def test_large_grids_read_alpha_from_global_memory(oracle, dim, level, precision, tol):
+    """Grids with more positions than shared memory holds (40,193 and 65,537 grid points): the
+    subspace kernels read alpha from global memory; results match the oracle's FP64 evaluation."""
+    rng = np.random.default_rng(dim * 1000 + level)
+    grid = sg.Grid.createLinearGrid(dim)
+    grid.getGenerator().regular(level)
+    m = 4000
+    x = rng.random((m, dim))
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    a = rng.standard_normal(grid.getSize())
+    v = rng.standard_normal(m)
+    if precision == "float":
+        tol = max(tol, 2.0 ** (level - 23))
+    st = oracle.stream(x)
+    op = _op(grid, x, precision, "subspace")
+    out, outt = np.zeros(m), np.zeros(grid.getSize())
+    op.mult(a, out)
+    op.multTranspose(v, outt)
+    assert rel_err(out, st.mult(lp, ix, a)) < tol
+    assert rel_err(outt, st.mult_transpose(lp, ix, v)) < tol
+
+
 @pytest.mark.parametrize("products", ["half", "float"])
 def test_mixed_fit_inner_products(products):
     """params "inner_products": the inner solves stream the FP16 or the FP32 copy of the
