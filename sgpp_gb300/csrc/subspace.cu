@@ -430,6 +430,7 @@ __global__ void __launch_bounds__(kMulttThreads) sub_multt_kernel(
 // clamp. FP32: the per-dimension product is the one of the mult kernel. DF: as sub_mult_df_kernel,
 // with float-float per-tile sums.
 constexpr int kOwnMaxThreads = 512;
+constexpr size_t kOwnSmemBudget = 200 * 1024;  // shared memory of an owner-computes CTA
 constexpr int kActOwnThreads = 512;  // FP32 owner kernel (128-thread CTAs measured slower)
 constexpr int kActFlushTiles = 4;    // FP32 owner kernel: tiles summed in FP32 per flush
 
@@ -940,9 +941,17 @@ cudaError_t launch_multt(const SubPlan& p, cudaStream_t s, const float* xt, int6
   return cudaGetLastError();
 }
 
+// threads (subspaces) per CTA of the owner-computes multTranspose: one per subspace up to the
+// kernel's width, fewer when the per-thread cell sums (cmax of them) would overflow the shared
+// memory budget next to the staged rows
 int own_threads(const SubPlan& p, bool df) {
-  return static_cast<int>(std::min<int64_t>(df ? kOwnMaxThreads : kActOwnThreads,
-                                            (p.n_sub + 31) / 32 * 32));
+  const int64_t w = df ? (2 * p.dim + 2 + 3) / 4 * 4 : (2 + 2 * p.dim + 3) / 4 * 4;
+  const int64_t rows = static_cast<int64_t>(sizeof(float)) * kOwnTile * w;
+  const int64_t per = (df ? 8 : 4) * std::max(p.cmax, 1);
+  const int64_t fit = (static_cast<int64_t>(kOwnSmemBudget) - rows) / per / 32 * 32;
+  int64_t t = std::min<int64_t>(df ? kOwnMaxThreads : kActOwnThreads, (p.n_sub + 31) / 32 * 32);
+  t = std::min<int64_t>(t, std::max<int64_t>(fit, 32));
+  return static_cast<int>(t);
 }
 
 size_t own_smem(const SubPlan& p, int dim, bool df) {
@@ -1251,7 +1260,6 @@ cudaError_t subspace_mult_df(const SubPlan& p, cudaStream_t s, const float* xh, 
 }
 
 namespace {
-constexpr size_t kOwnSmemBudget = 200 * 1024;
 
 cudaError_t own_finish(const SubPlan& p, cudaStream_t s, int64_t npad, double* out64,
                        const double* add, double scale_add) {
