@@ -129,14 +129,14 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
           const float4 p = Prod<HALF>::get(ring[u]);
           const uint32_t cs = cring[u];
           if (g + kAhead < kGroups) {
-            ring[u] = __ldcs(src + static_cast<int64_t>(g + kAhead) * s_pad);
-            cring[u] = __ldcs(csrc + static_cast<int64_t>(g + kAhead) * s_pad);
+            ring[u] = __ldcs(src + (g + kAhead) * s_pad);
+            cring[u] = __ldcs(csrc + (g + kAhead) * s_pad);
           }
-          // (the clamps only guard shared memory against a corrupted cell table)
-          const float v0 = a_col[min(cs & 0xFFu, cm1) * s_pad] * p.x;
-          const float v1 = a_col[min((cs >> 8) & 0xFFu, cm1) * s_pad] * p.y;
-          const float v2 = a_col[min((cs >> 16) & 0xFFu, cm1) * s_pad] * p.z;
-          const float v3 = a_col[min(cs >> 24, cm1) * s_pad] * p.w;
+          // cells are below cmax by construction (the build writes c < cells of s <= cmax)
+          const float v0 = a_col[(cs & 0xFFu) * s_pad] * p.x;
+          const float v1 = a_col[((cs >> 8) & 0xFFu) * s_pad] * p.y;
+          const float v2 = a_col[((cs >> 16) & 0xFFu) * s_pad] * p.z;
+          const float v3 = a_col[(cs >> 24) * s_pad] * p.w;
           const float r = reduce4(v0, v1, v2, v3, lane);
           if ((lane & 7) == 0) {
             float* dst = part + 4 * g + (lane >> 3);
@@ -201,14 +201,15 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
           const float4 p = Prod<HALF>::get(ring[u]);
           const uint32_t cs = cring[u];
           if (g + kAhead < kGroups) {
-            ring[u] = __ldcs(src + static_cast<int64_t>(g + kAhead) * s_pad);
-            cring[u] = __ldcs(csrc + static_cast<int64_t>(g + kAhead) * s_pad);
+            ring[u] = __ldcs(src + (g + kAhead) * s_pad);
+            cring[u] = __ldcs(csrc + (g + kAhead) * s_pad);
           }
           const float4 vv = vt[g];  // the same four values for every lane
-          acc[min(cs & 0xFFu, cm1) * nth] += vv.x * p.x;
-          acc[min((cs >> 8) & 0xFFu, cm1) * nth] += vv.y * p.y;
-          acc[min((cs >> 16) & 0xFFu, cm1) * nth] += vv.z * p.z;
-          acc[min(cs >> 24, cm1) * nth] += vv.w * p.w;
+          // cells are below cmax by construction
+          acc[(cs & 0xFFu) * nth] += vv.x * p.x;
+          acc[((cs >> 8) & 0xFFu) * nth] += vv.y * p.y;
+          acc[((cs >> 16) & 0xFFu) * nth] += vv.z * p.z;
+          acc[(cs >> 24) * nth] += vv.w * p.w;
         }
       }
       ++since;
