@@ -43,6 +43,11 @@ constexpr int kMatMaxCells = 256;             // cell indices are stored in one 
 // point groups in flight per thread: a ring of loads issued this many groups ahead of their use
 // (fewer for the float-float kernels, whose arithmetic holds more registers)
 constexpr int kAhead = 4, kAheadDf = 2;
+// FP16 products take 8 bytes per group instead of 16: a deeper ring keeps as many bytes in flight
+template <bool HALF>
+struct Ahead {
+  static constexpr int value = HALF ? 8 : kAhead;
+};
 static_assert(kGroups % kAhead == 0 && kGroups % kAheadDf == 0, "the ring must divide a tile");
 // multT: FP32 sums over this many tiles (1024 points) before they go into the FP64 row
 constexpr int kFlushTiles = 4;
@@ -115,22 +120,22 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
       const float* a_col = s_at + sid;
       float* part = s_part + warp * kOwnTile;
       const bool first = s0 == 0;
-      PT ring[kAhead];
-      uint32_t cring[kAhead];
+      PT ring[Ahead<HALF>::value];
+      uint32_t cring[Ahead<HALF>::value];
 #pragma unroll
-      for (int u = 0; u < kAhead; ++u) {
+      for (int u = 0; u < Ahead<HALF>::value; ++u) {
         ring[u] = __ldcs(src + static_cast<int64_t>(u) * s_pad);
         cring[u] = __ldcs(csrc + static_cast<int64_t>(u) * s_pad);
       }
-      for (int g0 = 0; g0 < kGroups; g0 += kAhead) {
+      for (int g0 = 0; g0 < kGroups; g0 += Ahead<HALF>::value) {
 #pragma unroll
-        for (int u = 0; u < kAhead; ++u) {
+        for (int u = 0; u < Ahead<HALF>::value; ++u) {
           const int g = g0 + u;
           const float4 p = Prod<HALF>::get(ring[u]);
           const uint32_t cs = cring[u];
-          if (g + kAhead < kGroups) {
-            ring[u] = __ldcs(src + (g + kAhead) * s_pad);
-            cring[u] = __ldcs(csrc + (g + kAhead) * s_pad);
+          if (g + Ahead<HALF>::value < kGroups) {
+            ring[u] = __ldcs(src + (g + Ahead<HALF>::value) * s_pad);
+            cring[u] = __ldcs(csrc + (g + Ahead<HALF>::value) * s_pad);
           }
           // cells are below cmax by construction (the build writes c < cells of s <= cmax)
           const float v0 = a_col[(cs & 0xFFu) * s_pad] * p.x;
@@ -187,22 +192,22 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
       const PT* src = pm + at;
       const uint32_t* csrc = cm + at;
       const float4* vt = v4 + tile * kGroups;
-      PT ring[kAhead];
-      uint32_t cring[kAhead];
+      PT ring[Ahead<HALF>::value];
+      uint32_t cring[Ahead<HALF>::value];
 #pragma unroll
-      for (int u = 0; u < kAhead; ++u) {
+      for (int u = 0; u < Ahead<HALF>::value; ++u) {
         ring[u] = __ldcs(src + static_cast<int64_t>(u) * s_pad);
         cring[u] = __ldcs(csrc + static_cast<int64_t>(u) * s_pad);
       }
-      for (int g0 = 0; g0 < kGroups; g0 += kAhead) {
+      for (int g0 = 0; g0 < kGroups; g0 += Ahead<HALF>::value) {
 #pragma unroll
-        for (int u = 0; u < kAhead; ++u) {
+        for (int u = 0; u < Ahead<HALF>::value; ++u) {
           const int g = g0 + u;
           const float4 p = Prod<HALF>::get(ring[u]);
           const uint32_t cs = cring[u];
-          if (g + kAhead < kGroups) {
-            ring[u] = __ldcs(src + (g + kAhead) * s_pad);
-            cring[u] = __ldcs(csrc + (g + kAhead) * s_pad);
+          if (g + Ahead<HALF>::value < kGroups) {
+            ring[u] = __ldcs(src + (g + Ahead<HALF>::value) * s_pad);
+            cring[u] = __ldcs(csrc + (g + Ahead<HALF>::value) * s_pad);
           }
           const float4 vv = vt[g];  // the same four values for every lane
           // cells are below cmax by construction
