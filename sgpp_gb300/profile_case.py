@@ -40,8 +40,12 @@ KINDS = {("mult", "float", "dense"): sg.SGMEV_KERNEL_MULT_FP32,
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["mult", "multT", "system"], default="mult",
-                    help="system: B^T (B a) + lambda M a (systemApply)")
+    ap.add_argument("--kernel", choices=["mult", "multT", "system", "fit"], default="mult",
+                    help="system: B^T (B a) + lambda M a (systemApply); fit: one mixed-precision "
+                         "fit (its inner solves stream the FP16 products); reports the kernel "
+                         "given by --report")
+    ap.add_argument("--report", choices=["mult16", "multT16"], default="mult16",
+                    help="with --kernel fit: which kernel's launches to report")
     ap.add_argument("--precision", choices=["float", "double", "df64"], default="float")
     ap.add_argument("--algo", choices=["dense", "subspace", "materialized"], default="dense",
                     help="materialized: subspace products kept in device memory (FP32)")
@@ -72,7 +76,9 @@ def main() -> int:
     out_t = np.zeros(n)
 
     def run():
-        if args.kernel == "system":
+        if args.kernel == "fit":
+            op.fit(v, 1e-4, 100000, 1e-8, mode=sg.SGMEV_SOLVE_MIXED)
+        elif args.kernel == "system":
             op.systemApply(a, out_t, 1e-4 * args.points)
         elif args.kernel == "mult":
             op.mult(a, out_m)
@@ -85,7 +91,11 @@ def main() -> int:
     for _ in range(args.launches):
         run()
     algo = "dense" if args.precision == "double" else args.algo
-    cnt, sec = op.profileRead(KINDS[(args.kernel, args.precision, algo)])
+    if args.kernel == "fit":
+        kind = sg.SGMEV_KERNEL_MULT_MAT16 if args.report == "mult16" else sg.SGMEV_KERNEL_MULTT_MAT16
+    else:
+        kind = KINDS[(args.kernel, args.precision, algo)]
+    cnt, sec = op.profileRead(kind)
     op.profile(False)
     flop = 6.0 * n * args.points * args.dim
     avg = sec / max(cnt, 1)
