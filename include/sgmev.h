@@ -7,6 +7,11 @@
  *   mult           result_j = sum_i alpha_i  prod_t max(1 - |2^{l_it} x_jt - i_it|, 0)
  *   multTranspose  result_i = sum_j source_j prod_t max(1 - |2^{l_it} x_jt - i_it|, 0)
  *
+ * and the same products for the modified linear basis of ModLinear grids (params "basis"):
+ * a level-1 factor is 1, i = 1 gives max(2 - 2^l x, 0), i = 2^l - 1 gives max(2^l x - i + 1, 0)
+ * (base/.../basis/LinearModifiedBasis.hpp:40-58, streamed as
+ * datadriven/.../OperationMultiEvalModMaskStreaming).
+ *
  * All entry points take plain host pointers (or, for the *_device variants, device pointers)
  * and sizes; none uses C++ or torch types. Every function returns SGMEV_OK (0) or a negative
  * status; sgmev_last_error() then returns a message for the calling thread. No entry point
@@ -68,9 +73,10 @@ SGMEV_API int sgmev_device_count(void);
 /*
  * Create an operator for one grid and one data set; replaces
  *   sgpp::op_factory::createOperationMultipleEval(Grid&, DataMatrix&, OperationMultipleEvalConfiguration&)
- *   datadriven/src/sgpp/datadriven/DatadrivenOpFactory.cpp:409-552 (new branch: Linear grid,
- *   STREAMING type, CUDA subtype) and the operator constructor
- *   datadriven/.../OperationMultiEvalStreaming/OperationMultiEvalStreaming.cpp:13-25.
+ *   datadriven/src/sgpp/datadriven/DatadrivenOpFactory.cpp:409-552 (new branches: Linear and
+ *   ModLinear grids, STREAMING type, CUDA subtype) and the operator constructors
+ *   datadriven/.../OperationMultiEvalStreaming/OperationMultiEvalStreaming.cpp:13-25 and
+ *   datadriven/.../OperationMultiEvalModMaskStreaming/OperationMultiEvalModMaskStreaming.cpp:19-29.
  * The data are copied to the device once (dim-major, padded), as the reference operator copies
  * and transposes its dataset; the caller's buffers may be freed afterwards.
  * bb_left/bb_right: optional bounding box ([dim] each, both NULL for the unit cube); data are
@@ -96,6 +102,12 @@ SGMEV_API int sgmev_device_count(void);
  * "half" (default) or "float" — the inner FP32 solves of mixed fits stream an FP16 copy of the
  * products (3 bytes per entry instead of 5; the FP64-accurate outer residual keeps the result
  * exact to the fit's tolerance).
+ * "basis": "linear" (default) or "modlinear" — the basis of the grid. level_pow2/index stay the
+ * (2^l, i) arrays of getLevelIndexArraysForEval for both (a ModLinear grid has the same points).
+ * ModLinear functions next to a face extrapolate linearly beyond it, as the reference's mask
+ * evaluation does; the materialised products are used for ModLinear only when every data
+ * coordinate lies in [0, 1] (otherwise the dense kernels run), and the FP16 inner products only
+ * for subspaces of at most 15 active dimensions (products reach 2^15).
  */
 SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double* level_pow2,
                            const double* index, int64_t n_data, const double* data,

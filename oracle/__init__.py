@@ -72,6 +72,22 @@ class Oracle:
                                  _vp, ctypes.POINTER(_c_i64), ctypes.POINTER(_c_dbl)]
         L.orc_max_threads.restype = _c_int
         L.orc_set_threads.argtypes = [_c_int]
+        L.orc_modlinear_eval.restype = _c_dbl
+        L.orc_modlinear_eval.argtypes = [_c_int, _c_int, _c_dbl]
+        for name in ("orc_mult_naive_mod", "orc_mult_transpose_naive_mod"):
+            f = getattr(L, name)
+            f.restype = None
+            f.argtypes = [_c_int, _c_i64, _vp, _vp, _c_i64, _vp, _vp, _vp]
+        L.orc_mod_mask_arrays.restype = None
+        L.orc_mod_mask_arrays.argtypes = [_c_int, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp]
+        for name in ("orc_stream_mult_mod", "orc_stream_mult_transpose_mod"):
+            f = getattr(L, name)
+            f.restype = None
+            f.argtypes = [_vp, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp]
+        L.orc_cg_fit_mod.restype = _c_int
+        L.orc_cg_fit_mod.argtypes = [_vp, _c_i64, _vp, _vp, _vp, _vp, _vp, _c_dbl, _c_i64,
+                                     _c_dbl, _c_int, _vp, ctypes.POINTER(_c_i64),
+                                     ctypes.POINTER(_c_dbl)]
 
     # ---- grids -------------------------------------------------------------------------
     def regular_grid(self, dim: int, level: int):
@@ -101,6 +117,37 @@ class Oracle:
         """(2^l, i) as doubles, the reference's getLevelIndexArraysForEval layout."""
         return (np.left_shift(1, lev.astype(np.int64)).astype(np.float64),
                 idx.astype(np.float64))
+
+    def mod_arrays(self, lev, idx):
+        """ModLinear streaming layout (level, index, mask, offset), each [N x d] doubles; mask
+        holds raw 64-bit sign masks (getLevelIndexMaskArraysForModEval)."""
+        lev = np.ascontiguousarray(lev, np.int32)
+        idx = np.ascontiguousarray(idx, np.int32)
+        n, dim = lev.shape
+        out = [np.zeros((n, dim), np.float64) for _ in range(4)]
+        self.lib.orc_mod_mask_arrays(dim, n, _ptr(lev), _ptr(idx), *(_ptr(a) for a in out))
+        return tuple(out)
+
+    def modlinear_eval(self, l: int, i: int, x: float) -> float:
+        return float(self.lib.orc_modlinear_eval(int(l), int(i), float(x)))
+
+    def mult_naive_mod(self, lev, idx, data, alpha):
+        lev, idx = (np.ascontiguousarray(a, np.int32) for a in (lev, idx))
+        data, alpha = (np.ascontiguousarray(a, np.float64) for a in (data, alpha))
+        n, dim = lev.shape
+        out = np.zeros(data.shape[0], np.float64)
+        self.lib.orc_mult_naive_mod(dim, n, _ptr(lev), _ptr(idx), data.shape[0], _ptr(data),
+                                    _ptr(alpha), _ptr(out))
+        return out
+
+    def mult_transpose_naive_mod(self, lev, idx, data, source):
+        lev, idx = (np.ascontiguousarray(a, np.int32) for a in (lev, idx))
+        data, source = (np.ascontiguousarray(a, np.float64) for a in (data, source))
+        n, dim = lev.shape
+        out = np.zeros(n, np.float64)
+        self.lib.orc_mult_transpose_naive_mod(dim, n, _ptr(lev), _ptr(idx), data.shape[0],
+                                              _ptr(data), _ptr(source), _ptr(out))
+        return out
 
     def bb_to_unit(self, data, left, right):
         data = np.ascontiguousarray(data, np.float64)
@@ -186,6 +233,36 @@ class OracleStream:
                                 ctypes.byref(it), ctypes.byref(res))
         return alpha, int(it.value), float(res.value)
 
+    # ---- ModLinear (arrays from Oracle.mod_arrays) ---------------------------------------
+    def mult_mod(self, arrays, alpha):
+        arrays = [np.ascontiguousarray(a, np.float64) for a in arrays]
+        alpha = np.ascontiguousarray(alpha, np.float64)
+        out = np.zeros(self.m, np.float64)
+        self.orc.lib.orc_stream_mult_mod(self.h, arrays[0].shape[0], *(_ptr(a) for a in arrays),
+                                         _ptr(alpha), _ptr(out))
+        return out
+
+    def mult_transpose_mod(self, arrays, source):
+        arrays = [np.ascontiguousarray(a, np.float64) for a in arrays]
+        source = np.ascontiguousarray(source, np.float64)
+        out = np.zeros(arrays[0].shape[0], np.float64)
+        self.orc.lib.orc_stream_mult_transpose_mod(self.h, arrays[0].shape[0],
+                                                   *(_ptr(a) for a in arrays), _ptr(source),
+                                                   _ptr(out))
+        return out
+
+    def cg_fit_mod(self, arrays, y, lam, imax, eps, alpha0=None):
+        arrays = [np.ascontiguousarray(a, np.float64) for a in arrays]
+        y = np.ascontiguousarray(y, np.float64)
+        n = arrays[0].shape[0]
+        alpha = (np.zeros(n) if alpha0 is None else np.array(alpha0, np.float64, copy=True))
+        it = _c_i64(0)
+        res = _c_dbl(0.0)
+        self.orc.lib.orc_cg_fit_mod(self.h, n, *(_ptr(a) for a in arrays), _ptr(y), float(lam),
+                                    int(imax), float(eps), 0 if alpha0 is None else 1,
+                                    _ptr(alpha), ctypes.byref(it), ctypes.byref(res))
+        return alpha, int(it.value), float(res.value)
+
 
 REF_DEFAULT, REF_STREAMING, REF_NAIVE = 0, 1, 2
 
@@ -203,6 +280,9 @@ class Reference:
         L.ref_last_error.restype = ctypes.c_char_p
         L.ref_grid_create_linear.restype = _vp
         L.ref_grid_create_linear.argtypes = [_c_int]
+        L.ref_grid_create_modlinear.restype = _vp
+        L.ref_grid_create_modlinear.argtypes = [_c_int]
+        L.ref_grid_mask_arrays.argtypes = [_vp, _vp, _vp, _vp, _vp]
         L.ref_grid_destroy.argtypes = [_vp]
         L.ref_grid_regular.argtypes = [_vp, _c_int]
         L.ref_grid_size.restype = _c_i64
@@ -226,8 +306,8 @@ class Reference:
         if rc != 0:
             raise RuntimeError(self.lib.ref_last_error().decode())
 
-    def grid(self, dim: int, level: int | None = None):
-        return RefGrid(self, dim, level)
+    def grid(self, dim: int, level: int | None = None, basis: str = "linear"):
+        return RefGrid(self, dim, level, basis)
 
     def set_threads(self, n: int) -> None:
         self.lib.ref_set_threads(int(n))
@@ -237,10 +317,16 @@ class Reference:
 
 
 class RefGrid:
-    def __init__(self, ref: Reference, dim: int, level: int | None):
+    def __init__(self, ref: Reference, dim: int, level: int | None, basis: str = "linear"):
         self.ref = ref
         self.dim = dim
-        self.h = ref.lib.ref_grid_create_linear(dim)
+        self.basis = basis
+        if basis == "linear":
+            self.h = ref.lib.ref_grid_create_linear(dim)
+        elif basis == "modlinear":
+            self.h = ref.lib.ref_grid_create_modlinear(dim)
+        else:
+            raise ValueError(f"unknown basis {basis!r}")
         if level is not None:
             ref._check(ref.lib.ref_grid_regular(self.h, level))
 
@@ -269,6 +355,12 @@ class RefGrid:
         ix = np.zeros((n, self.dim))
         self.ref._check(self.ref.lib.ref_grid_level_index(self.h, _ptr(lp), _ptr(ix)))
         return lp, ix
+
+    def mask_arrays(self):
+        n = self.size
+        out = [np.zeros((n, self.dim)) for _ in range(4)]
+        self.ref._check(self.ref.lib.ref_grid_mask_arrays(self.h, *(_ptr(a) for a in out)))
+        return tuple(out)
 
     def set_bounding_box(self, left, right):
         l = np.ascontiguousarray(left, np.float64)

@@ -2,7 +2,8 @@
  * ORACLE — test infrastructure only.
  *
  * A plain-C, FP64 restatement of SG++'s multi-evaluation path for the piecewise-linear hat
- * basis on Linear (no-boundary) sparse grids. Only tests/, __graft_entry__.smoke() and the
+ * basis on Linear (no-boundary) sparse grids, and for the modified linear basis on ModLinear
+ * grids (the same grid points; boundary-adjacent functions extrapolate to the cube faces). Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline leg of bench.py may load this library, and only as the checker (or the timed
  * CPU baseline). The shipped CUDA path never calls into it.
  *
@@ -352,6 +353,58 @@ ORC_API void orc_mult_transpose_naive(int dim, int64_t n, const double* level_po
 }
 
 /* ------------------------------------------------------------------------------------------
+ * Modified linear basis, LinearModifiedBasis::eval
+ * (base/src/sgpp/base/operation/hash/common/basis/LinearModifiedBasis.hpp:40-58), raw (l, i):
+ *   l == 1        -> 1
+ *   i == 1        -> 2 - 2^l x   for x <= 2 / 2^l, else 0
+ *   i == 2^l - 1  -> 2^l x - i + 1   for x >= 1 - 2 / 2^l, else 0
+ *   otherwise     -> max(1 - |2^l x - i|, 0)
+ * NAIVE-shaped products over it (every grid point per data point, the summation order of
+ * orc_mult_naive); the reference's DEFAULT ModLinear operator (OperationMultipleEvalModLinear.cpp,
+ * AlgorithmDGEMV over this basis) gives the same values up to summation order.
+ * ------------------------------------------------------------------------------------------ */
+ORC_API double orc_modlinear_eval(int l, int i, double x) {
+  const double hinv = (double)(1 << l);
+  if (l == 1) return 1.0;
+  if (i == 1) return x <= 2.0 / hinv ? 2.0 - hinv * x : 0.0;
+  if (i == (1 << l) - 1) return x >= 1.0 - 2.0 / hinv ? hinv * x - (double)i + 1.0 : 0.0;
+  const double v = 1.0 - fabs(hinv * x - (double)i);
+  return v > 0.0 ? v : 0.0;
+}
+
+static double mod_product(int dim, const int32_t* lev, const int32_t* idx, const double* x) {
+  double v = 1.0;
+  for (int t = 0; t < dim; ++t) {
+    const double h = orc_modlinear_eval(lev[t], idx[t], x[t]);
+    if (h == 0.0) return 0.0;
+    v *= h;
+  }
+  return v;
+}
+
+ORC_API void orc_mult_naive_mod(int dim, int64_t n, const int32_t* lev, const int32_t* idx,
+                                int64_t m, const double* data, const double* alpha,
+                                double* result) {
+  for (int64_t j = 0; j < m; ++j) {
+    double acc = 0.0;
+    for (int64_t i = 0; i < n; ++i)
+      acc += alpha[i] * mod_product(dim, lev + i * dim, idx + i * dim, data + j * dim);
+    result[j] = acc;
+  }
+}
+
+ORC_API void orc_mult_transpose_naive_mod(int dim, int64_t n, const int32_t* lev,
+                                          const int32_t* idx, int64_t m, const double* data,
+                                          const double* source, double* result) {
+  for (int64_t i = 0; i < n; ++i) {
+    double acc = 0.0;
+    for (int64_t j = 0; j < m; ++j)
+      acc += source[j] * mod_product(dim, lev + i * dim, idx + i * dim, data + j * dim);
+    result[i] = acc;
+  }
+}
+
+/* ------------------------------------------------------------------------------------------
  * STREAMING-shaped dense kernels (the CPU baseline restatement).
  * OperationMultiEvalStreaming.cpp:92-143 with the portable kernels
  * OperationMultiEvalStreaming_multImpl.cpp:577-623 and _multTransposeImpl.cpp:485-510:
@@ -452,6 +505,120 @@ ORC_API void orc_stream_mult_transpose(void* h, int64_t n, const double* level_p
   }
 }
 
+/* ------------------------------------------------------------------------------------------
+ * ModLinear STREAMING (OperationMultiEvalModMaskStreaming).
+ * Layout, HashGridStorage::getLevelIndexMaskArraysForModEval (HashGridStorage.cpp:519-559) and
+ * OperationMultiEvalModMaskStreaming::recalculateLevelIndexMask (.cpp:182-250), per (point, dim)
+ * with raw (l, i):
+ *   l == 1        : level 0,     index 0, mask 0,        offset 1
+ *   i == 1        : level -2^l,  index 0, mask 0,        offset 2
+ *   i == 2^l - 1  : level 2^l,   index i, mask 0,        offset 1
+ *   otherwise     : level 2^l,   index i, mask sign bit, offset 1
+ * Evaluation, _multImpl.cpp:83-122 / _multTransposeImpl.cpp (same steps):
+ *   phi = max(offset + (mask | (level * x - index)), 0)
+ * where `|` is the bitwise or of the 64-bit patterns (the sign bit turns t into -|t|).
+ * The mask array holds the raw bit patterns in double storage, as in the reference.
+ * ------------------------------------------------------------------------------------------ */
+ORC_API void orc_mod_mask_arrays(int dim, int64_t n, const int32_t* lev, const int32_t* idx,
+                                 double* level, double* index, double* mask, double* offset) {
+  for (int64_t g = 0; g < n; ++g)
+    for (int t = 0; t < dim; ++t) {
+      const int64_t k = g * dim + t;
+      const int l = lev[k], i = idx[k];
+      uint64_t bits = 0;
+      if (l == 1) {
+        level[k] = 0.0;
+        index[k] = 0.0;
+        offset[k] = 1.0;
+      } else if (i == 1) {
+        level[k] = -(double)(1 << l);
+        index[k] = 0.0;
+        offset[k] = 2.0;
+      } else if (i == (1 << l) - 1) {
+        level[k] = (double)(1 << l);
+        index[k] = (double)i;
+        offset[k] = 1.0;
+      } else {
+        level[k] = (double)(1 << l);
+        index[k] = (double)i;
+        bits = 0x8000000000000000ull;
+        offset[k] = 1.0;
+      }
+      memcpy(&mask[k], &bits, sizeof bits);
+    }
+}
+
+static inline double mod_mask_eval(double level, double index, double mask, double offset,
+                                   double x) {
+  double t = level * x - index;
+  uint64_t tb, mb;
+  memcpy(&tb, &t, sizeof tb);
+  memcpy(&mb, &mask, sizeof mb);
+  tb |= mb;
+  memcpy(&t, &tb, sizeof t);
+  const double v = offset + t;
+  return v > 0.0 ? v : 0.0;
+}
+
+ORC_API void orc_stream_mult_mod(void* h, int64_t n, const double* level, const double* index,
+                                 const double* mask, const double* offset, const double* alpha,
+                                 double* result) {
+  const orc_stream_data* s = (const orc_stream_data*)h;
+  const int dim = s->dim;
+  const int64_t nchunks = s->mpad / ORC_CHUNK;
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < nchunks; ++c) {
+    double acc[ORC_CHUNK];
+    double cur[ORC_CHUNK];
+    const int64_t base = c * ORC_CHUNK;
+    for (int k = 0; k < ORC_CHUNK; ++k) acc[k] = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+      const double a = alpha[i];
+      for (int k = 0; k < ORC_CHUNK; ++k) cur[k] = a;
+      for (int t = 0; t < dim; ++t) {
+        const int64_t q = i * dim + t;
+        const double* x = &s->xt[t * s->mpad + base];
+        for (int k = 0; k < ORC_CHUNK; ++k)
+          cur[k] *= mod_mask_eval(level[q], index[q], mask[q], offset[q], x[k]);
+      }
+      for (int k = 0; k < ORC_CHUNK; ++k) acc[k] += cur[k];
+    }
+    for (int k = 0; k < ORC_CHUNK; ++k) {
+      if (base + k < s->m) result[base + k] = acc[k];
+    }
+  }
+}
+
+ORC_API void orc_stream_mult_transpose_mod(void* h, int64_t n, const double* level,
+                                           const double* index, const double* mask,
+                                           const double* offset, const double* source,
+                                           double* result) {
+  const orc_stream_data* s = (const orc_stream_data*)h;
+  const int dim = s->dim;
+  const int64_t nchunks = s->mpad / ORC_CHUNK;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < n; ++i) {
+    double part[ORC_CHUNK];
+    double cur[ORC_CHUNK];
+    for (int k = 0; k < ORC_CHUNK; ++k) part[k] = 0.0;
+    for (int64_t c = 0; c < nchunks; ++c) {
+      const int64_t base = c * ORC_CHUNK;
+      for (int k = 0; k < ORC_CHUNK; ++k)
+        cur[k] = (base + k < s->m) ? source[base + k] : 0.0; /* padding source = 0 */
+      for (int t = 0; t < dim; ++t) {
+        const int64_t q = i * dim + t;
+        const double* x = &s->xt[t * s->mpad + base];
+        for (int k = 0; k < ORC_CHUNK; ++k)
+          cur[k] *= mod_mask_eval(level[q], index[q], mask[q], offset[q], x[k]);
+      }
+      for (int k = 0; k < ORC_CHUNK; ++k) part[k] += cur[k];
+    }
+    double total = 0.0;
+    for (int k = 0; k < ORC_CHUNK; ++k) total += part[k];
+    result[i] = total;
+  }
+}
+
 ORC_API int orc_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();
@@ -475,10 +642,31 @@ ORC_API void orc_set_threads(int n) {
  * relative stopping test delta_new <= eps^2 delta_0, true residual recomputed every 50
  * iterations, optional warm start (reuse).
  * ------------------------------------------------------------------------------------------ */
-static void sys_apply(void* h, int64_t n, const double* lp, const double* ix, double lambda_m,
-                      const double* a, double* out, double* tmp) {
-  orc_stream_mult(h, n, lp, ix, a, tmp);
-  orc_stream_mult_transpose(h, n, lp, ix, tmp, out);
+/* level/index arrays of either basis: mask == NULL selects the Linear (level_pow2, index) pair,
+ * otherwise the ModLinear (level, index, mask, offset) streaming layout */
+typedef struct {
+  const double *level, *index, *mask, *offset;
+} orc_arrays;
+
+static void arr_mult(void* h, int64_t n, const orc_arrays* A, const double* a, double* out) {
+  if (A->mask)
+    orc_stream_mult_mod(h, n, A->level, A->index, A->mask, A->offset, a, out);
+  else
+    orc_stream_mult(h, n, A->level, A->index, a, out);
+}
+
+static void arr_mult_transpose(void* h, int64_t n, const orc_arrays* A, const double* v,
+                               double* out) {
+  if (A->mask)
+    orc_stream_mult_transpose_mod(h, n, A->level, A->index, A->mask, A->offset, v, out);
+  else
+    orc_stream_mult_transpose(h, n, A->level, A->index, v, out);
+}
+
+static void sys_apply(void* h, int64_t n, const orc_arrays* A, double lambda_m, const double* a,
+                      double* out, double* tmp) {
+  arr_mult(h, n, A, a, tmp);
+  arr_mult_transpose(h, n, A, tmp, out);
   for (int64_t i = 0; i < n; ++i) out[i] += lambda_m * a[i];
 }
 
@@ -488,9 +676,9 @@ static double dot(int64_t n, const double* a, const double* b) {
   return s;
 }
 
-ORC_API int orc_cg_fit(void* h, int64_t n, const double* level_pow2, const double* index,
-                       const double* y, double lambda, int64_t imax, double eps, int reuse,
-                       double* alpha, int64_t* iterations, double* residual) {
+static int cg_fit(void* h, int64_t n, const orc_arrays* A, const double* y, double lambda,
+                  int64_t imax, double eps, int reuse, double* alpha, int64_t* iterations,
+                  double* residual) {
   const orc_stream_data* s = (const orc_stream_data*)h;
   const double lambda_m = (double)s->m * lambda;
   double* tmp = (double*)malloc(sizeof(double) * (size_t)s->mpad);
@@ -499,7 +687,7 @@ ORC_API int orc_cg_fit(void* h, int64_t n, const double* level_pow2, const doubl
   double* d = (double*)malloc(sizeof(double) * (size_t)n);
   double* q = (double*)malloc(sizeof(double) * (size_t)n);
   double* t = (double*)malloc(sizeof(double) * (size_t)n);
-  orc_stream_mult_transpose((void*)s, n, level_pow2, index, y, b); /* generateb, :49-56 */
+  arr_mult_transpose((void*)s, n, A, y, b); /* generateb, :49-56 */
 
   const double eps2 = eps * eps;
   double delta_0 = 0.0;
@@ -510,20 +698,20 @@ ORC_API int orc_cg_fit(void* h, int64_t n, const double* level_pow2, const doubl
   } else {
     for (int64_t i = 0; i < n; ++i) alpha[i] = 0.0;
   }
-  sys_apply((void*)s, n, level_pow2, index, lambda_m, alpha, t, tmp);
+  sys_apply((void*)s, n, A, lambda_m, alpha, t, tmp);
   for (int64_t i = 0; i < n; ++i) r[i] -= t[i];
   memcpy(d, r, sizeof(double) * (size_t)n);
   double delta_new = dot(n, r, r);
   if (!reuse) delta_0 = delta_new * eps2;
   int64_t it = 0;
   while (it < imax && delta_new > delta_0 && delta_new > 0.0) {
-    sys_apply((void*)s, n, level_pow2, index, lambda_m, d, q, tmp);
+    sys_apply((void*)s, n, A, lambda_m, d, q, tmp);
     const double dq = dot(n, d, q);
     if (dq == 0.0) break;
     const double a = delta_new / dq;
     for (int64_t i = 0; i < n; ++i) alpha[i] += a * d[i];
     if (it % 50 == 0 && it > 0) {
-      sys_apply((void*)s, n, level_pow2, index, lambda_m, alpha, t, tmp);
+      sys_apply((void*)s, n, A, lambda_m, alpha, t, tmp);
       for (int64_t i = 0; i < n; ++i) r[i] = b[i] - t[i];
     } else {
       for (int64_t i = 0; i < n; ++i) r[i] -= a * q[i];
@@ -543,4 +731,21 @@ ORC_API int orc_cg_fit(void* h, int64_t n, const double* level_pow2, const doubl
   free(q);
   free(t);
   return 0;
+}
+
+ORC_API int orc_cg_fit(void* h, int64_t n, const double* level_pow2, const double* index,
+                       const double* y, double lambda, int64_t imax, double eps, int reuse,
+                       double* alpha, int64_t* iterations, double* residual) {
+  const orc_arrays A = {level_pow2, index, NULL, NULL};
+  return cg_fit(h, n, &A, y, lambda, imax, eps, reuse, alpha, iterations, residual);
+}
+
+/* the same fit on a ModLinear grid (the reference factory gives SystemMatrixLeastSquaresIdentity
+ * OperationMultiEvalModMaskStreaming for STREAMING there, DatadrivenOpFactory.cpp:479-483) */
+ORC_API int orc_cg_fit_mod(void* h, int64_t n, const double* level, const double* index,
+                           const double* mask, const double* offset, const double* y,
+                           double lambda, int64_t imax, double eps, int reuse, double* alpha,
+                           int64_t* iterations, double* residual) {
+  const orc_arrays A = {level, index, mask, offset};
+  return cg_fit(h, n, &A, y, lambda, imax, eps, reuse, alpha, iterations, residual);
 }

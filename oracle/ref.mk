@@ -6,7 +6,8 @@
 #   make -f oracle/ref.mk -j8 REF=/path/to/reference
 #
 # Sources: every base/src translation unit except the OpenCL manager (no OpenCL headers
-# exist here), solver/src, the STREAMING operator and the two system-matrix files.
+# exist here), solver/src, the STREAMING operators of the Linear and ModLinear bases and the
+# two system-matrix files.
 # Quirks needed with g++ 13: -include cstdint -include memory (missing includes in the
 # reference headers, e.g. base/src/sgpp/base/grid/storage/hashmap/HashGridPoint.hpp).
 
@@ -32,6 +33,9 @@ DD := $(REF)/datadriven/src/sgpp/datadriven
 DD_SRCS := $(DD)/operation/hash/OperationMultiEvalStreaming/OperationMultiEvalStreaming.cpp \
            $(DD)/operation/hash/OperationMultiEvalStreaming/OperationMultiEvalStreaming_multImpl.cpp \
            $(DD)/operation/hash/OperationMultiEvalStreaming/OperationMultiEvalStreaming_multTransposeImpl.cpp \
+           $(DD)/operation/hash/OperationMultiEvalModMaskStreaming/OperationMultiEvalModMaskStreaming.cpp \
+           $(DD)/operation/hash/OperationMultiEvalModMaskStreaming/OperationMultiEvalModMaskStreaming_multImpl.cpp \
+           $(DD)/operation/hash/OperationMultiEvalModMaskStreaming/OperationMultiEvalModMaskStreaming_multTransposeImpl.cpp \
            $(DD)/algorithm/SystemMatrixLeastSquaresIdentity.cpp \
            $(DD)/algorithm/DMSystemMatrixBase.cpp
 

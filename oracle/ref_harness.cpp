@@ -14,6 +14,12 @@
 //             -> OperationMultipleEvalLinear            base/.../BaseOpFactory.cpp:595-598
 //   NAIVE     OperationMultipleEvalLinearNaive          base/.../OperationMultipleEvalLinearNaive.cpp
 //   STREAMING OperationMultiEvalStreaming               datadriven/.../OperationMultiEvalStreaming.cpp
+//   ModLinear Grid::createModLinearGrid                 base/src/sgpp/base/grid/Grid.cpp
+//             DEFAULT -> OperationMultipleEvalModLinear base/.../BaseOpFactory.cpp (ModLinear branch)
+//             STREAMING -> OperationMultiEvalModMaskStreaming
+//                                                       datadriven/.../OperationMultiEvalModMaskStreaming.cpp
+//             HashGridStorage::getLevelIndexMaskArraysForModEval
+//                                                       base/.../HashGridStorage.cpp:519-559
 //   CG fit    SystemMatrixLeastSquaresIdentity + solver::ConjugateGradients
 //                                                       datadriven/.../SystemMatrixLeastSquaresIdentity.cpp
 //                                                       solver/src/sgpp/solver/sle/ConjugateGradients.cpp
@@ -22,7 +28,7 @@
 // (datadriven/src/sgpp/datadriven/DatadrivenOpFactory.cpp:409). That factory's translation
 // unit pulls in every datadriven operator, so this harness defines the one factory overload
 // itself and routes (DEFAULT) and (STREAMING, DEFAULT) exactly as the reference factory does
-// for Linear grids (DatadrivenOpFactory.cpp:439-452).
+// for Linear grids (DatadrivenOpFactory.cpp:439-452) and ModLinear grids (:479-483).
 
 #include <sgpp/base/datatypes/DataMatrix.hpp>
 #include <sgpp/base/datatypes/DataVector.hpp>
@@ -36,6 +42,7 @@
 #include <sgpp/base/tools/GaussLegendreQuadRule1D.hpp>
 #include <sgpp/datadriven/algorithm/SystemMatrixLeastSquaresIdentity.hpp>
 #include <sgpp/datadriven/operation/hash/DatadrivenOperationCommon.hpp>
+#include <sgpp/datadriven/operation/hash/OperationMultiEvalModMaskStreaming/OperationMultiEvalModMaskStreaming.hpp>
 #include <sgpp/datadriven/operation/hash/OperationMultiEvalStreaming/OperationMultiEvalStreaming.hpp>
 #include <sgpp/solver/sle/ConjugateGradients.hpp>
 
@@ -67,8 +74,9 @@ GaussLegendreQuadRule1D& GaussLegendreQuadRule1D::getInstance() {
 }  // namespace base
 
 namespace op_factory {
-// Routing for Linear grids as in DatadrivenOpFactory.cpp:439-452 (DEFAULT -> base factory,
-// STREAMING/DEFAULT -> OperationMultiEvalStreaming); every other combination throws, like
+// Routing as in DatadrivenOpFactory.cpp:439-452 and :479-483 (DEFAULT -> base factory;
+// STREAMING/DEFAULT -> OperationMultiEvalStreaming for Linear grids and
+// OperationMultiEvalModMaskStreaming for ModLinear grids); every other combination throws, like
 // the reference's final `throw factory_exception` (DatadrivenOpFactory.cpp:551).
 base::OperationMultipleEval* createOperationMultipleEval(
     base::Grid& grid, base::DataMatrix& dataset,
@@ -82,6 +90,11 @@ base::OperationMultipleEval* createOperationMultipleEval(
       configuration.getType() == OperationMultipleEvalType::STREAMING &&
       configuration.getSubType() == OperationMultipleEvalSubType::DEFAULT) {
     return new datadriven::OperationMultiEvalStreaming(grid, dataset);
+  }
+  if (grid.getType() == base::GridType::ModLinear &&
+      configuration.getType() == OperationMultipleEvalType::STREAMING &&
+      configuration.getSubType() == OperationMultipleEvalSubType::DEFAULT) {
+    return new datadriven::OperationMultiEvalModMaskStreaming(grid, dataset);
   }
   throw base::factory_exception("oracle harness: unsupported multi-eval configuration");
 }
@@ -112,8 +125,13 @@ std::unique_ptr<sgpp::base::OperationMultipleEval> make_op(RefGrid* g,
       return std::unique_ptr<sgpp::base::OperationMultipleEval>(
           sgpp::op_factory::createOperationMultipleEval(*g->grid, data));
     case REF_STREAMING:
+      if (g->grid->getType() == sgpp::base::GridType::ModLinear)
+        return std::make_unique<sgpp::datadriven::OperationMultiEvalModMaskStreaming>(*g->grid,
+                                                                                      data);
       return std::make_unique<sgpp::datadriven::OperationMultiEvalStreaming>(*g->grid, data);
     case REF_NAIVE:
+      if (g->grid->getType() != sgpp::base::GridType::Linear)
+        throw sgpp::base::factory_exception("the NAIVE kind is Linear only");
       return std::make_unique<sgpp::base::OperationMultipleEvalLinearNaive>(*g->grid, data);
     default:
       throw sgpp::base::factory_exception("unknown reference kind");
@@ -162,6 +180,12 @@ void* ref_grid_create_linear(int dim) {
   return g;
 }
 
+void* ref_grid_create_modlinear(int dim) {
+  RefGrid* g = new RefGrid;
+  g->grid.reset(sgpp::base::Grid::createModLinearGrid(static_cast<size_t>(dim)));
+  return g;
+}
+
 void ref_grid_destroy(void* h) { delete static_cast<RefGrid*>(h); }
 
 int ref_grid_regular(void* h, int level) {
@@ -186,6 +210,23 @@ int ref_grid_level_index(void* h, double* level_pow2, double* index) {
     st.getLevelIndexArraysForEval(lv, ix);
     std::memcpy(level_pow2, lv.getPointer(), sizeof(double) * lv.getSize());
     std::memcpy(index, ix.getPointer(), sizeof(double) * ix.getSize());
+  });
+}
+
+// The ModLinear streaming layout (HashGridStorage::getLevelIndexMaskArraysForModEval): four
+// [N x d] row-major arrays; mask holds raw 64-bit sign masks in double storage.
+int ref_grid_mask_arrays(void* h, double* level, double* index, double* mask, double* offset) {
+  return guarded([&] {
+    auto& st = static_cast<RefGrid*>(h)->grid->getStorage();
+    sgpp::base::DataMatrix lv(st.getSize(), st.getDimension());
+    sgpp::base::DataMatrix ix(st.getSize(), st.getDimension());
+    sgpp::base::DataMatrix mk(st.getSize(), st.getDimension());
+    sgpp::base::DataMatrix of(st.getSize(), st.getDimension());
+    st.getLevelIndexMaskArraysForModEval(lv, ix, mk, of);
+    std::memcpy(level, lv.getPointer(), sizeof(double) * lv.getSize());
+    std::memcpy(index, ix.getPointer(), sizeof(double) * ix.getSize());
+    std::memcpy(mask, mk.getPointer(), sizeof(double) * mk.getSize());
+    std::memcpy(offset, of.getPointer(), sizeof(double) * of.getSize());
   });
 }
 
@@ -279,7 +320,7 @@ int ref_streaming_time(void* h, const double* data, int64_t m, const double* alp
     RefGrid* g = static_cast<RefGrid*>(h);
     const int dim = static_cast<int>(g->grid->getDimension());
     sgpp::base::DataMatrix x = make_matrix(data, m, dim);
-    sgpp::datadriven::OperationMultiEvalStreaming op(*g->grid, x);
+    auto op = make_op(g, x, REF_STREAMING);
     sgpp::base::DataVector a(g->grid->getSize());
     std::memcpy(a.getPointer(), alpha, sizeof(double) * a.getSize());
     sgpp::base::DataVector s(static_cast<size_t>(m));
@@ -287,10 +328,10 @@ int ref_streaming_time(void* h, const double* data, int64_t m, const double* alp
     sgpp::base::DataVector r1(static_cast<size_t>(m));
     sgpp::base::DataVector r2(g->grid->getSize());
     for (int k = 0; k < reps; ++k) {
-      op.mult(a, r1);
-      mult_seconds[k] = op.getDuration();
-      op.multTranspose(s, r2);
-      multt_seconds[k] = op.getDuration();
+      op->mult(a, r1);
+      mult_seconds[k] = op->getDuration();
+      op->multTranspose(s, r2);
+      multt_seconds[k] = op->getDuration();
     }
   });
 }

@@ -195,6 +195,7 @@ def fma_peak(precision: int = SGMEV_FP32):
 # ---- grids --------------------------------------------------------------------------------
 class GridType(enum.IntEnum):
     Linear = 0
+    ModLinear = 1
 
 
 class BoundingBox1D:
@@ -320,17 +321,26 @@ class GridGenerator:
 
 
 class Grid:
-    """A Linear (hat basis, no boundary) sparse grid (Grid::createLinearGrid, Grid.cpp:73)."""
+    """A sparse grid without boundary points: Linear (hat basis, Grid::createLinearGrid,
+    Grid.cpp:73) or ModLinear (the same points with the modified linear basis,
+    Grid::createModLinearGrid; LinearModifiedBasis.hpp:40-58)."""
 
-    def __init__(self, dim: int):
+    def __init__(self, dim: int, gridType: GridType = GridType.Linear):
         self._storage = GridStorage(dim)
         self._generator = GridGenerator(self)
+        self._type = GridType(gridType)
 
     @staticmethod
     def createLinearGrid(dim: int) -> "Grid":
         if dim < 1:
             raise GenerationException("dimension must be >= 1")
         return Grid(int(dim))
+
+    @staticmethod
+    def createModLinearGrid(dim: int) -> "Grid":
+        if dim < 1:
+            raise GenerationException("dimension must be >= 1")
+        return Grid(int(dim), GridType.ModLinear)
 
     @staticmethod
     def regularSize(dim: int, level: int) -> int:
@@ -341,10 +351,10 @@ class Grid:
         return int(n.value)
 
     @staticmethod
-    def fromArrays(level, index) -> "Grid":
+    def fromArrays(level, index, gridType: GridType = GridType.Linear) -> "Grid":
         """A grid from raw [N x d] level / index rows (e.g. exported from an SG++ storage)."""
         level = np.ascontiguousarray(level, np.int32)
-        g = Grid(level.shape[1])
+        g = Grid(level.shape[1], gridType)
         g._storage.level = level.copy()
         g._storage.index = np.ascontiguousarray(index, np.int32).copy()
         return g
@@ -365,7 +375,7 @@ class Grid:
         return self._storage.getDimension()
 
     def getType(self) -> GridType:
-        return GridType.Linear
+        return self._type
 
 
 # ---- operator configuration (DatadrivenOperationCommon.hpp:17-95) ---------------------------
@@ -451,7 +461,7 @@ def _precision_of(params: dict) -> int:
 
 
 class OperationMultiEvalCuda:
-    """B / B^T on the GPU for a Linear grid (OperationMultipleEval interface)."""
+    """B / B^T on the GPU for a Linear or ModLinear grid (OperationMultipleEval interface)."""
 
     def __init__(self, grid: Grid, dataset, precision: int = SGMEV_FP64,
                  params: Optional[dict] = None):
@@ -471,6 +481,8 @@ class OperationMultiEvalCuda:
         knobs = {k: str(v) for k, v in (params or {}).items()
                  if k in ("precond", "algo", "inner_tol", "materialize", "materialize_multt",
                           "inner_products")}
+        if grid.getType() == GridType.ModLinear:
+            knobs["basis"] = "modlinear"
         pj = json.dumps(knobs).encode() if knobs else None
         _check(L.sgmev_create(ctypes.byref(h), st.getDimension(), st.getSize(), _vp(lp), _vp(ix),
                               self.dataset.shape[0], _vp(self.dataset), _vp(left), _vp(right),
@@ -653,6 +665,8 @@ class BatchEngine:
 
     def add(self, grid: Grid, X, Y, lam: float, epsilon: float = 1e-8,
             max_iterations: int = 100000) -> int:
+        if grid.getType() != GridType.Linear:
+            raise FactoryException("the batch engine serves Linear grids")
         st = grid.getStorage()
         lp, ix = st.getLevelIndexArraysForEval()
         X = _as_matrix(X)
@@ -710,15 +724,16 @@ class BatchEngine:
 
 def createOperationMultipleEval(grid: Grid, dataset,
                                 configuration: Optional[OperationMultipleEvalConfiguration] = None):
-    """op_factory::createOperationMultipleEval with the new CUDA branch for Linear grids.
+    """op_factory::createOperationMultipleEval with the new CUDA branch for Linear and ModLinear
+    grids (DatadrivenOpFactory.cpp:439-452 and :479-483).
 
-    (Linear, STREAMING, CUDA) and, when no configuration is given, the default route both give
-    the GPU operator; every other combination raises FactoryException, as the reference does for
-    combinations it was not built with (DatadrivenOpFactory.cpp:551)."""
+    (Linear or ModLinear, STREAMING, CUDA) and, when no configuration is given, the default route
+    give the GPU operator; every other combination raises FactoryException, as the reference does
+    for combinations it was not built with (DatadrivenOpFactory.cpp:551)."""
     if configuration is None:
         configuration = OperationMultipleEvalConfiguration(
             OperationMultipleEvalType.STREAMING, OperationMultipleEvalSubType.CUDA)
-    if grid.getType() != GridType.Linear:
+    if grid.getType() not in (GridType.Linear, GridType.ModLinear):
         raise FactoryException("OperationMultipleEval is not implemented for this grid type.")
     if (configuration.getType() == OperationMultipleEvalType.STREAMING
             and configuration.getSubType() == OperationMultipleEvalSubType.CUDA

@@ -25,8 +25,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3,-fvisib
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall",
              "-I" + os.path.join(ROOT, "include")]
 
-CU_SOURCES = ["sgmev.cu", "peak.cu", "noalloc.cu", "batch.cu", "subspace.cu", "subspace_mat.cu",
-              "devmem.cu"]
+CU_SOURCES = ["sgmev.cu", "dense_mod.cu", "peak.cu", "noalloc.cu", "batch.cu", "subspace.cu",
+              "subspace_mat.cu", "devmem.cu"]
 CPP_SOURCES = ["grid.cpp"]
 
 

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/sgmev.h"
+#include "dense.h"
 #include "kernels.cuh"
 #include "devmem.h"
 #include "subspace.h"
@@ -48,12 +49,8 @@ static int fail(int code, const std::string& msg) {
     if (rc_ != SGMEV_OK) return rc_; \
   } while (0)
 
-constexpr int kBlock = 128;
-constexpr int kGT = 32;       // grid points per shared-memory tile (mult)
-constexpr int kDT = 64;       // data points per shared-memory tile (multT)
 constexpr int64_t kMPadTo = 1024;
 constexpr int64_t kNPadTo = 512;
-constexpr int kMaxTemplDim = 16;
 constexpr int kReduceBlocks = 1216;  // 8 x 152 SMs
 constexpr int kDotBlocks = 304;
 constexpr int kDotThreads = 256;
@@ -61,21 +58,6 @@ constexpr int kCgSlots = 10;
 
 static inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
-
-// Register blocking per precision and dimension (data points per thread for mult, grid points
-// per thread for multT).
-template <typename T>
-struct Blocking;
-template <>
-struct Blocking<float> {
-  static constexpr int mult_r(int dim) { return dim <= 12 ? 8 : 4; }
-  static constexpr int multt_r(int) { return 4; }
-};
-template <>
-struct Blocking<double> {
-  static constexpr int mult_r(int) { return 4; }
-  static constexpr int multt_r(int) { return 2; }
-};
 
 struct Plan {
   int64_t tiles = 0;   // CTAs along the tiled axis
@@ -102,7 +84,11 @@ struct sgmev_op {
   double2* li64 = nullptr;
   float2* li32 = nullptr;
   float4* gq = nullptr;     // df64 grid constants (2^l, 1 - i, 1 + i, 0)
+  double* gs64 = nullptr;   // ModLinear: per-grid-point factor 2^b (0 on padding)
+  float* gs32 = nullptr;
   int64_t npad_cap = 0;
+  bool mod = false;         // modified linear basis (ModLinear grid; params "basis")
+  bool in_cube = true;      // every data coordinate lies in [0, 1]
 
   // work vectors
   double* a64 = nullptr;   // [npad] converted input (mult) / padded grid vector
@@ -177,6 +163,13 @@ enum {
 constexpr int kKinds = 17;
 
 template <typename T>
+static const T* gscale(const sgmev_op* op);
+template <>
+const float* gscale<float>(const sgmev_op* op) { return op->gs32; }
+template <>
+const double* gscale<double>(const sgmev_op* op) { return op->gs64; }
+
+template <typename T>
 static int kind_mult() { return sizeof(T) == 4 ? KIND_MULT_FP32 : KIND_MULT_FP64; }
 template <typename T>
 static int kind_multt() { return sizeof(T) == 4 ? KIND_MULTT_FP32 : KIND_MULTT_FP64; }
@@ -246,6 +239,65 @@ __global__ void stage_grid_kernel(const double* __restrict__ level_pow2,
   }
 }
 
+// ModLinear: (2^l, i) rows -> the scaled pairs and float-float constants of kernels.cuh and the
+// per-grid-point factors 2^b; one thread per grid point (padded rows: hat 0, factor 0)
+__global__ void stage_grid_mod_kernel(const double* __restrict__ level_pow2,
+                                      const double* __restrict__ index, int64_t n, int dim,
+                                      int64_t npad, double2* __restrict__ li64,
+                                      float2* __restrict__ li32, float4* __restrict__ gq,
+                                      double* __restrict__ gs64, float* __restrict__ gs32) {
+  for (int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; g < npad;
+       g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double scale = g < n ? 1.0 : 0.0;
+    for (int t = 0; t < dim; ++t) {
+      const int64_t k = g * dim + t;
+      double a = 0.0, c = 2.0;                  // padded row: t = -2, hat 0
+      float4 q = make_float4(0.0f, -1.0f, 3.0f, 0.0f);
+      if (g < n) {
+        const double L = level_pow2[k], I = index[k];
+        if (L == 2.0) {                         // level 1: constant 1
+          a = 0.0;
+          c = 0.0;
+          q = make_float4(0.0f, 1.0f, 1.0f, 0.0f);
+        } else if (I == 1.0) {                  // 2 (1 - (L / 2) x)
+          a = 0.5 * L;
+          c = -0.0;
+          q = make_float4(static_cast<float>(0.5 * L), kModOpen, 1.0f, 0.0f);
+          scale *= 2.0;
+        } else if (I == L - 1.0) {              // 2 (1 - (L / 2) (1 - x))
+          a = -0.5 * L;
+          c = -0.5 * L;
+          q = make_float4(static_cast<float>(0.5 * L), static_cast<float>(1.0 - 0.5 * L),
+                          kModOpen, 0.0f);
+          scale *= 2.0;
+        } else {
+          a = L;
+          c = I;
+          q = make_float4(static_cast<float>(L), static_cast<float>(1.0 - I),
+                          static_cast<float>(1.0 + I), 0.0f);
+        }
+      }
+      li64[k] = make_double2(a, c);
+      li32[k] = make_float2(static_cast<float>(a), static_cast<float>(c));
+      gq[k] = q;
+    }
+    gs64[g] = scale;
+    gs32[g] = static_cast<float>(scale);
+  }
+}
+
+// flag |= 1 when a staged coordinate lies outside [0, 1] (or is NaN)
+__global__ void cube_check_kernel(const double* __restrict__ xt, int64_t total,
+                                  unsigned int* __restrict__ flag) {
+  bool out = false;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const double x = xt[k];
+    out = out || !(x >= 0.0 && x <= 1.0);
+  }
+  if (__syncthreads_or(out) && threadIdx.x == 0) atomicOr(flag, 1u);
+}
+
 __global__ void convert_pad_kernel(const double* __restrict__ in, int64_t n, int64_t npad,
                                    double* __restrict__ out64, float* __restrict__ out32,
                                    float* __restrict__ out32lo) {
@@ -257,57 +309,6 @@ __global__ void convert_pad_kernel(const double* __restrict__ in, int64_t n, int
     if (out32) out32[k] = h;
     if (out32lo) out32lo[k] = static_cast<float>(v - static_cast<double>(h));
   }
-}
-
-// generic-dimension df64 kernels
-__global__ void mult_df_generic_kernel(const float* __restrict__ xh_t, const float* __restrict__ xl_t,
-                                       int64_t mpad, int dim, const float4* __restrict__ gq,
-                                       const float* __restrict__ ah_v, const float* __restrict__ al_v,
-                                       int64_t npad, int64_t chunk_len, int64_t j_offset,
-                                       int64_t j_count, float2* __restrict__ part) {
-  const int64_t j = j_offset + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (j >= j_offset + j_count) return;
-  const int64_t g_begin = static_cast<int64_t>(blockIdx.y) * chunk_len;
-  int64_t g_end = g_begin + chunk_len;
-  if (g_end > npad) g_end = npad;
-  ff acc{0.0f, 0.0f};
-  for (int64_t g = g_begin; g < g_end; ++g) {
-    ff p = hat_ff(xh_t[j], xl_t[j], gq[g * dim]);
-    for (int t = 1; t < dim; ++t) {
-      const int64_t src = static_cast<int64_t>(t) * mpad + j;
-      p = mul_ff(p, hat_ff(xh_t[src], xl_t[src], gq[g * dim + t]));
-    }
-    add_ff(acc, mul_ff(p, ff{ah_v[g], al_v[g]}));
-    if ((g & 31) == 31) renorm_ff(acc);
-  }
-  renorm_ff(acc);
-  part[static_cast<int64_t>(blockIdx.y) * mpad + j] = make_float2(acc.h, acc.l);
-}
-
-__global__ void mult_transpose_df_generic_kernel(const float* __restrict__ xh_t,
-                                                 const float* __restrict__ xl_t,
-                                                 const float* __restrict__ vh,
-                                                 const float* __restrict__ vl, int64_t mpad, int dim,
-                                                 const float4* __restrict__ gq, int64_t npad,
-                                                 int64_t chunk_len, int64_t g_offset,
-                                                 int64_t g_count, float2* __restrict__ part) {
-  const int64_t g = g_offset + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (g >= g_offset + g_count) return;
-  const int64_t j_begin = static_cast<int64_t>(blockIdx.y) * chunk_len;
-  int64_t j_end = j_begin + chunk_len;
-  if (j_end > mpad) j_end = mpad;
-  ff acc{0.0f, 0.0f};
-  for (int64_t j = j_begin; j < j_end; ++j) {
-    ff p = hat_ff(xh_t[j], xl_t[j], gq[g * dim]);
-    for (int t = 1; t < dim; ++t) {
-      const int64_t src = static_cast<int64_t>(t) * mpad + j;
-      p = mul_ff(p, hat_ff(xh_t[src], xl_t[src], gq[g * dim + t]));
-    }
-    add_ff(acc, mul_ff(p, ff{vh[j], vl[j]}));
-    if ((j & 31) == 31) renorm_ff(acc);
-  }
-  renorm_ff(acc);
-  part[static_cast<int64_t>(blockIdx.y) * npad + g] = make_float2(acc.h, acc.l);
 }
 
 // deterministic dot product: fixed grid, fixed tree
@@ -441,9 +442,6 @@ static void launch_multt_dim(sgmev_op* op, const T* xt, const T* v,
       xt, v, op->mpad, li, op->npad, p.chunk, tile_offset, part);
 }
 
-#define SGMEV_DIM_CASES(F) \
-  F(1) F(2) F(3) F(4) F(5) F(6) F(7) F(8) F(9) F(10) F(11) F(12) F(13) F(14) F(15) F(16)
-
 // mult over data range [j_begin, j_end): partial sums into op->part, returns the plan used.
 template <typename T>
 static int run_mult(sgmev_op* op, const T* xt, const typename Pair<T>::type* li, const T* alpha,
@@ -455,15 +453,21 @@ static int run_mult(sgmev_op* op, const T* xt, const typename Pair<T>::type* li,
     const int64_t t1 = ceil_div(j_end, tile_pts);
     Plan p = plan_mult<T>(op, t1 - t0);
     const long ev = prof_begin(op, kind_mult<T>());
-    switch (op->dim) {
+    if (op->mod) {
+      mod_mult_launch<T>(op->dim, dim3(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit)),
+                         op->stream, xt, op->mpad, li, alpha, gscale<T>(op), op->npad, p.chunk,
+                         t0, 0, part);
+    } else {
+      switch (op->dim) {
 #define F(D)                                                         \
   case D:                                                            \
     launch_mult_dim<T, D>(op, xt, li, alpha, p, t0, part);           \
     break;
-      SGMEV_DIM_CASES(F)
+        SGMEV_DIM_CASES(F)
 #undef F
-      default:
-        break;
+        default:
+          break;
+      }
     }
     prof_end(op, ev);
     *used = p;
@@ -472,9 +476,14 @@ static int run_mult(sgmev_op* op, const T* xt, const typename Pair<T>::type* li,
     Plan p = plan_mult<T>(op, ceil_div(count, kBlock));
     dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
     const long ev = prof_begin(op, kind_mult<T>());
-    mult_generic_kernel<T><<<grid, kBlock, 0, op->stream>>>(xt, op->mpad, op->dim, li, alpha,
-                                                            op->npad, p.chunk, j_begin, count,
-                                                            part);
+    if (op->mod) {
+      mod_mult_launch<T>(op->dim, grid, op->stream, xt, op->mpad, li, alpha, gscale<T>(op),
+                         op->npad, p.chunk, j_begin, count, part);
+    } else {
+      mult_generic_kernel<T><<<grid, kBlock, 0, op->stream>>>(xt, op->mpad, op->dim, li, alpha,
+                                                              op->npad, p.chunk, j_begin, count,
+                                                              part);
+    }
     prof_end(op, ev);
     *used = p;
   }
@@ -493,15 +502,21 @@ static int run_multt(sgmev_op* op, const T* xt, const T* v, const typename Pair<
     const int64_t t1 = ceil_div(g_end, tile_pts);
     Plan p = plan_multt<T>(op, t1 - t0);
     const long ev = prof_begin(op, kind_multt<T>());
-    switch (op->dim) {
+    if (op->mod) {
+      mod_multt_launch<T, false>(op->dim, dim3(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit)),
+                                 op->stream, xt, v, op->mpad, li, gscale<T>(op), op->npad, p.chunk,
+                                 t0, 0, part);
+    } else {
+      switch (op->dim) {
 #define F(D)                                                      \
   case D:                                                         \
     launch_multt_dim<T, D>(op, xt, v, li, p, t0, part);           \
     break;
-      SGMEV_DIM_CASES(F)
+        SGMEV_DIM_CASES(F)
 #undef F
-      default:
-        break;
+        default:
+          break;
+      }
     }
     prof_end(op, ev);
     *used = p;
@@ -510,8 +525,13 @@ static int run_multt(sgmev_op* op, const T* xt, const T* v, const typename Pair<
     Plan p = plan_multt<T>(op, ceil_div(count, kBlock));
     dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
     const long ev = prof_begin(op, kind_multt<T>());
-    mult_transpose_generic_kernel<T><<<grid, kBlock, 0, op->stream>>>(
-        xt, v, op->mpad, op->dim, li, op->npad, p.chunk, g_begin, count, part);
+    if (op->mod) {
+      mod_multt_launch<T, false>(op->dim, grid, op->stream, xt, v, op->mpad, li, gscale<T>(op),
+                                 op->npad, p.chunk, g_begin, count, part);
+    } else {
+      mult_transpose_generic_kernel<T><<<grid, kBlock, 0, op->stream>>>(
+          xt, v, op->mpad, op->dim, li, op->npad, p.chunk, g_begin, count, part);
+    }
     prof_end(op, ev);
     *used = p;
   }
@@ -536,10 +556,6 @@ static int run_reduce(sgmev_op* op, int nsplit, int64_t stride, int64_t begin, i
 static unsigned vec_blocks(int64_t n) {
   return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(kReduceBlocks, ceil_div(n, 256))));
 }
-
-// df64 tile kernels (float-float), R = 4 data points / RG = 2 grid points per thread
-constexpr int kDfMultR = 4;
-constexpr int kDfMulttRG = 2;
 
 template <int DIM>
 static void launch_mult_df_dim(sgmev_op* op, const float* ah, const float* al, const Plan& p,
@@ -566,15 +582,21 @@ static int run_mult_df(sgmev_op* op, const float* ah, const float* al, int64_t j
     const int64_t t1 = ceil_div(j_end, tile_pts);
     Plan p = plan_mult<float>(op, t1 - t0);
     const long ev = prof_begin(op, KIND_MULT_DF64);
-    switch (op->dim) {
+    if (op->mod) {
+      mod_mult_df_launch(op->dim, dim3(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit)),
+                         op->stream, op->xt32, op->xt32lo, op->mpad, op->gq, ah, al, op->gs32,
+                         op->npad, p.chunk, t0, 0, part);
+    } else {
+      switch (op->dim) {
 #define F(D)                                               \
   case D:                                                  \
     launch_mult_df_dim<D>(op, ah, al, p, t0, part);        \
     break;
-      SGMEV_DIM_CASES(F)
+        SGMEV_DIM_CASES(F)
 #undef F
-      default:
-        break;
+        default:
+          break;
+      }
     }
     prof_end(op, ev);
     *used = p;
@@ -583,9 +605,14 @@ static int run_mult_df(sgmev_op* op, const float* ah, const float* al, int64_t j
     Plan p = plan_mult<float>(op, ceil_div(count, kBlock));
     dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
     const long ev = prof_begin(op, KIND_MULT_DF64);
-    mult_df_generic_kernel<<<grid, kBlock, 0, op->stream>>>(op->xt32, op->xt32lo, op->mpad, op->dim,
-                                                            op->gq, ah, al, op->npad, p.chunk,
-                                                            j_begin, count, part);
+    if (op->mod) {
+      mod_mult_df_launch(op->dim, grid, op->stream, op->xt32, op->xt32lo, op->mpad, op->gq, ah,
+                         al, op->gs32, op->npad, p.chunk, j_begin, count, part);
+    } else {
+      mult_df_generic_kernel<false><<<grid, kBlock, 0, op->stream>>>(
+          op->xt32, op->xt32lo, op->mpad, op->dim, op->gq, ah, al, op->npad, p.chunk, j_begin,
+          count, part);
+    }
     prof_end(op, ev);
     *used = p;
   }
@@ -603,15 +630,21 @@ static int run_multt_df(sgmev_op* op, const float* vh, const float* vl, int64_t 
     const int64_t t1 = ceil_div(g_end, tile_pts);
     Plan p = plan_multt<float>(op, t1 - t0);
     const long ev = prof_begin(op, KIND_MULTT_DF64);
-    switch (op->dim) {
+    if (op->mod) {
+      mod_multt_df_launch(op->dim, dim3(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit)),
+                          op->stream, op->xt32, op->xt32lo, vh, vl, op->mpad, op->gq, op->gs32,
+                          op->npad, p.chunk, t0, 0, part);
+    } else {
+      switch (op->dim) {
 #define F(D)                                                \
   case D:                                                   \
     launch_multt_df_dim<D>(op, vh, vl, p, t0, part);        \
     break;
-      SGMEV_DIM_CASES(F)
+        SGMEV_DIM_CASES(F)
 #undef F
-      default:
-        break;
+        default:
+          break;
+      }
     }
     prof_end(op, ev);
     *used = p;
@@ -620,9 +653,14 @@ static int run_multt_df(sgmev_op* op, const float* vh, const float* vl, int64_t 
     Plan p = plan_multt<float>(op, ceil_div(count, kBlock));
     dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
     const long ev = prof_begin(op, KIND_MULTT_DF64);
-    mult_transpose_df_generic_kernel<<<grid, kBlock, 0, op->stream>>>(
-        op->xt32, op->xt32lo, vh, vl, op->mpad, op->dim, op->gq, op->npad, p.chunk, g_begin,
-        count, part);
+    if (op->mod) {
+      mod_multt_df_launch(op->dim, grid, op->stream, op->xt32, op->xt32lo, vh, vl, op->mpad,
+                          op->gq, op->gs32, op->npad, p.chunk, g_begin, count, part);
+    } else {
+      mult_transpose_df_generic_kernel<false><<<grid, kBlock, 0, op->stream>>>(
+          op->xt32, op->xt32lo, vh, vl, op->mpad, op->dim, op->gq, op->npad, p.chunk, g_begin,
+          count, part);
+    }
     prof_end(op, ev);
     *used = p;
   }
@@ -656,6 +694,9 @@ static bool mat_ready(sgmev_op* op) {
   using namespace sgmev;
   if (op->sub.pmat) return true;
   if (op->mat_mode == 0 || op->mat_failed || !subspace_mat_fits(op->sub, false)) return false;
+  // ModLinear products are built for data in the cube (the cell of a boundary-adjacent function
+  // is clamped there); data outside it stays on the dense kernels, which extrapolate
+  if (op->mod && !op->in_cube) return false;
   const int64_t bytes = subspace_mat_bytes(op->sub, op->mpad);
   if (op->mat_mode == 1) {
     size_t free_b = 0, total_b = 0;
@@ -706,7 +747,7 @@ static int dev_mult(sgmev_op* op, int prec, const double* a64, const float* a32,
                                     j_begin, j_end, op->num_sms));
     prof_end(op, ev);
     op->launches += 2;
-  } else if (prec == SGMEV_DF64 && op->sub_ok && out64 && !out32) {
+  } else if (prec == SGMEV_DF64 && op->sub_ok && !op->mod && out64 && !out32) {
     const long ev = prof_begin(op, KIND_MULT_SUBDF);
     SGMEV_CUDA(subspace_mult_df(op->sub, op->stream, op->xt32, op->xt32lo, op->mpad, op->m, a32,
                                 a32lo, out64, j_begin, j_end, op->num_sms));
@@ -722,7 +763,7 @@ static int dev_mult(sgmev_op* op, int prec, const double* a64, const float* a32,
                                  j_begin, j_end, op->num_sms, op->use_half));
     prof_end(op, ev);
     op->launches += 2;
-  } else if (op->sub_ok) {
+  } else if (op->sub_ok && !op->mod) {
     const long ev = prof_begin(op, KIND_MULT_SUB32);
     SGMEV_CUDA(subspace_mult(op->sub, op->stream, op->xt32, op->mpad, op->m, a32, out32, out64,
                              j_begin, j_end, op->num_sms));
@@ -754,7 +795,7 @@ static int dev_multt(sgmev_op* op, int prec, const double* v64, const float* v32
                                      add, scale, op->num_sms));
     prof_end(op, ev);
     op->launches += 3;
-  } else if (prec == SGMEV_DF64 && op->sub_ok && subspace_owner_fits(op->sub, true)) {
+  } else if (prec == SGMEV_DF64 && op->sub_ok && !op->mod && subspace_owner_fits(op->sub, true)) {
     // the subspace sums produce every grid entry at once (the range is a subset of them)
     const long ev = prof_begin(op, KIND_MULTT_SUBDF);
     SGMEV_CUDA(subspace_multt_df(op->sub, op->stream, op->xt32, op->xt32lo, op->mpad, op->m, v32,
@@ -771,7 +812,7 @@ static int dev_multt(sgmev_op* op, int prec, const double* v64, const float* v32
                                   out64, add, scale, op->num_sms, op->use_half));
     prof_end(op, ev);
     op->launches += 3;
-  } else if (op->sub_ok) {
+  } else if (op->sub_ok && !op->mod) {
     // the subspace scatter produces every grid entry at once (the range is a subset of it)
     const long ev = prof_begin(op, KIND_MULTT_SUB32);
     SGMEV_CUDA(subspace_multt(op->sub, op->stream, op->xt32, op->mpad, op->m, v32, op->npad,
@@ -897,6 +938,10 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
     SGMEV_TRY(dalloc(op->stream, &op->li64, static_cast<size_t>(npad * op->dim)));
     SGMEV_TRY(dalloc(op->stream, &op->li32, static_cast<size_t>(npad * op->dim)));
     SGMEV_TRY(dalloc(op->stream, &op->gq, static_cast<size_t>(npad * op->dim)));
+    if (op->mod) {
+      SGMEV_TRY(dalloc(op->stream, &op->gs64, static_cast<size_t>(npad)));
+      SGMEV_TRY(dalloc(op->stream, &op->gs32, static_cast<size_t>(npad)));
+    }
     SGMEV_TRY(dalloc(op->stream, &op->a64, static_cast<size_t>(npad)));
     SGMEV_TRY(dalloc(op->stream, &op->a32, static_cast<size_t>(npad)));
     SGMEV_TRY(dalloc(op->stream, &op->a32lo, static_cast<size_t>(npad)));
@@ -919,8 +964,13 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
     cudaMemcpyAsync(d_l, level_pow2, bytes, cudaMemcpyHostToDevice, op->stream);
     cudaMemcpyAsync(d_i, index, bytes, cudaMemcpyHostToDevice, op->stream);
   }
-  stage_grid_kernel<<<vec_blocks(npad * op->dim), 256, 0, op->stream>>>(
-      d_l, d_i, n, op->dim, npad, op->li64, op->li32, op->gq);
+  if (op->mod) {
+    stage_grid_mod_kernel<<<vec_blocks(npad), 256, 0, op->stream>>>(
+        d_l, d_i, n, op->dim, npad, op->li64, op->li32, op->gq, op->gs64, op->gs32);
+  } else {
+    stage_grid_kernel<<<vec_blocks(npad * op->dim), 256, 0, op->stream>>>(
+        d_l, d_i, n, op->dim, npad, op->li64, op->li32, op->gq);
+  }
   op->launches += 1;
   e = cudaStreamSynchronize(op->stream);
   dev_free(d_l, op->stream);
@@ -935,6 +985,7 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
   if (op->algo != 0 && n > 0) {
     std::string why;
     if (subspace_build(&op->sub, op->dim, n, level_pow2, index, op->stream, &why)) {
+      op->sub.mod = op->mod;
       const double dense_cost = 3.0 * op->dim * static_cast<double>(n);
       const double sub_cost = 8.0 * static_cast<double>(op->sub.act_work) + 10.0 * op->sub.n_sub;
       op->sub_ok = op->algo == 1 || sub_cost * 1.5 < dense_cost;
@@ -964,7 +1015,7 @@ static void release(sgmev_op* op) {
   // only; frees are stream-ordered and never synchronise the device)
   if (op->stream) cudaStreamSynchronize(op->stream);
   subspace_free(&op->sub);
-  void* ptrs[] = {op->xt64, op->xt32, op->xt32lo, op->li64, op->li32, op->gq, op->a64,
+  void* ptrs[] = {op->xt64, op->xt32, op->xt32lo, op->li64, op->li32, op->gq, op->gs64, op->gs32, op->a64,
                   op->a32,  op->a32lo, op->v64,   op->v32,  op->v32lo, op->out64, op->part,
                   op->cg,   op->dot_part, op->dot_out};
   for (void* p : ptrs) dev_free(p, op->stream);
@@ -1083,6 +1134,9 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   const std::string inner_p = json_string(params_json, "inner_products");
   if (!inner_p.empty() && inner_p != "half" && inner_p != "float")
     return fail(SGMEV_ERR_INVALID, "params: inner_products must be \"half\" or \"float\"");
+  const std::string basis = json_string(params_json, "basis");
+  if (!basis.empty() && basis != "linear" && basis != "modlinear")
+    return fail(SGMEV_ERR_INVALID, "params: basis must be \"linear\" or \"modlinear\"");
   const std::string mat_t = json_string(params_json, "materialize_multt");
   if (!mat_t.empty() && mat_t != "on" && mat_t != "off")
     return fail(SGMEV_ERR_INVALID, "params: materialize_multt must be \"on\" or \"off\"");
@@ -1101,6 +1155,7 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   op->mat_mode = mat == "off" ? 0 : (mat == "on" ? 2 : 1);
   op->mat_multt = mat_t != "off";
   op->inner_half = inner_p != "float";
+  op->mod = basis == "modlinear";
   {
     const std::string it = json_string(params_json, "inner_tol");
     if (!it.empty()) {
@@ -1178,10 +1233,21 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
         d_rows, n_data, dim, op->mpad, d_bb, d_bb ? d_bb + dim : nullptr, op->xt64, op->xt32,
         op->xt32lo);
     op->launches += 1;
+    unsigned int* flag = reinterpret_cast<unsigned int*>(op->dot_out);
+    if (op->mod) {
+      // the ModLinear subspace products want the data in the cube (see mat_ready)
+      cudaMemsetAsync(flag, 0, sizeof(unsigned int), op->stream);
+      cube_check_kernel<<<vec_blocks(op->mpad * dim), 256, 0, op->stream>>>(
+          op->xt64, op->mpad * dim, flag);
+      op->launches += 1;
+      cudaMemcpyAsync(op->host_scalar, flag, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                      op->stream);
+    }
     cudaError_t e = cudaStreamSynchronize(op->stream);
     dev_free(d_rows, op->stream);
     dev_free(d_bb, op->stream);
     if (e != cudaSuccess) return bail(fail(SGMEV_ERR_CUDA, std::string("stage data: ") + cudaGetErrorString(e)));
+    if (op->mod) op->in_cube = *reinterpret_cast<const unsigned int*>(op->host_scalar) == 0;
   }
   CREATE_TRY(stage_grid(op, n_grid, level_pow2, index));
 #undef CREATE_CUDA
@@ -1462,7 +1528,14 @@ static int dev_precond(sgmev_op* op, double lm) {
   op->launches += 1;
   Plan p;
   float* part = static_cast<float*>(op->part);
-  if (op->dim <= kMaxTemplDim) {
+  if (op->mod) {
+    const bool tiled = op->dim <= kMaxTemplDim;
+    p = plan_multt<float>(op, tiled ? np / (kBlock * Blocking<float>::multt_r(op->dim))
+                                    : ceil_div(np, kBlock));
+    dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
+    mod_multt_launch<float, true>(op->dim, grid, op->stream, op->xt32, op->v32, op->mpad,
+                                  op->li32, op->gs32, np, p.chunk, 0, np, part);
+  } else if (op->dim <= kMaxTemplDim) {
     const int64_t tiles = np / (kBlock * Blocking<float>::multt_r(op->dim));
     p = plan_multt<float>(op, tiles);
     dim3 grid(static_cast<unsigned>(p.tiles), static_cast<unsigned>(p.nsplit));
@@ -1622,7 +1695,10 @@ static int fit_common(sgmev_op* op, int mode, const double* y, bool y_on_device,
       // is FP64-accurate, so the refinement still converges to the FP64 solution
       struct HalfScope {
         sgmev_op* o;
-        explicit HalfScope(sgmev_op* op_) : o(op_) { o->use_half = o->inner_half; }
+        // ModLinear products reach 2^(active dimensions): FP16 holds them up to 15
+        explicit HalfScope(sgmev_op* op_) : o(op_) {
+          o->use_half = o->inner_half && (!o->mod || o->sub.na_max <= 15);
+        }
         ~HalfScope() { o->use_half = false; }
       } half_scope(op);
       if (op->precond) {

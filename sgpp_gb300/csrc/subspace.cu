@@ -441,7 +441,8 @@ struct OwnLayout {
   using Acc = typename std::conditional<DF, float2, float>::type;
 };
 
-template <int DIM, bool DF>
+// MOD (modified linear basis, data in [0, 1]): every real point is evaluated, faces included.
+template <int DIM, bool DF, bool MOD = false>
 __device__ __forceinline__ void own_stage_tile(float* s_pt, int64_t tile,
                                                const float* __restrict__ xh_t,
                                                const float* __restrict__ xl_t, int64_t mpad,
@@ -463,7 +464,9 @@ __device__ __forceinline__ void own_stage_tile(float* s_pt, int64_t tile,
 #pragma unroll
     for (int t = 0; t < DIM; ++t) {
       const float h = row[t];
-      if constexpr (DF) {
+      if constexpr (MOD) {
+        (void)h;
+      } else if constexpr (DF) {
         const float l = row[DIM + t];
         inside = inside && (h > 0.0f || (h == 0.0f && l > 0.0f)) &&
                  (h < 1.0f || (h == 1.0f && l < 0.0f));
@@ -591,7 +594,13 @@ __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_multt_own_kernel(
 // of its basis function (renormalised: hi = the FP32 rounding of the pair) and the cell index, in
 // the layout P_hi[g][s], P_lo[g][s] (float4: points 4g .. 4g+3) and C[g][s] (a byte per point).
 // The arithmetic is the one of the float-float kernels above, so the cells follow x_hi + x_lo.
-template <int DIM>
+// MOD: the modified linear basis (LinearModifiedBasis.hpp:40-58) for data in [0, 1]. A level-1
+// factor is 1; the cell is clamped to [0, S - 1] (x = 1 lies in the last cell); in the first
+// cell of a level >= 2 the function is the falling branch 2 - 2^l x throughout, in the last cell
+// the rising branch 2^l x - 2^l + 2, elsewhere the hat. The falling branch next to x = 0 is not
+// an exact FP32 number, so its rounding error is recovered with Knuth's two-sum (TAOCP vol. 2,
+// 4.2.2) into the low part.
+template <int DIM, bool MOD>
 __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_mat_build_kernel(
     const int4* __restrict__ desc, const int4* __restrict__ sinfo, int n_sub, int s_pad,
     const float* __restrict__ xh_t, const float* __restrict__ xl_t, int64_t mpad, int64_t m,
@@ -617,7 +626,7 @@ __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_mat_build_kernel(
     }
     for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
       __syncthreads();  // the previous tile's rows are no longer read
-      own_stage_tile<DIM, true>(s_pt, tile, xh_t, xl_t, mpad, m, nullptr, nullptr);
+      own_stage_tile<DIM, true, MOD>(s_pt, tile, xh_t, xl_t, mpad, m, nullptr, nullptr);
       if (sid >= s_pad) continue;
       const int64_t at = tile * kGroupsPerTile * static_cast<int64_t>(s_pad) + sid;
       for (int g = 0; g < kGroupsPerTile; ++g) {
@@ -635,12 +644,29 @@ __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_mat_build_kernel(
               const float xh = rw[t], xl = rw[DIM + t];
               const float sl = L[t] * xl;
               const float t2 = __fmaf_rd(xh, L[t], sl);
-              const float rr = __fmaf_rd(t2, 0.5f, kMagic);
+              float rr = __fmaf_rd(t2, 0.5f, kMagic);
+              if constexpr (MOD) rr = fminf(fmaxf(rr, kMagic), kMagic + (0.5f * L[t] - 1.0f));
               const float m2k = fmaf(rr, -2.0f, kTwoMagic);
               const float a = fmaf(xh, L[t], m2k);
               const float b = fmaf(xh, -L[t], 2.0f - m2k);
-              const bool rise = fmaf(2.0f, sl, a - b) <= 0.0f;
-              const ff h{rise ? a : b, rise ? sl : -sl};
+              bool rise = fmaf(2.0f, sl, a - b) <= 0.0f;
+              ff h{rise ? a : b, rise ? sl : -sl};
+              if constexpr (MOD) {
+                const uint32_t k = __float_as_uint(rr) - kMagicBits;
+                const uint32_t last = static_cast<uint32_t>(0.5f * L[t]) - 1u;
+                if (L[t] == 2.0f) {
+                  h = ff{1.0f, 0.0f};
+                } else {
+                  if (k == 0u) rise = false;
+                  else if (k == last) rise = true;
+                  const float y = xh * L[t];  // exact
+                  const float P = rise ? y : -y, Q = rise ? m2k : 2.0f - m2k;
+                  const float hh = rise ? a : b;  // fl(P + Q)
+                  const float bb = hh - P;
+                  const float err = (P - (hh - bb)) + (Q - bb);
+                  h = ff{hh, err + (rise ? sl : -sl)};
+                }
+              }
               p = t == 0 ? h : mul_ff(p, h);
               c += __float_as_uint(rr) * st[t];
             }
@@ -672,7 +698,7 @@ cudaError_t launch_mat_build(const SubPlan& p, cudaStream_t s, const float* xh, 
                              int64_t mpad, int64_t m, int num_sms) {
   using Lay = OwnLayout<DIM, true>;
   const size_t sm = sizeof(float) * kOwnTile * Lay::W;
-  auto kern = sub_mat_build_kernel<DIM>;
+  auto kern = p.mod ? sub_mat_build_kernel<DIM, true> : sub_mat_build_kernel<DIM, false>;
   cudaError_t e = set_smem_cap(kern, sm);
   if (e != cudaSuccess) return e;
   const int64_t nt = mpad / kOwnTile;

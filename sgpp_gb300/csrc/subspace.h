@@ -58,6 +58,7 @@ struct SubPlan {
   int64_t s_pad = 0;
   int64_t mat_mpad = 0;
   cudaStream_t stream = nullptr;  // device memory of the plan is allocated and freed on it
+  bool mod = false;  // modified linear basis (ModLinear): only the materialised products support it
 };
 
 // position count up to which alpha is staged in shared memory (and the fixed-point scatter, two

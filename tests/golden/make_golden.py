@@ -16,6 +16,11 @@ from the unmodified reference sources plus oracle/ref_harness.cpp), on seeded in
   bt_linear.npz the reference's golden B^T matrices for the hat basis
                 (datadriven/datasets/BT_BBT/BT_phi_li_hut_*), reduced to the row sums and sorted
                 column sums that datadriven/tests/testBT.cpp compares, plus their data points
+  modlinear.npz ModLinear grids: the streaming layout (getLevelIndexMaskArraysForModEval),
+                mult / multTranspose of the DEFAULT (OperationMultipleEvalModLinear) and STREAMING
+                (OperationMultiEvalModMaskStreaming) operators, regression fits, and the golden
+                B^T matrices of the modified basis (BT_phi_li_ausgeklappt_*, testBT.cpp suite
+                TestOperationBTModLinear) reduced like bt_linear.npz
 """
 from __future__ import annotations
 
@@ -222,6 +227,91 @@ def make_bt(ref: Reference):
     np.savez_compressed(os.path.join(HERE, "bt_linear.npz"), **out)
 
 
+def make_modlinear(ref: Reference):
+    out = {}
+    rng = np.random.default_rng(20261204)
+    cases = [
+        ("d1_l4_m40", 1, 4, 40, 0),
+        ("d2_l5_m300", 2, 5, 300, 0),
+        ("d3_l4_m512", 3, 4, 512, 0),
+        ("d5_l4_m777", 5, 4, 777, 0),          # ragged M
+        ("d10_l3_m300", 10, 3, 300, 0),
+        ("d6_l4_ad2_m600", 6, 4, 600, 2),      # adaptive: 2 surplus-refinement rounds of 30
+        ("d4_l3_m1", 4, 3, 1, 0),              # single data point
+    ]
+    names = []
+    for name, d, l, m, rounds in cases:
+        g = ref.grid(d, l, "modlinear")
+        for _ in range(rounds):
+            g.refine_surplus(rng.standard_normal(g.size), 30, 0.0)
+        lev, idx, _ = g.points()
+        x = edge_points(rng, m, d)            # nodes on the faces 0 and 1 included
+        alpha = rng.standard_normal(g.size)
+        v = rng.standard_normal(m)
+        level, index, mask, offset = g.mask_arrays()
+        out[name + "_level"] = lev.astype(np.int8)
+        out[name + "_index"] = idx.astype(np.int16)
+        out[name + "_mask_level"] = level
+        out[name + "_mask_index"] = index
+        out[name + "_mask_bits"] = mask.view(np.uint64)
+        out[name + "_mask_offset"] = offset
+        out[name + "_x"] = x
+        out[name + "_alpha"] = alpha
+        out[name + "_v"] = v
+        out[name + "_mult_default"] = g.mult(REF_DEFAULT, x, alpha)
+        out[name + "_mult_streaming"] = g.mult(REF_STREAMING, x, alpha)
+        out[name + "_multt_default"] = g.mult_transpose(REF_DEFAULT, x, v)
+        out[name + "_multt_streaming"] = g.mult_transpose(REF_STREAMING, x, v)
+        names.append(name)
+    out["cases"] = np.array(names)
+    # points outside the cube: the STREAMING operator extrapolates the boundary-adjacent functions
+    g = ref.grid(3, 4, "modlinear")
+    lev, idx, _ = g.points()
+    x = rng.random((200, 3)) * 1.4 - 0.2
+    alpha = rng.standard_normal(g.size)
+    v = rng.standard_normal(200)
+    out["outside_level"] = lev.astype(np.int8)
+    out["outside_index"] = idx.astype(np.int16)
+    out["outside_x"] = x
+    out["outside_alpha"] = alpha
+    out["outside_v"] = v
+    out["outside_mult_streaming"] = g.mult(REF_STREAMING, x, alpha)
+    out["outside_multt_streaming"] = g.mult_transpose(REF_STREAMING, x, v)
+    # regression fits through SystemMatrixLeastSquaresIdentity (STREAMING -> ModMaskStreaming)
+    for name, d, l, m, lam in [("fit_d4_l4", 4, 4, 3000, 1e-3), ("fit_d6_l3", 6, 3, 2500, 1e-4)]:
+        g = ref.grid(d, l, "modlinear")
+        x = rng.random((m, d))
+        y = (10 * np.sin(np.pi * x[:, 0] * x[:, 1]) + 20 * (x[:, 2] - 0.5) ** 2 + 10 * x[:, 3]
+             + 0.1 * rng.standard_normal(m))
+        lev, idx, _ = g.points()
+        a, it, res = g.cg_fit(REF_STREAMING, x, y, lam, 1000, 1e-12)
+        out[name + "_level"] = lev.astype(np.int8)
+        out[name + "_index"] = idx.astype(np.int16)
+        out[name + "_x"] = x
+        out[name + "_y"] = y
+        out[name + "_lambda"] = np.float64(lam)
+        out[name + "_alpha"] = a
+        out[name + "_iterations"] = np.int64(it)
+        out[name + "_residual"] = np.float64(res)
+    # golden B^T matrices of the modified basis (testBT.cpp, TestOperationBTModLinear)
+    base = os.path.join(REF_SRC, "datadriven", "datasets", "BT_BBT")
+    for key, d, l, data_file, mat_file in [
+            ("bt_d1_l3", 1, 3, "data_dim_1_nops_8_float.arff.gz", "BT_phi_li_ausgeklappt_dim_1_nopsgrid_7_float.dat.gz"),
+            ("bt_d1_l5", 1, 5, "data_dim_1_nops_8_float.arff.gz", "BT_phi_li_ausgeklappt_dim_1_nopsgrid_31_float.dat.gz"),
+            ("bt_d3_l3", 3, 3, "data_dim_3_nops_512_float.arff.gz", "BT_phi_li_ausgeklappt_dim_3_nopsgrid_31_float.dat.gz"),
+            ("bt_d3_l4", 3, 4, "data_dim_3_nops_512_float.arff.gz", "BT_phi_li_ausgeklappt_dim_3_nopsgrid_111_float.dat.gz")]:
+        x = read_arff(os.path.join(base, data_file))
+        mat = read_matrix(os.path.join(base, mat_file))
+        g = ref.grid(d, l, "modlinear")
+        assert mat.shape == (x.shape[0], g.size), (key, mat.shape, x.shape, g.size)
+        out[key + "_x"] = x
+        out[key + "_row_sums"] = mat.sum(axis=1)
+        out[key + "_col_sums_sorted"] = np.sort(mat.sum(axis=0))
+        out[key + "_dim"] = np.int64(d)
+        out[key + "_level"] = np.int64(l)
+    np.savez_compressed(os.path.join(HERE, "modlinear.npz"), **out)
+
+
 def main():
     ref = Reference()
     ref.set_threads(os.cpu_count() or 1)
@@ -230,6 +320,7 @@ def main():
     make_multeval(ref)
     make_cgfit(ref)
     make_bt(ref)
+    make_modlinear(ref)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
