@@ -29,6 +29,11 @@ cpu_baseline  the oracle port of the reference's STREAMING FP64 path on the host
 
 --impl reference prints the same line for the reference's CPU implementation of the path
 (the oracle port: the compiled reference needs its sources, which do not travel).
+
+--basis modlinear runs the same workload on a ModLinear grid (the same points with the modified
+linear basis; the reference streams it with OperationMultiEvalModMaskStreaming), with the oracle's
+port of that operator as the CPU baseline. --count-iterations prints the plain CG iteration count
+of one fit (FP64-accurate df64 products, untimed), the figure REFERENCE_ITERATIONS holds.
 """
 from __future__ import annotations
 
@@ -125,8 +130,9 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_fit_seconds(x, grid_lp, grid_ix, cg_ops: float, threads: int):
-    """Oracle port of the reference's STREAMING FP64 path on the host cores: time one
+def cpu_fit_seconds(x, grid_lp, grid_ix, cg_ops: float, threads: int, basis: str = "linear"):
+    """Oracle port of the reference's STREAMING FP64 path on the host cores
+    (OperationMultiEvalStreaming, or OperationMultiEvalModMaskStreaming for ModLinear): time one
     B^T (B a) on CPU_SAMPLE_POINTS points, scale linearly to all points and to the number of
     operator applications one CG fit performs. Returns (seconds per fit, sample description)."""
     from oracle import Oracle
@@ -136,11 +142,20 @@ def cpu_fit_seconds(x, grid_lp, grid_ix, cg_ops: float, threads: int):
     ms = min(CPU_SAMPLE_POINTS, x.shape[0])
     st = orc.stream(x[:ms])
     a = np.random.default_rng(0).standard_normal(grid_lp.shape[0])
-    st.mult_transpose(grid_lp, grid_ix, st.mult(grid_lp, grid_ix, a))  # warm-up
+    if basis == "modlinear":
+        lev = np.rint(np.log2(grid_lp)).astype(np.int32)
+        arrays = orc.mod_arrays(lev, grid_ix.astype(np.int32))
+
+        def apply():
+            st.mult_transpose_mod(arrays, st.mult_mod(arrays, a))
+    else:
+        def apply():
+            st.mult_transpose(grid_lp, grid_ix, st.mult(grid_lp, grid_ix, a))
+    apply()  # warm-up
     ts = []
     for _ in range(3):
         t0 = time.perf_counter()
-        st.mult_transpose(grid_lp, grid_ix, st.mult(grid_lp, grid_ix, a))
+        apply()
         ts.append(time.perf_counter() - t0)
     st.close()
     t_apply = statistics.median(ts) * (x.shape[0] / ms)
@@ -156,13 +171,20 @@ def cg_operator_applications(iterations: int) -> float:
     return iterations + iterations // 50 + 0.5
 
 
-def grid_arrays():
+def grid_arrays(basis: str = "linear"):
     import sgpp_gb300 as sg
 
-    grid = sg.Grid.createLinearGrid(DIM)
+    grid = (sg.Grid.createModLinearGrid(DIM) if basis == "modlinear"
+            else sg.Grid.createLinearGrid(DIM))
     grid.getGenerator().regular(LEVEL)
     lp, ix = grid.getStorage().getLevelIndexArraysForEval()
     return grid, lp, ix
+
+
+# Plain CG iterations of one fit to relative residual 1e-8 on this seeded workload, per basis
+# (bench.py --count-iterations: SGMEV_SOLVE_PLAIN with the FP64-accurate df64 products); they
+# scale the per-application CPU timings of the reference path to one fit.
+REFERENCE_ITERATIONS = {"linear": 75, "modlinear": 768}
 
 
 def subspace_count(lp):
@@ -189,11 +211,6 @@ def hbm_peak_gbs():
         return 6800.0, "fallback 6.8 TB/s (of fallback)"
 
 
-# Iterations of the plain FP64 CG on this workload to relative residual 1e-8; used only to scale
-# per-iteration CPU timings of the reference path to one fit. Measured with the plain FP64 CUDA
-# CG (sgmev_fit, SGMEV_SOLVE_PLAIN) on this exact seeded workload; bench.py re-measures the FP32
-# CG count live and reports both.
-PLAIN_FP64_CG_ITERATIONS = None
 
 
 def run_reference(args):
@@ -202,13 +219,13 @@ def run_reference(args):
         return 0
     threads = os.cpu_count() or 1
     x, y = make_workload(args.seed)
-    _, lp, ix = grid_arrays()
-    iters = args.reference_iterations
+    _, lp, ix = grid_arrays(args.basis)
+    iters = args.reference_iterations or REFERENCE_ITERATIONS[args.basis]
     cg_ops = cg_operator_applications(iters)
     times = []
     sample = ""
     for k in range(args.warmup + args.steps):
-        t_fit, sample = cpu_fit_seconds(x, lp, ix, cg_ops, threads)
+        t_fit, sample = cpu_fit_seconds(x, lp, ix, cg_ops, threads, args.basis)
         if k >= args.warmup:
             times.append(t_fit)
     sec = statistics.median(times)
@@ -218,8 +235,9 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"regression fit, regular Linear grid d={DIM} level {LEVEL} "
-                               f"(N=13441), M={M_POINTS} Gaussian-mixture points, lambda={LAMBDA}",
+        "config": {"workload": f"regression fit, regular {grid_name(args.basis)} grid d={DIM} "
+                               f"level {LEVEL} (N=13441), M={M_POINTS} Gaussian-mixture points, "
+                               f"lambda={LAMBDA}",
                    "cg_iterations_per_fit": iters, "l2_policy": "inputs larger than L2"},
         "cpu_baseline": {"value": value, "unit": "fits/s", "cores": threads, "kind": "port",
                          "sample": sample, "host": os.uname().machine},
@@ -227,6 +245,30 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def grid_name(basis: str) -> str:
+    return "ModLinear" if basis == "modlinear" else "Linear"
+
+
+def count_iterations(args):
+    """Plain CG iterations of one fit with the FP64-accurate df64 products (untimed)."""
+    import sgpp_gb300 as sg
+
+    x, y = make_workload(args.seed)
+    grid, _, _ = grid_arrays(args.basis)
+    params = {"precision": "df64"}
+    params.update(dict(kv.split("=", 1) for kv in args.param))
+    cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                sg.OperationMultipleEvalSubType.CUDA,
+                                                parameters=params)
+    op = sg.createOperationMultipleEval(grid, x, cfg)
+    t0 = time.perf_counter()
+    _, it, res = op.fit(y, LAMBDA, 20000, args.epsilon, mode=sg.SGMEV_SOLVE_PLAIN)
+    print(json.dumps({"basis": args.basis, "plain_cg_iterations": it, "residual": res,
+                      "epsilon": args.epsilon, "seconds": time.perf_counter() - t0}), flush=True)
+    op.close()
     return 0
 
 
@@ -259,7 +301,7 @@ def run_ours(args):
         raise RuntimeError("bench.py needs a CUDA device")
 
     x, y = make_workload(args.seed + rank)
-    grid, lp, ix = grid_arrays()
+    grid, lp, ix = grid_arrays(args.basis)
     n, m = grid.getSize(), x.shape[0]
     work_per_op = FLOP_PER_PAIR_DIM * n * m * DIM
 
@@ -396,8 +438,9 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        iters_fit = args.reference_iterations
-        t_fit, sample = cpu_fit_seconds(x, lp, ix, cg_operator_applications(iters_fit), threads)
+        iters_fit = args.reference_iterations or REFERENCE_ITERATIONS[args.basis]
+        t_fit, sample = cpu_fit_seconds(x, lp, ix, cg_operator_applications(iters_fit), threads,
+                                        args.basis)
         cpu = {"value": 1.0 / t_fit, "unit": "fits/s", "cores": threads, "kind": "port",
                "sample": sample, "cg_iterations_per_fit": iters_fit,
                "host": os.uname().machine}
@@ -415,9 +458,10 @@ def run_ours(args):
         t_fp64 = e0.elapsed_time(e1) * 1e-3
     plain = None
     if t_fp64:
-        t_plain_fit = t_fp64 * cg_operator_applications(args.reference_iterations)
+        iters_plain = args.reference_iterations or REFERENCE_ITERATIONS[args.basis]
+        t_plain_fit = t_fp64 * cg_operator_applications(iters_plain)
         plain = {"fits_per_sec": 1.0 / t_plain_fit, "system_apply_ms": t_fp64 * 1e3,
-                 "cg_iterations_per_fit": args.reference_iterations,
+                 "cg_iterations_per_fit": iters_plain,
                  "speedup_mixed_vs_plain_fp64": value / world * t_plain_fit}
 
     if rank == 0:
@@ -428,9 +472,10 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
-            "config": {"workload": f"regression fit, regular Linear grid d={DIM} level {LEVEL} "
-                                   f"(N={n}), M={m} Gaussian-mixture points, lambda={LAMBDA}, "
-                                   f"mixed-precision CG to relative FP64 residual {args.epsilon}",
+            "config": {"workload": f"regression fit, regular {grid_name(args.basis)} grid "
+                                   f"d={DIM} level {LEVEL} (N={n}), M={m} Gaussian-mixture "
+                                   f"points, lambda={LAMBDA}, mixed-precision CG to relative "
+                                   f"FP64 residual {args.epsilon}",
                        "l2_policy": "inputs larger than L2: every CG system product streams "
                                     "the materialised subspace products (5.4 GB at M=2^20) from "
                                     "HBM",
@@ -461,7 +506,10 @@ def main():
     ap.add_argument("--epsilon", type=float, default=1e-8)
     ap.add_argument("--ref-epsilon", type=float, default=1e-12)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--reference-iterations", type=int, default=110)
+    ap.add_argument("--reference-iterations", type=int, default=0,
+                    help="plain CG iterations per fit for the CPU scaling (0: REFERENCE_ITERATIONS)")
+    ap.add_argument("--basis", default="linear", choices=["linear", "modlinear"])
+    ap.add_argument("--count-iterations", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-fp64-probe", type=int, default=1)
     ap.add_argument("--inner-tol", type=float, default=None,
@@ -473,6 +521,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.count_iterations:
+        return count_iterations(args)
     return run_ours(args)
 
 

@@ -12,13 +12,18 @@
 //   * getDuration() returns the device seconds of the last call;
 //   * failures throw sgpp::base::operation_exception (never exit()).
 //
-// Factory branch (DatadrivenOpFactory.cpp, inside `if (grid.getType() == base::GridType::Linear)`,
-// next to the STREAMING/OCLMP branches at :439-452):
+// Factory branches (DatadrivenOpFactory.cpp, inside `if (grid.getType() == base::GridType::Linear)`
+// next to the STREAMING/OCLMP branches at :439-452, and the same inside
+// `else if (grid.getType() == base::GridType::ModLinear)` next to :480-483):
 //
 //   if (configuration.getType() == datadriven::OperationMultipleEvalType::STREAMING &&
 //       configuration.getSubType() == datadriven::OperationMultipleEvalSubType::CUDA) {
 //     return new sgpp_gb300::OperationMultiEvalCudaLinear(grid, dataset, configuration);
 //   }
+//
+// The operator takes its basis from the grid: the hat basis for Linear grids, the modified
+// linear basis (LinearModifiedBasis.hpp:40-58, streamed by OperationMultiEvalModMaskStreaming)
+// for ModLinear grids; any other grid type throws.
 #pragma once
 
 #include <sgpp/base/datatypes/DataMatrix.hpp>
@@ -112,12 +117,22 @@ class OperationMultiEvalCudaLinear : public sgpp::base::OperationMultipleEval {
   double getDuration() override { return sgmev_get_duration(op_); }
 
   std::string getImplementationName() override {
-    return precision_ == SGMEV_FP32 ? "CUDA_LINEAR_FP32"
-                                     : (precision_ == SGMEV_DF64 ? "CUDA_LINEAR_DF64" : "CUDA_LINEAR_FP64");
+    const std::string base = modlinear() ? "CUDA_MODLINEAR_" : "CUDA_LINEAR_";
+    return base + (precision_ == SGMEV_FP32 ? "FP32" : (precision_ == SGMEV_DF64 ? "DF64" : "FP64"));
   }
 
  private:
+  bool modlinear() const { return grid.getType() == sgpp::base::GridType::ModLinear; }
+
   void create() {
+    if (grid.getType() != sgpp::base::GridType::Linear && !modlinear()) {
+      throw sgpp::base::operation_exception("OperationMultiEvalCudaLinear: Linear and ModLinear "
+                                            "grids only");
+    }
+    if (modlinear()) {
+      knobs_ = knobs_.empty() ? std::string("{\"basis\":\"modlinear\"}")
+                              : knobs_.substr(0, knobs_.size() - 1) + ",\"basis\":\"modlinear\"}";
+    }
     std::vector<double> level, index;
     export_grid(level, index);
     n_data_ = static_cast<int64_t>(dataset.getNrows());

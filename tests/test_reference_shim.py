@@ -27,6 +27,7 @@ DRIVER = r"""
 #include <sgpp/base/grid/Grid.hpp>
 #include <sgpp/base/operation/BaseOpFactory.hpp>
 #include <sgpp/datadriven/algorithm/SystemMatrixLeastSquaresIdentity.hpp>
+#include <sgpp/datadriven/operation/hash/OperationMultiEvalModMaskStreaming/OperationMultiEvalModMaskStreaming.hpp>
 #include <sgpp/datadriven/operation/hash/OperationMultiEvalStreaming/OperationMultiEvalStreaming.hpp>
 #include <sgpp/solver/sle/ConjugateGradients.hpp>
 
@@ -36,9 +37,10 @@ using sgpp::base::DataMatrix;
 using sgpp::base::DataVector;
 namespace dd = sgpp::datadriven;
 
-// The datadriven factory with the one added branch (Linear, STREAMING, CUDA); the other
-// routes are the reference's for Linear grids (DatadrivenOpFactory.cpp:436-452). Defined in the
-// executable, it takes precedence over the library's definition, as the patched factory would.
+// The datadriven factory with the two added branches ((Linear | ModLinear), STREAMING, CUDA);
+// the other routes are the reference's for these grids (DatadrivenOpFactory.cpp:436-452 and
+// :479-483). Defined in the executable, it takes precedence over the library's definition, as the
+// patched factory would.
 namespace sgpp {
 namespace op_factory {
 base::OperationMultipleEval* createOperationMultipleEval(
@@ -52,12 +54,32 @@ base::OperationMultipleEval* createOperationMultipleEval(
     if (cfg.getSubType() == dd::OperationMultipleEvalSubType::CUDA)
       return new sgpp_gb300::OperationMultiEvalCudaLinear(grid, dataset, cfg);
   }
+  if (grid.getType() == base::GridType::ModLinear &&
+      cfg.getType() == dd::OperationMultipleEvalType::STREAMING) {
+    if (cfg.getSubType() == dd::OperationMultipleEvalSubType::DEFAULT)
+      return new dd::OperationMultiEvalModMaskStreaming(grid, dataset);
+    if (cfg.getSubType() == dd::OperationMultipleEvalSubType::CUDA)
+      return new sgpp_gb300::OperationMultiEvalCudaLinear(grid, dataset, cfg);
+  }
   throw base::factory_exception("OperationMultiEval is not implemented for this grid type.");
 }
 }  // namespace op_factory
 }  // namespace sgpp
 
 int main() {
+  {
+    // a grid of another basis is refused before any device work
+    std::unique_ptr<sgpp::base::Grid> poly(sgpp::base::Grid::createPolyGrid(2, 3));
+    poly->getGenerator().regular(2);
+    DataMatrix px(4, 2);
+    try {
+      sgpp_gb300::OperationMultiEvalCudaLinear op(*poly, px);
+      std::printf("POLY_ACCEPTED\n");
+      return 4;
+    } catch (sgpp::base::operation_exception& e) {
+      std::printf("POLY_REJECTED %s\n", e.what());
+    }
+  }
   std::unique_ptr<sgpp::base::Grid> grid(sgpp::base::Grid::createLinearGrid(4));
   grid->getGenerator().regular(4);
   const size_t n = grid->getSize(), m = 2000;
@@ -111,7 +133,31 @@ int main() {
     mx = std::fmax(mx, std::fabs(ref[j]));
   }
   std::printf("MULT_REL_ERR %.3e\n", err / mx);
-  return (err / mx < 1e-12 && ea / ma < 1e-8) ? 0 : 1;
+
+  // ModLinear: the reference's streaming route (OperationMultiEvalModMaskStreaming) against the
+  // CUDA one, through the same system matrix and CG
+  std::unique_ptr<sgpp::base::Grid> mgrid(sgpp::base::Grid::createModLinearGrid(4));
+  mgrid->getGenerator().regular(4);
+  const size_t nm = mgrid->getSize();
+  dd::SystemMatrixLeastSquaresIdentity AM(*mgrid, x, 1e-3);
+  AM.setImplementation(dd::OperationMultipleEvalConfiguration(
+      dd::OperationMultipleEvalType::STREAMING, dd::OperationMultipleEvalSubType::DEFAULT));
+  DataVector bm_ref(nm), am_ref(nm), bm(nm), am(nm);
+  AM.generateb(y, bm_ref);
+  sgpp::solver::ConjugateGradients cgm_ref(2000, 1e-10);
+  cgm_ref.solve(AM, am_ref, bm_ref, false, false, 0.0);
+  AM.setImplementation(cuda_cfg);
+  AM.generateb(y, bm);
+  sgpp::solver::ConjugateGradients cgm(2000, 1e-10);
+  cgm.solve(AM, am, bm, false, false, 0.0);
+  double em = 0.0, mm = 0.0;
+  for (size_t i = 0; i < nm; ++i) {
+    em = std::fmax(em, std::fabs(am[i] - am_ref[i]));
+    mm = std::fmax(mm, std::fabs(am_ref[i]));
+  }
+  std::printf("MODLINEAR_FIT_REL_ERR %.3e iterations %zu / %zu\n", em / mm,
+              cgm.getNumberIterations(), cgm_ref.getNumberIterations());
+  return (err / mx < 1e-12 && ea / ma < 1e-8 && em / mm < 1e-8) ? 0 : 1;
 }
 """
 
@@ -135,6 +181,7 @@ def test_shim_compiles_links_and_fails_loudly_without_gpu(lib, tmp_path):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert "POLY_REJECTED" in run.stdout and "ModLinear" in run.stdout, run.stdout
     if lib.sgmev_device_count() == 0:
         assert run.returncode == 3, run.stdout + run.stderr
         assert "no CUDA device" in run.stdout
