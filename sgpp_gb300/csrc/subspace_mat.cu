@@ -13,9 +13,10 @@
 // Both kernels are owner-computes: thread k of a pass owns subspace s = pass * blockDim + k and
 // walks the CTA's tiles of points; a warp reads P[g][32 consecutive s] as 512 contiguous bytes
 // (and C as 128), through a four-deep ring of loads in registers.
-//   mult:  lane s forms alpha_s[c] * p for 4 points; a butterfly over the warp (xor 16, 8, then
-//          4, 2, 1) reduces the 4 values to 4 per-point sums, which go to per-warp partials in
-//          shared memory; after all passes the partials are added in warp order.
+//   mult:  lane s forms alpha_s[c] * p for 4 points, for subspaces s and s + 32 at once (their
+//          terms added in registers); a butterfly over the warp (xor 16, 8, then 4, 2, 1) reduces
+//          the 4 values to 4 per-point sums, which go to per-warp partials in shared memory;
+//          after all passes the partials are added in warp order.
 //   multT: lane s adds v_j * p into its cells ([cell][thread] in shared memory, conflict-free) and
 //          flushes them into the CTA's FP64 row every kFlushTiles tiles; rows are added in CTA
 //          order.
@@ -85,6 +86,21 @@ struct Prod<true> {
   }
 };
 
+// mult: a lane takes subspaces s and s + 32 of the same four points (two 32-wide blocks per
+// warp), adds their four terms in registers and then runs one butterfly, so the butterfly's
+// cost is shared by two subspaces. A warp whose second block lies beyond s_pad reads its first
+// block twice and multiplies the copy by a zero column of alpha (s_at is kMultBlock-padded).
+constexpr int kMultBlock = 64;  // subspaces per warp and pass
+template <bool HALF>
+struct Ahead2 {
+  static constexpr int value = HALF ? 4 : 2;  // the same bytes in flight as one block at Ahead
+};
+static_assert(kGroups % 4 == 0 && kGroups % 2 == 0, "the ring must divide a tile");
+
+__host__ __device__ constexpr int mult_at_pad(int s_pad) {
+  return (s_pad + kMultBlock - 1) / kMultBlock * kMultBlock;
+}
+
 template <bool HALF>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
@@ -92,14 +108,16 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
     const typename Prod<HALF>::T* __restrict__ pm, const uint32_t* __restrict__ cm,
     float* __restrict__ out32, double* __restrict__ out64) {
   using PT = typename Prod<HALF>::T;
+  constexpr int A = Ahead2<HALF>::value;
   extern __shared__ __align__(16) unsigned char smem[];
+  const int sp = mult_at_pad(s_pad);                // row length of s_at
   float* s_part = reinterpret_cast<float*>(smem);   // [warps][kOwnTile]
-  float* s_at = s_part + kMatWarps * kOwnTile;      // [cmax][s_pad] alpha by (cell, subspace)
+  float* s_at = s_part + kMatWarps * kOwnTile;      // [cmax][sp] alpha by (cell, subspace)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t cm1 = static_cast<uint32_t>(cmax - 1);
-  // alpha transposed: s_at[c * s_pad + s] = alpha at position offset_s + c (0 beyond the cells)
-  for (int k = tid; k < cmax * s_pad; k += blockDim.x) {
-    const int c = k / s_pad, sidx = k - c * s_pad;
+  // alpha transposed: s_at[c * sp + s] = alpha at position offset_s + c (0 beyond the cells and
+  // for s >= n_sub)
+  for (int k = tid; k < cmax * sp; k += blockDim.x) {
+    const int c = k / sp, sidx = k - c * sp;
     float a = 0.0f;
     if (sidx < n_sub) {
       const int4 info = sact[sidx];
@@ -111,37 +129,52 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
   __syncthreads();
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t gt = tile_begin + tile;
-    for (int s0 = 0; s0 < s_pad; s0 += blockDim.x) {
-      if (s0 + warp * 32 >= s_pad) continue;  // whole warps: s_pad is a multiple of 32
-      const int sid = s0 + tid;
+    for (int s0 = 0; s0 < s_pad; s0 += kMultBlock * kMatWarps) {
+      const int wb = s0 + warp * kMultBlock;  // first subspace of this warp's two blocks
+      if (wb >= s_pad) continue;              // whole warps: s_pad is a multiple of 32
+      const int sid = wb + lane;
+      const bool two = wb + 32 < s_pad;       // warp-uniform
       const int64_t at = gt * kGroups * static_cast<int64_t>(s_pad) + sid;
       const PT* src = pm + at;
       const uint32_t* csrc = cm + at;
+      const PT* src2 = two ? src + 32 : src;
+      const uint32_t* csrc2 = two ? csrc + 32 : csrc;
       const float* a_col = s_at + sid;
+      const float* a_col2 = a_col + 32;       // zeros when the second block is absent
       float* part = s_part + warp * kOwnTile;
       const bool first = s0 == 0;
-      PT ring[Ahead<HALF>::value];
-      uint32_t cring[Ahead<HALF>::value];
+      PT ring[A], ring2[A];
+      uint32_t cring[A], cring2[A];
 #pragma unroll
-      for (int u = 0; u < Ahead<HALF>::value; ++u) {
+      for (int u = 0; u < A; ++u) {
         ring[u] = __ldcs(src + static_cast<int64_t>(u) * s_pad);
         cring[u] = __ldcs(csrc + static_cast<int64_t>(u) * s_pad);
+        ring2[u] = __ldcs(src2 + static_cast<int64_t>(u) * s_pad);
+        cring2[u] = __ldcs(csrc2 + static_cast<int64_t>(u) * s_pad);
       }
-      for (int g0 = 0; g0 < kGroups; g0 += Ahead<HALF>::value) {
+      for (int g0 = 0; g0 < kGroups; g0 += A) {
 #pragma unroll
-        for (int u = 0; u < Ahead<HALF>::value; ++u) {
+        for (int u = 0; u < A; ++u) {
           const int g = g0 + u;
           const float4 p = Prod<HALF>::get(ring[u]);
-          const uint32_t cs = cring[u];
-          if (g + Ahead<HALF>::value < kGroups) {
-            ring[u] = __ldcs(src + (g + Ahead<HALF>::value) * s_pad);
-            cring[u] = __ldcs(csrc + (g + Ahead<HALF>::value) * s_pad);
+          const float4 q = Prod<HALF>::get(ring2[u]);
+          const uint32_t cs = cring[u], cq = cring2[u];
+          if (g + A < kGroups) {
+            const int64_t o = static_cast<int64_t>(g + A) * s_pad;
+            ring[u] = __ldcs(src + o);
+            cring[u] = __ldcs(csrc + o);
+            ring2[u] = __ldcs(src2 + o);
+            cring2[u] = __ldcs(csrc2 + o);
           }
           // cells are below cmax by construction (the build writes c < cells of s <= cmax)
-          const float v0 = a_col[(cs & 0xFFu) * s_pad] * p.x;
-          const float v1 = a_col[((cs >> 8) & 0xFFu) * s_pad] * p.y;
-          const float v2 = a_col[((cs >> 16) & 0xFFu) * s_pad] * p.z;
-          const float v3 = a_col[(cs >> 24) * s_pad] * p.w;
+          float v0 = a_col[(cs & 0xFFu) * sp] * p.x;
+          float v1 = a_col[((cs >> 8) & 0xFFu) * sp] * p.y;
+          float v2 = a_col[((cs >> 16) & 0xFFu) * sp] * p.z;
+          float v3 = a_col[(cs >> 24) * sp] * p.w;
+          v0 = fmaf(a_col2[(cq & 0xFFu) * sp], q.x, v0);
+          v1 = fmaf(a_col2[((cq >> 8) & 0xFFu) * sp], q.y, v1);
+          v2 = fmaf(a_col2[((cq >> 16) & 0xFFu) * sp], q.z, v2);
+          v3 = fmaf(a_col2[(cq >> 24) * sp], q.w, v3);
           const float r = reduce4(v0, v1, v2, v3, lane);
           if ((lane & 7) == 0) {
             float* dst = part + 4 * g + (lane >> 3);
@@ -151,8 +184,8 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
       }
     }
     __syncthreads();
-    // warp w wrote its partials in pass 0 iff w * 32 < s_pad (s_pad is a multiple of 32)
-    const int wrote = min(kMatWarps, s_pad / 32);
+    // warp w wrote its partials in pass 0 iff w * kMultBlock < s_pad
+    const int wrote = min(kMatWarps, (s_pad + kMultBlock - 1) / kMultBlock);
     for (int jj = tid; jj < kOwnTile; jj += blockDim.x) {
       float r = 0.0f;
       for (int w = 0; w < wrote; ++w) r += s_part[w * kOwnTile + jj];
@@ -576,7 +609,8 @@ size_t mat_system_smem(int cmax, int64_t s_pad) {
 int mat_threads(int64_t s_pad) { return static_cast<int>(std::min<int64_t>(kMatThreads, s_pad)); }
 
 size_t mat_mult_smem(int cmax, int64_t s_pad) {
-  return sizeof(float) * kMatWarps * kOwnTile + sizeof(float) * static_cast<size_t>(cmax) * s_pad;
+  return sizeof(float) * kMatWarps * kOwnTile +
+         sizeof(float) * static_cast<size_t>(cmax) * mult_at_pad(static_cast<int>(s_pad));
 }
 
 size_t mat_multt_smem(int cmax, int64_t s_pad) {
