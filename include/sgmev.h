@@ -277,6 +277,32 @@ SGMEV_API int sgmev_batch_info(sgmev_batch* b, int64_t* steps, int64_t* launches
                                int* free_slots);
 
 /* ---- sparse-grid construction on the host (native C++) --------------------------------- */
+/* ---- dataset ingest (host) ----------------------------------------------------------------
+ * ARFF and CSV text read exactly as the reference's readers read it
+ *   datadriven/src/sgpp/datadriven/tools/ARFFTools.cpp  readARFFSize / readARFF (:60-170)
+ *   datadriven/src/sgpp/datadriven/tools/CSVTools.cpp   readCSVSize / readCSV
+ * (the rules are listed in sgpp_gb300/csrc/datasets.cpp). The text is passed as bytes; the
+ * library opens no files. The rows go to sgmev_create as they are (with the grid's bounding box,
+ * if any, applied there on the device).
+ */
+#define SGDATA_ARFF 0
+#define SGDATA_CSV 1
+
+/* Number of admissible instances and the dimension (columns, less the target column when
+ * has_targets); replaces ARFFTools::readARFFSize / CSVTools::readCSVSize. skip_first_line: CSV
+ * only (a header line). targets/n_targets: optional target filter (0.001 tolerance). */
+SGMEV_API int sgdata_size(int format, const char* text, int64_t len, int has_targets,
+                          int skip_first_line, const double* targets, int n_targets,
+                          int64_t* n_instances, int64_t* dim);
+
+/* Read the rows: data [n_read x dim_out] row-major, y [n_read] (when has_targets); replaces
+ * ARFFTools::readARFF / CSVTools::readCSV. cutoff < 0: no instance cutoff. cols/n_cols: optional
+ * column selection (order kept). n_cap: rows the caller's buffers hold (sgdata_size's count). */
+SGMEV_API int sgdata_read(int format, const char* text, int64_t len, int has_targets,
+                          int skip_first_line, int64_t cutoff, const int64_t* cols, int n_cols,
+                          const double* targets, int n_targets, double* data, double* y,
+                          int64_t n_cap, int64_t* n_read, int64_t* dim_out);
+
 /*
  * Regular Linear sparse grid without boundary in the reference's storage order; replaces
  *   Grid::createLinearGrid(d)->getGenerator().regular(level)

@@ -301,10 +301,33 @@ class Reference:
                                  _vp, ctypes.POINTER(_c_i64), ctypes.POINTER(_c_dbl)]
         L.ref_max_threads.restype = _c_int
         L.ref_set_threads.argtypes = [_c_int]
+        L.ref_read_dataset.argtypes = [_c_int, ctypes.c_char_p, _c_i64, _c_int, _c_int, _c_i64,
+                                       _vp, _c_int, _vp, _c_int, _vp, _vp, _c_i64, _c_i64,
+                                       ctypes.POINTER(_c_i64), ctypes.POINTER(_c_i64)]
+
+    def read_dataset(self, fmt: int, text: bytes, has_targets=True, skip_first=False, cutoff=-1,
+                     cols=None, targets=None, n_cap=1 << 16, dim_cap=64):
+        """The reference's ARFFTools::readARFF (fmt 0) / CSVTools::readCSV (fmt 1) on `text`:
+        (data, y) or raises RuntimeError with the reference's message."""
+        c = np.ascontiguousarray(cols or [], np.int64)
+        t = np.ascontiguousarray(targets or [], np.float64)
+        data = np.zeros((n_cap, dim_cap))
+        y = np.zeros(n_cap)
+        n = _c_i64(0)
+        d = _c_i64(0)
+        self._check(self.lib.ref_read_dataset(fmt, text, len(text), int(has_targets),
+                                              int(skip_first), int(cutoff),
+                                              _ptr(c) if c.size else None, int(c.size),
+                                              _ptr(t) if t.size else None, int(t.size),
+                                              _ptr(data), _ptr(y), n_cap, dim_cap,
+                                              ctypes.byref(n), ctypes.byref(d)))
+        nn, dd = int(n.value), int(d.value)
+        assert nn <= n_cap and dd <= dim_cap
+        return data[:nn, :dd].copy(), y[:nn].copy()
 
     def _check(self, rc):
         if rc != 0:
-            raise RuntimeError(self.lib.ref_last_error().decode())
+            raise RuntimeError(self.lib.ref_last_error().decode(errors="replace"))
 
     def grid(self, dim: int, level: int | None = None, basis: str = "linear"):
         return RefGrid(self, dim, level, basis)

@@ -6,8 +6,8 @@
 #   make -f oracle/ref.mk -j8 REF=/path/to/reference
 #
 # Sources: every base/src translation unit except the OpenCL manager (no OpenCL headers
-# exist here), solver/src, the STREAMING operators of the Linear and ModLinear bases and the
-# two system-matrix files.
+# exist here), solver/src, the STREAMING operators of the Linear and ModLinear bases, the two
+# system-matrix files and the ARFF/CSV readers.
 # Quirks needed with g++ 13: -include cstdint -include memory (missing includes in the
 # reference headers, e.g. base/src/sgpp/base/grid/storage/hashmap/HashGridPoint.hpp).
 
@@ -36,6 +36,7 @@ DD_SRCS := $(DD)/operation/hash/OperationMultiEvalStreaming/OperationMultiEvalSt
            $(DD)/operation/hash/OperationMultiEvalModMaskStreaming/OperationMultiEvalModMaskStreaming.cpp \
            $(DD)/operation/hash/OperationMultiEvalModMaskStreaming/OperationMultiEvalModMaskStreaming_multImpl.cpp \
            $(DD)/operation/hash/OperationMultiEvalModMaskStreaming/OperationMultiEvalModMaskStreaming_multTransposeImpl.cpp \
+           $(DD)/tools/ARFFTools.cpp $(DD)/tools/CSVTools.cpp $(DD)/tools/Dataset.cpp \
            $(DD)/algorithm/SystemMatrixLeastSquaresIdentity.cpp \
            $(DD)/algorithm/DMSystemMatrixBase.cpp
 

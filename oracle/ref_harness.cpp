@@ -20,6 +20,8 @@
 //                                                       datadriven/.../OperationMultiEvalModMaskStreaming.cpp
 //             HashGridStorage::getLevelIndexMaskArraysForModEval
 //                                                       base/.../HashGridStorage.cpp:519-559
+//   datasets  ARFFTools::readARFF, CSVTools::readCSV (on a string stream)
+//                                                       datadriven/.../tools/ARFFTools.cpp, CSVTools.cpp
 //   CG fit    SystemMatrixLeastSquaresIdentity + solver::ConjugateGradients
 //                                                       datadriven/.../SystemMatrixLeastSquaresIdentity.cpp
 //                                                       solver/src/sgpp/solver/sle/ConjugateGradients.cpp
@@ -42,6 +44,8 @@
 #include <sgpp/base/tools/GaussLegendreQuadRule1D.hpp>
 #include <sgpp/datadriven/algorithm/SystemMatrixLeastSquaresIdentity.hpp>
 #include <sgpp/datadriven/operation/hash/DatadrivenOperationCommon.hpp>
+#include <sgpp/datadriven/tools/ARFFTools.hpp>
+#include <sgpp/datadriven/tools/CSVTools.hpp>
 #include <sgpp/datadriven/operation/hash/OperationMultiEvalModMaskStreaming/OperationMultiEvalModMaskStreaming.hpp>
 #include <sgpp/datadriven/operation/hash/OperationMultiEvalStreaming/OperationMultiEvalStreaming.hpp>
 #include <sgpp/solver/sle/ConjugateGradients.hpp>
@@ -54,6 +58,7 @@
 #include <cstring>
 #include <exception>
 #include <memory>
+#include <sstream>
 #include <string>
 
 // The reference snapshot ships GaussLegendreQuadRule1D.hpp without its .cpp. Linear-grid code
@@ -332,6 +337,33 @@ int ref_streaming_time(void* h, const double* data, int64_t m, const double* alp
       mult_seconds[k] = op->getDuration();
       op->multTranspose(s, r2);
       multt_seconds[k] = op->getDuration();
+    }
+  });
+}
+
+// A data set through the reference's readers: format 0 = ARFF, 1 = CSV. Writes at most
+// n_cap rows of data (row-major, dim_cap columns) and targets; *n / *d get the Dataset's sizes.
+int ref_read_dataset(int format, const char* text, int64_t len, int has_targets, int skip_first,
+                     int64_t cutoff, const int64_t* cols, int n_cols, const double* targets,
+                     int n_targets, double* data, double* y, int64_t n_cap, int64_t dim_cap,
+                     int64_t* n, int64_t* d) {
+  return guarded([&] {
+    const std::string content(text, static_cast<size_t>(len));
+    std::vector<size_t> sel;
+    for (int k = 0; k < n_cols; ++k) sel.push_back(static_cast<size_t>(cols[k]));
+    std::vector<double> tg(targets, targets + n_targets);
+    const size_t cut = cutoff < 0 ? static_cast<size_t>(-1) : static_cast<size_t>(cutoff);
+    std::istringstream stream(content);
+    sgpp::datadriven::Dataset ds =
+        format == 0 ? sgpp::datadriven::ARFFTools::readARFF(stream, has_targets != 0, cut, sel, tg)
+                    : sgpp::datadriven::CSVTools::readCSV(stream, skip_first != 0,
+                                                          has_targets != 0, cut, sel, tg);
+    *n = static_cast<int64_t>(ds.getNumberInstances());
+    *d = static_cast<int64_t>(ds.getDimension());
+    for (int64_t i = 0; i < *n && i < n_cap; ++i) {
+      for (int64_t t = 0; t < *d && t < dim_cap; ++t)
+        data[i * dim_cap + t] = ds.getData().get(static_cast<size_t>(i), static_cast<size_t>(t));
+      if (has_targets) y[i] = ds.getTargets()[static_cast<size_t>(i)];
     }
   });
 }

@@ -102,6 +102,10 @@ class NotImplementedException(SGppException):
     """not_implemented_exception"""
 
 
+class FileException(SGppException):
+    """base::file_exception: unreadable or malformed dataset text."""
+
+
 class GenerationException(SGppException):
     """generation_exception"""
 
@@ -165,6 +169,9 @@ def load_library(path: str = LIBRARY_PATH):
         "sgmev_batch_info": (c_int, [vp, pi64, pi64, ctypes.POINTER(c_int)]),
         "sgmev_profile": (c_int, [vp, c_int]),
         "sgmev_profile_read": (c_int, [vp, c_int, pi64, pdbl]),
+        "sgdata_size": (c_int, [c_int, ctypes.c_char_p, i64, c_int, c_int, vp, c_int, pi64, pi64]),
+        "sgdata_read": (c_int, [c_int, ctypes.c_char_p, i64, c_int, c_int, i64, vp, c_int, vp,
+                                c_int, vp, vp, i64, pi64, pi64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -859,3 +866,133 @@ __all__ = [
     "SGMEV_FP32", "SGMEV_DF64", "SGMEV_SOLVE_PLAIN", "SGMEV_SOLVE_MIXED",
     "SGMEV_SOLVE_MIXED_NATIVE64",
 ]
+
+
+# ---- datasets (datadriven/src/sgpp/datadriven/tools/{Dataset,ARFFTools,CSVTools}.cpp) ------
+SGDATA_ARFF, SGDATA_CSV = 0, 1
+
+
+class Dataset:
+    """Data matrix [instances x dimension] and targets (datadriven/.../tools/Dataset.hpp)."""
+
+    def __init__(self, data=None, targets=None):
+        self._data = np.zeros((0, 0)) if data is None else np.ascontiguousarray(data, np.float64)
+        n = self._data.shape[0]
+        self._targets = (np.zeros(n) if targets is None
+                         else np.ascontiguousarray(targets, np.float64))
+
+    def getData(self) -> np.ndarray:
+        return self._data
+
+    def getTargets(self) -> np.ndarray:
+        return self._targets
+
+    def getNumberInstances(self) -> int:
+        return int(self._data.shape[0])
+
+    def getDimension(self) -> int:
+        return int(self._data.shape[1]) if self._data.ndim == 2 else 0
+
+
+def _text_bytes(content) -> bytes:
+    return content.encode() if isinstance(content, str) else bytes(content)
+
+
+def _file_bytes(filename: str) -> bytes:
+    """A dataset file's bytes (gzip-compressed files, *.gz, are expanded)."""
+    import gzip
+    try:
+        if filename.endswith(".gz"):
+            with gzip.open(filename, "rb") as f:
+                return f.read()
+        with open(filename, "rb") as f:
+            return f.read()
+    except OSError as e:
+        raise FileException(f"Unable to open file: {filename} ({e})") from e
+
+
+def _data_size(fmt, text: bytes, has_targets, skip_first, targets):
+    t = np.ascontiguousarray(targets if targets is not None else [], np.float64)
+    n = ctypes.c_int64(0)
+    d = ctypes.c_int64(0)
+    _check(load_library().sgdata_size(fmt, text, len(text), int(bool(has_targets)),
+                                      int(bool(skip_first)), _vp(t) if t.size else None,
+                                      int(t.size), ctypes.byref(n), ctypes.byref(d)),
+           FileException)
+    return int(n.value), int(d.value)
+
+
+def _data_read(fmt, text: bytes, has_targets, skip_first, cutoff, cols, targets) -> Dataset:
+    n, dim = _data_size(fmt, text, has_targets, skip_first, targets)
+    c = np.ascontiguousarray(cols if cols else [], np.int64)
+    t = np.ascontiguousarray(targets if targets is not None else [], np.float64)
+    ncap = n if cutoff is None or cutoff < 0 else min(n, int(cutoff))
+    width = c.size if c.size else dim
+    data = np.zeros((max(ncap, 1), max(width, 1)))
+    y = np.zeros(max(ncap, 1))
+    nr = ctypes.c_int64(0)
+    dout = ctypes.c_int64(0)
+    _check(load_library().sgdata_read(fmt, text, len(text), int(bool(has_targets)),
+                                      int(bool(skip_first)),
+                                      -1 if cutoff is None or cutoff < 0 else int(cutoff),
+                                      _vp(c) if c.size else None, int(c.size),
+                                      _vp(t) if t.size else None, int(t.size), _vp(data), _vp(y),
+                                      int(ncap), ctypes.byref(nr), ctypes.byref(dout)),
+           FileException)
+    rows = int(nr.value)
+    return Dataset(data[:rows, :int(dout.value)].copy(),
+                   y[:rows].copy() if has_targets else np.zeros(rows))
+
+
+class ARFFTools:
+    """ARFF reading as datadriven/.../tools/ARFFTools.cpp (sgdata_* in the library)."""
+
+    @staticmethod
+    def readARFFSizeFromString(content, hasTargets: bool = True, selectedTargets=None):
+        return _data_size(SGDATA_ARFF, _text_bytes(content), hasTargets, False, selectedTargets)
+
+    @staticmethod
+    def readARFFSizeFromFile(filename: str, hasTargets: bool = True, selectedTargets=None):
+        return _data_size(SGDATA_ARFF, _file_bytes(filename), hasTargets, False, selectedTargets)
+
+    @staticmethod
+    def readARFFFromString(content, hasTargets: bool = True, instanceCutoff: int = -1,
+                           selectedCols=None, selectedTargets=None) -> Dataset:
+        return _data_read(SGDATA_ARFF, _text_bytes(content), hasTargets, False, instanceCutoff,
+                          selectedCols, selectedTargets)
+
+    @staticmethod
+    def readARFFFromFile(filename: str, hasTargets: bool = True, instanceCutoff: int = -1,
+                         selectedCols=None, selectedTargets=None) -> Dataset:
+        return _data_read(SGDATA_ARFF, _file_bytes(filename), hasTargets, False, instanceCutoff,
+                          selectedCols, selectedTargets)
+
+
+class CSVTools:
+    """CSV reading as datadriven/.../tools/CSVTools.cpp (sgdata_* in the library)."""
+
+    @staticmethod
+    def readCSVSizeFromString(content, skipFirstLine: bool = False, hasTargets: bool = True,
+                              selectedTargets=None):
+        return _data_size(SGDATA_CSV, _text_bytes(content), hasTargets, skipFirstLine,
+                          selectedTargets)
+
+    @staticmethod
+    def readCSVSizeFromFile(filename: str, skipFirstLine: bool = False, hasTargets: bool = True,
+                            selectedTargets=None):
+        return _data_size(SGDATA_CSV, _file_bytes(filename), hasTargets, skipFirstLine,
+                          selectedTargets)
+
+    @staticmethod
+    def readCSVFromString(content, skipFirstLine: bool = False, hasTargets: bool = True,
+                          instanceCutoff: int = -1, selectedCols=None,
+                          selectedTargets=None) -> Dataset:
+        return _data_read(SGDATA_CSV, _text_bytes(content), hasTargets, skipFirstLine,
+                          instanceCutoff, selectedCols, selectedTargets)
+
+    @staticmethod
+    def readCSVFromFile(filename: str, skipFirstLine: bool = False, hasTargets: bool = True,
+                        instanceCutoff: int = -1, selectedCols=None,
+                        selectedTargets=None) -> Dataset:
+        return _data_read(SGDATA_CSV, _file_bytes(filename), hasTargets, skipFirstLine,
+                          instanceCutoff, selectedCols, selectedTargets)

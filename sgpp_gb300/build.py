@@ -27,7 +27,7 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall",
 
 CU_SOURCES = ["sgmev.cu", "dense_mod.cu", "peak.cu", "noalloc.cu", "batch.cu", "subspace.cu",
               "subspace_mat.cu", "devmem.cu"]
-CPP_SOURCES = ["grid.cpp"]
+CPP_SOURCES = ["grid.cpp", "datasets.cpp"]
 
 
 def _nvcc() -> str:

@@ -16,6 +16,11 @@ from the unmodified reference sources plus oracle/ref_harness.cpp), on seeded in
   bt_linear.npz the reference's golden B^T matrices for the hat basis
                 (datadriven/datasets/BT_BBT/BT_phi_li_hut_*), reduced to the row sums and sorted
                 column sums that datadriven/tests/testBT.cpp compares, plus their data points
+  datasets.npz  ARFF / CSV text through the reference's ARFFTools::readARFF and CSVTools::readCSV:
+                seeded synthetic texts (written by this script) under every reading option, the
+                reference's own reader fixtures datadriven/datasets/dataread/simple.{arff,csv}
+                (their SHA-256 and parsed outputs only, for the cases test_readARFF.cpp and
+                test_readCSV.cpp check), and a regression data set as ARFF text
   modlinear.npz ModLinear grids: the streaming layout (getLevelIndexMaskArraysForModEval),
                 mult / multTranspose of the DEFAULT (OperationMultipleEvalModLinear) and STREAMING
                 (OperationMultiEvalModMaskStreaming) operators, regression fits, and the golden
@@ -312,6 +317,107 @@ def make_modlinear(ref: Reference):
     np.savez_compressed(os.path.join(HERE, "modlinear.npz"), **out)
 
 
+def synthetic_texts(rng):
+    """Seeded ARFF / CSV texts that exercise the readers' rules (this script's own inputs)."""
+    def num(v, style):
+        return {0: f"{v:.6f}", 1: f"{v:.3e}", 2: f" {v:g} ", 3: f"{v:.17g}", 4: f"{int(round(v))}"}[style]
+
+    texts = []
+    for k in range(12):
+        rows, cols = int(rng.integers(1, 9)), int(rng.integers(1, 6))
+        vals = rng.standard_normal((rows, cols)) * 10.0 ** int(rng.integers(-3, 4))
+        targets = rng.choice([0.0, 1.0, 7.0, 42.42, -5.0], size=rows)
+        lines = []
+        arff = k % 2 == 0
+        if arff:
+            lines += ["% generated", "@RELATION synthetic"]
+            lines += [f"@ATTRIBUTE x{t} NUMERIC" for t in range(cols)] + ["@ATTRIBUTE y NUMERIC", "",
+                                                                          "@DATA"]
+        elif k % 4 == 1:
+            lines.append(",".join(f"h{t}" for t in range(cols + 1)))
+        for r in range(rows):
+            style = int(rng.integers(0, 5))
+            lines.append(",".join(num(v, style) for v in vals[r]) + "," + num(targets[r], 0))
+            if rng.random() < 0.2:
+                lines.append("")
+            if arff and rng.random() < 0.2:
+                lines.append("% a comment line")
+        sep = "\r\n" if k % 3 == 2 else "\n"
+        text = sep.join(lines) + (sep if k % 5 != 4 else "")
+        texts.append((("arff" if arff else "csv"), text, k % 4 == 1))
+    # rules at the edges
+    texts.append(("arff", "1\n2,3\n4,5\n", False))               # first data line without commas
+    texts.append(("arff", "1,2,3\n1,2\n", False))                  # ragged line: an error
+    texts.append(("arff", "@DATA\n0.5,0.25,1\n\n0.75,,2\n", False))  # an empty field
+    texts.append(("csv", "\nx,y,t\n1,2,3\n4,5,6\n", True))         # empty first line + header
+    texts.append(("csv", "1,2,3", False))                             # no trailing newline
+    texts.append(("arff", "", False))                                 # empty text
+    return texts
+
+
+# (has_targets, cutoff, cols, targets). A cutoff of 0 is left out: the reference then writes row
+# 0 of an empty matrix (ARFFTools.cpp readARFF, CSVTools.cpp readCSV) and crashes.
+OPTIONS = [
+    (True, -1, None, None), (False, -1, None, None), (True, 2, None, None),
+    (True, -1, [1, 0], None), (True, -1, None, [7.0, 42.42]),
+]
+
+
+def make_datasets(ref: Reference):
+    out = {}
+    rng = np.random.default_rng(20261205)
+    texts = synthetic_texts(rng)
+    keys = []
+    for i, (fmt, text, header) in enumerate(texts):
+        out[f"t{i}_text"] = np.array(text)
+        out[f"t{i}_format"] = np.int64(0 if fmt == "arff" else 1)
+        out[f"t{i}_header"] = np.int64(int(header))
+        for j, (ht, cut, cols, tg) in enumerate(OPTIONS):
+            key = f"t{i}_o{j}"
+            try:
+                data, y = ref.read_dataset(0 if fmt == "arff" else 1, text.encode(), ht, header,
+                                           cut, cols, tg)
+                out[key + "_data"] = data
+                out[key + "_y"] = y
+                out[key + "_error"] = np.array("")
+            except RuntimeError:
+                # the reference's file_exception keeps a pointer into a freed string, so only
+                # the failure itself is recorded
+                out[key + "_error"] = np.array("error")
+            keys.append(key)
+    out["cases"] = np.array(keys)
+    out["options"] = np.array([json_opt(o) for o in OPTIONS])
+    # the reference's own reader fixtures, as test_readARFF.cpp / test_readCSV.cpp read them
+    base = os.path.join(REF_SRC, "datadriven", "datasets", "dataread")
+    for fmt, name in ((0, "simple.arff"), (1, "simple.csv")):
+        raw = open(os.path.join(base, name), "rb").read()
+        tag = name.replace(".", "_")
+        out[tag + "_sha256"] = np.array(hashlib.sha256(raw).hexdigest())
+        for j, (ht, cut, cols, tg) in enumerate([(True, -1, None, None), (False, -1, None, None),
+                                                 (True, 2, None, None), (True, -1, [4, 2, 0], None),
+                                                 (True, -1, None, [7.0, 42.42])]):
+            data, y = ref.read_dataset(fmt, raw, ht, fmt == 1, cut, cols, tg)
+            out[f"{tag}_c{j}_data"] = data
+            out[f"{tag}_c{j}_y"] = y
+    # a regression data set as ARFF text, for the end-to-end fit (read -> device -> fit)
+    x = rng.random((1500, 4)) * 2.0 - 0.5       # outside the unit cube: a bounding box maps it
+    y = np.sin(2 * x[:, 0]) + x[:, 1] * x[:, 2] - 0.5 * x[:, 3] + 0.01 * rng.standard_normal(1500)
+    lines = ["@RELATION regression", *[f"@ATTRIBUTE x{t} NUMERIC" for t in range(4)],
+             "@ATTRIBUTE y NUMERIC", "@DATA"]
+    lines += [",".join(f"{v:.17g}" for v in row) + f",{t:.17g}" for row, t in zip(x, y)]
+    text = "\n".join(lines) + "\n"
+    data, yy = ref.read_dataset(0, text.encode(), True, False, -1, None, None, n_cap=2000, dim_cap=8)
+    out["fit_text"] = np.array(text)
+    out["fit_data"] = data
+    out["fit_y"] = yy
+    np.savez_compressed(os.path.join(HERE, "datasets.npz"), **out)
+
+
+def json_opt(o):
+    import json
+    return json.dumps({"has_targets": o[0], "cutoff": o[1], "cols": o[2], "targets": o[3]})
+
+
 def main():
     ref = Reference()
     ref.set_threads(os.cpu_count() or 1)
@@ -321,6 +427,7 @@ def main():
     make_cgfit(ref)
     make_bt(ref)
     make_modlinear(ref)
+    make_datasets(ref)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
