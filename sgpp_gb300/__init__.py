@@ -63,7 +63,7 @@ EXPORTED_SYMBOLS = (
     "sgmev_profile_read", "sgmev_fit_device", "sgmev_mult_transpose_noalloc",
     "sgmev_batch_create", "sgmev_batch_destroy", "sgmev_batch_footprint", "sgmev_batch_add",
     "sgmev_batch_remove", "sgmev_batch_step", "sgmev_batch_solve", "sgmev_batch_result",
-    "sgmev_batch_info",
+    "sgmev_batch_info", "sgdata_size", "sgdata_read",
 )
 
 SGMEV_KERNEL_MULT_FP32 = 0
@@ -864,7 +864,8 @@ __all__ = [
     "ConjugateGradients", "BatchEngine", "OperationException", "FactoryException", "NotImplementedException",
     "GenerationException", "load_library", "device_count", "EXPORTED_SYMBOLS", "SGMEV_FP64",
     "SGMEV_FP32", "SGMEV_DF64", "SGMEV_SOLVE_PLAIN", "SGMEV_SOLVE_MIXED",
-    "SGMEV_SOLVE_MIXED_NATIVE64",
+    "SGMEV_SOLVE_MIXED_NATIVE64", "Dataset", "ARFFTools", "CSVTools", "FileException",
+    "SGDATA_ARFF", "SGDATA_CSV",
 ]
 
 
