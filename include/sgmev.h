@@ -277,6 +277,53 @@ SGMEV_API int sgmev_batch_info(sgmev_batch* b, int64_t* steps, int64_t* launches
                                int* free_slots);
 
 /* ---- sparse-grid construction on the host (native C++) --------------------------------- */
+/* ---- least-squares fitting with spatial adaptivity -----------------------------------------
+ * The reference's ModelFittingLeastSquares
+ *   datadriven/src/sgpp/datadriven/datamining/modules/fitting/ModelFittingLeastSquares.cpp:51-140
+ * (fit / adapt / update / evaluate) over one device-resident operator: the data stay on the GPU
+ * from fit() on, adapt() refines the grid on the host (SurplusRefinementFunctor), re-stages it
+ * and solves again from the zero-extended alpha, which never leaves the device except for the
+ * refinement functor. Solves are CG with reuse, as assembleSystemAndSolve does.
+ */
+typedef struct sgfit sgfit;
+typedef struct {
+  int level;                      /* regular grid level (RegularGridConfiguration::level_) */
+  int basis;                      /* 0 Linear, 1 ModLinear (RegularGridConfiguration::type_) */
+  double lambda;                  /* RegularizationConfiguration::lambda_ */
+  double final_eps;               /* solverFinalConfig eps_ / maxIterations_ */
+  int64_t final_max_iterations;
+  double refine_eps;              /* solverRefineConfig eps_ / maxIterations_ */
+  int64_t refine_max_iterations;
+  int64_t num_refinements;        /* AdaptivityConfiguration::numRefinements_ */
+  int64_t num_refinement_points;  /* numRefinementPoints_ */
+  double refinement_threshold;    /* refinementThreshold_ */
+  int mode;                       /* SGMEV_SOLVE_PLAIN (the reference's CG) or a mixed mode */
+  int precision;                  /* operator precision: SGMEV_FP64, SGMEV_FP32, SGMEV_DF64 */
+} sgfit_config;
+
+/* The reference's defaults (FitterConfiguration::setupDefaults): level 3, Linear, lambda 0.01,
+ * eps 1e-12 and 100 iterations for both solver configurations, one refinement of one point. */
+SGMEV_API void sgfit_config_defaults(sgfit_config* config);
+/* params_json: optional operator knobs as for sgmev_create ("basis" is set from the config). */
+SGMEV_API int sgfit_create(sgfit** out, const sgfit_config* config, const char* params_json);
+SGMEV_API int sgfit_destroy(sgfit* fitter);
+/* ModelFittingLeastSquares::fit: regular grid on `dim` dimensions, alpha = 0, solve.
+ * x: [m x dim] row-major, y: [m]. */
+SGMEV_API int sgfit_fit(sgfit* fitter, int64_t m, int dim, const double* x, const double* y);
+/* ModelFittingLeastSquares::adapt: *refined = 1 when the grid grew and was solved again. */
+SGMEV_API int sgfit_adapt(sgfit* fitter, int* refined);
+/* ModelFittingLeastSquares::update: the current grid and alpha on new data (fit() if none). */
+SGMEV_API int sgfit_update(sgfit* fitter, int64_t m, int dim, const double* x, const double* y);
+/* ModelFittingLeastSquares::evaluate(samples, results): out[m] = B(x) alpha. */
+SGMEV_API int sgfit_evaluate(sgfit* fitter, int64_t m, const double* x, double* out);
+/* The grid (level/index [n x dim] raw int32, NULL to get the sizes) and alpha [n]. */
+SGMEV_API int sgfit_grid(const sgfit* fitter, int* dim, int64_t* n_grid, int32_t* level,
+                         int32_t* index);
+SGMEV_API int sgfit_alpha(const sgfit* fitter, double* alpha);
+/* CG iterations and residual of the last solve, refinement rounds done. */
+SGMEV_API int sgfit_stats(const sgfit* fitter, int64_t* iterations, double* residual,
+                          int64_t* refinements);
+
 /* ---- dataset ingest (host) ----------------------------------------------------------------
  * ARFF and CSV text read exactly as the reference's readers read it
  *   datadriven/src/sgpp/datadriven/tools/ARFFTools.cpp  readARFFSize / readARFF (:60-170)

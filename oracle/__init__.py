@@ -301,9 +301,33 @@ class Reference:
                                  _vp, ctypes.POINTER(_c_i64), ctypes.POINTER(_c_dbl)]
         L.ref_max_threads.restype = _c_int
         L.ref_set_threads.argtypes = [_c_int]
+        L.ref_fit_adapt.argtypes = [_c_int, _c_int, _c_int, _vp, _c_i64, _vp, _c_dbl, _c_dbl,
+                                    _c_i64, _c_dbl, _c_i64, _c_i64, _c_i64, _c_dbl, _c_i64, _vp,
+                                    _vp, _vp, ctypes.POINTER(_c_i64), _vp]
         L.ref_read_dataset.argtypes = [_c_int, ctypes.c_char_p, _c_i64, _c_int, _c_int, _c_i64,
                                        _vp, _c_int, _vp, _c_int, _vp, _vp, _c_i64, _c_i64,
                                        ctypes.POINTER(_c_i64), ctypes.POINTER(_c_i64)]
+
+    def fit_adapt(self, basis: int, x, y, level: int, lam: float, final_eps: float,
+                  final_maxit: int, refine_eps: float, refine_maxit: int, rounds: int,
+                  points: int, threshold: float = 0.0, cap: int = 100000):
+        """ModelFittingLeastSquares::fit + adapt() rounds through the reference's classes:
+        (level [n x d], index [n x d], alpha [n], CG iterations per solve)."""
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.ascontiguousarray(y, np.float64)
+        m, d = x.shape
+        lev = np.zeros((cap, d), np.int32)
+        idx = np.zeros((cap, d), np.int32)
+        alpha = np.zeros(cap)
+        n = _c_i64(0)
+        iters = np.zeros(rounds + 1, np.int64)
+        self._check(self.lib.ref_fit_adapt(basis, d, level, _ptr(x), m, _ptr(y), float(lam),
+                                           float(final_eps), int(final_maxit), float(refine_eps),
+                                           int(refine_maxit), int(rounds), int(points),
+                                           float(threshold), cap, _ptr(lev), _ptr(idx),
+                                           _ptr(alpha), ctypes.byref(n), _ptr(iters)))
+        k = int(n.value)
+        return lev[:k].copy(), idx[:k].copy(), alpha[:k].copy(), iters
 
     def read_dataset(self, fmt: int, text: bytes, has_targets=True, skip_first=False, cutoff=-1,
                      cols=None, targets=None, n_cap=1 << 16, dim_cap=64):

@@ -341,6 +341,61 @@ int ref_streaming_time(void* h, const double* data, int64_t m, const double* alp
   });
 }
 
+// ModelFittingLeastSquares::fit followed by up to `rounds` adapt() calls
+// (datadriven/.../fitting/ModelFittingLeastSquares.cpp:51-101, assembleSystemAndSolve :129-140)
+// with the reference's own classes: a regular grid, SystemMatrixLeastSquaresIdentity with the
+// default multiple-eval configuration, b = generateb(y), ConjugateGradients(maxIterations, eps)
+// solving with reuse = true; adapt() refines with SurplusRefinementFunctor and zero-extends
+// alpha. Returns the final grid (raw level/index rows, storage order), alpha, and the CG
+// iterations of every solve (iters_out[rounds + 1], -1 where no solve happened).
+int ref_fit_adapt(int basis, int dim, int level, const double* x, int64_t m, const double* y,
+                  double lambda, double final_eps, int64_t final_maxit, double refine_eps,
+                  int64_t refine_maxit, int64_t rounds, int64_t points, double threshold,
+                  int64_t cap, int32_t* level_out, int32_t* index_out, double* alpha_out,
+                  int64_t* n_out, int64_t* iters_out) {
+  return guarded([&] {
+    std::unique_ptr<sgpp::base::Grid> grid(
+        basis == 1 ? sgpp::base::Grid::createModLinearGrid(static_cast<size_t>(dim))
+                   : sgpp::base::Grid::createLinearGrid(static_cast<size_t>(dim)));
+    grid->getGenerator().regular(level);
+    sgpp::base::DataMatrix X = make_matrix(x, m, dim);
+    sgpp::base::DataVector Y(static_cast<size_t>(m));
+    std::memcpy(Y.getPointer(), y, sizeof(double) * static_cast<size_t>(m));
+    sgpp::base::DataVector alpha(grid->getSize());
+    alpha.setAll(0.0);
+    auto solve = [&](double eps, int64_t maxit) -> int64_t {
+      sgpp::datadriven::SystemMatrixLeastSquaresIdentity A(*grid, X, lambda);
+      sgpp::datadriven::OperationMultipleEvalConfiguration cfg;
+      A.setImplementation(cfg);
+      sgpp::base::DataVector b(grid->getSize());
+      A.generateb(Y, b);
+      sgpp::solver::ConjugateGradients cg(static_cast<size_t>(maxit), eps);
+      cg.solve(A, alpha, b, true, false, -1.0);
+      return static_cast<int64_t>(cg.getNumberIterations());
+    };
+    for (int64_t r = 0; r <= rounds; ++r) iters_out[r] = -1;
+    iters_out[0] = solve(final_eps, final_maxit);
+    for (int64_t r = 0; r < rounds; ++r) {
+      sgpp::base::SurplusRefinementFunctor f(alpha, static_cast<size_t>(points), threshold);
+      const size_t n0 = grid->getSize();
+      grid->getGenerator().refine(f);
+      if (grid->getSize() <= n0) break;
+      alpha.resizeZero(grid->getSize());
+      iters_out[r + 1] = solve(refine_eps, refine_maxit);
+    }
+    auto& st = grid->getStorage();
+    *n_out = static_cast<int64_t>(st.getSize());
+    if (*n_out > cap) throw sgpp::base::factory_exception("ref_fit_adapt: cap too small");
+    for (size_t s = 0; s < st.getSize(); ++s) {
+      for (int t = 0; t < dim; ++t) {
+        level_out[s * dim + t] = static_cast<int32_t>(st.getPoint(s).getLevel(t));
+        index_out[s * dim + t] = static_cast<int32_t>(st.getPoint(s).getIndex(t));
+      }
+      alpha_out[s] = alpha[s];
+    }
+  });
+}
+
 // A data set through the reference's readers: format 0 = ARFF, 1 = CSV. Writes at most
 // n_cap rows of data (row-major, dim_cap columns) and targets; *n / *d get the Dataset's sizes.
 int ref_read_dataset(int format, const char* text, int64_t len, int has_targets, int skip_first,

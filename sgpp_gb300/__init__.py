@@ -63,7 +63,9 @@ EXPORTED_SYMBOLS = (
     "sgmev_profile_read", "sgmev_fit_device", "sgmev_mult_transpose_noalloc",
     "sgmev_batch_create", "sgmev_batch_destroy", "sgmev_batch_footprint", "sgmev_batch_add",
     "sgmev_batch_remove", "sgmev_batch_step", "sgmev_batch_solve", "sgmev_batch_result",
-    "sgmev_batch_info", "sgdata_size", "sgdata_read",
+    "sgmev_batch_info", "sgdata_size", "sgdata_read", "sgfit_config_defaults", "sgfit_create",
+    "sgfit_destroy", "sgfit_fit", "sgfit_adapt", "sgfit_update", "sgfit_evaluate", "sgfit_grid",
+    "sgfit_alpha", "sgfit_stats",
 )
 
 SGMEV_KERNEL_MULT_FP32 = 0

@@ -8,6 +8,12 @@ re-staged (prepare(), SystemMatrixLeastSquaresIdentity::prepareGrid), alpha is e
 the whole loop; only the grid is re-staged.
 
     python -m sgpp_gb300.adaptive        # the adaptive-grid configuration, one JSON line per round
+
+--engine fitter (default) runs the loop as ModelFittingLeastSquares fit() + adapt() on the
+device-resident fitter (sgpp_gb300.fitting: y and alpha stay on the GPU, one operator for all
+rounds); --engine operator runs adaptive_fit() below on the Python-level operator (alpha and y
+cross to the host every round). --throughput adds per-round kernel throughputs (extra operators,
+outside the fit timing).
 """
 from __future__ import annotations
 
@@ -77,6 +83,37 @@ def _throughput(op, grid, m, d):
     return out
 
 
+def fitter_rounds(grid_dim, X, y, level, lam, rounds, per_round, epsilon, mode="mixed"):
+    """The loop on the device-resident fitter: (model, per-round records)."""
+    from . import fitting
+
+    c = fitting.FitterConfigurationLeastSquares()
+    c.getGridConfig().level_ = level
+    c.getRegularizationConfig().lambda_ = lam
+    for sc in (c.getSolverFinalConfig(), c.getSolverRefineConfig()):
+        sc.eps_, sc.maxIterations_ = epsilon, 100000
+    c.getRefinementConfig().numRefinements_ = rounds
+    c.getRefinementConfig().numRefinementPoints_ = per_round
+    c.getMultipleEvalConfig().getParameters()["solve"] = mode
+    model = fitting.ModelFittingLeastSquares(c)
+    records = []
+    t0 = time.perf_counter()
+    model.fit(sg.Dataset(X, y))
+    st = model.stats()
+    records.append({"round": 0, "n_grid": model.getGrid().getSize(),
+                    "cg_iterations": st["cg_iterations"], "seconds": time.perf_counter() - t0})
+    for r in range(rounds):
+        t0 = time.perf_counter()
+        grew = model.adapt()
+        st = model.stats()
+        records.append({"round": r + 1, "n_grid": model.getGrid().getSize(),
+                        "cg_iterations": st["cg_iterations"] if grew else 0,
+                        "seconds": time.perf_counter() - t0})
+        if not grew:
+            break
+    return model, records
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--dim", type=int, default=8)
@@ -87,30 +124,49 @@ def main() -> int:
     ap.add_argument("--lam", type=float, default=1e-4)
     ap.add_argument("--epsilon", type=float, default=1e-8)
     ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--engine", choices=["fitter", "operator"], default="fitter")
+    ap.add_argument("--throughput", action="store_true")
     args = ap.parse_args()
     rng = np.random.default_rng(args.seed)
     X = rng.random((args.points, args.dim))
     y = np.prod(4.0 * X * (1.0 - X), axis=1) + 0.01 * rng.standard_normal(args.points)
-    grid = sg.Grid.createLinearGrid(args.dim)
-    grid.getGenerator().regular(args.level)
 
-    def on_round(op, rec):
-        for prec, name in ((sg.SGMEV_FP32, "fp32"), (sg.SGMEV_FP64, "fp64"),
-                           (sg.SGMEV_DF64, "df64")):
-            cfg = sg.OperationMultipleEvalConfiguration(
-                sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
-                parameters={"precision": {sg.SGMEV_FP32: "float", sg.SGMEV_FP64: "double",
-                                          sg.SGMEV_DF64: "df64"}[prec]})
-            o2 = sg.createOperationMultipleEval(grid, X, cfg)
-            rec[name] = _throughput(o2, grid, args.points, args.dim)
-            o2.close()
-        print(json.dumps(rec), flush=True)
+    if args.engine == "fitter":
+        t0 = time.perf_counter()
+        model, records = fitter_rounds(args.dim, X, y, args.level, args.lam, args.rounds,
+                                       args.per_round, args.epsilon)
+        total = time.perf_counter() - t0
+        for rec in records:
+            print(json.dumps(rec), flush=True)
+        n_final = model.getGrid().getSize()
+        model.close()
+    else:
+        grid = sg.Grid.createLinearGrid(args.dim)
+        grid.getGenerator().regular(args.level)
+        timing = {"measure": 0.0}
 
-    t0 = time.perf_counter()
-    alpha, records = adaptive_fit(grid, X, y, args.lam, args.rounds, args.per_round,
+        def on_round(op, rec):
+            if args.throughput:
+                t_m = time.perf_counter()
+                for prec, name in ((sg.SGMEV_FP32, "fp32"), (sg.SGMEV_FP64, "fp64"),
+                                   (sg.SGMEV_DF64, "df64")):
+                    cfg = sg.OperationMultipleEvalConfiguration(
+                        sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
+                        parameters={"precision": {sg.SGMEV_FP32: "float", sg.SGMEV_FP64: "double",
+                                                  sg.SGMEV_DF64: "df64"}[prec]})
+                    o2 = sg.createOperationMultipleEval(grid, X, cfg)
+                    rec[name] = _throughput(o2, grid, args.points, args.dim)
+                    o2.close()
+                timing["measure"] += time.perf_counter() - t_m
+            print(json.dumps(rec), flush=True)
+
+        t0 = time.perf_counter()
+        _, records = adaptive_fit(grid, X, y, args.lam, args.rounds, args.per_round,
                                   args.epsilon, on_round=on_round)
-    print(json.dumps({"metric": "adaptive_fit_seconds", "value": time.perf_counter() - t0,
-                      "final_n_grid": grid.getSize(),
+        total = time.perf_counter() - t0 - timing["measure"]
+        n_final = grid.getSize()
+    print(json.dumps({"metric": "adaptive_fit_seconds", "value": total, "engine": args.engine,
+                      "final_n_grid": n_final,
                       "total_cg_iterations": sum(r["cg_iterations"] for r in records),
                       "config": vars(args)}))
     return 0

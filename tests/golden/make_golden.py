@@ -21,6 +21,10 @@ from the unmodified reference sources plus oracle/ref_harness.cpp), on seeded in
                 reference's own reader fixtures datadriven/datasets/dataread/simple.{arff,csv}
                 (their SHA-256 and parsed outputs only, for the cases test_readARFF.cpp and
                 test_readCSV.cpp check), and a regression data set as ARFF text
+  fit_adapt.npz ModelFittingLeastSquares::fit followed by adapt() rounds, replayed with the
+                reference's own classes (grid, SurplusRefinementFunctor,
+                SystemMatrixLeastSquaresIdentity, ConjugateGradients with reuse): final grid,
+                alpha and the CG iterations of every solve
   modlinear.npz ModLinear grids: the streaming layout (getLevelIndexMaskArraysForModEval),
                 mult / multTranspose of the DEFAULT (OperationMultipleEvalModLinear) and STREAMING
                 (OperationMultiEvalModMaskStreaming) operators, regression fits, and the golden
@@ -413,6 +417,31 @@ def make_datasets(ref: Reference):
     np.savez_compressed(os.path.join(HERE, "datasets.npz"), **out)
 
 
+FIT_ADAPT_CASES = [
+    # name, basis, dim, level, m, lambda, final (eps, maxit), refine (eps, maxit), rounds, points
+    ("lin_d2_l3", 0, 2, 3, 500, 1e-4, (1e-10, 1000), (1e-10, 1000), 3, 5),
+    ("mod_d3_l2", 1, 3, 2, 800, 1e-3, (1e-10, 1000), (1e-10, 1000), 2, 3),
+    ("defaults_d4_l3", 0, 4, 3, 600, 0.01, (1e-12, 100), (1e-12, 100), 1, 1),
+]
+
+
+def make_fit_adapt(ref: Reference):
+    out = {}
+    rng = np.random.default_rng(20261206)
+    for name, basis, d, l, m, lam, fin, refi, rounds, pts in FIT_ADAPT_CASES:
+        x = rng.random((m, d))
+        y = np.sin(3 * x[:, 0]) * (1 + x[:, 1]) + 0.5 * x[:, d - 1] ** 2 + 0.01 * rng.standard_normal(m)
+        lev, idx, alpha, iters = ref.fit_adapt(basis, x, y, l, lam, fin[0], fin[1], refi[0],
+                                               refi[1], rounds, pts)
+        out[name + "_x"] = x
+        out[name + "_y"] = y
+        out[name + "_level"] = lev.astype(np.int8)
+        out[name + "_index"] = idx.astype(np.int16)
+        out[name + "_alpha"] = alpha
+        out[name + "_iterations"] = iters
+    np.savez_compressed(os.path.join(HERE, "fit_adapt.npz"), **out)
+
+
 def json_opt(o):
     import json
     return json.dumps({"has_targets": o[0], "cutoff": o[1], "cols": o[2], "targets": o[3]})
@@ -428,6 +457,7 @@ def main():
     make_bt(ref)
     make_modlinear(ref)
     make_datasets(ref)
+    make_fit_adapt(ref)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
