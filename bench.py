@@ -18,7 +18,7 @@ e2e     fits/s through the public API from pinned host buffers: create the opera
         host data matrix (H2D copy inside the timed region), fit with host y, read alpha back
 roofline  the kernel with the most device time in the fits. When it streams the materialised
         subspace products (the default), it is HBM-bound: achieved = its algorithmic bytes per
-        launch (5 B per padded point and padded subspace in FP32, 9 B in df64, plus the vectors)
+        launch (FP16 2 B, FP32 4 B, df64 8 B per padded point and padded subspace, plus the cell index, and the vectors)
         over its CUDA-event duration, against MEASURED_PEAKS.json's copy bandwidth. A kernel that
         evaluates hats is reported against the FP32/FP64 FMA peak measured in the same run, with
         the reference's count of 6 N M d FLOP per launch
@@ -192,11 +192,18 @@ def subspace_count(lp):
     return len({tuple(row) for row in np.asarray(lp, dtype=np.int64).tolist()})
 
 
+def cell_bytes(lp) -> float:
+    """Bytes per stored cell index: a nibble when no subspace has more than 16 cells."""
+    levels = np.rint(np.log2(np.asarray(lp, dtype=np.float64))).astype(np.int64)
+    cmax = int(2 ** int((levels - 1).sum(axis=1).max()))
+    return 0.5 if cmax <= 16 else 1.0
+
+
 def mat_bytes_per_launch(kernel: str, lp, m: int, n: int) -> float:
     """Algorithmic HBM bytes of one launch of a kernel streaming the materialised products."""
     mpad = -(-m // 1024) * 1024
     s_pad = -(-subspace_count(lp) // 32) * 32
-    per_entry = 9 if "df64" in kernel else (3 if "mat16" in kernel else 5)
+    per_entry = (8 if "df64" in kernel else (2 if "mat16" in kernel else 4)) + cell_bytes(lp)
     vec = (8 if "df64" in kernel else 4) * m + 8 * n
     return float(mpad) * s_pad * per_entry + vec
 
@@ -393,9 +400,10 @@ def run_ours(args):
                     "launches_timed": cnt, "avg_launch_ms": avg * 1e3,
                     "peak_source": peak_src,
                     "bytes_per_launch": by,
-                    "bytes_model": "materialised products read once per launch (FP32: 4 B product + "
-                                   "1 B cell; df64: 8 + 1 B) per padded point and padded subspace, "
-                                   "plus the input and output vectors"}
+                    "bytes_model": "materialised products read once per launch (FP16: 2 B, FP32: "
+                                   "4 B, df64: 8 B per product, plus its cell index: a nibble when "
+                                   "no subspace has more than 16 cells, else a byte) per padded "
+                                   "point and padded subspace, plus the input and output vectors"}
     else:
         achieved = work_per_op / avg / 1e12
         is64 = dom.endswith("fp64") and not dom.endswith("df64")

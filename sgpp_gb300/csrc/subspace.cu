@@ -706,7 +706,8 @@ cudaError_t launch_mat_build(const SubPlan& p, cudaStream_t s, const float* xh, 
   const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, 2LL * num_sms));
   kern<<<static_cast<unsigned>(blocks), nth, sm, s>>>(p.desc, p.sinfo, p.n_sub,
                                                       static_cast<int>(p.s_pad), xh, xl, mpad, m,
-                                                      nt, p.pmat, p.pmat_lo, p.pmat16, p.cmat);
+                                                      nt, p.pmat, p.pmat_lo, p.pmat16,
+                                                      static_cast<uint32_t*>(p.cmat));
   return cudaGetLastError();
 }
 

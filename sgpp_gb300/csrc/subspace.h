@@ -54,7 +54,8 @@ struct SubPlan {
   float4* pmat = nullptr;
   float4* pmat_lo = nullptr;
   uint2* pmat16 = nullptr;  // the same products rounded to FP16 (four halves per entry)
-  uint32_t* cmat = nullptr;
+  void* cmat = nullptr;  // cell words: uint32_t (a byte per point) or uint16_t (a nibble)
+  int cell_bits = 8;     // 8 or 4 bits per cell in cmat
   int64_t s_pad = 0;
   int64_t mat_mpad = 0;
   cudaStream_t stream = nullptr;  // device memory of the plan is allocated and freed on it

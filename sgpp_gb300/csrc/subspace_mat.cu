@@ -53,6 +53,15 @@ static_assert(kGroups % kAhead == 0 && kGroups % kAheadDf == 0, "the ring must d
 // multT: FP32 sums over this many tiles (1024 points) before they go into the FP64 row
 constexpr int kFlushTiles = 4;
 
+// Cell words: four points' cell indices in one word, a byte each (uint32_t, grids whose
+// subspaces have up to 256 cells) or a nibble each (uint16_t, up to 16 cells: 0.5 byte per entry
+// instead of 1, which the streaming kernels feel directly, being bound by HBM bytes).
+template <typename CW>
+__device__ __forceinline__ uint32_t cell_of(uint32_t w, int i) {
+  constexpr int kBits = sizeof(CW) * 2;
+  return (w >> (kBits * i)) & ((1u << kBits) - 1u);
+}
+
 // ---- mult --------------------------------------------------------------------------------
 // lane sums of 4 values -> the 32-lane sum of value (2 * bit4 + bit3) of the lane index
 __device__ __forceinline__ float reduce4(float v0, float v1, float v2, float v3, int lane) {
@@ -101,11 +110,11 @@ __host__ __device__ constexpr int mult_at_pad(int s_pad) {
   return (s_pad + kMultBlock - 1) / kMultBlock * kMultBlock;
 }
 
-template <bool HALF>
+template <bool HALF, typename CW>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
     const float* __restrict__ asub, int64_t m, int64_t tile_begin, int64_t n_tiles,
-    const typename Prod<HALF>::T* __restrict__ pm, const uint32_t* __restrict__ cm,
+    const typename Prod<HALF>::T* __restrict__ pm, const CW* __restrict__ cm,
     float* __restrict__ out32, double* __restrict__ out64) {
   using PT = typename Prod<HALF>::T;
   constexpr int A = Ahead2<HALF>::value;
@@ -136,15 +145,15 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
       const bool two = wb + 32 < s_pad;       // warp-uniform
       const int64_t at = gt * kGroups * static_cast<int64_t>(s_pad) + sid;
       const PT* src = pm + at;
-      const uint32_t* csrc = cm + at;
+      const CW* csrc = cm + at;
       const PT* src2 = two ? src + 32 : src;
-      const uint32_t* csrc2 = two ? csrc + 32 : csrc;
+      const CW* csrc2 = two ? csrc + 32 : csrc;
       const float* a_col = s_at + sid;
       const float* a_col2 = a_col + 32;       // zeros when the second block is absent
       float* part = s_part + warp * kOwnTile;
       const bool first = s0 == 0;
       PT ring[A], ring2[A];
-      uint32_t cring[A], cring2[A];
+      CW cring[A], cring2[A];
 #pragma unroll
       for (int u = 0; u < A; ++u) {
         ring[u] = __ldcs(src + static_cast<int64_t>(u) * s_pad);
@@ -167,14 +176,14 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
             cring2[u] = __ldcs(csrc2 + o);
           }
           // cells are below cmax by construction (the build writes c < cells of s <= cmax)
-          float v0 = a_col[(cs & 0xFFu) * sp] * p.x;
-          float v1 = a_col[((cs >> 8) & 0xFFu) * sp] * p.y;
-          float v2 = a_col[((cs >> 16) & 0xFFu) * sp] * p.z;
-          float v3 = a_col[(cs >> 24) * sp] * p.w;
-          v0 = fmaf(a_col2[(cq & 0xFFu) * sp], q.x, v0);
-          v1 = fmaf(a_col2[((cq >> 8) & 0xFFu) * sp], q.y, v1);
-          v2 = fmaf(a_col2[((cq >> 16) & 0xFFu) * sp], q.z, v2);
-          v3 = fmaf(a_col2[(cq >> 24) * sp], q.w, v3);
+          float v0 = a_col[cell_of<CW>(cs, 0) * sp] * p.x;
+          float v1 = a_col[cell_of<CW>(cs, 1) * sp] * p.y;
+          float v2 = a_col[cell_of<CW>(cs, 2) * sp] * p.z;
+          float v3 = a_col[cell_of<CW>(cs, 3) * sp] * p.w;
+          v0 = fmaf(a_col2[cell_of<CW>(cq, 0) * sp], q.x, v0);
+          v1 = fmaf(a_col2[cell_of<CW>(cq, 1) * sp], q.y, v1);
+          v2 = fmaf(a_col2[cell_of<CW>(cq, 2) * sp], q.z, v2);
+          v3 = fmaf(a_col2[cell_of<CW>(cq, 3) * sp], q.w, v3);
           const float r = reduce4(v0, v1, v2, v3, lane);
           if ((lane & 7) == 0) {
             float* dst = part + 4 * g + (lane >> 3);
@@ -199,11 +208,11 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
 }
 
 // ---- multTranspose -------------------------------------------------------------------------
-template <bool HALF>
+template <bool HALF, typename CW>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
     const float* __restrict__ v, int64_t n_tiles, const typename Prod<HALF>::T* __restrict__ pm,
-    const uint32_t* __restrict__ cm, double* __restrict__ rows) {
+    const CW* __restrict__ cm, double* __restrict__ rows) {
   using PT = typename Prod<HALF>::T;
   extern __shared__ __align__(16) unsigned char smem[];
   float* s_acc = reinterpret_cast<float*>(smem);  // [cmax][blockDim]
@@ -223,10 +232,10 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
     for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
       const int64_t at = tile * kGroups * static_cast<int64_t>(s_pad) + sid;
       const PT* src = pm + at;
-      const uint32_t* csrc = cm + at;
+      const CW* csrc = cm + at;
       const float4* vt = v4 + tile * kGroups;
       PT ring[Ahead<HALF>::value];
-      uint32_t cring[Ahead<HALF>::value];
+      CW cring[Ahead<HALF>::value];
 #pragma unroll
       for (int u = 0; u < Ahead<HALF>::value; ++u) {
         ring[u] = __ldcs(src + static_cast<int64_t>(u) * s_pad);
@@ -244,10 +253,10 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
           }
           const float4 vv = vt[g];  // the same four values for every lane
           // cells are below cmax by construction
-          acc[(cs & 0xFFu) * nth] += vv.x * p.x;
-          acc[((cs >> 8) & 0xFFu) * nth] += vv.y * p.y;
-          acc[((cs >> 16) & 0xFFu) * nth] += vv.z * p.z;
-          acc[(cs >> 24) * nth] += vv.w * p.w;
+          acc[cell_of<CW>(cs, 0) * nth] += vv.x * p.x;
+          acc[cell_of<CW>(cs, 1) * nth] += vv.y * p.y;
+          acc[cell_of<CW>(cs, 2) * nth] += vv.z * p.z;
+          acc[cell_of<CW>(cs, 3) * nth] += vv.w * p.w;
         }
       }
       ++since;
@@ -287,11 +296,12 @@ __device__ __forceinline__ ff reduce4_ff(ff v0, ff v1, ff v2, ff v3, int lane) {
   return b;
 }
 
+template <typename CW>
 __global__ void __launch_bounds__(kMatThreads, 1) mat_mult_df_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
     const float2* __restrict__ asub2, int64_t m, int64_t tile_begin, int64_t n_tiles,
     const float4* __restrict__ phi, const float4* __restrict__ plo,
-    const uint32_t* __restrict__ cm, double* __restrict__ out64) {
+    const CW* __restrict__ cm, double* __restrict__ out64) {
   extern __shared__ __align__(16) unsigned char smem[];
   float2* s_part = reinterpret_cast<float2*>(smem);  // [warps][kOwnTile]
   float2* s_at = s_part + kMatWarps * kOwnTile;      // [cmax][s_pad]
@@ -318,7 +328,7 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_mult_df_kernel(
       float2* part = s_part + warp * kOwnTile;
       const bool first = s0 == 0;
       float4 rh[kAheadDf], rl[kAheadDf];
-      uint32_t rc[kAheadDf];
+      CW rc[kAheadDf];
 #pragma unroll
       for (int u = 0; u < kAheadDf; ++u) {
         rh[u] = __ldcs(phi + at + static_cast<int64_t>(u) * s_pad);
@@ -337,10 +347,10 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_mult_df_kernel(
             rl[u] = __ldcs(plo + k);
             rc[u] = __ldcs(cm + k);
           }
-          const float2 a0 = a_col[min(cs & 0xFFu, cm1) * s_pad];
-          const float2 a1 = a_col[min((cs >> 8) & 0xFFu, cm1) * s_pad];
-          const float2 a2 = a_col[min((cs >> 16) & 0xFFu, cm1) * s_pad];
-          const float2 a3 = a_col[min(cs >> 24, cm1) * s_pad];
+          const float2 a0 = a_col[min(cell_of<CW>(cs, 0), cm1) * s_pad];
+          const float2 a1 = a_col[min(cell_of<CW>(cs, 1), cm1) * s_pad];
+          const float2 a2 = a_col[min(cell_of<CW>(cs, 2), cm1) * s_pad];
+          const float2 a3 = a_col[min(cell_of<CW>(cs, 3), cm1) * s_pad];
           const ff r = reduce4_ff(mul_ff(ff{ph.x, pl.x}, ff{a0.x, a0.y}),
                                   mul_ff(ff{ph.y, pl.y}, ff{a1.x, a1.y}),
                                   mul_ff(ff{ph.z, pl.z}, ff{a2.x, a2.y}),
@@ -369,11 +379,12 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_mult_df_kernel(
   }
 }
 
+template <typename CW>
 __global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
     const float* __restrict__ vh, const float* __restrict__ vl, int64_t n_tiles,
     const float4* __restrict__ phi, const float4* __restrict__ plo,
-    const uint32_t* __restrict__ cm, double* __restrict__ rows) {
+    const CW* __restrict__ cm, double* __restrict__ rows) {
   extern __shared__ __align__(16) unsigned char smem[];
   float2* s_acc = reinterpret_cast<float2*>(smem);  // [cmax][blockDim]
   double* row = rows + static_cast<int64_t>(blockIdx.x) * total;
@@ -393,7 +404,7 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
     for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
       const int64_t at = tile * kGroups * static_cast<int64_t>(s_pad) + sid;
       float4 rh[kAheadDf], rl[kAheadDf];
-      uint32_t rc[kAheadDf];
+      CW rc[kAheadDf];
 #pragma unroll
       for (int u = 0; u < kAheadDf; ++u) {
         rh[u] = __ldcs(phi + at + static_cast<int64_t>(u) * s_pad);
@@ -417,7 +428,7 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
           const float vh_[4] = {vvh.x, vvh.y, vvh.z, vvh.w}, vl_[4] = {vvl.x, vvl.y, vvl.z, vvl.w};
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
-            float2* slot = acc + min((cs >> (8 * i)) & 0xFFu, cm1) * nth;
+            float2* slot = acc + min(cell_of<CW>(cs, i), cm1) * nth;
             ff a{slot->x, slot->y};
             add_ff(a, mul_ff(ff{ph_[i], pl_[i]}, ff{vh_[i], vl_[i]}));
             *slot = make_float2(a.h, a.l);
@@ -460,10 +471,11 @@ constexpr int kSysFlushTiles = 32;           // FP32 sums over 1024 points per f
 constexpr int kSysMaxSub = 1024;
 static_assert(kSysGroups % kSysAhead == 0, "the ring must divide a tile");
 
+template <typename CW>
 __global__ void __launch_bounds__(kSysThreads, 1) mat_system_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
     const float* __restrict__ asub, int64_t n_tiles, const float4* __restrict__ pm,
-    const uint32_t* __restrict__ cm, double* __restrict__ rows) {
+    const CW* __restrict__ cm, double* __restrict__ rows) {
   extern __shared__ __align__(16) unsigned char smem[];
   float* s_at = reinterpret_cast<float*>(smem);            // [cmax][s_pad] alpha by (cell, s)
   float* s_acc = s_at + static_cast<size_t>(cmax) * s_pad;  // [cmax][s_pad] sums by (cell, s)
@@ -493,7 +505,7 @@ __global__ void __launch_bounds__(kSysThreads, 1) mat_system_kernel(
       asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(pm + nb),
                    "r"(static_cast<uint32_t>(sizeof(float4) * kSysGroups * s_pad)) : "memory");
       asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(cm + nb),
-                   "r"(static_cast<uint32_t>(sizeof(uint32_t) * kSysGroups * s_pad)) : "memory");
+                   "r"(static_cast<uint32_t>(sizeof(CW) * kSysGroups * s_pad)) : "memory");
     }
     // phase A: (B a)_j for the tile's points
     for (int s0 = 0; s0 < s_pad; s0 += blockDim.x) {
@@ -504,7 +516,7 @@ __global__ void __launch_bounds__(kSysThreads, 1) mat_system_kernel(
       float* part = s_part + warp * kSysTile;
       const bool pass0 = s0 == 0;
       float4 ring[kSysAhead];
-      uint32_t cring[kSysAhead];
+      CW cring[kSysAhead];
 #pragma unroll
       for (int u = 0; u < kSysAhead; ++u) {
         ring[u] = __ldcg(pm + at + static_cast<int64_t>(u) * s_pad);
@@ -520,10 +532,10 @@ __global__ void __launch_bounds__(kSysThreads, 1) mat_system_kernel(
             ring[u] = __ldcg(pm + at + static_cast<int64_t>(g + kSysAhead) * s_pad);
             cring[u] = __ldcg(cm + at + static_cast<int64_t>(g + kSysAhead) * s_pad);
           }
-          const float v0 = a_col[min(cs & 0xFFu, cm1) * s_pad] * p.x;
-          const float v1 = a_col[min((cs >> 8) & 0xFFu, cm1) * s_pad] * p.y;
-          const float v2 = a_col[min((cs >> 16) & 0xFFu, cm1) * s_pad] * p.z;
-          const float v3 = a_col[min(cs >> 24, cm1) * s_pad] * p.w;
+          const float v0 = a_col[min(cell_of<CW>(cs, 0), cm1) * s_pad] * p.x;
+          const float v1 = a_col[min(cell_of<CW>(cs, 1), cm1) * s_pad] * p.y;
+          const float v2 = a_col[min(cell_of<CW>(cs, 2), cm1) * s_pad] * p.z;
+          const float v3 = a_col[min(cell_of<CW>(cs, 3), cm1) * s_pad] * p.w;
           const float r = reduce4(v0, v1, v2, v3, lane);
           if ((lane & 7) == 0) {
             float* dst = part + 4 * g + (lane >> 3);
@@ -547,7 +559,7 @@ __global__ void __launch_bounds__(kSysThreads, 1) mat_system_kernel(
       const int64_t at = g_base * s_pad + sid;
       float* acc = s_acc + sid;
       float4 ring[kSysAhead];
-      uint32_t cring[kSysAhead];
+      CW cring[kSysAhead];
 #pragma unroll
       for (int u = 0; u < kSysAhead; ++u) {
         ring[u] = __ldcs(pm + at + static_cast<int64_t>(u) * s_pad);
@@ -564,10 +576,10 @@ __global__ void __launch_bounds__(kSysThreads, 1) mat_system_kernel(
             cring[u] = __ldcs(cm + at + static_cast<int64_t>(g + kSysAhead) * s_pad);
           }
           const float4 ba = *reinterpret_cast<const float4*>(s_ba + 4 * g);
-          acc[min(cs & 0xFFu, cm1) * s_pad] += ba.x * p.x;
-          acc[min((cs >> 8) & 0xFFu, cm1) * s_pad] += ba.y * p.y;
-          acc[min((cs >> 16) & 0xFFu, cm1) * s_pad] += ba.z * p.z;
-          acc[min(cs >> 24, cm1) * s_pad] += ba.w * p.w;
+          acc[min(cell_of<CW>(cs, 0), cm1) * s_pad] += ba.x * p.x;
+          acc[min(cell_of<CW>(cs, 1), cm1) * s_pad] += ba.y * p.y;
+          acc[min(cell_of<CW>(cs, 2), cm1) * s_pad] += ba.z * p.z;
+          acc[min(cell_of<CW>(cs, 3), cm1) * s_pad] += ba.w * p.w;
         }
       }
     }
@@ -639,9 +651,28 @@ bool subspace_mat_fits(const SubPlan& p, bool df) {
          mat_multt_smem(p.cmax, s_pad) <= kMatSmemBudget;
 }
 
+// nibble cells when every subspace has at most 16 cells
+bool mat_cell4(const SubPlan& p) { return p.cmax <= 16; }
+
 int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad) {
-  return mpad * ((p.n_sub + 31) / 32 * 32) * static_cast<int64_t>(2 * sizeof(float) + 2 + 1);
+  // P_hi, P_lo (4 + 4 bytes), the FP16 copy (2) and the cells (1 byte, or a nibble; during the
+  // build the byte cells and the nibbles coexist)
+  const double per = 2 * sizeof(float) + 2 + (mat_cell4(p) ? 1.5 : 1.0);
+  return static_cast<int64_t>(static_cast<double>(mpad) * ((p.n_sub + 31) / 32 * 32) * per);
 }
+
+namespace {
+// byte cells -> nibble cells (four per uint16)
+__global__ void pack_cells_kernel(const uint32_t* __restrict__ in, int64_t n,
+                                  uint16_t* __restrict__ out) {
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const uint32_t w = in[k];
+    out[k] = static_cast<uint16_t>((w & 0xFu) | ((w >> 4) & 0xF0u) | ((w >> 8) & 0xF00u) |
+                                   ((w >> 12) & 0xF000u));
+  }
+}
+}  // namespace
 
 cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, const float* xl,
                                  int64_t mpad, int64_t m, int num_sms) {
@@ -652,25 +683,57 @@ cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, co
   p->pmat = p->pmat_lo = nullptr;
   p->pmat16 = nullptr;
   p->cmat = nullptr;
+  p->cell_bits = 8;
   p->s_pad = (p->n_sub + 31) / 32 * 32;
   p->mat_mpad = mpad;
   const size_t entries = static_cast<size_t>(mpad / 4) * static_cast<size_t>(p->s_pad);
-  cudaError_t e = dev_malloc(&p->pmat, entries * sizeof(float4), s);
-  if (e == cudaSuccess) e = dev_malloc(&p->pmat_lo, entries * sizeof(float4), s);
-  if (e == cudaSuccess) e = dev_malloc(&p->pmat16, entries * sizeof(uint2), s);
-  if (e == cudaSuccess) e = dev_malloc(&p->cmat, entries * sizeof(uint32_t), s);
-  if (e != cudaSuccess) {
+  uint32_t* cm8 = nullptr;
+  auto release = [&]() {
     dev_free(p->pmat, s);
     dev_free(p->pmat_lo, s);
     dev_free(p->pmat16, s);
-    dev_free(p->cmat, s);
+    dev_free(cm8, s);
     p->pmat = p->pmat_lo = nullptr;
     p->pmat16 = nullptr;
     p->cmat = nullptr;
     (void)cudaGetLastError();
+  };
+  cudaError_t e = dev_malloc(&p->pmat, entries * sizeof(float4), s);
+  if (e == cudaSuccess) e = dev_malloc(&p->pmat_lo, entries * sizeof(float4), s);
+  if (e == cudaSuccess) e = dev_malloc(&p->pmat16, entries * sizeof(uint2), s);
+  if (e == cudaSuccess) e = dev_malloc(&cm8, entries * sizeof(uint32_t), s);
+  if (e != cudaSuccess) {
+    release();
     return e;
   }
-  return subspace_mat_build(*p, s, xh, xl, mpad, m, num_sms);
+  p->cmat = cm8;
+  e = subspace_mat_build(*p, s, xh, xl, mpad, m, num_sms);
+  if (e != cudaSuccess) {
+    release();
+    return e;
+  }
+  if (mat_cell4(*p)) {
+    uint16_t* cm4 = nullptr;
+    e = dev_malloc(&cm4, entries * sizeof(uint16_t), s);
+    if (e != cudaSuccess) {
+      // keep the byte cells: every kernel reads either form
+      (void)cudaGetLastError();
+      return cudaSuccess;
+    }
+    const unsigned blocks = static_cast<unsigned>(std::min<int64_t>(
+        16 * num_sms, std::max<int64_t>(1, (static_cast<int64_t>(entries) + 255) / 256)));
+    pack_cells_kernel<<<blocks, 256, 0, s>>>(cm8, static_cast<int64_t>(entries), cm4);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      dev_free(cm4, s);
+      release();
+      return e;
+    }
+    dev_free(cm8, s);
+    p->cmat = cm4;
+    p->cell_bits = 4;
+  }
+  return cudaSuccess;
 }
 
 bool subspace_system_mat_fits(const SubPlan& p) {
@@ -679,21 +742,103 @@ bool subspace_system_mat_fits(const SubPlan& p) {
          mat_system_smem(p.cmax, s_pad) <= kMatSmemBudget;
 }
 
+namespace {
+template <typename CW>
+cudaError_t launch_system(const SubPlan& p, cudaStream_t s, int64_t nt, int64_t rows) {
+  auto kern = mat_system_kernel<CW>;
+  const size_t sm = mat_system_smem(p.cmax, p.s_pad);
+  cudaError_t e = set_smem_cap(kern, sm);
+  if (e != cudaSuccess) return e;
+  kern<<<static_cast<unsigned>(rows), kSysThreads, sm, s>>>(
+      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), p.asub, nt,
+      p.pmat, static_cast<const CW*>(p.cmat), p.rows);
+  return cudaGetLastError();
+}
+
+template <typename CW>
+cudaError_t launch_mult_df(const SubPlan& p, cudaStream_t s, int64_t m, double* out64, int64_t t0,
+                           int64_t nt, int num_sms) {
+  auto kern = mat_mult_df_kernel<CW>;
+  const size_t sm = mat_mult_df_smem(p.cmax, p.s_pad);
+  cudaError_t e = set_smem_cap(kern, sm);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMatThreads, sm);
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
+  kern<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
+      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub2, m, t0, nt, p.pmat, p.pmat_lo,
+      static_cast<const CW*>(p.cmat), out64);
+  return cudaGetLastError();
+}
+
+template <typename CW>
+cudaError_t launch_multt_df(const SubPlan& p, cudaStream_t s, int64_t mpad, const float* vh,
+                            const float* vl, int num_sms, int64_t* rows) {
+  auto kern = mat_multt_df_kernel<CW>;
+  const size_t sm = mat_multt_df_smem(p.cmax, p.s_pad);
+  const int nth = mat_threads(p.s_pad);
+  cudaError_t e = set_smem_cap(kern, sm);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
+  if (e != cudaSuccess) return e;
+  const int64_t nt = mpad / kOwnTile;
+  *rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
+  kern<<<static_cast<unsigned>(*rows), nth, sm, s>>>(
+      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), vh, vl, nt,
+      p.pmat, p.pmat_lo, static_cast<const CW*>(p.cmat), p.rows);
+  return cudaGetLastError();
+}
+
+template <bool HALF, typename CW>
+cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, const typename Prod<HALF>::T* pm,
+                            int64_t m, float* out32, double* out64, int64_t t0, int64_t nt,
+                            int num_sms) {
+  auto kern = mat_mult_kernel<HALF, CW>;
+  const size_t sm = mat_mult_smem(p.cmax, p.s_pad);
+  cudaError_t e = set_smem_cap(kern, sm);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMatThreads, sm);
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
+  kern<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
+      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub, m, t0, nt, pm,
+      static_cast<const CW*>(p.cmat), out32, out64);
+  return cudaGetLastError();
+}
+
+template <bool HALF, typename CW>
+cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, const typename Prod<HALF>::T* pm,
+                             int64_t mpad, const float* v32, int num_sms, int64_t* rows) {
+  auto kern = mat_multt_kernel<HALF, CW>;
+  const size_t sm = mat_multt_smem(p.cmax, p.s_pad);
+  const int nth = mat_threads(p.s_pad);
+  cudaError_t e = set_smem_cap(kern, sm);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
+  if (e != cudaSuccess) return e;
+  const int64_t nt = mpad / kOwnTile;
+  *rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
+  kern<<<static_cast<unsigned>(*rows), nth, sm, s>>>(p.sact, p.n_sub, static_cast<int>(p.s_pad),
+                                                     p.cmax, static_cast<int>(p.total), v32, nt,
+                                                     pm, static_cast<const CW*>(p.cmat), p.rows);
+  return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t subspace_system_mat(const SubPlan& p, cudaStream_t s, int64_t mpad,
                                 const float* alpha32, int64_t npad, double* out64,
                                 const double* add, double scale_add, int num_sms) {
   if (!p.pmat || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
   cudaError_t e = subspace_scatter_alpha(p, s, alpha32);
   if (e != cudaSuccess) return e;
-  const size_t sm = mat_system_smem(p.cmax, p.s_pad);
-  e = set_smem_cap(mat_system_kernel, sm);
-  if (e != cudaSuccess) return e;
   const int64_t nt = mpad / kSysTile;
   const int64_t rows = std::min<int64_t>(num_sms, std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
-  mat_system_kernel<<<static_cast<unsigned>(rows), kSysThreads, sm, s>>>(
-      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), p.asub, nt,
-      p.pmat, p.cmat, p.rows);
-  e = cudaGetLastError();
+  e = p.cell_bits == 4 ? launch_system<uint16_t>(p, s, nt, rows)
+                       : launch_system<uint32_t>(p, s, nt, rows);
   if (e != cudaSuccess) return e;
   return subspace_finish_rows(p, s, rows, npad, out64, add, scale_add);
 }
@@ -707,78 +852,20 @@ cudaError_t subspace_mult_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad,
   const int64_t t0 = j_begin / kOwnTile;
   const int64_t nt = (j_end + kOwnTile - 1) / kOwnTile - t0;
   if (nt <= 0) return cudaSuccess;
-  const size_t sm = mat_mult_df_smem(p.cmax, p.s_pad);
-  e = set_smem_cap(mat_mult_df_kernel, sm);
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mat_mult_df_kernel, kMatThreads, sm);
-  if (e != cudaSuccess) return e;
-  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
-  mat_mult_df_kernel<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
-      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub2, m, t0, nt, p.pmat, p.pmat_lo,
-      p.cmat, out64);
-  return cudaGetLastError();
+  return p.cell_bits == 4 ? launch_mult_df<uint16_t>(p, s, m, out64, t0, nt, num_sms)
+                          : launch_mult_df<uint32_t>(p, s, m, out64, t0, nt, num_sms);
 }
 
 cudaError_t subspace_multt_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad,
                                   const float* vh, const float* vl, int64_t npad, double* out64,
                                   const double* add, double scale_add, int num_sms) {
   if (!p.pmat || !p.pmat_lo || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
-  const size_t sm = mat_multt_df_smem(p.cmax, p.s_pad);
-  const int nth = mat_threads(p.s_pad);
-  cudaError_t e = set_smem_cap(mat_multt_df_kernel, sm);
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mat_multt_df_kernel, nth, sm);
-  if (e != cudaSuccess) return e;
-  const int64_t nt = mpad / kOwnTile;
-  const int64_t rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
-  mat_multt_df_kernel<<<static_cast<unsigned>(rows), nth, sm, s>>>(
-      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), vh, vl, nt,
-      p.pmat, p.pmat_lo, p.cmat, p.rows);
-  e = cudaGetLastError();
+  int64_t rows = 0;
+  cudaError_t e = p.cell_bits == 4 ? launch_multt_df<uint16_t>(p, s, mpad, vh, vl, num_sms, &rows)
+                                   : launch_multt_df<uint32_t>(p, s, mpad, vh, vl, num_sms, &rows);
   if (e != cudaSuccess) return e;
   return subspace_finish_rows(p, s, rows, npad, out64, add, scale_add);
 }
-
-namespace {
-template <bool HALF>
-cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, const typename Prod<HALF>::T* pm,
-                            int64_t m, float* out32, double* out64, int64_t t0, int64_t nt,
-                            int num_sms) {
-  auto kern = mat_mult_kernel<HALF>;
-  const size_t sm = mat_mult_smem(p.cmax, p.s_pad);
-  cudaError_t e = set_smem_cap(kern, sm);
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMatThreads, sm);
-  if (e != cudaSuccess) return e;
-  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
-  kern<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
-      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub, m, t0, nt, pm, p.cmat, out32,
-      out64);
-  return cudaGetLastError();
-}
-
-template <bool HALF>
-cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, const typename Prod<HALF>::T* pm,
-                             int64_t mpad, const float* v32, int num_sms, int64_t* rows) {
-  auto kern = mat_multt_kernel<HALF>;
-  const size_t sm = mat_multt_smem(p.cmax, p.s_pad);
-  const int nth = mat_threads(p.s_pad);
-  cudaError_t e = set_smem_cap(kern, sm);
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
-  if (e != cudaSuccess) return e;
-  const int64_t nt = mpad / kOwnTile;
-  *rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
-  kern<<<static_cast<unsigned>(*rows), nth, sm, s>>>(p.sact, p.n_sub, static_cast<int>(p.s_pad),
-                                                     p.cmax, static_cast<int>(p.total), v32, nt,
-                                                     pm, p.cmat, p.rows);
-  return cudaGetLastError();
-}
-}  // namespace
 
 cudaError_t subspace_mult_mat(const SubPlan& p, cudaStream_t s, const float* /*xt*/, int64_t mpad,
                               int64_t m, const float* alpha32, float* out32, double* out64,
@@ -789,8 +876,11 @@ cudaError_t subspace_mult_mat(const SubPlan& p, cudaStream_t s, const float* /*x
   const int64_t t0 = j_begin / kOwnTile;
   const int64_t nt = (j_end + kOwnTile - 1) / kOwnTile - t0;
   if (nt <= 0) return cudaSuccess;
-  return half ? launch_mat_mult<true>(p, s, p.pmat16, m, out32, out64, t0, nt, num_sms)
-              : launch_mat_mult<false>(p, s, p.pmat, m, out32, out64, t0, nt, num_sms);
+  if (p.cell_bits == 4)
+    return half ? launch_mat_mult<true, uint16_t>(p, s, p.pmat16, m, out32, out64, t0, nt, num_sms)
+                : launch_mat_mult<false, uint16_t>(p, s, p.pmat, m, out32, out64, t0, nt, num_sms);
+  return half ? launch_mat_mult<true, uint32_t>(p, s, p.pmat16, m, out32, out64, t0, nt, num_sms)
+              : launch_mat_mult<false, uint32_t>(p, s, p.pmat, m, out32, out64, t0, nt, num_sms);
 }
 
 cudaError_t subspace_multt_mat(const SubPlan& p, cudaStream_t s, const float* /*xt*/, int64_t mpad,
@@ -798,8 +888,13 @@ cudaError_t subspace_multt_mat(const SubPlan& p, cudaStream_t s, const float* /*
                                const double* add, double scale_add, int num_sms, bool half) {
   if (!p.pmat || !p.pmat16 || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
   int64_t rows = 0;
-  cudaError_t e = half ? launch_mat_multt<true>(p, s, p.pmat16, mpad, v32, num_sms, &rows)
-                       : launch_mat_multt<false>(p, s, p.pmat, mpad, v32, num_sms, &rows);
+  cudaError_t e;
+  if (p.cell_bits == 4)
+    e = half ? launch_mat_multt<true, uint16_t>(p, s, p.pmat16, mpad, v32, num_sms, &rows)
+             : launch_mat_multt<false, uint16_t>(p, s, p.pmat, mpad, v32, num_sms, &rows);
+  else
+    e = half ? launch_mat_multt<true, uint32_t>(p, s, p.pmat16, mpad, v32, num_sms, &rows)
+             : launch_mat_multt<false, uint32_t>(p, s, p.pmat, mpad, v32, num_sms, &rows);
   if (e != cudaSuccess) return e;
   return subspace_finish_rows(p, s, rows, npad, out64, add, scale_add);
 }
