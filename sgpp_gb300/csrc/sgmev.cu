@@ -108,6 +108,7 @@ struct sgmev_op {
   double pc_lm = 0.0;
   double* dot_part = nullptr;
   double* dot_out = nullptr;
+  double* scal = nullptr;      // CG scalars on the device (+ the last-block ticket at scal + 8)
   double* host_scalar = nullptr;  // pinned
 
   cudaStream_t own_stream = nullptr;
@@ -352,6 +353,111 @@ __global__ void axpy_kernel(int64_t n, double a, const double* __restrict__ x,
 // d = beta*d + r
 __global__ void xpby_kernel(int64_t n, const double* __restrict__ r, double beta,
                             double* __restrict__ d) {
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    d[i] = fma(beta, d[i], r[i]);
+}
+
+// ---- CG with its scalars on the device ---------------------------------------------------
+// scal[0] delta_new, [1] delta_old, [2] d.q, [3] alpha, [4] beta; a ticket counter (scal + 8)
+// lets the last block of a launch add the partials. Every sum has the thread mapping and the
+// tree of dot_partial_kernel + dot_final_kernel, so the scalars are bit-identical to the
+// host-driven loop's.
+__device__ __forceinline__ double block_tree_sum(double acc, double* s) {
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = kDotThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  return s[0];
+}
+
+// the last block to finish sums part[0..gridDim.x) as dot_final_kernel does; true in its threads
+__device__ __forceinline__ bool last_block_total(double block_sum, double* part,
+                                                 unsigned int* ticket, double* s,
+                                                 double* total) {
+  __shared__ bool is_last;
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = block_sum;
+    __threadfence();
+    is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!is_last) return false;
+  __threadfence();
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < static_cast<int>(gridDim.x); i += kDotThreads)
+    acc += reinterpret_cast<volatile double*>(part)[i];
+  *total = block_tree_sum(acc, s);
+  if (threadIdx.x == 0) *ticket = 0u;
+  return true;
+}
+
+// dq = d.q, alpha = delta_new / dq (0 when dq is 0: the loop then stops without a step)
+__global__ void __launch_bounds__(kDotThreads) cg_alpha_kernel(const double* __restrict__ d,
+                                                              const double* __restrict__ q,
+                                                              int64_t n, double* __restrict__ part,
+                                                              double* __restrict__ scal) {
+  __shared__ double s[kDotThreads];
+  double acc = 0.0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    acc = fma(d[i], q[i], acc);
+  const double b = block_tree_sum(acc, s);
+  double dq = 0.0;
+  if (last_block_total(b, part, reinterpret_cast<unsigned int*>(scal + 8), s, &dq) &&
+      threadIdx.x == 0) {
+    scal[2] = dq;
+    scal[3] = dq != 0.0 ? scal[0] / dq : 0.0;
+  }
+}
+
+// x += alpha d; r -= alpha q (unless r_fixed: r was recomputed); then delta_old = delta_new,
+// delta_new = r.r, beta = delta_new / delta_old. with_x = false skips the x update.
+__global__ void __launch_bounds__(kDotThreads) cg_update_kernel(int64_t n, const double* __restrict__ d,
+                                                               const double* __restrict__ q,
+                                                               double* __restrict__ x,
+                                                               double* __restrict__ r, int with_x,
+                                                               int r_fixed,
+                                                               double* __restrict__ part,
+                                                               double* __restrict__ scal) {
+  __shared__ double s[kDotThreads];
+  const double a = scal[3];
+  double acc = 0.0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (with_x) x[i] = fma(a, d[i], x[i]);
+    double ri = r[i];
+    if (!r_fixed) {
+      ri = fma(-a, q[i], ri);
+      r[i] = ri;
+    }
+    acc = fma(ri, ri, acc);
+  }
+  const double b = block_tree_sum(acc, s);
+  double rr = 0.0;
+  if (last_block_total(b, part, reinterpret_cast<unsigned int*>(scal + 8), s, &rr) &&
+      threadIdx.x == 0) {
+    scal[1] = scal[0];
+    scal[0] = rr;
+    scal[4] = rr / scal[1];
+  }
+}
+
+// x += alpha d (alpha on the device)
+__global__ void axpy_dev_kernel(int64_t n, const double* __restrict__ scal,
+                                const double* __restrict__ d, double* __restrict__ x) {
+  const double a = scal[3];
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    x[i] = fma(a, d[i], x[i]);
+}
+
+// d = beta d + r (beta on the device)
+__global__ void xpby_dev_kernel(int64_t n, const double* __restrict__ r,
+                                const double* __restrict__ scal, double* __restrict__ d) {
+  const double beta = scal[4];
   for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x)
     d[i] = fma(beta, d[i], r[i]);
@@ -1017,7 +1123,7 @@ static void release(sgmev_op* op) {
   subspace_free(&op->sub);
   void* ptrs[] = {op->xt64, op->xt32, op->xt32lo, op->li64, op->li32, op->gq, op->gs64, op->gs32, op->a64,
                   op->a32,  op->a32lo, op->v64,   op->v32,  op->v32lo, op->out64, op->part,
-                  op->cg,   op->dot_part, op->dot_out};
+                  op->cg,   op->dot_part, op->dot_out, op->scal};
   for (void* p : ptrs) dev_free(p, op->stream);
   pinned_release(op->host_scalar);
   op->host_scalar = nullptr;
@@ -1199,6 +1305,8 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   if (!op->host_scalar) return bail(fail(SGMEV_ERR_OOM, "pinned host block"));
   CREATE_TRY(dalloc(op->stream, &op->dot_part, kDotBlocks));
   CREATE_TRY(dalloc(op->stream, &op->dot_out, 8));
+  CREATE_TRY(dalloc(op->stream, &op->scal, 16));
+  CREATE_CUDA(cudaMemsetAsync(op->scal, 0, sizeof(double) * 16, op->stream));
 
   // data
   CREATE_TRY(dalloc(op->stream, &op->xt64, static_cast<size_t>(op->mpad * dim)));
@@ -1486,29 +1594,48 @@ static int cg_core(sgmev_op* op, int prec, const double* rhs, double* x, double 
     op->launches += 1;
   }
   SGMEV_CUDA(cudaMemcpyAsync(d, r, sizeof(double) * np, cudaMemcpyDeviceToDevice, op->stream));
-  double delta_new = 0.0;
-  SGMEV_TRY(dev_dot(op, r, r, np, &delta_new));
+  // the scalars live on the device (alpha and beta never visit the host); the host reads
+  // delta_new and d.q once per iteration for the stopping test
+  double* sc = op->scal;
+  double* host = op->host_scalar;  // pinned: [0] delta_new, [1] delta_old, [2] d.q
+  auto read_scalars = [&]() -> int {
+    SGMEV_CUDA(cudaMemcpyAsync(host, sc, sizeof(double) * 3, cudaMemcpyDeviceToHost, op->stream));
+    SGMEV_CUDA(cudaStreamSynchronize(op->stream));
+    return SGMEV_OK;
+  };
+  // delta_new = r.r (the update kernel without steps)
+  cg_update_kernel<<<kDotBlocks, kDotThreads, 0, op->stream>>>(np, d, q, x, r, 0, 1,
+                                                                 op->dot_part, sc);
+  op->launches += 1;
+  SGMEV_CUDA(cudaGetLastError());
+  SGMEV_TRY(read_scalars());
+  double delta_new = host[0];
   if (!reuse) delta_0 = delta_new * eps2;
   int64_t it = 0;
   while (it < imax && delta_new > delta_0 && delta_new > 0.0) {
     SGMEV_TRY(dev_system(op, prec, d, q, lm));
-    double dq = 0.0;
-    SGMEV_TRY(dev_dot(op, d, q, np, &dq));
-    if (dq == 0.0) break;
-    const double a = delta_new / dq;
-    SGMEV_TRY(dev_axpy(op, np, a, d, x));
+    cg_alpha_kernel<<<kDotBlocks, kDotThreads, 0, op->stream>>>(d, q, np, op->dot_part, sc);
+    op->launches += 1;
     if (it % 50 == 0 && it > 0) {
+      // the true residual every 50 iterations (ConjugateGradients.cpp:99-104)
+      axpy_dev_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, sc, d, x);
       SGMEV_TRY(dev_system(op, prec, x, t, lm));
       sub_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, rhs, t, r);
-      op->launches += 1;
+      cg_update_kernel<<<kDotBlocks, kDotThreads, 0, op->stream>>>(np, d, q, x, r, 0, 1,
+                                                                     op->dot_part, sc);
+      op->launches += 3;
     } else {
-      SGMEV_TRY(dev_axpy(op, np, -a, q, r));
+      cg_update_kernel<<<kDotBlocks, kDotThreads, 0, op->stream>>>(np, d, q, x, r, 1, 0,
+                                                                     op->dot_part, sc);
+      op->launches += 1;
     }
-    const double delta_old = delta_new;
-    SGMEV_TRY(dev_dot(op, r, r, np, &delta_new));
-    const double beta = delta_new / delta_old;
-    xpby_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, r, beta, d);
+    xpby_dev_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, r, sc, d);
     op->launches += 1;
+    SGMEV_CUDA(cudaGetLastError());
+    SGMEV_TRY(read_scalars());
+    // d.q == 0: alpha was 0, so x and r did not move; stop as the reference does before a step
+    if (host[2] == 0.0) break;
+    delta_new = host[0];
     ++it;
   }
   SGMEV_CUDA(cudaGetLastError());
