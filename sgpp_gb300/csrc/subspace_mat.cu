@@ -304,6 +304,8 @@ __device__ __forceinline__ ff reduce4_ff(ff v0, ff v1, ff v2, ff v3, int lane) {
   return b;
 }
 
+// The float-float mult with the structure of mat_mult_kernel: a lane takes subspaces s and s + 32
+// of the same four points, adds their float-float terms and runs one float-float butterfly.
 template <typename CW>
 __global__ void __launch_bounds__(kMatThreads, 1) mat_mult_df_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
@@ -311,12 +313,12 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_mult_df_kernel(
     const float4* __restrict__ phi, const float4* __restrict__ plo,
     const CW* __restrict__ cm, double* __restrict__ out64) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const int sp = mult_at_pad(s_pad);                  // row length of s_at
   float2* s_part = reinterpret_cast<float2*>(smem);  // [warps][kOwnTile]
-  float2* s_at = s_part + kMatWarps * kOwnTile;      // [cmax][s_pad]
+  float2* s_at = s_part + kMatWarps * kOwnTile;      // [cmax][sp]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t cm1 = static_cast<uint32_t>(cmax - 1);
-  for (int k = tid; k < cmax * s_pad; k += blockDim.x) {
-    const int c = k / s_pad, sidx = k - c * s_pad;
+  for (int k = tid; k < cmax * sp; k += blockDim.x) {
+    const int c = k / sp, sidx = k - c * sp;
     float2 a = make_float2(0.0f, 0.0f);
     if (sidx < n_sub) {
       const int4 info = sact[sidx];
@@ -328,41 +330,55 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_mult_df_kernel(
   __syncthreads();
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t gt = tile_begin + tile;
-    for (int s0 = 0; s0 < s_pad; s0 += blockDim.x) {
-      if (s0 + warp * 32 >= s_pad) continue;  // whole warps: s_pad is a multiple of 32
-      const int sid = s0 + tid;
+    for (int s0 = 0; s0 < s_pad; s0 += kMultBlock * kMatWarps) {
+      const int wb = s0 + warp * kMultBlock;
+      if (wb >= s_pad) continue;  // whole warps: s_pad is a multiple of 32
+      const int sid = wb + lane;
+      const bool two = wb + 32 < s_pad;  // warp-uniform
       const int64_t at = gt * kGroups * static_cast<int64_t>(s_pad) + sid;
+      const int64_t at2 = two ? at + 32 : at;  // the first block again, times a zero column
       const float2* a_col = s_at + sid;
+      const float2* a_col2 = a_col + 32;
       float2* part = s_part + warp * kOwnTile;
       const bool first = s0 == 0;
-      float4 rh[kAheadDf], rl[kAheadDf];
-      CW rc[kAheadDf];
+      float4 rh[kAheadDf], rl[kAheadDf], qh[kAheadDf], ql[kAheadDf];
+      CW rc[kAheadDf], qc[kAheadDf];
 #pragma unroll
       for (int u = 0; u < kAheadDf; ++u) {
         rh[u] = __ldcs(phi + at + static_cast<int64_t>(u) * s_pad);
         rl[u] = __ldcs(plo + at + static_cast<int64_t>(u) * s_pad);
         rc[u] = __ldcs(cm + at + static_cast<int64_t>(u) * s_pad);
+        qh[u] = __ldcs(phi + at2 + static_cast<int64_t>(u) * s_pad);
+        ql[u] = __ldcs(plo + at2 + static_cast<int64_t>(u) * s_pad);
+        qc[u] = __ldcs(cm + at2 + static_cast<int64_t>(u) * s_pad);
       }
       for (int g0 = 0; g0 < kGroups; g0 += kAheadDf) {
 #pragma unroll
         for (int u = 0; u < kAheadDf; ++u) {
           const int g = g0 + u;
-          const float4 ph = rh[u], pl = rl[u];
-          const uint32_t cs = rc[u];
+          const float4 ph = rh[u], pl = rl[u], gh = qh[u], gl = ql[u];
+          const uint32_t cs = rc[u], cq = qc[u];
           if (g + kAheadDf < kGroups) {
-            const int64_t k = at + static_cast<int64_t>(g + kAheadDf) * s_pad;
-            rh[u] = __ldcs(phi + k);
-            rl[u] = __ldcs(plo + k);
-            rc[u] = __ldcs(cm + k);
+            const int64_t o = static_cast<int64_t>(g + kAheadDf) * s_pad;
+            rh[u] = __ldcs(phi + at + o);
+            rl[u] = __ldcs(plo + at + o);
+            rc[u] = __ldcs(cm + at + o);
+            qh[u] = __ldcs(phi + at2 + o);
+            ql[u] = __ldcs(plo + at2 + o);
+            qc[u] = __ldcs(cm + at2 + o);
           }
-          const float2 a0 = a_col[min(cell_of<CW>(cs, 0), cm1) * s_pad];
-          const float2 a1 = a_col[min(cell_of<CW>(cs, 1), cm1) * s_pad];
-          const float2 a2 = a_col[min(cell_of<CW>(cs, 2), cm1) * s_pad];
-          const float2 a3 = a_col[min(cell_of<CW>(cs, 3), cm1) * s_pad];
-          const ff r = reduce4_ff(mul_ff(ff{ph.x, pl.x}, ff{a0.x, a0.y}),
-                                  mul_ff(ff{ph.y, pl.y}, ff{a1.x, a1.y}),
-                                  mul_ff(ff{ph.z, pl.z}, ff{a2.x, a2.y}),
-                                  mul_ff(ff{ph.w, pl.w}, ff{a3.x, a3.y}), lane);
+          // cells are below cmax by construction
+          const float ph_[4] = {ph.x, ph.y, ph.z, ph.w}, pl_[4] = {pl.x, pl.y, pl.z, pl.w};
+          const float gh_[4] = {gh.x, gh.y, gh.z, gh.w}, gl_[4] = {gl.x, gl.y, gl.z, gl.w};
+          ff v[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float2 a = a_col[cell_of<CW>(cs, i) * sp];
+            const float2 b2 = a_col2[cell_of<CW>(cq, i) * sp];
+            v[i] = mul_ff(ff{ph_[i], pl_[i]}, ff{a.x, a.y});
+            add_ff(v[i], mul_ff(ff{gh_[i], gl_[i]}, ff{b2.x, b2.y}));
+          }
+          const ff r = reduce4_ff(v[0], v[1], v[2], v[3], lane);
           if ((lane & 7) == 0) {
             float2* dst = part + 4 * g + (lane >> 3);
             ff acc = first ? ff{0.0f, 0.0f} : ff{dst->x, dst->y};
@@ -373,7 +389,8 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_mult_df_kernel(
       }
     }
     __syncthreads();
-    const int wrote = min(kMatWarps, s_pad / 32);
+    // warp w wrote its partials in pass 0 iff w * kMultBlock < s_pad
+    const int wrote = min(kMatWarps, (s_pad + kMultBlock - 1) / kMultBlock);
     for (int jj = tid; jj < kOwnTile; jj += blockDim.x) {
       ff r{0.0f, 0.0f};
       for (int w = 0; w < wrote; ++w) {
@@ -387,16 +404,19 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_mult_df_kernel(
   }
 }
 
-template <typename CW>
+// SACC as in mat_multt_kernel: the flushes go into FP64 sums in shared memory and the row is
+// written once per pass.
+template <typename CW, bool SACC>
 __global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
     const float* __restrict__ vh, const float* __restrict__ vl, int64_t n_tiles,
     const float4* __restrict__ phi, const float4* __restrict__ plo,
     const CW* __restrict__ cm, double* __restrict__ rows) {
   extern __shared__ __align__(16) unsigned char smem[];
-  float2* s_acc = reinterpret_cast<float2*>(smem);  // [cmax][blockDim]
-  double* row = rows + static_cast<int64_t>(blockIdx.x) * total;
   const int tid = threadIdx.x, nth = blockDim.x;
+  double* s_sum = reinterpret_cast<double*>(smem);  // [cmax][blockDim] (SACC)
+  float2* s_acc = reinterpret_cast<float2*>(SACC ? smem + sizeof(double) * cmax * nth : smem);  // [cmax][blockDim]
+  double* row = rows + static_cast<int64_t>(blockIdx.x) * total;
   const uint32_t cm1 = static_cast<uint32_t>(cmax - 1);
   const float4* vh4 = reinterpret_cast<const float4*>(vh);
   const float4* vl4 = reinterpret_cast<const float4*>(vl);
@@ -448,7 +468,7 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
         for (int c = 0; c < info.y; ++c) {
           const float2 a = acc[c * nth];
           const double v = static_cast<double>(a.x) + static_cast<double>(a.y);
-          double* dst = row + offset + c;
+          double* dst = SACC ? s_sum + c * nth + tid : row + offset + c;
           *dst = first ? v : *dst + v;
           acc[c * nth] = make_float2(0.0f, 0.0f);
         }
@@ -456,8 +476,11 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
         since = 0;
       }
     }
-    if (first)
+    if (first) {
       for (int c = 0; c < info.y; ++c) row[offset + c] = 0.0;
+    } else if (SACC) {
+      for (int c = 0; c < info.y; ++c) row[offset + c] = s_sum[c * nth + tid];
+    }
   }
 }
 
@@ -645,11 +668,20 @@ size_t mat_multt_smem(int cmax, int64_t s_pad) {
 }
 
 size_t mat_mult_df_smem(int cmax, int64_t s_pad) {
-  return sizeof(float2) * kMatWarps * kOwnTile + sizeof(float2) * static_cast<size_t>(cmax) * s_pad;
+  return sizeof(float2) * kMatWarps * kOwnTile +
+         sizeof(float2) * static_cast<size_t>(cmax) * mult_at_pad(static_cast<int>(s_pad));
+}
+
+// FP64 flush sums in shared memory while float-float cells and FP64 sums stay within 128 KB (the
+// float-float kernels run one CTA per SM)
+bool mat_multt_df_sacc(int cmax, int64_t s_pad) {
+  return (sizeof(float2) + sizeof(double)) * static_cast<size_t>(cmax) * mat_threads(s_pad) <=
+         128 * 1024;
 }
 
 size_t mat_multt_df_smem(int cmax, int64_t s_pad) {
-  return sizeof(float2) * static_cast<size_t>(cmax) * mat_threads(s_pad);
+  const size_t per = mat_multt_df_sacc(cmax, s_pad) ? sizeof(float2) + sizeof(double) : sizeof(float2);
+  return per * static_cast<size_t>(cmax) * mat_threads(s_pad);
 }
 
 constexpr size_t kMatSmemBudget = 200 * 1024;
@@ -790,7 +822,8 @@ cudaError_t launch_mult_df(const SubPlan& p, cudaStream_t s, int64_t m, double* 
 template <typename CW>
 cudaError_t launch_multt_df(const SubPlan& p, cudaStream_t s, int64_t mpad, const float* vh,
                             const float* vl, int num_sms, int64_t* rows) {
-  auto kern = mat_multt_df_kernel<CW>;
+  auto kern = mat_multt_df_sacc(p.cmax, p.s_pad) ? mat_multt_df_kernel<CW, true>
+                                                 : mat_multt_df_kernel<CW, false>;
   const size_t sm = mat_multt_df_smem(p.cmax, p.s_pad);
   const int nth = mat_threads(p.s_pad);
   cudaError_t e = set_smem_cap(kern, sm);
