@@ -161,19 +161,29 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
         ring2[u] = __ldcs(src2 + static_cast<int64_t>(u) * s_pad);
         cring2[u] = __ldcs(csrc2 + static_cast<int64_t>(u) * s_pad);
       }
+      // refills go through pointers bumped by one row; the last ring's worth of groups of the
+      // tile refills nothing (fetch is uniform over an unrolled ring pass)
+      const PT* nsrc = src + static_cast<int64_t>(A) * s_pad;
+      const CW* ncsrc = csrc + static_cast<int64_t>(A) * s_pad;
+      const PT* nsrc2 = src2 + static_cast<int64_t>(A) * s_pad;
+      const CW* ncsrc2 = csrc2 + static_cast<int64_t>(A) * s_pad;
       for (int g0 = 0; g0 < kGroups; g0 += A) {
+        const bool fetch = g0 + A < kGroups;
 #pragma unroll
         for (int u = 0; u < A; ++u) {
           const int g = g0 + u;
           const float4 p = Prod<HALF>::get(ring[u]);
           const float4 q = Prod<HALF>::get(ring2[u]);
           const uint32_t cs = cring[u], cq = cring2[u];
-          if (g + A < kGroups) {
-            const int64_t o = static_cast<int64_t>(g + A) * s_pad;
-            ring[u] = __ldcs(src + o);
-            cring[u] = __ldcs(csrc + o);
-            ring2[u] = __ldcs(src2 + o);
-            cring2[u] = __ldcs(csrc2 + o);
+          if (fetch) {
+            ring[u] = __ldcs(nsrc);
+            cring[u] = __ldcs(ncsrc);
+            ring2[u] = __ldcs(nsrc2);
+            cring2[u] = __ldcs(ncsrc2);
+            nsrc += s_pad;
+            ncsrc += s_pad;
+            nsrc2 += s_pad;
+            ncsrc2 += s_pad;
           }
           // cells are below cmax by construction (the build writes c < cells of s <= cmax)
           float v0 = a_col[cell_of<CW>(cs, 0) * sp] * p.x;
