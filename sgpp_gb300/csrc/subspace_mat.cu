@@ -18,8 +18,9 @@
 //          the 4 values to 4 per-point sums, which go to per-warp partials in shared memory;
 //          after all passes the partials are added in warp order.
 //   multT: lane s adds v_j * p into its cells ([cell][thread] in shared memory, conflict-free) and
-//          flushes them into the CTA's FP64 row every kFlushTiles tiles; rows are added in CTA
-//          order.
+//          flushes them into FP64 sums every kFlushTiles tiles; rows are added in row order. The
+//          FP16/FP32 kernel gives each pass of subspaces its own CTA: the CTAs of all passes of
+//          one stream of tiles share a row and read the parts of the same product rows together.
 // The float-float variants do the same with float-float products, sums and butterfly.
 // Every sum has a fixed order, so results are the same bit for bit from run to run.
 #include <cuda_fp16.h>
@@ -60,6 +61,31 @@ template <typename CW>
 __device__ __forceinline__ uint32_t cell_of(uint32_t w, int i) {
   constexpr int kBits = sizeof(CW) * 2;
   return (w >> (kBits * i)) & ((1u << kBits) - 1u);
+}
+
+// Streaming loads of the products and cells: each entry is read once per launch, so they skip
+// L1 allocation (ld.global.L1::no_allocate) and leave L1 to the vectors that are re-read.
+__device__ __forceinline__ uint2 ld_stream(const uint2* p) {
+  uint2 v;
+  asm("ld.global.L1::no_allocate.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float4 ld_stream(const float4* p) {
+  float4 v;
+  asm("ld.global.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p));
+  return v;
+}
+__device__ __forceinline__ uint16_t ld_stream(const uint16_t* p) {
+  unsigned short v;
+  asm("ld.global.L1::no_allocate.u16 %0, [%1];" : "=h"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_stream(const uint32_t* p) {
+  uint32_t v;
+  asm("ld.global.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
 }
 
 // ---- mult --------------------------------------------------------------------------------
@@ -226,16 +252,20 @@ template <bool HALF, typename CW, bool SACC>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
     const float* __restrict__ v, int64_t n_tiles, const typename Prod<HALF>::T* __restrict__ pm,
-    const CW* __restrict__ cm, double* __restrict__ rows) {
+    const CW* __restrict__ cm, double* __restrict__ rows, int streams) {
   using PT = typename Prod<HALF>::T;
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, nth = blockDim.x;
   double* s_sum = reinterpret_cast<double*>(smem);  // [cmax][blockDim] (SACC)
   float* s_acc = reinterpret_cast<float*>(SACC ? smem + sizeof(double) * cmax * nth : smem);  // [cmax][blockDim]
-  double* row = rows + static_cast<int64_t>(blockIdx.x) * total;
+  // CTA b takes the subspaces of pass b / streams over the tiles of stream b % streams, so the
+  // CTAs of all passes of a stream read the parts of the same product rows at about the same time
+  const int pass = blockIdx.x / streams, stream = blockIdx.x - pass * streams;
+  const int passes = gridDim.x / streams;
+  double* row = rows + static_cast<int64_t>(stream) * total;
   const uint32_t cm1 = static_cast<uint32_t>(cmax - 1);
   const float4* v4 = reinterpret_cast<const float4*>(v);
-  for (int s0 = 0; s0 < n_sub; s0 += nth) {
+  for (int s0 = pass * nth; s0 < n_sub; s0 += nth * passes) {
     const int sid = s0 + tid;
     if (sid >= n_sub) continue;  // no barriers below: threads run independently
     const int4 info = sact[sid];
@@ -244,7 +274,7 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
     for (int c = 0; c < info.y; ++c) acc[c * nth] = 0.0f;
     bool first = true;
     int since = 0;  // tiles summed in s_acc since the last flush
-    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    for (int64_t tile = stream; tile < n_tiles; tile += streams) {
       const int64_t at = tile * kGroups * static_cast<int64_t>(s_pad) + sid;
       const PT* src = pm + at;
       const CW* csrc = cm + at;
@@ -253,8 +283,8 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
       CW cring[Ahead<HALF>::value];
 #pragma unroll
       for (int u = 0; u < Ahead<HALF>::value; ++u) {
-        ring[u] = __ldcs(src + static_cast<int64_t>(u) * s_pad);
-        cring[u] = __ldcs(csrc + static_cast<int64_t>(u) * s_pad);
+        ring[u] = ld_stream(src + static_cast<int64_t>(u) * s_pad);
+        cring[u] = ld_stream(csrc + static_cast<int64_t>(u) * s_pad);
       }
       for (int g0 = 0; g0 < kGroups; g0 += Ahead<HALF>::value) {
 #pragma unroll
@@ -263,8 +293,8 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
           const float4 p = Prod<HALF>::get(ring[u]);
           const uint32_t cs = cring[u];
           if (g + Ahead<HALF>::value < kGroups) {
-            ring[u] = __ldcs(src + (g + Ahead<HALF>::value) * s_pad);
-            cring[u] = __ldcs(csrc + (g + Ahead<HALF>::value) * s_pad);
+            ring[u] = ld_stream(src + (g + Ahead<HALF>::value) * s_pad);
+            cring[u] = ld_stream(csrc + (g + Ahead<HALF>::value) * s_pad);
           }
           const float4 vv = vt[g];  // the same four values for every lane
           // cells are below cmax by construction
@@ -275,7 +305,7 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
         }
       }
       ++since;
-      if (since == kFlushTiles || tile + gridDim.x >= n_tiles) {
+      if (since == kFlushTiles || tile + streams >= n_tiles) {
         for (int c = 0; c < info.y; ++c) {
           double* dst = SACC ? s_sum + c * nth + tid : row + offset + c;
           *dst = first ? static_cast<double>(acc[c * nth]) : *dst + static_cast<double>(acc[c * nth]);
@@ -880,10 +910,15 @@ cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, const typename Pr
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
   if (e != cudaSuccess) return e;
   const int64_t nt = mpad / kOwnTile;
-  *rows = std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms), std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1)));
-  kern<<<static_cast<unsigned>(*rows), nth, sm, s>>>(p.sact, p.n_sub, static_cast<int>(p.s_pad),
-                                                     p.cmax, static_cast<int>(p.total), v32, nt,
-                                                     pm, static_cast<const CW*>(p.cmat), p.rows);
+  // one CTA per (stream, pass): the resident CTAs split into passes, each stream a row
+  const int64_t passes = (p.n_sub + nth - 1) / nth;
+  const int64_t streams = std::max<int64_t>(
+      1, std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms) / passes,
+                           std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1))));
+  *rows = streams;
+  kern<<<static_cast<unsigned>(streams * passes), nth, sm, s>>>(
+      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), v32, nt, pm,
+      static_cast<const CW*>(p.cmat), p.rows, static_cast<int>(streams));
   return cudaGetLastError();
 }
 }  // namespace
