@@ -823,9 +823,10 @@ static bool mat_ready(sgmev_op* op) {
     dev_free(op->sub.pmat_lo, op->stream);
     dev_free(op->sub.pmat16, op->stream);
     dev_free(op->sub.cmat, op->stream);
+    dev_free(op->sub.cpair, op->stream);
     op->sub.pmat = op->sub.pmat_lo = nullptr;
     op->sub.pmat16 = nullptr;
-    op->sub.cmat = nullptr;
+    op->sub.cmat = op->sub.cpair = nullptr;
     op->mat_failed = true;
     return false;
   }

@@ -604,7 +604,7 @@ template <int DIM, bool MOD>
 __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_mat_build_kernel(
     const int4* __restrict__ desc, const int4* __restrict__ sinfo, int n_sub, int s_pad,
     const float* __restrict__ xh_t, const float* __restrict__ xl_t, int64_t mpad, int64_t m,
-    int64_t n_tiles, float4* __restrict__ phi, float4* __restrict__ plo, uint2* __restrict__ p16,
+    int64_t n_tiles, float4* __restrict__ phi, float4* __restrict__ plo, uint4* __restrict__ p16,
     uint32_t* __restrict__ cm) {
   using Lay = OwnLayout<DIM, true>;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -685,8 +685,11 @@ __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_mat_build_kernel(
         phi[k] = make_float4(hv[0], hv[1], hv[2], hv[3]);
         plo[k] = make_float4(lv[0], lv[1], lv[2], lv[3]);
         const __half2 h01 = __floats2half2_rn(hv[0], hv[1]), h23 = __floats2half2_rn(hv[2], hv[3]);
-        p16[k] = make_uint2(*reinterpret_cast<const uint32_t*>(&h01),
-                            *reinterpret_cast<const uint32_t*>(&h23));
+        // FP16 copy by pairs of groups: group gg is half gg % 2 of pair gg / 2
+        const int64_t gg = tile * kGroupsPerTile + g;
+        reinterpret_cast<uint2*>(p16 + (gg >> 1) * s_pad + sid)[gg & 1] =
+            make_uint2(*reinterpret_cast<const uint32_t*>(&h01),
+                       *reinterpret_cast<const uint32_t*>(&h23));
         cm[k] = cells;
       }
     }
@@ -1197,8 +1200,8 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
 void subspace_free(SubPlan* p) {
   const cudaStream_t st = p->stream;
   void* ptrs[] = {p->desc, p->sinfo, p->act,  p->sact,    p->pmat,  p->pmat_lo, p->pmat16,
-                  p->cmat, p->rows,  p->base, p->pos,     p->asub,  p->asub2,   p->acc,
-                  p->maxbits};
+                  p->cmat, p->cpair, p->rows, p->base, p->pos,  p->asub,    p->asub2,
+                  p->acc,  p->maxbits};
   for (void* q : ptrs) dev_free(q, st);
   *p = SubPlan{};
 }

@@ -53,8 +53,13 @@ struct SubPlan {
   // built
   float4* pmat = nullptr;
   float4* pmat_lo = nullptr;
-  uint2* pmat16 = nullptr;  // the same products rounded to FP16 (four halves per entry)
+  // the same products rounded to FP16 by pairs of point groups: P16[j / 8][s] holds the eight
+  // halves of points 8 (j / 8) .. 8 (j / 8) + 7, so the FP16 kernels load two groups at once
+  uint4* pmat16 = nullptr;
   void* cmat = nullptr;  // cell words: uint32_t (a byte per point) or uint16_t (a nibble)
+  // the cell words by pairs of point groups, C2[j / 8][s] (two uint16_t words in a uint32_t, or
+  // two uint32_t in a uint2), for the FP16 kernels
+  void* cpair = nullptr;
   int cell_bits = 8;     // 8 or 4 bits per cell in cmat
   int64_t s_pad = 0;
   int64_t mat_mpad = 0;
@@ -104,7 +109,8 @@ cudaError_t subspace_finish_rows(const SubPlan& p, cudaStream_t s, int64_t nrows
                                  double* out64, const double* add, double scale_add);
 cudaError_t subspace_scatter_alpha_df(const SubPlan& p, cudaStream_t s, const float* ah,
                                       const float* al);
-// fills pmat, pmat_lo, pmat16 and cmat (allocated, s_pad set) from the float-float data (xh, xl)
+// fills pmat, pmat_lo, pmat16 and cmat (allocated, s_pad set) from the float-float data (xh, xl);
+// cpair is derived from cmat afterwards
 cudaError_t subspace_mat_build(const SubPlan& p, cudaStream_t s, const float* xh,
                                const float* xl, int64_t mpad, int64_t m, int num_sms);
 

@@ -5,9 +5,11 @@
 // and kept in HBM as
 //     P_hi[g][s], P_lo[g][s] : float4, the products of points 4g .. 4g+3 as float-float pairs
 //     C[g][s]                : uint32, their cell indices, one byte each
-// with s padded to a multiple of 32 (padded entries 0). The FP32 mult and multTranspose stream
-// P_hi and C (5 bytes per point and subspace), the FP64-accurate ones all three (9 bytes); none
-// touches a coordinate, so they are bounded by HBM bandwidth rather than the hat arithmetic.
+// with s padded to a multiple of 32 (padded entries 0), and for the inner solves of mixed fits an
+// FP16 copy of P_hi with the cell words, laid out by pairs of point groups (see the FP16 section).
+// The FP32 mult and multTranspose stream P_hi and C (5 bytes per point and subspace), the
+// FP64-accurate ones all three (9 bytes), the FP16 ones the copy (3); none touches a coordinate,
+// so they are bounded by HBM bandwidth rather than the hat arithmetic.
 // Points outside the domain have P = 0 (and cell 0), so they need no test.
 //
 // Both kernels are owner-computes: thread k of a pass owns subspace s = pass * blockDim + k and
@@ -45,11 +47,6 @@ constexpr int kMatMaxCells = 256;             // cell indices are stored in one 
 // point groups in flight per thread: a ring of loads issued this many groups ahead of their use
 // (fewer for the float-float kernels, whose arithmetic holds more registers)
 constexpr int kAhead = 4, kAheadDf = 2;
-// FP16 products take 8 bytes per group instead of 16: a deeper ring keeps as many bytes in flight
-template <bool HALF>
-struct Ahead {
-  static constexpr int value = HALF ? 8 : kAhead;
-};
 static_assert(kGroups % kAhead == 0 && kGroups % kAheadDf == 0, "the ring must divide a tile");
 // multT: FP32 sums over this many tiles (1024 points) before they go into the FP64 row
 constexpr int kFlushTiles = 4;
@@ -74,6 +71,13 @@ __device__ __forceinline__ float4 ld_stream(const float4* p) {
   float4 v;
   asm("ld.global.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
       : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p));
+  return v;
+}
+__device__ __forceinline__ uint4 ld_stream(const uint4* p) {
+  uint4 v;
+  asm("ld.global.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+      : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
       : "l"(p));
   return v;
 }
@@ -105,45 +109,33 @@ __device__ __forceinline__ float reduce4(float v0, float v1, float v2, float v3,
   return b;
 }
 
-// products of a point group as stored: FP32 (float4) or FP16 (four halves in a uint2)
-template <bool HALF>
-struct Prod {
-  using T = float4;
-  static __device__ __forceinline__ float4 get(float4 v) { return v; }
-};
-template <>
-struct Prod<true> {
-  using T = uint2;
-  static __device__ __forceinline__ float4 get(uint2 v) {
-    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&v.x));
-    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&v.y));
-    return make_float4(a.x, a.y, b.x, b.y);
-  }
-};
+// four FP16 products (two half2 words) as floats
+__device__ __forceinline__ float4 halves4(uint32_t lo, uint32_t hi) {
+  const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&lo));
+  const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&hi));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
 
 // mult: a lane takes subspaces s and s + 32 of the same four points (two 32-wide blocks per
 // warp), adds their four terms in registers and then runs one butterfly, so the butterfly's
 // cost is shared by two subspaces. A warp whose second block lies beyond s_pad reads its first
 // block twice and multiplies the copy by a zero column of alpha (s_at is kMultBlock-padded).
 constexpr int kMultBlock = 64;  // subspaces per warp and pass
-template <bool HALF>
-struct Ahead2 {
-  static constexpr int value = HALF ? 4 : 2;  // the same bytes in flight as one block at Ahead
-};
+constexpr int kAhead2 = 2;  // groups in flight per block: the bytes of one block at kAhead
 static_assert(kGroups % 4 == 0 && kGroups % 2 == 0, "the ring must divide a tile");
 
 __host__ __device__ constexpr int mult_at_pad(int s_pad) {
   return (s_pad + kMultBlock - 1) / kMultBlock * kMultBlock;
 }
 
-template <bool HALF, typename CW>
+template <typename CW>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
     const float* __restrict__ asub, int64_t m, int64_t tile_begin, int64_t n_tiles,
-    const typename Prod<HALF>::T* __restrict__ pm, const CW* __restrict__ cm,
-    float* __restrict__ out32, double* __restrict__ out64) {
-  using PT = typename Prod<HALF>::T;
-  constexpr int A = Ahead2<HALF>::value;
+    const float4* __restrict__ pm, const CW* __restrict__ cm, float* __restrict__ out32,
+    double* __restrict__ out64) {
+  using PT = float4;
+  constexpr int A = kAhead2;
   extern __shared__ __align__(16) unsigned char smem[];
   const int sp = mult_at_pad(s_pad);                // row length of s_at
   float* s_part = reinterpret_cast<float*>(smem);   // [warps][kOwnTile]
@@ -198,8 +190,8 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
 #pragma unroll
         for (int u = 0; u < A; ++u) {
           const int g = g0 + u;
-          const float4 p = Prod<HALF>::get(ring[u]);
-          const float4 q = Prod<HALF>::get(ring2[u]);
+          const float4 p = ring[u];
+          const float4 q = ring2[u];
           const uint32_t cs = cring[u], cq = cring2[u];
           if (fetch) {
             ring[u] = __ldcs(nsrc);
@@ -248,12 +240,13 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
 // cells), and the CTA's row is written once per pass: the same additions in the same order as
 // flushing into the row itself, without a read-modify-write of global memory per flush (the
 // flushes were a tenth of the kernel's time). Used when both arrays leave room for two CTAs per SM.
-template <bool HALF, typename CW, bool SACC>
+template <typename CW, bool SACC>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
-    const float* __restrict__ v, int64_t n_tiles, const typename Prod<HALF>::T* __restrict__ pm,
+    const float* __restrict__ v, int64_t n_tiles, const float4* __restrict__ pm,
     const CW* __restrict__ cm, double* __restrict__ rows, int streams) {
-  using PT = typename Prod<HALF>::T;
+  using PT = float4;
+  constexpr int A = kAhead;
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, nth = blockDim.x;
   double* s_sum = reinterpret_cast<double*>(smem);  // [cmax][blockDim] (SACC)
@@ -263,7 +256,6 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
   const int pass = blockIdx.x / streams, stream = blockIdx.x - pass * streams;
   const int passes = gridDim.x / streams;
   double* row = rows + static_cast<int64_t>(stream) * total;
-  const uint32_t cm1 = static_cast<uint32_t>(cmax - 1);
   const float4* v4 = reinterpret_cast<const float4*>(v);
   for (int s0 = pass * nth; s0 < n_sub; s0 += nth * passes) {
     const int sid = s0 + tid;
@@ -279,22 +271,22 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
       const PT* src = pm + at;
       const CW* csrc = cm + at;
       const float4* vt = v4 + tile * kGroups;
-      PT ring[Ahead<HALF>::value];
-      CW cring[Ahead<HALF>::value];
+      PT ring[A];
+      CW cring[A];
 #pragma unroll
-      for (int u = 0; u < Ahead<HALF>::value; ++u) {
+      for (int u = 0; u < A; ++u) {
         ring[u] = ld_stream(src + static_cast<int64_t>(u) * s_pad);
         cring[u] = ld_stream(csrc + static_cast<int64_t>(u) * s_pad);
       }
-      for (int g0 = 0; g0 < kGroups; g0 += Ahead<HALF>::value) {
+      for (int g0 = 0; g0 < kGroups; g0 += A) {
 #pragma unroll
-        for (int u = 0; u < Ahead<HALF>::value; ++u) {
+        for (int u = 0; u < A; ++u) {
           const int g = g0 + u;
-          const float4 p = Prod<HALF>::get(ring[u]);
+          const float4 p = ring[u];
           const uint32_t cs = cring[u];
-          if (g + Ahead<HALF>::value < kGroups) {
-            ring[u] = ld_stream(src + (g + Ahead<HALF>::value) * s_pad);
-            cring[u] = ld_stream(csrc + (g + Ahead<HALF>::value) * s_pad);
+          if (g + A < kGroups) {
+            ring[u] = ld_stream(src + (g + A) * s_pad);
+            cring[u] = ld_stream(csrc + (g + A) * s_pad);
           }
           const float4 vv = vt[g];  // the same four values for every lane
           // cells are below cmax by construction
@@ -316,6 +308,221 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
       }
     }
     if (first) {  // no tile for this CTA: its row holds zeros
+      for (int c = 0; c < info.y; ++c) row[offset + c] = 0.0;
+    } else if (SACC) {
+      for (int c = 0; c < info.y; ++c) row[offset + c] = s_sum[c * nth + tid];
+    }
+  }
+}
+
+// ---- FP16 products by pairs of point groups -------------------------------------------------
+// The inner solves of mixed fits stream the FP16 copy of the products, P16[k][s] (uint4: the eight
+// halves of points 8k .. 8k + 7, point groups 2k and 2k + 1), with the cell words of the same
+// pair, C2[k][s] (PairCells). A lane loads 16 bytes of products and 4 (nibble cells) or 8 (byte
+// cells) bytes of cells per two groups: half the memory requests of one load per group, for the
+// same bytes (0.483 -> 0.444 ms for B a and 0.561 -> 0.540 ms for B^T v on the benchmark
+// workload). The arithmetic and its order are those of the [g][s] kernels above.
+constexpr int kPairs = kGroups / 2;  // pairs of point groups per tile
+
+template <typename CW>
+struct PairCells;
+template <>
+struct PairCells<uint16_t> {  // two nibble words in one uint32_t, group 2k in the low half
+  using T = uint32_t;
+  static __device__ __forceinline__ uint32_t word(uint32_t w, int h) { return h ? w >> 16 : w; }
+};
+template <>
+struct PairCells<uint32_t> {  // two byte words
+  using T = uint2;
+  static __device__ __forceinline__ uint32_t word(uint2 w, int h) { return h ? w.y : w.x; }
+};
+
+constexpr int kPairAheadMult = 2;   // pairs in flight per block: the 4 groups of the FP16 ring
+constexpr int kPairAheadMultT = 4;  // pairs in flight: 8 groups
+static_assert(kPairs % kPairAheadMult == 0 && kPairs % kPairAheadMultT == 0,
+              "the ring must divide a tile");
+
+// mat_mult_kernel on the pair layout: a lane takes subspaces s and s + 32, two point groups per
+// ring slot
+template <typename CW>
+__global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
+    const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
+    const float* __restrict__ asub, int64_t m, int64_t tile_begin, int64_t n_tiles,
+    const uint4* __restrict__ pp, const typename PairCells<CW>::T* __restrict__ cp,
+    float* __restrict__ out32, double* __restrict__ out64) {
+  using PC = PairCells<CW>;
+  using CT = typename PC::T;
+  constexpr int A = kPairAheadMult;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sp = mult_at_pad(s_pad);
+  float* s_part = reinterpret_cast<float*>(smem);   // [warps][kOwnTile]
+  float* s_at = s_part + kMatWarps * kOwnTile;      // [cmax][sp] alpha by (cell, subspace)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int k = tid; k < cmax * sp; k += blockDim.x) {
+    const int c = k / sp, sidx = k - c * sp;
+    float a = 0.0f;
+    if (sidx < n_sub) {
+      const int4 info = sact[sidx];
+      const int off = static_cast<int>(static_cast<uint32_t>(info.x) - static_cast<uint32_t>(info.z));
+      if (c < info.y) a = asub[off + c];
+    }
+    s_at[k] = a;
+  }
+  __syncthreads();
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t gt = tile_begin + tile;
+    for (int s0 = 0; s0 < s_pad; s0 += kMultBlock * kMatWarps) {
+      const int wb = s0 + warp * kMultBlock;
+      if (wb >= s_pad) continue;
+      const int sid = wb + lane;
+      const bool two = wb + 32 < s_pad;
+      const int64_t at = gt * kPairs * static_cast<int64_t>(s_pad) + sid;
+      const uint4* src = pp + at;
+      const CT* csrc = cp + at;
+      const uint4* src2 = two ? src + 32 : src;
+      const CT* csrc2 = two ? csrc + 32 : csrc;
+      const float* a_col = s_at + sid;
+      const float* a_col2 = a_col + 32;  // zeros when the second block is absent
+      float* part = s_part + warp * kOwnTile;
+      const bool first = s0 == 0;
+      uint4 ring[A], ring2[A];
+      CT cring[A], cring2[A];
+#pragma unroll
+      for (int u = 0; u < A; ++u) {
+        ring[u] = ld_stream(src + static_cast<int64_t>(u) * s_pad);
+        cring[u] = ld_stream(csrc + static_cast<int64_t>(u) * s_pad);
+        ring2[u] = ld_stream(src2 + static_cast<int64_t>(u) * s_pad);
+        cring2[u] = ld_stream(csrc2 + static_cast<int64_t>(u) * s_pad);
+      }
+      const uint4* nsrc = src + static_cast<int64_t>(A) * s_pad;
+      const CT* ncsrc = csrc + static_cast<int64_t>(A) * s_pad;
+      const uint4* nsrc2 = src2 + static_cast<int64_t>(A) * s_pad;
+      const CT* ncsrc2 = csrc2 + static_cast<int64_t>(A) * s_pad;
+      for (int k0 = 0; k0 < kPairs; k0 += A) {
+        const bool fetch = k0 + A < kPairs;
+#pragma unroll
+        for (int u = 0; u < A; ++u) {
+          const int k = k0 + u;
+          const uint4 pw = ring[u], qw = ring2[u];
+          const CT cs = cring[u], cq = cring2[u];
+          if (fetch) {
+            ring[u] = ld_stream(nsrc);
+            cring[u] = ld_stream(ncsrc);
+            ring2[u] = ld_stream(nsrc2);
+            cring2[u] = ld_stream(ncsrc2);
+            nsrc += s_pad;
+            ncsrc += s_pad;
+            nsrc2 += s_pad;
+            ncsrc2 += s_pad;
+          }
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float4 p = h ? halves4(pw.z, pw.w) : halves4(pw.x, pw.y);
+            const float4 q = h ? halves4(qw.z, qw.w) : halves4(qw.x, qw.y);
+            const uint32_t ws = PC::word(cs, h), wq = PC::word(cq, h);
+            float v0 = a_col[cell_of<CW>(ws, 0) * sp] * p.x;
+            float v1 = a_col[cell_of<CW>(ws, 1) * sp] * p.y;
+            float v2 = a_col[cell_of<CW>(ws, 2) * sp] * p.z;
+            float v3 = a_col[cell_of<CW>(ws, 3) * sp] * p.w;
+            v0 = fmaf(a_col2[cell_of<CW>(wq, 0) * sp], q.x, v0);
+            v1 = fmaf(a_col2[cell_of<CW>(wq, 1) * sp], q.y, v1);
+            v2 = fmaf(a_col2[cell_of<CW>(wq, 2) * sp], q.z, v2);
+            v3 = fmaf(a_col2[cell_of<CW>(wq, 3) * sp], q.w, v3);
+            const float r = reduce4(v0, v1, v2, v3, lane);
+            if ((lane & 7) == 0) {
+              float* dst = part + 4 * (2 * k + h) + (lane >> 3);
+              *dst = first ? r : *dst + r;
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const int wrote = min(kMatWarps, (s_pad + kMultBlock - 1) / kMultBlock);
+    for (int jj = tid; jj < kOwnTile; jj += blockDim.x) {
+      float r = 0.0f;
+      for (int w = 0; w < wrote; ++w) r += s_part[w * kOwnTile + jj];
+      const int64_t j = gt * kOwnTile + jj;
+      const float v = j < m ? r : 0.0f;
+      if (out32) out32[j] = v;
+      if (out64) out64[j] = static_cast<double>(v);
+    }
+    __syncthreads();  // the partials are read before the next tile overwrites them
+  }
+}
+
+// mat_multt_kernel on the pair layout
+template <typename CW, bool SACC>
+__global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
+    const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
+    const float* __restrict__ v, int64_t n_tiles, const uint4* __restrict__ pp,
+    const typename PairCells<CW>::T* __restrict__ cp, double* __restrict__ rows, int streams) {
+  using PC = PairCells<CW>;
+  using CT = typename PC::T;
+  constexpr int A = kPairAheadMultT;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x, nth = blockDim.x;
+  double* s_sum = reinterpret_cast<double*>(smem);  // [cmax][blockDim] (SACC)
+  float* s_acc = reinterpret_cast<float*>(SACC ? smem + sizeof(double) * cmax * nth : smem);
+  const int pass = blockIdx.x / streams, stream = blockIdx.x - pass * streams;
+  const int passes = gridDim.x / streams;
+  double* row = rows + static_cast<int64_t>(stream) * total;
+  const float4* v4 = reinterpret_cast<const float4*>(v);
+  for (int s0 = pass * nth; s0 < n_sub; s0 += nth * passes) {
+    const int sid = s0 + tid;
+    if (sid >= n_sub) continue;  // no barriers below: threads run independently
+    const int4 info = sact[sid];
+    const uint32_t offset = static_cast<uint32_t>(info.x) - static_cast<uint32_t>(info.z);
+    float* acc = s_acc + tid;
+    for (int c = 0; c < info.y; ++c) acc[c * nth] = 0.0f;
+    bool first = true;
+    int since = 0;
+    for (int64_t tile = stream; tile < n_tiles; tile += streams) {
+      const int64_t at = tile * kPairs * static_cast<int64_t>(s_pad) + sid;
+      const uint4* src = pp + at;
+      const CT* csrc = cp + at;
+      const float4* vt = v4 + tile * kGroups;
+      uint4 ring[A];
+      CT cring[A];
+#pragma unroll
+      for (int u = 0; u < A; ++u) {
+        ring[u] = ld_stream(src + static_cast<int64_t>(u) * s_pad);
+        cring[u] = ld_stream(csrc + static_cast<int64_t>(u) * s_pad);
+      }
+      for (int k0 = 0; k0 < kPairs; k0 += A) {
+#pragma unroll
+        for (int u = 0; u < A; ++u) {
+          const int k = k0 + u;
+          const uint4 pw = ring[u];
+          const CT cs = cring[u];
+          if (k + A < kPairs) {
+            ring[u] = ld_stream(src + (k + A) * s_pad);
+            cring[u] = ld_stream(csrc + (k + A) * s_pad);
+          }
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float4 p = h ? halves4(pw.z, pw.w) : halves4(pw.x, pw.y);
+            const uint32_t w = PC::word(cs, h);
+            const float4 vv = vt[2 * k + h];  // the same four values for every lane
+            acc[cell_of<CW>(w, 0) * nth] += vv.x * p.x;
+            acc[cell_of<CW>(w, 1) * nth] += vv.y * p.y;
+            acc[cell_of<CW>(w, 2) * nth] += vv.z * p.z;
+            acc[cell_of<CW>(w, 3) * nth] += vv.w * p.w;
+          }
+        }
+      }
+      ++since;
+      if (since == kFlushTiles || tile + streams >= n_tiles) {
+        for (int c = 0; c < info.y; ++c) {
+          double* dst = SACC ? s_sum + c * nth + tid : row + offset + c;
+          *dst = first ? static_cast<double>(acc[c * nth]) : *dst + static_cast<double>(acc[c * nth]);
+          acc[c * nth] = 0.0f;
+        }
+        first = false;
+        since = 0;
+      }
+    }
+    if (first) {
       for (int c = 0; c < info.y; ++c) row[offset + c] = 0.0;
     } else if (SACC) {
       for (int c = 0; c < info.y; ++c) row[offset + c] = s_sum[c * nth + tid];
@@ -742,83 +949,111 @@ bool subspace_mat_fits(const SubPlan& p, bool df) {
 bool mat_cell4(const SubPlan& p) { return p.cmax <= 16; }
 
 int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad) {
-  // P_hi, P_lo (4 + 4 bytes), the FP16 copy (2) and the cells (1 byte, or a nibble; during the
-  // build the byte cells and the nibbles coexist)
-  const double per = 2 * sizeof(float) + 2 + (mat_cell4(p) ? 1.5 : 1.0);
+  // P_hi, P_lo (4 + 4 bytes), the FP16 copy (2) and the cells: byte cells (1) and their pair copy
+  // (1), or during the build the byte cells beside the nibbles (0.5) and their pair copy (0.5)
+  const double per = 2 * sizeof(float) + 2 + 2.0;
   return static_cast<int64_t>(static_cast<double>(mpad) * ((p.n_sub + 31) / 32 * 32) * per);
 }
 
 namespace {
-// byte cells -> nibble cells (four per uint16)
-__global__ void pack_cells_kernel(const uint32_t* __restrict__ in, int64_t n,
-                                  uint16_t* __restrict__ out) {
-  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
-       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const uint32_t w = in[k];
-    out[k] = static_cast<uint16_t>((w & 0xFu) | ((w >> 4) & 0xF0u) | ((w >> 8) & 0xF00u) |
-                                   ((w >> 12) & 0xF000u));
+// byte cells [g][s] -> nibble cells [g][s] (four per uint16) and their pair copy [g / 2][s] (two
+// nibble words per uint32)
+__global__ void pack_cells_kernel(const uint32_t* __restrict__ in, int64_t n_pairs, int s_pad,
+                                  uint16_t* __restrict__ out, uint32_t* __restrict__ pair) {
+  const int64_t n = n_pairs * s_pad;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t k = e / s_pad;
+    const int64_t a = e + k * s_pad;  // group 2k of the same subspace, then group 2k + 1
+    uint32_t nib[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint32_t w = in[a + h * s_pad];
+      nib[h] = (w & 0xFu) | ((w >> 4) & 0xF0u) | ((w >> 8) & 0xF00u) | ((w >> 12) & 0xF000u);
+      out[a + h * s_pad] = static_cast<uint16_t>(nib[h]);
+    }
+    pair[e] = nib[0] | (nib[1] << 16);
+  }
+}
+
+// byte cells [g][s] -> their pair copy [g / 2][s] (two words per uint2)
+__global__ void pair_cells_kernel(const uint32_t* __restrict__ in, int64_t n_pairs, int s_pad,
+                                  uint2* __restrict__ pair) {
+  const int64_t n = n_pairs * s_pad;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t a = e + (e / s_pad) * s_pad;
+    pair[e] = make_uint2(in[a], in[a + s_pad]);
   }
 }
 }  // namespace
 
 cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, const float* xl,
                                  int64_t mpad, int64_t m, int num_sms) {
-  dev_free(p->pmat, s);
-  dev_free(p->pmat_lo, s);
-  dev_free(p->pmat16, s);
-  dev_free(p->cmat, s);
-  p->pmat = p->pmat_lo = nullptr;
-  p->pmat16 = nullptr;
-  p->cmat = nullptr;
+  auto release = [&](uint32_t* cm8) {
+    dev_free(p->pmat, s);
+    dev_free(p->pmat_lo, s);
+    dev_free(p->pmat16, s);
+    dev_free(p->cpair, s);
+    if (cm8 != p->cmat) dev_free(cm8, s);
+    dev_free(p->cmat, s);
+    p->pmat = p->pmat_lo = nullptr;
+    p->pmat16 = nullptr;
+    p->cmat = p->cpair = nullptr;
+  };
+  release(nullptr);  // a previous build of this plan
   p->cell_bits = 8;
   p->s_pad = (p->n_sub + 31) / 32 * 32;
   p->mat_mpad = mpad;
   const size_t entries = static_cast<size_t>(mpad / 4) * static_cast<size_t>(p->s_pad);
+  const int64_t n_pairs = mpad / 8;  // mpad is a multiple of the tile (256 points)
   uint32_t* cm8 = nullptr;
-  auto release = [&]() {
-    dev_free(p->pmat, s);
-    dev_free(p->pmat_lo, s);
-    dev_free(p->pmat16, s);
-    dev_free(cm8, s);
-    p->pmat = p->pmat_lo = nullptr;
-    p->pmat16 = nullptr;
-    p->cmat = nullptr;
-    (void)cudaGetLastError();
-  };
   cudaError_t e = dev_malloc(&p->pmat, entries * sizeof(float4), s);
   if (e == cudaSuccess) e = dev_malloc(&p->pmat_lo, entries * sizeof(float4), s);
-  if (e == cudaSuccess) e = dev_malloc(&p->pmat16, entries * sizeof(uint2), s);
+  if (e == cudaSuccess) e = dev_malloc(&p->pmat16, entries / 2 * sizeof(uint4), s);
   if (e == cudaSuccess) e = dev_malloc(&cm8, entries * sizeof(uint32_t), s);
   if (e != cudaSuccess) {
-    release();
+    release(cm8);
+    (void)cudaGetLastError();
     return e;
   }
   p->cmat = cm8;
   e = subspace_mat_build(*p, s, xh, xl, mpad, m, num_sms);
-  if (e != cudaSuccess) {
-    release();
-    return e;
-  }
-  if (mat_cell4(*p)) {
+  const unsigned blocks = static_cast<unsigned>(std::min<int64_t>(
+      16 * num_sms, std::max<int64_t>(1, (n_pairs * p->s_pad + 255) / 256)));
+  if (e == cudaSuccess && mat_cell4(*p)) {
+    // nibble cells, and their pair copy for the FP16 kernels (0.5 + 0.5 byte per entry)
     uint16_t* cm4 = nullptr;
+    uint32_t* cp = nullptr;
     e = dev_malloc(&cm4, entries * sizeof(uint16_t), s);
-    if (e != cudaSuccess) {
-      // keep the byte cells: every kernel reads either form
-      (void)cudaGetLastError();
-      return cudaSuccess;
+    if (e == cudaSuccess) e = dev_malloc(&cp, entries / 2 * sizeof(uint32_t), s);
+    if (e == cudaSuccess) {
+      pack_cells_kernel<<<blocks, 256, 0, s>>>(cm8, n_pairs, static_cast<int>(p->s_pad), cm4, cp);
+      e = cudaGetLastError();
     }
-    const unsigned blocks = static_cast<unsigned>(std::min<int64_t>(
-        16 * num_sms, std::max<int64_t>(1, (static_cast<int64_t>(entries) + 255) / 256)));
-    pack_cells_kernel<<<blocks, 256, 0, s>>>(cm8, static_cast<int64_t>(entries), cm4);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) {
+    if (e == cudaSuccess) {
+      dev_free(cm8, s);
+      p->cmat = cm4;
+      p->cpair = cp;
+      p->cell_bits = 4;
+    } else {
       dev_free(cm4, s);
-      release();
-      return e;
+      dev_free(cp, s);
     }
-    dev_free(cm8, s);
-    p->cmat = cm4;
-    p->cell_bits = 4;
+  } else if (e == cudaSuccess) {
+    uint2* cp = nullptr;
+    e = dev_malloc(&cp, entries / 2 * sizeof(uint2), s);
+    if (e == cudaSuccess) {
+      pair_cells_kernel<<<blocks, 256, 0, s>>>(cm8, n_pairs, static_cast<int>(p->s_pad), cp);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) p->cpair = cp;
+    else dev_free(cp, s);
+  }
+  if (e != cudaSuccess) {
+    release(cm8);
+    (void)cudaGetLastError();
+    return e;
   }
   return cudaSuccess;
 }
@@ -879,47 +1114,66 @@ cudaError_t launch_multt_df(const SubPlan& p, cudaStream_t s, int64_t mpad, cons
   return cudaGetLastError();
 }
 
+// HALF: the FP16 kernels on the pair layout (pmat16, cpair), else the FP32 ones ([g][s]: pmat, cmat)
 template <bool HALF, typename CW>
-cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, const typename Prod<HALF>::T* pm,
-                            int64_t m, float* out32, double* out64, int64_t t0, int64_t nt,
-                            int num_sms) {
-  auto kern = mat_mult_kernel<HALF, CW>;
+cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, int64_t m, float* out32,
+                            double* out64, int64_t t0, int64_t nt, int num_sms) {
   const size_t sm = mat_mult_smem(p.cmax, p.s_pad);
-  cudaError_t e = set_smem_cap(kern, sm);
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMatThreads, sm);
-  if (e != cudaSuccess) return e;
-  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
-  kern<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
-      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub, m, t0, nt, pm,
-      static_cast<const CW*>(p.cmat), out32, out64);
-  return cudaGetLastError();
+  auto go = [&](auto kern, auto pm, auto cm) -> cudaError_t {
+    cudaError_t e = set_smem_cap(kern, sm);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMatThreads, sm);
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = std::max<int64_t>(
+        1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
+    kern<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
+        p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub, m, t0, nt, pm, cm, out32,
+        out64);
+    return cudaGetLastError();
+  };
+  if constexpr (HALF)
+    return go(mat_mult_half_kernel<CW>, static_cast<const uint4*>(p.pmat16),
+              static_cast<const typename PairCells<CW>::T*>(p.cpair));
+  else
+    return go(mat_mult_kernel<CW>, static_cast<const float4*>(p.pmat),
+              static_cast<const CW*>(p.cmat));
 }
 
 template <bool HALF, typename CW>
-cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, const typename Prod<HALF>::T* pm,
-                             int64_t mpad, const float* v32, int num_sms, int64_t* rows) {
-  auto kern = mat_multt_sacc(p.cmax, p.s_pad) ? mat_multt_kernel<HALF, CW, true>
-                                              : mat_multt_kernel<HALF, CW, false>;
+cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, int64_t mpad, const float* v32,
+                             int num_sms, int64_t* rows) {
   const size_t sm = mat_multt_smem(p.cmax, p.s_pad);
   const int nth = mat_threads(p.s_pad);
-  cudaError_t e = set_smem_cap(kern, sm);
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
-  if (e != cudaSuccess) return e;
-  const int64_t nt = mpad / kOwnTile;
-  // one CTA per (stream, pass): the resident CTAs split into passes, each stream a row
-  const int64_t passes = (p.n_sub + nth - 1) / nth;
-  const int64_t streams = std::max<int64_t>(
-      1, std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms) / passes,
-                           std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1))));
-  *rows = streams;
-  kern<<<static_cast<unsigned>(streams * passes), nth, sm, s>>>(
-      p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), v32, nt, pm,
-      static_cast<const CW*>(p.cmat), p.rows, static_cast<int>(streams));
-  return cudaGetLastError();
+  const bool sacc = mat_multt_sacc(p.cmax, p.s_pad);
+  auto go = [&](auto kern, auto pm, auto cm) -> cudaError_t {
+    cudaError_t e = set_smem_cap(kern, sm);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sm);
+    if (e != cudaSuccess) return e;
+    const int64_t nt = mpad / kOwnTile;
+    // one CTA per (stream, pass): the resident CTAs split into passes, each stream a row
+    const int64_t passes = (p.n_sub + nth - 1) / nth;
+    const int64_t streams = std::max<int64_t>(
+        1, std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms) / passes,
+                             std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1))));
+    *rows = streams;
+    kern<<<static_cast<unsigned>(streams * passes), nth, sm, s>>>(
+        p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), v32, nt,
+        pm, cm, p.rows, static_cast<int>(streams));
+    return cudaGetLastError();
+  };
+  if constexpr (HALF) {
+    const uint4* pm = p.pmat16;
+    const auto* cm = static_cast<const typename PairCells<CW>::T*>(p.cpair);
+    return sacc ? go(mat_multt_half_kernel<CW, true>, pm, cm)
+                : go(mat_multt_half_kernel<CW, false>, pm, cm);
+  } else {
+    const float4* pm = p.pmat;
+    const CW* cm = static_cast<const CW*>(p.cmat);
+    return sacc ? go(mat_multt_kernel<CW, true>, pm, cm) : go(mat_multt_kernel<CW, false>, pm, cm);
+  }
 }
 }  // namespace
 
@@ -964,31 +1218,31 @@ cudaError_t subspace_multt_mat_df(const SubPlan& p, cudaStream_t s, int64_t mpad
 cudaError_t subspace_mult_mat(const SubPlan& p, cudaStream_t s, const float* /*xt*/, int64_t mpad,
                               int64_t m, const float* alpha32, float* out32, double* out64,
                               int64_t j_begin, int64_t j_end, int num_sms, bool half) {
-  if (!p.pmat || !p.pmat16 || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
+  if (!p.pmat || !p.pmat16 || !p.cmat || !p.cpair || p.mat_mpad != mpad) return cudaErrorInvalidValue;
   cudaError_t e = subspace_scatter_alpha(p, s, alpha32);
   if (e != cudaSuccess) return e;
   const int64_t t0 = j_begin / kOwnTile;
   const int64_t nt = (j_end + kOwnTile - 1) / kOwnTile - t0;
   if (nt <= 0) return cudaSuccess;
   if (p.cell_bits == 4)
-    return half ? launch_mat_mult<true, uint16_t>(p, s, p.pmat16, m, out32, out64, t0, nt, num_sms)
-                : launch_mat_mult<false, uint16_t>(p, s, p.pmat, m, out32, out64, t0, nt, num_sms);
-  return half ? launch_mat_mult<true, uint32_t>(p, s, p.pmat16, m, out32, out64, t0, nt, num_sms)
-              : launch_mat_mult<false, uint32_t>(p, s, p.pmat, m, out32, out64, t0, nt, num_sms);
+    return half ? launch_mat_mult<true, uint16_t>(p, s, m, out32, out64, t0, nt, num_sms)
+                : launch_mat_mult<false, uint16_t>(p, s, m, out32, out64, t0, nt, num_sms);
+  return half ? launch_mat_mult<true, uint32_t>(p, s, m, out32, out64, t0, nt, num_sms)
+              : launch_mat_mult<false, uint32_t>(p, s, m, out32, out64, t0, nt, num_sms);
 }
 
 cudaError_t subspace_multt_mat(const SubPlan& p, cudaStream_t s, const float* /*xt*/, int64_t mpad,
                                int64_t /*m*/, const float* v32, int64_t npad, double* out64,
                                const double* add, double scale_add, int num_sms, bool half) {
-  if (!p.pmat || !p.pmat16 || !p.cmat || p.mat_mpad != mpad) return cudaErrorInvalidValue;
+  if (!p.pmat || !p.pmat16 || !p.cmat || !p.cpair || p.mat_mpad != mpad) return cudaErrorInvalidValue;
   int64_t rows = 0;
   cudaError_t e;
   if (p.cell_bits == 4)
-    e = half ? launch_mat_multt<true, uint16_t>(p, s, p.pmat16, mpad, v32, num_sms, &rows)
-             : launch_mat_multt<false, uint16_t>(p, s, p.pmat, mpad, v32, num_sms, &rows);
+    e = half ? launch_mat_multt<true, uint16_t>(p, s, mpad, v32, num_sms, &rows)
+             : launch_mat_multt<false, uint16_t>(p, s, mpad, v32, num_sms, &rows);
   else
-    e = half ? launch_mat_multt<true, uint32_t>(p, s, p.pmat16, mpad, v32, num_sms, &rows)
-             : launch_mat_multt<false, uint32_t>(p, s, p.pmat, mpad, v32, num_sms, &rows);
+    e = half ? launch_mat_multt<true, uint32_t>(p, s, mpad, v32, num_sms, &rows)
+             : launch_mat_multt<false, uint32_t>(p, s, mpad, v32, num_sms, &rows);
   if (e != cudaSuccess) return e;
   return subspace_finish_rows(p, s, rows, npad, out64, add, scale_add);
 }
