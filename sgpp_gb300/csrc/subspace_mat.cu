@@ -343,7 +343,9 @@ static_assert(kPairs % kPairAheadMult == 0 && kPairs % kPairAheadMultT == 0,
               "the ring must divide a tile");
 
 // mat_mult_kernel on the pair layout: a lane takes subspaces s and s + 32, two point groups per
-// ring slot
+// ring slot. A CTA takes a contiguous range of tiles, and with one pass over the subspaces its
+// ring runs from one tile into the next instead of starting again at each tile (a ring restart
+// waits a full memory latency, about 2.5 us at this load, against ~30 us of work per tile).
 template <typename CW>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
@@ -369,37 +371,44 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
     s_at[k] = a;
   }
   __syncthreads();
-  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+  // the CTA's tiles are contiguous; with one pass over the subspaces the ring runs on from one
+  // tile into the next without restarting
+  const int64_t t_first = blockIdx.x * n_tiles / gridDim.x;
+  const int64_t t_last = (blockIdx.x + 1) * n_tiles / gridDim.x;
+  const bool one_pass = s_pad <= kMultBlock * kMatWarps;
+  const int wb0 = warp * kMultBlock;
+  uint4 ring[A], ring2[A];
+  CT cring[A], cring2[A];
+  const uint4* nsrc = nullptr;
+  const CT* ncsrc = nullptr;
+  for (int64_t tile = t_first; tile < t_last; ++tile) {
     const int64_t gt = tile_begin + tile;
     for (int s0 = 0; s0 < s_pad; s0 += kMultBlock * kMatWarps) {
-      const int wb = s0 + warp * kMultBlock;
-      if (wb >= s_pad) continue;
+      const int wb = s0 + wb0;
+      if (wb >= s_pad) continue;  // whole warps: s_pad is a multiple of 32
       const int sid = wb + lane;
-      const bool two = wb + 32 < s_pad;
-      const int64_t at = gt * kPairs * static_cast<int64_t>(s_pad) + sid;
-      const uint4* src = pp + at;
-      const CT* csrc = cp + at;
-      const uint4* src2 = two ? src + 32 : src;
-      const CT* csrc2 = two ? csrc + 32 : csrc;
+      const bool two = wb + 32 < s_pad;  // warp-uniform
       const float* a_col = s_at + sid;
       const float* a_col2 = a_col + 32;  // zeros when the second block is absent
       float* part = s_part + warp * kOwnTile;
       const bool first = s0 == 0;
-      uint4 ring[A], ring2[A];
-      CT cring[A], cring2[A];
+      const int off2 = two ? 32 : 0;
+      if (!one_pass || tile == t_first) {
+        const int64_t at = gt * kPairs * static_cast<int64_t>(s_pad) + sid;
 #pragma unroll
-      for (int u = 0; u < A; ++u) {
-        ring[u] = ld_stream(src + static_cast<int64_t>(u) * s_pad);
-        cring[u] = ld_stream(csrc + static_cast<int64_t>(u) * s_pad);
-        ring2[u] = ld_stream(src2 + static_cast<int64_t>(u) * s_pad);
-        cring2[u] = ld_stream(csrc2 + static_cast<int64_t>(u) * s_pad);
+        for (int u = 0; u < A; ++u) {
+          ring[u] = ld_stream(pp + at + static_cast<int64_t>(u) * s_pad);
+          cring[u] = ld_stream(cp + at + static_cast<int64_t>(u) * s_pad);
+          ring2[u] = ld_stream(pp + at + off2 + static_cast<int64_t>(u) * s_pad);
+          cring2[u] = ld_stream(cp + at + off2 + static_cast<int64_t>(u) * s_pad);
+        }
+        nsrc = pp + at + static_cast<int64_t>(A) * s_pad;
+        ncsrc = cp + at + static_cast<int64_t>(A) * s_pad;
       }
-      const uint4* nsrc = src + static_cast<int64_t>(A) * s_pad;
-      const CT* ncsrc = csrc + static_cast<int64_t>(A) * s_pad;
-      const uint4* nsrc2 = src2 + static_cast<int64_t>(A) * s_pad;
-      const CT* ncsrc2 = csrc2 + static_cast<int64_t>(A) * s_pad;
+      // refills run into the next tile when the ring continues there
+      const bool more = one_pass && tile + 1 < t_last;
       for (int k0 = 0; k0 < kPairs; k0 += A) {
-        const bool fetch = k0 + A < kPairs;
+        const bool fetch = k0 + A < kPairs || more;
 #pragma unroll
         for (int u = 0; u < A; ++u) {
           const int k = k0 + u;
@@ -408,12 +417,10 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
           if (fetch) {
             ring[u] = ld_stream(nsrc);
             cring[u] = ld_stream(ncsrc);
-            ring2[u] = ld_stream(nsrc2);
-            cring2[u] = ld_stream(ncsrc2);
+            ring2[u] = ld_stream(nsrc + off2);
+            cring2[u] = ld_stream(ncsrc + off2);
             nsrc += s_pad;
             ncsrc += s_pad;
-            nsrc2 += s_pad;
-            ncsrc2 += s_pad;
           }
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
@@ -451,7 +458,8 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
   }
 }
 
-// mat_multt_kernel on the pair layout
+// mat_multt_kernel on the pair layout; a stream's tiles are contiguous and its ring runs over all
+// of them (0.537 -> 0.496 ms on the benchmark workload against a ring restarted per tile)
 template <typename CW, bool SACC>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
@@ -476,12 +484,13 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
     float* acc = s_acc + tid;
     for (int c = 0; c < info.y; ++c) acc[c * nth] = 0.0f;
     bool first = true;
-    int since = 0;
-    for (int64_t tile = stream; tile < n_tiles; tile += streams) {
-      const int64_t at = tile * kPairs * static_cast<int64_t>(s_pad) + sid;
-      const uint4* src = pp + at;
-      const CT* csrc = cp + at;
-      const float4* vt = v4 + tile * kGroups;
+    // the stream's tiles are contiguous, so the ring runs over all of them without restarting
+    const int64_t k_begin = (stream * n_tiles / streams) * kPairs;
+    const int64_t k_end = ((stream + 1) * n_tiles / streams) * kPairs;
+    if (k_begin < k_end) {
+      const uint4* src = pp + k_begin * s_pad + sid;
+      const CT* csrc = cp + k_begin * s_pad + sid;
+      const float4* vt = v4 + 2 * k_begin;
       uint4 ring[A];
       CT cring[A];
 #pragma unroll
@@ -489,37 +498,43 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
         ring[u] = ld_stream(src + static_cast<int64_t>(u) * s_pad);
         cring[u] = ld_stream(csrc + static_cast<int64_t>(u) * s_pad);
       }
-      for (int k0 = 0; k0 < kPairs; k0 += A) {
+      src += static_cast<int64_t>(A) * s_pad;
+      csrc += static_cast<int64_t>(A) * s_pad;
+      int since = 0;  // pairs summed in s_acc since the last flush
+      for (int64_t k0 = k_begin; k0 < k_end; k0 += A) {
+        const bool fetch = k0 + A < k_end;
 #pragma unroll
         for (int u = 0; u < A; ++u) {
-          const int k = k0 + u;
           const uint4 pw = ring[u];
           const CT cs = cring[u];
-          if (k + A < kPairs) {
-            ring[u] = ld_stream(src + (k + A) * s_pad);
-            cring[u] = ld_stream(csrc + (k + A) * s_pad);
+          if (fetch) {
+            ring[u] = ld_stream(src);
+            cring[u] = ld_stream(csrc);
+            src += s_pad;
+            csrc += s_pad;
           }
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
             const float4 p = h ? halves4(pw.z, pw.w) : halves4(pw.x, pw.y);
             const uint32_t w = PC::word(cs, h);
-            const float4 vv = vt[2 * k + h];  // the same four values for every lane
+            const float4 vv = vt[2 * u + h];  // the same four values for every lane
             acc[cell_of<CW>(w, 0) * nth] += vv.x * p.x;
             acc[cell_of<CW>(w, 1) * nth] += vv.y * p.y;
             acc[cell_of<CW>(w, 2) * nth] += vv.z * p.z;
             acc[cell_of<CW>(w, 3) * nth] += vv.w * p.w;
           }
         }
-      }
-      ++since;
-      if (since == kFlushTiles || tile + streams >= n_tiles) {
-        for (int c = 0; c < info.y; ++c) {
-          double* dst = SACC ? s_sum + c * nth + tid : row + offset + c;
-          *dst = first ? static_cast<double>(acc[c * nth]) : *dst + static_cast<double>(acc[c * nth]);
-          acc[c * nth] = 0.0f;
+        vt += 2 * A;
+        since += A;
+        if (since == kFlushTiles * kPairs || !fetch) {
+          for (int c = 0; c < info.y; ++c) {
+            double* dst = SACC ? s_sum + c * nth + tid : row + offset + c;
+            *dst = first ? static_cast<double>(acc[c * nth]) : *dst + static_cast<double>(acc[c * nth]);
+            acc[c * nth] = 0.0f;
+          }
+          first = false;
+          since = 0;
         }
-        first = false;
-        since = 0;
       }
     }
     if (first) {
