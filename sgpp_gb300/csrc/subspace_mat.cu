@@ -154,39 +154,43 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
     s_at[k] = a;
   }
   __syncthreads();
-  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+  // the CTA's tiles are contiguous; with one pass over the subspaces the ring runs on from one
+  // tile into the next without restarting
+  const int64_t t_first = blockIdx.x * n_tiles / gridDim.x;
+  const int64_t t_last = (blockIdx.x + 1) * n_tiles / gridDim.x;
+  const bool one_pass = s_pad <= kMultBlock * kMatWarps;
+  PT ring[A], ring2[A];
+  CW cring[A], cring2[A];
+  const PT* nsrc = nullptr;
+  const CW* ncsrc = nullptr;
+  for (int64_t tile = t_first; tile < t_last; ++tile) {
     const int64_t gt = tile_begin + tile;
     for (int s0 = 0; s0 < s_pad; s0 += kMultBlock * kMatWarps) {
       const int wb = s0 + warp * kMultBlock;  // first subspace of this warp's two blocks
       if (wb >= s_pad) continue;              // whole warps: s_pad is a multiple of 32
       const int sid = wb + lane;
       const bool two = wb + 32 < s_pad;       // warp-uniform
-      const int64_t at = gt * kGroups * static_cast<int64_t>(s_pad) + sid;
-      const PT* src = pm + at;
-      const CW* csrc = cm + at;
-      const PT* src2 = two ? src + 32 : src;
-      const CW* csrc2 = two ? csrc + 32 : csrc;
+      const int off2 = two ? 32 : 0;          // the second block (the first again when absent)
       const float* a_col = s_at + sid;
       const float* a_col2 = a_col + 32;       // zeros when the second block is absent
       float* part = s_part + warp * kOwnTile;
       const bool first = s0 == 0;
-      PT ring[A], ring2[A];
-      CW cring[A], cring2[A];
+      if (!one_pass || tile == t_first) {
+        const int64_t at = gt * kGroups * static_cast<int64_t>(s_pad) + sid;
 #pragma unroll
-      for (int u = 0; u < A; ++u) {
-        ring[u] = __ldcs(src + static_cast<int64_t>(u) * s_pad);
-        cring[u] = __ldcs(csrc + static_cast<int64_t>(u) * s_pad);
-        ring2[u] = __ldcs(src2 + static_cast<int64_t>(u) * s_pad);
-        cring2[u] = __ldcs(csrc2 + static_cast<int64_t>(u) * s_pad);
+        for (int u = 0; u < A; ++u) {
+          ring[u] = ld_stream(pm + at + static_cast<int64_t>(u) * s_pad);
+          cring[u] = ld_stream(cm + at + static_cast<int64_t>(u) * s_pad);
+          ring2[u] = ld_stream(pm + at + off2 + static_cast<int64_t>(u) * s_pad);
+          cring2[u] = ld_stream(cm + at + off2 + static_cast<int64_t>(u) * s_pad);
+        }
+        nsrc = pm + at + static_cast<int64_t>(A) * s_pad;
+        ncsrc = cm + at + static_cast<int64_t>(A) * s_pad;
       }
-      // refills go through pointers bumped by one row; the last ring's worth of groups of the
-      // tile refills nothing (fetch is uniform over an unrolled ring pass)
-      const PT* nsrc = src + static_cast<int64_t>(A) * s_pad;
-      const CW* ncsrc = csrc + static_cast<int64_t>(A) * s_pad;
-      const PT* nsrc2 = src2 + static_cast<int64_t>(A) * s_pad;
-      const CW* ncsrc2 = csrc2 + static_cast<int64_t>(A) * s_pad;
+      // refills run into the next tile when the ring continues there
+      const bool more = one_pass && tile + 1 < t_last;
       for (int g0 = 0; g0 < kGroups; g0 += A) {
-        const bool fetch = g0 + A < kGroups;
+        const bool fetch = g0 + A < kGroups || more;
 #pragma unroll
         for (int u = 0; u < A; ++u) {
           const int g = g0 + u;
@@ -194,14 +198,12 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
           const float4 q = ring2[u];
           const uint32_t cs = cring[u], cq = cring2[u];
           if (fetch) {
-            ring[u] = __ldcs(nsrc);
-            cring[u] = __ldcs(ncsrc);
-            ring2[u] = __ldcs(nsrc2);
-            cring2[u] = __ldcs(ncsrc2);
+            ring[u] = ld_stream(nsrc);
+            cring[u] = ld_stream(ncsrc);
+            ring2[u] = ld_stream(nsrc + off2);
+            cring2[u] = ld_stream(ncsrc + off2);
             nsrc += s_pad;
             ncsrc += s_pad;
-            nsrc2 += s_pad;
-            ncsrc2 += s_pad;
           }
           // cells are below cmax by construction (the build writes c < cells of s <= cmax)
           float v0 = a_col[cell_of<CW>(cs, 0) * sp] * p.x;
@@ -265,46 +267,53 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_kernel(
     float* acc = s_acc + tid;
     for (int c = 0; c < info.y; ++c) acc[c * nth] = 0.0f;
     bool first = true;
-    int since = 0;  // tiles summed in s_acc since the last flush
-    for (int64_t tile = stream; tile < n_tiles; tile += streams) {
-      const int64_t at = tile * kGroups * static_cast<int64_t>(s_pad) + sid;
-      const PT* src = pm + at;
-      const CW* csrc = cm + at;
-      const float4* vt = v4 + tile * kGroups;
+    // the stream's tiles are contiguous and its ring runs over all of them
+    const int64_t g_begin = (stream * n_tiles / streams) * kGroups;
+    const int64_t g_end = ((stream + 1) * n_tiles / streams) * kGroups;
+    if (g_begin < g_end) {
+      const PT* src = pm + g_begin * s_pad + sid;
+      const CW* csrc = cm + g_begin * s_pad + sid;
+      const float4* vt = v4 + g_begin;
       PT ring[A];
       CW cring[A];
 #pragma unroll
       for (int u = 0; u < A; ++u) {
-        ring[u] = ld_stream(src + static_cast<int64_t>(u) * s_pad);
-        cring[u] = ld_stream(csrc + static_cast<int64_t>(u) * s_pad);
+        ring[u] = ld_stream(src);
+        cring[u] = ld_stream(csrc);
+        src += s_pad;
+        csrc += s_pad;
       }
-      for (int g0 = 0; g0 < kGroups; g0 += A) {
+      int since = 0;  // groups summed in s_acc since the last flush
+      for (int64_t g0 = g_begin; g0 < g_end; g0 += A) {
+        const bool fetch = g0 + A < g_end;
 #pragma unroll
         for (int u = 0; u < A; ++u) {
-          const int g = g0 + u;
           const float4 p = ring[u];
           const uint32_t cs = cring[u];
-          if (g + A < kGroups) {
-            ring[u] = ld_stream(src + (g + A) * s_pad);
-            cring[u] = ld_stream(csrc + (g + A) * s_pad);
+          if (fetch) {
+            ring[u] = ld_stream(src);
+            cring[u] = ld_stream(csrc);
+            src += s_pad;
+            csrc += s_pad;
           }
-          const float4 vv = vt[g];  // the same four values for every lane
+          const float4 vv = vt[u];  // the same four values for every lane
           // cells are below cmax by construction
           acc[cell_of<CW>(cs, 0) * nth] += vv.x * p.x;
           acc[cell_of<CW>(cs, 1) * nth] += vv.y * p.y;
           acc[cell_of<CW>(cs, 2) * nth] += vv.z * p.z;
           acc[cell_of<CW>(cs, 3) * nth] += vv.w * p.w;
         }
-      }
-      ++since;
-      if (since == kFlushTiles || tile + streams >= n_tiles) {
-        for (int c = 0; c < info.y; ++c) {
-          double* dst = SACC ? s_sum + c * nth + tid : row + offset + c;
-          *dst = first ? static_cast<double>(acc[c * nth]) : *dst + static_cast<double>(acc[c * nth]);
-          acc[c * nth] = 0.0f;
+        vt += A;
+        since += A;
+        if (since == kFlushTiles * kGroups || !fetch) {
+          for (int c = 0; c < info.y; ++c) {
+            double* dst = SACC ? s_sum + c * nth + tid : row + offset + c;
+            *dst = first ? static_cast<double>(acc[c * nth]) : *dst + static_cast<double>(acc[c * nth]);
+            acc[c * nth] = 0.0f;
+          }
+          first = false;
+          since = 0;
         }
-        first = false;
-        since = 0;
       }
     }
     if (first) {  // no tile for this CTA: its row holds zeros
@@ -690,30 +699,36 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
     float2* acc = s_acc + tid;
     for (int c = 0; c < info.y; ++c) acc[c * nth] = make_float2(0.0f, 0.0f);
     bool first = true;
-    int since = 0;
-    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-      const int64_t at = tile * kGroups * static_cast<int64_t>(s_pad) + sid;
+    // the CTA's tiles are contiguous and the ring runs over all of them, instead of starting again
+    // at each tile
+    const int64_t g_begin = (blockIdx.x * n_tiles / gridDim.x) * kGroups;
+    const int64_t g_end = ((blockIdx.x + 1) * n_tiles / gridDim.x) * kGroups;
+    if (g_begin < g_end) {
+      int64_t nxt = g_begin * s_pad + sid;
       float4 rh[kAheadDf], rl[kAheadDf];
       CW rc[kAheadDf];
 #pragma unroll
       for (int u = 0; u < kAheadDf; ++u) {
-        rh[u] = __ldcs(phi + at + static_cast<int64_t>(u) * s_pad);
-        rl[u] = __ldcs(plo + at + static_cast<int64_t>(u) * s_pad);
-        rc[u] = __ldcs(cm + at + static_cast<int64_t>(u) * s_pad);
+        rh[u] = ld_stream(phi + nxt);
+        rl[u] = ld_stream(plo + nxt);
+        rc[u] = ld_stream(cm + nxt);
+        nxt += s_pad;
       }
-      for (int g0 = 0; g0 < kGroups; g0 += kAheadDf) {
+      int since = 0;  // groups summed in s_acc since the last flush
+      for (int64_t g0 = g_begin; g0 < g_end; g0 += kAheadDf) {
+        const bool fetch = g0 + kAheadDf < g_end;
 #pragma unroll
         for (int u = 0; u < kAheadDf; ++u) {
-          const int g = g0 + u;
+          const int64_t g = g0 + u;
           const float4 ph = rh[u], pl = rl[u];
           const uint32_t cs = rc[u];
-          if (g + kAheadDf < kGroups) {
-            const int64_t k = at + static_cast<int64_t>(g + kAheadDf) * s_pad;
-            rh[u] = __ldcs(phi + k);
-            rl[u] = __ldcs(plo + k);
-            rc[u] = __ldcs(cm + k);
+          if (fetch) {
+            rh[u] = ld_stream(phi + nxt);
+            rl[u] = ld_stream(plo + nxt);
+            rc[u] = ld_stream(cm + nxt);
+            nxt += s_pad;
           }
-          const float4 vvh = vh4[tile * kGroups + g], vvl = vl4[tile * kGroups + g];
+          const float4 vvh = vh4[g], vvl = vl4[g];
           const float ph_[4] = {ph.x, ph.y, ph.z, ph.w}, pl_[4] = {pl.x, pl.y, pl.z, pl.w};
           const float vh_[4] = {vvh.x, vvh.y, vvh.z, vvh.w}, vl_[4] = {vvl.x, vvl.y, vvl.z, vvl.w};
 #pragma unroll
@@ -724,18 +739,18 @@ __global__ void __launch_bounds__(kMatThreads, 1) mat_multt_df_kernel(
             *slot = make_float2(a.h, a.l);
           }
         }
-      }
-      ++since;
-      if (since == kFlushTiles || tile + gridDim.x >= n_tiles) {
-        for (int c = 0; c < info.y; ++c) {
-          const float2 a = acc[c * nth];
-          const double v = static_cast<double>(a.x) + static_cast<double>(a.y);
-          double* dst = SACC ? s_sum + c * nth + tid : row + offset + c;
-          *dst = first ? v : *dst + v;
-          acc[c * nth] = make_float2(0.0f, 0.0f);
+        since += kAheadDf;
+        if (since == kFlushTiles * kGroups || !fetch) {
+          for (int c = 0; c < info.y; ++c) {
+            const float2 a = acc[c * nth];
+            const double v = static_cast<double>(a.x) + static_cast<double>(a.y);
+            double* dst = SACC ? s_sum + c * nth + tid : row + offset + c;
+            *dst = first ? v : *dst + v;
+            acc[c * nth] = make_float2(0.0f, 0.0f);
+          }
+          first = false;
+          since = 0;
         }
-        first = false;
-        since = 0;
       }
     }
     if (first) {
