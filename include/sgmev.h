@@ -98,7 +98,9 @@ SGMEV_API int sgmev_device_count(void);
  * it takes at most half of the free device memory and 64 GiB. The products are kept as
  * float-float pairs with their cell index (9 bytes each; grids whose subspaces have at most 256
  * cells), so the df64 (FP64-accurate) products stream them too. "materialize_multt": "on"
- * (default) or "off" — whether multTranspose streams them as well as mult. "inner_products":
+ * (default) or "off" — whether multTranspose streams them as well as mult. "system_product":
+ * "separate" (default) or "fused" — FP32 system products B^T (B a) on the materialised products
+ * as the mult and multTranspose kernels or in one fused pass. "inner_products":
  * "half" (default) or "float" — the inner FP32 solves of mixed fits stream an FP16 copy of the
  * products (3 bytes per entry instead of 5; the FP64-accurate outer residual keeps the result
  * exact to the fit's tolerance).

@@ -45,7 +45,8 @@ class OperationMultiEvalCudaLinear : public sgpp::base::OperationMultipleEval {
   // precision: SGMEV_FP64 (default, parity with the reference), SGMEV_FP32 or SGMEV_DF64; read
   // from the configuration's parameters ("precision": "double" | "float" | "df64") when one is
   // given, together with the library's other knobs ("algo", "materialize", "materialize_multt",
-  // "inner_tol", "precond", "inner_products"; see include/sgmev.h), passed through unchanged.
+  // "inner_tol", "precond", "inner_products", "system_product"; see include/sgmev.h), passed
+  // through unchanged.
   OperationMultiEvalCudaLinear(sgpp::base::Grid& grid, sgpp::base::DataMatrix& dataset,
                                int precision = SGMEV_FP64)
       : OperationMultipleEval(grid, dataset), precision_(precision) {
@@ -63,7 +64,7 @@ class OperationMultiEvalCudaLinear : public sgpp::base::OperationMultipleEval {
     }
     if (params) {
       for (const char* key : {"algo", "materialize", "materialize_multt", "inner_tol", "precond",
-                              "inner_products"}) {
+                              "inner_products", "system_product"}) {
         if (!params->contains(key)) continue;
         knobs_ += knobs_.empty() ? "{" : ",";
         knobs_ += std::string("\"") + key + "\":\"" + (*params)[key].get() + "\"";

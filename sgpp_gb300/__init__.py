@@ -120,6 +120,12 @@ def _vp(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
+# operator parameters passed to sgmev_create (the other configuration parameters, such as
+# "precision", are read by the Python side)
+OP_KNOBS = ("precond", "algo", "inner_tol", "materialize", "materialize_multt", "inner_products",
+            "system_product")
+
+
 def load_library(path: str = LIBRARY_PATH):
     """Load libsgpp_gb300.so (built by sgpp_gb300.build). Raises OperationException if absent."""
     global _lib
@@ -487,9 +493,7 @@ class OperationMultiEvalCuda:
         if not bb.isUnitCube():
             left, right = bb.arrays()
         h = ctypes.c_void_p(None)
-        knobs = {k: str(v) for k, v in (params or {}).items()
-                 if k in ("precond", "algo", "inner_tol", "materialize", "materialize_multt",
-                          "inner_products")}
+        knobs = {k: str(v) for k, v in (params or {}).items() if k in OP_KNOBS}
         if grid.getType() == GridType.ModLinear:
             knobs["basis"] = "modlinear"
         pj = json.dumps(knobs).encode() if knobs else None

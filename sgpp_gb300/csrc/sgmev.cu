@@ -120,6 +120,10 @@ struct sgmev_op {
   double inner_tol = 1e-4;  // relative tolerance of the inner solves of mixed fits ("inner_tol")
   int mat_mode = 1;         // materialised FP32 products: 0 off, 1 auto, 2 on ("materialize")
   bool mat_multt = true;    // multTranspose streams them too ("materialize_multt")
+  // FP32 system products B^T (B a) in one fused pass over the materialised products instead of
+  // the mult and multTranspose kernels ("system_product": "fused"; the separate kernels, each
+  // at the HBM copy bandwidth, are faster: 1.44 against 1.50 ms on the benchmark workload)
+  bool fused_system = false;
   bool mat_failed = false;  // a build was refused or failed for the current grid
   bool inner_half = true;   // inner solves of mixed fits use the FP16 products ("inner_products")
   bool use_half = false;    // set while such an inner solve runs
@@ -945,7 +949,7 @@ static int dev_convert(sgmev_op* op, const double* in, int64_t n, int64_t npad, 
 static int dev_system(sgmev_op* op, int prec, const double* a64, double* out64, double lm) {
   if (prec == SGMEV_FP32) {
     SGMEV_TRY(dev_convert(op, a64, op->npad, op->npad, nullptr, op->a32, nullptr));
-    if (!op->use_half && op->sub_ok && op->mat_multt && mat_ready(op) &&
+    if (op->fused_system && !op->use_half && op->sub_ok && op->mat_multt && mat_ready(op) &&
         subspace_system_mat_fits(op->sub)) {
       // one pass over the materialised products for B^T (B a)
       const long ev = prof_begin(op, KIND_SYSTEM_MAT32);
@@ -1244,6 +1248,9 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   const std::string basis = json_string(params_json, "basis");
   if (!basis.empty() && basis != "linear" && basis != "modlinear")
     return fail(SGMEV_ERR_INVALID, "params: basis must be \"linear\" or \"modlinear\"");
+  const std::string sys_p = json_string(params_json, "system_product");
+  if (!sys_p.empty() && sys_p != "separate" && sys_p != "fused")
+    return fail(SGMEV_ERR_INVALID, "params: system_product must be \"separate\" or \"fused\"");
   const std::string mat_t = json_string(params_json, "materialize_multt");
   if (!mat_t.empty() && mat_t != "on" && mat_t != "off")
     return fail(SGMEV_ERR_INVALID, "params: materialize_multt must be \"on\" or \"off\"");
@@ -1261,6 +1268,7 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   op->precond = precond == "jacobi";
   op->mat_mode = mat == "off" ? 0 : (mat == "on" ? 2 : 1);
   op->mat_multt = mat_t != "off";
+  op->fused_system = sys_p == "fused";
   op->inner_half = inner_p != "float";
   op->mod = basis == "modlinear";
   {

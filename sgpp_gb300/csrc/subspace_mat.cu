@@ -468,7 +468,10 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
 }
 
 // mat_multt_kernel on the pair layout; a stream's tiles are contiguous and its ring runs over all
-// of them (0.537 -> 0.496 ms on the benchmark workload against a ring restarted per tile)
+// of them (0.537 -> 0.496 ms on the benchmark workload against a ring restarted per tile). The
+// FP32 cell sums are flushed into float-float sums (a two-sum, at the FP32 rate) instead of FP64
+// ones, whose adds run at a small fraction of that rate on this part (0.496 -> 0.487 ms); they
+// become FP64 once, when the row is written.
 template <typename CW, bool SACC>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
@@ -479,7 +482,7 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
   constexpr int A = kPairAheadMultT;
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, nth = blockDim.x;
-  double* s_sum = reinterpret_cast<double*>(smem);  // [cmax][blockDim] (SACC)
+  float2* s_sum = reinterpret_cast<float2*>(smem);  // [cmax][blockDim] float-float (SACC)
   float* s_acc = reinterpret_cast<float*>(SACC ? smem + sizeof(double) * cmax * nth : smem);
   const int pass = blockIdx.x / streams, stream = blockIdx.x - pass * streams;
   const int passes = gridDim.x / streams;
@@ -537,8 +540,20 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
         since += A;
         if (since == kFlushTiles * kPairs || !fetch) {
           for (int c = 0; c < info.y; ++c) {
-            double* dst = SACC ? s_sum + c * nth + tid : row + offset + c;
-            *dst = first ? static_cast<double>(acc[c * nth]) : *dst + static_cast<double>(acc[c * nth]);
+            const float a = acc[c * nth];
+            if constexpr (SACC) {
+              float2* d = s_sum + c * nth + tid;
+              if (first) {
+                *d = make_float2(a, 0.0f);
+              } else {
+                ff t{d->x, d->y};
+                add_ff(t, ff{a, 0.0f});
+                *d = make_float2(t.h, t.l);
+              }
+            } else {
+              double* dst = row + offset + c;
+              *dst = first ? static_cast<double>(a) : *dst + static_cast<double>(a);
+            }
             acc[c * nth] = 0.0f;
           }
           first = false;
@@ -549,7 +564,10 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
     if (first) {
       for (int c = 0; c < info.y; ++c) row[offset + c] = 0.0;
     } else if (SACC) {
-      for (int c = 0; c < info.y; ++c) row[offset + c] = s_sum[c * nth + tid];
+      for (int c = 0; c < info.y; ++c) {
+        const float2 t = s_sum[c * nth + tid];
+        row[offset + c] = static_cast<double>(t.x) + static_cast<double>(t.y);
+      }
     }
   }
 }

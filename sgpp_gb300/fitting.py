@@ -15,7 +15,7 @@ from typing import Optional
 import numpy as np
 
 from . import (SGMEV_DF64, SGMEV_FP32, SGMEV_FP64, SGMEV_SOLVE_MIXED, SGMEV_SOLVE_PLAIN, Dataset,
-               Grid, GridType, OperationException, OperationMultipleEvalConfiguration,
+               OP_KNOBS, Grid, GridType, OperationException, OperationMultipleEvalConfiguration,
                OperationMultipleEvalSubType, OperationMultipleEvalType, _as_matrix, _check,
                _precision_of, _vp, load_library)
 
@@ -116,7 +116,7 @@ class FitterConfigurationLeastSquares:
         return self.multipleEvalConfig
 
 
-_OP_KNOBS = ("precond", "algo", "inner_tol", "materialize", "materialize_multt", "inner_products")
+_OP_KNOBS = OP_KNOBS
 
 
 class ModelFittingLeastSquares:

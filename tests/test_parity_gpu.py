@@ -250,6 +250,40 @@ def test_system_apply_matches_oracle(oracle):
         assert rel_err(out, ref) < FP32_TOL
 
 
+@pytest.mark.parametrize("route", ["separate", "fused"])
+def test_system_product_knob(oracle, route):
+    """params "system_product": FP32 system products on the materialised products as the mult and
+    multTranspose kernels (default) or one fused pass; both match the oracle, and a plain FP32 fit
+    through either reaches the FP32 solution. Other values raise."""
+    rng = np.random.default_rng(17)
+    grid = sg.Grid.createLinearGrid(5)
+    grid.getGenerator().regular(4)
+    x = rng.random((5000, 5))
+    a = rng.standard_normal(grid.getSize())
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    st = oracle.stream(x)
+    lam_m = 5000 * 1e-3
+    ref = st.mult_transpose(lp, ix, st.mult(lp, ix, a)) + lam_m * a
+    cfg = sg.OperationMultipleEvalConfiguration(
+        sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
+        parameters={"precision": "float", "algo": "subspace", "materialize": "on",
+                    "system_product": route})
+    op = sg.createOperationMultipleEval(grid, x, cfg)
+    out = np.zeros(grid.getSize())
+    op.systemApply(a, out, lam_m)
+    assert rel_err(out, ref) < FP32_TOL
+    y = np.sin(2 * x[:, 0]) + x[:, 1] * x[:, 2]
+    alpha, _, _ = op.fit(y, 1e-3, 2000, 1e-6)
+    want, _, _ = st.cg_fit(lp, ix, y, 1e-3, 2000, 1e-10)
+    assert rel_err(alpha, want) < 1e-4
+    op.close()
+    bad = sg.OperationMultipleEvalConfiguration(
+        sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
+        parameters={"system_product": "both"})
+    with pytest.raises(Exception):
+        sg.createOperationMultipleEval(grid, x, bad)
+
+
 @pytest.mark.parametrize("precision", ["double", "df64"])
 @pytest.mark.parametrize("name", ["d4_l4", "d6_l3"])
 def test_device_cg_fit_matches_reference(name, precision):
