@@ -147,6 +147,32 @@ def test_create_validates_before_touching_the_device(lib):
     assert rc == sg.SGMEV_ERR_INVALID
 
 
+@pytest.mark.parametrize("knob", ["precond", "algo", "materialize", "inner_products",
+                                  "system_product", "materialize_multt"])
+def test_operator_knobs_are_validated_before_the_device(lib, knob):
+    """A bad value of an operator parameter fails sgmev_create with SGMEV_ERR_INVALID and names
+    the parameter, before any device work; the Python configuration forwards every parameter of
+    OP_KNOBS, so the same value raises there (no GPU needed for either)."""
+    import ctypes
+    import json
+    assert knob in sg.OP_KNOBS
+    lp = np.array([[2.0, 4.0]])
+    ix = np.array([[1.0, 3.0]])
+    x = np.zeros((4, 2))
+    h = ctypes.c_void_p(None)
+    rc = lib.sgmev_create(ctypes.byref(h), 2, 1, lp.ctypes.data, ix.ctypes.data, 4, x.ctypes.data,
+                          None, None, sg.SGMEV_FP64, json.dumps({knob: "bogus"}).encode())
+    assert rc == sg.SGMEV_ERR_INVALID
+    assert knob.encode() in lib.sgmev_last_error()
+    grid = sg.Grid.createLinearGrid(2)
+    grid.getGenerator().regular(2)
+    cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                sg.OperationMultipleEvalSubType.CUDA,
+                                                parameters={knob: "bogus"})
+    with pytest.raises(sg.OperationException, match=knob):
+        sg.createOperationMultipleEval(grid, np.zeros((3, 2)), cfg)
+
+
 def test_no_device_fails_loudly(lib):
     if lib.sgmev_device_count() > 0:
         pytest.skip("a GPU is visible; this checks the no-GPU error path")
