@@ -450,6 +450,28 @@ def test_mixed_fit_inner_products(products):
         sg.createOperationMultipleEval(grid, g[name + "_x"], cfg)
 
 
+@pytest.mark.parametrize("dim,level", [(2, 7), (3, 6)])
+def test_mixed_fit_with_byte_cells(oracle, dim, level):
+    """Grids whose subspaces have more than 16 cells keep byte cell indices: the FP16 inner
+    products then read two byte-cell words per pair of point groups (the uint2 pair copy). The
+    mixed fit on the materialised products still reaches the oracle's FP64 solution."""
+    rng = np.random.default_rng(41)
+    grid = sg.Grid.createLinearGrid(dim)
+    grid.getGenerator().regular(level)
+    m = 20000
+    x = rng.random((m, dim))
+    y = np.sin(5 * x[:, 0]) * np.cos(3 * x[:, 1]) + 0.01 * rng.standard_normal(m)
+    cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                sg.OperationMultipleEvalSubType.CUDA,
+                                                parameters={"algo": "subspace", "materialize": "on"})
+    op = sg.createOperationMultipleEval(grid, x, cfg)
+    alpha, _, _ = op.fit(y, 1e-4, 20000, 1e-10, mode=sg.SGMEV_SOLVE_MIXED)
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    ref, _, _ = oracle.stream(x).cg_fit(lp, ix, y, 1e-4, 20000, 1e-12)
+    assert rel_err(alpha, ref) < 1e-6
+    op.close()
+
+
 def test_inner_tolerance_knob():
     """params "inner_tol": any value in (0, 1) reaches the same FP64 solution; others raise."""
     g = load_golden("cgfit.npz")
