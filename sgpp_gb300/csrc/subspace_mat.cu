@@ -4,25 +4,27 @@
 // calls. They are computed once, in float-float arithmetic (sub_mat_build_kernel in subspace.cu),
 // and kept in HBM as
 //     P_hi[g][s], P_lo[g][s] : float4, the products of points 4g .. 4g+3 as float-float pairs
-//     C[g][s]                : uint32, their cell indices, one byte each
+//     C[g][s]                : their cell indices, a byte each (uint32) or, when no subspace has
+//                              more than 16 cells, a nibble each (uint16)
 // with s padded to a multiple of 32 (padded entries 0), and for the inner solves of mixed fits an
-// FP16 copy of P_hi with the cell words, laid out by pairs of point groups (see the FP16 section).
-// The FP32 mult and multTranspose stream P_hi and C (5 bytes per point and subspace), the
-// FP64-accurate ones all three (9 bytes), the FP16 ones the copy (3); none touches a coordinate,
-// so they are bounded by HBM bandwidth rather than the hat arithmetic.
+// FP16 copy of P_hi with a copy of the cell words, both laid out by pairs of point groups (see
+// the FP16 section). The FP32 mult and multTranspose stream P_hi and C (4.5-5 bytes per point and
+// subspace), the FP64-accurate ones all three (8.5-9 bytes), the FP16 ones the copy (2.5-3); none
+// touches a coordinate, so they are bounded by HBM bandwidth rather than the hat arithmetic.
 // Points outside the domain have P = 0 (and cell 0), so they need no test.
 //
-// Both kernels are owner-computes: thread k of a pass owns subspace s = pass * blockDim + k and
-// walks the CTA's tiles of points; a warp reads P[g][32 consecutive s] as 512 contiguous bytes
-// (and C as 128), through a four-deep ring of loads in registers.
+// The kernels are owner-computes: thread k of a pass owns subspace s = pass * blockDim + k and
+// walks a contiguous range of tiles of points; a warp reads P[g][32 consecutive s] as one
+// contiguous run, through a ring of loads in registers that runs on from one tile into the next.
 //   mult:  lane s forms alpha_s[c] * p for 4 points, for subspaces s and s + 32 at once (their
 //          terms added in registers); a butterfly over the warp (xor 16, 8, then 4, 2, 1) reduces
 //          the 4 values to 4 per-point sums, which go to per-warp partials in shared memory;
 //          after all passes the partials are added in warp order.
 //   multT: lane s adds v_j * p into its cells ([cell][thread] in shared memory, conflict-free) and
-//          flushes them into FP64 sums every kFlushTiles tiles; rows are added in row order. The
-//          FP16/FP32 kernel gives each pass of subspaces its own CTA: the CTAs of all passes of
-//          one stream of tiles share a row and read the parts of the same product rows together.
+//          flushes them every kFlushTiles tiles into FP64 sums (float-float in the FP16 kernel);
+//          rows are added in row order. The FP16/FP32 kernels give each pass of subspaces its own
+//          CTA: the CTAs of all passes of one stream of tiles share a row and read the parts of
+//          the same product rows together.
 // The float-float variants do the same with float-float products, sums and butterfly.
 // Every sum has a fixed order, so results are the same bit for bit from run to run.
 #include <cuda_fp16.h>
