@@ -1,0 +1,140 @@
+"""Host logic of the fit servers (sgpp_gb300/serving.py), on the CPU.
+
+The servers' scheduling is plain Python around the GPU work: FitServer admits requests in arrival
+order into the batch engine's slots and retires them when their phase is done; PoolServer hands
+requests to worker threads. Here the GPU parts are replaced by fakes, so the order of admission,
+the bookkeeping of times, the deadline and the error paths are checked without a device.
+"""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+import sgpp_gb300 as sg
+from sgpp_gb300 import serving
+
+
+def _requests(n, gap=0.0, y_cols=1):
+    return [serving.Request(rid=k, arrival=k * gap, grid=None, X=np.zeros((4, 2)),
+                            Y=np.full((4, y_cols), float(k)), lam=1e-3)
+            for k in range(n)]
+
+
+class FakeEngine:
+    """The BatchEngine calls FitServer makes: tryAdd / step / result / remove."""
+    PHASE_DONE = sg.BatchEngine.PHASE_DONE
+
+    def __init__(self, slots, steps_to_finish=2):
+        self.slots = [None] * slots
+        self.left = {}
+        self.steps_to_finish = steps_to_finish
+        self.added = []
+
+    def tryAdd(self, grid, X, Y, lam, eps):
+        for s, occupant in enumerate(self.slots):
+            if occupant is None:
+                self.slots[s] = float(Y[0, 0])
+                self.left[s] = self.steps_to_finish
+                self.added.append(int(Y[0, 0]))
+                return s
+        return None
+
+    def step(self, n):
+        phases = [0] * len(self.slots)
+        for s in list(self.left):
+            self.left[s] -= 1
+            if self.left[s] <= 0:
+                phases[s] = self.PHASE_DONE
+        return phases
+
+    def result(self, slot):
+        return np.array([self.slots[slot]]), 7, 1e-9, 0
+
+    def remove(self, slot):
+        self.slots[slot] = None
+        del self.left[slot]
+
+
+def _fit_server(engine):
+    srv = serving.FitServer.__new__(serving.FitServer)
+    srv.engine = engine
+    srv.steps_per_poll = 1
+    srv.queue_depths = []
+    return srv
+
+
+def test_fit_server_admits_in_arrival_order_and_retires_every_request():
+    engine = FakeEngine(slots=3)
+    srv = _fit_server(engine)
+    reqs = _requests(10, gap=1e-4)
+    done = srv.run(list(reversed(reqs)))  # the server sorts by arrival
+    assert sorted(r.rid for r in done) == list(range(10))
+    assert engine.added == list(range(10))  # FIFO admission
+    for r in done:
+        assert r.alpha[0] == float(r.rid)  # each slot's own result
+        assert r.iterations == 7 and r.residual == 1e-9
+        assert r.arrival <= r.admitted <= r.finished
+    assert max(srv.queue_depths) <= 10 and all(s is None for s in engine.slots)
+
+
+def test_fit_server_rejects_a_request_that_does_not_fit_an_empty_engine():
+    srv = _fit_server(FakeEngine(slots=0))
+    with pytest.raises(sg.OperationException, match="does not fit into an empty engine"):
+        srv.run(_requests(1))
+
+
+class FakePool(serving.PoolServer):
+    def __init__(self, workers, fail_rid=None, delay=0.002):
+        super().__init__(workers=workers)
+        self.fail_rid = fail_rid
+        self.delay = delay
+        self.concurrent = 0
+        self.peak = 0
+        self._lock = threading.Lock()
+
+    def _fit(self, r, keep_alpha):
+        with self._lock:
+            self.concurrent += 1
+            self.peak = max(self.peak, self.concurrent)
+        try:
+            time.sleep(self.delay)
+            if r.rid == self.fail_rid:
+                raise sg.OperationException(f"fit of request {r.rid} failed")
+            r.iterations = 3
+            r.alpha = np.array([float(r.rid)]) if keep_alpha else None
+        finally:
+            with self._lock:
+                self.concurrent -= 1
+
+
+def test_pool_server_serves_every_request_with_bounded_concurrency():
+    srv = FakePool(workers=3)
+    done = srv.run(_requests(12, gap=0.0005))
+    assert sorted(r.rid for r in done) == list(range(12))
+    assert 1 <= srv.peak <= 3
+    for r in done:
+        assert r.arrival <= r.admitted + 1e-3 and r.admitted <= r.finished
+        assert r.alpha[0] == float(r.rid)
+    assert len(srv.queue_depths) == 12
+
+
+def test_pool_server_reports_a_failed_fit_after_the_run():
+    srv = FakePool(workers=2, fail_rid=4)
+    with pytest.raises(sg.OperationException, match="request 4 failed"):
+        srv.run(_requests(8))
+
+
+def test_pool_server_drops_queued_requests_past_the_deadline():
+    srv = FakePool(workers=1, delay=0.02)
+    done = srv.run(_requests(20), max_seconds=0.05)
+    assert 1 <= len(done) < 20
+    assert sorted(r.rid for r in done) == list(range(len(done)))  # served in arrival order
+
+
+def test_percentile():
+    assert np.isnan(serving.percentile([], 0.5))
+    v = [5.0, 1.0, 3.0, 2.0, 4.0]
+    assert serving.percentile(v, 0.0) == 1.0
+    assert serving.percentile(v, 0.5) == 3.0
+    assert serving.percentile(v, 1.0) == 5.0
