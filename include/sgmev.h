@@ -93,16 +93,18 @@ SGMEV_API int sgmev_device_count(void);
  * function per subspace and data point, as the reference's DEFAULT operator; grids of dim <= 16
  * with at most 24,576 subspace positions); "auto" takes subspace when it needs fewer instructions.
  * "materialize": "auto" (default), "on" or "off" — whether the subspace FP32 products keep
- * p_s(x_j) for every data point and subspace in device memory (4 bytes each, built on the first
+ * p_s(x_j) for every data point and subspace in device memory (built on the first
  * FP32 product) and streams it, instead of evaluating the hats on every call; "auto" does so when
  * it takes at most half of the free device memory and 64 GiB. The products are kept as
- * float-float pairs with their cell index (9 bytes each; grids whose subspaces have at most 256
- * cells), so the df64 (FP64-accurate) products stream them too. "materialize_multt": "on"
+ * float-float pairs with their cell index (8 bytes and a byte, or a nibble when no subspace has
+ * more than 16 cells; grids whose subspaces have at most 256 cells), so the df64 (FP64-accurate)
+ * products stream them too, beside an FP16 copy with its own copy of the cell indices for the
+ * inner solves of mixed fits (11 to 12 bytes per point and subspace in all). "materialize_multt": "on"
  * (default) or "off" — whether multTranspose streams them as well as mult. "system_product":
  * "separate" (default) or "fused" — FP32 system products B^T (B a) on the materialised products
  * as the mult and multTranspose kernels or in one fused pass. "inner_products":
  * "half" (default) or "float" — the inner FP32 solves of mixed fits stream an FP16 copy of the
- * products (3 bytes per entry instead of 5; the FP64-accurate outer residual keeps the result
+ * products (2.5-3 bytes per entry instead of 4.5-5; the FP64-accurate outer residual keeps the result
  * exact to the fit's tolerance).
  * "basis": "linear" (default) or "modlinear" — the basis of the grid. level_pow2/index stay the
  * (2^l, i) arrays of getLevelIndexArraysForEval for both (a ModLinear grid has the same points).
