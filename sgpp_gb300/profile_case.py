@@ -41,9 +41,10 @@ KINDS = {("mult", "float", "dense"): sg.SGMEV_KERNEL_MULT_FP32,
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel", choices=["mult", "multT", "system", "fit"], default="mult",
-                    help="system: B^T (B a) + lambda M a (systemApply); fit: one mixed-precision "
-                         "fit (its inner solves stream the FP16 products); reports the kernel "
-                         "given by --report")
+                    help="system: B^T (B a) + lambda M a (systemApply; with materialized "
+                         "products the fused kernel, system_product=fused); fit: one "
+                         "mixed-precision fit (its inner solves stream the FP16 products); "
+                         "reports the kernel given by --report")
     ap.add_argument("--report", choices=["mult16", "multT16"], default="mult16",
                     help="with --kernel fit: which kernel's launches to report")
     ap.add_argument("--precision", choices=["float", "double", "df64"], default="float")
@@ -68,7 +69,8 @@ def main() -> int:
                                                     "precision": args.precision,
                                                     "algo": "subspace" if mat else args.algo,
                                                     "materialize": "on" if mat else "off",
-                                                    "materialize_multt": "on" if mat else "off"})
+                                                    "materialize_multt": "on" if mat else "off",
+                                                    "system_product": "fused"})
     op = sg.createOperationMultipleEval(grid, x, cfg)
     a = rng.standard_normal(n)
     v = rng.standard_normal(args.points)
@@ -98,11 +100,16 @@ def main() -> int:
     cnt, sec = op.profileRead(kind)
     op.profile(False)
     flop = 6.0 * n * args.points * args.dim
-    avg = sec / max(cnt, 1)
+    avg = sec / cnt if cnt else None
     print(json.dumps({"kernel": args.kernel, "precision": args.precision, "algo": algo,
                       "dim": args.dim,
                       "level": args.level, "n_grid": n, "points": args.points, "launches": cnt,
-                      "avg_ms": avg * 1e3, "tflops_ref_count": flop / avg / 1e12}))
+                      "avg_ms": avg * 1e3 if avg else None,
+                      "tflops_ref_count": flop / avg / 1e12 if avg else None}))
+    if not cnt:
+        print(f"no launches of the reported kernel kind {kind}", file=sys.stderr)
+        op.close()
+        return 1
     op.close()
     return 0
 
