@@ -209,8 +209,8 @@ def mat_bytes_per_launch(kernel: str, lp, m: int, n: int) -> float:
 
 
 def hbm_peak_gbs():
-    """(GB/s, source): the measured HBM copy bandwidth of the GB300s (driver-written
-    MEASURED_PEAKS.json), else the 6.8 TB/s fallback of an earlier GB300 measurement."""
+    """(GB/s, source): the measured HBM copy bandwidth of these GB300s (MEASURED_PEAKS.json),
+    else the 6.8 TB/s fallback of an earlier GB300 measurement."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         return float(json.load(open(path))["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"

@@ -6,7 +6,7 @@ the ranged interface OperationMultipleEval::mult(alpha, result, start, end),
 OperationMultipleEval.hpp:70-73). mult needs no communication (alpha is replicated); B^T v and the
 system product B^T(B a) + lambda M a need one sum of N-vectors over ranks, done as an all-gather
 followed by a sum in rank order, so every rank gets bit-identical results independent of the
-communication library's reduction order. The CG driver then runs replicated on every rank.
+communication library's reduction order. The CG loop then runs replicated on every rank.
 
 The local operator is any object with mult(alpha, out) / multTranspose(v, out) over the rank's
 data shard — on a GPU host the CUDA operator built on that shard.

@@ -32,7 +32,7 @@ def test_regular_grid_matches_reference_order(oracle, d, l):
         np.testing.assert_array_equal(idx, g[key + "_index"])
 
 
-def test_regular_grid_sizes_survey(oracle):
+def test_regular_grid_sizes_match_the_reference_counts(oracle):
     # sizes the survey measured with the reference (d=5 l=6, d=10 l=5, d=8 l=4, d=12 l=7)
     assert oracle.lib.orc_regular_grid_size(5, 6) == 5503
     assert oracle.lib.orc_regular_grid_size(10, 5) == 13441
