@@ -81,7 +81,7 @@ def make_grids(ref: Reference):
 
 def make_refine(ref: Reference):
     out = {}
-    seqs = [("small", 4, 3, 3, 10, 11), ("cfg3", 8, 4, 6, 40, 12)]
+    seqs = [("small", 4, 3, 3, 10, 11), ("adaptive_d8_l4", 8, 4, 6, 40, 12)]
     for name, d, l, rounds, npts, seed in seqs:
         rng = np.random.default_rng(seed)
         g = ref.grid(d, l)

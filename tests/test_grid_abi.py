@@ -61,7 +61,7 @@ def test_regular_twice_raises(lib):
         grid.getGenerator().regular(2)
 
 
-@pytest.mark.parametrize("seq", ["small", "cfg3"])
+@pytest.mark.parametrize("seq", ["small", "adaptive_d8_l4"])
 def test_product_refinement_equals_reference_set(lib, seq):
     g = load_golden("refine.npz")
     rows = lambda L, I: set(map(tuple, np.hstack([L, I]).tolist()))

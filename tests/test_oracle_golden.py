@@ -33,7 +33,7 @@ def test_regular_grid_matches_reference_order(oracle, d, l):
 
 
 def test_regular_grid_sizes_match_the_reference_counts(oracle):
-    # sizes the survey measured with the reference (d=5 l=6, d=10 l=5, d=8 l=4, d=12 l=7)
+    # sizes of the reference's regular grids (d=5 l=6, d=10 l=5, d=8 l=4, d=12 l=7)
     assert oracle.lib.orc_regular_grid_size(5, 6) == 5503
     assert oracle.lib.orc_regular_grid_size(10, 5) == 13441
     assert oracle.lib.orc_regular_grid_size(8, 4) == 1121
@@ -44,7 +44,7 @@ def _rows(lev, idx):
     return set(map(tuple, np.hstack([lev, idx]).tolist()))
 
 
-@pytest.mark.parametrize("seq", ["small", "cfg3"])
+@pytest.mark.parametrize("seq", ["small", "adaptive_d8_l4"])
 def test_refinement_point_sets_match_reference(oracle, seq):
     g = load_golden("refine.npz")
     rounds = int(g[f"{seq}_rounds"])
