@@ -754,7 +754,7 @@ def createOperationMultipleEval(grid: Grid, dataset,
         return OperationMultiEvalCuda(grid, dataset, _precision_of(configuration.getParameters()),
                                       configuration.getParameters())
     raise FactoryException("OperationMultipleEval is not implemented for this combination of "
-                           "type, subtype and MPI type in this build.")
+                           "type, subtype and MPI type (the CUDA subtype: STREAMING, no MPI).")
 
 
 # ---- least-squares system and CG (the callers that drive the operator unchanged) -----------
