@@ -8,9 +8,9 @@ y = 10 sin(pi x1 x2) + 20 (x3 - 0.5)^2 + 10 x4 + 5 x5 + N(0, 0.1^2); lambda = 1e
 Synthetic, seeded data of that shape (no dataset files are read).
 
 One step = one regression fit: b = B^T y, then CG on (B^T B + lambda M I) alpha = b to the
-relative FP64 residual `epsilon`, mixed precision (FP32 hat kernels inside CG; the outer
-iterative-refinement residual b - A alpha with the FP64-accurate float-float "df64" kernels),
-all state resident on the GPU.
+relative FP64 residual `epsilon`, mixed precision (inside CG, FP32 arithmetic on the FP16 copy of
+the materialised subspace products; the outer iterative-refinement residual b - A alpha with the
+FP64-accurate float-float "df64" products), all state resident on the GPU.
 Each fit's alpha is checked against an FP64 solution computed once before timing.
 
 value   fits/s with the data resident in HBM (device pointers for y and alpha)
