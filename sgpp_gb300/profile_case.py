@@ -49,7 +49,8 @@ def main() -> int:
                     help="with --kernel fit: which kernel's launches to report")
     ap.add_argument("--precision", choices=["float", "double", "df64"], default="float")
     ap.add_argument("--algo", choices=["dense", "subspace", "materialized"], default="dense",
-                    help="materialized: subspace products kept in device memory (FP32)")
+                    help="materialized: subspace products kept in device memory (float-float, "
+                         "with an FP16 copy for the inner solves of --kernel fit)")
     ap.add_argument("--dim", type=int, default=10)
     ap.add_argument("--level", type=int, default=5)
     ap.add_argument("--points", type=int, default=1 << 22)
