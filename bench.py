@@ -10,25 +10,32 @@ Synthetic, seeded data of that shape (no dataset files are read).
 One step = one regression fit: b = B^T y, then CG on (B^T B + lambda M I) alpha = b to the
 relative FP64 residual `epsilon`, mixed precision (inside CG, FP32 arithmetic on the FP16 copy of
 the materialised subspace products; the outer iterative-refinement residual b - A alpha with the
-FP64-accurate float-float "df64" products), all state resident on the GPU.
-Each fit's alpha is checked against an FP64 solution computed once before timing.
+FP64-accurate float-float "df64" products), all state resident on the GPU. Each fit's alpha is
+checked against the reference's own FP64 CG solution of this workload (SG++'s
+SystemMatrixLeastSquaresIdentity + ConjugateGradients at epsilon 1e-12, the fixture
+tests/golden/regression_d10_l5.npz).
 
 value   fits/s with the data resident in HBM (device pointers for y and alpha)
 e2e     fits/s through the public API from pinned host buffers: create the operator from the
         host data matrix (H2D copy inside the timed region), fit with host y, read alpha back
 roofline  the kernel with the most device time in the fits. When it streams the materialised
         subspace products (the default), it is HBM-bound: achieved = its algorithmic bytes per
-        launch (FP16 2 B, FP32 4 B, df64 8 B per padded point and padded subspace, plus the cell index, and the vectors)
-        over its CUDA-event duration, against MEASURED_PEAKS.json's copy bandwidth. A kernel that
-        evaluates hats is reported against the FP32/FP64 FMA peak measured in the same run, with
-        the reference's count of 6 N M d FLOP per launch
+        launch (FP16 2 B, FP32 4 B, df64 8 B per padded point and padded subspace, plus the cell
+        index, and the vectors) over its CUDA-event duration, against MEASURED_PEAKS.json's copy
+        bandwidth. A kernel that evaluates hats is reported against the FP32/FP64 FMA peak
+        measured in the same run, with the reference's count of 6 N M d FLOP per launch
         (LearnerVectorizedPerformanceCalculator.cpp:91-93).
-cpu_baseline  the oracle port of the reference's STREAMING FP64 path on the host cores
-        (bounded sample: one B^T B application on 2^16 of the points, scaled to M and to the
-        CG operation count of one fit)
+mult_gflops  one launch each of the dense FP32 and FP64 mult kernels (STREAMING's algorithm) on
+        this workload: GFLOP/s by the reference's count and the fraction of the FMA peaks
+        measured in this run
+plain_fp64_path  whole plain FP64-accurate CG fits (the reference's algorithm) on a df64
+        operator, and the mixed fits' speed-up over them
+cpu_baseline  the oracle port of the reference's STREAMING FP64 path on the host cores: one
+        B^T(B a) on all points (median of 3), times the operator applications of one CG fit
 
 --impl reference prints the same line for the reference's CPU implementation of the path
-(the oracle port: the compiled reference needs its sources, which do not travel).
+(the oracle port: the compiled reference needs its sources, which do not travel); its steps are
+single B^T(B a) applications on all points, and it loads nothing of this library.
 
 --basis modlinear runs the same workload on a ModLinear grid (the same points with the modified
 linear basis; the reference streams it with OperationMultiEvalModMaskStreaming), with the oracle's
@@ -56,7 +63,6 @@ if ROOT not in sys.path:
 
 DIM, LEVEL, M_POINTS, LAMBDA = 10, 5, 1 << 20, 1e-4
 FLOP_PER_PAIR_DIM = 6.0  # reference's count per (grid point, data point, dimension)
-CPU_SAMPLE_POINTS = 1 << 16
 
 
 def make_workload(seed: int, m: int = M_POINTS, d: int = DIM):
@@ -130,39 +136,67 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_fit_seconds(x, grid_lp, grid_ix, cg_ops: float, threads: int, basis: str = "linear"):
+class CpuReference:
     """Oracle port of the reference's STREAMING FP64 path on the host cores
-    (OperationMultiEvalStreaming, or OperationMultiEvalModMaskStreaming for ModLinear): time one
-    B^T (B a) on CPU_SAMPLE_POINTS points, scale linearly to all points and to the number of
-    operator applications one CG fit performs. Returns (seconds per fit, sample description)."""
-    from oracle import Oracle
+    (OperationMultiEvalStreaming, or OperationMultiEvalModMaskStreaming for ModLinear): one
+    application of the system's data term B^T (B a) on ALL points per call, the operation a
+    ConjugateGradients iteration performs (SystemMatrixLeastSquaresIdentity.cpp:32-47)."""
 
-    orc = Oracle()
-    orc.set_threads(threads)
-    ms = min(CPU_SAMPLE_POINTS, x.shape[0])
-    st = orc.stream(x[:ms])
-    a = np.random.default_rng(0).standard_normal(grid_lp.shape[0])
-    if basis == "modlinear":
-        lev = np.rint(np.log2(grid_lp)).astype(np.int32)
-        arrays = orc.mod_arrays(lev, grid_ix.astype(np.int32))
+    def __init__(self, x, grid_lp, grid_ix, threads: int, basis: str = "linear"):
+        from oracle import Oracle
 
-        def apply():
-            st.mult_transpose_mod(arrays, st.mult_mod(arrays, a))
-    else:
-        def apply():
-            st.mult_transpose(grid_lp, grid_ix, st.mult(grid_lp, grid_ix, a))
-    apply()  # warm-up
-    ts = []
-    for _ in range(3):
+        self.orc = Oracle()
+        self.orc.set_threads(threads)
+        self.threads = threads
+        self.x = x
+        self.basis = basis
+        self.lp, self.ix = grid_lp, grid_ix
+        self.a = np.random.default_rng(0).standard_normal(grid_lp.shape[0])
+        if basis == "modlinear":
+            lev = np.rint(np.log2(grid_lp)).astype(np.int32)
+            self.arrays = self.orc.mod_arrays(lev, grid_ix.astype(np.int32))
+        self.full = self.orc.stream(x)
+        self.sample = None
+
+    def _apply(self, st):
+        if self.basis == "modlinear":
+            st.mult_transpose_mod(self.arrays, st.mult_mod(self.arrays, self.a))
+        else:
+            st.mult_transpose(self.lp, self.ix, st.mult(self.lp, self.ix, self.a))
+
+    def warm(self):
+        """One application on 1/16 of the points (threads and code paths warm; seconds)."""
+        if self.sample is None:
+            self.sample = self.orc.stream(self.x[: max(1, self.x.shape[0] // 16)])
+        self._apply(self.sample)
+
+    def apply_seconds(self) -> float:
         t0 = time.perf_counter()
-        apply()
-        ts.append(time.perf_counter() - t0)
-    st.close()
-    t_apply = statistics.median(ts) * (x.shape[0] / ms)
-    sample = (f"one B^T(B a) (mult + multTranspose, FP64) on {ms} of the {x.shape[0]} points, "
-              f"median of 3 after 1 warm-up, {threads} OpenMP threads, scaled x{x.shape[0] / ms:g} "
-              f"to all points and x{cg_ops:g} operator applications per fit")
-    return t_apply * cg_ops, sample
+        self._apply(self.full)
+        return time.perf_counter() - t0
+
+    def close(self):
+        self.full.close()
+        if self.sample is not None:
+            self.sample.close()
+
+    def describe(self, reps: int, cg_ops: float) -> str:
+        return (f"one B^T(B a) (mult + multTranspose, FP64) on all {self.x.shape[0]} points per "
+                f"sample, median of {reps} after a warm-up on 1/16 of the points, {self.threads} "
+                f"OpenMP threads, x{cg_ops:g} operator applications per fit "
+                f"(ConjugateGradients.cpp:22-151)")
+
+
+def cpu_fit_seconds(x, grid_lp, grid_ix, cg_ops: float, threads: int, basis: str = "linear",
+                    reps: int = 3):
+    """Seconds per fit of the reference's CPU path: the median of `reps` applications of
+    B^T (B a) on all points (after a warm-up), times the operator applications of one CG fit.
+    Returns (seconds per fit, sample description)."""
+    ref = CpuReference(x, grid_lp, grid_ix, threads, basis)
+    ref.warm()
+    ts = [ref.apply_seconds() for _ in range(reps)]
+    ref.close()
+    return statistics.median(ts) * cg_ops, ref.describe(reps, cg_ops)
 
 
 def cg_operator_applications(iterations: int) -> float:
@@ -179,6 +213,26 @@ def grid_arrays(basis: str = "linear"):
     grid.getGenerator().regular(LEVEL)
     lp, ix = grid.getStorage().getLevelIndexArraysForEval()
     return grid, lp, ix
+
+
+def oracle_grid_arrays():
+    """The benchmark grid's eval arrays from the oracle's restatement of the reference's
+    regular-grid generator (the same point order; a ModLinear grid has the same points). The
+    reference arm uses these, so that it loads nothing of this library."""
+    from oracle import Oracle
+
+    lev, idx = Oracle().regular_grid(DIM, LEVEL)
+    return Oracle.eval_arrays(lev, idx)
+
+
+def bench_config(basis: str, n: int, m: int, epsilon: float, world: int) -> dict:
+    """The `config` object of both arms' lines (the same workload, so the same dict)."""
+    return {"workload": f"regression fit, regular {grid_name(basis)} grid d={DIM} level {LEVEL} "
+                        f"(N={n}), M={m} Gaussian-mixture points, lambda={LAMBDA}, CG to "
+                        f"relative residual {epsilon}",
+            "l2_policy": "inputs larger than L2: every system product streams the data term "
+                         "(GPU: the materialised subspace products, 5.4 GB at M=2^20) from memory",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 # Plain CG iterations of one fit to relative residual 1e-8 on this seeded workload, per basis
@@ -221,33 +275,39 @@ def hbm_peak_gbs():
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path (the oracle port of its STREAMING FP64
+    operator, all host cores): each step is one B^T (B a) on all points, the work of one CG
+    iteration; fits/s = 1 / (median step time x the operator applications of one fit). Warm-up
+    steps run on 1/16 of the points. Imports nothing of this library."""
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    x, y = make_workload(args.seed)
-    _, lp, ix = grid_arrays(args.basis)
+    x, _ = make_workload(args.seed)
+    lp, ix = oracle_grid_arrays()
+    n, m = lp.shape[0], x.shape[0]
     iters = args.reference_iterations or REFERENCE_ITERATIONS[args.basis]
     cg_ops = cg_operator_applications(iters)
-    times = []
-    sample = ""
-    for k in range(args.warmup + args.steps):
-        t_fit, sample = cpu_fit_seconds(x, lp, ix, cg_ops, threads, args.basis)
-        if k >= args.warmup:
-            times.append(t_fit)
-    sec = statistics.median(times)
-    value = 1.0 / sec
+    ref = CpuReference(x, lp, ix, threads, args.basis)
+    for _ in range(args.warmup):
+        ref.warm()
+    times = [ref.apply_seconds() for _ in range(args.steps)]
+    ref.close()
+    step = statistics.median(times)
+    value = 1.0 / (step * cg_ops)
     line = {
         "impl": "reference", "metric": "fits_per_sec", "value": value, "unit": "fits/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"regression fit, regular {grid_name(args.basis)} grid d={DIM} "
-                               f"level {LEVEL} (N=13441), M={M_POINTS} Gaussian-mixture points, "
-                               f"lambda={LAMBDA}",
-                   "cg_iterations_per_fit": iters, "l2_policy": "inputs larger than L2"},
+        "ms_per_step": sum(times) * 1e3 / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": bench_config(args.basis, n, m, args.epsilon, world),
+        "precision": "FP64 (the reference's STREAMING operator and ConjugateGradients)",
+        "step": "one B^T(B a) on all points (one CG iteration's operator work); fits/s = 1 / "
+                f"(median step x {cg_ops:g} operator applications per fit)",
+        "seconds_per_fit": step * cg_ops,
         "cpu_baseline": {"value": value, "unit": "fits/s", "cores": threads, "kind": "port",
-                         "sample": sample, "host": os.uname().machine},
+                         "sample": ref.describe(args.steps, cg_ops),
+                         "cg_iterations_per_fit": iters, "host": os.uname().machine},
         "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -277,6 +337,107 @@ def count_iterations(args):
                       "epsilon": args.epsilon, "seconds": time.perf_counter() - t0}), flush=True)
     op.close()
     return 0
+
+
+REGRESSION_FIXTURE = os.path.join(ROOT, "tests", "golden", "regression_d10_l5.npz")
+
+
+def workload_checksums(x: np.ndarray, y: np.ndarray) -> np.ndarray:
+    """Sums, sums of squares and a few entries of x and y; the regression fixture records them
+    (tests/golden/make_regression_alpha.py) so that a numpy whose generator streams differ is
+    noticed."""
+    return np.array([x.sum(), (x * x).sum(), y.sum(), (y * y).sum(), x[0, 0], x[-1, -1],
+                     y[0], y[-1]], dtype=np.float64)
+
+
+def reference_alpha(args, x, y):
+    """(alpha, note): the reference's own FP64 CG solution of this workload (SG++'s
+    SystemMatrixLeastSquaresIdentity + ConjugateGradients at epsilon 1e-12, committed as a
+    fixture), or (None, why not) when the run's workload is not the fixture's."""
+    if args.basis != "linear" or not os.path.exists(REGRESSION_FIXTURE):
+        return None, "no reference fixture for this workload"
+    f = np.load(REGRESSION_FIXTURE)
+    if int(f["seed"]) != args.seed or int(f["m"]) != x.shape[0]:
+        return None, "no reference fixture for this seed"
+    want = f["checksums"]
+    got = workload_checksums(x, y)
+    if not np.allclose(got, want, rtol=1e-12, atol=0.0):
+        return None, "the regenerated workload differs from the fixture's (numpy streams)"
+    return (f["alpha"], f"the reference's FP64 ConjugateGradients solution (epsilon "
+                        f"{float(f['epsilon']):g}, {int(f['iterations'])} iterations, "
+                        "tests/golden/regression_d10_l5.npz)")
+
+
+def dense_mult_gflops(args, grid, x, work_per_op, peak32, peak64):
+    """One launch each of the dense FP32 and native FP64 mult kernels (the STREAMING algorithm)
+    on the benchmark workload, untimed by the fits: GFLOP/s by the reference's count
+    (LearnerVectorizedPerformanceCalculator.cpp:89-109, 6 N M d per op) and the fraction of the
+    FP32 / FP64 FMA peak measured in this run (sgmev_fma_peak, 2 FLOP per FMA)."""
+    import sgpp_gb300 as sg
+
+    out = {}
+    for name, prec, kind, peak in (("fp32_dense", "float", sg.SGMEV_KERNEL_MULT_FP32, peak32),
+                                   ("fp64_dense", "double", sg.SGMEV_KERNEL_MULT_FP64, peak64)):
+        cfg = sg.OperationMultipleEvalConfiguration(
+            sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
+            parameters={"precision": prec, "algo": "dense", "materialize": "off"})
+        op = sg.createOperationMultipleEval(grid, x, cfg)
+        a = np.random.default_rng(3).standard_normal(grid.getSize())
+        out_m = np.zeros(x.shape[0])
+        op.mult(a, out_m)  # warm-up
+        op.profile(True)
+        for _ in range(args.dense_probe):
+            op.mult(a, out_m)
+        cnt, sec = op.profileRead(kind)
+        op.profile(False)
+        op.close()
+        if not cnt:
+            out[name] = None
+            continue
+        avg = sec / cnt
+        gflops = work_per_op / avg / 1e9
+        out[name] = {"gflops_ref_count": gflops, "ms_per_launch": avg * 1e3, "launches": cnt,
+                     "peak_gflops_measured": peak / 1e9, "frac_of_peak": gflops / (peak / 1e9)}
+    return out
+
+
+def plain_fp64_fit(args, grid, x, d_y, stream, mixed_fits_per_sec, local_rank):
+    """The plain per-problem FP64 path: one FP64-accurate CG fit (SGMEV_SOLVE_PLAIN, the
+    reference's algorithm) on a df64 operator, whose products stream the materialised
+    float-float subspace products, timed whole on the device after one warm-up fit."""
+    import torch
+
+    import sgpp_gb300 as sg
+
+    params = dict(kv.split("=", 1) for kv in args.param)
+    params["precision"] = "df64"
+    cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                sg.OperationMultipleEvalSubType.CUDA,
+                                                parameters=params)
+    op = sg.createOperationMultipleEval(grid, x, cfg)
+    op.setStream(stream.cuda_stream)
+    n = grid.getSize()
+    d_a = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local_rank}")
+    op.fitDevice(d_y.data_ptr(), d_a.data_ptr(), LAMBDA, 20000, args.epsilon,
+                 mode=sg.SGMEV_SOLVE_PLAIN)  # warm-up (builds the products)
+    times, its = [], []
+    for _ in range(args.plain_fp64_probe):
+        d_a.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        it, _ = op.fitDevice(d_y.data_ptr(), d_a.data_ptr(), LAMBDA, 20000, args.epsilon,
+                             mode=sg.SGMEV_SOLVE_PLAIN)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+        its.append(it)
+    op.close()
+    t = statistics.median(times)
+    return {"fits_per_sec": 1.0 / t, "ms_per_fit": t * 1e3, "cg_iterations": its,
+            "what": "SGMEV_SOLVE_PLAIN on a df64 operator (FP64-accurate float-float products "
+                    "streamed from the materialised subspace products), the reference's CG",
+            "speedup_mixed_vs_plain_fp64": mixed_fits_per_sec * t}
 
 
 def op_config(args):
@@ -319,10 +480,12 @@ def run_ours(args):
     d_alpha = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local_rank}")
     d_ref = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local_rank}")
 
-    # FP64 solution for the error check (untimed): refinement to a tight FP64 residual
+    # FP64 solutions for the error check (untimed): the reference's own CG solution of this
+    # workload (fixture) and this library's refinement to a tight FP64 residual
     it_ref, _ = op.fitDevice(d_y.data_ptr(), d_ref.data_ptr(), LAMBDA, 20000, args.ref_epsilon,
                              mode=sg.SGMEV_SOLVE_MIXED)
     alpha_ref = d_ref.cpu().numpy()
+    alpha_fixture, fixture_note = reference_alpha(args, x, y)
 
     def one_fit():
         return op.fitDevice(d_y.data_ptr(), d_alpha.data_ptr(), LAMBDA, 20000, args.epsilon,
@@ -375,6 +538,8 @@ def run_ours(args):
     op.profile(False)
     alpha = d_alpha.cpu().numpy()
     err = float(np.abs(alpha - alpha_ref).max() / np.abs(alpha_ref).max())
+    err_ref = (float(np.abs(alpha - alpha_fixture).max() / np.abs(alpha_fixture).max())
+               if alpha_fixture is not None else None)
 
     if dist:
         t = torch.tensor([total_s], device=f"cuda:{local_rank}")
@@ -416,10 +581,11 @@ def run_ours(args):
                     "peaks_measured_tflops": {"fp32": peak32 / 1e12, "fp64": peak64 / 1e12},
                     "flop_per_launch": work_per_op}
 
-    # mult GFLOP/s (reference count) of the FP32 mult kernel
-    mc, msec = kstats["mult_fp32"]
-    mult_tflops = work_per_op / (msec / max(mc, 1)) / 1e12 if mc else None
-
+    # mult GFLOP/s by the reference's count (6 N M d per op) of the dense kernels (the
+    # STREAMING algorithm: every grid point for every data point), against the FMA peaks
+    # measured in this run
+    mult_gflops = dense_mult_gflops(args, grid, x, work_per_op, peak32, peak64) \
+        if args.dense_probe else None
     # end to end through the public API from pinned host buffers
     e2e = None
     if args.e2e_steps > 0:
@@ -453,24 +619,10 @@ def run_ours(args):
                "sample": sample, "cg_iterations_per_fit": iters_fit,
                "host": os.uname().machine}
 
-    # plain FP64 path (same CG, native FP64 kernels): one timed B^T B application, scaled
-    t_fp64 = None
-    if args.plain_fp64_probe:
-        d_t = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local_rank}")
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        op.systemApplyDevice(d_alpha.data_ptr(), d_t.data_ptr(), LAMBDA * m)
-        e0.record(stream)
-        op.systemApplyDevice(d_alpha.data_ptr(), d_t.data_ptr(), LAMBDA * m)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        t_fp64 = e0.elapsed_time(e1) * 1e-3
-    plain = None
-    if t_fp64:
-        iters_plain = args.reference_iterations or REFERENCE_ITERATIONS[args.basis]
-        t_plain_fit = t_fp64 * cg_operator_applications(iters_plain)
-        plain = {"fits_per_sec": 1.0 / t_plain_fit, "system_apply_ms": t_fp64 * 1e3,
-                 "cg_iterations_per_fit": iters_plain,
-                 "speedup_mixed_vs_plain_fp64": value / world * t_plain_fit}
+    # plain FP64 path: one FP64-accurate plain CG fit (SGMEV_SOLVE_PLAIN) on the df64
+    # materialised products, the fastest FP64-accurate operator here, timed whole on the device
+    plain = plain_fp64_fit(args, grid, x, d_y, stream, value / world, local_rank) \
+        if args.plain_fp64_probe else None
 
     if rank == 0:
         lat = sorted(step_ms)
@@ -478,21 +630,21 @@ def run_ours(args):
         line = {
             "metric": "fits_per_sec", "value": value, "unit": "fits/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-            "data": "synthetic",
-            "config": {"workload": f"regression fit, regular {grid_name(args.basis)} grid "
-                                   f"d={DIM} level {LEVEL} (N={n}), M={m} Gaussian-mixture "
-                                   f"points, lambda={LAMBDA}, mixed-precision CG to relative "
-                                   f"FP64 residual {args.epsilon}",
-                       "l2_policy": "inputs larger than L2: every CG system product streams "
-                                    "the materialised subspace products (5.4 GB at M=2^20) from "
-                                    "HBM",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f16+f32+df64", "data": "synthetic",
+            "config": bench_config(args.basis, n, m, args.epsilon, world),
+            "precision": "mixed: inner CG in FP32 arithmetic on FP16 copies of the materialised "
+                         "subspace products (2^-11 relative per product) with FP64 vectors; "
+                         "outer iterative-refinement residual with FP64-accurate float-float "
+                         "(df64) products",
             "latency_ms": {"p50": p(0.5), "p99": p(0.99)},
-            "alpha_rel_err_vs_fp64": err, "cg_iterations": iters,
-            "fp64_solution_iterations": it_ref,
-            "mult_tflops_ref_count": mult_tflops,
-            "mult_frac_of_fp32_peak": (mult_tflops / (peak32 / 1e12)) if mult_tflops else None,
+            "alpha_rel_err_vs_fp64": err_ref if err_ref is not None else err,
+            "alpha_rel_err_vs_fp64_source": (fixture_note if err_ref is not None else
+                                             "this library's df64 refinement to relative "
+                                             f"residual {args.ref_epsilon} ({fixture_note})"),
+            "alpha_rel_err_vs_df64_refinement": err,
+            "cg_iterations": iters, "fp64_solution_iterations": it_ref,
+            "mult_gflops": mult_gflops,
             "kernel_stats": {k: {"launches": c, "ms_total": s * 1e3} for k, (c, s) in kstats.items()},
             "roofline": roofline, "clocks": clocks, "gpu_launches": int(launches),
             "e2e": e2e, "cpu_baseline": cpu, "plain_fp64_path": plain,
@@ -519,7 +671,10 @@ def main():
     ap.add_argument("--basis", default="linear", choices=["linear", "modlinear"])
     ap.add_argument("--count-iterations", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--plain-fp64-probe", type=int, default=1)
+    ap.add_argument("--plain-fp64-probe", type=int, default=2,
+                    help="timed plain FP64-accurate fits on a df64 operator (0: skip)")
+    ap.add_argument("--dense-probe", type=int, default=1,
+                    help="timed launches of the dense FP32 and FP64 mult kernels (0: skip)")
     ap.add_argument("--inner-tol", type=float, default=None,
                     help="inner tolerance of the mixed fits (library default when omitted)")
     ap.add_argument("--param", action="append", default=[], metavar="KEY=VALUE",

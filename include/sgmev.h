@@ -228,7 +228,10 @@ SGMEV_API int sgmev_fit_device(sgmev_op* op, int mode, const double* d_y, double
  */
 SGMEV_API double sgmev_get_duration(sgmev_op* op);
 
-/* Use `stream` (a cudaStream_t) for all following work of this op; NULL restores the op's own. */
+/* Use `stream` (a cudaStream_t) for all following work of this op; NULL restores the op's own.
+ * The new stream is made to wait (an event) for the work the op enqueued on the previous one, so
+ * sgmev_synchronize and sgmev_destroy (which frees on the current stream) cover the op's work on
+ * every stream it used. */
 SGMEV_API int sgmev_set_stream(sgmev_op* op, void* stream);
 
 /* Block until all work enqueued by this op has finished. */

@@ -32,6 +32,14 @@ def _ptr(a: np.ndarray):
     return a.ctypes.data_as(_vp)
 
 
+def reference_source() -> str | None:
+    """The reference checkout that the build recipe (oracle/ref.mk) and the fixture scripts read:
+    $SGPP_REFERENCE_SRC when set, else the build container's checkout; None when the sources are
+    not there (the GPU host has none, and nothing run there needs them)."""
+    path = os.environ.get("SGPP_REFERENCE_SRC") or "/root/reference"
+    return path if os.path.isdir(os.path.join(path, "base", "src")) else None
+
+
 def build() -> None:
     """Compile liboracle.so (gcc, seconds)."""
     subprocess.run(["make", "-s", "-C", _HERE], check=True)

@@ -11,7 +11,11 @@
 # Quirks needed with g++ 13: -include cstdint -include memory (missing includes in the
 # reference headers, e.g. base/src/sgpp/base/grid/storage/hashmap/HashGridPoint.hpp).
 
-REF ?= /root/reference
+# REF: the reference checkout (no default; __graft_entry__.build() passes the one that
+# oracle.reference_source() finds)
+ifndef REF
+$(error set REF=<reference checkout>)
+endif
 OUT := oracle/_ref
 OBJ := $(OUT)/obj
 

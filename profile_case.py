@@ -1,6 +1,6 @@
 """Run a few launches of one tile kernel on a synthetic case, for profilers (ncu) and timing.
 
-    python -m sgpp_gb300.profile_case --kernel mult --precision float --dim 10 --level 5 \
+    python profile_case.py --kernel mult --precision float --dim 10 --level 5 \
         --points 4194304 --launches 3
 
 Data are uniform on [0, 1]^d (seeded); the grid is the regular Linear grid of the given level.
@@ -15,7 +15,7 @@ import sys
 
 import numpy as np
 
-ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 

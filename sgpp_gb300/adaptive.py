@@ -32,6 +32,15 @@ if ROOT not in sys.path:
 import sgpp_gb300 as sg  # noqa: E402
 
 
+def adaptive_workload(seed: int = 3, m: int = 524288, dim: int = 8):
+    """The adaptive-grid configuration's data: x uniform on [0, 1]^dim (seeded),
+    y = prod_k 4 x_k (1 - x_k) + N(0, 0.01^2)."""
+    rng = np.random.default_rng(seed)
+    X = rng.random((m, dim))
+    y = np.prod(4.0 * X * (1.0 - X), axis=1) + 0.01 * rng.standard_normal(m)
+    return X, y
+
+
 def adaptive_fit(grid, X, y, lam: float, rounds: int, points_per_round: int,
                  epsilon: float = 1e-8, mode: int = sg.SGMEV_SOLVE_MIXED, precision="double",
                  on_round=None):
@@ -127,9 +136,7 @@ def main() -> int:
     ap.add_argument("--engine", choices=["fitter", "operator"], default="fitter")
     ap.add_argument("--throughput", action="store_true")
     args = ap.parse_args()
-    rng = np.random.default_rng(args.seed)
-    X = rng.random((args.points, args.dim))
-    y = np.prod(4.0 * X * (1.0 - X), axis=1) + 0.01 * rng.standard_normal(args.points)
+    X, y = adaptive_workload(args.seed, args.points, args.dim)
 
     if args.engine == "fitter":
         t0 = time.perf_counter()

@@ -8,38 +8,51 @@ namespace sgmev {
 
 namespace {
 std::mutex g_mu;
-std::vector<int> g_pool_ready;  // per device: release threshold raised
-std::vector<void*> g_pinned;    // recycled pinned blocks
+std::vector<cudaMemPool_t> g_pools;  // per device: the library's own pool (nullptr: not made yet)
+std::vector<void*> g_pinned;         // recycled pinned blocks
 constexpr size_t kPinnedBytes = 64;
 
-void prepare_pool() {
+// The library allocates from a pool of its own, not from the device's default pool: its release
+// threshold is raised so that freed blocks stay for the next operator, and raising it on the
+// default pool would stop every other cudaMallocAsync user of the process from returning memory.
+cudaMemPool_t library_pool() {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return;
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (static_cast<int>(g_pool_ready.size()) <= dev) g_pool_ready.resize(dev + 1, 0);
-  if (g_pool_ready[dev]) return;
-  cudaMemPool_t pool;
-  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-    uint64_t keep = UINT64_MAX;  // keep freed blocks for the next operator
-    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
   }
-  (void)cudaGetLastError();
-  g_pool_ready[dev] = 1;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (static_cast<int>(g_pools.size()) <= dev) g_pools.resize(dev + 1, nullptr);
+  if (g_pools[dev]) return g_pools[dev];
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  uint64_t keep = UINT64_MAX;  // keep freed blocks for the next operator
+  if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess)
+    (void)cudaGetLastError();
+  g_pools[dev] = pool;
+  return pool;
 }
 }  // namespace
 
 cudaError_t dev_malloc(void** p, size_t bytes, cudaStream_t s) {
-  prepare_pool();
   *p = nullptr;
-  cudaError_t e = cudaMallocAsync(p, bytes == 0 ? 1 : bytes, s);
+  cudaMemPool_t pool = library_pool();
+  if (!pool) return cudaErrorMemoryAllocation;
+  const size_t n = bytes == 0 ? 1 : bytes;
+  cudaError_t e = cudaMallocFromPoolAsync(p, n, pool, s);
   if (e == cudaErrorMemoryAllocation) {
     // hand the pool's unused blocks back to the device and try once more
     (void)cudaGetLastError();
-    int dev = 0;
-    cudaMemPool_t pool;
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
-      cudaMemPoolTrimTo(pool, 0);
-    e = cudaMallocAsync(p, bytes == 0 ? 1 : bytes, s);
+    cudaMemPoolTrimTo(pool, 0);
+    e = cudaMallocFromPoolAsync(p, n, pool, s);
   }
   if (e != cudaSuccess) {
     *p = nullptr;

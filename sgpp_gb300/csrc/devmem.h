@@ -8,8 +8,9 @@
 
 namespace sgmev {
 
-// cudaMallocAsync on `s` from the device's default pool, which keeps freed memory for reuse
-// (its release threshold is raised once per device); *p is nullptr on failure
+// stream-ordered allocation on `s` from the library's own memory pool on the current device
+// (created once per device; it keeps freed memory for reuse and is trimmed when an allocation
+// fails); *p is nullptr on failure
 cudaError_t dev_malloc(void** p, size_t bytes, cudaStream_t s);
 
 template <typename T>

@@ -176,13 +176,20 @@ extern "C" SGMEV_API int sgmev_mult_transpose_noalloc(int dim, int64_t n_grid,
   if (n_grid == 0) return SGMEV_OK;
   if (!d_level_pow2 || !d_index || !d_result || (n_data > 0 && (!d_data || !d_source)))
     return fail(SGMEV_ERR_INVALID, "NULL device pointer");
+  // an error another component left pending on this thread is drained here, so that the checks
+  // after the launches below report only this call's own failures
+  (void)cudaGetLastError();
   double* scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
   if (rc != SGMEV_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  int devnum = 0, sms = 152;
-  cudaGetDevice(&devnum);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, devnum);
+  int devnum = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&devnum);
+  if (e != cudaSuccess) return fail(SGMEV_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, devnum);
+  if (e != cudaSuccess || sms < 1)
+    return fail(SGMEV_ERR_CUDA, std::string("cudaDeviceGetAttribute(multiprocessor count): ") +
+                                    cudaGetErrorString(e));
 
   const bool templ = dim <= kMaxTemplDim;
   const int64_t tiles = templ ? ceil_div(n_grid, kBlock * kRG) : ceil_div(n_grid, kBlock);
@@ -211,11 +218,15 @@ extern "C" SGMEV_API int sgmev_mult_transpose_noalloc(int dim, int64_t n_grid,
                                                           d_data, d_source, n_data, chunk,
                                                           scratch);
   }
+  e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return fail(SGMEV_ERR_CUDA, std::string("no-alloc multTranspose launch: ") + cudaGetErrorString(e));
   const unsigned rblocks =
       static_cast<unsigned>(std::min<int64_t>(8 * int64_t(sms), ceil_div(n_grid, 256)));
   noalloc_reduce_kernel<<<rblocks, 256, 0, s>>>(scratch, static_cast<int>(nsplit), n_grid,
                                                 d_result);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return fail(SGMEV_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return fail(SGMEV_ERR_CUDA, std::string("no-alloc reduction launch: ") + cudaGetErrorString(e));
   return SGMEV_OK;
 }

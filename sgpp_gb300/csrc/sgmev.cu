@@ -114,6 +114,7 @@ struct sgmev_op {
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+  cudaEvent_t ev_switch = nullptr;  // orders a new stream after the work of the previous one
   double last_seconds = -1.0;
   int64_t launches = 0;
   bool precond = false;  // Jacobi-preconditioned inner CG in the mixed fits (params "precond")
@@ -1122,9 +1123,12 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
 }
 
 static void release(sgmev_op* op) {
-  // the operator's own work is done before its memory is handed back (a wait on its stream
-  // only; frees are stream-ordered and never synchronise the device)
+  // the operator's own work is done before its memory is handed back (a wait on its streams
+  // only; frees are stream-ordered and never synchronise the device). The current stream was
+  // ordered after every stream the op used before (sgmev_set_stream), so waiting on it and on
+  // the op's own stream covers all of the op's work.
   if (op->stream) cudaStreamSynchronize(op->stream);
+  if (op->own_stream && op->own_stream != op->stream) cudaStreamSynchronize(op->own_stream);
   subspace_free(&op->sub);
   void* ptrs[] = {op->xt64, op->xt32, op->xt32lo, op->li64, op->li32, op->gq, op->gs64, op->gs32, op->a64,
                   op->a32,  op->a32lo, op->v64,   op->v32,  op->v32lo, op->out64, op->part,
@@ -1135,6 +1139,7 @@ static void release(sgmev_op* op) {
   for (cudaEvent_t e : op->prof_events) cudaEventDestroy(e);
   if (op->ev_start) cudaEventDestroy(op->ev_start);
   if (op->ev_stop) cudaEventDestroy(op->ev_stop);
+  if (op->ev_switch) cudaEventDestroy(op->ev_switch);
   if (op->own_stream) cudaStreamDestroy(op->own_stream);
   (void)cudaGetLastError();
 }
@@ -1310,6 +1315,7 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
   op->stream = op->own_stream;
   CREATE_CUDA(cudaEventCreate(&op->ev_start));
   CREATE_CUDA(cudaEventCreate(&op->ev_stop));
+  CREATE_CUDA(cudaEventCreateWithFlags(&op->ev_switch, cudaEventDisableTiming));
   op->host_scalar = static_cast<double*>(pinned_block());
   if (!op->host_scalar) return bail(fail(SGMEV_ERR_OOM, "pinned host block"));
   CREATE_TRY(dalloc(op->stream, &op->dot_part, kDotBlocks));
@@ -1404,7 +1410,14 @@ SGMEV_API int sgmev_get_sizes(const sgmev_op* op, int* dim, int64_t* n_grid, int
 SGMEV_API int sgmev_set_stream(sgmev_op* op, void* stream) {
   using namespace sgmev;
   SGMEV_TRY(check_op(op));
-  op->stream = stream ? static_cast<cudaStream_t>(stream) : op->own_stream;
+  cudaStream_t next = stream ? static_cast<cudaStream_t>(stream) : op->own_stream;
+  if (next != op->stream) {
+    // work enqueued from now on (including stream-ordered frees of the op's buffers) runs after
+    // everything the op enqueued on the previous stream
+    SGMEV_CUDA(cudaEventRecord(op->ev_switch, op->stream));
+    SGMEV_CUDA(cudaStreamWaitEvent(next, op->ev_switch, 0));
+    op->stream = next;
+  }
   return SGMEV_OK;
 }
 

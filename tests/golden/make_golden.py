@@ -44,9 +44,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from oracle import REF_DEFAULT, REF_STREAMING, Reference  # noqa: E402
+from oracle import REF_DEFAULT, REF_STREAMING, Reference, reference_source  # noqa: E402
 
-REF_SRC = os.environ.get("SGPP_REFERENCE_SRC", "/root/reference")
+REF_SRC = reference_source() or ""
 
 
 def sha(a: np.ndarray) -> str:

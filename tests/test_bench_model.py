@@ -58,3 +58,41 @@ def test_peak_comes_from_the_measured_file():
     else:
         assert gbs == 6800.0 and "of fallback" in src
     assert np.isfinite(gbs) and gbs > 0
+
+
+def test_reference_arm_grid_matches_the_library_grid():
+    """The reference arm builds the grid with the oracle; it must be the benchmark grid in the
+    same point order as the library's (alpha indices line up)."""
+    _, lp, ix = bench.grid_arrays()
+    lp2, ix2 = bench.oracle_grid_arrays()
+    np.testing.assert_array_equal(lp, lp2)
+    np.testing.assert_array_equal(ix, ix2)
+
+
+def test_reference_arm_loads_nothing_of_the_library():
+    """bench.py --impl reference times the reference's CPU path only: its grid, data and timing
+    helpers import no module of this library (checked in a fresh interpreter)."""
+    import subprocess
+    import sys
+
+    code = ("import sys, numpy as np, bench\n"
+            "lp, ix = bench.oracle_grid_arrays()\n"
+            "x, y = bench.make_workload(42, m=2048)\n"
+            "ref = bench.CpuReference(x, lp, ix, 2)\n"
+            "ref.warm(); ref.apply_seconds(); ref.close()\n"
+            "bad = [k for k in sys.modules if k.startswith('sgpp_gb300')]\n"
+            "assert not bad, bad\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_both_arms_print_the_same_config():
+    a = bench.bench_config("linear", 13441, 1 << 20, 1e-8, 1)
+    b = bench.bench_config("linear", 13441, 1 << 20, 1e-8, 1)
+    assert a == b and "13441" in a["workload"] and "1e-08" in a["workload"]
+    assert "mixed" not in a["workload"]  # the precision scheme is a key of its own
+
+
+def test_cpu_operator_count_per_fit():
+    # ConjugateGradients.cpp:22-151: one B^T B per iteration, a true residual every 50, b = B^T y
+    assert bench.cg_operator_applications(75) == 75 + 1 + 0.5

@@ -1,0 +1,109 @@
+"""GPU parity at the configurations' own sizes.
+
+* Plain-method configuration (Grid::createLinearGrid(5) regular(6): N = 5,503; M = 65,536 points
+  uniform on [0, 1]^5, seed 42; alpha, v ~ N(0, 1)): one mult and one multTranspose of every
+  precision and algorithm against the oracle's restatement of the reference's STREAMING operator
+  (pinned against the reference's own outputs by test_oracle_golden.py), at 1e-12 relative for the
+  FP64-accurate kernels and 1e-4 for FP32.
+* Adaptive-grid configuration (d = 8, start level 4, M = 2^19, 6 rounds of 40 refined points,
+  lambda = 1e-4): the grid after every round and the final alpha against the reference's own loop
+  (tests/golden/adaptive_d8_l4.npz, SG++'s grid, HashRefinement, SystemMatrixLeastSquaresIdentity
+  and ConjugateGradients at epsilon 1e-12). The reference appends refined points in its hash map's
+  order, so points are matched by (level, index), not by position.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, rel_err
+
+import bench
+import sgpp_gb300 as sg
+from sgpp_gb300.adaptive import adaptive_fit, adaptive_workload
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu(lib):
+    if lib.sgmev_device_count() < 1:
+        pytest.fail("no CUDA device visible to libsgpp_gb300 (the GPU tests need one)")
+
+
+def _op(grid, x, precision, algo):
+    params = {"precision": precision, "algo": "subspace" if algo == "materialized" else algo}
+    if algo in ("subspace", "materialized"):
+        params["materialize"] = "on" if algo == "materialized" else "off"
+        params["materialize_multt"] = "on" if algo == "materialized" else "off"
+    cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                sg.OperationMultipleEvalSubType.CUDA,
+                                                parameters=params)
+    return sg.createOperationMultipleEval(grid, x, cfg)
+
+
+@pytest.fixture(scope="module")
+def plain_config(oracle):
+    rng = np.random.default_rng(42)
+    d, level, m = 5, 6, 65536
+    x = rng.random((m, d))
+    grid = sg.Grid.createLinearGrid(d)
+    grid.getGenerator().regular(level)
+    assert grid.getSize() == 5503
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    alpha = rng.standard_normal(grid.getSize())
+    v = rng.standard_normal(m)
+    st = oracle.stream(x)
+    ref_m = st.mult(lp, ix, alpha)
+    ref_t = st.mult_transpose(lp, ix, v)
+    st.close()
+    return grid, x, alpha, v, ref_m, ref_t
+
+
+@pytest.mark.parametrize("precision,tol,algo", [("double", FP64_TOL, "dense"),
+                                                ("double", FP64_TOL, "auto"),
+                                                ("df64", FP64_TOL, "dense"),
+                                                ("df64", FP64_TOL, "subspace"),
+                                                ("df64", FP64_TOL, "materialized"),
+                                                ("float", FP32_TOL, "dense"),
+                                                ("float", FP32_TOL, "subspace"),
+                                                ("float", FP32_TOL, "materialized")])
+def test_plain_method_configuration_at_full_size(plain_config, precision, tol, algo):
+    grid, x, alpha, v, ref_m, ref_t = plain_config
+    op = _op(grid, x, precision, algo)
+    out = np.zeros(x.shape[0])
+    op.mult(alpha, out)
+    assert rel_err(out, ref_m) < tol
+    outt = np.zeros(grid.getSize())
+    op.multTranspose(v, outt)
+    assert rel_err(outt, ref_t) < tol
+    op.close()
+
+
+def _keyed(level, index):
+    return {(tuple(l), tuple(i)): k for k, (l, i) in
+            enumerate(zip(np.asarray(level, np.int64).tolist(), np.asarray(index, np.int64).tolist()))}
+
+
+@pytest.mark.parametrize("mode,tol", [(sg.SGMEV_SOLVE_PLAIN, 1e-9), (sg.SGMEV_SOLVE_MIXED, 1e-6)])
+def test_adaptive_configuration_matches_reference_loop(mode, tol):
+    f = np.load(os.path.join(GOLDEN, "adaptive_d8_l4.npz"))
+    d, level, m = int(f["dim"]), int(f["start_level"]), int(f["m"])
+    x, y = adaptive_workload(int(f["seed"]), m, d)
+    np.testing.assert_allclose(bench.workload_checksums(x, y), f["checksums"], rtol=1e-12)
+    grid = sg.Grid.createLinearGrid(d)
+    grid.getGenerator().regular(level)
+    alpha, records = adaptive_fit(grid, x, y, float(f["lambda"]), int(f["rounds"]),
+                                  int(f["per_round"]), epsilon=float(f["epsilon"]), mode=mode,
+                                  precision="df64")
+    assert [r["n_grid"] for r in records] == [int(s) for s in f["sizes"]]
+    st = grid.getStorage()
+    ours = _keyed(st.level, st.index)
+    theirs = _keyed(f["level"], f["index"])
+    assert set(ours) == set(theirs)
+    order = np.array([ours[k] for k in theirs])  # reference position -> our position
+    ref_alpha = f["alpha"][np.array(list(theirs.values()))]
+    assert rel_err(alpha[order], ref_alpha) < tol

@@ -18,13 +18,14 @@ import numpy as np
 import pytest
 
 from conftest import load_golden, rel_err
+from oracle import reference_source
 
 import sgpp_gb300 as sg
 
 G = load_golden("datasets.npz")
 CASES = [str(c) for c in G["cases"]]
 OPTIONS = [json.loads(str(o)) for o in G["options"]]
-REF_SRC = os.environ.get("SGPP_REFERENCE_SRC", "/root/reference")
+REF_SRC = reference_source() or ""
 
 
 def _read(fmt, text, header, opt):

@@ -13,8 +13,9 @@ import subprocess
 import pytest
 
 from conftest import ROOT
+from oracle import reference_source
 
-REF = "/root/reference"
+REF = reference_source() or ""
 REF_LIB = os.path.join(ROOT, "oracle", "_ref")
 
 DRIVER = r"""
@@ -163,7 +164,7 @@ int main() {
 
 
 def _have_reference():
-    return (os.path.isdir(os.path.join(REF, "base", "src"))
+    return (bool(REF) and os.path.isdir(os.path.join(REF, "base", "src"))
             and os.path.exists(os.path.join(REF_LIB, "libsgpp_ref.so")))
 
 

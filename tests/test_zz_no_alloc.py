@@ -4,8 +4,9 @@ Such callers — an application whose own memory manager owns the whole device b
 latency-critical loop that cannot afford the implicit synchronisation of cudaMalloc / cudaFree —
 pass device buffers they already own; the entry point keeps its scratch in a fixed array inside
 the library. This test calls it through the C ABI and compares it with the existing entry point
-(sgmev_mult_transpose on an operator) at the FP64 tolerance of the other parity tests, on two
-calls in a row with different inputs (the shared scratch must not leak between calls).
+(sgmev_mult_transpose on an operator) and with the oracle's FP64 multTranspose, at the FP64
+tolerance of the other parity tests, on two calls in a row with different inputs (the shared
+scratch must not leak between calls), and checks that an empty data set gives zeros.
 
 The file is named so that pytest collects it last.
 """
@@ -15,6 +16,7 @@ import numpy as np
 import pytest
 
 import sgpp_gb300 as sg
+from oracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -30,6 +32,7 @@ def test_noalloc_matches_existing_entry_point_on_two_calls(lib, dim, level, m):
     torch = pytest.importorskip("torch")
     if lib.sgmev_device_count() < 1:
         pytest.fail("no CUDA device visible")
+    orc = Oracle()
     rng = np.random.default_rng(100 + dim)
     grid = sg.Grid.createLinearGrid(dim)
     grid.getGenerator().regular(level)
@@ -57,7 +60,30 @@ def test_noalloc_matches_existing_entry_point_on_two_calls(lib, dim, level, m):
         got = d_out.cpu().numpy()
         assert np.isfinite(got).all()
         assert _rel(got, expected) < FP64_TOL, (call, _rel(got, expected))
+        ref = orc.mult_transpose_naive(lp, ix, x, v)
+        assert _rel(got, ref) < FP64_TOL, (call, _rel(got, ref))
     op.close()
+
+
+def test_noalloc_empty_data_gives_zeros(lib):
+    torch = pytest.importorskip("torch")
+    if lib.sgmev_device_count() < 1:
+        pytest.fail("no CUDA device visible")
+    grid = sg.Grid.createLinearGrid(4)
+    grid.getGenerator().regular(3)
+    n = grid.getSize()
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    dev = torch.device("cuda:0")
+    d_lp = torch.from_numpy(np.ascontiguousarray(lp)).to(dev)
+    d_ix = torch.from_numpy(np.ascontiguousarray(ix)).to(dev)
+    d_out = torch.full((n,), float("nan"), dtype=torch.float64, device=dev)
+    vp = ctypes.c_void_p
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    rc = lib.sgmev_mult_transpose_noalloc(4, n, vp(d_lp.data_ptr()), vp(d_ix.data_ptr()), 0, None,
+                                          None, vp(d_out.data_ptr()), vp(stream or None))
+    assert rc == sg.SGMEV_OK, lib.sgmev_last_error()
+    torch.cuda.synchronize(dev)
+    assert (d_out.cpu().numpy() == 0.0).all()
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(lib):
