@@ -476,6 +476,12 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     op = sg.createOperationMultipleEval(grid, x, op_config(args))  # FP64 op + FP32 copies
     op.setStream(stream.cuda_stream)
+    tuned = None
+    if args.autotune:
+        from sgpp_gb300 import autotune
+
+        # launch shapes of the inner solves' kernels, searched once per device and shape (untimed)
+        tuned = autotune.tune_and_cache(op, grid, m, ["multT16"])
     d_y = torch.from_numpy(y).to(f"cuda:{local_rank}")
     d_alpha = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local_rank}")
     d_ref = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local_rank}")
@@ -647,12 +653,107 @@ def run_ours(args):
             "mult_gflops": mult_gflops,
             "kernel_stats": {k: {"launches": c, "ms_total": s * 1e3} for k, (c, s) in kstats.items()},
             "roofline": roofline, "clocks": clocks, "gpu_launches": int(launches),
+            "launch_shape": tuned,
             "e2e": e2e, "cpu_baseline": cpu, "plain_fp64_path": plain,
         }
         print(json.dumps(line), flush=True)
     op.close()
     if dist:
         dist.destroy_process_group()
+    return 0
+
+
+def run_block(args):
+    """16 regression fits sharing the benchmark's grid and data (targets y and y + N(0, 1) noise)
+    through sgmev_fit_block: BF16 tensor-core inner solves over the 16 columns, df64 outer
+    residuals. value = fits/s (16 per step); compared with 16 single-target mixed fits."""
+    import torch
+
+    import sgpp_gb300 as sg
+    from sgpp_gb300 import autotune
+
+    torch.cuda.set_device(0)
+    x, y = make_workload(args.seed)
+    grid, lp, ix = grid_arrays(args.basis)
+    n, m = grid.getSize(), x.shape[0]
+    K = sg.SGMEV_BLOCK_RHS
+    rng = np.random.default_rng(args.seed + 1)
+    Y = np.empty((K, m))
+    Y[0] = y
+    Y[1:] = y + rng.standard_normal((K - 1, m))
+    stream = torch.cuda.Stream()
+    op = sg.createOperationMultipleEval(grid, x, op_config(args))
+    op.setStream(stream.cuda_stream)
+    tuned = None
+    if args.autotune:
+        tuned = autotune.tune_and_cache(op, grid, m, ["block"])
+    d_y = torch.from_numpy(Y).cuda()
+    d_a = torch.zeros((K, n), dtype=torch.float64, device="cuda")
+    for _ in range(args.warmup):
+        op.fitBlockDevice(d_y.data_ptr(), d_a.data_ptr(), LAMBDA, 100000, args.epsilon)
+    op.profile(True)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms, its = [], None
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        its, res = op.fitBlockDevice(d_y.data_ptr(), d_a.data_ptr(), LAMBDA, 100000, args.epsilon)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    clocks = sampler.stop()
+    kst = {k: op.profileRead(kind) for k, kind in (("block_mult", sg.SGMEV_KERNEL_BLOCK_MULT),
+                                                   ("block_multT", sg.SGMEV_KERNEL_BLOCK_MULTT),
+                                                   ("mult_matdf64", sg.SGMEV_KERNEL_MULT_MATDF),
+                                                   ("multT_matdf64", sg.SGMEV_KERNEL_MULTT_MATDF))}
+    op.profile(False)
+    alpha = d_a.cpu().numpy()
+    ref, note = reference_alpha(args, x, y)
+    err0 = float(np.abs(alpha[0] - ref).max() / np.abs(ref).max()) if ref is not None else None
+    # one single-target mixed fit (the per-problem path), timed, and its alpha for column K-1
+    d_y1 = torch.from_numpy(Y[K - 1].copy()).cuda()
+    d_a1 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    op.fitDevice(d_y1.data_ptr(), d_a1.data_ptr(), LAMBDA, 100000, args.epsilon,
+                 mode=sg.SGMEV_SOLVE_MIXED)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    it1, _ = op.fitDevice(d_y1.data_ptr(), d_a1.data_ptr(), LAMBDA, 100000, args.epsilon,
+                          mode=sg.SGMEV_SOLVE_MIXED)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    single_ms = e0.elapsed_time(e1)
+    a1 = d_a1.cpu().numpy()
+    err_last = float(np.abs(alpha[K - 1] - a1).max() / np.abs(a1).max())
+    op.close()
+    step = statistics.median(ms)
+    value = K / (step * 1e-3)
+    bm = kst["block_mult"]
+    bt = kst["block_multT"]
+    line = {
+        "metric": "fits_per_sec", "value": value, "unit": "fits/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step,
+        "higher_is_better": True, "workload": "block",
+        "config": {"workload": f"16 regression fits sharing one grid and data set: "
+                               f"{bench_config(args.basis, n, m, args.epsilon, 1)['workload']}; "
+                               "targets y and y + N(0, 1)"},
+        "dtype": "bf16 (tensor cores, FP32 accumulation) + df64",
+        "precision": "inner block CG on BF16 tcgen05 products (products rounded to BF16, vectors "
+                     "as BF16 high + low parts, FP32 accumulation in tensor memory), FP64 vectors; "
+                     "outer residuals with FP64-accurate float-float products per column",
+        "inner_cg_steps_per_column": [int(v) for v in its],
+        "alpha_rel_err_vs_fp64_column0": err0, "alpha_rel_err_source": note,
+        "alpha_rel_err_vs_single_mixed_fit_column15": err_last,
+        "single_target_mixed_fit_ms": single_ms, "single_target_iterations": it1,
+        "speedup_vs_16_single_fits": 16 * single_ms / step,
+        "block_kernels": {"mult": {"launches": bm[0], "ms_avg": bm[1] / max(bm[0], 1) * 1e3},
+                          "multT": {"launches": bt[0], "ms_avg": bt[1] / max(bt[0], 1) * 1e3}},
+        "df64_residual_ms": (kst["mult_matdf64"][1] + kst["multT_matdf64"][1]) * 1e3 / args.steps,
+        "launch_shape": tuned, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -677,6 +778,10 @@ def main():
                     help="timed launches of the dense FP32 and FP64 mult kernels (0: skip)")
     ap.add_argument("--inner-tol", type=float, default=None,
                     help="inner tolerance of the mixed fits (library default when omitted)")
+    ap.add_argument("--workload", default="regression", choices=["regression", "block"],
+                    help="block: 16 fits sharing the data (tensor-core block fits)")
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="pick launch shapes with sgpp_gb300.autotune before timing (cached)")
     ap.add_argument("--param", action="append", default=[], metavar="KEY=VALUE",
                     help="operator knob passed to createOperationMultipleEval (repeatable)")
     args = ap.parse_args()
@@ -686,6 +791,8 @@ def main():
         return run_reference(args)
     if args.count_iterations:
         return count_iterations(args)
+    if args.workload == "block":
+        return run_block(args)
     return run_ours(args)
 
 

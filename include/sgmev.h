@@ -106,6 +106,9 @@ SGMEV_API int sgmev_device_count(void);
  * "half" (default) or "float" — the inner FP32 solves of mixed fits stream an FP16 copy of the
  * products (2.5-3 bytes per entry instead of 4.5-5; the FP64-accurate outer residual keeps the result
  * exact to the fit's tolerance).
+ * "multt_batch": "1" (default), "2" or "4" — points per read-modify-write round of the owner's
+ * cell sums in the FP16 multTranspose (the same bits for each; a launch-shape choice of the
+ * autotuner, sgpp_gb300.autotune).
  * "basis": "linear" (default) or "modlinear" — the basis of the grid. level_pow2/index stay the
  * (2^l, i) arrays of getLevelIndexArraysForEval for both (a ModLinear grid has the same points).
  * ModLinear functions next to a face extrapolate linearly beyond it, as the reference's mask
@@ -234,11 +237,59 @@ SGMEV_API double sgmev_get_duration(sgmev_op* op);
  * every stream it used. */
 SGMEV_API int sgmev_set_stream(sgmev_op* op, void* stream);
 
+/* Change launch-shape knobs of a live operator: params_json may hold only "multt_batch" and the
+ * "block_mult_tiles", "block_mult_groups", "block_multt_groups", "block_stages" knobs (see
+ * sgmev_create); they change no result bits except how the block products are cut into launches.
+ * No counterpart in the reference (whose OpenCL kernels take such parameters from a
+ * configuration file written by StaticParameterTuner,
+ * datadriven/src/sgpp/datadriven/application/StaticParameterTuner.cpp:297-417); used by the
+ * autotuner (sgpp_gb300.autotune). Waits for the op's stream first. */
+SGMEV_API int sgmev_set_params(sgmev_op* op, const char* params_json);
+
 /* Block until all work enqueued by this op has finished. */
 SGMEV_API int sgmev_synchronize(sgmev_op* op);
 
 /* Number of kernels this op launched so far (instrumentation for benchmarks). */
 SGMEV_API int64_t sgmev_kernel_launches(const sgmev_op* op);
+
+/* ---- 16 right-hand sides: BF16 tensor-core products and fits ---------------------------- */
+/*
+ * The same operator applied to 16 vectors at once, on the 5th-generation tensor cores: per tile of
+ * 128 data points and group of 128 grid positions, the products of the materialised subspace
+ * products (rounded to BF16, 2^-8 relative) with the 16 vectors (split into BF16 high and low
+ * parts, about 2^-16) are tcgen05 MMAs accumulating in FP32. No counterpart in the reference,
+ * which applies OperationMultipleEval::mult / multTranspose (OperationMultipleEval.hpp:55, :81)
+ * to one vector at a time; column k here equals those products of vector k to BF16 accuracy.
+ * Needs the subspace algorithm with materialised products (params "algo": "subspace", the default
+ * where it pays) and subspaces of at most 128 cells; otherwise SGMEV_ERR_UNSUPPORTED.
+ * Vectors are column-major: vector k of length n at offset k * n. Host buffers; blocks.
+ * params "block_inner_tol" (default "1e-3"): inner tolerance of sgmev_fit_block; "block_mult_tiles",
+ * "block_mult_groups", "block_multt_groups", "block_stages": launch shape (the autotuner's
+ * choices, sgpp_gb300.autotune).
+ */
+#define SGMEV_BLOCK_RHS 16
+SGMEV_API int sgmev_mult_block(sgmev_op* op, const double* alpha, double* result);
+SGMEV_API int sgmev_mult_transpose_block(sgmev_op* op, const double* source, double* result);
+
+/*
+ * 16 regression fits sharing one operator (one grid, one data set, 16 target vectors y_k):
+ * per column the system of SystemMatrixLeastSquaresIdentity::mult / generateb
+ * (datadriven/src/sgpp/datadriven/algorithm/SystemMatrixLeastSquaresIdentity.cpp:32-56) solved
+ * as ConjugateGradients::solve would (solver/src/sgpp/solver/sle/ConjugateGradients.cpp:22-151),
+ * by mixed-precision iterative refinement: b_k = B^T y_k and the outer residuals b_k - A alpha_k
+ * with the FP64-accurate df64 products, the inner correction solves as one block CG over the 16
+ * columns on the BF16 tensor-core products (each column its own CG scalars); a column stops when
+ * ||b_k - A alpha_k||^2 <= epsilon^2 ||b_k||^2. y: [16 x n_data] column-major; alpha: [16 x n_grid]
+ * out (cold start); iterations[16]: inner CG steps of each column; residuals[16]: the final
+ * ||b_k - A alpha_k||^2 (either may be NULL).
+ */
+SGMEV_API int sgmev_fit_block(sgmev_op* op, const double* y, double lambda,
+                              int64_t max_iterations, double epsilon, double* alpha,
+                              int64_t* iterations, double* residuals);
+/* sgmev_fit_block with y and alpha as device pointers (column-major doubles). Blocks. */
+SGMEV_API int sgmev_fit_block_device(sgmev_op* op, const double* d_y, double lambda,
+                                     int64_t max_iterations, double epsilon, double* d_alpha,
+                                     int64_t* iterations, double* residuals);
 
 /* ---- batched fits: many independent problems, continuous batching ----------------------- */
 /*

@@ -44,6 +44,8 @@ SGMEV_API int sgmev_fma_peak(int precision, double* flops_per_second, int* sm_cl
 #define SGMEV_KERNEL_SYSTEM_MAT32 14 /* FP32 B^T (B a) in one pass over them */
 #define SGMEV_KERNEL_MULT_MAT16 15 /* mult streaming their FP16 copy (inner solves of mixed fits) */
 #define SGMEV_KERNEL_MULTT_MAT16 16 /* multTranspose streaming it */
+#define SGMEV_KERNEL_BLOCK_MULT 17  /* B [a_1 .. a_16], BF16 tensor-core tiles */
+#define SGMEV_KERNEL_BLOCK_MULTT 18 /* B^T [v_1 .. v_16], BF16 tensor-core tiles */
 SGMEV_API int sgmev_profile(sgmev_op* op, int enable);
 SGMEV_API int sgmev_profile_read(sgmev_op* op, int kind, int64_t* launches, double* seconds);
 

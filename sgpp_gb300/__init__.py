@@ -65,7 +65,8 @@ EXPORTED_SYMBOLS = (
     "sgmev_batch_remove", "sgmev_batch_step", "sgmev_batch_solve", "sgmev_batch_result",
     "sgmev_batch_info", "sgdata_size", "sgdata_read", "sgfit_config_defaults", "sgfit_create",
     "sgfit_destroy", "sgfit_fit", "sgfit_adapt", "sgfit_update", "sgfit_evaluate", "sgfit_grid",
-    "sgfit_alpha", "sgfit_stats",
+    "sgfit_alpha", "sgfit_stats", "sgmev_mult_block", "sgmev_mult_transpose_block",
+    "sgmev_fit_block", "sgmev_fit_block_device", "sgmev_set_params",
 )
 
 SGMEV_KERNEL_MULT_FP32 = 0
@@ -85,6 +86,9 @@ SGMEV_KERNEL_MULTT_MATDF = 13
 SGMEV_KERNEL_SYSTEM_MAT32 = 14
 SGMEV_KERNEL_MULT_MAT16 = 15
 SGMEV_KERNEL_MULTT_MAT16 = 16
+SGMEV_KERNEL_BLOCK_MULT = 17
+SGMEV_KERNEL_BLOCK_MULTT = 18
+SGMEV_BLOCK_RHS = 16
 
 
 # ---- exceptions (base/src/sgpp/base/exception/) --------------------------------------------
@@ -123,7 +127,8 @@ def _vp(a: Optional[np.ndarray]):
 # operator parameters passed to sgmev_create (the other configuration parameters, such as
 # "precision", are read by the Python side)
 OP_KNOBS = ("precond", "algo", "inner_tol", "materialize", "materialize_multt", "inner_products",
-            "system_product")
+            "system_product", "block_inner_tol", "block_mult_tiles", "block_mult_groups",
+            "block_multt_groups", "block_stages", "multt_batch")
 
 
 def load_library(path: str = LIBRARY_PATH):
@@ -164,6 +169,11 @@ def load_library(path: str = LIBRARY_PATH):
         "sggrid_level_index_for_eval": (c_int, [c_int, i64, vp, vp, vp, vp]),
         "sgmev_fma_peak": (c_int, [c_int, pdbl, ctypes.POINTER(c_int)]),
         "sgmev_fit_device": (c_int, [vp, c_int, vp, dbl, i64, dbl, c_int, vp, pi64, pdbl]),
+        "sgmev_mult_block": (c_int, [vp, vp, vp]),
+        "sgmev_set_params": (c_int, [vp, ctypes.c_char_p]),
+        "sgmev_mult_transpose_block": (c_int, [vp, vp, vp]),
+        "sgmev_fit_block": (c_int, [vp, vp, dbl, i64, dbl, vp, vp, vp]),
+        "sgmev_fit_block_device": (c_int, [vp, vp, dbl, i64, dbl, vp, vp, vp]),
         "sgmev_mult_transpose_noalloc": (c_int, [c_int, i64, vp, vp, i64, vp, vp, vp, vp]),
         "sgmev_batch_create": (c_int, [ctypes.POINTER(vp), c_int, c_int, i64, i64, ctypes.c_char_p]),
         "sgmev_batch_destroy": (c_int, [vp]),
@@ -635,6 +645,54 @@ class OperationMultiEvalCuda:
                                         float(epsilon), 0 if alpha is None else 1,
                                         _vp(alpha_out), ctypes.byref(it), ctypes.byref(res)))
         return alpha_out, int(it.value), float(res.value)
+
+    def setParams(self, params: dict) -> None:
+        """Change launch-shape knobs (multt_batch, block_*) of this live operator."""
+        pj = json.dumps({k: str(v) for k, v in params.items()}).encode()
+        _check(load_library().sgmev_set_params(self._h, pj))
+
+    # ---- 16 right-hand sides on the tensor cores (no counterpart in the reference) -----------
+    def _block(self, a, rows: int, name: str):
+        a = np.ascontiguousarray(a, np.float64)
+        if a.shape != (SGMEV_BLOCK_RHS, rows):
+            raise OperationException(f"{name} must be [{SGMEV_BLOCK_RHS} x {rows}] (one row per vector)")
+        return a
+
+    def multBlock(self, alpha):
+        """[16 x n_data] = the mult of each of the 16 rows of alpha [16 x n_grid] (BF16 tensor
+        cores: products rounded to BF16, vectors to about 2^-16, FP32 accumulation)."""
+        a = self._block(alpha, self._n, "alpha")
+        out = np.zeros((SGMEV_BLOCK_RHS, self._m))
+        _check(load_library().sgmev_mult_block(self._h, _vp(a), _vp(out)))
+        return out
+
+    def multTransposeBlock(self, source):
+        """[16 x n_grid] = the multTranspose of each of the 16 rows of source [16 x n_data]."""
+        v = self._block(source, self._m, "source")
+        out = np.zeros((SGMEV_BLOCK_RHS, self._n))
+        _check(load_library().sgmev_mult_transpose_block(self._h, _vp(v), _vp(out)))
+        return out
+
+    def fitBlock(self, y, lam: float, imax: int, epsilon: float):
+        """16 regression fits sharing this operator: y [16 x n_data] -> (alpha [16 x n_grid],
+        inner CG steps per column, final ||b - A alpha||^2 per column)."""
+        yv = self._block(y, self._m, "y")
+        alpha = np.zeros((SGMEV_BLOCK_RHS, self._n))
+        its = np.zeros(SGMEV_BLOCK_RHS, np.int64)
+        res = np.zeros(SGMEV_BLOCK_RHS)
+        _check(load_library().sgmev_fit_block(self._h, _vp(yv), float(lam), int(imax),
+                                              float(epsilon), _vp(alpha), _vp(its), _vp(res)))
+        return alpha, its, res
+
+    def fitBlockDevice(self, d_y: int, d_alpha: int, lam: float, imax: int, epsilon: float):
+        """fitBlock on device pointers (column-major float64 [16][n_data] and [16][n_grid])."""
+        its = np.zeros(SGMEV_BLOCK_RHS, np.int64)
+        res = np.zeros(SGMEV_BLOCK_RHS)
+        _check(load_library().sgmev_fit_block_device(self._h, ctypes.c_void_p(d_y), float(lam),
+                                                     int(imax), float(epsilon),
+                                                     ctypes.c_void_p(d_alpha), _vp(its),
+                                                     _vp(res)))
+        return its, res
 
 
 class BatchEngine:

@@ -26,7 +26,7 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall",
              "-I" + os.path.join(ROOT, "include")]
 
 CU_SOURCES = ["sgmev.cu", "dense_mod.cu", "peak.cu", "noalloc.cu", "batch.cu", "subspace.cu",
-              "subspace_mat.cu", "devmem.cu", "fitter.cu"]
+              "subspace_mat.cu", "devmem.cu", "fitter.cu", "block_tc.cu"]
 CPP_SOURCES = ["grid.cpp", "datasets.cpp"]
 
 

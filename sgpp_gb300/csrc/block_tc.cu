@@ -1,0 +1,881 @@
+// Products with 16 right-hand sides on the tensor cores: BF16 tcgen05 MMAs over weighted one-hot
+// tiles of the materialised subspace products (the scheme is described in block_tc.h).
+//
+// Both kernels run one CTA per SM: eight producer warps and one MMA warp.
+//   producers  read the packed BF16 products (2 bytes + the cell index per point and subspace,
+//              one 32-bit load) of a tile of 128 points and a group of 16 chunks and write the
+//              tile's rows of E into a shared-memory stage: 16 bytes per point and chunk, one
+//              non-zero BF16 per point and subspace (thread = point and half a group);
+//   MMA warp   one thread waits for a full stage and issues its eight 128 x 32 x 16 MMAs, then
+//              commits them to the stage's "empty" barrier, which frees the stage for the
+//              producers once the tensor cores have read it.
+// A stage holds 128 points x 16 chunks in the canonical no-swizzle layout: the 16-byte chunk of
+// point p and chunk q at (p / 8) * 2048 + q * 128 + (p % 8) * 16. Read K-major it is the A
+// operand of mult (M = points, K = rows); read MN-major it is the A operand of multT (M = rows,
+// K = points). Every wait is bounded: a wait that runs out sets the status word and the CTA
+// finishes without further work, after its issued MMAs have completed and its tensor memory is
+// freed.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "block_tc.h"
+#include "devmem.h"
+#include "tc_ptx.cuh"
+
+namespace sgmev {
+namespace {
+
+constexpr int kProdWarps = 8;
+constexpr int kProdThreads = kProdWarps * 32;
+constexpr int kBlockThreads = kProdThreads + 32;  // + the MMA warp
+constexpr uint32_t kStageBytes = 128u * 16u * 16u;  // 128 points x 16 chunks x 16 bytes
+constexpr uint32_t kCoefBytes = 4096u * 2u;         // 128 rows x 32 columns of BF16
+constexpr uint32_t kQBytes = 4096u * 2u;            // 128 points x 32 columns of BF16
+constexpr uint32_t kWaitLimit = 1u << 22;           // polls of one bounded wait
+constexpr int kMaxStages = 6;
+// core-matrix strides of the operands: 128 bytes between neighbouring core matrices along the
+// row dimension of a chunk / K-step (8 elements), 2048 bytes between groups of 8 points or of 8
+// output columns
+constexpr uint32_t kCoreK = 128, kCoreMN = 2048;
+
+__host__ __device__ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// barrier and bookkeeping words behind the stages
+struct Sync {
+  uint64_t full[kMaxStages];
+  uint64_t empty[kMaxStages];
+  uint64_t qempty[2];
+  uint64_t pass;
+  uint64_t last;
+  uint32_t tmem;
+  volatile int abort;
+};
+
+__device__ __forceinline__ void fail_wait(Sync* sy, int* status, int code) {
+  sy->abort = 1;
+  atomicOr(status, code);
+}
+
+// BF16 high/low split: v = hi + lo to about 16 significant bits
+__device__ __forceinline__ void split_bf16(float v, uint16_t* hi, uint16_t* lo) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+  *hi = *reinterpret_cast<const uint16_t*>(&h);
+  *lo = *reinterpret_cast<const uint16_t*>(&l);
+}
+
+// byte offset of element (column n, row r) of a 32-column operand block in the K-major layout
+__host__ __device__ inline uint32_t opnd_off(int n, int r) {
+  return static_cast<uint32_t>((n >> 3) * 2048 + (r >> 3) * 128 + (n & 7) * 16 + (r & 7) * 2);
+}
+
+// ---- producer: one stage of E ----------------------------------------------------------------
+// The thread's slots for a stage: up to 8 subspaces overlapping its half of the group.
+struct SlotLoads {
+  uint32_t w[8];   // packed product | cell << 16
+  uint32_t cn[8];  // chunk offset | chunk count << 8
+  int count;
+};
+
+__device__ __forceinline__ void load_slots(SlotLoads& L, const uint32_t* __restrict__ pc,
+                                           const int4* __restrict__ ghalf,
+                                           const uint16_t* __restrict__ slot_cn, int64_t mpad,
+                                           int group, int h, int64_t point) {
+  const int4 gh = __ldg(ghalf + 2 * group + h);
+  L.count = gh.z;
+  const uint32_t idx[2] = {static_cast<uint32_t>(gh.x), static_cast<uint32_t>(gh.y)};
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    if (i < L.count) {
+      const int sl = gh.w + static_cast<int>((idx[i >> 2] >> (8 * (i & 3))) & 0xFFu);
+      L.w[i] = __ldcs(pc + static_cast<int64_t>(sl) * mpad + point);
+      L.cn[i] = __ldg(slot_cn + sl);
+    } else {
+      L.w[i] = 0u;
+      L.cn[i] = 0u;
+    }
+  }
+}
+
+// rows of point p, chunks [8h, 8h + 8) of the group, into the stage
+__device__ __forceinline__ void write_stage(unsigned char* stage, int p, int h,
+                                            const SlotLoads& L) {
+  unsigned char* base = stage + (p >> 3) * 2048 + (p & 7) * 16;
+  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    if (i < L.count) {
+      const uint32_t w = L.w[i];
+      const int co = static_cast<int>(L.cn[i] & 0xFFu), nch = static_cast<int>(L.cn[i] >> 8);
+      const int c = static_cast<int>(w >> 16);
+      const int q = co + (c >> 3), e = c & 7;
+      const uint32_t val = (w & 0xFFFFu) << ((e & 1) * 16);
+      const int wd = e >> 1;
+      const uint4 one = make_uint4(wd == 0 ? val : 0u, wd == 1 ? val : 0u, wd == 2 ? val : 0u,
+                                   wd == 3 ? val : 0u);
+      const int lo = max(co, 8 * h), hi = min(co + nch, 8 * h + 8);
+      for (int qq = lo; qq < hi; ++qq)
+        *reinterpret_cast<uint4*>(base + qq * 128) = qq == q ? one : zero;
+    }
+  }
+}
+
+// ---- mult: Q[tile] = sum over groups of E[tile][group] C[group] -------------------------------
+// A CTA owns `tiles` consecutive tiles, whose accumulators (128 x 32 FP32 each) stay in tensor
+// memory, and walks the groups in passes of `gpp` groups whose coefficient rows it copies into
+// shared memory. Output: the BF16 Q tiles (operand layout of block_multt) and optionally Q in FP64.
+__global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
+    const uint32_t* __restrict__ pc, const int4* __restrict__ ghalf,
+    const uint16_t* __restrict__ slot_cn, const uint16_t* __restrict__ coef, int n_groups,
+    int64_t mpad, int64_t m, int n_tiles, int tiles, int gpp, int stages, uint32_t tmem_cols,
+    uint16_t* __restrict__ qtiles, double* __restrict__ out64, int* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* st = smem;                                       // stages
+  unsigned char* cf = smem + static_cast<size_t>(stages) * kStageBytes;  // coefficient rows
+  Sync* sy = reinterpret_cast<Sync*>(cf + static_cast<size_t>(gpp) * kCoefBytes);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int t0 = blockIdx.x * tiles;
+  const int nt = min(tiles, n_tiles - t0);
+  const int passes = static_cast<int>(cdiv(n_groups, gpp));
+
+  // zero the stages (rows a group leaves unused must hold finite values), barriers, tensor memory
+  for (uint32_t k = tid; k < static_cast<uint32_t>(stages) * kStageBytes / 16u; k += blockDim.x)
+    reinterpret_cast<uint4*>(st)[k] = make_uint4(0u, 0u, 0u, 0u);
+  if (tid == 0) {
+    for (int k = 0; k < stages; ++k) {
+      tc::mbar_init(tc::smem_u32(&sy->full[k]), kProdThreads);
+      tc::mbar_init(tc::smem_u32(&sy->empty[k]), 1);
+    }
+    tc::mbar_init(tc::smem_u32(&sy->pass), 1);
+    tc::mbar_init(tc::smem_u32(&sy->last), 1);
+    sy->abort = 0;
+    tc::mbar_init_fence();
+  }
+  if (warp == kProdWarps) tc::tmem_alloc(tc::smem_u32(&sy->tmem), tmem_cols);
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = sy->tmem;
+  const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, false, false);
+
+  int64_t i0 = 0;  // stages issued before this pass
+  for (int pass = 0; pass < passes; ++pass) {
+    const int g0 = pass * gpp, g1 = min(n_groups, g0 + gpp);
+    if (pass > 0 && !sy->abort) {
+      // the coefficient rows of the last pass are overwritten once its MMAs have completed
+      if (!tc::mbar_wait(tc::smem_u32(&sy->pass), (pass - 1) & 1, kWaitLimit))
+        fail_wait(sy, status, 1);
+    }
+    __syncthreads();
+    if (!sy->abort) {
+      const uint4* src = reinterpret_cast<const uint4*>(coef + static_cast<int64_t>(g0) * 4096);
+      uint4* dst = reinterpret_cast<uint4*>(cf);
+      const int words = (g1 - g0) * static_cast<int>(kCoefBytes / 16u);
+      for (int k = tid; k < words; k += blockDim.x) dst[k] = __ldg(src + k);
+      tc::fence_proxy_async();
+    }
+    __syncthreads();
+    const int per_pass = nt * (g1 - g0);
+    if (tid < kProdThreads) {
+      const int p = tid & 127, h = tid >> 7;
+      SlotLoads cur, nxt;
+      if (per_pass > 0 && !sy->abort)
+        load_slots(cur, pc, ghalf, slot_cn, mpad, g0, h, static_cast<int64_t>(t0) * 128 + p);
+      for (int k = 0; k < per_pass && !sy->abort; ++k) {
+        const int u = k / (g1 - g0), g = g0 + k % (g1 - g0);
+        if (k + 1 < per_pass) {
+          const int un = (k + 1) / (g1 - g0), gn = g0 + (k + 1) % (g1 - g0);
+          load_slots(nxt, pc, ghalf, slot_cn, mpad, gn, h,
+                     static_cast<int64_t>(t0 + un) * 128 + p);
+        }
+        const int64_t i = i0 + k;
+        const int sidx = static_cast<int>(i % stages);
+        const int64_t use = i / stages;
+        if (use > 0 &&
+            !tc::mbar_wait(tc::smem_u32(&sy->empty[sidx]), static_cast<uint32_t>((use - 1) & 1),
+                           kWaitLimit)) {
+          fail_wait(sy, status, 2);
+          break;
+        }
+        (void)u;
+        (void)g;
+        write_stage(st + static_cast<size_t>(sidx) * kStageBytes, p, h, cur);
+        tc::fence_proxy_async();
+        tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
+        cur = nxt;
+      }
+    } else if (tid == kProdThreads) {
+      // the MMA thread
+      for (int k = 0; k < per_pass && !sy->abort; ++k) {
+        const int u = k / (g1 - g0), gl = k % (g1 - g0);
+        const int64_t i = i0 + k;
+        const int sidx = static_cast<int>(i % stages);
+        const int64_t use = i / stages;
+        if (!tc::mbar_wait(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>(use & 1),
+                           kWaitLimit)) {
+          fail_wait(sy, status, 4);
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t a0 = tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes);
+        const uint32_t b0 = tc::smem_u32(cf + static_cast<size_t>(gl) * kCoefBytes);
+        const uint32_t d = tmem + static_cast<uint32_t>(u * kBlockCols);
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          tc::mma_bf16(d, tc::sdesc(a0 + j * 2 * kCoreK, kCoreK, kCoreMN),
+                       tc::sdesc(b0 + j * 2 * kCoreK, kCoreK, kCoreMN), idesc,
+                       pass > 0 || gl > 0 || j > 0);
+        tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
+      }
+      tc::mma_commit(tc::smem_u32(&sy->pass));
+    }
+    i0 += per_pass;
+  }
+  // every MMA of the CTA has completed once the last commit has
+  if (tid == kProdThreads) {
+    tc::mma_commit(tc::smem_u32(&sy->last));
+    if (!tc::mbar_wait(tc::smem_u32(&sy->last), 0, kWaitLimit)) fail_wait(sy, status, 8);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (!sy->abort && warp < kProdWarps) {
+    // warps 0-3 read the even tiles, warps 4-7 the odd ones; lane = point of the tile
+    const int quarter = warp & 3;
+    const int p = quarter * 32 + lane;
+    for (int u = warp >> 2; u < nt; u += 2) {
+      uint32_t r0[16], r1[16];
+      const uint32_t ta = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
+                          static_cast<uint32_t>(u * kBlockCols);
+      tc::tmem_ld16(ta, r0);
+      tc::tmem_ld16(ta + 16, r1);
+      tc::tmem_wait_ld();
+      const int64_t t = t0 + u;
+      const int64_t j = t * 128 + p;
+      uint16_t* qt = qtiles ? qtiles + t * 4096 : nullptr;
+#pragma unroll
+      for (int c = 0; c < kBlockRhs; ++c) {
+        const float q = __uint_as_float(r0[c]) + __uint_as_float(r1[c]);
+        if (out64) out64[static_cast<int64_t>(c) * mpad + j] = j < m ? static_cast<double>(q) : 0.0;
+        if (qt) {
+          uint16_t hi, lo;
+          split_bf16(j < m ? q : 0.0f, &hi, &lo);
+          qt[opnd_off(c, p) / 2] = hi;
+          qt[opnd_off(c + kBlockRhs, p) / 2] = lo;
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == kProdWarps) tc::tmem_dealloc(tmem, tmem_cols);
+}
+
+// ---- multT: R[group] = sum over tiles of E[tile][group]^T Q[tile] -----------------------------
+// CTA b takes the groups of pass b / streams (up to `gpc` accumulators of 128 rows x 32 FP32 in
+// tensor memory) and the tiles of stream b % streams; the Q tile (BF16, operand layout) is copied
+// into one of two shared-memory buffers per tile. The accumulators go out as FP64 partial rows of
+// the stream, summed over the streams in order by block_finish_kernel.
+// Operand A (E^T, MN-major) core-matrix offsets: along the rows (M) and along the points (K).
+constexpr uint32_t kMnA_LBO = 2048, kMnA_SBO = 128;
+
+__global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
+    const uint32_t* __restrict__ pc, const int4* __restrict__ ghalf,
+    const uint16_t* __restrict__ slot_cn, const uint16_t* __restrict__ qtiles, int n_groups,
+    int64_t mpad, int n_tiles, int gpc, int streams, int stages, uint32_t tmem_cols, int64_t rows,
+    double* __restrict__ part, int* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* st = smem;
+  unsigned char* qb = smem + static_cast<size_t>(stages) * kStageBytes;  // two Q tiles
+  Sync* sy = reinterpret_cast<Sync*>(qb + 2 * kQBytes);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int pass = blockIdx.x / streams, stream = blockIdx.x % streams;
+  const int g0 = pass * gpc, ng = min(gpc, n_groups - g0);
+  const int ta = static_cast<int>(static_cast<int64_t>(stream) * n_tiles / streams);
+  const int tb = static_cast<int>(static_cast<int64_t>(stream + 1) * n_tiles / streams);
+  const int64_t total = static_cast<int64_t>(tb - ta) * ng;
+
+  for (uint32_t k = tid; k < static_cast<uint32_t>(stages) * kStageBytes / 16u; k += blockDim.x)
+    reinterpret_cast<uint4*>(st)[k] = make_uint4(0u, 0u, 0u, 0u);
+  if (tid == 0) {
+    for (int k = 0; k < stages; ++k) {
+      tc::mbar_init(tc::smem_u32(&sy->full[k]), kProdThreads);
+      tc::mbar_init(tc::smem_u32(&sy->empty[k]), 1);
+    }
+    tc::mbar_init(tc::smem_u32(&sy->qempty[0]), 1);
+    tc::mbar_init(tc::smem_u32(&sy->qempty[1]), 1);
+    tc::mbar_init(tc::smem_u32(&sy->last), 1);
+    sy->abort = 0;
+    tc::mbar_init_fence();
+  }
+  if (warp == kProdWarps) tc::tmem_alloc(tc::smem_u32(&sy->tmem), tmem_cols);
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = sy->tmem;
+  const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, true, false);
+
+  if (tid < kProdThreads && ng > 0) {
+    const int p = tid & 127, h = tid >> 7;
+    SlotLoads cur, nxt;
+    if (total > 0) load_slots(cur, pc, ghalf, slot_cn, mpad, g0, h, static_cast<int64_t>(ta) * 128 + p);
+    for (int64_t k = 0; k < total && !sy->abort; ++k) {
+      const int tl = static_cast<int>(k / ng), gl = static_cast<int>(k % ng);
+      if (k + 1 < total) {
+        const int tn = static_cast<int>((k + 1) / ng), gn = static_cast<int>((k + 1) % ng);
+        load_slots(nxt, pc, ghalf, slot_cn, mpad, g0 + gn, h,
+                   static_cast<int64_t>(ta + tn) * 128 + p);
+      }
+      if (gl == 0) {
+        // the Q tile of this tile into buffer tl % 2, once the MMAs of tile tl - 2 are done
+        const int b = tl & 1, use = tl >> 1;
+        if (use > 0 && !tc::mbar_wait(tc::smem_u32(&sy->qempty[b]),
+                                      static_cast<uint32_t>((use - 1) & 1), kWaitLimit)) {
+          fail_wait(sy, status, 16);
+          break;
+        }
+        const uint4* src = reinterpret_cast<const uint4*>(qtiles + static_cast<int64_t>(ta + tl) * 4096);
+        uint4* dst = reinterpret_cast<uint4*>(qb + b * kQBytes);
+        for (int w = tid; w < static_cast<int>(kQBytes / 16u); w += kProdThreads) dst[w] = __ldg(src + w);
+      }
+      const int sidx = static_cast<int>(k % stages);
+      const int64_t use = k / stages;
+      if (use > 0 &&
+          !tc::mbar_wait(tc::smem_u32(&sy->empty[sidx]), static_cast<uint32_t>((use - 1) & 1),
+                         kWaitLimit)) {
+        fail_wait(sy, status, 2);
+        break;
+      }
+      write_stage(st + static_cast<size_t>(sidx) * kStageBytes, p, h, cur);
+      tc::fence_proxy_async();
+      tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
+      cur = nxt;
+    }
+  } else if (tid == kProdThreads && ng > 0) {
+    for (int64_t k = 0; k < total && !sy->abort; ++k) {
+      const int tl = static_cast<int>(k / ng), gl = static_cast<int>(k % ng);
+      const int sidx = static_cast<int>(k % stages);
+      const int64_t use = k / stages;
+      if (!tc::mbar_wait(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>(use & 1),
+                         kWaitLimit)) {
+        fail_wait(sy, status, 4);
+        break;
+      }
+      tc::fence_after_sync();
+      const uint32_t a0 = tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes);
+      const uint32_t b0 = tc::smem_u32(qb + (tl & 1) * kQBytes);
+      const uint32_t d = tmem + static_cast<uint32_t>(gl * kBlockCols);
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        tc::mma_bf16(d, tc::sdesc(a0 + j * 2 * kCoreMN, kMnA_LBO, kMnA_SBO),
+                     tc::sdesc(b0 + j * 2 * kCoreK, kCoreK, kCoreMN), idesc, tl > 0 || j > 0);
+      tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
+      if (gl == ng - 1) tc::mma_commit(tc::smem_u32(&sy->qempty[tl & 1]));
+    }
+  }
+  if (tid == kProdThreads) {
+    tc::mma_commit(tc::smem_u32(&sy->last));
+    if (!tc::mbar_wait(tc::smem_u32(&sy->last), 0, kWaitLimit)) fail_wait(sy, status, 8);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (!sy->abort && warp < kProdWarps) {
+    const int quarter = warp & 3;
+    const int r = quarter * 32 + lane;
+    for (int gl = warp >> 2; gl < ng; gl += 2) {
+      uint32_t r0[16], r1[16];
+      const uint32_t ta2 = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
+                           static_cast<uint32_t>(gl * kBlockCols);
+      tc::tmem_ld16(ta2, r0);
+      tc::tmem_ld16(ta2 + 16, r1);
+      tc::tmem_wait_ld();
+      const int64_t row = static_cast<int64_t>(g0 + gl) * 128 + r;
+#pragma unroll
+      for (int c = 0; c < kBlockRhs; ++c) {
+        const double v = total > 0 ? static_cast<double>(__uint_as_float(r0[c])) +
+                                         static_cast<double>(__uint_as_float(r1[c]))
+                                   : 0.0;
+        part[(static_cast<int64_t>(stream) * kBlockRhs + c) * rows + row] = v;
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == kProdWarps) tc::tmem_dealloc(tmem, tmem_cols);
+}
+
+// out[c][gp] = sum over streams (in order) of the partial rows + scale * add[c][gp]
+__global__ void block_finish_kernel(const double* __restrict__ part, int streams, int64_t rows,
+                                    const int* __restrict__ gp_row, int64_t n, int64_t npad,
+                                    double* __restrict__ out, const double* __restrict__ add,
+                                    double scale) {
+  const int64_t total = npad * kBlockRhs;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = static_cast<int>(k / npad);
+    const int64_t gp = k - static_cast<int64_t>(c) * npad;
+    double v = 0.0;
+    if (gp < n) {
+      const int64_t r = gp_row[gp];
+      for (int sidx = 0; sidx < streams; ++sidx)
+        v += part[(static_cast<int64_t>(sidx) * kBlockRhs + c) * rows + r];
+      if (add) v += scale * add[k];
+    }
+    out[k] = v;
+  }
+}
+
+// coefficient rows: p column-major FP64 [16][npad] in grid order -> BF16 (hi, lo) operand blocks
+__global__ void block_coef_kernel(const double* __restrict__ p, int64_t npad,
+                                  const int* __restrict__ row_gp, int64_t rows,
+                                  uint16_t* __restrict__ coef) {
+  const int64_t total = rows * kBlockRhs;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = static_cast<int>(k / rows);
+    const int64_t r = k - static_cast<int64_t>(c) * rows;
+    const int gp = row_gp[r];
+    const float v = gp >= 0 ? static_cast<float>(p[static_cast<int64_t>(c) * npad + gp]) : 0.0f;
+    uint16_t hi, lo;
+    split_bf16(v, &hi, &lo);
+    const int64_t g = r >> 7;
+    const int rr = static_cast<int>(r & 127);
+    coef[g * 4096 + opnd_off(c, rr) / 2] = hi;
+    coef[g * 4096 + opnd_off(c + kBlockRhs, rr) / 2] = lo;
+  }
+}
+
+// Q tiles from a data-side block v column-major FP64 [16][mpad] (zero beyond m)
+__global__ void block_qtile_kernel(const double* __restrict__ v, int64_t mpad, int64_t m,
+                                   uint16_t* __restrict__ qtiles) {
+  const int64_t total = mpad * kBlockRhs;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = static_cast<int>(k / mpad);
+    const int64_t j = k - static_cast<int64_t>(c) * mpad;
+    const float x = j < m ? static_cast<float>(v[k]) : 0.0f;
+    uint16_t hi, lo;
+    split_bf16(x, &hi, &lo);
+    const int64_t t = j >> 7;
+    const int pp = static_cast<int>(j & 127);
+    qtiles[t * 4096 + opnd_off(c, pp) / 2] = hi;
+    qtiles[t * 4096 + opnd_off(c + kBlockRhs, pp) / 2] = lo;
+  }
+}
+
+// packed BF16 products of every slot from the materialised float-float products and cells
+template <typename CW>
+__global__ void block_pack_kernel(const float4* __restrict__ pmat, const CW* __restrict__ cmat,
+                                  int64_t s_pad, const int* __restrict__ slot_sub, int n_slots,
+                                  int64_t m, int64_t mpad, uint32_t* __restrict__ pc) {
+  constexpr int kBits = sizeof(CW) * 2;
+  const int64_t total = static_cast<int64_t>(n_slots) * mpad;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int sl = static_cast<int>(k / mpad);
+    const int64_t j = k - static_cast<int64_t>(sl) * mpad;
+    uint32_t w = 0u;
+    if (j < m) {
+      const int64_t at = (j >> 2) * s_pad + slot_sub[sl];
+      const float4 q = pmat[at];
+      const int lane4 = static_cast<int>(j & 3);
+      const float v = lane4 == 0 ? q.x : lane4 == 1 ? q.y : lane4 == 2 ? q.z : q.w;
+      const uint32_t cell = (static_cast<uint32_t>(cmat[at]) >> (kBits * lane4)) & ((1u << kBits) - 1u);
+      const __nv_bfloat16 b = __float2bfloat16_rn(v);
+      w = static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(&b)) | (cell << 16);
+    }
+    pc[k] = w;
+  }
+}
+
+}  // namespace
+}  // namespace sgmev
+
+namespace sgmev {
+namespace {
+
+// ---- CG on 16 columns -------------------------------------------------------------------------
+// Vectors are column-major [16][np]; every dot product reduces in a fixed order (a shared-memory
+// tree per block, then the kBlockDotBlocks block sums in block order), so iterations are
+// reproducible bit for bit. Scalars (BlockCgScalars offsets) stay on the device.
+constexpr int kDotT = 256;
+
+__device__ __forceinline__ double block_tree_sum(double v, double* sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int w = kDotT / 2; w > 0; w >>= 1) {
+    if (static_cast<int>(threadIdx.x) < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double sum_parts(const double* __restrict__ part, int k) {
+  double s = 0.0;
+  for (int b = 0; b < kBlockDotBlocks; ++b) s += part[k * kBlockDotBlocks + b];
+  return s;
+}
+
+__global__ void __launch_bounds__(kDotT) bcg_dot_kernel(const double* __restrict__ a,
+                                                        const double* __restrict__ b, int64_t np,
+                                                        double* __restrict__ part) {
+  __shared__ double sh[kDotT];
+  const int k = blockIdx.y;
+  const double* ak = a + static_cast<int64_t>(k) * np;
+  const double* bk = b + static_cast<int64_t>(k) * np;
+  double v = 0.0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * kDotT + threadIdx.x; i < np;
+       i += static_cast<int64_t>(gridDim.x) * kDotT)
+    v += ak[i] * bk[i];
+  v = block_tree_sum(v, sh);
+  if (threadIdx.x == 0) part[k * kBlockDotBlocks + blockIdx.x] = v;
+}
+
+// d = r, e = 0, partial r.r
+__global__ void __launch_bounds__(kDotT) bcg_init_kernel(const double* __restrict__ r,
+                                                         double* __restrict__ d,
+                                                         double* __restrict__ e, int64_t np,
+                                                         double* __restrict__ part) {
+  __shared__ double sh[kDotT];
+  const int k = blockIdx.y;
+  const int64_t o = static_cast<int64_t>(k) * np;
+  double v = 0.0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * kDotT + threadIdx.x; i < np;
+       i += static_cast<int64_t>(gridDim.x) * kDotT) {
+    const double ri = r[o + i];
+    d[o + i] = ri;
+    e[o + i] = 0.0;
+    v += ri * ri;
+  }
+  v = block_tree_sum(v, sh);
+  if (threadIdx.x == 0) part[k * kBlockDotBlocks + blockIdx.x] = v;
+}
+
+// delta (slot 0) = delta_0 = the summed partials
+__global__ void bcg_set_delta_kernel(const double* __restrict__ part, double* __restrict__ sc) {
+  const int k = threadIdx.x;
+  if (k < kBlockRhs) {
+    const double v = sum_parts(part, k);
+    sc[kScDelta + k] = v;
+    sc[kScDelta0 + k] = v;
+  }
+}
+
+// alpha = delta / d.q on active columns; e += alpha d, r -= alpha q; partial r.r
+__global__ void __launch_bounds__(kDotT) bcg_update_kernel(
+    double* __restrict__ e, double* __restrict__ r, const double* __restrict__ d,
+    const double* __restrict__ q, int64_t np, const double* __restrict__ part_dq,
+    const double* __restrict__ sc, int cur, double* __restrict__ part_rr) {
+  __shared__ double sh[kDotT];
+  const int k = blockIdx.y;
+  const double delta = sc[kScDelta + cur * kBlockRhs + k];
+  const double dq = sum_parts(part_dq, k);
+  const bool active = delta > sc[kScTol2 + k] * sc[kScDelta0 + k] && dq != 0.0;
+  const double alpha = active ? delta / dq : 0.0;
+  const int64_t o = static_cast<int64_t>(k) * np;
+  double v = 0.0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * kDotT + threadIdx.x; i < np;
+       i += static_cast<int64_t>(gridDim.x) * kDotT) {
+    double ri = r[o + i];
+    if (active) {
+      e[o + i] = fma(alpha, d[o + i], e[o + i]);
+      ri = fma(-alpha, q[o + i], ri);
+      r[o + i] = ri;
+    }
+    v += ri * ri;
+  }
+  v = block_tree_sum(v, sh);
+  if (threadIdx.x == 0) part_rr[k * kBlockDotBlocks + blockIdx.x] = v;
+}
+
+// beta = delta_new / delta; d = r + beta d on active columns; delta_new into the other slot
+__global__ void __launch_bounds__(kDotT) bcg_direction_kernel(
+    const double* __restrict__ r, double* __restrict__ d, int64_t np,
+    const double* __restrict__ part_dq, const double* __restrict__ part_rr,
+    double* __restrict__ sc, int cur) {
+  const int k = blockIdx.y;
+  const double delta = sc[kScDelta + cur * kBlockRhs + k];
+  const double dq = sum_parts(part_dq, k);
+  const bool active = delta > sc[kScTol2 + k] * sc[kScDelta0 + k] && dq != 0.0;
+  const double dnew = sum_parts(part_rr, k);
+  const double beta = active ? dnew / delta : 0.0;
+  const int64_t o = static_cast<int64_t>(k) * np;
+  if (active) {
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * kDotT + threadIdx.x; i < np;
+         i += static_cast<int64_t>(gridDim.x) * kDotT)
+      d[o + i] = fma(beta, d[o + i], r[o + i]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // a column whose step was not taken keeps its delta (and stays inactive); d.q = 0 ends it
+    sc[kScDelta + (cur ^ 1) * kBlockRhs + k] = active ? dnew : delta;
+    sc[kScStalled + k] = (!active && dq == 0.0) ? 1.0 : 0.0;
+  }
+}
+
+}  // namespace
+
+cudaError_t block_dot(cudaStream_t s, const double* a, const double* b, int64_t np, double* part) {
+  bcg_dot_kernel<<<dim3(kBlockDotBlocks, kBlockRhs), kDotT, 0, s>>>(a, b, np, part);
+  return cudaGetLastError();
+}
+
+cudaError_t block_cg_init(cudaStream_t s, const double* r, double* d, double* e, int64_t np,
+                          double* part, double* sc) {
+  bcg_init_kernel<<<dim3(kBlockDotBlocks, kBlockRhs), kDotT, 0, s>>>(r, d, e, np, part);
+  bcg_set_delta_kernel<<<1, 32, 0, s>>>(part, sc);
+  return cudaGetLastError();
+}
+
+cudaError_t block_cg_step(cudaStream_t s, double* e, double* r, double* d, const double* q,
+                          int64_t np, double* part_dq, double* part_rr, double* sc, int cur) {
+  bcg_dot_kernel<<<dim3(kBlockDotBlocks, kBlockRhs), kDotT, 0, s>>>(d, q, np, part_dq);
+  bcg_update_kernel<<<dim3(kBlockDotBlocks, kBlockRhs), kDotT, 0, s>>>(e, r, d, q, np, part_dq,
+                                                                       sc, cur, part_rr);
+  bcg_direction_kernel<<<dim3(kBlockDotBlocks, kBlockRhs), kDotT, 0, s>>>(r, d, np, part_dq,
+                                                                          part_rr, sc, cur);
+  return cudaGetLastError();
+}
+
+}  // namespace sgmev
+
+namespace sgmev {
+
+namespace {
+// groups of coefficient rows a mult CTA holds: the shape's count, fewer when the stages leave less
+// shared memory (at least one)
+int mult_groups_fit(const BlockShape& sh, int smem_cap) {
+  const int64_t room = static_cast<int64_t>(smem_cap) - static_cast<int64_t>(sh.stages) * kStageBytes -
+                       static_cast<int64_t>(sizeof(Sync));
+  return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(sh.mult_groups, room / kCoefBytes)));
+}
+size_t mult_smem(const BlockShape& sh, int groups) {
+  return static_cast<size_t>(sh.stages) * kStageBytes + static_cast<size_t>(groups) * kCoefBytes +
+         sizeof(Sync);
+}
+int device_smem_cap() {
+  int dev = 0, cap = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return cap;
+}
+size_t multt_smem(const BlockShape& sh) {
+  return static_cast<size_t>(sh.stages) * kStageBytes + 2 * kQBytes + sizeof(Sync);
+}
+uint32_t tmem_cols_for(int accumulators) {
+  uint32_t c = 32;
+  while (c < static_cast<uint32_t>(accumulators * kBlockCols)) c <<= 1;
+  return c;
+}
+unsigned grid_for(int64_t n, int num_sms) {
+  return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(cdiv(n, 256), 8 * num_sms)));
+}
+}  // namespace
+
+void block_free(BlockPlan* b) {
+  void* ptrs[] = {b->row_gp, b->gp_row, b->ghalf, b->slot_cn, b->pc,
+                  b->coef,   b->qtiles, b->part,  b->status};
+  for (void* q : ptrs) dev_free(q, b->stream);
+  *b = BlockPlan{};
+}
+
+bool block_shape_ok(const BlockShape& sh, int smem_cap) {
+  return sh.stages >= 2 && sh.stages <= kMaxStages && sh.mult_tiles >= 1 && sh.mult_tiles <= 16 &&
+         sh.mult_groups >= 1 && sh.multt_groups >= 1 && sh.multt_groups <= 16 &&
+         mult_smem(sh, mult_groups_fit(sh, smem_cap)) <= static_cast<size_t>(smem_cap) &&
+         multt_smem(sh) <= static_cast<size_t>(smem_cap);
+}
+
+static int multt_streams(const BlockPlan& b, int num_sms) {
+  const int passes = static_cast<int>(cdiv(b.n_groups, b.shape.multt_groups));
+  return static_cast<int>(std::max<int64_t>(
+      1, std::min<int64_t>(num_sms / std::max(1, passes), b.mpad / kBlockTile)));
+}
+
+bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cudaStream_t s,
+                 int num_sms, std::string* err) {
+  block_free(b);
+  b->stream = s;
+  if (!sub.pmat || !sub.cmat || sub.h_sub.empty()) {
+    *err = "block products need the materialised subspace products";
+    return false;
+  }
+  if (sub.cmax > kBlockMaxCells) {
+    *err = "block products take subspaces of at most 128 cells";
+    return false;
+  }
+  if (mpad % kBlockTile != 0) {
+    *err = "block products need the points padded to a multiple of 128";
+    return false;
+  }
+  const int n_sub = sub.n_sub;
+  // subspaces by chunk count, largest first; packed into groups of 16 chunks
+  std::vector<int> order(n_sub);
+  std::iota(order.begin(), order.end(), 0);
+  auto chunks = [&](int sidx) { return std::max(1, sub.h_sub[sidx].y / 8); };
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int c) { return chunks(a) > chunks(c); });
+  std::vector<int> slot_sub, group_first;
+  std::vector<uint16_t> slot_cn;
+  int fill = 16;
+  for (int sidx : order) {
+    const int nch = chunks(sidx);
+    if (fill + nch > 16) {
+      group_first.push_back(static_cast<int>(slot_sub.size()));
+      fill = 0;
+    }
+    slot_sub.push_back(sidx);
+    slot_cn.push_back(static_cast<uint16_t>(fill | (nch << 8)));
+    fill += nch;
+  }
+  const int n_groups = static_cast<int>(group_first.size());
+  group_first.push_back(static_cast<int>(slot_sub.size()));
+  const int64_t rows = static_cast<int64_t>(n_groups) * kBlockGroupRows;
+  // rows <-> grid points
+  std::vector<int> pos_gp(static_cast<size_t>(sub.total), -1);
+  for (int64_t g = 0; g < sub.n; ++g) pos_gp[sub.h_pos[g]] = static_cast<int>(g);
+  std::vector<int> row_gp(static_cast<size_t>(rows), -1), gp_row(static_cast<size_t>(sub.n), 0);
+  std::vector<int4> ghalf(static_cast<size_t>(n_groups) * 2);
+  for (int g = 0; g < n_groups; ++g) {
+    int cnt[2] = {0, 0};
+    uint32_t idx[2][2] = {{0u, 0u}, {0u, 0u}};
+    for (int sl = group_first[g]; sl < group_first[g + 1]; ++sl) {
+      const int sidx = slot_sub[sl];
+      const int co = slot_cn[sl] & 0xFF, nch = slot_cn[sl] >> 8;
+      const int off = sub.h_sub[sidx].x, cells = sub.h_sub[sidx].y;
+      for (int c = 0; c < cells; ++c) {
+        const int64_t r = static_cast<int64_t>(g) * kBlockGroupRows + (co + c / 8) * 8 + c % 8;
+        const int gp = pos_gp[off + c];
+        row_gp[r] = gp;
+        if (gp >= 0) gp_row[gp] = static_cast<int>(r);
+      }
+      for (int h = 0; h < 2; ++h) {
+        if (co < 8 * h + 8 && co + nch > 8 * h) {
+          const uint32_t local = static_cast<uint32_t>(sl - group_first[g]);
+          idx[h][cnt[h] >> 2] |= local << (8 * (cnt[h] & 3));
+          ++cnt[h];
+        }
+      }
+    }
+    for (int h = 0; h < 2; ++h)
+      ghalf[2 * g + h] = make_int4(static_cast<int>(idx[h][0]), static_cast<int>(idx[h][1]),
+                                   cnt[h], group_first[g]);
+  }
+  b->n_groups = n_groups;
+  b->n_slots = static_cast<int>(slot_sub.size());
+  b->rows = rows;
+  b->n = sub.n;
+  b->m = m;
+  b->mpad = mpad;
+  b->part_streams = multt_streams(*b, num_sms);
+  int* d_slot_sub = nullptr;
+  auto alloc = [&](auto** q, size_t bytes) { return dev_malloc(q, bytes, s) == cudaSuccess; };
+  auto put = [&](void* dst, const void* src, size_t bytes) {
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  };
+  bool ok = alloc(&b->row_gp, sizeof(int) * rows) && alloc(&b->gp_row, sizeof(int) * sub.n) &&
+            alloc(&b->ghalf, sizeof(int4) * ghalf.size()) &&
+            alloc(&b->slot_cn, sizeof(uint16_t) * slot_cn.size()) &&
+            alloc(&d_slot_sub, sizeof(int) * slot_sub.size()) &&
+            alloc(&b->pc, sizeof(uint32_t) * static_cast<size_t>(b->n_slots) * mpad) &&
+            alloc(&b->coef, kCoefBytes * static_cast<size_t>(n_groups)) &&
+            alloc(&b->qtiles, kQBytes * static_cast<size_t>(mpad / kBlockTile)) &&
+            alloc(&b->part, sizeof(double) * b->part_streams * kBlockRhs * rows) &&
+            alloc(&b->status, sizeof(int));
+  ok = ok && put(b->row_gp, row_gp.data(), sizeof(int) * rows) &&
+       put(b->gp_row, gp_row.data(), sizeof(int) * sub.n) &&
+       put(b->ghalf, ghalf.data(), sizeof(int4) * ghalf.size()) &&
+       put(b->slot_cn, slot_cn.data(), sizeof(uint16_t) * slot_cn.size()) &&
+       put(d_slot_sub, slot_sub.data(), sizeof(int) * slot_sub.size()) &&
+       cudaMemsetAsync(b->status, 0, sizeof(int), s) == cudaSuccess;
+  if (ok) {
+    const unsigned blocks = grid_for(static_cast<int64_t>(b->n_slots) * mpad, num_sms);
+    if (sub.cell_bits == 4)
+      block_pack_kernel<uint16_t><<<blocks, 256, 0, s>>>(
+          sub.pmat, static_cast<const uint16_t*>(sub.cmat), sub.s_pad, d_slot_sub, b->n_slots, m,
+          mpad, b->pc);
+    else
+      block_pack_kernel<uint32_t><<<blocks, 256, 0, s>>>(
+          sub.pmat, static_cast<const uint32_t*>(sub.cmat), sub.s_pad, d_slot_sub, b->n_slots, m,
+          mpad, b->pc);
+    ok = cudaGetLastError() == cudaSuccess;
+  }
+  dev_free(d_slot_sub, s);
+  if (!ok) {
+    (void)cudaGetLastError();
+    block_free(b);
+    b->stream = s;
+    *err = "block products: allocation or launch failed";
+    return false;
+  }
+  return true;
+}
+
+cudaError_t block_mult(BlockPlan& b, cudaStream_t s, const double* p, int64_t npad,
+                       double* out64, int num_sms) {
+  const BlockShape& sh = b.shape;
+  block_coef_kernel<<<grid_for(b.rows * kBlockRhs, num_sms), 256, 0, s>>>(p, npad, b.row_gp,
+                                                                         b.rows, b.coef);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const uint32_t cols = tmem_cols_for(sh.mult_tiles);
+  const int gpp = mult_groups_fit(sh, device_smem_cap());
+  const size_t smem = cols > 256 ? std::max<size_t>(mult_smem(sh, gpp), 120 * 1024) : mult_smem(sh, gpp);
+  e = set_smem_cap(block_mult_kernel, smem);
+  if (e != cudaSuccess) return e;
+  const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
+  const unsigned ctas = static_cast<unsigned>(cdiv(n_tiles, sh.mult_tiles));
+  block_mult_kernel<<<ctas, kBlockThreads, smem, s>>>(
+      b.pc, b.ghalf, b.slot_cn, b.coef, b.n_groups, b.mpad, b.m, n_tiles, sh.mult_tiles, gpp,
+      sh.stages, cols, b.qtiles, out64, b.status);
+  return cudaGetLastError();
+}
+
+cudaError_t block_multt(BlockPlan& b, cudaStream_t s, const double* v, int64_t npad,
+                        double* out64, const double* add, double scale_add, int num_sms) {
+  const BlockShape& sh = b.shape;
+  cudaError_t e;
+  if (v) {
+    block_qtile_kernel<<<grid_for(b.mpad * kBlockRhs, num_sms), 256, 0, s>>>(v, b.mpad, b.m,
+                                                                             b.qtiles);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  // with more than half of the tensor memory per CTA, a second CTA on the SM would only wait for
+  // the first one's columns: ask for enough shared memory that it is never placed there
+  const uint32_t cols = tmem_cols_for(sh.multt_groups);
+  const size_t smem = cols > 256 ? std::max<size_t>(multt_smem(sh), 120 * 1024) : multt_smem(sh);
+  e = set_smem_cap(block_multt_kernel, smem);
+  if (e != cudaSuccess) return e;
+  const int passes = static_cast<int>(cdiv(b.n_groups, sh.multt_groups));
+  const int streams = std::min(b.part_streams, multt_streams(b, num_sms));
+  const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
+  block_multt_kernel<<<static_cast<unsigned>(passes * streams), kBlockThreads, smem, s>>>(
+      b.pc, b.ghalf, b.slot_cn, b.qtiles, b.n_groups, b.mpad, n_tiles, sh.multt_groups, streams,
+      sh.stages, cols, b.rows, b.part, b.status);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  block_finish_kernel<<<grid_for(npad * kBlockRhs, num_sms), 256, 0, s>>>(
+      b.part, streams, b.rows, b.gp_row, b.n, npad, out64, add, scale_add);
+  return cudaGetLastError();
+}
+
+cudaError_t block_status(BlockPlan& b, cudaStream_t s, int* host_status) {
+  cudaError_t e = cudaMemcpyAsync(host_status, b.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e;
+}
+
+}  // namespace sgmev

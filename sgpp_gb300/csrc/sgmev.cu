@@ -24,6 +24,7 @@
 #include "kernels.cuh"
 #include "devmem.h"
 #include "subspace.h"
+#include "block_tc.h"
 
 namespace sgmev {
 
@@ -131,6 +132,14 @@ struct sgmev_op {
   int algo = 2;          // FP32 products: 0 dense, 1 subspace, 2 auto (params "algo")
   SubPlan sub;           // subspace tables of the current grid
   bool sub_ok = false;   // sub is built and chosen for the FP32 products
+  // BF16 tensor-core products with 16 right-hand sides (built on the first block call)
+  sgmev::BlockPlan blk;
+  bool blk_ok = false;
+  bool blk_failed = false;
+  std::string blk_err;
+  sgmev::BlockShape blk_shape;  // launch shape ("block_*" knobs or the autotuner)
+  double block_inner_tol = 1e-3;  // inner tolerance of block fits ("block_inner_tol")
+  int multt_batch = 1;  // points per read-modify-write round of the FP16 multTranspose ("multt_batch")
 
   std::vector<double> bb_left, bb_width;
 
@@ -140,8 +149,8 @@ struct sgmev_op {
   std::vector<cudaEvent_t> prof_events;  // pool, 2 per launch
   std::vector<int> prof_kind;            // kind of launch i
   size_t prof_used = 0;                  // launches recorded since the last reset
-  int64_t prof_count[17] = {0};
-  double prof_seconds[17] = {0.0};
+  int64_t prof_count[19] = {0};
+  double prof_seconds[19] = {0.0};
 };
 
 namespace sgmev {
@@ -164,9 +173,11 @@ enum {
   KIND_MULTT_MATDF = 13,
   KIND_SYSTEM_MAT32 = 14,
   KIND_MULT_MAT16 = 15,
-  KIND_MULTT_MAT16 = 16
+  KIND_MULTT_MAT16 = 16,
+  KIND_BLOCK_MULT = 17,
+  KIND_BLOCK_MULTT = 18
 };
-constexpr int kKinds = 17;
+constexpr int kKinds = 19;
 
 template <typename T>
 static const T* gscale(const sgmev_op* op);
@@ -1093,11 +1104,15 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
   // and ~10 per subspace, against 3 per dimension for every grid point)
   op->sub_ok = false;
   op->mat_failed = false;
+  block_free(&op->blk);
+  op->blk_ok = false;
+  op->blk_failed = false;
   subspace_free(&op->sub);
   if (op->algo != 0 && n > 0) {
     std::string why;
     if (subspace_build(&op->sub, op->dim, n, level_pow2, index, op->stream, &why)) {
       op->sub.mod = op->mod;
+      op->sub.multt_batch = op->multt_batch;
       const double dense_cost = 3.0 * op->dim * static_cast<double>(n);
       const double sub_cost = 8.0 * static_cast<double>(op->sub.act_work) + 10.0 * op->sub.n_sub;
       op->sub_ok = op->algo == 1 || sub_cost * 1.5 < dense_cost;
@@ -1129,6 +1144,7 @@ static void release(sgmev_op* op) {
   // the op's own stream covers all of the op's work.
   if (op->stream) cudaStreamSynchronize(op->stream);
   if (op->own_stream && op->own_stream != op->stream) cudaStreamSynchronize(op->own_stream);
+  block_free(&op->blk);
   subspace_free(&op->sub);
   void* ptrs[] = {op->xt64, op->xt32, op->xt32lo, op->li64, op->li32, op->gq, op->gs64, op->gs32, op->a64,
                   op->a32,  op->a32lo, op->v64,   op->v32,  op->v32lo, op->out64, op->part,
@@ -1175,6 +1191,38 @@ static std::string json_string(const char* json, const char* key) {
   const size_t e = s.find('"', p + 1);
   if (e == std::string::npos) return "";
   return s.substr(p + 1, e - p - 1);
+}
+
+// Launch-shape knobs (the autotuner's choices): "multt_batch" and the "block_*" shape of the
+// tensor-core block products. They change no result (multt_batch) or only how the block products
+// are cut into launches, so they may also change on a live operator (sgmev_set_params).
+static int apply_shape_params(sgmev_op* op, const char* params_json) {
+  using namespace sgmev;
+  const std::string mb = json_string(params_json, "multt_batch");
+  int batch = op->multt_batch;
+  if (!mb.empty()) {
+    if (mb != "1" && mb != "2" && mb != "4")
+      return fail(SGMEV_ERR_INVALID, "params: multt_batch must be 1, 2 or 4");
+    batch = mb[0] - '0';
+  }
+  BlockShape sh = op->blk_shape;
+  const char* knobs[] = {"block_mult_tiles", "block_mult_groups", "block_multt_groups",
+                         "block_stages"};
+  int* fields[] = {&sh.mult_tiles, &sh.mult_groups, &sh.multt_groups, &sh.stages};
+  for (int k = 0; k < 4; ++k) {
+    const std::string v = json_string(params_json, knobs[k]);
+    if (v.empty()) continue;
+    char* end = nullptr;
+    const long x = std::strtol(v.c_str(), &end, 10);
+    if (!end || *end != '\0' || x < 1 || x > 64)
+      return fail(SGMEV_ERR_INVALID, std::string("params: ") + knobs[k] + " must be an integer in [1, 64]");
+    *fields[k] = static_cast<int>(x);
+  }
+  op->multt_batch = batch;
+  op->sub.multt_batch = batch;
+  op->blk_shape = sh;
+  op->blk.shape = sh;
+  return SGMEV_OK;
 }
 
 static int check_op(const sgmev_op* op) {
@@ -1287,6 +1335,23 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
         return fail(SGMEV_ERR_INVALID, "params: inner_tol must be a number in (0, 1)");
       }
       op->inner_tol = v;
+    }
+    const std::string bt = json_string(params_json, "block_inner_tol");
+    if (!bt.empty()) {
+      char* end = nullptr;
+      const double v = std::strtod(bt.c_str(), &end);
+      if (!end || *end != '\0' || !(v > 0.0) || !(v < 1.0)) {
+        release(op);
+        delete op;
+        return fail(SGMEV_ERR_INVALID, "params: block_inner_tol must be a number in (0, 1)");
+      }
+      op->block_inner_tol = v;
+    }
+    const int rc_shape = apply_shape_params(op, params_json);
+    if (rc_shape != SGMEV_OK) {
+      release(op);
+      delete op;
+      return rc_shape;
     }
   }
   op->algo = algo == "dense" ? 0 : (algo == "subspace" ? 1 : 2);
@@ -1417,6 +1482,39 @@ SGMEV_API int sgmev_set_stream(sgmev_op* op, void* stream) {
     SGMEV_CUDA(cudaEventRecord(op->ev_switch, op->stream));
     SGMEV_CUDA(cudaStreamWaitEvent(next, op->ev_switch, 0));
     op->stream = next;
+  }
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_set_params(sgmev_op* op, const char* params_json) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if (!params_json) return SGMEV_OK;
+  static const char* allowed[] = {"multt_batch", "block_mult_tiles", "block_mult_groups",
+                                  "block_multt_groups", "block_stages"};
+  // every key must be a launch-shape knob
+  for (const char* c = params_json; (c = std::strchr(c, '"')) != nullptr;) {
+    const char* e = std::strchr(c + 1, '"');
+    if (!e) break;
+    const std::string key(c + 1, e);
+    const char* after = e + 1;
+    while (*after == ' ') ++after;
+    if (*after == ':') {
+      bool ok = false;
+      for (const char* a : allowed) ok = ok || key == a;
+      if (!ok) return fail(SGMEV_ERR_INVALID, "sgmev_set_params: \"" + key + "\" is not a launch-shape knob");
+    }
+    c = e + 1;
+  }
+  SGMEV_CUDA(cudaStreamSynchronize(op->stream));
+  int cap = 0;
+  SGMEV_CUDA(cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, op->device));
+  const BlockShape before = op->blk_shape;
+  SGMEV_TRY(apply_shape_params(op, params_json));
+  if (!block_shape_ok(op->blk_shape, cap)) {
+    op->blk_shape = before;
+    op->blk.shape = before;
+    return fail(SGMEV_ERR_INVALID, "block launch shape does not fit the device's shared memory");
   }
   return SGMEV_OK;
 }
@@ -1893,6 +1991,257 @@ SGMEV_API int sgmev_profile_read(sgmev_op* op, int kind, int64_t* launches, doub
   if (launches) *launches = op->prof_count[kind];
   if (seconds) *seconds = op->prof_seconds[kind];
   return SGMEV_OK;
+}
+
+// ---- 16 right-hand sides: BF16 tensor-core block products and block fits ------------------
+// The block products need the subspace plan and its materialised products (grids whose subspaces
+// have at most 128 cells); they are built on the first block call and kept until prepare().
+static int block_ready(sgmev_op* op) {
+  using namespace sgmev;
+  if (op->blk_ok) return SGMEV_OK;
+  if (op->blk_failed) return fail(SGMEV_ERR_UNSUPPORTED, "block products: " + op->blk_err);
+  int cap = 0;
+  SGMEV_CUDA(cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, op->device));
+  if (!block_shape_ok(op->blk_shape, cap))
+    return fail(SGMEV_ERR_INVALID, "block launch shape does not fit the device's shared memory");
+  if (!op->sub_ok || !mat_ready(op)) {
+    op->blk_failed = true;
+    op->blk_err = "they stream the materialised subspace products (params \"algo\": \"subspace\", "
+                  "\"materialize\": not \"off\"), which this operator does not have";
+    return fail(SGMEV_ERR_UNSUPPORTED, "block products: " + op->blk_err);
+  }
+  std::string err;
+  if (!block_build(&op->blk, op->sub, op->m, op->mpad, op->stream, op->num_sms, &err)) {
+    op->blk_failed = true;
+    op->blk_err = err;
+    return fail(SGMEV_ERR_UNSUPPORTED, "block products: " + err);
+  }
+  op->blk.shape = op->blk_shape;
+  op->launches += 1;
+  op->blk_ok = true;
+  return SGMEV_OK;
+}
+
+static int block_check(sgmev_op* op) {
+  using namespace sgmev;
+  int st = 0;
+  SGMEV_CUDA(block_status(op->blk, op->stream, &st));
+  if (st != 0)
+    return fail(SGMEV_ERR_CUDA, "block products: a wait of the tensor-core kernels ran out (status " +
+                                    std::to_string(st) + ")");
+  return SGMEV_OK;
+}
+
+// q = B^T (B d) + lm d for 16 columns, on the tensor cores
+static int block_system(sgmev_op* op, const double* d, double* q, double lm) {
+  using namespace sgmev;
+  const long e0 = prof_begin(op, KIND_BLOCK_MULT);
+  SGMEV_CUDA(block_mult(op->blk, op->stream, d, op->npad, nullptr, op->num_sms));
+  prof_end(op, e0);
+  const long e1 = prof_begin(op, KIND_BLOCK_MULTT);
+  SGMEV_CUDA(block_multt(op->blk, op->stream, nullptr, op->npad, q, d, lm, op->num_sms));
+  prof_end(op, e1);
+  op->launches += 4;
+  return SGMEV_OK;
+}
+
+struct DevBuf {  // stream-ordered scratch of one call
+  cudaStream_t s;
+  void* p = nullptr;
+  explicit DevBuf(cudaStream_t st) : s(st) {}
+  ~DevBuf() { sgmev::dev_free(p, s); }
+};
+
+static int block_products_common(sgmev_op* op, bool transpose, const double* in, double* out) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if ((!in || !out) && (op->n > 0 && op->m > 0)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  SGMEV_TRY(block_ready(op));
+  const int64_t np = op->npad, mp = op->mpad, K = kBlockRhs;
+  const int64_t n_in = transpose ? op->m : op->n, pad_in = transpose ? mp : np;
+  const int64_t n_out = transpose ? op->n : op->m, pad_out = transpose ? np : mp;
+  DevBuf buf(op->stream);
+  SGMEV_CUDA(dev_malloc(&buf.p, sizeof(double) * K * (pad_in + pad_out), op->stream));
+  double* d_in = static_cast<double*>(buf.p);
+  double* d_out = d_in + K * pad_in;
+  SGMEV_TRY(begin_timed(op));
+  SGMEV_CUDA(cudaMemsetAsync(d_in, 0, sizeof(double) * K * pad_in, op->stream));
+  if (n_in > 0)
+    SGMEV_CUDA(cudaMemcpy2DAsync(d_in, sizeof(double) * pad_in, in, sizeof(double) * n_in,
+                                 sizeof(double) * n_in, K, cudaMemcpyHostToDevice, op->stream));
+  if (transpose) {
+    const long ev = prof_begin(op, KIND_BLOCK_MULTT);
+    SGMEV_CUDA(block_multt(op->blk, op->stream, d_in, np, d_out, nullptr, 0.0, op->num_sms));
+    prof_end(op, ev);
+  } else {
+    const long ev = prof_begin(op, KIND_BLOCK_MULT);
+    SGMEV_CUDA(block_mult(op->blk, op->stream, d_in, np, d_out, op->num_sms));
+    prof_end(op, ev);
+  }
+  op->launches += 3;
+  if (n_out > 0)
+    SGMEV_CUDA(cudaMemcpy2DAsync(out, sizeof(double) * n_out, d_out, sizeof(double) * pad_out,
+                                 sizeof(double) * n_out, K, cudaMemcpyDeviceToHost, op->stream));
+  SGMEV_TRY(end_timed(op, true));
+  return block_check(op);
+}
+
+SGMEV_API int sgmev_mult_block(sgmev_op* op, const double* alpha, double* result) {
+  return block_products_common(op, false, alpha, result);
+}
+
+SGMEV_API int sgmev_mult_transpose_block(sgmev_op* op, const double* source, double* result) {
+  return block_products_common(op, true, source, result);
+}
+
+static int fit_block_common(sgmev_op* op, const double* y, bool y_dev, double lambda,
+                            int64_t max_iterations, double epsilon, double* alpha, bool a_dev,
+                            int64_t* iterations, double* residuals) {
+  using namespace sgmev;
+  SGMEV_TRY(check_op(op));
+  if ((op->m > 0 && !y) || (op->n > 0 && !alpha)) return fail(SGMEV_ERR_INVALID, "NULL vector");
+  if (!(epsilon > 0.0) || max_iterations < 0) return fail(SGMEV_ERR_INVALID, "bad epsilon/max_iterations");
+  SGMEV_TRY(block_ready(op));
+  const int K = kBlockRhs;
+  const int64_t np = op->npad;
+  const double lm = static_cast<double>(op->m) * lambda;
+  // b, x, outer residual rr, inner solution e, inner residual r, direction d, product q, temp t
+  DevBuf buf(op->stream);
+  const size_t vec = static_cast<size_t>(K) * np;
+  const size_t parts = static_cast<size_t>(K) * kBlockDotBlocks;
+  SGMEV_CUDA(dev_malloc(&buf.p, sizeof(double) * (8 * vec + 2 * parts + kBlockScalars), op->stream));
+  double* b = static_cast<double*>(buf.p);
+  double* x = b + vec;
+  double* rr = x + vec;
+  double* e = rr + vec;
+  double* r = e + vec;
+  double* d = r + vec;
+  double* q = d + vec;
+  double* t = q + vec;
+  double* part_a = t + vec;
+  double* part_b = part_a + parts;
+  double* sc = part_b + parts;
+  SGMEV_TRY(begin_timed(op));
+  // b_k = B^T y_k with the FP64-accurate df64 products (generateb per column)
+  for (int k = 0; k < K; ++k) {
+    if (op->m > 0)
+      SGMEV_CUDA(cudaMemcpyAsync(op->out64, y + static_cast<int64_t>(k) * op->m,
+                                 sizeof(double) * op->m,
+                                 y_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                 op->stream));
+    SGMEV_TRY(dev_convert(op, op->out64, op->m, op->mpad, op->v64, op->v32, op->v32lo));
+    SGMEV_TRY(dev_multt(op, SGMEV_DF64, op->v64, op->v32, op->v32lo, b + k * np, 0, np, nullptr,
+                        0.0));
+  }
+  SGMEV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * vec, op->stream));
+  std::vector<double> host(3 * K + parts), rho(K, 0.0), rho0(K, 0.0), tol2(K, 0.0);
+  std::vector<int64_t> col_it(K, 0);
+  std::vector<char> done(K, 0);
+  auto block_norms = [&](const double* v, std::vector<double>& out) -> int {
+    SGMEV_CUDA(block_dot(op->stream, v, v, np, part_a));
+    SGMEV_CUDA(cudaMemcpyAsync(host.data(), part_a, sizeof(double) * parts, cudaMemcpyDeviceToHost,
+                               op->stream));
+    SGMEV_CUDA(cudaStreamSynchronize(op->stream));
+    for (int k = 0; k < K; ++k) {
+      double acc = 0.0;
+      for (int bl = 0; bl < kBlockDotBlocks; ++bl) acc += host[k * kBlockDotBlocks + bl];
+      out[k] = acc;
+    }
+    op->launches += 1;
+    return SGMEV_OK;
+  };
+  int64_t total_it = 0;
+  for (int outer = 0; outer < 64; ++outer) {
+    if (outer == 0) {
+      SGMEV_CUDA(cudaMemcpyAsync(rr, b, sizeof(double) * vec, cudaMemcpyDeviceToDevice, op->stream));
+    } else {
+      for (int k = 0; k < K; ++k) {
+        if (done[k]) continue;  // x_k did not move: its residual stands
+        SGMEV_TRY(dev_system(op, SGMEV_DF64, x + k * np, t, lm));
+        sub_kernel<<<vec_blocks(np), 256, 0, op->stream>>>(np, b + k * np, t, rr + k * np);
+        op->launches += 1;
+      }
+    }
+    SGMEV_TRY(block_norms(rr, rho));
+    if (outer == 0) rho0 = rho;
+    bool all_done = true;
+    for (int k = 0; k < K; ++k) {
+      done[k] = done[k] || rho[k] <= epsilon * epsilon * rho0[k] || rho[k] == 0.0;
+      all_done = all_done && done[k];
+      const double want = std::min(0.5, std::max(op->block_inner_tol,
+                                                 epsilon * std::sqrt(rho0[k] / std::max(rho[k], 1e-300)) * 0.5));
+      tol2[k] = done[k] ? HUGE_VAL : want * want;
+    }
+    if (all_done || total_it >= max_iterations) break;
+    // inner block CG on A e = rr with the BF16 tensor-core products, e = 0 at the start
+    SGMEV_CUDA(cudaMemcpyAsync(sc + kScTol2, tol2.data(), sizeof(double) * K, cudaMemcpyHostToDevice,
+                               op->stream));
+    SGMEV_CUDA(cudaMemcpyAsync(r, rr, sizeof(double) * vec, cudaMemcpyDeviceToDevice, op->stream));
+    SGMEV_CUDA(block_cg_init(op->stream, r, d, e, np, part_a, sc));
+    op->launches += 2;
+    int cur = 0;
+    while (total_it < max_iterations) {
+      SGMEV_CUDA(cudaMemcpyAsync(host.data(), sc + kScDelta + cur * K, sizeof(double) * K,
+                                 cudaMemcpyDeviceToHost, op->stream));
+      SGMEV_CUDA(cudaMemcpyAsync(host.data() + K, sc + kScDelta0, sizeof(double) * K,
+                                 cudaMemcpyDeviceToHost, op->stream));
+      SGMEV_CUDA(cudaMemcpyAsync(host.data() + 2 * K, sc + kScStalled, sizeof(double) * K,
+                                 cudaMemcpyDeviceToHost, op->stream));
+      SGMEV_CUDA(cudaStreamSynchronize(op->stream));
+      int active = 0;
+      bool stalled = false;
+      for (int k = 0; k < K; ++k) {
+        if (host[2 * K + k] != 0.0 && tol2[k] != HUGE_VAL) {
+          tol2[k] = HUGE_VAL;  // d.q = 0: the column cannot move (the reference stops there too)
+          stalled = true;
+        }
+        if (host[k] > tol2[k] * host[K + k]) {
+          ++active;
+          ++col_it[k];
+        }
+      }
+      if (stalled)
+        SGMEV_CUDA(cudaMemcpyAsync(sc + kScTol2, tol2.data(), sizeof(double) * K,
+                                   cudaMemcpyHostToDevice, op->stream));
+      if (active == 0) break;
+      SGMEV_TRY(block_system(op, d, q, lm));
+      SGMEV_CUDA(block_cg_step(op->stream, e, r, d, q, np, part_a, part_b, sc, cur));
+      op->launches += 3;
+      cur ^= 1;
+      ++total_it;
+    }
+    axpy_kernel<<<vec_blocks(static_cast<int64_t>(vec)), 256, 0, op->stream>>>(
+        static_cast<int64_t>(vec), 1.0, e, x);
+    op->launches += 1;
+    SGMEV_TRY(block_check(op));
+  }
+  for (int k = 0; k < K; ++k)
+    if (op->n > 0)
+      SGMEV_CUDA(cudaMemcpyAsync(alpha + static_cast<int64_t>(k) * op->n, x + k * np,
+                                 sizeof(double) * op->n,
+                                 a_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                 op->stream));
+  SGMEV_TRY(end_timed(op, true));
+  SGMEV_TRY(block_check(op));
+  for (int k = 0; k < K; ++k) {
+    if (iterations) iterations[k] = col_it[k];
+    if (residuals) residuals[k] = rho[k];
+  }
+  return SGMEV_OK;
+}
+
+SGMEV_API int sgmev_fit_block(sgmev_op* op, const double* y, double lambda,
+                              int64_t max_iterations, double epsilon, double* alpha,
+                              int64_t* iterations, double* residuals) {
+  return fit_block_common(op, y, false, lambda, max_iterations, epsilon, alpha, false, iterations,
+                          residuals);
+}
+
+SGMEV_API int sgmev_fit_block_device(sgmev_op* op, const double* d_y, double lambda,
+                                     int64_t max_iterations, double epsilon, double* d_alpha,
+                                     int64_t* iterations, double* residuals) {
+  return fit_block_common(op, d_y, true, lambda, max_iterations, epsilon, d_alpha, true,
+                          iterations, residuals);
 }
 
 }  // extern "C"

@@ -1146,6 +1146,9 @@ bool subspace_build(SubPlan* p, int dim, int64_t n, const double* level_pow2, co
   p->dim = dim;
   p->n_sub = static_cast<int>(groups.size());
   p->total = offset;
+  p->h_pos = pos;
+  p->h_sub.clear();
+  for (const int4& q : sinfo) p->h_sub.push_back(make_int2(q.x, q.y));
   p->n = n;
   p->cmax = static_cast<int>(cmax);
   p->na_max = na_max;

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 namespace sgmev {
 
@@ -64,7 +65,13 @@ struct SubPlan {
   int64_t s_pad = 0;
   int64_t mat_mpad = 0;
   cudaStream_t stream = nullptr;  // device memory of the plan is allocated and freed on it
+  // host copies: (offset, cells) per subspace and the position of every grid point
+  std::vector<int2> h_sub;
+  std::vector<int> h_pos;
   bool mod = false;  // modified linear basis (ModLinear): only the materialised products support it
+  // points per read-modify-write round of the FP16 multTranspose's cell sums (1, 2 or 4; the
+  // same bits for each)
+  int multt_batch = 1;
 };
 
 // position count up to which alpha is staged in shared memory (and the fixed-point scatter, two

@@ -474,7 +474,12 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
 // FP32 cell sums are flushed into float-float sums (a two-sum, at the FP32 rate) instead of FP64
 // ones, whose adds run at a small fraction of that rate on this part (0.496 -> 0.487 ms); they
 // become FP64 once, when the row is written.
-template <typename CW, bool SACC>
+// BATCH points share one read-modify-write round of the owner's cells: their sums are all read
+// before any is written back, so the reads' latency is paid once per batch instead of once per
+// point. Points of a batch in the same cell chain through registers (a point starts from the
+// latest earlier value of its cell), and the stores go in point order, so the last store of a cell
+// holds every term: the same additions in the same order as BATCH = 1, bit for bit.
+template <typename CW, bool SACC, int BATCH>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
     const float* __restrict__ v, int64_t n_tiles, const uint4* __restrict__ pp,
@@ -532,10 +537,34 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
             const float4 p = h ? halves4(pw.z, pw.w) : halves4(pw.x, pw.y);
             const uint32_t w = PC::word(cs, h);
             const float4 vv = vt[2 * u + h];  // the same four values for every lane
-            acc[cell_of<CW>(w, 0) * nth] += vv.x * p.x;
-            acc[cell_of<CW>(w, 1) * nth] += vv.y * p.y;
-            acc[cell_of<CW>(w, 2) * nth] += vv.z * p.z;
-            acc[cell_of<CW>(w, 3) * nth] += vv.w * p.w;
+            if constexpr (BATCH == 1) {
+              acc[cell_of<CW>(w, 0) * nth] += vv.x * p.x;
+              acc[cell_of<CW>(w, 1) * nth] += vv.y * p.y;
+              acc[cell_of<CW>(w, 2) * nth] += vv.z * p.z;
+              acc[cell_of<CW>(w, 3) * nth] += vv.w * p.w;
+            } else {
+              const float pv[4] = {p.x, p.y, p.z, p.w};
+              const float vw[4] = {vv.x, vv.y, vv.z, vv.w};
+#pragma unroll
+              for (int b0 = 0; b0 < 4; b0 += BATCH) {
+                uint32_t c[BATCH];
+                float old[BATCH], nv[BATCH];
+#pragma unroll
+                for (int i = 0; i < BATCH; ++i) {
+                  c[i] = cell_of<CW>(w, b0 + i);
+                  old[i] = acc[c[i] * nth];
+                }
+#pragma unroll
+                for (int i = 0; i < BATCH; ++i) {
+                  float base = old[i];
+#pragma unroll
+                  for (int j = 0; j < i; ++j) base = c[i] == c[j] ? nv[j] : base;
+                  nv[i] = fmaf(vw[b0 + i], pv[b0 + i], base);
+                }
+#pragma unroll
+                for (int i = 0; i < BATCH; ++i) acc[c[i] * nth] = nv[i];
+              }
+            }
           }
         }
         vt += 2 * A;
@@ -1217,8 +1246,17 @@ cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, int64_t mpad, con
   if constexpr (HALF) {
     const uint4* pm = p.pmat16;
     const auto* cm = static_cast<const typename PairCells<CW>::T*>(p.cpair);
-    return sacc ? go(mat_multt_half_kernel<CW, true>, pm, cm)
-                : go(mat_multt_half_kernel<CW, false>, pm, cm);
+    switch (p.multt_batch) {
+      case 2:
+        return sacc ? go(mat_multt_half_kernel<CW, true, 2>, pm, cm)
+                    : go(mat_multt_half_kernel<CW, false, 2>, pm, cm);
+      case 4:
+        return sacc ? go(mat_multt_half_kernel<CW, true, 4>, pm, cm)
+                    : go(mat_multt_half_kernel<CW, false, 4>, pm, cm);
+      default:
+        return sacc ? go(mat_multt_half_kernel<CW, true, 1>, pm, cm)
+                    : go(mat_multt_half_kernel<CW, false, 1>, pm, cm);
+    }
   } else {
     const float4* pm = p.pmat;
     const CW* cm = static_cast<const CW*>(p.cmat);

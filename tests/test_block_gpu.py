@@ -1,0 +1,135 @@
+"""16 right-hand sides on the tensor cores (sgmev_mult_block, sgmev_mult_transpose_block,
+sgmev_fit_block) through the C ABI.
+
+The block products round the materialised subspace products to BF16 (8 significant bits: at most
+2^-8 relative) and split the 16 vectors into BF16 high and low parts (about 2^-16), accumulating
+in FP32, so column k of B [a_1 .. a_16] may differ from the FP64 product B a_k by at most about
+2^-8 times sum_s |p_s(x_j)| |a_k[c_s(x_j)]|: the tests hold every entry to 2^-7 times that sum,
+which the oracle computes exactly as B |a_k| (hats are non-negative). The block fits refine with FP64-accurate
+residuals, so each column's alpha must match the oracle's FP64 CG solution to 1e-6.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, rel_err
+
+import bench
+import sgpp_gb300 as sg
+
+pytestmark = pytest.mark.gpu
+
+K = sg.SGMEV_BLOCK_RHS
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu(lib):
+    if lib.sgmev_device_count() < 1:
+        pytest.fail("no CUDA device visible to libsgpp_gb300 (the GPU tests need one)")
+
+
+def _op(grid, x, **params):
+    p = {"algo": "subspace", "materialize": "on"}
+    p.update({k: str(v) for k, v in params.items()})
+    cfg = sg.OperationMultipleEvalConfiguration(sg.OperationMultipleEvalType.STREAMING,
+                                                sg.OperationMultipleEvalSubType.CUDA, parameters=p)
+    return sg.createOperationMultipleEval(grid, x, cfg)
+
+
+def _grid(d, level):
+    g = sg.Grid.createLinearGrid(d)
+    g.getGenerator().regular(level)
+    return g
+
+
+SHAPES = [(5, 4, 3000), (10, 3, 4097), (2, 8, 2000), (8, 4, 20000), (1, 8, 513)]
+
+
+@pytest.mark.parametrize("d,level,m", SHAPES)
+def test_block_products_within_the_bf16_bound(oracle, d, level, m):
+    rng = np.random.default_rng(500 + d * 10 + level)
+    grid = _grid(d, level)
+    n = grid.getSize()
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    x = rng.random((m, d))
+    alpha = rng.standard_normal((K, n))
+    v = rng.standard_normal((K, m))
+    op = _op(grid, x)
+    got_m = op.multBlock(alpha)
+    got_t = op.multTransposeBlock(v)
+    for k in range(K):
+        ref = oracle.mult_naive(lp, ix, x, alpha[k])
+        bound = 2.0 ** -7 * oracle.mult_naive(lp, ix, x, np.abs(alpha[k])) + 1e-12
+        assert np.all(np.abs(got_m[k] - ref) <= bound), (k, np.max(np.abs(got_m[k] - ref) / bound))
+        ref_t = oracle.mult_transpose_naive(lp, ix, x, v[k])
+        bound_t = 2.0 ** -7 * oracle.mult_transpose_naive(lp, ix, x, np.abs(v[k])) + 1e-12
+        assert np.all(np.abs(got_t[k] - ref_t) <= bound_t), (k, np.max(np.abs(got_t[k] - ref_t) / bound_t))
+    op.close()
+
+
+def test_block_products_are_reproducible_and_columns_independent(oracle):
+    rng = np.random.default_rng(77)
+    grid = _grid(6, 4)
+    x = rng.random((5000, 6))
+    op = _op(grid, x)
+    a = rng.standard_normal((K, grid.getSize()))
+    first = op.multBlock(a)
+    again = op.multBlock(a)
+    np.testing.assert_array_equal(first, again)
+    # a column's result does not depend on the other columns
+    b = a.copy()
+    b[1:] = rng.standard_normal((K - 1, grid.getSize()))
+    np.testing.assert_array_equal(op.multBlock(b)[0], first[0])
+    op.close()
+
+
+@pytest.mark.parametrize("d,level,m,lam", [(4, 4, 3000, 1e-3), (6, 3, 2500, 1e-4)])
+def test_block_fit_matches_oracle_cg_per_column(oracle, d, level, m, lam):
+    rng = np.random.default_rng(900 + d)
+    grid = _grid(d, level)
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    x = rng.random((m, d))
+    y = np.empty((K, m))
+    y[0] = 10 * np.sin(np.pi * x[:, 0] * x[:, 1]) + 20 * (x[:, 2] - 0.5) ** 2 + 10 * x[:, 3]
+    y[1:] = rng.standard_normal((K - 1, m))
+    op = _op(grid, x)
+    alpha, its, res = op.fitBlock(y, lam, 100000, 1e-10)
+    st = oracle.stream(x)
+    for k in range(K):
+        ref, _, _ = st.cg_fit(lp, ix, y[k], lam, 100000, 1e-12)
+        assert rel_err(alpha[k], ref) < 1e-6, (k, rel_err(alpha[k], ref))
+        assert its[k] > 0
+    st.close()
+    op.close()
+
+
+def test_block_fit_on_the_regression_workload():
+    """The benchmark's regression workload (d=10 level 5, M=2^20): column 0 fits the benchmark's
+    y and must match the reference's own FP64 CG solution (fixture) to 1e-6; the other columns
+    fit other targets and must match this library's single-vector mixed fit to 1e-6."""
+    f = np.load(os.path.join(GOLDEN, "regression_d10_l5.npz"))
+    x, y0 = bench.make_workload(int(f["seed"]))
+    np.testing.assert_allclose(bench.workload_checksums(x, y0), f["checksums"], rtol=1e-12)
+    grid = _grid(bench.DIM, bench.LEVEL)
+    rng = np.random.default_rng(5)
+    y = np.empty((K, x.shape[0]))
+    y[0] = y0
+    y[1:] = y0 + rng.standard_normal((K - 1, x.shape[0]))
+    op = _op(grid, x)
+    alpha, its, res = op.fitBlock(y, bench.LAMBDA, 100000, 1e-8)
+    assert rel_err(alpha[0], f["alpha"]) < 1e-6, rel_err(alpha[0], f["alpha"])
+    for k in (1, K - 1):
+        a1, _, _ = op.fit(y[k], bench.LAMBDA, 100000, 1e-10, mode=sg.SGMEV_SOLVE_MIXED)
+        assert rel_err(alpha[k], a1) < 1e-6, (k, rel_err(alpha[k], a1))
+    op.close()
+
+
+def test_block_products_refuse_an_operator_without_materialised_products():
+    rng = np.random.default_rng(3)
+    grid = _grid(3, 3)
+    x = rng.random((100, 3))
+    op = _op(grid, x, materialize="off")
+    with pytest.raises(sg.OperationException, match="materialised"):
+        op.multBlock(np.zeros((K, grid.getSize())))
+    op.close()

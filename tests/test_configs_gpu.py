@@ -107,3 +107,26 @@ def test_adaptive_configuration_matches_reference_loop(mode, tol):
     order = np.array([ours[k] for k in theirs])  # reference position -> our position
     ref_alpha = f["alpha"][np.array(list(theirs.values()))]
     assert rel_err(alpha[order], ref_alpha) < tol
+
+
+@pytest.mark.parametrize("batch", ["2", "4"])
+def test_multt_batch_gives_the_same_bits(batch):
+    """The FP16 multTranspose's batched read-modify-write (multt_batch) adds the same terms in the
+    same order as one point at a time, so a mixed fit gives the same bits."""
+    rng = np.random.default_rng(31)
+    d, level, m = 6, 4, 30000
+    grid = sg.Grid.createLinearGrid(d)
+    grid.getGenerator().regular(level)
+    x = rng.random((m, d))
+    y = np.sin(3 * x[:, 0]) + x[:, 1] ** 2 + 0.1 * rng.standard_normal(m)
+    out = []
+    for b in ("1", batch):
+        cfg = sg.OperationMultipleEvalConfiguration(
+            sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
+            parameters={"algo": "subspace", "materialize": "on", "multt_batch": b})
+        op = sg.createOperationMultipleEval(grid, x, cfg)
+        a, it, _ = op.fit(y, 1e-4, 10000, 1e-10, mode=sg.SGMEV_SOLVE_MIXED)
+        out.append((a, it))
+        op.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1]
