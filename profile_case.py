@@ -40,11 +40,13 @@ KINDS = {("mult", "float", "dense"): sg.SGMEV_KERNEL_MULT_FP32,
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["mult", "multT", "system", "fit"], default="mult",
+    ap.add_argument("--kernel", choices=["mult", "multT", "system", "fit", "block_mult",
+                                         "block_multT"], default="mult",
                     help="system: B^T (B a) + lambda M a (systemApply; with materialized "
                          "products the fused kernel, system_product=fused); fit: one "
                          "mixed-precision fit (its inner solves stream the FP16 products); "
-                         "reports the kernel given by --report")
+                         "reports the kernel given by --report; block_mult / block_multT: the "
+                         "BF16 tensor-core products with 16 right-hand sides")
     ap.add_argument("--report", choices=["mult16", "multT16"], default="mult16",
                     help="with --kernel fit: which kernel's launches to report")
     ap.add_argument("--precision", choices=["float", "double", "df64"], default="float")
@@ -56,6 +58,8 @@ def main() -> int:
     ap.add_argument("--points", type=int, default=1 << 22)
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--param", action="append", default=[], metavar="KEY=VALUE",
+                    help="operator knob (repeatable), e.g. multt_batch=2")
     args = ap.parse_args()
 
     mat = args.algo == "materialized"
@@ -71,15 +75,23 @@ def main() -> int:
                                                     "algo": "subspace" if mat else args.algo,
                                                     "materialize": "on" if mat else "off",
                                                     "materialize_multt": "on" if mat else "off",
-                                                    "system_product": "fused"})
+                                                    "system_product": "fused",
+                                                    **dict(kv.split("=", 1) for kv in args.param)})
     op = sg.createOperationMultipleEval(grid, x, cfg)
     a = rng.standard_normal(n)
     v = rng.standard_normal(args.points)
     out_m = np.zeros(args.points)
     out_t = np.zeros(n)
 
+    ab = rng.standard_normal((sg.SGMEV_BLOCK_RHS, n))
+    vb = rng.standard_normal((sg.SGMEV_BLOCK_RHS, args.points))
+
     def run():
-        if args.kernel == "fit":
+        if args.kernel == "block_mult":
+            op.multBlock(ab)
+        elif args.kernel == "block_multT":
+            op.multTransposeBlock(vb)
+        elif args.kernel == "fit":
             op.fit(v, 1e-4, 100000, 1e-8, mode=sg.SGMEV_SOLVE_MIXED)
         elif args.kernel == "system":
             op.systemApply(a, out_t, 1e-4 * args.points)
@@ -96,6 +108,8 @@ def main() -> int:
     algo = "dense" if args.precision == "double" else args.algo
     if args.kernel == "fit":
         kind = sg.SGMEV_KERNEL_MULT_MAT16 if args.report == "mult16" else sg.SGMEV_KERNEL_MULTT_MAT16
+    elif args.kernel.startswith("block"):
+        kind = sg.SGMEV_KERNEL_BLOCK_MULT if args.kernel == "block_mult" else sg.SGMEV_KERNEL_BLOCK_MULTT
     else:
         kind = KINDS[(args.kernel, args.precision, algo)]
     cnt, sec = op.profileRead(kind)

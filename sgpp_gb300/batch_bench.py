@@ -31,6 +31,59 @@ import sgpp_gb300 as sg  # noqa: E402
 from sgpp_gb300.serving import MixGenerator  # noqa: E402
 
 
+def block_pool(probs, lam: float, epsilon: float, workers: int):
+    """Every problem's 16 right-hand sides as one block fit (sgmev_fit_block: BF16 tensor-core
+    inner solves, df64 residuals) on its own operator and stream, `workers` problems at a time.
+    A problem the block products do not take (a subspace above 128 cells, or products too large
+    to materialise) runs its right-hand sides as single mixed fits. Returns
+    (seconds, alphas, paths, inner steps per problem)."""
+    import queue
+    import threading
+
+    work = queue.Queue()
+    for k in range(len(probs)):
+        work.put(k)
+    alphas = [None] * len(probs)
+    paths = [None] * len(probs)
+    steps = [0] * len(probs)
+    errors = []
+
+    def run():
+        while True:
+            try:
+                k = work.get_nowait()
+            except queue.Empty:
+                return
+            g, X, Y = probs[k]
+            try:
+                op = sg.createOperationMultipleEval(g, X)
+                try:
+                    a, its, _ = op.fitBlock(np.ascontiguousarray(Y.T), lam, 100000, epsilon)
+                    alphas[k], paths[k], steps[k] = a.T, "block", int(max(its))
+                except sg.OperationException:
+                    cols = []
+                    for c in range(Y.shape[1]):
+                        a, it, _ = op.fit(np.ascontiguousarray(Y[:, c]), lam, 100000, epsilon,
+                                          mode=sg.SGMEV_SOLVE_MIXED)
+                        cols.append(a)
+                        steps[k] += it
+                    alphas[k], paths[k] = np.stack(cols, axis=1), "single"
+                op.close()
+            except BaseException as e:  # reported after the run
+                errors.append(e)
+
+    threads = [threading.Thread(target=run, daemon=True) for _ in range(workers)]
+    t0 = time.perf_counter()
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    sec = time.perf_counter() - t0
+    if errors:
+        raise errors[0]
+    return sec, alphas, paths, steps
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--problems", type=int, default=96)
@@ -41,7 +94,13 @@ def main() -> int:
     ap.add_argument("--check", type=int, default=4, help="problems checked against FP64 fits")
     ap.add_argument("--sequential", type=int, default=4, help="problems timed sequentially")
     ap.add_argument("--seed", type=int, default=11)
+    ap.add_argument("--engine", choices=["batch", "block"], default="batch",
+                    help="batch: the batch engine (dense kernels, one persistent launch per "
+                         "phase); block: per-problem block fits on the tensor cores")
+    ap.add_argument("--workers", type=int, default=4, help="block engine: problems in flight")
     args = ap.parse_args()
+    if args.engine == "block":
+        return main_block(args)
 
     gen = MixGenerator(args.seed, args.max_work, pool=4)
     probs = [gen.draw(args.rhs) for _ in range(args.problems)]
@@ -97,6 +156,52 @@ def main() -> int:
             args.problems * share / sum(seq_mixed) if seq_mixed else None),
         "sequential_note": (f"timed on the first {len(seq_plain)} problems x 1 right-hand side, "
                             "rescaled by their share of the batch's N*M*d work"),
+        "config": {"mix": "d 2..12, level 3..7, M log-uniform [1e3, 2^20], uniform data",
+                   "max_work_NMd": args.max_work, "epsilon": args.epsilon, "lambda": args.lam},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main_block(args) -> int:
+    gen = MixGenerator(args.seed, args.max_work, pool=4)
+    probs = [gen.draw(args.rhs) for _ in range(args.problems)]
+    if args.rhs != sg.SGMEV_BLOCK_RHS:
+        raise SystemExit(f"--engine block takes --rhs {sg.SGMEV_BLOCK_RHS}")
+    block_pool(probs[:2], args.lam, args.epsilon, 1)  # warm-up (library and kernels loaded)
+    sec, alphas, paths, steps = block_pool(probs, args.lam, args.epsilon, args.workers)
+    errs = []
+    for k in range(min(args.check, args.problems)):
+        g, X, Y = probs[k]
+        op = sg.createOperationMultipleEval(g, X)
+        for c in (0, args.rhs - 1):
+            ref, _, _ = op.fit(np.ascontiguousarray(Y[:, c]), args.lam, 100000, 1e-12,
+                               mode=sg.SGMEV_SOLVE_MIXED)
+            errs.append(float(np.abs(alphas[k][:, c] - ref).max() / np.abs(ref).max()))
+        op.close()
+    seq = []
+    for k in range(min(args.sequential, args.problems)):
+        g, X, Y = probs[k]
+        op = sg.createOperationMultipleEval(g, X)
+        t1 = time.perf_counter()
+        op.fit(np.ascontiguousarray(Y[:, 0]), args.lam, 100000, args.epsilon,
+               mode=sg.SGMEV_SOLVE_MIXED)
+        seq.append(time.perf_counter() - t1)
+        op.close()
+    work = np.array([g.getSize() * X.shape[0] * g.getDimension() for g, X, _ in probs], float)
+    share = work[: len(seq)].sum() / work.sum()
+    solves = args.problems * args.rhs
+    line = {
+        "metric": "batched_solves_per_sec", "value": solves / sec, "unit": "solves/s",
+        "engine": "block", "problems": args.problems, "rhs": args.rhs, "seconds": sec,
+        "workers": args.workers,
+        "paths": {p: paths.count(p) for p in set(paths)},
+        "inner_steps": {"min": int(min(steps)), "max": int(max(steps))},
+        "alpha_rel_err_vs_fp64": {"max": max(errs) if errs else None, "checked_solves": len(errs)},
+        "sequential_single_mixed_solves_per_sec_est": (
+            args.problems * share / sum(seq) if seq else None),
+        "sequential_note": (f"one right-hand side of the first {len(seq)} problems by the "
+                            "single-target mixed fit, rescaled by their share of the N*M*d work"),
         "config": {"mix": "d 2..12, level 3..7, M log-uniform [1e3, 2^20], uniform data",
                    "max_work_NMd": args.max_work, "epsilon": args.epsilon, "lambda": args.lam},
     }

@@ -32,12 +32,18 @@ namespace {
 
 constexpr int kProdWarps = 8;
 constexpr int kProdThreads = kProdWarps * 32;
-constexpr int kBlockThreads = kProdThreads + 32;  // + the MMA warp
+constexpr int kMmaWarp = kProdWarps;         // one thread issues the MMAs
+constexpr int kLoadWarp = kProdWarps + 1;    // one thread issues the bulk copies
+constexpr int kBlockThreads = kProdThreads + 64;
 constexpr uint32_t kStageBytes = 128u * 16u * 16u;  // 128 points x 16 chunks x 16 bytes
 constexpr uint32_t kCoefBytes = 4096u * 2u;         // 128 rows x 32 columns of BF16
 constexpr uint32_t kQBytes = 4096u * 2u;            // 128 points x 32 columns of BF16
+constexpr uint32_t kSlotRow = 128u * 4u;            // one slot's packed words of a tile
+constexpr uint32_t kLoadBytes = 16u * kSlotRow;     // a group has at most 16 slots
 constexpr uint32_t kWaitLimit = 1u << 22;           // polls of one bounded wait
+constexpr uint32_t kPollLimit = 1u << 25;           // idle rounds of the loader's polling loop
 constexpr int kMaxStages = 6;
+constexpr int kMaxLoads = 12;
 // core-matrix strides of the operands: 128 bytes between neighbouring core matrices along the
 // row dimension of a chunk / K-step (8 elements), 2048 bytes between groups of 8 points or of 8
 // output columns
@@ -45,12 +51,16 @@ constexpr uint32_t kCoreK = 128, kCoreMN = 2048;
 
 __host__ __device__ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
-// barrier and bookkeeping words behind the stages
+// barrier and bookkeeping words behind the buffers
 struct Sync {
-  uint64_t full[kMaxStages];
-  uint64_t empty[kMaxStages];
-  uint64_t qempty[2];
-  uint64_t pass;
+  uint64_t full[kMaxStages];   // E stage written (producers)
+  uint64_t empty[kMaxStages];  // E stage read by the tensor cores (MMA commit)
+  uint64_t lfull[kMaxLoads];   // packed products of a stage arrived (bulk copies)
+  uint64_t lempty[kMaxLoads];  // packed products read (producers)
+  uint64_t qfull[2];           // Q tile arrived (multT)
+  uint64_t qempty[2];          // Q tile read by the tensor cores (multT)
+  uint64_t cfull;              // coefficient rows of a pass arrived (mult)
+  uint64_t pass;               // MMAs of a pass completed (mult)
   uint64_t last;
   uint32_t tmem;
   volatile int abort;
@@ -74,6 +84,34 @@ __host__ __device__ inline uint32_t opnd_off(int n, int r) {
   return static_cast<uint32_t>((n >> 3) * 2048 + (r >> 3) * 128 + (n & 7) * 16 + (r & 7) * 2);
 }
 
+// ---- bulk copies (the loader thread) ------------------------------------------------------------
+__device__ __forceinline__ void bulk_expect(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes)
+               : "memory");
+}
+// global -> shared, `bytes` a multiple of 16, both addresses 16-byte aligned
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes,
+                                          uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
+
+// The packed products of stage (tile, group): the group's slot rows of the tile, one bulk copy
+// each, into load buffer `buf`
+__device__ __forceinline__ void load_stage(unsigned char* buf, uint32_t mbar,
+                                           const uint32_t* __restrict__ pc,
+                                           const int2* __restrict__ gslots, int64_t mpad,
+                                           int group, int64_t tile) {
+  const int2 gs = __ldg(gslots + group);
+  bulk_expect(mbar, static_cast<uint32_t>(gs.y) * kSlotRow);
+  for (int j = 0; j < gs.y; ++j)
+    bulk_copy(tc::smem_u32(buf + j * kSlotRow), pc + static_cast<int64_t>(gs.x + j) * mpad + tile * 128,
+              kSlotRow, mbar);
+}
+
 // ---- producer: one stage of E ----------------------------------------------------------------
 // The thread's slots for a stage: up to 8 subspaces overlapping its half of the group.
 struct SlotLoads {
@@ -82,19 +120,20 @@ struct SlotLoads {
   int count;
 };
 
-__device__ __forceinline__ void load_slots(SlotLoads& L, const uint32_t* __restrict__ pc,
+// the thread's words from the stage's load buffer ([slot in group][128 points])
+__device__ __forceinline__ void read_slots(SlotLoads& L, const uint32_t* lbuf,
                                            const int4* __restrict__ ghalf,
-                                           const uint16_t* __restrict__ slot_cn, int64_t mpad,
-                                           int group, int h, int64_t point) {
+                                           const uint16_t* __restrict__ slot_cn, int group, int h,
+                                           int p) {
   const int4 gh = __ldg(ghalf + 2 * group + h);
   L.count = gh.z;
   const uint32_t idx[2] = {static_cast<uint32_t>(gh.x), static_cast<uint32_t>(gh.y)};
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     if (i < L.count) {
-      const int sl = gh.w + static_cast<int>((idx[i >> 2] >> (8 * (i & 3))) & 0xFFu);
-      L.w[i] = __ldcs(pc + static_cast<int64_t>(sl) * mpad + point);
-      L.cn[i] = __ldg(slot_cn + sl);
+      const int local = static_cast<int>((idx[i >> 2] >> (8 * (i & 3))) & 0xFFu);
+      L.w[i] = lbuf[local * 128 + p];
+      L.cn[i] = __ldg(slot_cn + gh.w + local);
     } else {
       L.w[i] = 0u;
       L.cn[i] = 0u;
@@ -125,25 +164,69 @@ __device__ __forceinline__ void write_stage(unsigned char* stage, int p, int h,
   }
 }
 
-// ---- mult: Q[tile] = sum over groups of E[tile][group] C[group] -------------------------------
-// A CTA owns `tiles` consecutive tiles, whose accumulators (128 x 32 FP32 each) stay in tensor
-// memory, and walks the groups in passes of `gpp` groups whose coefficient rows it copies into
-// shared memory. Output: the BF16 Q tiles (operand layout of block_multt) and optionally Q in FP64.
-__global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
-    const uint32_t* __restrict__ pc, const int4* __restrict__ ghalf,
-    const uint16_t* __restrict__ slot_cn, const uint16_t* __restrict__ coef, int n_groups,
-    int64_t mpad, int64_t m, int n_tiles, int tiles, int gpp, int stages, uint32_t tmem_cols,
-    uint16_t* __restrict__ qtiles, double* __restrict__ out64, int* __restrict__ status) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* st = smem;                                       // stages
-  unsigned char* cf = smem + static_cast<size_t>(stages) * kStageBytes;  // coefficient rows
-  Sync* sy = reinterpret_cast<Sync*>(cf + static_cast<size_t>(gpp) * kCoefBytes);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int t0 = blockIdx.x * tiles;
-  const int nt = min(tiles, n_tiles - t0);
-  const int passes = static_cast<int>(cdiv(n_groups, gpp));
+// The producers' part of stage i: wait for its packed products, read them, free the load buffer,
+// wait for the E stage to be free, write it, mark it full. False when a wait ran out.
+__device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st,
+                                        unsigned char* lb, int stages, int loads, int64_t i,
+                                        const int4* __restrict__ ghalf,
+                                        const uint16_t* __restrict__ slot_cn, int group, int p,
+                                        int h) {
+  const int b = static_cast<int>(i % loads);
+  if (!tc::mbar_wait(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((i / loads) & 1),
+                     kWaitLimit)) {
+    fail_wait(sy, status, 32);
+    return false;
+  }
+  SlotLoads L;
+  read_slots(L, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes), ghalf,
+             slot_cn, group, h, p);
+  tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
+  const int sidx = static_cast<int>(i % stages);
+  const int64_t use = i / stages;
+  if (use > 0 && !tc::mbar_wait(tc::smem_u32(&sy->empty[sidx]),
+                                static_cast<uint32_t>((use - 1) & 1), kWaitLimit)) {
+    fail_wait(sy, status, 2);
+    return false;
+  }
+  write_stage(st + static_cast<size_t>(sidx) * kStageBytes, p, h, L);
+  tc::fence_proxy_async();
+  tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
+  return true;
+}
 
-  // zero the stages (rows a group leaves unused must hold finite values), barriers, tensor memory
+// The loader's part of stage i: wait for the load buffer to be free, issue the bulk copies.
+__device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, int loads,
+                                     int64_t i, const uint32_t* __restrict__ pc,
+                                     const int2* __restrict__ gslots, int64_t mpad, int group,
+                                     int64_t tile) {
+  const int b = static_cast<int>(i % loads);
+  const int64_t use = i / loads;
+  if (use > 0 && !tc::mbar_wait(tc::smem_u32(&sy->lempty[b]),
+                                static_cast<uint32_t>((use - 1) & 1), kWaitLimit)) {
+    fail_wait(sy, status, 64);
+    return false;
+  }
+  load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc, gslots,
+             mpad, group, tile);
+  return true;
+}
+
+// The loader's copies still in flight complete before the CTA may exit (the last `loads` stages
+// it issued)
+__device__ __forceinline__ void drain_loads(Sync* sy, int* status, int loads, int64_t issued) {
+  for (int64_t i = issued > loads ? issued - loads : 0; i < issued; ++i) {
+    const int b = static_cast<int>(i % loads);
+    if (!tc::mbar_wait(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((i / loads) & 1),
+                       kWaitLimit))
+      atomicOr(status, 128);
+  }
+}
+
+// Shared set-up of both kernels: zeroed E stages (rows a group leaves unused must hold finite
+// values), barriers, tensor memory.
+__device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int stages, int loads,
+                                            uint32_t tmem_cols) {
+  const int tid = threadIdx.x;
   for (uint32_t k = tid; k < static_cast<uint32_t>(stages) * kStageBytes / 16u; k += blockDim.x)
     reinterpret_cast<uint4*>(st)[k] = make_uint4(0u, 0u, 0u, 0u);
   if (tid == 0) {
@@ -151,73 +234,71 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
       tc::mbar_init(tc::smem_u32(&sy->full[k]), kProdThreads);
       tc::mbar_init(tc::smem_u32(&sy->empty[k]), 1);
     }
+    for (int k = 0; k < loads; ++k) {
+      tc::mbar_init(tc::smem_u32(&sy->lfull[k]), 1);
+      tc::mbar_init(tc::smem_u32(&sy->lempty[k]), kProdThreads);
+    }
+    for (int k = 0; k < 2; ++k) {
+      tc::mbar_init(tc::smem_u32(&sy->qfull[k]), 1);
+      tc::mbar_init(tc::smem_u32(&sy->qempty[k]), 1);
+    }
+    tc::mbar_init(tc::smem_u32(&sy->cfull), 1);
     tc::mbar_init(tc::smem_u32(&sy->pass), 1);
     tc::mbar_init(tc::smem_u32(&sy->last), 1);
     sy->abort = 0;
     tc::mbar_init_fence();
   }
-  if (warp == kProdWarps) tc::tmem_alloc(tc::smem_u32(&sy->tmem), tmem_cols);
+  if ((tid >> 5) == kMmaWarp) tc::tmem_alloc(tc::smem_u32(&sy->tmem), tmem_cols);
   tc::fence_proxy_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
+}
+
+// ---- mult: Q[tile] = sum over groups of E[tile][group] C[group] -------------------------------
+// A CTA owns `tiles` consecutive tiles, whose accumulators (128 x 32 FP32 each) stay in tensor
+// memory, and walks the groups in passes of `gpp` groups whose coefficient rows the loader copies
+// into shared memory once the previous pass's MMAs have completed. Output: the BF16 Q tiles
+// (operand layout of block_multt) and optionally Q in FP64.
+__global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
+    const uint32_t* __restrict__ pc, const int4* __restrict__ ghalf,
+    const int2* __restrict__ gslots, const uint16_t* __restrict__ slot_cn,
+    const uint16_t* __restrict__ coef, int n_groups, int64_t mpad, int64_t m, int n_tiles,
+    int tiles, int gpp, int stages, int loads, uint32_t tmem_cols, uint16_t* __restrict__ qtiles,
+    double* __restrict__ out64, int* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* st = smem;
+  unsigned char* lb = st + static_cast<size_t>(stages) * kStageBytes;
+  unsigned char* cf = lb + static_cast<size_t>(loads) * kLoadBytes;
+  Sync* sy = reinterpret_cast<Sync*>(cf + static_cast<size_t>(gpp) * kCoefBytes);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int t0 = blockIdx.x * tiles;
+  const int nt = min(tiles, n_tiles - t0);
+  const int passes = static_cast<int>(cdiv(n_groups, gpp));
+  block_setup(sy, st, stages, loads, tmem_cols);
   const uint32_t tmem = sy->tmem;
   const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, false, false);
 
-  int64_t i0 = 0;  // stages issued before this pass
-  for (int pass = 0; pass < passes; ++pass) {
-    const int g0 = pass * gpp, g1 = min(n_groups, g0 + gpp);
-    if (pass > 0 && !sy->abort) {
-      // the coefficient rows of the last pass are overwritten once its MMAs have completed
-      if (!tc::mbar_wait(tc::smem_u32(&sy->pass), (pass - 1) & 1, kWaitLimit))
+  if (tid < kProdThreads) {
+    const int p = tid & 127, h = tid >> 7;
+    int64_t i = 0;
+    for (int pass = 0; pass < passes && !sy->abort; ++pass) {
+      const int g0 = pass * gpp, ng = min(n_groups, g0 + gpp) - g0;
+      for (int k = 0; k < nt * ng; ++k, ++i)
+        if (!produce(sy, status, st, lb, stages, loads, i, ghalf, slot_cn, g0 + k % ng, p, h)) break;
+    }
+  } else if (tid == kMmaWarp * 32) {
+    int64_t i = 0;
+    for (int pass = 0; pass < passes && !sy->abort; ++pass) {
+      const int g0 = pass * gpp, ng = min(n_groups, g0 + gpp) - g0;
+      if (!tc::mbar_wait(tc::smem_u32(&sy->cfull), static_cast<uint32_t>(pass & 1), kWaitLimit)) {
         fail_wait(sy, status, 1);
-    }
-    __syncthreads();
-    if (!sy->abort) {
-      const uint4* src = reinterpret_cast<const uint4*>(coef + static_cast<int64_t>(g0) * 4096);
-      uint4* dst = reinterpret_cast<uint4*>(cf);
-      const int words = (g1 - g0) * static_cast<int>(kCoefBytes / 16u);
-      for (int k = tid; k < words; k += blockDim.x) dst[k] = __ldg(src + k);
-      tc::fence_proxy_async();
-    }
-    __syncthreads();
-    const int per_pass = nt * (g1 - g0);
-    if (tid < kProdThreads) {
-      const int p = tid & 127, h = tid >> 7;
-      SlotLoads cur, nxt;
-      if (per_pass > 0 && !sy->abort)
-        load_slots(cur, pc, ghalf, slot_cn, mpad, g0, h, static_cast<int64_t>(t0) * 128 + p);
-      for (int k = 0; k < per_pass && !sy->abort; ++k) {
-        const int u = k / (g1 - g0), g = g0 + k % (g1 - g0);
-        if (k + 1 < per_pass) {
-          const int un = (k + 1) / (g1 - g0), gn = g0 + (k + 1) % (g1 - g0);
-          load_slots(nxt, pc, ghalf, slot_cn, mpad, gn, h,
-                     static_cast<int64_t>(t0 + un) * 128 + p);
-        }
-        const int64_t i = i0 + k;
-        const int sidx = static_cast<int>(i % stages);
-        const int64_t use = i / stages;
-        if (use > 0 &&
-            !tc::mbar_wait(tc::smem_u32(&sy->empty[sidx]), static_cast<uint32_t>((use - 1) & 1),
-                           kWaitLimit)) {
-          fail_wait(sy, status, 2);
-          break;
-        }
-        (void)u;
-        (void)g;
-        write_stage(st + static_cast<size_t>(sidx) * kStageBytes, p, h, cur);
-        tc::fence_proxy_async();
-        tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
-        cur = nxt;
+        break;
       }
-    } else if (tid == kProdThreads) {
-      // the MMA thread
-      for (int k = 0; k < per_pass && !sy->abort; ++k) {
-        const int u = k / (g1 - g0), gl = k % (g1 - g0);
-        const int64_t i = i0 + k;
+      for (int k = 0; k < nt * ng; ++k, ++i) {
+        const int u = k / ng, gl = k % ng;
         const int sidx = static_cast<int>(i % stages);
-        const int64_t use = i / stages;
-        if (!tc::mbar_wait(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>(use & 1),
+        if (!tc::mbar_wait(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>((i / stages) & 1),
                            kWaitLimit)) {
           fail_wait(sy, status, 4);
           break;
@@ -235,10 +316,60 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
       }
       tc::mma_commit(tc::smem_u32(&sy->pass));
     }
-    i0 += per_pass;
+  } else if (tid == kLoadWarp * 32) {
+    // The loader interleaves two streams of copies without blocking on either: the packed
+    // products of the next stage (as soon as its load buffer is free) and the coefficient rows of
+    // the next pass (as soon as the last pass's MMAs have completed). Waiting for one while the
+    // other is due could stall the MMA thread on coefficients that are never issued.
+    auto issue_coef = [&](int pass) {
+      const int g0 = pass * gpp, ng = min(n_groups, g0 + gpp) - g0;
+      const uint32_t cb = tc::smem_u32(&sy->cfull);
+      bulk_expect(cb, static_cast<uint32_t>(ng) * kCoefBytes);
+      for (int g = 0; g < ng; ++g)
+        bulk_copy(tc::smem_u32(cf + static_cast<size_t>(g) * kCoefBytes),
+                  coef + static_cast<int64_t>(g0 + g) * 4096, kCoefBytes, cb);
+    };
+    issue_coef(0);
+    int coef_next = 1;
+    int64_t next = 0;                   // next stage to load
+    int lpass = 0, lk = 0;              // its pass and index within the pass
+    int lng = min(n_groups, gpp);       // groups of that pass
+    uint32_t idle = 0;
+    while (!sy->abort && (lpass < passes || coef_next < passes)) {
+      bool progress = false;
+      if (coef_next < passes &&
+          tc::mbar_poll(tc::smem_u32(&sy->pass), static_cast<uint32_t>((coef_next - 1) & 1))) {
+        issue_coef(coef_next++);
+        progress = true;
+      }
+      if (lpass < passes) {
+        const int b = static_cast<int>(next % loads);
+        const int64_t use = next / loads;
+        if (use == 0 || tc::mbar_poll(tc::smem_u32(&sy->lempty[b]), static_cast<uint32_t>((use - 1) & 1))) {
+          load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc,
+                     gslots, mpad, lpass * gpp + lk % lng, t0 + lk / lng);
+          ++next;
+          if (++lk == nt * lng) {
+            lk = 0;
+            ++lpass;
+            lng = min(n_groups, (lpass + 1) * gpp) - lpass * gpp;
+          }
+          progress = true;
+        }
+      }
+      idle = progress ? 0u : idle + 1u;
+      if (!progress) __nanosleep(20);  // leave the issue slots to the producers
+      if (idle > kPollLimit) {
+        fail_wait(sy, status, 64);
+        break;
+      }
+    }
+    drain_loads(sy, status, loads, next);
+    if (!tc::mbar_wait(tc::smem_u32(&sy->cfull), static_cast<uint32_t>((coef_next - 1) & 1), kWaitLimit))
+      atomicOr(status, 128);
   }
   // every MMA of the CTA has completed once the last commit has
-  if (tid == kProdThreads) {
+  if (tid == kMmaWarp * 32) {
     tc::mma_commit(tc::smem_u32(&sy->last));
     if (!tc::mbar_wait(tc::smem_u32(&sy->last), 0, kWaitLimit)) fail_wait(sy, status, 8);
   }
@@ -274,96 +405,55 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == kProdWarps) tc::tmem_dealloc(tmem, tmem_cols);
+  if (warp == kMmaWarp) tc::tmem_dealloc(tmem, tmem_cols);
 }
 
 // ---- multT: R[group] = sum over tiles of E[tile][group]^T Q[tile] -----------------------------
 // CTA b takes the groups of pass b / streams (up to `gpc` accumulators of 128 rows x 32 FP32 in
-// tensor memory) and the tiles of stream b % streams; the Q tile (BF16, operand layout) is copied
-// into one of two shared-memory buffers per tile. The accumulators go out as FP64 partial rows of
-// the stream, summed over the streams in order by block_finish_kernel.
-// Operand A (E^T, MN-major) core-matrix offsets: along the rows (M) and along the points (K).
+// tensor memory) and the tiles of stream b % streams; the loader copies each tile's Q (BF16,
+// operand layout) into one of two buffers ahead of its first stage. The accumulators go out as
+// FP64 partial rows of the stream, summed over the streams in order by block_finish_kernel.
+// Operand A (E^T, MN-major) core-matrix offsets: along the points (K, leading) and along the
+// rows (M, strided).
 constexpr uint32_t kMnA_LBO = 2048, kMnA_SBO = 128;
 
 __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
     const uint32_t* __restrict__ pc, const int4* __restrict__ ghalf,
-    const uint16_t* __restrict__ slot_cn, const uint16_t* __restrict__ qtiles, int n_groups,
-    int64_t mpad, int n_tiles, int gpc, int streams, int stages, uint32_t tmem_cols, int64_t rows,
+    const int2* __restrict__ gslots, const uint16_t* __restrict__ slot_cn,
+    const uint16_t* __restrict__ qtiles, int n_groups, int64_t mpad, int n_tiles, int gpc,
+    int streams, int stages, int loads, uint32_t tmem_cols, int64_t rows,
     double* __restrict__ part, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* st = smem;
-  unsigned char* qb = smem + static_cast<size_t>(stages) * kStageBytes;  // two Q tiles
+  unsigned char* lb = st + static_cast<size_t>(stages) * kStageBytes;
+  unsigned char* qb = lb + static_cast<size_t>(loads) * kLoadBytes;  // two Q tiles
   Sync* sy = reinterpret_cast<Sync*>(qb + 2 * kQBytes);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int pass = blockIdx.x / streams, stream = blockIdx.x % streams;
   const int g0 = pass * gpc, ng = min(gpc, n_groups - g0);
   const int ta = static_cast<int>(static_cast<int64_t>(stream) * n_tiles / streams);
   const int tb = static_cast<int>(static_cast<int64_t>(stream + 1) * n_tiles / streams);
-  const int64_t total = static_cast<int64_t>(tb - ta) * ng;
-
-  for (uint32_t k = tid; k < static_cast<uint32_t>(stages) * kStageBytes / 16u; k += blockDim.x)
-    reinterpret_cast<uint4*>(st)[k] = make_uint4(0u, 0u, 0u, 0u);
-  if (tid == 0) {
-    for (int k = 0; k < stages; ++k) {
-      tc::mbar_init(tc::smem_u32(&sy->full[k]), kProdThreads);
-      tc::mbar_init(tc::smem_u32(&sy->empty[k]), 1);
-    }
-    tc::mbar_init(tc::smem_u32(&sy->qempty[0]), 1);
-    tc::mbar_init(tc::smem_u32(&sy->qempty[1]), 1);
-    tc::mbar_init(tc::smem_u32(&sy->last), 1);
-    sy->abort = 0;
-    tc::mbar_init_fence();
-  }
-  if (warp == kProdWarps) tc::tmem_alloc(tc::smem_u32(&sy->tmem), tmem_cols);
-  tc::fence_proxy_async();
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
+  const int64_t total = ng > 0 ? static_cast<int64_t>(tb - ta) * ng : 0;
+  block_setup(sy, st, stages, loads, tmem_cols);
   const uint32_t tmem = sy->tmem;
   const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, true, false);
 
-  if (tid < kProdThreads && ng > 0) {
+  if (tid < kProdThreads) {
     const int p = tid & 127, h = tid >> 7;
-    SlotLoads cur, nxt;
-    if (total > 0) load_slots(cur, pc, ghalf, slot_cn, mpad, g0, h, static_cast<int64_t>(ta) * 128 + p);
+    for (int64_t k = 0; k < total && !sy->abort; ++k)
+      if (!produce(sy, status, st, lb, stages, loads, k, ghalf, slot_cn,
+                   g0 + static_cast<int>(k % ng), p, h))
+        break;
+  } else if (tid == kMmaWarp * 32) {
     for (int64_t k = 0; k < total && !sy->abort; ++k) {
       const int tl = static_cast<int>(k / ng), gl = static_cast<int>(k % ng);
-      if (k + 1 < total) {
-        const int tn = static_cast<int>((k + 1) / ng), gn = static_cast<int>((k + 1) % ng);
-        load_slots(nxt, pc, ghalf, slot_cn, mpad, g0 + gn, h,
-                   static_cast<int64_t>(ta + tn) * 128 + p);
-      }
-      if (gl == 0) {
-        // the Q tile of this tile into buffer tl % 2, once the MMAs of tile tl - 2 are done
-        const int b = tl & 1, use = tl >> 1;
-        if (use > 0 && !tc::mbar_wait(tc::smem_u32(&sy->qempty[b]),
-                                      static_cast<uint32_t>((use - 1) & 1), kWaitLimit)) {
-          fail_wait(sy, status, 16);
-          break;
-        }
-        const uint4* src = reinterpret_cast<const uint4*>(qtiles + static_cast<int64_t>(ta + tl) * 4096);
-        uint4* dst = reinterpret_cast<uint4*>(qb + b * kQBytes);
-        for (int w = tid; w < static_cast<int>(kQBytes / 16u); w += kProdThreads) dst[w] = __ldg(src + w);
-      }
-      const int sidx = static_cast<int>(k % stages);
-      const int64_t use = k / stages;
-      if (use > 0 &&
-          !tc::mbar_wait(tc::smem_u32(&sy->empty[sidx]), static_cast<uint32_t>((use - 1) & 1),
-                         kWaitLimit)) {
-        fail_wait(sy, status, 2);
+      if (gl == 0 && !tc::mbar_wait(tc::smem_u32(&sy->qfull[tl & 1]),
+                                    static_cast<uint32_t>((tl >> 1) & 1), kWaitLimit)) {
+        fail_wait(sy, status, 16);
         break;
       }
-      write_stage(st + static_cast<size_t>(sidx) * kStageBytes, p, h, cur);
-      tc::fence_proxy_async();
-      tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
-      cur = nxt;
-    }
-  } else if (tid == kProdThreads && ng > 0) {
-    for (int64_t k = 0; k < total && !sy->abort; ++k) {
-      const int tl = static_cast<int>(k / ng), gl = static_cast<int>(k % ng);
       const int sidx = static_cast<int>(k % stages);
-      const int64_t use = k / stages;
-      if (!tc::mbar_wait(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>(use & 1),
+      if (!tc::mbar_wait(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>((k / stages) & 1),
                          kWaitLimit)) {
         fail_wait(sy, status, 4);
         break;
@@ -379,8 +469,35 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
       tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
       if (gl == ng - 1) tc::mma_commit(tc::smem_u32(&sy->qempty[tl & 1]));
     }
+  } else if (tid == kLoadWarp * 32) {
+    // Q of tile tl waits only for the MMAs of tile tl - 2, whose stages were loaded before: the
+    // loader may block on either kind of wait without stalling the pipeline for good
+    int64_t k = 0;
+    int q_issued = 0;
+    for (; k < total && !sy->abort; ++k) {
+      const int tl = static_cast<int>(k / ng), gl = static_cast<int>(k % ng);
+      if (gl == 0) {
+        const int b = tl & 1, use = tl >> 1;
+        if (use > 0 && !tc::mbar_wait(tc::smem_u32(&sy->qempty[b]), static_cast<uint32_t>((use - 1) & 1),
+                                      kWaitLimit)) {
+          fail_wait(sy, status, 16);
+          break;
+        }
+        const uint32_t qbar = tc::smem_u32(&sy->qfull[b]);
+        bulk_expect(qbar, kQBytes);
+        bulk_copy(tc::smem_u32(qb + b * kQBytes), qtiles + static_cast<int64_t>(ta + tl) * 4096, kQBytes,
+                  qbar);
+        q_issued = tl + 1;
+      }
+      if (!load(sy, status, lb, loads, k, pc, gslots, mpad, g0 + gl, ta + tl)) break;
+    }
+    drain_loads(sy, status, loads, k);
+    for (int tl = q_issued > 2 ? q_issued - 2 : 0; tl < q_issued; ++tl)
+      if (!tc::mbar_wait(tc::smem_u32(&sy->qfull[tl & 1]), static_cast<uint32_t>((tl >> 1) & 1),
+                         kWaitLimit))
+        atomicOr(status, 128);
   }
-  if (tid == kProdThreads) {
+  if (tid == kMmaWarp * 32) {
     tc::mma_commit(tc::smem_u32(&sy->last));
     if (!tc::mbar_wait(tc::smem_u32(&sy->last), 0, kWaitLimit)) fail_wait(sy, status, 8);
   }
@@ -409,7 +526,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == kProdWarps) tc::tmem_dealloc(tmem, tmem_cols);
+  if (warp == kMmaWarp) tc::tmem_dealloc(tmem, tmem_cols);
 }
 
 // out[c][gp] = sum over streams (in order) of the partial rows + scale * add[c][gp]
@@ -655,12 +772,12 @@ namespace {
 // shared memory (at least one)
 int mult_groups_fit(const BlockShape& sh, int smem_cap) {
   const int64_t room = static_cast<int64_t>(smem_cap) - static_cast<int64_t>(sh.stages) * kStageBytes -
-                       static_cast<int64_t>(sizeof(Sync));
+                       static_cast<int64_t>(sh.loads) * kLoadBytes - static_cast<int64_t>(sizeof(Sync));
   return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(sh.mult_groups, room / kCoefBytes)));
 }
 size_t mult_smem(const BlockShape& sh, int groups) {
-  return static_cast<size_t>(sh.stages) * kStageBytes + static_cast<size_t>(groups) * kCoefBytes +
-         sizeof(Sync);
+  return static_cast<size_t>(sh.stages) * kStageBytes + static_cast<size_t>(sh.loads) * kLoadBytes +
+         static_cast<size_t>(groups) * kCoefBytes + sizeof(Sync);
 }
 int device_smem_cap() {
   int dev = 0, cap = 0;
@@ -672,7 +789,8 @@ int device_smem_cap() {
   return cap;
 }
 size_t multt_smem(const BlockShape& sh) {
-  return static_cast<size_t>(sh.stages) * kStageBytes + 2 * kQBytes + sizeof(Sync);
+  return static_cast<size_t>(sh.stages) * kStageBytes + static_cast<size_t>(sh.loads) * kLoadBytes +
+         2 * kQBytes + sizeof(Sync);
 }
 uint32_t tmem_cols_for(int accumulators) {
   uint32_t c = 32;
@@ -685,14 +803,15 @@ unsigned grid_for(int64_t n, int num_sms) {
 }  // namespace
 
 void block_free(BlockPlan* b) {
-  void* ptrs[] = {b->row_gp, b->gp_row, b->ghalf, b->slot_cn, b->pc,
+  void* ptrs[] = {b->row_gp, b->gp_row, b->ghalf, b->gslots, b->slot_cn, b->pc,
                   b->coef,   b->qtiles, b->part,  b->status};
   for (void* q : ptrs) dev_free(q, b->stream);
   *b = BlockPlan{};
 }
 
 bool block_shape_ok(const BlockShape& sh, int smem_cap) {
-  return sh.stages >= 2 && sh.stages <= kMaxStages && sh.mult_tiles >= 1 && sh.mult_tiles <= 16 &&
+  return sh.stages >= 2 && sh.stages <= kMaxStages && sh.loads >= 2 && sh.loads <= kMaxLoads &&
+         sh.mult_tiles >= 1 && sh.mult_tiles <= 16 &&
          sh.mult_groups >= 1 && sh.multt_groups >= 1 && sh.multt_groups <= 16 &&
          mult_smem(sh, mult_groups_fit(sh, smem_cap)) <= static_cast<size_t>(smem_cap) &&
          multt_smem(sh) <= static_cast<size_t>(smem_cap);
@@ -748,6 +867,7 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
   for (int64_t g = 0; g < sub.n; ++g) pos_gp[sub.h_pos[g]] = static_cast<int>(g);
   std::vector<int> row_gp(static_cast<size_t>(rows), -1), gp_row(static_cast<size_t>(sub.n), 0);
   std::vector<int4> ghalf(static_cast<size_t>(n_groups) * 2);
+  std::vector<int2> gslots(static_cast<size_t>(n_groups));
   for (int g = 0; g < n_groups; ++g) {
     int cnt[2] = {0, 0};
     uint32_t idx[2][2] = {{0u, 0u}, {0u, 0u}};
@@ -769,6 +889,7 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
         }
       }
     }
+    gslots[g] = make_int2(group_first[g], group_first[g + 1] - group_first[g]);
     for (int h = 0; h < 2; ++h)
       ghalf[2 * g + h] = make_int4(static_cast<int>(idx[h][0]), static_cast<int>(idx[h][1]),
                                    cnt[h], group_first[g]);
@@ -787,6 +908,7 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
   };
   bool ok = alloc(&b->row_gp, sizeof(int) * rows) && alloc(&b->gp_row, sizeof(int) * sub.n) &&
             alloc(&b->ghalf, sizeof(int4) * ghalf.size()) &&
+            alloc(&b->gslots, sizeof(int2) * gslots.size()) &&
             alloc(&b->slot_cn, sizeof(uint16_t) * slot_cn.size()) &&
             alloc(&d_slot_sub, sizeof(int) * slot_sub.size()) &&
             alloc(&b->pc, sizeof(uint32_t) * static_cast<size_t>(b->n_slots) * mpad) &&
@@ -797,6 +919,7 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
   ok = ok && put(b->row_gp, row_gp.data(), sizeof(int) * rows) &&
        put(b->gp_row, gp_row.data(), sizeof(int) * sub.n) &&
        put(b->ghalf, ghalf.data(), sizeof(int4) * ghalf.size()) &&
+       put(b->gslots, gslots.data(), sizeof(int2) * gslots.size()) &&
        put(b->slot_cn, slot_cn.data(), sizeof(uint16_t) * slot_cn.size()) &&
        put(d_slot_sub, slot_sub.data(), sizeof(int) * slot_sub.size()) &&
        cudaMemsetAsync(b->status, 0, sizeof(int), s) == cudaSuccess;
@@ -838,8 +961,8 @@ cudaError_t block_mult(BlockPlan& b, cudaStream_t s, const double* p, int64_t np
   const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
   const unsigned ctas = static_cast<unsigned>(cdiv(n_tiles, sh.mult_tiles));
   block_mult_kernel<<<ctas, kBlockThreads, smem, s>>>(
-      b.pc, b.ghalf, b.slot_cn, b.coef, b.n_groups, b.mpad, b.m, n_tiles, sh.mult_tiles, gpp,
-      sh.stages, cols, b.qtiles, out64, b.status);
+      b.pc, b.ghalf, b.gslots, b.slot_cn, b.coef, b.n_groups, b.mpad, b.m, n_tiles, sh.mult_tiles,
+      gpp, sh.stages, sh.loads, cols, b.qtiles, out64, b.status);
   return cudaGetLastError();
 }
 
@@ -863,8 +986,8 @@ cudaError_t block_multt(BlockPlan& b, cudaStream_t s, const double* v, int64_t n
   const int streams = std::min(b.part_streams, multt_streams(b, num_sms));
   const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
   block_multt_kernel<<<static_cast<unsigned>(passes * streams), kBlockThreads, smem, s>>>(
-      b.pc, b.ghalf, b.slot_cn, b.qtiles, b.n_groups, b.mpad, n_tiles, sh.multt_groups, streams,
-      sh.stages, cols, b.rows, b.part, b.status);
+      b.pc, b.ghalf, b.gslots, b.slot_cn, b.qtiles, b.n_groups, b.mpad, n_tiles, sh.multt_groups,
+      streams, sh.stages, sh.loads, cols, b.rows, b.part, b.status);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   block_finish_kernel<<<grid_for(npad * kBlockRhs, num_sms), 256, 0, s>>>(

@@ -37,7 +37,8 @@ struct BlockShape {
   int mult_tiles = 8;      // tiles per mult CTA (their accumulators stay in tensor memory)
   int mult_groups = 16;    // groups whose coefficient rows a mult CTA holds in shared memory
   int multt_groups = 16;   // groups (accumulators) per multT CTA
-  int stages = 3;          // shared-memory stages of E in flight
+  int stages = 2;          // shared-memory stages of E in flight
+  int loads = 6;           // stages of packed products in flight (bulk copies ahead of use)
 };
 
 struct BlockPlan {
@@ -50,6 +51,7 @@ struct BlockPlan {
   int* row_gp = nullptr;      // [rows] grid point of a row, -1 when none
   int* gp_row = nullptr;      // [n] row of a grid point
   int4* ghalf = nullptr;      // [n_groups * 2] slots of each half group (8 byte indices, count, first slot)
+  int2* gslots = nullptr;     // [n_groups] first slot and slot count of each group
   uint16_t* slot_cn = nullptr;  // [n_slots] chunk offset in its group | chunk count << 8
   uint32_t* pc = nullptr;     // [n_slots][mpad] BF16 product | cell << 16
   uint16_t* coef = nullptr;   // [n_groups][4096] coefficient rows, BF16, operand layout

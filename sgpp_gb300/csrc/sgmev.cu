@@ -1207,9 +1207,9 @@ static int apply_shape_params(sgmev_op* op, const char* params_json) {
   }
   BlockShape sh = op->blk_shape;
   const char* knobs[] = {"block_mult_tiles", "block_mult_groups", "block_multt_groups",
-                         "block_stages"};
-  int* fields[] = {&sh.mult_tiles, &sh.mult_groups, &sh.multt_groups, &sh.stages};
-  for (int k = 0; k < 4; ++k) {
+                         "block_stages", "block_loads"};
+  int* fields[] = {&sh.mult_tiles, &sh.mult_groups, &sh.multt_groups, &sh.stages, &sh.loads};
+  for (int k = 0; k < 5; ++k) {
     const std::string v = json_string(params_json, knobs[k]);
     if (v.empty()) continue;
     char* end = nullptr;
@@ -1491,7 +1491,7 @@ SGMEV_API int sgmev_set_params(sgmev_op* op, const char* params_json) {
   SGMEV_TRY(check_op(op));
   if (!params_json) return SGMEV_OK;
   static const char* allowed[] = {"multt_batch", "block_mult_tiles", "block_mult_groups",
-                                  "block_multt_groups", "block_stages"};
+                                  "block_multt_groups", "block_stages", "block_loads"};
   // every key must be a launch-shape knob
   for (const char* c = params_json; (c = std::strchr(c, '"')) != nullptr;) {
     const char* e = std::strchr(c + 1, '"');
@@ -2121,6 +2121,7 @@ static int fit_block_common(sgmev_op* op, const double* y, bool y_dev, double la
   double* part_a = t + vec;
   double* part_b = part_a + parts;
   double* sc = part_b + parts;
+  SGMEV_CUDA(cudaMemsetAsync(sc, 0, sizeof(double) * kBlockScalars, op->stream));
   SGMEV_TRY(begin_timed(op));
   // b_k = B^T y_k with the FP64-accurate df64 products (generateb per column)
   for (int k = 0; k < K; ++k) {
@@ -2180,6 +2181,7 @@ static int fit_block_common(sgmev_op* op, const double* y, bool y_dev, double la
     SGMEV_CUDA(block_cg_init(op->stream, r, d, e, np, part_a, sc));
     op->launches += 2;
     int cur = 0;
+    int64_t steps = 0;
     while (total_it < max_iterations) {
       SGMEV_CUDA(cudaMemcpyAsync(host.data(), sc + kScDelta + cur * K, sizeof(double) * K,
                                  cudaMemcpyDeviceToHost, op->stream));
@@ -2209,11 +2211,13 @@ static int fit_block_common(sgmev_op* op, const double* y, bool y_dev, double la
       op->launches += 3;
       cur ^= 1;
       ++total_it;
+      ++steps;
     }
     axpy_kernel<<<vec_blocks(static_cast<int64_t>(vec)), 256, 0, op->stream>>>(
         static_cast<int64_t>(vec), 1.0, e, x);
     op->launches += 1;
     SGMEV_TRY(block_check(op));
+    if (steps == 0) break;  // no column could take a step: further refinement cannot move
   }
   for (int k = 0; k < K; ++k)
     if (op->n > 0)

@@ -107,6 +107,17 @@ __device__ __forceinline__ bool mbar_test(uint32_t saddr, uint32_t parity) {
       : "memory");
   return done != 0;
 }
+// non-blocking test of the same (never suspends the thread)
+__device__ __forceinline__ bool mbar_poll(uint32_t saddr, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(saddr), "r"(parity)
+      : "memory");
+  return done != 0;
+}
 // Wait for the phase of the given parity to complete, at most `limit` polls (each try_wait
 // suspends the thread for a while). Returns false when the limit ran out.
 __device__ __forceinline__ bool mbar_wait(uint32_t saddr, uint32_t parity, uint32_t limit) {
