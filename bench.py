@@ -757,6 +757,27 @@ def run_block(args):
     return 0
 
 
+def run_module_workload(args):
+    """The other configurations' benchmarks, each printing its own JSON line: the adaptive-grid
+    loop (d=8 level 4, M=2^19, 6 rounds of 40 points), the batched mix (96 problems x 16 targets
+    on block fits) and the serving loop (Poisson arrivals, 200 req/s for 60 s)."""
+    argv = {"adaptive": ["--engine", "fitter"],
+            "batched": ["--engine", "block", "--problems", "96", "--rhs", "16",
+                        "--max-work", "1e12"],
+            "serving": ["--rate", "200", "--duration", "60", "--max-work", "1e12"]}[args.workload]
+    module = {"adaptive": "sgpp_gb300.adaptive", "batched": "sgpp_gb300.batch_bench",
+              "serving": "sgpp_gb300.serving"}[args.workload]
+    import importlib
+
+    mod = importlib.import_module(module)
+    saved = sys.argv
+    sys.argv = [module] + argv
+    try:
+        return mod.main()
+    finally:
+        sys.argv = saved
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -778,8 +799,12 @@ def main():
                     help="timed launches of the dense FP32 and FP64 mult kernels (0: skip)")
     ap.add_argument("--inner-tol", type=float, default=None,
                     help="inner tolerance of the mixed fits (library default when omitted)")
-    ap.add_argument("--workload", default="regression", choices=["regression", "block"],
-                    help="block: 16 fits sharing the data (tensor-core block fits)")
+    ap.add_argument("--workload", default="regression",
+                    choices=["regression", "block", "adaptive", "batched", "serving"],
+                    help="block: 16 fits sharing the data (tensor-core block fits); adaptive: "
+                         "the adaptive-grid loop (sgpp_gb300.adaptive); batched: 96 problems x "
+                         "16 targets (sgpp_gb300.batch_bench --engine block); serving: Poisson "
+                         "arrivals at 200 req/s (sgpp_gb300.serving)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="pick launch shapes with sgpp_gb300.autotune before timing (cached)")
     ap.add_argument("--param", action="append", default=[], metavar="KEY=VALUE",
@@ -793,6 +818,8 @@ def main():
         return count_iterations(args)
     if args.workload == "block":
         return run_block(args)
+    if args.workload in ("adaptive", "batched", "serving"):
+        return run_module_workload(args)
     return run_ours(args)
 
 

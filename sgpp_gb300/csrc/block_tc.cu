@@ -40,8 +40,8 @@ constexpr uint32_t kCoefBytes = 4096u * 2u;         // 128 rows x 32 columns of 
 constexpr uint32_t kQBytes = 4096u * 2u;            // 128 points x 32 columns of BF16
 constexpr uint32_t kSlotRow = 128u * 4u;            // one slot's packed words of a tile
 constexpr uint32_t kLoadBytes = 16u * kSlotRow;     // a group has at most 16 slots
-constexpr uint32_t kWaitLimit = 1u << 22;           // polls of one bounded wait
-constexpr uint32_t kPollLimit = 1u << 25;           // idle rounds of the loader's polling loop
+constexpr uint64_t kWaitNs = 2000000000ull;         // a bounded wait gives up after 2 s
+constexpr uint64_t kPollNs = 4000000000ull;         // the loader's idle polling, after 4 s
 constexpr int kMaxStages = 6;
 constexpr int kMaxLoads = 12;
 // core-matrix strides of the operands: 128 bytes between neighbouring core matrices along the
@@ -113,54 +113,44 @@ __device__ __forceinline__ void load_stage(unsigned char* buf, uint32_t mbar,
 }
 
 // ---- producer: one stage of E ----------------------------------------------------------------
-// The thread's slots for a stage: up to 8 subspaces overlapping its half of the group.
-struct SlotLoads {
-  uint32_t w[8];   // packed product | cell << 16
-  uint32_t cn[8];  // chunk offset | chunk count << 8
-  int count;
+// Each group carries a 16-byte chunk header: byte q describes chunk q of the group — the slot
+// (subspace) it belongs to, as an index among the group's slots (high nibble), and which of the
+// slot's chunks it is (low nibble); 0xFF marks a chunk no slot uses. Thread (p, h) writes chunks
+// 8h .. 8h + 7 of point p: the chunk holds the point's product at element c % 8 when the point's
+// cell c in that subspace lies in it (c / 8 == the slot's chunk), zeros otherwise.
+struct ChunkWords {
+  uint32_t w[8];  // packed product | cell << 16 of the chunk's slot, 0 for an unused chunk
+  uint32_t hdr;   // header bytes of the thread's chunks 0..3
+  uint32_t hdr2;  // and 4..7
 };
 
-// the thread's words from the stage's load buffer ([slot in group][128 points])
-__device__ __forceinline__ void read_slots(SlotLoads& L, const uint32_t* lbuf,
-                                           const int4* __restrict__ ghalf,
-                                           const uint16_t* __restrict__ slot_cn, int group, int h,
-                                           int p) {
-  const int4 gh = __ldg(ghalf + 2 * group + h);
-  L.count = gh.z;
-  const uint32_t idx[2] = {static_cast<uint32_t>(gh.x), static_cast<uint32_t>(gh.y)};
+__device__ __forceinline__ void read_chunks(ChunkWords& C, const uint32_t* lbuf,
+                                            const uint4* __restrict__ gheader, int group, int h,
+                                            int p) {
+  const uint4 hd = __ldg(gheader + group);
+  C.hdr = h ? hd.z : hd.x;
+  C.hdr2 = h ? hd.w : hd.y;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    if (i < L.count) {
-      const int local = static_cast<int>((idx[i >> 2] >> (8 * (i & 3))) & 0xFFu);
-      L.w[i] = lbuf[local * 128 + p];
-      L.cn[i] = __ldg(slot_cn + gh.w + local);
-    } else {
-      L.w[i] = 0u;
-      L.cn[i] = 0u;
-    }
+    const uint32_t byte = ((i < 4 ? C.hdr : C.hdr2) >> (8 * (i & 3))) & 0xFFu;
+    C.w[i] = byte == 0xFFu ? 0u : lbuf[(byte >> 4) * 128 + p];
   }
 }
 
-// rows of point p, chunks [8h, 8h + 8) of the group, into the stage
-__device__ __forceinline__ void write_stage(unsigned char* stage, int p, int h,
-                                            const SlotLoads& L) {
-  unsigned char* base = stage + (p >> 3) * 2048 + (p & 7) * 16;
-  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+__device__ __forceinline__ void write_chunks(unsigned char* stage, int p, int h,
+                                             const ChunkWords& C) {
+  unsigned char* base = stage + (p >> 3) * 2048 + (p & 7) * 16 + 8 * h * 128;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    if (i < L.count) {
-      const uint32_t w = L.w[i];
-      const int co = static_cast<int>(L.cn[i] & 0xFFu), nch = static_cast<int>(L.cn[i] >> 8);
-      const int c = static_cast<int>(w >> 16);
-      const int q = co + (c >> 3), e = c & 7;
-      const uint32_t val = (w & 0xFFFFu) << ((e & 1) * 16);
-      const int wd = e >> 1;
-      const uint4 one = make_uint4(wd == 0 ? val : 0u, wd == 1 ? val : 0u, wd == 2 ? val : 0u,
-                                   wd == 3 ? val : 0u);
-      const int lo = max(co, 8 * h), hi = min(co + nch, 8 * h + 8);
-      for (int qq = lo; qq < hi; ++qq)
-        *reinterpret_cast<uint4*>(base + qq * 128) = qq == q ? one : zero;
-    }
+    const uint32_t byte = ((i < 4 ? C.hdr : C.hdr2) >> (8 * (i & 3))) & 0xFFu;
+    if (byte == 0xFFu) continue;  // unused chunk: its coefficient rows are zero
+    const uint32_t w = C.w[i];
+    const uint32_t c = w >> 16;
+    const uint32_t v = (c >> 3) == (byte & 0xFu) ? (w & 0xFFFFu) : 0u;
+    const uint32_t val = v << ((c & 1u) * 16u);
+    const uint32_t wd = (c >> 1) & 3u;
+    *reinterpret_cast<uint4*>(base + i * 128) =
+        make_uint4(wd == 0 ? val : 0u, wd == 1 ? val : 0u, wd == 2 ? val : 0u, wd == 3 ? val : 0u);
   }
 }
 
@@ -168,27 +158,26 @@ __device__ __forceinline__ void write_stage(unsigned char* stage, int p, int h,
 // wait for the E stage to be free, write it, mark it full. False when a wait ran out.
 __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st,
                                         unsigned char* lb, int stages, int loads, int64_t i,
-                                        const int4* __restrict__ ghalf,
-                                        const uint16_t* __restrict__ slot_cn, int group, int p,
+                                        const uint4* __restrict__ gheader, int group, int p,
                                         int h) {
   const int b = static_cast<int>(i % loads);
-  if (!tc::mbar_wait(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((i / loads) & 1),
-                     kWaitLimit)) {
+  if (!tc::mbar_wait_ns(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((i / loads) & 1),
+                        kWaitNs)) {
     fail_wait(sy, status, 32);
     return false;
   }
-  SlotLoads L;
-  read_slots(L, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes), ghalf,
-             slot_cn, group, h, p);
+  ChunkWords C;
+  read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes),
+              gheader, group, h, p);
   tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
   const int sidx = static_cast<int>(i % stages);
   const int64_t use = i / stages;
-  if (use > 0 && !tc::mbar_wait(tc::smem_u32(&sy->empty[sidx]),
-                                static_cast<uint32_t>((use - 1) & 1), kWaitLimit)) {
+  if (use > 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->empty[sidx]),
+                                   static_cast<uint32_t>((use - 1) & 1), kWaitNs)) {
     fail_wait(sy, status, 2);
     return false;
   }
-  write_stage(st + static_cast<size_t>(sidx) * kStageBytes, p, h, L);
+  write_chunks(st + static_cast<size_t>(sidx) * kStageBytes, p, h, C);
   tc::fence_proxy_async();
   tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
   return true;
@@ -201,8 +190,8 @@ __device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, i
                                      int64_t tile) {
   const int b = static_cast<int>(i % loads);
   const int64_t use = i / loads;
-  if (use > 0 && !tc::mbar_wait(tc::smem_u32(&sy->lempty[b]),
-                                static_cast<uint32_t>((use - 1) & 1), kWaitLimit)) {
+  if (use > 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->lempty[b]),
+                                static_cast<uint32_t>((use - 1) & 1), kWaitNs)) {
     fail_wait(sy, status, 64);
     return false;
   }
@@ -216,8 +205,8 @@ __device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, i
 __device__ __forceinline__ void drain_loads(Sync* sy, int* status, int loads, int64_t issued) {
   for (int64_t i = issued > loads ? issued - loads : 0; i < issued; ++i) {
     const int b = static_cast<int>(i % loads);
-    if (!tc::mbar_wait(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((i / loads) & 1),
-                       kWaitLimit))
+    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((i / loads) & 1),
+                       kWaitNs))
       atomicOr(status, 128);
   }
 }
@@ -261,9 +250,8 @@ __device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int sta
 // into shared memory once the previous pass's MMAs have completed. Output: the BF16 Q tiles
 // (operand layout of block_multt) and optionally Q in FP64.
 __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
-    const uint32_t* __restrict__ pc, const int4* __restrict__ ghalf,
-    const int2* __restrict__ gslots, const uint16_t* __restrict__ slot_cn,
-    const uint16_t* __restrict__ coef, int n_groups, int64_t mpad, int64_t m, int n_tiles,
+    const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
+    const int2* __restrict__ gslots, const uint16_t* __restrict__ coef, int n_groups, int64_t mpad, int64_t m, int n_tiles,
     int tiles, int gpp, int stages, int loads, uint32_t tmem_cols, uint16_t* __restrict__ qtiles,
     double* __restrict__ out64, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -285,21 +273,21 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
     for (int pass = 0; pass < passes && !sy->abort; ++pass) {
       const int g0 = pass * gpp, ng = min(n_groups, g0 + gpp) - g0;
       for (int k = 0; k < nt * ng; ++k, ++i)
-        if (!produce(sy, status, st, lb, stages, loads, i, ghalf, slot_cn, g0 + k % ng, p, h)) break;
+        if (!produce(sy, status, st, lb, stages, loads, i, gheader, g0 + k % ng, p, h)) break;
     }
   } else if (tid == kMmaWarp * 32) {
     int64_t i = 0;
     for (int pass = 0; pass < passes && !sy->abort; ++pass) {
       const int g0 = pass * gpp, ng = min(n_groups, g0 + gpp) - g0;
-      if (!tc::mbar_wait(tc::smem_u32(&sy->cfull), static_cast<uint32_t>(pass & 1), kWaitLimit)) {
+      if (!tc::mbar_wait_ns(tc::smem_u32(&sy->cfull), static_cast<uint32_t>(pass & 1), kWaitNs)) {
         fail_wait(sy, status, 1);
         break;
       }
       for (int k = 0; k < nt * ng; ++k, ++i) {
         const int u = k / ng, gl = k % ng;
         const int sidx = static_cast<int>(i % stages);
-        if (!tc::mbar_wait(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>((i / stages) & 1),
-                           kWaitLimit)) {
+        if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>((i / stages) & 1),
+                           kWaitNs)) {
           fail_wait(sy, status, 4);
           break;
         }
@@ -334,7 +322,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
     int64_t next = 0;                   // next stage to load
     int lpass = 0, lk = 0;              // its pass and index within the pass
     int lng = min(n_groups, gpp);       // groups of that pass
-    uint32_t idle = 0;
+    uint64_t idle_since = 0;
     while (!sy->abort && (lpass < passes || coef_next < passes)) {
       bool progress = false;
       if (coef_next < passes &&
@@ -357,21 +345,26 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
           progress = true;
         }
       }
-      idle = progress ? 0u : idle + 1u;
-      if (!progress) __nanosleep(20);  // leave the issue slots to the producers
-      if (idle > kPollLimit) {
+      if (progress) {
+        idle_since = 0;
+        continue;
+      }
+      __nanosleep(100);  // leave the issue slots to the producers
+      const uint64_t now = tc::globaltimer_ns();
+      if (idle_since == 0) idle_since = now;
+      if (now - idle_since > kPollNs) {
         fail_wait(sy, status, 64);
         break;
       }
     }
     drain_loads(sy, status, loads, next);
-    if (!tc::mbar_wait(tc::smem_u32(&sy->cfull), static_cast<uint32_t>((coef_next - 1) & 1), kWaitLimit))
+    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->cfull), static_cast<uint32_t>((coef_next - 1) & 1), kWaitNs))
       atomicOr(status, 128);
   }
   // every MMA of the CTA has completed once the last commit has
   if (tid == kMmaWarp * 32) {
     tc::mma_commit(tc::smem_u32(&sy->last));
-    if (!tc::mbar_wait(tc::smem_u32(&sy->last), 0, kWaitLimit)) fail_wait(sy, status, 8);
+    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->last), 0, kWaitNs)) fail_wait(sy, status, 8);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -418,9 +411,8 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
 constexpr uint32_t kMnA_LBO = 2048, kMnA_SBO = 128;
 
 __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
-    const uint32_t* __restrict__ pc, const int4* __restrict__ ghalf,
-    const int2* __restrict__ gslots, const uint16_t* __restrict__ slot_cn,
-    const uint16_t* __restrict__ qtiles, int n_groups, int64_t mpad, int n_tiles, int gpc,
+    const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
+    const int2* __restrict__ gslots, const uint16_t* __restrict__ qtiles, int n_groups, int64_t mpad, int n_tiles, int gpc,
     int streams, int stages, int loads, uint32_t tmem_cols, int64_t rows,
     double* __restrict__ part, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -441,20 +433,20 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
   if (tid < kProdThreads) {
     const int p = tid & 127, h = tid >> 7;
     for (int64_t k = 0; k < total && !sy->abort; ++k)
-      if (!produce(sy, status, st, lb, stages, loads, k, ghalf, slot_cn,
-                   g0 + static_cast<int>(k % ng), p, h))
+      if (!produce(sy, status, st, lb, stages, loads, k, gheader, g0 + static_cast<int>(k % ng), p,
+                   h))
         break;
   } else if (tid == kMmaWarp * 32) {
     for (int64_t k = 0; k < total && !sy->abort; ++k) {
       const int tl = static_cast<int>(k / ng), gl = static_cast<int>(k % ng);
-      if (gl == 0 && !tc::mbar_wait(tc::smem_u32(&sy->qfull[tl & 1]),
-                                    static_cast<uint32_t>((tl >> 1) & 1), kWaitLimit)) {
+      if (gl == 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]),
+                                    static_cast<uint32_t>((tl >> 1) & 1), kWaitNs)) {
         fail_wait(sy, status, 16);
         break;
       }
       const int sidx = static_cast<int>(k % stages);
-      if (!tc::mbar_wait(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>((k / stages) & 1),
-                         kWaitLimit)) {
+      if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>((k / stages) & 1),
+                         kWaitNs)) {
         fail_wait(sy, status, 4);
         break;
       }
@@ -478,8 +470,8 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
       const int tl = static_cast<int>(k / ng), gl = static_cast<int>(k % ng);
       if (gl == 0) {
         const int b = tl & 1, use = tl >> 1;
-        if (use > 0 && !tc::mbar_wait(tc::smem_u32(&sy->qempty[b]), static_cast<uint32_t>((use - 1) & 1),
-                                      kWaitLimit)) {
+        if (use > 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qempty[b]), static_cast<uint32_t>((use - 1) & 1),
+                                      kWaitNs)) {
           fail_wait(sy, status, 16);
           break;
         }
@@ -493,13 +485,13 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
     }
     drain_loads(sy, status, loads, k);
     for (int tl = q_issued > 2 ? q_issued - 2 : 0; tl < q_issued; ++tl)
-      if (!tc::mbar_wait(tc::smem_u32(&sy->qfull[tl & 1]), static_cast<uint32_t>((tl >> 1) & 1),
-                         kWaitLimit))
+      if (!tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]), static_cast<uint32_t>((tl >> 1) & 1),
+                         kWaitNs))
         atomicOr(status, 128);
   }
   if (tid == kMmaWarp * 32) {
     tc::mma_commit(tc::smem_u32(&sy->last));
-    if (!tc::mbar_wait(tc::smem_u32(&sy->last), 0, kWaitLimit)) fail_wait(sy, status, 8);
+    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->last), 0, kWaitNs)) fail_wait(sy, status, 8);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -803,7 +795,7 @@ unsigned grid_for(int64_t n, int num_sms) {
 }  // namespace
 
 void block_free(BlockPlan* b) {
-  void* ptrs[] = {b->row_gp, b->gp_row, b->ghalf, b->gslots, b->slot_cn, b->pc,
+  void* ptrs[] = {b->row_gp, b->gp_row, b->gheader, b->gslots, b->pc,
                   b->coef,   b->qtiles, b->part,  b->status};
   for (void* q : ptrs) dev_free(q, b->stream);
   *b = BlockPlan{};
@@ -866,11 +858,11 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
   std::vector<int> pos_gp(static_cast<size_t>(sub.total), -1);
   for (int64_t g = 0; g < sub.n; ++g) pos_gp[sub.h_pos[g]] = static_cast<int>(g);
   std::vector<int> row_gp(static_cast<size_t>(rows), -1), gp_row(static_cast<size_t>(sub.n), 0);
-  std::vector<int4> ghalf(static_cast<size_t>(n_groups) * 2);
+  std::vector<uint4> gheader(static_cast<size_t>(n_groups));
   std::vector<int2> gslots(static_cast<size_t>(n_groups));
   for (int g = 0; g < n_groups; ++g) {
-    int cnt[2] = {0, 0};
-    uint32_t idx[2][2] = {{0u, 0u}, {0u, 0u}};
+    uint8_t bytes[16];
+    std::memset(bytes, 0xFF, sizeof(bytes));
     for (int sl = group_first[g]; sl < group_first[g + 1]; ++sl) {
       const int sidx = slot_sub[sl];
       const int co = slot_cn[sl] & 0xFF, nch = slot_cn[sl] >> 8;
@@ -881,18 +873,11 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
         row_gp[r] = gp;
         if (gp >= 0) gp_row[gp] = static_cast<int>(r);
       }
-      for (int h = 0; h < 2; ++h) {
-        if (co < 8 * h + 8 && co + nch > 8 * h) {
-          const uint32_t local = static_cast<uint32_t>(sl - group_first[g]);
-          idx[h][cnt[h] >> 2] |= local << (8 * (cnt[h] & 3));
-          ++cnt[h];
-        }
-      }
+      for (int q = co; q < co + nch; ++q)
+        bytes[q] = static_cast<uint8_t>(((sl - group_first[g]) << 4) | (q - co));
     }
+    std::memcpy(&gheader[g], bytes, sizeof(bytes));
     gslots[g] = make_int2(group_first[g], group_first[g + 1] - group_first[g]);
-    for (int h = 0; h < 2; ++h)
-      ghalf[2 * g + h] = make_int4(static_cast<int>(idx[h][0]), static_cast<int>(idx[h][1]),
-                                   cnt[h], group_first[g]);
   }
   b->n_groups = n_groups;
   b->n_slots = static_cast<int>(slot_sub.size());
@@ -907,9 +892,8 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
   };
   bool ok = alloc(&b->row_gp, sizeof(int) * rows) && alloc(&b->gp_row, sizeof(int) * sub.n) &&
-            alloc(&b->ghalf, sizeof(int4) * ghalf.size()) &&
+            alloc(&b->gheader, sizeof(uint4) * gheader.size()) &&
             alloc(&b->gslots, sizeof(int2) * gslots.size()) &&
-            alloc(&b->slot_cn, sizeof(uint16_t) * slot_cn.size()) &&
             alloc(&d_slot_sub, sizeof(int) * slot_sub.size()) &&
             alloc(&b->pc, sizeof(uint32_t) * static_cast<size_t>(b->n_slots) * mpad) &&
             alloc(&b->coef, kCoefBytes * static_cast<size_t>(n_groups)) &&
@@ -918,9 +902,8 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
             alloc(&b->status, sizeof(int));
   ok = ok && put(b->row_gp, row_gp.data(), sizeof(int) * rows) &&
        put(b->gp_row, gp_row.data(), sizeof(int) * sub.n) &&
-       put(b->ghalf, ghalf.data(), sizeof(int4) * ghalf.size()) &&
+       put(b->gheader, gheader.data(), sizeof(uint4) * gheader.size()) &&
        put(b->gslots, gslots.data(), sizeof(int2) * gslots.size()) &&
-       put(b->slot_cn, slot_cn.data(), sizeof(uint16_t) * slot_cn.size()) &&
        put(d_slot_sub, slot_sub.data(), sizeof(int) * slot_sub.size()) &&
        cudaMemsetAsync(b->status, 0, sizeof(int), s) == cudaSuccess;
   if (ok) {
@@ -961,7 +944,7 @@ cudaError_t block_mult(BlockPlan& b, cudaStream_t s, const double* p, int64_t np
   const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
   const unsigned ctas = static_cast<unsigned>(cdiv(n_tiles, sh.mult_tiles));
   block_mult_kernel<<<ctas, kBlockThreads, smem, s>>>(
-      b.pc, b.ghalf, b.gslots, b.slot_cn, b.coef, b.n_groups, b.mpad, b.m, n_tiles, sh.mult_tiles,
+      b.pc, b.gheader, b.gslots, b.coef, b.n_groups, b.mpad, b.m, n_tiles, sh.mult_tiles,
       gpp, sh.stages, sh.loads, cols, b.qtiles, out64, b.status);
   return cudaGetLastError();
 }
@@ -986,7 +969,7 @@ cudaError_t block_multt(BlockPlan& b, cudaStream_t s, const double* v, int64_t n
   const int streams = std::min(b.part_streams, multt_streams(b, num_sms));
   const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
   block_multt_kernel<<<static_cast<unsigned>(passes * streams), kBlockThreads, smem, s>>>(
-      b.pc, b.ghalf, b.gslots, b.slot_cn, b.qtiles, b.n_groups, b.mpad, n_tiles, sh.multt_groups,
+      b.pc, b.gheader, b.gslots, b.qtiles, b.n_groups, b.mpad, n_tiles, sh.multt_groups,
       streams, sh.stages, sh.loads, cols, b.rows, b.part, b.status);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

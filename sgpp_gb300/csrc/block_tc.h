@@ -50,9 +50,9 @@ struct BlockPlan {
   int64_t m = 0;
   int* row_gp = nullptr;      // [rows] grid point of a row, -1 when none
   int* gp_row = nullptr;      // [n] row of a grid point
-  int4* ghalf = nullptr;      // [n_groups * 2] slots of each half group (8 byte indices, count, first slot)
+  uint4* gheader = nullptr;   // [n_groups] chunk headers: per chunk, its slot in the group << 4 | which
+                              // of the slot's chunks it is (0xFF: unused)
   int2* gslots = nullptr;     // [n_groups] first slot and slot count of each group
-  uint16_t* slot_cn = nullptr;  // [n_slots] chunk offset in its group | chunk count << 8
   uint32_t* pc = nullptr;     // [n_slots][mpad] BF16 product | cell << 16
   uint16_t* coef = nullptr;   // [n_groups][4096] coefficient rows, BF16, operand layout
   uint16_t* qtiles = nullptr; // [mpad / 128][4096] Q tiles, BF16, operand layout

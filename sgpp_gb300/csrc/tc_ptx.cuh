@@ -126,5 +126,33 @@ __device__ __forceinline__ bool mbar_wait(uint32_t saddr, uint32_t parity, uint3
   return false;
 }
 
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// try_wait that may suspend the thread for up to `hint_ns` while the phase is incomplete, so that
+// waiting threads do not take issue slots from working ones
+__device__ __forceinline__ bool mbar_test_suspend(uint32_t saddr, uint32_t parity, uint32_t hint_ns) {
+  uint32_t done;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(saddr), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return done != 0;
+}
+// Wait for the phase of the given parity to complete, for at most `limit_ns` nanoseconds of the
+// global timer. Returns false when the time ran out.
+__device__ __forceinline__ bool mbar_wait_ns(uint32_t saddr, uint32_t parity, uint64_t limit_ns) {
+  if (mbar_test(saddr, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (;;) {
+    if (mbar_test_suspend(saddr, parity, 20000u)) return true;
+    if (globaltimer_ns() - t0 > limit_ns) return false;
+  }
+}
+
 }  // namespace tc
 }  // namespace sgmev
