@@ -161,25 +161,33 @@ __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st
                                         const uint4* __restrict__ gheader, int group, int p,
                                         int h) {
   const int b = static_cast<int>(i % loads);
-  if (!tc::mbar_wait_ns(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((i / loads) & 1),
-                        kWaitNs)) {
+  // the warp's lanes decide together (a lane that gave up alone would leave the others waiting
+  // at the warp's synchronisation below)
+  if (!__all_sync(0xffffffffu, tc::mbar_wait_ns(tc::smem_u32(&sy->lfull[b]),
+                                                static_cast<uint32_t>((i / loads) & 1), kWaitNs))) {
     fail_wait(sy, status, 32);
     return false;
   }
   ChunkWords C;
   read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes),
               gheader, group, h, p);
-  tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
+  // one arrival per warp (the barriers count warps): 256 arrivals on one word per stage
+  // serialised on the shared-memory atomics
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
   const int sidx = static_cast<int>(i % stages);
   const int64_t use = i / stages;
-  if (use > 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->empty[sidx]),
-                                   static_cast<uint32_t>((use - 1) & 1), kWaitNs)) {
+  const bool free_stage =
+      use == 0 || tc::mbar_wait_ns(tc::smem_u32(&sy->empty[sidx]),
+                                   static_cast<uint32_t>((use - 1) & 1), kWaitNs);
+  if (!__all_sync(0xffffffffu, free_stage)) {
     fail_wait(sy, status, 2);
     return false;
   }
   write_chunks(st + static_cast<size_t>(sidx) * kStageBytes, p, h, C);
   tc::fence_proxy_async();
-  tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
   return true;
 }
 
@@ -220,12 +228,12 @@ __device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int sta
     reinterpret_cast<uint4*>(st)[k] = make_uint4(0u, 0u, 0u, 0u);
   if (tid == 0) {
     for (int k = 0; k < stages; ++k) {
-      tc::mbar_init(tc::smem_u32(&sy->full[k]), kProdThreads);
+      tc::mbar_init(tc::smem_u32(&sy->full[k]), kProdWarps);
       tc::mbar_init(tc::smem_u32(&sy->empty[k]), 1);
     }
     for (int k = 0; k < loads; ++k) {
       tc::mbar_init(tc::smem_u32(&sy->lfull[k]), 1);
-      tc::mbar_init(tc::smem_u32(&sy->lempty[k]), kProdThreads);
+      tc::mbar_init(tc::smem_u32(&sy->lempty[k]), kProdWarps);
     }
     for (int k = 0; k < 2; ++k) {
       tc::mbar_init(tc::smem_u32(&sy->qfull[k]), 1);
