@@ -99,17 +99,17 @@ __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_
       : "memory");
 }
 
-// The packed products of stage (tile, group): the group's slot rows of the tile, one bulk copy
-// each, into load buffer `buf`
+// The packed products of stage (tile, group) into load buffer `buf`. They are stored tile by
+// tile, pc[tile][slot][128 points], so a group's slots of a tile are one contiguous run and a stage
+// is one bulk copy (one 512-byte copy per slot kept the copy engine, not the memory, busy).
 __device__ __forceinline__ void load_stage(unsigned char* buf, uint32_t mbar,
                                            const uint32_t* __restrict__ pc,
-                                           const int2* __restrict__ gslots, int64_t mpad,
+                                           const int2* __restrict__ gslots, int n_slots,
                                            int group, int64_t tile) {
   const int2 gs = __ldg(gslots + group);
-  bulk_expect(mbar, static_cast<uint32_t>(gs.y) * kSlotRow);
-  for (int j = 0; j < gs.y; ++j)
-    bulk_copy(tc::smem_u32(buf + j * kSlotRow), pc + static_cast<int64_t>(gs.x + j) * mpad + tile * 128,
-              kSlotRow, mbar);
+  const uint32_t bytes = static_cast<uint32_t>(gs.y) * kSlotRow;
+  bulk_expect(mbar, bytes);
+  bulk_copy(tc::smem_u32(buf), pc + (tile * n_slots + gs.x) * 128, bytes, mbar);
 }
 
 // ---- producer: one stage of E ----------------------------------------------------------------
@@ -194,7 +194,7 @@ __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st
 // The loader's part of stage i: wait for the load buffer to be free, issue the bulk copies.
 __device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, int loads,
                                      int64_t i, const uint32_t* __restrict__ pc,
-                                     const int2* __restrict__ gslots, int64_t mpad, int group,
+                                     const int2* __restrict__ gslots, int n_slots, int group,
                                      int64_t tile) {
   const int b = static_cast<int>(i % loads);
   const int64_t use = i / loads;
@@ -204,7 +204,7 @@ __device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, i
     return false;
   }
   load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc, gslots,
-             mpad, group, tile);
+             n_slots, group, tile);
   return true;
 }
 
@@ -259,7 +259,7 @@ __device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int sta
 // (operand layout of block_multt) and optionally Q in FP64.
 __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
     const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
-    const int2* __restrict__ gslots, const uint16_t* __restrict__ coef, int n_groups, int64_t mpad, int64_t m, int n_tiles,
+    const int2* __restrict__ gslots, const uint16_t* __restrict__ coef, int n_groups, int n_slots, int64_t mpad, int64_t m, int n_tiles,
     int tiles, int gpp, int stages, int loads, uint32_t tmem_cols, uint16_t* __restrict__ qtiles,
     double* __restrict__ out64, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -303,11 +303,11 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
         const uint32_t a0 = tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes);
         const uint32_t b0 = tc::smem_u32(cf + static_cast<size_t>(gl) * kCoefBytes);
         const uint32_t d = tmem + static_cast<uint32_t>(u * kBlockCols);
+        // K-step j moves both start addresses by 2 core matrices (256 bytes: 16 in the descriptor)
+        const uint64_t ad = tc::sdesc(a0, kCoreK, kCoreMN), bd = tc::sdesc(b0, kCoreK, kCoreMN);
 #pragma unroll
         for (int j = 0; j < 8; ++j)
-          tc::mma_bf16(d, tc::sdesc(a0 + j * 2 * kCoreK, kCoreK, kCoreMN),
-                       tc::sdesc(b0 + j * 2 * kCoreK, kCoreK, kCoreMN), idesc,
-                       pass > 0 || gl > 0 || j > 0);
+          tc::mma_bf16(d, ad + 16u * j, bd + 16u * j, idesc, pass > 0 || gl > 0 || j > 0);
         tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
       }
       tc::mma_commit(tc::smem_u32(&sy->pass));
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
         const int64_t use = next / loads;
         if (use == 0 || tc::mbar_poll(tc::smem_u32(&sy->lempty[b]), static_cast<uint32_t>((use - 1) & 1))) {
           load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc,
-                     gslots, mpad, lpass * gpp + lk % lng, t0 + lk / lng);
+                     gslots, n_slots, lpass * gpp + lk % lng, t0 + lk / lng);
           ++next;
           if (++lk == nt * lng) {
             lk = 0;
@@ -420,7 +420,7 @@ constexpr uint32_t kMnA_LBO = 2048, kMnA_SBO = 128;
 
 __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
     const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
-    const int2* __restrict__ gslots, const uint16_t* __restrict__ qtiles, int n_groups, int64_t mpad, int n_tiles, int gpc,
+    const int2* __restrict__ gslots, const uint16_t* __restrict__ qtiles, int n_groups, int n_slots, int64_t mpad, int n_tiles, int gpc,
     int streams, int stages, int loads, uint32_t tmem_cols, int64_t rows,
     double* __restrict__ part, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -462,10 +462,11 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
       const uint32_t a0 = tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes);
       const uint32_t b0 = tc::smem_u32(qb + (tl & 1) * kQBytes);
       const uint32_t d = tmem + static_cast<uint32_t>(gl * kBlockCols);
+      // K-step j: A moves by 2 point groups (4096 bytes: 256 in the descriptor), B by 256 bytes
+      const uint64_t ad = tc::sdesc(a0, kMnA_LBO, kMnA_SBO), bd = tc::sdesc(b0, kCoreK, kCoreMN);
 #pragma unroll
       for (int j = 0; j < 8; ++j)
-        tc::mma_bf16(d, tc::sdesc(a0 + j * 2 * kCoreMN, kMnA_LBO, kMnA_SBO),
-                     tc::sdesc(b0 + j * 2 * kCoreK, kCoreK, kCoreMN), idesc, tl > 0 || j > 0);
+        tc::mma_bf16(d, ad + 256u * j, bd + 16u * j, idesc, tl > 0 || j > 0);
       tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
       if (gl == ng - 1) tc::mma_commit(tc::smem_u32(&sy->qempty[tl & 1]));
     }
@@ -489,7 +490,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
                   qbar);
         q_issued = tl + 1;
       }
-      if (!load(sy, status, lb, loads, k, pc, gslots, mpad, g0 + gl, ta + tl)) break;
+      if (!load(sy, status, lb, loads, k, pc, gslots, n_slots, g0 + gl, ta + tl)) break;
     }
     drain_loads(sy, status, loads, k);
     for (int tl = q_issued > 2 ? q_issued - 2 : 0; tl < q_issued; ++tl)
@@ -597,8 +598,11 @@ __global__ void block_pack_kernel(const float4* __restrict__ pmat, const CW* __r
   const int64_t total = static_cast<int64_t>(n_slots) * mpad;
   for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
        k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const int sl = static_cast<int>(k / mpad);
-    const int64_t j = k - static_cast<int64_t>(sl) * mpad;
+    // k = (tile * n_slots + slot) * 128 + point within the tile
+    const int64_t t = k / (static_cast<int64_t>(n_slots) * 128);
+    const int64_t rem = k - t * n_slots * 128;
+    const int sl = static_cast<int>(rem / 128);
+    const int64_t j = t * 128 + (rem & 127);
     uint32_t w = 0u;
     if (j < m) {
       const int64_t at = (j >> 2) * s_pad + slot_sub[sl];
@@ -952,7 +956,7 @@ cudaError_t block_mult(BlockPlan& b, cudaStream_t s, const double* p, int64_t np
   const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
   const unsigned ctas = static_cast<unsigned>(cdiv(n_tiles, sh.mult_tiles));
   block_mult_kernel<<<ctas, kBlockThreads, smem, s>>>(
-      b.pc, b.gheader, b.gslots, b.coef, b.n_groups, b.mpad, b.m, n_tiles, sh.mult_tiles,
+      b.pc, b.gheader, b.gslots, b.coef, b.n_groups, b.n_slots, b.mpad, b.m, n_tiles, sh.mult_tiles,
       gpp, sh.stages, sh.loads, cols, b.qtiles, out64, b.status);
   return cudaGetLastError();
 }
@@ -977,7 +981,7 @@ cudaError_t block_multt(BlockPlan& b, cudaStream_t s, const double* v, int64_t n
   const int streams = std::min(b.part_streams, multt_streams(b, num_sms));
   const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
   block_multt_kernel<<<static_cast<unsigned>(passes * streams), kBlockThreads, smem, s>>>(
-      b.pc, b.gheader, b.gslots, b.qtiles, b.n_groups, b.mpad, n_tiles, sh.multt_groups,
+      b.pc, b.gheader, b.gslots, b.qtiles, b.n_groups, b.n_slots, b.mpad, n_tiles, sh.multt_groups,
       streams, sh.stages, sh.loads, cols, b.rows, b.part, b.status);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

@@ -53,7 +53,7 @@ struct BlockPlan {
   uint4* gheader = nullptr;   // [n_groups] chunk headers: per chunk, its slot in the group << 4 | which
                               // of the slot's chunks it is (0xFF: unused)
   int2* gslots = nullptr;     // [n_groups] first slot and slot count of each group
-  uint32_t* pc = nullptr;     // [n_slots][mpad] BF16 product | cell << 16
+  uint32_t* pc = nullptr;     // [mpad / 128][n_slots][128] BF16 product | cell << 16, tile by tile
   uint16_t* coef = nullptr;   // [n_groups][4096] coefficient rows, BF16, operand layout
   uint16_t* qtiles = nullptr; // [mpad / 128][4096] Q tiles, BF16, operand layout
   double* part = nullptr;     // [streams][16][rows] partial rows of multT
