@@ -39,7 +39,8 @@ constexpr uint32_t kStageBytes = 128u * 16u * 16u;  // 128 points x 16 chunks x 
 constexpr uint32_t kCoefBytes = 4096u * 2u;         // 128 rows x 32 columns of BF16
 constexpr uint32_t kQBytes = 4096u * 2u;            // 128 points x 32 columns of BF16
 constexpr uint32_t kSlotRow = 128u * 4u;            // one slot's packed words of a tile
-constexpr uint32_t kLoadBytes = 16u * kSlotRow;     // a group has at most 16 slots
+constexpr uint32_t kHeaderAt = 16u * kSlotRow;      // a group has at most 16 slots, then its
+constexpr uint32_t kLoadBytes = kHeaderAt + 128u;   // 16-byte chunk header (padded)
 constexpr uint64_t kWaitNs = 2000000000ull;         // a bounded wait gives up after 2 s
 constexpr uint64_t kPollNs = 4000000000ull;         // the loader's idle polling, after 4 s
 constexpr int kMaxStages = 6;
@@ -50,6 +51,20 @@ constexpr int kMaxLoads = 12;
 constexpr uint32_t kCoreK = 128, kCoreMN = 2048;
 
 __host__ __device__ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Position in a ring of buffers: the buffer index and the number of completed rounds, whose
+// parity is the phase to wait for. Advanced without divisions: a 64-bit division is a software
+// routine on the GPU, and four of them per stage had cost more than the stage's own work.
+struct Ring {
+  int idx = 0;
+  uint32_t round = 0;
+  __device__ __forceinline__ void next(int n) {
+    if (++idx == n) {
+      idx = 0;
+      ++round;
+    }
+  }
+};
 
 // barrier and bookkeeping words behind the buffers
 struct Sync {
@@ -102,14 +117,18 @@ __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_
 // The packed products of stage (tile, group) into load buffer `buf`. They are stored tile by
 // tile, pc[tile][slot][128 points], so a group's slots of a tile are one contiguous run and a stage
 // is one bulk copy (one 512-byte copy per slot kept the copy engine, not the memory, busy).
+// The group's chunk header comes along into the same buffer (a header read from global memory
+// per stage, on the producers' critical path, cost them more than writing the stage).
 __device__ __forceinline__ void load_stage(unsigned char* buf, uint32_t mbar,
                                            const uint32_t* __restrict__ pc,
-                                           const int2* __restrict__ gslots, int n_slots,
+                                           const int2* __restrict__ gslots,
+                                           const uint4* __restrict__ gheader, int n_slots,
                                            int group, int64_t tile) {
   const int2 gs = __ldg(gslots + group);
   const uint32_t bytes = static_cast<uint32_t>(gs.y) * kSlotRow;
-  bulk_expect(mbar, bytes);
+  bulk_expect(mbar, bytes + 16u);
   bulk_copy(tc::smem_u32(buf), pc + (tile * n_slots + gs.x) * 128, bytes, mbar);
+  bulk_copy(tc::smem_u32(buf + kHeaderAt), gheader + group, 16u, mbar);
 }
 
 // ---- producer: one stage of E ----------------------------------------------------------------
@@ -124,10 +143,8 @@ struct ChunkWords {
   uint32_t hdr2;  // and 4..7
 };
 
-__device__ __forceinline__ void read_chunks(ChunkWords& C, const uint32_t* lbuf,
-                                            const uint4* __restrict__ gheader, int group, int h,
-                                            int p) {
-  const uint4 hd = __ldg(gheader + group);
+__device__ __forceinline__ void read_chunks(ChunkWords& C, const uint32_t* lbuf, int h, int p) {
+  const uint4 hd = *reinterpret_cast<const uint4*>(lbuf + kHeaderAt / 4);
   C.hdr = h ? hd.z : hd.x;
   C.hdr2 = h ? hd.w : hd.y;
 #pragma unroll
@@ -157,29 +174,27 @@ __device__ __forceinline__ void write_chunks(unsigned char* stage, int p, int h,
 // The producers' part of stage i: wait for its packed products, read them, free the load buffer,
 // wait for the E stage to be free, write it, mark it full. False when a wait ran out.
 __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st,
-                                        unsigned char* lb, int stages, int loads, int64_t i,
-                                        const uint4* __restrict__ gheader, int group, int p,
-                                        int h) {
-  const int b = static_cast<int>(i % loads);
+                                        unsigned char* lb, Ring& lr, int loads, Ring& sr,
+                                        int stages, int p, int h) {
+  const int b = lr.idx;
   // the warp's lanes decide together (a lane that gave up alone would leave the others waiting
   // at the warp's synchronisation below)
-  if (!__all_sync(0xffffffffu, tc::mbar_wait_ns(tc::smem_u32(&sy->lfull[b]),
-                                                static_cast<uint32_t>((i / loads) & 1), kWaitNs))) {
+  if (!__all_sync(0xffffffffu, tc::mbar_wait_ns(tc::smem_u32(&sy->lfull[b]), lr.round & 1u,
+                                                kWaitNs))) {
     fail_wait(sy, status, 32);
     return false;
   }
   ChunkWords C;
-  read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes),
-              gheader, group, h, p);
+  read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes), h, p);
   // one arrival per warp (the barriers count warps): 256 arrivals on one word per stage
   // serialised on the shared-memory atomics
   __syncwarp();
   if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
-  const int sidx = static_cast<int>(i % stages);
-  const int64_t use = i / stages;
+  lr.next(loads);
+  const int sidx = sr.idx;
   const bool free_stage =
-      use == 0 || tc::mbar_wait_ns(tc::smem_u32(&sy->empty[sidx]),
-                                   static_cast<uint32_t>((use - 1) & 1), kWaitNs);
+      sr.round == 0 ||
+      tc::mbar_wait_ns(tc::smem_u32(&sy->empty[sidx]), (sr.round - 1u) & 1u, kWaitNs);
   if (!__all_sync(0xffffffffu, free_stage)) {
     fail_wait(sy, status, 2);
     return false;
@@ -188,23 +203,25 @@ __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st
   tc::fence_proxy_async();
   __syncwarp();
   if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
+  sr.next(stages);
   return true;
 }
 
-// The loader's part of stage i: wait for the load buffer to be free, issue the bulk copies.
-__device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, int loads,
-                                     int64_t i, const uint32_t* __restrict__ pc,
-                                     const int2* __restrict__ gslots, int n_slots, int group,
+// The loader's part of a stage: wait for the load buffer to be free, issue the bulk copies.
+__device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, Ring& lr, int loads,
+                                     const uint32_t* __restrict__ pc,
+                                     const int2* __restrict__ gslots,
+                                     const uint4* __restrict__ gheader, int n_slots, int group,
                                      int64_t tile) {
-  const int b = static_cast<int>(i % loads);
-  const int64_t use = i / loads;
-  if (use > 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->lempty[b]),
-                                static_cast<uint32_t>((use - 1) & 1), kWaitNs)) {
+  const int b = lr.idx;
+  if (lr.round > 0 &&
+      !tc::mbar_wait_ns(tc::smem_u32(&sy->lempty[b]), (lr.round - 1u) & 1u, kWaitNs)) {
     fail_wait(sy, status, 64);
     return false;
   }
   load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc, gslots,
-             n_slots, group, tile);
+             gheader, n_slots, group, tile);
+  lr.next(loads);
   return true;
 }
 
@@ -277,26 +294,26 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
 
   if (tid < kProdThreads) {
     const int p = tid & 127, h = tid >> 7;
-    int64_t i = 0;
-    for (int pass = 0; pass < passes && !sy->abort; ++pass) {
-      const int g0 = pass * gpp, ng = min(n_groups, g0 + gpp) - g0;
-      for (int k = 0; k < nt * ng; ++k, ++i)
-        if (!produce(sy, status, st, lb, stages, loads, i, gheader, g0 + k % ng, p, h)) break;
+    Ring lr, sr;
+    bool ok = true;
+    for (int pass = 0; pass < passes && ok && !sy->abort; ++pass) {
+      const int ng = min(n_groups, pass * gpp + gpp) - pass * gpp;
+      for (int k = 0; k < nt * ng && ok; ++k) ok = produce(sy, status, st, lb, lr, loads, sr, stages, p, h);
     }
   } else if (tid == kMmaWarp * 32) {
-    int64_t i = 0;
-    for (int pass = 0; pass < passes && !sy->abort; ++pass) {
-      const int g0 = pass * gpp, ng = min(n_groups, g0 + gpp) - g0;
+    Ring sr;
+    bool ok = true;
+    for (int pass = 0; pass < passes && ok && !sy->abort; ++pass) {
+      const int ng = min(n_groups, pass * gpp + gpp) - pass * gpp;
       if (!tc::mbar_wait_ns(tc::smem_u32(&sy->cfull), static_cast<uint32_t>(pass & 1), kWaitNs)) {
         fail_wait(sy, status, 1);
         break;
       }
-      for (int k = 0; k < nt * ng; ++k, ++i) {
-        const int u = k / ng, gl = k % ng;
-        const int sidx = static_cast<int>(i % stages);
-        if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>((i / stages) & 1),
-                           kWaitNs)) {
+      for (int u = 0, gl = 0; u < nt && ok; ) {
+        const int sidx = sr.idx;
+        if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
           fail_wait(sy, status, 4);
+          ok = false;
           break;
         }
         tc::fence_after_sync();
@@ -309,6 +326,11 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
         for (int j = 0; j < 8; ++j)
           tc::mma_bf16(d, ad + 16u * j, bd + 16u * j, idesc, pass > 0 || gl > 0 || j > 0);
         tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
+        sr.next(stages);
+        if (++gl == ng) {
+          gl = 0;
+          ++u;
+        }
       }
       tc::mma_commit(tc::smem_u32(&sy->pass));
     }
@@ -327,8 +349,9 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
     };
     issue_coef(0);
     int coef_next = 1;
-    int64_t next = 0;                   // next stage to load
-    int lpass = 0, lk = 0;              // its pass and index within the pass
+    int64_t next = 0;                   // stages loaded so far
+    Ring lr;
+    int lpass = 0, lu = 0, lg = 0;      // the next stage's pass, tile and group within the pass
     int lng = min(n_groups, gpp);       // groups of that pass
     uint64_t idle_since = 0;
     while (!sy->abort && (lpass < passes || coef_next < passes)) {
@@ -339,16 +362,19 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
         progress = true;
       }
       if (lpass < passes) {
-        const int b = static_cast<int>(next % loads);
-        const int64_t use = next / loads;
-        if (use == 0 || tc::mbar_poll(tc::smem_u32(&sy->lempty[b]), static_cast<uint32_t>((use - 1) & 1))) {
+        const int b = lr.idx;
+        if (lr.round == 0 || tc::mbar_poll(tc::smem_u32(&sy->lempty[b]), (lr.round - 1u) & 1u)) {
           load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc,
-                     gslots, n_slots, lpass * gpp + lk % lng, t0 + lk / lng);
+                     gslots, gheader, n_slots, lpass * gpp + lg, t0 + lu);
+          lr.next(loads);
           ++next;
-          if (++lk == nt * lng) {
-            lk = 0;
-            ++lpass;
-            lng = min(n_groups, (lpass + 1) * gpp) - lpass * gpp;
+          if (++lg == lng) {
+            lg = 0;
+            if (++lu == nt) {
+              lu = 0;
+              ++lpass;
+              lng = min(n_groups, (lpass + 1) * gpp) - lpass * gpp;
+            }
           }
           progress = true;
         }
@@ -357,7 +383,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
         idle_since = 0;
         continue;
       }
-      __nanosleep(100);  // leave the issue slots to the producers
+      __nanosleep(64);  // leave the issue slots to the producers
       const uint64_t now = tc::globaltimer_ns();
       if (idle_since == 0) idle_since = now;
       if (now - idle_since > kPollNs) {
@@ -438,64 +464,70 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
   const uint32_t tmem = sy->tmem;
   const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, true, false);
 
-  if (tid < kProdThreads) {
+  const int nt = tb - ta;
+  if (tid < kProdThreads && ng > 0) {
     const int p = tid & 127, h = tid >> 7;
+    Ring lr, sr;
     for (int64_t k = 0; k < total && !sy->abort; ++k)
-      if (!produce(sy, status, st, lb, stages, loads, k, gheader, g0 + static_cast<int>(k % ng), p,
-                   h))
-        break;
-  } else if (tid == kMmaWarp * 32) {
-    for (int64_t k = 0; k < total && !sy->abort; ++k) {
-      const int tl = static_cast<int>(k / ng), gl = static_cast<int>(k % ng);
-      if (gl == 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]),
-                                    static_cast<uint32_t>((tl >> 1) & 1), kWaitNs)) {
+      if (!produce(sy, status, st, lb, lr, loads, sr, stages, p, h)) break;
+  } else if (tid == kMmaWarp * 32 && ng > 0) {
+    Ring sr;
+    bool ok = true;
+    for (int tl = 0; tl < nt && ok && !sy->abort; ++tl) {
+      if (!tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]), static_cast<uint32_t>((tl >> 1) & 1),
+                            kWaitNs)) {
         fail_wait(sy, status, 16);
         break;
       }
-      const int sidx = static_cast<int>(k % stages);
-      if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), static_cast<uint32_t>((k / stages) & 1),
-                         kWaitNs)) {
-        fail_wait(sy, status, 4);
-        break;
-      }
-      tc::fence_after_sync();
-      const uint32_t a0 = tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes);
       const uint32_t b0 = tc::smem_u32(qb + (tl & 1) * kQBytes);
-      const uint32_t d = tmem + static_cast<uint32_t>(gl * kBlockCols);
-      // K-step j: A moves by 2 point groups (4096 bytes: 256 in the descriptor), B by 256 bytes
-      const uint64_t ad = tc::sdesc(a0, kMnA_LBO, kMnA_SBO), bd = tc::sdesc(b0, kCoreK, kCoreMN);
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-        tc::mma_bf16(d, ad + 256u * j, bd + 16u * j, idesc, tl > 0 || j > 0);
-      tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
-      if (gl == ng - 1) tc::mma_commit(tc::smem_u32(&sy->qempty[tl & 1]));
-    }
-  } else if (tid == kLoadWarp * 32) {
-    // Q of tile tl waits only for the MMAs of tile tl - 2, whose stages were loaded before: the
-    // loader may block on either kind of wait without stalling the pipeline for good
-    int64_t k = 0;
-    int q_issued = 0;
-    for (; k < total && !sy->abort; ++k) {
-      const int tl = static_cast<int>(k / ng), gl = static_cast<int>(k % ng);
-      if (gl == 0) {
-        const int b = tl & 1, use = tl >> 1;
-        if (use > 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qempty[b]), static_cast<uint32_t>((use - 1) & 1),
-                                      kWaitNs)) {
-          fail_wait(sy, status, 16);
+      for (int gl = 0; gl < ng; ++gl) {
+        const int sidx = sr.idx;
+        if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
+          fail_wait(sy, status, 4);
+          ok = false;
           break;
         }
-        const uint32_t qbar = tc::smem_u32(&sy->qfull[b]);
-        bulk_expect(qbar, kQBytes);
-        bulk_copy(tc::smem_u32(qb + b * kQBytes), qtiles + static_cast<int64_t>(ta + tl) * 4096, kQBytes,
-                  qbar);
-        q_issued = tl + 1;
+        tc::fence_after_sync();
+        const uint32_t a0 = tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes);
+        const uint32_t d = tmem + static_cast<uint32_t>(gl * kBlockCols);
+        // K-step j: A moves by 2 point groups (4096 bytes: 256 in the descriptor), B by 256 bytes
+        const uint64_t ad = tc::sdesc(a0, kMnA_LBO, kMnA_SBO), bd = tc::sdesc(b0, kCoreK, kCoreMN);
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          tc::mma_bf16(d, ad + 256u * j, bd + 16u * j, idesc, tl > 0 || j > 0);
+        tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
+        sr.next(stages);
       }
-      if (!load(sy, status, lb, loads, k, pc, gslots, n_slots, g0 + gl, ta + tl)) break;
+      if (ok) tc::mma_commit(tc::smem_u32(&sy->qempty[tl & 1]));
     }
-    drain_loads(sy, status, loads, k);
+  } else if (tid == kLoadWarp * 32 && ng > 0) {
+    // Q of tile tl waits only for the MMAs of tile tl - 2, whose stages were loaded before: the
+    // loader may block on either kind of wait without stalling the pipeline for good
+    int64_t issued = 0;
+    int q_issued = 0;
+    Ring lr;
+    bool ok = true;
+    for (int tl = 0; tl < nt && ok && !sy->abort; ++tl) {
+      const int b = tl & 1, use = tl >> 1;
+      if (use > 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qempty[b]),
+                                       static_cast<uint32_t>((use - 1) & 1), kWaitNs)) {
+        fail_wait(sy, status, 16);
+        break;
+      }
+      const uint32_t qbar = tc::smem_u32(&sy->qfull[b]);
+      bulk_expect(qbar, kQBytes);
+      bulk_copy(tc::smem_u32(qb + b * kQBytes), qtiles + static_cast<int64_t>(ta + tl) * 4096,
+                kQBytes, qbar);
+      q_issued = tl + 1;
+      for (int gl = 0; gl < ng && ok; ++gl) {
+        ok = load(sy, status, lb, lr, loads, pc, gslots, gheader, n_slots, g0 + gl, ta + tl);
+        if (ok) ++issued;
+      }
+    }
+    drain_loads(sy, status, loads, issued);
     for (int tl = q_issued > 2 ? q_issued - 2 : 0; tl < q_issued; ++tl)
       if (!tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]), static_cast<uint32_t>((tl >> 1) & 1),
-                         kWaitNs))
+                            kWaitNs))
         atomicOr(status, 128);
   }
   if (tid == kMmaWarp * 32) {
