@@ -207,6 +207,59 @@ __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st
   return true;
 }
 
+// produce() for the mult kernel's tensor-memory A operand: the stage's rows go to tensor memory
+// (lane = point, 4 columns per chunk: the chunk's 8 BF16 elements as 4 pairs) with one 32-column
+// store per thread instead of shared memory, so the tensor cores read A without the shared-memory
+// traffic of writing and reading it. All 8 chunks are written (zeros included), which also
+// overwrites whatever an earlier group left in the columns.
+__device__ __forceinline__ bool produce_tmem(Sync* sy, int* status, unsigned char* lb, Ring& lr,
+                                             int loads, Ring& sr, int stages, uint32_t a_taddr,
+                                             int p, int h) {
+  const int b = lr.idx;
+  if (!__all_sync(0xffffffffu, tc::mbar_wait_ns(tc::smem_u32(&sy->lfull[b]), lr.round & 1u,
+                                                kWaitNs))) {
+    fail_wait(sy, status, 32);
+    return false;
+  }
+  ChunkWords C;
+  read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes), h, p);
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
+  lr.next(loads);
+  const int sidx = sr.idx;
+  const bool free_stage =
+      sr.round == 0 ||
+      tc::mbar_wait_ns(tc::smem_u32(&sy->empty[sidx]), (sr.round - 1u) & 1u, kWaitNs);
+  if (!__all_sync(0xffffffffu, free_stage)) {
+    fail_wait(sy, status, 2);
+    return false;
+  }
+  uint32_t r[32];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const uint32_t byte = ((i < 4 ? C.hdr : C.hdr2) >> (8 * (i & 3))) & 0xFFu;
+    const uint32_t w = C.w[i];
+    const uint32_t c = w >> 16;
+    const uint32_t v = byte != 0xFFu && (c >> 3) == (byte & 0xFu) ? (w & 0xFFFFu) : 0u;
+    const uint32_t val = v << ((c & 1u) * 16u);
+    const uint32_t wd = (c >> 1) & 3u;
+    r[4 * i + 0] = wd == 0 ? val : 0u;
+    r[4 * i + 1] = wd == 1 ? val : 0u;
+    r[4 * i + 2] = wd == 2 ? val : 0u;
+    r[4 * i + 3] = wd == 3 ? val : 0u;
+  }
+  // lanes 32 (warp % 4) ...; this half's 8 chunks are columns 32 h .. 32 h + 31 of the stage
+  tc::tmem_st32(a_taddr + (static_cast<uint32_t>((threadIdx.x >> 5) & 3) << 21) +
+                    static_cast<uint32_t>(sidx * 64 + 32 * h),
+                r);
+  tc::tmem_wait_st();
+  tc::fence_before_sync();
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
+  sr.next(stages);
+  return true;
+}
+
 // The loader's part of a stage: wait for the load buffer to be free, issue the bulk copies.
 __device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, Ring& lr, int loads,
                                      const uint32_t* __restrict__ pc,
@@ -238,10 +291,10 @@ __device__ __forceinline__ void drain_loads(Sync* sy, int* status, int loads, in
 
 // Shared set-up of both kernels: zeroed E stages (rows a group leaves unused must hold finite
 // values), barriers, tensor memory.
-__device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int stages, int loads,
-                                            uint32_t tmem_cols) {
+__device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int smem_stages,
+                                            int stages, int loads, uint32_t tmem_cols) {
   const int tid = threadIdx.x;
-  for (uint32_t k = tid; k < static_cast<uint32_t>(stages) * kStageBytes / 16u; k += blockDim.x)
+  for (uint32_t k = tid; k < static_cast<uint32_t>(smem_stages) * kStageBytes / 16u; k += blockDim.x)
     reinterpret_cast<uint4*>(st)[k] = make_uint4(0u, 0u, 0u, 0u);
   if (tid == 0) {
     for (int k = 0; k < stages; ++k) {
@@ -274,22 +327,27 @@ __device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int sta
 // memory, and walks the groups in passes of `gpp` groups whose coefficient rows the loader copies
 // into shared memory once the previous pass's MMAs have completed. Output: the BF16 Q tiles
 // (operand layout of block_multt) and optionally Q in FP64.
+// TMEM_A: the A operand (the stages of E) lives in tensor memory after the accumulators, 64
+// columns per stage, instead of in shared memory.
+template <bool TMEM_A>
 __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
     const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
     const int2* __restrict__ gslots, const uint16_t* __restrict__ coef, int n_groups, int n_slots, int64_t mpad, int64_t m, int n_tiles,
     int tiles, int gpp, int stages, int loads, uint32_t tmem_cols, uint16_t* __restrict__ qtiles,
     double* __restrict__ out64, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
+  const int smem_stages = TMEM_A ? 0 : stages;
   unsigned char* st = smem;
-  unsigned char* lb = st + static_cast<size_t>(stages) * kStageBytes;
+  unsigned char* lb = st + static_cast<size_t>(smem_stages) * kStageBytes;
   unsigned char* cf = lb + static_cast<size_t>(loads) * kLoadBytes;
   Sync* sy = reinterpret_cast<Sync*>(cf + static_cast<size_t>(gpp) * kCoefBytes);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int t0 = blockIdx.x * tiles;
   const int nt = min(tiles, n_tiles - t0);
   const int passes = static_cast<int>(cdiv(n_groups, gpp));
-  block_setup(sy, st, stages, loads, tmem_cols);
+  block_setup(sy, st, smem_stages, stages, loads, tmem_cols);
   const uint32_t tmem = sy->tmem;
+  const uint32_t a_col = static_cast<uint32_t>(tiles * kBlockCols);  // first A column (TMEM_A)
   const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, false, false);
 
   if (tid < kProdThreads) {
@@ -298,7 +356,9 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
     bool ok = true;
     for (int pass = 0; pass < passes && ok && !sy->abort; ++pass) {
       const int ng = min(n_groups, pass * gpp + gpp) - pass * gpp;
-      for (int k = 0; k < nt * ng && ok; ++k) ok = produce(sy, status, st, lb, lr, loads, sr, stages, p, h);
+      for (int k = 0; k < nt * ng && ok; ++k)
+        ok = TMEM_A ? produce_tmem(sy, status, lb, lr, loads, sr, stages, tmem + a_col, p, h)
+                    : produce(sy, status, st, lb, lr, loads, sr, stages, p, h);
     }
   } else if (tid == kMmaWarp * 32) {
     Ring sr;
@@ -317,14 +377,23 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
           break;
         }
         tc::fence_after_sync();
-        const uint32_t a0 = tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes);
         const uint32_t b0 = tc::smem_u32(cf + static_cast<size_t>(gl) * kCoefBytes);
         const uint32_t d = tmem + static_cast<uint32_t>(u * kBlockCols);
-        // K-step j moves both start addresses by 2 core matrices (256 bytes: 16 in the descriptor)
-        const uint64_t ad = tc::sdesc(a0, kCoreK, kCoreMN), bd = tc::sdesc(b0, kCoreK, kCoreMN);
+        // K-step j: B moves by 2 core matrices (256 bytes: 16 in the descriptor); A by 256 bytes
+        // in shared memory, or by 8 columns in tensor memory
+        const uint64_t bd = tc::sdesc(b0, kCoreK, kCoreMN);
+        if constexpr (TMEM_A) {
+          const uint32_t at = tmem + a_col + static_cast<uint32_t>(sidx * 64);
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-          tc::mma_bf16(d, ad + 16u * j, bd + 16u * j, idesc, pass > 0 || gl > 0 || j > 0);
+          for (int j = 0; j < 8; ++j)
+            tc::mma_bf16_ts(d, at + 8u * j, bd + 16u * j, idesc, pass > 0 || gl > 0 || j > 0);
+        } else {
+          const uint32_t a0 = tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes);
+          const uint64_t ad = tc::sdesc(a0, kCoreK, kCoreMN);
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            tc::mma_bf16(d, ad + 16u * j, bd + 16u * j, idesc, pass > 0 || gl > 0 || j > 0);
+        }
         tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
         sr.next(stages);
         if (++gl == ng) {
@@ -460,7 +529,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
   const int ta = static_cast<int>(static_cast<int64_t>(stream) * n_tiles / streams);
   const int tb = static_cast<int>(static_cast<int64_t>(stream + 1) * n_tiles / streams);
   const int64_t total = ng > 0 ? static_cast<int64_t>(tb - ta) * ng : 0;
-  block_setup(sy, st, stages, loads, tmem_cols);
+  block_setup(sy, st, stages, stages, loads, tmem_cols);
   const uint32_t tmem = sy->tmem;
   const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, true, false);
 
@@ -806,14 +875,22 @@ namespace sgmev {
 namespace {
 // groups of coefficient rows a mult CTA holds: the shape's count, fewer when the stages leave less
 // shared memory (at least one)
+// shared-memory stages of E of the mult kernel (none when A lives in tensor memory)
+int mult_smem_stages(const BlockShape& sh) { return sh.mult_tmem ? 0 : sh.stages; }
 int mult_groups_fit(const BlockShape& sh, int smem_cap) {
-  const int64_t room = static_cast<int64_t>(smem_cap) - static_cast<int64_t>(sh.stages) * kStageBytes -
+  const int64_t room = static_cast<int64_t>(smem_cap) -
+                       static_cast<int64_t>(mult_smem_stages(sh)) * kStageBytes -
                        static_cast<int64_t>(sh.loads) * kLoadBytes - static_cast<int64_t>(sizeof(Sync));
   return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(sh.mult_groups, room / kCoefBytes)));
 }
 size_t mult_smem(const BlockShape& sh, int groups) {
-  return static_cast<size_t>(sh.stages) * kStageBytes + static_cast<size_t>(sh.loads) * kLoadBytes +
-         static_cast<size_t>(groups) * kCoefBytes + sizeof(Sync);
+  return static_cast<size_t>(mult_smem_stages(sh)) * kStageBytes +
+         static_cast<size_t>(sh.loads) * kLoadBytes + static_cast<size_t>(groups) * kCoefBytes +
+         sizeof(Sync);
+}
+// tensor-memory columns of the mult kernel: the accumulators, then the A stages
+int mult_tmem_need(const BlockShape& sh) {
+  return sh.mult_tiles * kBlockCols + (sh.mult_tmem ? sh.stages * 64 : 0);
 }
 int device_smem_cap() {
   int dev = 0, cap = 0;
@@ -847,7 +924,7 @@ void block_free(BlockPlan* b) {
 
 bool block_shape_ok(const BlockShape& sh, int smem_cap) {
   return sh.stages >= 2 && sh.stages <= kMaxStages && sh.loads >= 2 && sh.loads <= kMaxLoads &&
-         sh.mult_tiles >= 1 && sh.mult_tiles <= 16 &&
+         sh.mult_tiles >= 1 && sh.mult_tiles <= 16 && mult_tmem_need(sh) <= 512 &&
          sh.mult_groups >= 1 && sh.multt_groups >= 1 && sh.multt_groups <= 16 &&
          mult_smem(sh, mult_groups_fit(sh, smem_cap)) <= static_cast<size_t>(smem_cap) &&
          multt_smem(sh) <= static_cast<size_t>(smem_cap);
@@ -980,14 +1057,17 @@ cudaError_t block_mult(BlockPlan& b, cudaStream_t s, const double* p, int64_t np
                                                                          b.rows, b.coef);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const uint32_t cols = tmem_cols_for(sh.mult_tiles);
+  const uint32_t cols = tmem_cols_for(cdiv(mult_tmem_need(sh), kBlockCols));
   const int gpp = mult_groups_fit(sh, device_smem_cap());
+  // with more than half of the tensor memory per CTA, a second CTA on the SM would only wait for
+  // the first one's columns: ask for enough shared memory that it is never placed there
   const size_t smem = cols > 256 ? std::max<size_t>(mult_smem(sh, gpp), 120 * 1024) : mult_smem(sh, gpp);
-  e = set_smem_cap(block_mult_kernel, smem);
+  auto kern = sh.mult_tmem ? block_mult_kernel<true> : block_mult_kernel<false>;
+  e = set_smem_cap(kern, smem);
   if (e != cudaSuccess) return e;
   const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
   const unsigned ctas = static_cast<unsigned>(cdiv(n_tiles, sh.mult_tiles));
-  block_mult_kernel<<<ctas, kBlockThreads, smem, s>>>(
+  kern<<<ctas, kBlockThreads, smem, s>>>(
       b.pc, b.gheader, b.gslots, b.coef, b.n_groups, b.n_slots, b.mpad, b.m, n_tiles, sh.mult_tiles,
       gpp, sh.stages, sh.loads, cols, b.qtiles, out64, b.status);
   return cudaGetLastError();

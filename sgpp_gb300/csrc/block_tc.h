@@ -35,10 +35,12 @@ constexpr int kBlockMaxCells = 128;   // largest subspace the block products tak
 // Tunable launch shapes (picked per operator by the autotuner, sgmev_tune_block)
 struct BlockShape {
   int mult_tiles = 8;      // tiles per mult CTA (their accumulators stay in tensor memory)
-  int mult_groups = 16;    // groups whose coefficient rows a mult CTA holds in shared memory
+  int mult_groups = 32;    // groups whose coefficient rows a mult CTA holds (fewer when shared
+                           // memory runs out)
   int multt_groups = 16;   // groups (accumulators) per multT CTA
   int stages = 2;          // shared-memory stages of E in flight
   int loads = 6;           // stages of packed products in flight (bulk copies ahead of use)
+  int mult_tmem = 1;       // mult keeps its A operand (the stages of E) in tensor memory
 };
 
 struct BlockPlan {

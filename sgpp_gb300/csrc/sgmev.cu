@@ -1218,6 +1218,12 @@ static int apply_shape_params(sgmev_op* op, const char* params_json) {
       return fail(SGMEV_ERR_INVALID, std::string("params: ") + knobs[k] + " must be an integer in [1, 64]");
     *fields[k] = static_cast<int>(x);
   }
+  const std::string ma = json_string(params_json, "block_mult_a");
+  if (!ma.empty()) {
+    if (ma != "tmem" && ma != "smem")
+      return fail(SGMEV_ERR_INVALID, "params: block_mult_a must be \"tmem\" or \"smem\"");
+    sh.mult_tmem = ma == "tmem" ? 1 : 0;
+  }
   op->multt_batch = batch;
   op->sub.multt_batch = batch;
   op->blk_shape = sh;
@@ -1491,7 +1497,8 @@ SGMEV_API int sgmev_set_params(sgmev_op* op, const char* params_json) {
   SGMEV_TRY(check_op(op));
   if (!params_json) return SGMEV_OK;
   static const char* allowed[] = {"multt_batch", "block_mult_tiles", "block_mult_groups",
-                                  "block_multt_groups", "block_stages", "block_loads"};
+                                  "block_multt_groups", "block_stages", "block_loads",
+                                  "block_mult_a"};
   // every key must be a launch-shape knob
   for (const char* c = params_json; (c = std::strchr(c, '"')) != nullptr;) {
     const char* e = std::strchr(c + 1, '"');

@@ -133,3 +133,19 @@ def test_block_products_refuse_an_operator_without_materialised_products():
     with pytest.raises(sg.OperationException, match="materialised"):
         op.multBlock(np.zeros((K, grid.getSize())))
     op.close()
+
+
+@pytest.mark.parametrize("d,level,m", [(5, 4, 3000), (2, 8, 2000)])
+def test_mult_a_operand_in_tensor_or_shared_memory_gives_the_same_bits(d, level, m):
+    """block_mult_a: the mult's A operand (the one-hot tiles of the products) in tensor memory or
+    in shared memory feeds the same MMAs with the same values, so the results are identical."""
+    rng = np.random.default_rng(60 + d)
+    grid = _grid(d, level)
+    x = rng.random((m, d))
+    a = rng.standard_normal((K, grid.getSize()))
+    out = []
+    for where in ("tmem", "smem"):
+        op = _op(grid, x, block_mult_a=where)
+        out.append(op.multBlock(a))
+        op.close()
+    np.testing.assert_array_equal(out[0], out[1])
