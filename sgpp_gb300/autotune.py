@@ -11,7 +11,7 @@ themselves with CUDA events (sgmev_profile), and the parameters are set on the l
 
 Tunables:
   multT16   "multt_batch"            points per read-modify-write round of the FP16 multTranspose
-  block     "block_mult_a", "block_mult_tiles", "block_stages", "block_loads",
+  block     "block_window", "block_mult_a", "block_mult_tiles", "block_stages",
             "block_multt_groups"
                                       the tensor-core products with 16 right-hand sides
 
@@ -49,10 +49,10 @@ class TunableParameter:
 
 TUNABLES: Dict[str, List[TunableParameter]] = {
     "multT16": [TunableParameter("multt_batch", [1, 2, 4])],
-    "block": [TunableParameter("block_mult_a", ["tmem", "smem"]),
+    "block": [TunableParameter("block_window", [1, 2, 3]),
+              TunableParameter("block_mult_a", ["tmem", "smem"]),
               TunableParameter("block_mult_tiles", [4, 8]),
-              TunableParameter("block_stages", [2, 3]),
-              TunableParameter("block_loads", [4, 8]),
+              TunableParameter("block_stages", [3, 4]),
               TunableParameter("block_multt_groups", [8, 16])],
 }
 

@@ -45,6 +45,7 @@ constexpr uint64_t kWaitNs = 2000000000ull;         // a bounded wait gives up a
 constexpr uint64_t kPollNs = 4000000000ull;         // the loader's idle polling, after 4 s
 constexpr int kMaxStages = 6;
 constexpr int kMaxLoads = 12;
+constexpr int kMaxWindow = 4;  // stages the MMA thread interleaves
 // core-matrix strides of the operands: 128 bytes between neighbouring core matrices along the
 // row dimension of a chunk / K-step (8 elements), 2048 bytes between groups of 8 points or of 8
 // output columns
@@ -333,7 +334,7 @@ template <bool TMEM_A>
 __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
     const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
     const int2* __restrict__ gslots, const uint16_t* __restrict__ coef, int n_groups, int n_slots, int64_t mpad, int64_t m, int n_tiles,
-    int tiles, int gpp, int stages, int loads, uint32_t tmem_cols, uint16_t* __restrict__ qtiles,
+    int tiles, int gpp, int stages, int loads, int win, uint32_t tmem_cols, uint16_t* __restrict__ qtiles,
     double* __restrict__ out64, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int smem_stages = TMEM_A ? 0 : stages;
@@ -369,37 +370,52 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
         fail_wait(sy, status, 1);
         break;
       }
-      for (int u = 0, gl = 0; u < nt && ok; ) {
-        const int sidx = sr.idx;
-        if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
-          fail_wait(sy, status, 4);
-          ok = false;
-          break;
+      // stages in the pass: groups outer, tiles inner, so that neighbouring stages feed
+      // different accumulators; a window of `win` stages is issued round-robin, one K-step of
+      // each in turn (the MMAs of one accumulator are serial, so a lone stage left the tensor
+      // cores waiting on each MMA's latency)
+      for (int u = 0, gl = 0; gl < ng && ok;) {
+        int w_sidx[kMaxWindow], w_u[kMaxWindow], w_gl[kMaxWindow], w = 0;
+        for (; w < win && gl < ng; ++w) {
+          const int sidx = sr.idx;
+          if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
+            fail_wait(sy, status, 4);
+            ok = false;
+            break;
+          }
+          w_sidx[w] = sidx;
+          w_u[w] = u;
+          w_gl[w] = gl;
+          sr.next(stages);
+          if (++u == nt) {
+            u = 0;
+            ++gl;
+          }
         }
+        if (!ok) break;
         tc::fence_after_sync();
-        const uint32_t b0 = tc::smem_u32(cf + static_cast<size_t>(gl) * kCoefBytes);
-        const uint32_t d = tmem + static_cast<uint32_t>(u * kBlockCols);
         // K-step j: B moves by 2 core matrices (256 bytes: 16 in the descriptor); A by 256 bytes
         // in shared memory, or by 8 columns in tensor memory
-        const uint64_t bd = tc::sdesc(b0, kCoreK, kCoreMN);
-        if constexpr (TMEM_A) {
-          const uint32_t at = tmem + a_col + static_cast<uint32_t>(sidx * 64);
 #pragma unroll
-          for (int j = 0; j < 8; ++j)
-            tc::mma_bf16_ts(d, at + 8u * j, bd + 16u * j, idesc, pass > 0 || gl > 0 || j > 0);
-        } else {
-          const uint32_t a0 = tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes);
-          const uint64_t ad = tc::sdesc(a0, kCoreK, kCoreMN);
-#pragma unroll
-          for (int j = 0; j < 8; ++j)
-            tc::mma_bf16(d, ad + 16u * j, bd + 16u * j, idesc, pass > 0 || gl > 0 || j > 0);
+        for (int j = 0; j < 8; ++j) {
+          for (int q = 0; q < w; ++q) {
+            const uint32_t d = tmem + static_cast<uint32_t>(w_u[q] * kBlockCols);
+            const uint64_t bd =
+                tc::sdesc(tc::smem_u32(cf + static_cast<size_t>(w_gl[q]) * kCoefBytes), kCoreK,
+                          kCoreMN) + 16u * j;
+            const bool acc = pass > 0 || w_gl[q] > 0 || j > 0;
+            if constexpr (TMEM_A) {
+              tc::mma_bf16_ts(d, tmem + a_col + static_cast<uint32_t>(w_sidx[q] * 64 + 8 * j), bd,
+                              idesc, acc);
+            } else {
+              const uint64_t ad =
+                  tc::sdesc(tc::smem_u32(st + static_cast<size_t>(w_sidx[q]) * kStageBytes),
+                            kCoreK, kCoreMN) + 16u * j;
+              tc::mma_bf16(d, ad, bd, idesc, acc);
+            }
+          }
         }
-        tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
-        sr.next(stages);
-        if (++gl == ng) {
-          gl = 0;
-          ++u;
-        }
+        for (int q = 0; q < w; ++q) tc::mma_commit(tc::smem_u32(&sy->empty[w_sidx[q]]));
       }
       tc::mma_commit(tc::smem_u32(&sy->pass));
     }
@@ -420,7 +436,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
     int coef_next = 1;
     int64_t next = 0;                   // stages loaded so far
     Ring lr;
-    int lpass = 0, lu = 0, lg = 0;      // the next stage's pass, tile and group within the pass
+    int lpass = 0, lu = 0, lg = 0;      // the next stage's pass, group within the pass and tile
     int lng = min(n_groups, gpp);       // groups of that pass
     uint64_t idle_since = 0;
     while (!sy->abort && (lpass < passes || coef_next < passes)) {
@@ -437,10 +453,10 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
                      gslots, gheader, n_slots, lpass * gpp + lg, t0 + lu);
           lr.next(loads);
           ++next;
-          if (++lg == lng) {
-            lg = 0;
-            if (++lu == nt) {
-              lu = 0;
+          if (++lu == nt) {
+            lu = 0;
+            if (++lg == lng) {
+              lg = 0;
               ++lpass;
               lng = min(n_groups, (lpass + 1) * gpp) - lpass * gpp;
             }
@@ -516,7 +532,7 @@ constexpr uint32_t kMnA_LBO = 2048, kMnA_SBO = 128;
 __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
     const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
     const int2* __restrict__ gslots, const uint16_t* __restrict__ qtiles, int n_groups, int n_slots, int64_t mpad, int n_tiles, int gpc,
-    int streams, int stages, int loads, uint32_t tmem_cols, int64_t rows,
+    int streams, int stages, int loads, int win, uint32_t tmem_cols, int64_t rows,
     double* __restrict__ part, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* st = smem;
@@ -540,34 +556,53 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
     for (int64_t k = 0; k < total && !sy->abort; ++k)
       if (!produce(sy, status, st, lb, lr, loads, sr, stages, p, h)) break;
   } else if (tid == kMmaWarp * 32 && ng > 0) {
+    // windows of `win` consecutive stages (groups inner: different accumulators), issued
+    // round-robin one K-step at a time, as in the mult kernel
     Ring sr;
     bool ok = true;
-    for (int tl = 0; tl < nt && ok && !sy->abort; ++tl) {
-      if (!tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]), static_cast<uint32_t>((tl >> 1) & 1),
-                            kWaitNs)) {
-        fail_wait(sy, status, 16);
-        break;
-      }
-      const uint32_t b0 = tc::smem_u32(qb + (tl & 1) * kQBytes);
-      for (int gl = 0; gl < ng; ++gl) {
+    for (int tl = 0, gl = 0; tl < nt && ok && !sy->abort;) {
+      int w_sidx[kMaxWindow], w_gl[kMaxWindow], w_tl[kMaxWindow], w = 0;
+      for (; w < win && tl < nt; ++w) {
+        if (gl == 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]),
+                                         static_cast<uint32_t>((tl >> 1) & 1), kWaitNs)) {
+          fail_wait(sy, status, 16);
+          ok = false;
+          break;
+        }
         const int sidx = sr.idx;
         if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
           fail_wait(sy, status, 4);
           ok = false;
           break;
         }
-        tc::fence_after_sync();
-        const uint32_t a0 = tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes);
-        const uint32_t d = tmem + static_cast<uint32_t>(gl * kBlockCols);
-        // K-step j: A moves by 2 point groups (4096 bytes: 256 in the descriptor), B by 256 bytes
-        const uint64_t ad = tc::sdesc(a0, kMnA_LBO, kMnA_SBO), bd = tc::sdesc(b0, kCoreK, kCoreMN);
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-          tc::mma_bf16(d, ad + 256u * j, bd + 16u * j, idesc, tl > 0 || j > 0);
-        tc::mma_commit(tc::smem_u32(&sy->empty[sidx]));
+        w_sidx[w] = sidx;
+        w_gl[w] = gl;
+        w_tl[w] = tl;
         sr.next(stages);
+        if (++gl == ng) {
+          gl = 0;
+          ++tl;
+        }
       }
-      if (ok) tc::mma_commit(tc::smem_u32(&sy->qempty[tl & 1]));
+      if (!ok) break;
+      tc::fence_after_sync();
+      // K-step j: A moves by 2 point groups (4096 bytes: 256 in the descriptor), B by 256 bytes
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        for (int q = 0; q < w; ++q) {
+          const uint64_t ad =
+              tc::sdesc(tc::smem_u32(st + static_cast<size_t>(w_sidx[q]) * kStageBytes), kMnA_LBO,
+                        kMnA_SBO) + 256u * j;
+          const uint64_t bd =
+              tc::sdesc(tc::smem_u32(qb + (w_tl[q] & 1) * kQBytes), kCoreK, kCoreMN) + 16u * j;
+          tc::mma_bf16(tmem + static_cast<uint32_t>(w_gl[q] * kBlockCols), ad, bd, idesc,
+                       w_tl[q] > 0 || j > 0);
+        }
+      }
+      for (int q = 0; q < w; ++q) {
+        tc::mma_commit(tc::smem_u32(&sy->empty[w_sidx[q]]));
+        if (w_gl[q] == ng - 1) tc::mma_commit(tc::smem_u32(&sy->qempty[w_tl[q] & 1]));
+      }
     }
   } else if (tid == kLoadWarp * 32 && ng > 0) {
     // Q of tile tl waits only for the MMAs of tile tl - 2, whose stages were loaded before: the
@@ -924,6 +959,7 @@ void block_free(BlockPlan* b) {
 
 bool block_shape_ok(const BlockShape& sh, int smem_cap) {
   return sh.stages >= 2 && sh.stages <= kMaxStages && sh.loads >= 2 && sh.loads <= kMaxLoads &&
+         sh.window >= 1 && sh.window <= kMaxWindow &&
          sh.mult_tiles >= 1 && sh.mult_tiles <= 16 && mult_tmem_need(sh) <= 512 &&
          sh.mult_groups >= 1 && sh.multt_groups >= 1 && sh.multt_groups <= 16 &&
          mult_smem(sh, mult_groups_fit(sh, smem_cap)) <= static_cast<size_t>(smem_cap) &&
@@ -1069,7 +1105,7 @@ cudaError_t block_mult(BlockPlan& b, cudaStream_t s, const double* p, int64_t np
   const unsigned ctas = static_cast<unsigned>(cdiv(n_tiles, sh.mult_tiles));
   kern<<<ctas, kBlockThreads, smem, s>>>(
       b.pc, b.gheader, b.gslots, b.coef, b.n_groups, b.n_slots, b.mpad, b.m, n_tiles, sh.mult_tiles,
-      gpp, sh.stages, sh.loads, cols, b.qtiles, out64, b.status);
+      gpp, sh.stages, sh.loads, std::min(sh.window, sh.stages), cols, b.qtiles, out64, b.status);
   return cudaGetLastError();
 }
 
@@ -1094,7 +1130,7 @@ cudaError_t block_multt(BlockPlan& b, cudaStream_t s, const double* v, int64_t n
   const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
   block_multt_kernel<<<static_cast<unsigned>(passes * streams), kBlockThreads, smem, s>>>(
       b.pc, b.gheader, b.gslots, b.qtiles, b.n_groups, b.n_slots, b.mpad, n_tiles, sh.multt_groups,
-      streams, sh.stages, sh.loads, cols, b.rows, b.part, b.status);
+      streams, sh.stages, sh.loads, std::min(sh.window, sh.stages), cols, b.rows, b.part, b.status);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   block_finish_kernel<<<grid_for(npad * kBlockRhs, num_sms), 256, 0, s>>>(

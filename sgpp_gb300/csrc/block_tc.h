@@ -41,6 +41,7 @@ struct BlockShape {
   int stages = 2;          // shared-memory stages of E in flight
   int loads = 6;           // stages of packed products in flight (bulk copies ahead of use)
   int mult_tmem = 1;       // mult keeps its A operand (the stages of E) in tensor memory
+  int window = 2;          // stages whose MMAs one issue round interleaves (at most `stages`)
 };
 
 struct BlockPlan {

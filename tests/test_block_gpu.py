@@ -149,3 +149,21 @@ def test_mult_a_operand_in_tensor_or_shared_memory_gives_the_same_bits(d, level,
         out.append(op.multBlock(a))
         op.close()
     np.testing.assert_array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("window", ["1", "3"])
+def test_interleaved_mma_window_gives_the_same_bits(window):
+    """block_window: the MMA thread interleaves the K-steps of neighbouring stages, which feed
+    different accumulators, so every accumulator still receives its MMAs in the same order."""
+    rng = np.random.default_rng(61)
+    grid = _grid(6, 4)
+    x = rng.random((20000, 6))
+    a = rng.standard_normal((K, grid.getSize()))
+    v = rng.standard_normal((K, x.shape[0]))
+    out = []
+    for w in ("2", window):
+        op = _op(grid, x, block_window=w, block_stages=3)
+        out.append((op.multBlock(a), op.multTransposeBlock(v)))
+        op.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
