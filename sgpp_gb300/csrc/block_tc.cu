@@ -374,22 +374,36 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
       // different accumulators; a window of `win` stages is issued round-robin, one K-step of
       // each in turn (the MMAs of one accumulator are serial, so a lone stage left the tensor
       // cores waiting on each MMA's latency)
+      // (every loop over the window is unrolled over kMaxWindow with a guard, so that the
+      // window's values stay in registers: the MMA thread's issue rate bounds the kernel)
       for (int u = 0, gl = 0; gl < ng && ok;) {
-        int w_sidx[kMaxWindow], w_u[kMaxWindow], w_gl[kMaxWindow], w = 0;
-        for (; w < win && gl < ng; ++w) {
-          const int sidx = sr.idx;
-          if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
-            fail_wait(sy, status, 4);
-            ok = false;
-            break;
-          }
-          w_sidx[w] = sidx;
-          w_u[w] = u;
-          w_gl[w] = gl;
-          sr.next(stages);
-          if (++u == nt) {
-            u = 0;
-            ++gl;
+        int w_sidx[kMaxWindow], w_acc[kMaxWindow];
+        uint32_t w_d[kMaxWindow], w_a[kMaxWindow];
+        uint64_t w_ad[kMaxWindow], w_bd[kMaxWindow];
+        int w = 0;
+#pragma unroll
+        for (int q = 0; q < kMaxWindow; ++q) {
+          if (q < win && gl < ng && ok) {
+            const int sidx = sr.idx;
+            if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
+              fail_wait(sy, status, 4);
+              ok = false;
+            } else {
+              w_sidx[q] = sidx;
+              w_d[q] = tmem + static_cast<uint32_t>(u * kBlockCols);
+              w_acc[q] = pass > 0 || gl > 0;
+              w_bd[q] = tc::sdesc(tc::smem_u32(cf + static_cast<size_t>(gl) * kCoefBytes), kCoreK,
+                                  kCoreMN);
+              w_a[q] = tmem + a_col + static_cast<uint32_t>(sidx * 64);
+              w_ad[q] = tc::sdesc(tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes),
+                                  kCoreK, kCoreMN);
+              ++w;
+              sr.next(stages);
+              if (++u == nt) {
+                u = 0;
+                ++gl;
+              }
+            }
           }
         }
         if (!ok) break;
@@ -398,24 +412,21 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
         // in shared memory, or by 8 columns in tensor memory
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          for (int q = 0; q < w; ++q) {
-            const uint32_t d = tmem + static_cast<uint32_t>(w_u[q] * kBlockCols);
-            const uint64_t bd =
-                tc::sdesc(tc::smem_u32(cf + static_cast<size_t>(w_gl[q]) * kCoefBytes), kCoreK,
-                          kCoreMN) + 16u * j;
-            const bool acc = pass > 0 || w_gl[q] > 0 || j > 0;
-            if constexpr (TMEM_A) {
-              tc::mma_bf16_ts(d, tmem + a_col + static_cast<uint32_t>(w_sidx[q] * 64 + 8 * j), bd,
-                              idesc, acc);
-            } else {
-              const uint64_t ad =
-                  tc::sdesc(tc::smem_u32(st + static_cast<size_t>(w_sidx[q]) * kStageBytes),
-                            kCoreK, kCoreMN) + 16u * j;
-              tc::mma_bf16(d, ad, bd, idesc, acc);
+#pragma unroll
+          for (int q = 0; q < kMaxWindow; ++q) {
+            if (q < w) {
+              if constexpr (TMEM_A)
+                tc::mma_bf16_ts(w_d[q], w_a[q] + 8u * j, w_bd[q] + 16u * j, idesc,
+                                w_acc[q] || j > 0);
+              else
+                tc::mma_bf16(w_d[q], w_ad[q] + 16u * j, w_bd[q] + 16u * j, idesc,
+                             w_acc[q] || j > 0);
             }
           }
         }
-        for (int q = 0; q < w; ++q) tc::mma_commit(tc::smem_u32(&sy->empty[w_sidx[q]]));
+#pragma unroll
+        for (int q = 0; q < kMaxWindow; ++q)
+          if (q < w) tc::mma_commit(tc::smem_u32(&sy->empty[w_sidx[q]]));
       }
       tc::mma_commit(tc::smem_u32(&sy->pass));
     }
@@ -561,27 +572,38 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
     Ring sr;
     bool ok = true;
     for (int tl = 0, gl = 0; tl < nt && ok && !sy->abort;) {
-      int w_sidx[kMaxWindow], w_gl[kMaxWindow], w_tl[kMaxWindow], w = 0;
-      for (; w < win && tl < nt; ++w) {
-        if (gl == 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]),
-                                         static_cast<uint32_t>((tl >> 1) & 1), kWaitNs)) {
-          fail_wait(sy, status, 16);
-          ok = false;
-          break;
-        }
-        const int sidx = sr.idx;
-        if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
-          fail_wait(sy, status, 4);
-          ok = false;
-          break;
-        }
-        w_sidx[w] = sidx;
-        w_gl[w] = gl;
-        w_tl[w] = tl;
-        sr.next(stages);
-        if (++gl == ng) {
-          gl = 0;
-          ++tl;
+      int w_sidx[kMaxWindow], w_acc[kMaxWindow], w_qend[kMaxWindow];
+      uint32_t w_d[kMaxWindow];
+      uint64_t w_ad[kMaxWindow], w_bd[kMaxWindow];
+      int w = 0;
+#pragma unroll
+      for (int q = 0; q < kMaxWindow; ++q) {
+        if (q < win && tl < nt && ok) {
+          if (gl == 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]),
+                                           static_cast<uint32_t>((tl >> 1) & 1), kWaitNs)) {
+            fail_wait(sy, status, 16);
+            ok = false;
+          } else {
+            const int sidx = sr.idx;
+            if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
+              fail_wait(sy, status, 4);
+              ok = false;
+            } else {
+              w_sidx[q] = sidx;
+              w_d[q] = tmem + static_cast<uint32_t>(gl * kBlockCols);
+              w_acc[q] = tl > 0;
+              w_qend[q] = gl == ng - 1 ? (tl & 1) : -1;
+              w_ad[q] = tc::sdesc(tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes),
+                                  kMnA_LBO, kMnA_SBO);
+              w_bd[q] = tc::sdesc(tc::smem_u32(qb + (tl & 1) * kQBytes), kCoreK, kCoreMN);
+              ++w;
+              sr.next(stages);
+              if (++gl == ng) {
+                gl = 0;
+                ++tl;
+              }
+            }
+          }
         }
       }
       if (!ok) break;
@@ -589,19 +611,17 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
       // K-step j: A moves by 2 point groups (4096 bytes: 256 in the descriptor), B by 256 bytes
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        for (int q = 0; q < w; ++q) {
-          const uint64_t ad =
-              tc::sdesc(tc::smem_u32(st + static_cast<size_t>(w_sidx[q]) * kStageBytes), kMnA_LBO,
-                        kMnA_SBO) + 256u * j;
-          const uint64_t bd =
-              tc::sdesc(tc::smem_u32(qb + (w_tl[q] & 1) * kQBytes), kCoreK, kCoreMN) + 16u * j;
-          tc::mma_bf16(tmem + static_cast<uint32_t>(w_gl[q] * kBlockCols), ad, bd, idesc,
-                       w_tl[q] > 0 || j > 0);
-        }
+#pragma unroll
+        for (int q = 0; q < kMaxWindow; ++q)
+          if (q < w)
+            tc::mma_bf16(w_d[q], w_ad[q] + 256u * j, w_bd[q] + 16u * j, idesc, w_acc[q] || j > 0);
       }
-      for (int q = 0; q < w; ++q) {
-        tc::mma_commit(tc::smem_u32(&sy->empty[w_sidx[q]]));
-        if (w_gl[q] == ng - 1) tc::mma_commit(tc::smem_u32(&sy->qempty[w_tl[q] & 1]));
+#pragma unroll
+      for (int q = 0; q < kMaxWindow; ++q) {
+        if (q < w) {
+          tc::mma_commit(tc::smem_u32(&sy->empty[w_sidx[q]]));
+          if (w_qend[q] >= 0) tc::mma_commit(tc::smem_u32(&sy->qempty[w_qend[q]]));
+        }
       }
     }
   } else if (tid == kLoadWarp * 32 && ng > 0) {
