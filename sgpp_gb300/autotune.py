@@ -49,7 +49,7 @@ class TunableParameter:
 
 TUNABLES: Dict[str, List[TunableParameter]] = {
     "multT16": [TunableParameter("multt_batch", [1, 2, 4])],
-    "block": [TunableParameter("block_window", [1, 2, 3]),
+    "block": [TunableParameter("block_window", [1, 2]),
               TunableParameter("block_mult_a", ["tmem", "smem"]),
               TunableParameter("block_mult_tiles", [4, 8]),
               TunableParameter("block_stages", [3, 4]),

@@ -45,11 +45,14 @@ constexpr uint64_t kWaitNs = 2000000000ull;         // a bounded wait gives up a
 constexpr uint64_t kPollNs = 4000000000ull;         // the loader's idle polling, after 4 s
 constexpr int kMaxStages = 6;
 constexpr int kMaxLoads = 12;
-constexpr int kMaxWindow = 4;  // stages the MMA thread interleaves
+constexpr int kMaxWindow = 3;  // stages the MMA thread interleaves
 // core-matrix strides of the operands: 128 bytes between neighbouring core matrices along the
 // row dimension of a chunk / K-step (8 elements), 2048 bytes between groups of 8 points or of 8
 // output columns
 constexpr uint32_t kCoreK = 128, kCoreMN = 2048;
+// operand A of multT (E^T, MN-major): core-matrix offsets along the points (K, leading) and along
+// the rows (M, strided)
+constexpr uint32_t kMnA_LBO = 2048, kMnA_SBO = 128;
 
 __host__ __device__ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
@@ -328,6 +331,105 @@ __device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int sme
 // memory, and walks the groups in passes of `gpp` groups whose coefficient rows the loader copies
 // into shared memory once the previous pass's MMAs have completed. Output: the BF16 Q tiles
 // (operand layout of block_multt) and optionally Q in FP64.
+// The MMA thread's issue of W consecutive stages: wait for each to be full, then issue their
+// K-steps round-robin (neighbouring stages feed different accumulators, and the MMAs of one
+// accumulator are serial, so interleaving keeps the tensor cores busy), then free each stage.
+// W is a compile-time constant so that the window's values stay in registers; the MMA thread's
+// issue rate bounds the kernels.
+template <int W, bool TMEM_A>
+__device__ __forceinline__ bool mult_window(Sync* sy, int* status, Ring& sr, int stages, int& u,
+                                            int& gl, int nt, bool later_pass, uint32_t tmem,
+                                            uint32_t a_col, unsigned char* st, unsigned char* cf,
+                                            uint32_t idesc) {
+  int sidx[W];
+  uint32_t d[W], a[W];
+  uint64_t ad[W], bd[W];
+  bool acc[W];
+#pragma unroll
+  for (int q = 0; q < W; ++q) {
+    sidx[q] = sr.idx;
+    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx[q]]), sr.round & 1u, kWaitNs)) {
+      fail_wait(sy, status, 4);
+      return false;
+    }
+    d[q] = tmem + static_cast<uint32_t>(u * kBlockCols);
+    acc[q] = later_pass || gl > 0;
+    bd[q] = tc::sdesc(tc::smem_u32(cf + static_cast<size_t>(gl) * kCoefBytes), kCoreK, kCoreMN);
+    a[q] = tmem + a_col + static_cast<uint32_t>(sidx[q] * 64);
+    ad[q] = tc::sdesc(tc::smem_u32(st + static_cast<size_t>(sidx[q]) * kStageBytes), kCoreK,
+                      kCoreMN);
+    sr.next(stages);
+    if (++u == nt) {
+      u = 0;
+      ++gl;
+    }
+  }
+  tc::fence_after_sync();
+  // K-step j: B moves by 2 core matrices (256 bytes: 16 in the descriptor); A by 256 bytes in
+  // shared memory, or by 8 columns in tensor memory
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+      if constexpr (TMEM_A)
+        tc::mma_bf16_ts(d[q], a[q] + 8u * j, bd[q] + 16u * j, idesc, acc[q] || j > 0);
+      else
+        tc::mma_bf16(d[q], ad[q] + 16u * j, bd[q] + 16u * j, idesc, acc[q] || j > 0);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < W; ++q) tc::mma_commit(tc::smem_u32(&sy->empty[sidx[q]]));
+  return true;
+}
+
+template <int W>
+__device__ __forceinline__ bool multt_window(Sync* sy, int* status, Ring& sr, int stages, int& tl,
+                                             int& gl, int ng, uint32_t tmem, unsigned char* st,
+                                             unsigned char* qb, uint32_t idesc) {
+  int sidx[W], qend[W];
+  uint32_t d[W];
+  uint64_t ad[W], bd[W];
+  bool acc[W];
+#pragma unroll
+  for (int q = 0; q < W; ++q) {
+    if (gl == 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]),
+                                     static_cast<uint32_t>((tl >> 1) & 1), kWaitNs)) {
+      fail_wait(sy, status, 16);
+      return false;
+    }
+    sidx[q] = sr.idx;
+    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx[q]]), sr.round & 1u, kWaitNs)) {
+      fail_wait(sy, status, 4);
+      return false;
+    }
+    d[q] = tmem + static_cast<uint32_t>(gl * kBlockCols);
+    acc[q] = tl > 0;
+    qend[q] = gl == ng - 1 ? (tl & 1) : -1;
+    ad[q] = tc::sdesc(tc::smem_u32(st + static_cast<size_t>(sidx[q]) * kStageBytes), kMnA_LBO,
+                      kMnA_SBO);
+    bd[q] = tc::sdesc(tc::smem_u32(qb + (tl & 1) * kQBytes), kCoreK, kCoreMN);
+    sr.next(stages);
+    if (++gl == ng) {
+      gl = 0;
+      ++tl;
+    }
+  }
+  tc::fence_after_sync();
+  // K-step j: A moves by 2 point groups (4096 bytes: 256 in the descriptor), B by 256 bytes
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+#pragma unroll
+    for (int q = 0; q < W; ++q)
+      tc::mma_bf16(d[q], ad[q] + 256u * j, bd[q] + 16u * j, idesc, acc[q] || j > 0);
+  }
+#pragma unroll
+  for (int q = 0; q < W; ++q) {
+    tc::mma_commit(tc::smem_u32(&sy->empty[sidx[q]]));
+    if (qend[q] >= 0) tc::mma_commit(tc::smem_u32(&sy->qempty[qend[q]]));
+  }
+  return true;
+}
+
 // TMEM_A: the A operand (the stages of E) lives in tensor memory after the accumulators, 64
 // columns per stage, instead of in shared memory.
 template <bool TMEM_A>
@@ -374,59 +476,20 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
       // different accumulators; a window of `win` stages is issued round-robin, one K-step of
       // each in turn (the MMAs of one accumulator are serial, so a lone stage left the tensor
       // cores waiting on each MMA's latency)
-      // (every loop over the window is unrolled over kMaxWindow with a guard, so that the
-      // window's values stay in registers: the MMA thread's issue rate bounds the kernel)
-      for (int u = 0, gl = 0; gl < ng && ok;) {
-        int w_sidx[kMaxWindow], w_acc[kMaxWindow];
-        uint32_t w_d[kMaxWindow], w_a[kMaxWindow];
-        uint64_t w_ad[kMaxWindow], w_bd[kMaxWindow];
-        int w = 0;
-#pragma unroll
-        for (int q = 0; q < kMaxWindow; ++q) {
-          if (q < win && gl < ng && ok) {
-            const int sidx = sr.idx;
-            if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
-              fail_wait(sy, status, 4);
-              ok = false;
-            } else {
-              w_sidx[q] = sidx;
-              w_d[q] = tmem + static_cast<uint32_t>(u * kBlockCols);
-              w_acc[q] = pass > 0 || gl > 0;
-              w_bd[q] = tc::sdesc(tc::smem_u32(cf + static_cast<size_t>(gl) * kCoefBytes), kCoreK,
-                                  kCoreMN);
-              w_a[q] = tmem + a_col + static_cast<uint32_t>(sidx * 64);
-              w_ad[q] = tc::sdesc(tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes),
-                                  kCoreK, kCoreMN);
-              ++w;
-              sr.next(stages);
-              if (++u == nt) {
-                u = 0;
-                ++gl;
-              }
-            }
-          }
+      for (int u = 0, gl = 0, left = nt * ng; left > 0 && ok;) {
+        if (win >= 3 && left >= 3) {
+          ok = mult_window<3, TMEM_A>(sy, status, sr, stages, u, gl, nt, pass > 0, tmem, a_col, st,
+                                      cf, idesc);
+          left -= 3;
+        } else if (win >= 2 && left >= 2) {
+          ok = mult_window<2, TMEM_A>(sy, status, sr, stages, u, gl, nt, pass > 0, tmem, a_col, st,
+                                      cf, idesc);
+          left -= 2;
+        } else {
+          ok = mult_window<1, TMEM_A>(sy, status, sr, stages, u, gl, nt, pass > 0, tmem, a_col, st,
+                                      cf, idesc);
+          left -= 1;
         }
-        if (!ok) break;
-        tc::fence_after_sync();
-        // K-step j: B moves by 2 core matrices (256 bytes: 16 in the descriptor); A by 256 bytes
-        // in shared memory, or by 8 columns in tensor memory
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-#pragma unroll
-          for (int q = 0; q < kMaxWindow; ++q) {
-            if (q < w) {
-              if constexpr (TMEM_A)
-                tc::mma_bf16_ts(w_d[q], w_a[q] + 8u * j, w_bd[q] + 16u * j, idesc,
-                                w_acc[q] || j > 0);
-              else
-                tc::mma_bf16(w_d[q], w_ad[q] + 16u * j, w_bd[q] + 16u * j, idesc,
-                             w_acc[q] || j > 0);
-            }
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < kMaxWindow; ++q)
-          if (q < w) tc::mma_commit(tc::smem_u32(&sy->empty[w_sidx[q]]));
       }
       tc::mma_commit(tc::smem_u32(&sy->pass));
     }
@@ -538,7 +601,6 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
 // FP64 partial rows of the stream, summed over the streams in order by block_finish_kernel.
 // Operand A (E^T, MN-major) core-matrix offsets: along the points (K, leading) and along the
 // rows (M, strided).
-constexpr uint32_t kMnA_LBO = 2048, kMnA_SBO = 128;
 
 __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
     const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
@@ -571,57 +633,16 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
     // round-robin one K-step at a time, as in the mult kernel
     Ring sr;
     bool ok = true;
-    for (int tl = 0, gl = 0; tl < nt && ok && !sy->abort;) {
-      int w_sidx[kMaxWindow], w_acc[kMaxWindow], w_qend[kMaxWindow];
-      uint32_t w_d[kMaxWindow];
-      uint64_t w_ad[kMaxWindow], w_bd[kMaxWindow];
-      int w = 0;
-#pragma unroll
-      for (int q = 0; q < kMaxWindow; ++q) {
-        if (q < win && tl < nt && ok) {
-          if (gl == 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]),
-                                           static_cast<uint32_t>((tl >> 1) & 1), kWaitNs)) {
-            fail_wait(sy, status, 16);
-            ok = false;
-          } else {
-            const int sidx = sr.idx;
-            if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx]), sr.round & 1u, kWaitNs)) {
-              fail_wait(sy, status, 4);
-              ok = false;
-            } else {
-              w_sidx[q] = sidx;
-              w_d[q] = tmem + static_cast<uint32_t>(gl * kBlockCols);
-              w_acc[q] = tl > 0;
-              w_qend[q] = gl == ng - 1 ? (tl & 1) : -1;
-              w_ad[q] = tc::sdesc(tc::smem_u32(st + static_cast<size_t>(sidx) * kStageBytes),
-                                  kMnA_LBO, kMnA_SBO);
-              w_bd[q] = tc::sdesc(tc::smem_u32(qb + (tl & 1) * kQBytes), kCoreK, kCoreMN);
-              ++w;
-              sr.next(stages);
-              if (++gl == ng) {
-                gl = 0;
-                ++tl;
-              }
-            }
-          }
-        }
-      }
-      if (!ok) break;
-      tc::fence_after_sync();
-      // K-step j: A moves by 2 point groups (4096 bytes: 256 in the descriptor), B by 256 bytes
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-#pragma unroll
-        for (int q = 0; q < kMaxWindow; ++q)
-          if (q < w)
-            tc::mma_bf16(w_d[q], w_ad[q] + 256u * j, w_bd[q] + 16u * j, idesc, w_acc[q] || j > 0);
-      }
-#pragma unroll
-      for (int q = 0; q < kMaxWindow; ++q) {
-        if (q < w) {
-          tc::mma_commit(tc::smem_u32(&sy->empty[w_sidx[q]]));
-          if (w_qend[q] >= 0) tc::mma_commit(tc::smem_u32(&sy->qempty[w_qend[q]]));
-        }
+    for (int tl = 0, gl = 0, left = nt * ng; left > 0 && ok && !sy->abort;) {
+      if (win >= 3 && left >= 3) {
+        ok = multt_window<3>(sy, status, sr, stages, tl, gl, ng, tmem, st, qb, idesc);
+        left -= 3;
+      } else if (win >= 2 && left >= 2) {
+        ok = multt_window<2>(sy, status, sr, stages, tl, gl, ng, tmem, st, qb, idesc);
+        left -= 2;
+      } else {
+        ok = multt_window<1>(sy, status, sr, stages, tl, gl, ng, tmem, st, qb, idesc);
+        left -= 1;
       }
     }
   } else if (tid == kLoadWarp * 32 && ng > 0) {

@@ -38,7 +38,7 @@ struct BlockShape {
   int mult_groups = 32;    // groups whose coefficient rows a mult CTA holds (fewer when shared
                            // memory runs out)
   int multt_groups = 16;   // groups (accumulators) per multT CTA
-  int stages = 2;          // shared-memory stages of E in flight
+  int stages = 3;          // stages of E in flight (shared or tensor memory)
   int loads = 6;           // stages of packed products in flight (bulk copies ahead of use)
   int mult_tmem = 1;       // mult keeps its A operand (the stages of E) in tensor memory
   int window = 2;          // stages whose MMAs one issue round interleaves (at most `stages`)
