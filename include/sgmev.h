@@ -239,7 +239,7 @@ SGMEV_API int sgmev_set_stream(sgmev_op* op, void* stream);
 
 /* Change launch-shape knobs of a live operator: params_json may hold only "multt_batch" and the
  * "block_mult_tiles", "block_mult_groups", "block_multt_groups", "block_stages", "block_loads",
- * "block_window", "block_mult_a" knobs (see
+ * "block_window", "block_teams", "block_mult_a" knobs (see
  * sgmev_create); they change no result bits except how the block products are cut into launches.
  * No counterpart in the reference (whose OpenCL kernels take such parameters from a
  * configuration file written by StaticParameterTuner,
@@ -266,7 +266,9 @@ SGMEV_API int64_t sgmev_kernel_launches(const sgmev_op* op);
  * Vectors are column-major: vector k of length n at offset k * n. Host buffers; blocks.
  * params "block_inner_tol" (default "1e-3"): inner tolerance of sgmev_fit_block; "block_mult_tiles",
  * "block_mult_groups", "block_multt_groups", "block_stages" (default 3), "block_loads": launch
- * shape; "block_window" (1-3, default 2): stages whose MMAs one issue round interleaves; and
+ * shape; "block_window" (1-3, default 2): stages whose MMAs one issue round interleaves;
+ * "block_teams" (1-4, default 2, at most block_stages and block_loads): producer teams of 4 warps
+ * that write alternate stages; and
  * "block_mult_a": "tmem" (default) or "smem", where the mult keeps its A operand (the autotuner's
  * choices, sgpp_gb300.autotune).
  */

@@ -30,11 +30,13 @@
 namespace sgmev {
 namespace {
 
-constexpr int kProdWarps = 8;
-constexpr int kProdThreads = kProdWarps * 32;
-constexpr int kMmaWarp = kProdWarps;         // one thread issues the MMAs
-constexpr int kLoadWarp = kProdWarps + 1;    // one thread issues the bulk copies
-constexpr int kBlockThreads = kProdThreads + 64;
+// The producers form teams of 4 warps (one warp per 32 points of a stage, the tensor-memory lanes
+// its warp may access); team t writes stages t, t + teams, t + 2 teams, ... so that the teams'
+// waits and latencies overlap. Behind the producers: one warp whose first thread issues the MMAs,
+// one whose first thread issues the bulk copies.
+constexpr int kTeamWarps = 4;
+constexpr int kMaxTeams = 4;
+constexpr int kMaxThreads = (kTeamWarps * kMaxTeams + 2) * 32;
 constexpr uint32_t kStageBytes = 128u * 16u * 16u;  // 128 points x 16 chunks x 16 bytes
 constexpr uint32_t kCoefBytes = 4096u * 2u;         // 128 rows x 32 columns of BF16
 constexpr uint32_t kQBytes = 4096u * 2u;            // 128 points x 32 columns of BF16
@@ -65,6 +67,14 @@ struct Ring {
   __device__ __forceinline__ void next(int n) {
     if (++idx == n) {
       idx = 0;
+      ++round;
+    }
+  }
+  // `by` positions on (by <= n): a team's next stage
+  __device__ __forceinline__ void step(int by, int n) {
+    idx += by;
+    if (idx >= n) {
+      idx -= n;
       ++round;
     }
   }
@@ -140,30 +150,35 @@ __device__ __forceinline__ void load_stage(unsigned char* buf, uint32_t mbar,
 // (subspace) it belongs to, as an index among the group's slots (high nibble), and which of the
 // slot's chunks it is (low nibble); 0xFF marks a chunk no slot uses. Thread (p, h) writes chunks
 // 8h .. 8h + 7 of point p: the chunk holds the point's product at element c % 8 when the point's
-// cell c in that subspace lies in it (c / 8 == the slot's chunk), zeros otherwise.
+// cell c in that subspace lies in it (c / 8 == the slot's chunk), zeros otherwise. Thread p of a
+// team writes the 16 chunks of point p.
 struct ChunkWords {
-  uint32_t w[8];  // packed product | cell << 16 of the chunk's slot, 0 for an unused chunk
-  uint32_t hdr;   // header bytes of the thread's chunks 0..3
-  uint32_t hdr2;  // and 4..7
+  uint32_t w[16];  // packed product | cell << 16 of the chunk's slot, 0 for an unused chunk
+  uint32_t hdr[4]; // header bytes of chunks 4i .. 4i + 3
 };
 
-__device__ __forceinline__ void read_chunks(ChunkWords& C, const uint32_t* lbuf, int h, int p) {
+__device__ __forceinline__ uint32_t chunk_byte(const ChunkWords& C, int i) {
+  return (C.hdr[i >> 2] >> (8 * (i & 3))) & 0xFFu;
+}
+
+__device__ __forceinline__ void read_chunks(ChunkWords& C, const uint32_t* lbuf, int p) {
   const uint4 hd = *reinterpret_cast<const uint4*>(lbuf + kHeaderAt / 4);
-  C.hdr = h ? hd.z : hd.x;
-  C.hdr2 = h ? hd.w : hd.y;
+  C.hdr[0] = hd.x;
+  C.hdr[1] = hd.y;
+  C.hdr[2] = hd.z;
+  C.hdr[3] = hd.w;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const uint32_t byte = ((i < 4 ? C.hdr : C.hdr2) >> (8 * (i & 3))) & 0xFFu;
+  for (int i = 0; i < 16; ++i) {
+    const uint32_t byte = chunk_byte(C, i);
     C.w[i] = byte == 0xFFu ? 0u : lbuf[(byte >> 4) * 128 + p];
   }
 }
 
-__device__ __forceinline__ void write_chunks(unsigned char* stage, int p, int h,
-                                             const ChunkWords& C) {
-  unsigned char* base = stage + (p >> 3) * 2048 + (p & 7) * 16 + 8 * h * 128;
+__device__ __forceinline__ void write_chunks(unsigned char* stage, int p, const ChunkWords& C) {
+  unsigned char* base = stage + (p >> 3) * 2048 + (p & 7) * 16;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const uint32_t byte = ((i < 4 ? C.hdr : C.hdr2) >> (8 * (i & 3))) & 0xFFu;
+  for (int i = 0; i < 16; ++i) {
+    const uint32_t byte = chunk_byte(C, i);
     if (byte == 0xFFu) continue;  // unused chunk: its coefficient rows are zero
     const uint32_t w = C.w[i];
     const uint32_t c = w >> 16;
@@ -175,11 +190,12 @@ __device__ __forceinline__ void write_chunks(unsigned char* stage, int p, int h,
   }
 }
 
-// The producers' part of stage i: wait for its packed products, read them, free the load buffer,
-// wait for the E stage to be free, write it, mark it full. False when a wait ran out.
+// A team's part of its next stage: wait for the packed products, read them, free the load
+// buffer, wait for the E stage to be free, write it, mark it full, step both rings past the
+// other teams' stages. False when a wait ran out.
 __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st,
                                         unsigned char* lb, Ring& lr, int loads, Ring& sr,
-                                        int stages, int p, int h) {
+                                        int stages, int p, int teams) {
   const int b = lr.idx;
   // the warp's lanes decide together (a lane that gave up alone would leave the others waiting
   // at the warp's synchronisation below)
@@ -189,12 +205,12 @@ __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st
     return false;
   }
   ChunkWords C;
-  read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes), h, p);
-  // one arrival per warp (the barriers count warps): 256 arrivals on one word per stage
+  read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes), p);
+  // one arrival per warp (the barriers count warps): 128 arrivals on one word per stage
   // serialised on the shared-memory atomics
   __syncwarp();
   if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
-  lr.next(loads);
+  lr.step(teams, loads);
   const int sidx = sr.idx;
   const bool free_stage =
       sr.round == 0 ||
@@ -203,22 +219,22 @@ __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st
     fail_wait(sy, status, 2);
     return false;
   }
-  write_chunks(st + static_cast<size_t>(sidx) * kStageBytes, p, h, C);
+  write_chunks(st + static_cast<size_t>(sidx) * kStageBytes, p, C);
   tc::fence_proxy_async();
   __syncwarp();
   if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
-  sr.next(stages);
+  sr.step(teams, stages);
   return true;
 }
 
 // produce() for the mult kernel's tensor-memory A operand: the stage's rows go to tensor memory
-// (lane = point, 4 columns per chunk: the chunk's 8 BF16 elements as 4 pairs) with one 32-column
-// store per thread instead of shared memory, so the tensor cores read A without the shared-memory
-// traffic of writing and reading it. All 8 chunks are written (zeros included), which also
-// overwrites whatever an earlier group left in the columns.
+// (lane = point, 4 columns per chunk: the chunk's 8 BF16 elements as 4 pairs) with two 32-column
+// stores per thread instead of shared memory, so the tensor cores read A without the
+// shared-memory traffic of writing and reading it. All 16 chunks are written (zeros included),
+// which also overwrites whatever an earlier group left in the columns.
 __device__ __forceinline__ bool produce_tmem(Sync* sy, int* status, unsigned char* lb, Ring& lr,
                                              int loads, Ring& sr, int stages, uint32_t a_taddr,
-                                             int p, int h) {
+                                             int p, int teams) {
   const int b = lr.idx;
   if (!__all_sync(0xffffffffu, tc::mbar_wait_ns(tc::smem_u32(&sy->lfull[b]), lr.round & 1u,
                                                 kWaitNs))) {
@@ -226,10 +242,10 @@ __device__ __forceinline__ bool produce_tmem(Sync* sy, int* status, unsigned cha
     return false;
   }
   ChunkWords C;
-  read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes), h, p);
+  read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes), p);
   __syncwarp();
   if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
-  lr.next(loads);
+  lr.step(teams, loads);
   const int sidx = sr.idx;
   const bool free_stage =
       sr.round == 0 ||
@@ -238,29 +254,32 @@ __device__ __forceinline__ bool produce_tmem(Sync* sy, int* status, unsigned cha
     fail_wait(sy, status, 2);
     return false;
   }
-  uint32_t r[32];
+  // lanes 32 (warp % 4) ...; chunks 8 h .. 8 h + 7 are columns 32 h .. 32 h + 31 of the stage
+  const uint32_t at = a_taddr + (static_cast<uint32_t>((threadIdx.x >> 5) & 3) << 21) +
+                      static_cast<uint32_t>(sidx * 64);
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const uint32_t byte = ((i < 4 ? C.hdr : C.hdr2) >> (8 * (i & 3))) & 0xFFu;
-    const uint32_t w = C.w[i];
-    const uint32_t c = w >> 16;
-    const uint32_t v = byte != 0xFFu && (c >> 3) == (byte & 0xFu) ? (w & 0xFFFFu) : 0u;
-    const uint32_t val = v << ((c & 1u) * 16u);
-    const uint32_t wd = (c >> 1) & 3u;
-    r[4 * i + 0] = wd == 0 ? val : 0u;
-    r[4 * i + 1] = wd == 1 ? val : 0u;
-    r[4 * i + 2] = wd == 2 ? val : 0u;
-    r[4 * i + 3] = wd == 3 ? val : 0u;
+  for (int h = 0; h < 2; ++h) {
+    uint32_t r[32];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const uint32_t byte = chunk_byte(C, 8 * h + i);
+      const uint32_t w = C.w[8 * h + i];
+      const uint32_t c = w >> 16;
+      const uint32_t v = byte != 0xFFu && (c >> 3) == (byte & 0xFu) ? (w & 0xFFFFu) : 0u;
+      const uint32_t val = v << ((c & 1u) * 16u);
+      const uint32_t wd = (c >> 1) & 3u;
+      r[4 * i + 0] = wd == 0 ? val : 0u;
+      r[4 * i + 1] = wd == 1 ? val : 0u;
+      r[4 * i + 2] = wd == 2 ? val : 0u;
+      r[4 * i + 3] = wd == 3 ? val : 0u;
+    }
+    tc::tmem_st32(at + 32u * h, r);
   }
-  // lanes 32 (warp % 4) ...; this half's 8 chunks are columns 32 h .. 32 h + 31 of the stage
-  tc::tmem_st32(a_taddr + (static_cast<uint32_t>((threadIdx.x >> 5) & 3) << 21) +
-                    static_cast<uint32_t>(sidx * 64 + 32 * h),
-                r);
   tc::tmem_wait_st();
   tc::fence_before_sync();
   __syncwarp();
   if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
-  sr.next(stages);
+  sr.step(teams, stages);
   return true;
 }
 
@@ -296,18 +315,19 @@ __device__ __forceinline__ void drain_loads(Sync* sy, int* status, int loads, in
 // Shared set-up of both kernels: zeroed E stages (rows a group leaves unused must hold finite
 // values), barriers, tensor memory.
 __device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int smem_stages,
-                                            int stages, int loads, uint32_t tmem_cols) {
+                                            int stages, int loads, uint32_t tmem_cols,
+                                            int mma_warp) {
   const int tid = threadIdx.x;
   for (uint32_t k = tid; k < static_cast<uint32_t>(smem_stages) * kStageBytes / 16u; k += blockDim.x)
     reinterpret_cast<uint4*>(st)[k] = make_uint4(0u, 0u, 0u, 0u);
   if (tid == 0) {
     for (int k = 0; k < stages; ++k) {
-      tc::mbar_init(tc::smem_u32(&sy->full[k]), kProdWarps);
+      tc::mbar_init(tc::smem_u32(&sy->full[k]), kTeamWarps);
       tc::mbar_init(tc::smem_u32(&sy->empty[k]), 1);
     }
     for (int k = 0; k < loads; ++k) {
       tc::mbar_init(tc::smem_u32(&sy->lfull[k]), 1);
-      tc::mbar_init(tc::smem_u32(&sy->lempty[k]), kProdWarps);
+      tc::mbar_init(tc::smem_u32(&sy->lempty[k]), kTeamWarps);
     }
     for (int k = 0; k < 2; ++k) {
       tc::mbar_init(tc::smem_u32(&sy->qfull[k]), 1);
@@ -319,7 +339,7 @@ __device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int sme
     sy->abort = 0;
     tc::mbar_init_fence();
   }
-  if ((tid >> 5) == kMmaWarp) tc::tmem_alloc(tc::smem_u32(&sy->tmem), tmem_cols);
+  if ((tid >> 5) == mma_warp) tc::tmem_alloc(tc::smem_u32(&sy->tmem), tmem_cols);
   tc::fence_proxy_async();
   tc::fence_before_sync();
   __syncthreads();
@@ -433,10 +453,10 @@ __device__ __forceinline__ bool multt_window(Sync* sy, int* status, Ring& sr, in
 // TMEM_A: the A operand (the stages of E) lives in tensor memory after the accumulators, 64
 // columns per stage, instead of in shared memory.
 template <bool TMEM_A>
-__global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
+__global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
     const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
     const int2* __restrict__ gslots, const uint16_t* __restrict__ coef, int n_groups, int n_slots, int64_t mpad, int64_t m, int n_tiles,
-    int tiles, int gpp, int stages, int loads, int win, uint32_t tmem_cols, uint16_t* __restrict__ qtiles,
+    int tiles, int gpp, int teams, int stages, int loads, int win, uint32_t tmem_cols, uint16_t* __restrict__ qtiles,
     double* __restrict__ out64, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int smem_stages = TMEM_A ? 0 : stages;
@@ -448,22 +468,21 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
   const int t0 = blockIdx.x * tiles;
   const int nt = min(tiles, n_tiles - t0);
   const int passes = static_cast<int>(cdiv(n_groups, gpp));
-  block_setup(sy, st, smem_stages, stages, loads, tmem_cols);
+  const int prod_warps = kTeamWarps * teams, mma_warp = prod_warps, load_warp = prod_warps + 1;
+  block_setup(sy, st, smem_stages, stages, loads, tmem_cols, mma_warp);
   const uint32_t tmem = sy->tmem;
   const uint32_t a_col = static_cast<uint32_t>(tiles * kBlockCols);  // first A column (TMEM_A)
   const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, false, false);
 
-  if (tid < kProdThreads) {
-    const int p = tid & 127, h = tid >> 7;
-    Ring lr, sr;
+  if (warp < prod_warps) {
+    // the stages of all passes in order (the passes matter only to the MMA thread and the loader)
+    const int p = tid & 127, team = warp >> 2;
+    Ring lr{team, 0u}, sr{team, 0u};
     bool ok = true;
-    for (int pass = 0; pass < passes && ok && !sy->abort; ++pass) {
-      const int ng = min(n_groups, pass * gpp + gpp) - pass * gpp;
-      for (int k = 0; k < nt * ng && ok; ++k)
-        ok = TMEM_A ? produce_tmem(sy, status, lb, lr, loads, sr, stages, tmem + a_col, p, h)
-                    : produce(sy, status, st, lb, lr, loads, sr, stages, p, h);
-    }
-  } else if (tid == kMmaWarp * 32) {
+    for (int k = team; k < nt * n_groups && ok && !sy->abort; k += teams)
+      ok = TMEM_A ? produce_tmem(sy, status, lb, lr, loads, sr, stages, tmem + a_col, p, teams)
+                  : produce(sy, status, st, lb, lr, loads, sr, stages, p, teams);
+  } else if (tid == mma_warp * 32) {
     Ring sr;
     bool ok = true;
     for (int pass = 0; pass < passes && ok && !sy->abort; ++pass) {
@@ -493,7 +512,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
       }
       tc::mma_commit(tc::smem_u32(&sy->pass));
     }
-  } else if (tid == kLoadWarp * 32) {
+  } else if (tid == load_warp * 32) {
     // The loader interleaves two streams of copies without blocking on either: the packed
     // products of the next stage (as soon as its load buffer is free) and the coefficient rows of
     // the next pass (as soon as the last pass's MMAs have completed). Waiting for one while the
@@ -555,18 +574,18 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
       atomicOr(status, 128);
   }
   // every MMA of the CTA has completed once the last commit has
-  if (tid == kMmaWarp * 32) {
+  if (tid == mma_warp * 32) {
     tc::mma_commit(tc::smem_u32(&sy->last));
     if (!tc::mbar_wait_ns(tc::smem_u32(&sy->last), 0, kWaitNs)) fail_wait(sy, status, 8);
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (!sy->abort && warp < kProdWarps) {
-    // warps 0-3 read the even tiles, warps 4-7 the odd ones; lane = point of the tile
+  if (!sy->abort && warp < prod_warps) {
+    // team t reads tiles t, t + teams, ...; lane = point of the tile
     const int quarter = warp & 3;
     const int p = quarter * 32 + lane;
-    for (int u = warp >> 2; u < nt; u += 2) {
+    for (int u = warp >> 2; u < nt; u += teams) {
       uint32_t r0[16], r1[16];
       const uint32_t ta = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
                           static_cast<uint32_t>(u * kBlockCols);
@@ -591,7 +610,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == kMmaWarp) tc::tmem_dealloc(tmem, tmem_cols);
+  if (warp == mma_warp) tc::tmem_dealloc(tmem, tmem_cols);
 }
 
 // ---- multT: R[group] = sum over tiles of E[tile][group]^T Q[tile] -----------------------------
@@ -602,10 +621,10 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_mult_kernel(
 // Operand A (E^T, MN-major) core-matrix offsets: along the points (K, leading) and along the
 // rows (M, strided).
 
-__global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
+__global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
     const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
     const int2* __restrict__ gslots, const uint16_t* __restrict__ qtiles, int n_groups, int n_slots, int64_t mpad, int n_tiles, int gpc,
-    int streams, int stages, int loads, int win, uint32_t tmem_cols, int64_t rows,
+    int streams, int teams, int stages, int loads, int win, uint32_t tmem_cols, int64_t rows,
     double* __restrict__ part, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* st = smem;
@@ -618,17 +637,18 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
   const int ta = static_cast<int>(static_cast<int64_t>(stream) * n_tiles / streams);
   const int tb = static_cast<int>(static_cast<int64_t>(stream + 1) * n_tiles / streams);
   const int64_t total = ng > 0 ? static_cast<int64_t>(tb - ta) * ng : 0;
-  block_setup(sy, st, stages, stages, loads, tmem_cols);
+  const int prod_warps = kTeamWarps * teams, mma_warp = prod_warps, load_warp = prod_warps + 1;
+  block_setup(sy, st, stages, stages, loads, tmem_cols, mma_warp);
   const uint32_t tmem = sy->tmem;
   const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, true, false);
 
   const int nt = tb - ta;
-  if (tid < kProdThreads && ng > 0) {
-    const int p = tid & 127, h = tid >> 7;
-    Ring lr, sr;
-    for (int64_t k = 0; k < total && !sy->abort; ++k)
-      if (!produce(sy, status, st, lb, lr, loads, sr, stages, p, h)) break;
-  } else if (tid == kMmaWarp * 32 && ng > 0) {
+  if (warp < prod_warps && ng > 0) {
+    const int p = tid & 127, team = warp >> 2;
+    Ring lr{team, 0u}, sr{team, 0u};
+    for (int64_t k = team; k < total && !sy->abort; k += teams)
+      if (!produce(sy, status, st, lb, lr, loads, sr, stages, p, teams)) break;
+  } else if (tid == mma_warp * 32 && ng > 0) {
     // windows of `win` consecutive stages (groups inner: different accumulators), issued
     // round-robin one K-step at a time, as in the mult kernel
     Ring sr;
@@ -645,7 +665,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
         left -= 1;
       }
     }
-  } else if (tid == kLoadWarp * 32 && ng > 0) {
+  } else if (tid == load_warp * 32 && ng > 0) {
     // Q of tile tl waits only for the MMAs of tile tl - 2, whose stages were loaded before: the
     // loader may block on either kind of wait without stalling the pipeline for good
     int64_t issued = 0;
@@ -675,17 +695,17 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
                             kWaitNs))
         atomicOr(status, 128);
   }
-  if (tid == kMmaWarp * 32) {
+  if (tid == mma_warp * 32) {
     tc::mma_commit(tc::smem_u32(&sy->last));
     if (!tc::mbar_wait_ns(tc::smem_u32(&sy->last), 0, kWaitNs)) fail_wait(sy, status, 8);
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (!sy->abort && warp < kProdWarps) {
+  if (!sy->abort && warp < prod_warps) {
     const int quarter = warp & 3;
     const int r = quarter * 32 + lane;
-    for (int gl = warp >> 2; gl < ng; gl += 2) {
+    for (int gl = warp >> 2; gl < ng; gl += teams) {
       uint32_t r0[16], r1[16];
       const uint32_t ta2 = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
                            static_cast<uint32_t>(gl * kBlockCols);
@@ -704,7 +724,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_multt_kernel(
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == kMmaWarp) tc::tmem_dealloc(tmem, tmem_cols);
+  if (warp == mma_warp) tc::tmem_dealloc(tmem, tmem_cols);
 }
 
 // out[c][gp] = sum over streams (in order) of the partial rows + scale * add[c][gp]
@@ -1000,7 +1020,8 @@ void block_free(BlockPlan* b) {
 
 bool block_shape_ok(const BlockShape& sh, int smem_cap) {
   return sh.stages >= 2 && sh.stages <= kMaxStages && sh.loads >= 2 && sh.loads <= kMaxLoads &&
-         sh.window >= 1 && sh.window <= kMaxWindow &&
+         sh.window >= 1 && sh.window <= kMaxWindow && sh.teams >= 1 && sh.teams <= kMaxTeams &&
+         sh.teams <= sh.stages && sh.teams <= sh.loads &&
          sh.mult_tiles >= 1 && sh.mult_tiles <= 16 && mult_tmem_need(sh) <= 512 &&
          sh.mult_groups >= 1 && sh.multt_groups >= 1 && sh.multt_groups <= 16 &&
          mult_smem(sh, mult_groups_fit(sh, smem_cap)) <= static_cast<size_t>(smem_cap) &&
@@ -1144,9 +1165,9 @@ cudaError_t block_mult(BlockPlan& b, cudaStream_t s, const double* p, int64_t np
   if (e != cudaSuccess) return e;
   const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
   const unsigned ctas = static_cast<unsigned>(cdiv(n_tiles, sh.mult_tiles));
-  kern<<<ctas, kBlockThreads, smem, s>>>(
+  kern<<<ctas, (kTeamWarps * sh.teams + 2) * 32, smem, s>>>(
       b.pc, b.gheader, b.gslots, b.coef, b.n_groups, b.n_slots, b.mpad, b.m, n_tiles, sh.mult_tiles,
-      gpp, sh.stages, sh.loads, std::min(sh.window, sh.stages), cols, b.qtiles, out64, b.status);
+      gpp, sh.teams, sh.stages, sh.loads, std::min(sh.window, sh.stages), cols, b.qtiles, out64, b.status);
   return cudaGetLastError();
 }
 
@@ -1169,9 +1190,10 @@ cudaError_t block_multt(BlockPlan& b, cudaStream_t s, const double* v, int64_t n
   const int passes = static_cast<int>(cdiv(b.n_groups, sh.multt_groups));
   const int streams = std::min(b.part_streams, multt_streams(b, num_sms));
   const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
-  block_multt_kernel<<<static_cast<unsigned>(passes * streams), kBlockThreads, smem, s>>>(
+  block_multt_kernel<<<static_cast<unsigned>(passes * streams), (kTeamWarps * sh.teams + 2) * 32,
+                       smem, s>>>(
       b.pc, b.gheader, b.gslots, b.qtiles, b.n_groups, b.n_slots, b.mpad, n_tiles, sh.multt_groups,
-      streams, sh.stages, sh.loads, std::min(sh.window, sh.stages), cols, b.rows, b.part, b.status);
+      streams, sh.teams, sh.stages, sh.loads, std::min(sh.window, sh.stages), cols, b.rows, b.part, b.status);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   block_finish_kernel<<<grid_for(npad * kBlockRhs, num_sms), 256, 0, s>>>(

@@ -1207,10 +1207,10 @@ static int apply_shape_params(sgmev_op* op, const char* params_json) {
   }
   BlockShape sh = op->blk_shape;
   const char* knobs[] = {"block_mult_tiles", "block_mult_groups", "block_multt_groups",
-                         "block_stages", "block_loads", "block_window"};
+                         "block_stages", "block_loads", "block_window", "block_teams"};
   int* fields[] = {&sh.mult_tiles, &sh.mult_groups, &sh.multt_groups, &sh.stages, &sh.loads,
-                   &sh.window};
-  for (int k = 0; k < 6; ++k) {
+                   &sh.window, &sh.teams};
+  for (int k = 0; k < 7; ++k) {
     const std::string v = json_string(params_json, knobs[k]);
     if (v.empty()) continue;
     char* end = nullptr;
@@ -1499,7 +1499,7 @@ SGMEV_API int sgmev_set_params(sgmev_op* op, const char* params_json) {
   if (!params_json) return SGMEV_OK;
   static const char* allowed[] = {"multt_batch", "block_mult_tiles", "block_mult_groups",
                                   "block_multt_groups", "block_stages", "block_loads",
-                                  "block_mult_a", "block_window"};
+                                  "block_mult_a", "block_window", "block_teams"};
   // every key must be a launch-shape knob
   for (const char* c = params_json; (c = std::strchr(c, '"')) != nullptr;) {
     const char* e = std::strchr(c + 1, '"');

@@ -167,3 +167,23 @@ def test_interleaved_mma_window_gives_the_same_bits(window):
         op.close()
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("teams", ["1", "3", "4"])
+def test_producer_teams_give_the_same_bits(teams):
+    """block_teams: teams of 4 producer warps write alternate stages; every stage still holds the
+    same values and the MMAs consume the stages in the same order, so the results are identical."""
+    rng = np.random.default_rng(62)
+    grid = _grid(6, 4)
+    x = rng.random((20000, 6))
+    a = rng.standard_normal((K, grid.getSize()))
+    v = rng.standard_normal((K, x.shape[0]))
+    out = []
+    for t in ("2", teams):
+        for where in ("tmem", "smem"):
+            op = _op(grid, x, block_teams=t, block_stages=4, block_mult_a=where)
+            out.append((op.multBlock(a), op.multTransposeBlock(v)))
+            op.close()
+    for o in out[1:]:
+        np.testing.assert_array_equal(out[0][0], o[0])
+        np.testing.assert_array_equal(out[0][1], o[1])
