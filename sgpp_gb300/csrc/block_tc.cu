@@ -100,6 +100,21 @@ __device__ __forceinline__ void fail_wait(Sync* sy, int* status, int code) {
   atomicOr(status, code);
 }
 
+// The MMA warp's decisions are warp-uniform (its lanes run one loop together): a bounded wait
+// that every lane passed, and the abort flag as lane 0 read it.
+__device__ __forceinline__ bool warp_wait(uint32_t mbar, uint32_t parity) {
+  return __all_sync(0xffffffffu, tc::mbar_wait_ns(mbar, parity, kWaitNs));
+}
+__device__ __forceinline__ bool warp_aborted(const Sync* sy) {
+  return __shfl_sync(0xffffffffu, sy->abort, 0) != 0;
+}
+// lane 0's non-blocking test, for the whole warp
+__device__ __forceinline__ bool warp_poll(uint32_t mbar, uint32_t parity) {
+  bool done = false;
+  if ((threadIdx.x & 31) == 0) done = tc::mbar_poll(mbar, parity);
+  return __shfl_sync(0xffffffffu, done, 0);
+}
+
 // BF16 high/low split: v = hi + lo to about 16 significant bits
 __device__ __forceinline__ void split_bf16(float v, uint16_t* hi, uint16_t* lo) {
   const __nv_bfloat16 h = __float2bfloat16_rn(v);
@@ -283,20 +298,23 @@ __device__ __forceinline__ bool produce_tmem(Sync* sy, int* status, unsigned cha
   return true;
 }
 
-// The loader's part of a stage: wait for the load buffer to be free, issue the bulk copies.
+// The loader warp's part of a stage: wait for the load buffer to be free, issue the bulk copies
+// from the elected lane (copies issued by a lone thread of a diverged warp had left the loader
+// busy for most of a stage).
 __device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, Ring& lr, int loads,
                                      const uint32_t* __restrict__ pc,
                                      const int2* __restrict__ gslots,
                                      const uint4* __restrict__ gheader, int n_slots, int group,
                                      int64_t tile) {
   const int b = lr.idx;
-  if (lr.round > 0 &&
-      !tc::mbar_wait_ns(tc::smem_u32(&sy->lempty[b]), (lr.round - 1u) & 1u, kWaitNs)) {
+  if (lr.round > 0 && !warp_wait(tc::smem_u32(&sy->lempty[b]), (lr.round - 1u) & 1u)) {
     fail_wait(sy, status, 64);
     return false;
   }
-  load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc, gslots,
-             gheader, n_slots, group, tile);
+  if (tc::elect_one())
+    load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc, gslots,
+               gheader, n_slots, group, tile);
+  __syncwarp();
   lr.next(loads);
   return true;
 }
@@ -306,8 +324,8 @@ __device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, R
 __device__ __forceinline__ void drain_loads(Sync* sy, int* status, int loads, int64_t issued) {
   for (int64_t i = issued > loads ? issued - loads : 0; i < issued; ++i) {
     const int b = static_cast<int>(i % loads);
-    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((i / loads) & 1),
-                       kWaitNs))
+    if (!warp_wait(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((i / loads) & 1)) &&
+        (threadIdx.x & 31) == 0)
       atomicOr(status, 128);
   }
 }
@@ -351,11 +369,10 @@ __device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int sme
 // memory, and walks the groups in passes of `gpp` groups whose coefficient rows the loader copies
 // into shared memory once the previous pass's MMAs have completed. Output: the BF16 Q tiles
 // (operand layout of block_multt) and optionally Q in FP64.
-// The MMA thread's issue of W consecutive stages: wait for each to be full, then issue their
-// K-steps round-robin (neighbouring stages feed different accumulators, and the MMAs of one
-// accumulator are serial, so interleaving keeps the tensor cores busy), then free each stage.
-// W is a compile-time constant so that the window's values stay in registers; the MMA thread's
-// issue rate bounds the kernels.
+// The MMA warp's issue of W consecutive stages: wait for each to be full, then issue their
+// K-steps round-robin (neighbouring stages feed different accumulators), then free each stage.
+// W is a compile-time constant so that the window's values stay in registers and the MMAs are
+// one straight run; the elected lane issues them.
 template <int W, bool TMEM_A>
 __device__ __forceinline__ bool mult_window(Sync* sy, int* status, Ring& sr, int stages, int& u,
                                             int& gl, int nt, bool later_pass, uint32_t tmem,
@@ -368,7 +385,7 @@ __device__ __forceinline__ bool mult_window(Sync* sy, int* status, Ring& sr, int
 #pragma unroll
   for (int q = 0; q < W; ++q) {
     sidx[q] = sr.idx;
-    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx[q]]), sr.round & 1u, kWaitNs)) {
+    if (!warp_wait(tc::smem_u32(&sy->full[sidx[q]]), sr.round & 1u)) {
       fail_wait(sy, status, 4);
       return false;
     }
@@ -391,14 +408,20 @@ __device__ __forceinline__ bool mult_window(Sync* sy, int* status, Ring& sr, int
   for (int j = 0; j < 8; ++j) {
 #pragma unroll
     for (int q = 0; q < W; ++q) {
-      if constexpr (TMEM_A)
-        tc::mma_bf16_ts(d[q], a[q] + 8u * j, bd[q] + 16u * j, idesc, acc[q] || j > 0);
-      else
-        tc::mma_bf16(d[q], ad[q] + 16u * j, bd[q] + 16u * j, idesc, acc[q] || j > 0);
+      if (tc::elect_one()) {
+        if constexpr (TMEM_A)
+          tc::mma_bf16_ts(d[q], a[q] + 8u * j, bd[q] + 16u * j, idesc, acc[q] || j > 0);
+        else
+          tc::mma_bf16(d[q], ad[q] + 16u * j, bd[q] + 16u * j, idesc, acc[q] || j > 0);
+      }
+      __syncwarp();
     }
   }
+  if (tc::elect_one()) {
 #pragma unroll
-  for (int q = 0; q < W; ++q) tc::mma_commit(tc::smem_u32(&sy->empty[sidx[q]]));
+    for (int q = 0; q < W; ++q) tc::mma_commit(tc::smem_u32(&sy->empty[sidx[q]]));
+  }
+  __syncwarp();
   return true;
 }
 
@@ -412,13 +435,13 @@ __device__ __forceinline__ bool multt_window(Sync* sy, int* status, Ring& sr, in
   bool acc[W];
 #pragma unroll
   for (int q = 0; q < W; ++q) {
-    if (gl == 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]),
-                                     static_cast<uint32_t>((tl >> 1) & 1), kWaitNs)) {
+    if (gl == 0 &&
+        !warp_wait(tc::smem_u32(&sy->qfull[tl & 1]), static_cast<uint32_t>((tl >> 1) & 1))) {
       fail_wait(sy, status, 16);
       return false;
     }
     sidx[q] = sr.idx;
-    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->full[sidx[q]]), sr.round & 1u, kWaitNs)) {
+    if (!warp_wait(tc::smem_u32(&sy->full[sidx[q]]), sr.round & 1u)) {
       fail_wait(sy, status, 4);
       return false;
     }
@@ -439,14 +462,20 @@ __device__ __forceinline__ bool multt_window(Sync* sy, int* status, Ring& sr, in
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
 #pragma unroll
-    for (int q = 0; q < W; ++q)
-      tc::mma_bf16(d[q], ad[q] + 256u * j, bd[q] + 16u * j, idesc, acc[q] || j > 0);
+    for (int q = 0; q < W; ++q) {
+      if (tc::elect_one())
+        tc::mma_bf16(d[q], ad[q] + 256u * j, bd[q] + 16u * j, idesc, acc[q] || j > 0);
+      __syncwarp();
+    }
   }
+  if (tc::elect_one()) {
 #pragma unroll
-  for (int q = 0; q < W; ++q) {
-    tc::mma_commit(tc::smem_u32(&sy->empty[sidx[q]]));
-    if (qend[q] >= 0) tc::mma_commit(tc::smem_u32(&sy->qempty[qend[q]]));
+    for (int q = 0; q < W; ++q) {
+      tc::mma_commit(tc::smem_u32(&sy->empty[sidx[q]]));
+      if (qend[q] >= 0) tc::mma_commit(tc::smem_u32(&sy->qempty[qend[q]]));
+    }
   }
+  __syncwarp();
   return true;
 }
 
@@ -479,15 +508,15 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
     const int p = tid & 127, team = warp >> 2;
     Ring lr{team, 0u}, sr{team, 0u};
     bool ok = true;
-    for (int k = team; k < nt * n_groups && ok && !sy->abort; k += teams)
+    for (int k = team; k < nt * n_groups && ok && !warp_aborted(sy); k += teams)
       ok = TMEM_A ? produce_tmem(sy, status, lb, lr, loads, sr, stages, tmem + a_col, p, teams)
                   : produce(sy, status, st, lb, lr, loads, sr, stages, p, teams);
-  } else if (tid == mma_warp * 32) {
+  } else if (warp == mma_warp) {
     Ring sr;
     bool ok = true;
-    for (int pass = 0; pass < passes && ok && !sy->abort; ++pass) {
+    for (int pass = 0; pass < passes && ok && !warp_aborted(sy); ++pass) {
       const int ng = min(n_groups, pass * gpp + gpp) - pass * gpp;
-      if (!tc::mbar_wait_ns(tc::smem_u32(&sy->cfull), static_cast<uint32_t>(pass & 1), kWaitNs)) {
+      if (!warp_wait(tc::smem_u32(&sy->cfull), static_cast<uint32_t>(pass & 1))) {
         fail_wait(sy, status, 1);
         break;
       }
@@ -510,20 +539,25 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
           left -= 1;
         }
       }
-      tc::mma_commit(tc::smem_u32(&sy->pass));
+      if (tc::elect_one()) tc::mma_commit(tc::smem_u32(&sy->pass));
+      __syncwarp();
     }
-  } else if (tid == load_warp * 32) {
-    // The loader interleaves two streams of copies without blocking on either: the packed
+  } else if (warp == load_warp) {
+    // The loader warp interleaves two streams of copies without blocking on either: the packed
     // products of the next stage (as soon as its load buffer is free) and the coefficient rows of
     // the next pass (as soon as the last pass's MMAs have completed). Waiting for one while the
-    // other is due could stall the MMA thread on coefficients that are never issued.
+    // other is due could stall the MMA warp on coefficients that are never issued. Its lanes run
+    // the loop together; the elected lane issues the copies.
     auto issue_coef = [&](int pass) {
       const int g0 = pass * gpp, ng = min(n_groups, g0 + gpp) - g0;
-      const uint32_t cb = tc::smem_u32(&sy->cfull);
-      bulk_expect(cb, static_cast<uint32_t>(ng) * kCoefBytes);
-      for (int g = 0; g < ng; ++g)
-        bulk_copy(tc::smem_u32(cf + static_cast<size_t>(g) * kCoefBytes),
-                  coef + static_cast<int64_t>(g0 + g) * 4096, kCoefBytes, cb);
+      if (tc::elect_one()) {
+        const uint32_t cb = tc::smem_u32(&sy->cfull);
+        bulk_expect(cb, static_cast<uint32_t>(ng) * kCoefBytes);
+        for (int g = 0; g < ng; ++g)
+          bulk_copy(tc::smem_u32(cf + static_cast<size_t>(g) * kCoefBytes),
+                    coef + static_cast<int64_t>(g0 + g) * 4096, kCoefBytes, cb);
+      }
+      __syncwarp();
     };
     issue_coef(0);
     int coef_next = 1;
@@ -532,18 +566,20 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
     int lpass = 0, lu = 0, lg = 0;      // the next stage's pass, group within the pass and tile
     int lng = min(n_groups, gpp);       // groups of that pass
     uint64_t idle_since = 0;
-    while (!sy->abort && (lpass < passes || coef_next < passes)) {
+    while (!warp_aborted(sy) && (lpass < passes || coef_next < passes)) {
       bool progress = false;
       if (coef_next < passes &&
-          tc::mbar_poll(tc::smem_u32(&sy->pass), static_cast<uint32_t>((coef_next - 1) & 1))) {
+          warp_poll(tc::smem_u32(&sy->pass), static_cast<uint32_t>((coef_next - 1) & 1))) {
         issue_coef(coef_next++);
         progress = true;
       }
       if (lpass < passes) {
         const int b = lr.idx;
-        if (lr.round == 0 || tc::mbar_poll(tc::smem_u32(&sy->lempty[b]), (lr.round - 1u) & 1u)) {
-          load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc,
-                     gslots, gheader, n_slots, lpass * gpp + lg, t0 + lu);
+        if (lr.round == 0 || warp_poll(tc::smem_u32(&sy->lempty[b]), (lr.round - 1u) & 1u)) {
+          if (tc::elect_one())
+            load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc,
+                       gslots, gheader, n_slots, lpass * gpp + lg, t0 + lu);
+          __syncwarp();
           lr.next(loads);
           ++next;
           if (++lu == nt) {
@@ -564,19 +600,21 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
       __nanosleep(64);  // leave the issue slots to the producers
       const uint64_t now = tc::globaltimer_ns();
       if (idle_since == 0) idle_since = now;
-      if (now - idle_since > kPollNs) {
+      if (__shfl_sync(0xffffffffu, now - idle_since > kPollNs, 0)) {
         fail_wait(sy, status, 64);
         break;
       }
     }
     drain_loads(sy, status, loads, next);
-    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->cfull), static_cast<uint32_t>((coef_next - 1) & 1), kWaitNs))
+    if (!warp_wait(tc::smem_u32(&sy->cfull), static_cast<uint32_t>((coef_next - 1) & 1)) &&
+        lane == 0)
       atomicOr(status, 128);
   }
   // every MMA of the CTA has completed once the last commit has
-  if (tid == mma_warp * 32) {
-    tc::mma_commit(tc::smem_u32(&sy->last));
-    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->last), 0, kWaitNs)) fail_wait(sy, status, 8);
+  if (warp == mma_warp) {
+    if (tc::elect_one()) tc::mma_commit(tc::smem_u32(&sy->last));
+    __syncwarp();
+    if (!warp_wait(tc::smem_u32(&sy->last), 0)) fail_wait(sy, status, 8);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -646,14 +684,14 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
   if (warp < prod_warps && ng > 0) {
     const int p = tid & 127, team = warp >> 2;
     Ring lr{team, 0u}, sr{team, 0u};
-    for (int64_t k = team; k < total && !sy->abort; k += teams)
+    for (int64_t k = team; k < total && !warp_aborted(sy); k += teams)
       if (!produce(sy, status, st, lb, lr, loads, sr, stages, p, teams)) break;
-  } else if (tid == mma_warp * 32 && ng > 0) {
+  } else if (warp == mma_warp && ng > 0) {
     // windows of `win` consecutive stages (groups inner: different accumulators), issued
     // round-robin one K-step at a time, as in the mult kernel
     Ring sr;
     bool ok = true;
-    for (int tl = 0, gl = 0, left = nt * ng; left > 0 && ok && !sy->abort;) {
+    for (int tl = 0, gl = 0, left = nt * ng; left > 0 && ok && !warp_aborted(sy);) {
       if (win >= 3 && left >= 3) {
         ok = multt_window<3>(sy, status, sr, stages, tl, gl, ng, tmem, st, qb, idesc);
         left -= 3;
@@ -665,24 +703,27 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
         left -= 1;
       }
     }
-  } else if (tid == load_warp * 32 && ng > 0) {
+  } else if (warp == load_warp && ng > 0) {
     // Q of tile tl waits only for the MMAs of tile tl - 2, whose stages were loaded before: the
     // loader may block on either kind of wait without stalling the pipeline for good
     int64_t issued = 0;
     int q_issued = 0;
     Ring lr;
     bool ok = true;
-    for (int tl = 0; tl < nt && ok && !sy->abort; ++tl) {
+    for (int tl = 0; tl < nt && ok && !warp_aborted(sy); ++tl) {
       const int b = tl & 1, use = tl >> 1;
-      if (use > 0 && !tc::mbar_wait_ns(tc::smem_u32(&sy->qempty[b]),
-                                       static_cast<uint32_t>((use - 1) & 1), kWaitNs)) {
+      if (use > 0 &&
+          !warp_wait(tc::smem_u32(&sy->qempty[b]), static_cast<uint32_t>((use - 1) & 1))) {
         fail_wait(sy, status, 16);
         break;
       }
-      const uint32_t qbar = tc::smem_u32(&sy->qfull[b]);
-      bulk_expect(qbar, kQBytes);
-      bulk_copy(tc::smem_u32(qb + b * kQBytes), qtiles + static_cast<int64_t>(ta + tl) * 4096,
-                kQBytes, qbar);
+      if (tc::elect_one()) {
+        const uint32_t qbar = tc::smem_u32(&sy->qfull[b]);
+        bulk_expect(qbar, kQBytes);
+        bulk_copy(tc::smem_u32(qb + b * kQBytes), qtiles + static_cast<int64_t>(ta + tl) * 4096,
+                  kQBytes, qbar);
+      }
+      __syncwarp();
       q_issued = tl + 1;
       for (int gl = 0; gl < ng && ok; ++gl) {
         ok = load(sy, status, lb, lr, loads, pc, gslots, gheader, n_slots, g0 + gl, ta + tl);
@@ -691,13 +732,14 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
     }
     drain_loads(sy, status, loads, issued);
     for (int tl = q_issued > 2 ? q_issued - 2 : 0; tl < q_issued; ++tl)
-      if (!tc::mbar_wait_ns(tc::smem_u32(&sy->qfull[tl & 1]), static_cast<uint32_t>((tl >> 1) & 1),
-                            kWaitNs))
+      if (!warp_wait(tc::smem_u32(&sy->qfull[tl & 1]), static_cast<uint32_t>((tl >> 1) & 1)) &&
+          lane == 0)
         atomicOr(status, 128);
   }
-  if (tid == mma_warp * 32) {
-    tc::mma_commit(tc::smem_u32(&sy->last));
-    if (!tc::mbar_wait_ns(tc::smem_u32(&sy->last), 0, kWaitNs)) fail_wait(sy, status, 8);
+  if (warp == mma_warp) {
+    if (tc::elect_one()) tc::mma_commit(tc::smem_u32(&sy->last));
+    __syncwarp();
+    if (!warp_wait(tc::smem_u32(&sy->last), 0)) fail_wait(sy, status, 8);
   }
   tc::fence_before_sync();
   __syncthreads();

