@@ -32,8 +32,13 @@ namespace {
 
 // The producers form teams of 4 warps (one warp per 32 points of a stage, the tensor-memory lanes
 // its warp may access); team t writes stages t, t + teams, t + 2 teams, ... so that the teams'
-// waits and latencies overlap. Behind the producers: one warp whose first thread issues the MMAs,
-// one whose first thread issues the bulk copies.
+// waits and latencies overlap. Behind the producers: the MMA warp and the loader warp.
+// Ring safety: a parity wait tells a barrier's phase only from the one before it, so no waiter may
+// run two phases ahead. Load buffer b serves stages b, b + loads, ...; with loads a multiple of
+// teams they all belong to one team, which waits for each in turn (bulk copies may land out of
+// order, so a buffer shared between teams could be waited on for its next use before its current
+// one had landed). An E stage slot may pass between teams: its waits stay within one phase when
+// teams <= stages, since a team's previous stage already waited for the MMAs of the stage before.
 constexpr int kTeamWarps = 4;
 constexpr int kMaxTeams = 4;
 constexpr int kMaxThreads = (kTeamWarps * kMaxTeams + 2) * 32;
@@ -42,7 +47,8 @@ constexpr uint32_t kCoefBytes = 4096u * 2u;         // 128 rows x 32 columns of 
 constexpr uint32_t kQBytes = 4096u * 2u;            // 128 points x 32 columns of BF16
 constexpr uint32_t kSlotRow = 128u * 4u;            // one slot's packed words of a tile
 constexpr uint32_t kHeaderAt = 16u * kSlotRow;      // a group has at most 16 slots, then its
-constexpr uint32_t kLoadBytes = kHeaderAt + 128u;   // 16-byte chunk header (padded)
+constexpr uint32_t kLoadBytes = kHeaderAt + 128u;   // 128-byte chunk header
+constexpr int32_t kUnusedBase = 0x40000000;         // shift base of a chunk no slot uses
 constexpr uint64_t kWaitNs = 2000000000ull;         // a bounded wait gives up after 2 s
 constexpr uint64_t kPollNs = 4000000000ull;         // the loader's idle polling, after 4 s
 constexpr int kMaxStages = 6;
@@ -151,57 +157,70 @@ __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_
 __device__ __forceinline__ void load_stage(unsigned char* buf, uint32_t mbar,
                                            const uint32_t* __restrict__ pc,
                                            const int2* __restrict__ gslots,
-                                           const uint4* __restrict__ gheader, int n_slots,
+                                           const BlockHeader* __restrict__ gheader, int n_slots,
                                            int group, int64_t tile) {
   const int2 gs = __ldg(gslots + group);
   const uint32_t bytes = static_cast<uint32_t>(gs.y) * kSlotRow;
-  bulk_expect(mbar, bytes + 16u);
+  bulk_expect(mbar, bytes + static_cast<uint32_t>(sizeof(BlockHeader)));
   bulk_copy(tc::smem_u32(buf), pc + (tile * n_slots + gs.x) * 128, bytes, mbar);
-  bulk_copy(tc::smem_u32(buf + kHeaderAt), gheader + group, 16u, mbar);
+  bulk_copy(tc::smem_u32(buf + kHeaderAt), gheader + group, sizeof(BlockHeader), mbar);
 }
 
 // ---- producer: one stage of E ----------------------------------------------------------------
-// Each group carries a 16-byte chunk header: byte q describes chunk q of the group — the slot
-// (subspace) it belongs to, as an index among the group's slots (high nibble), and which of the
-// slot's chunks it is (low nibble); 0xFF marks a chunk no slot uses. Thread (p, h) writes chunks
-// 8h .. 8h + 7 of point p: the chunk holds the point's product at element c % 8 when the point's
-// cell c in that subspace lies in it (c / 8 == the slot's chunk), zeros otherwise. Thread p of a
-// team writes the 16 chunks of point p.
+// A packed word holds a point's BF16 product in one subspace (low half) and 16 x its cell c in
+// that subspace (high half). Each group carries a header (BlockHeader): for chunk q, the byte
+// offset of its slot's row in the load buffer and the shift base 128 x (which of the slot's
+// chunks q is), or kUnusedBase for a chunk no slot uses. The chunk holds the point's product at
+// element c - 8 x that index when that lies in 0..7, zeros otherwise; with s = 16 c - base, word k
+// of the chunk (elements 2k, 2k + 1) is the product shifted left by s - 32 k, since a shift by 32
+// or more, or by a negative amount read as unsigned, gives 0. Thread p of a team writes the 16
+// chunks of point p.
 struct ChunkWords {
-  uint32_t w[16];  // packed product | cell << 16 of the chunk's slot, 0 for an unused chunk
-  uint32_t hdr[4]; // header bytes of chunks 4i .. 4i + 3
+  uint32_t v[16];  // product bits
+  uint32_t s[16];  // shift of the product within the chunk's 128 bits
 };
 
-__device__ __forceinline__ uint32_t chunk_byte(const ChunkWords& C, int i) {
-  return (C.hdr[i >> 2] >> (8 * (i & 3))) & 0xFFu;
+__device__ __forceinline__ uint32_t shl_clamped(uint32_t v, uint32_t s) {
+  uint32_t r;
+  asm("shl.b32 %0, %1, %2;" : "=r"(r) : "r"(v), "r"(s));
+  return r;
 }
 
-__device__ __forceinline__ void read_chunks(ChunkWords& C, const uint32_t* lbuf, int p) {
-  const uint4 hd = *reinterpret_cast<const uint4*>(lbuf + kHeaderAt / 4);
-  C.hdr[0] = hd.x;
-  C.hdr[1] = hd.y;
-  C.hdr[2] = hd.z;
-  C.hdr[3] = hd.w;
+__device__ __forceinline__ void read_chunks(ChunkWords& C, const unsigned char* lbuf, int p) {
+  const BlockHeader& hd = *reinterpret_cast<const BlockHeader*>(lbuf + kHeaderAt);
+  int32_t row[16], base[16];
+#pragma unroll
+  for (int i = 0; i < 16; i += 4) {
+    const int4 r4 = *reinterpret_cast<const int4*>(&hd.row[i]);
+    const int4 b4 = *reinterpret_cast<const int4*>(&hd.base[i]);
+    row[i] = r4.x, row[i + 1] = r4.y, row[i + 2] = r4.z, row[i + 3] = r4.w;
+    base[i] = b4.x, base[i + 1] = b4.y, base[i + 2] = b4.z, base[i + 3] = b4.w;
+  }
+  const unsigned char* lp = lbuf + 4 * p;
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
-    const uint32_t byte = chunk_byte(C, i);
-    C.w[i] = byte == 0xFFu ? 0u : lbuf[(byte >> 4) * 128 + p];
+    const uint32_t w = *reinterpret_cast<const uint32_t*>(lp + row[i]);
+    C.v[i] = w & 0xFFFFu;
+    C.s[i] = (w >> 16) - static_cast<uint32_t>(base[i]);
   }
+}
+
+// words 4i .. 4i + 3 of a point's row of E: chunk i
+__device__ __forceinline__ void chunk_words(const ChunkWords& C, int i, uint32_t& r0, uint32_t& r1,
+                                            uint32_t& r2, uint32_t& r3) {
+  r0 = shl_clamped(C.v[i], C.s[i]);
+  r1 = shl_clamped(C.v[i], C.s[i] - 32u);
+  r2 = shl_clamped(C.v[i], C.s[i] - 64u);
+  r3 = shl_clamped(C.v[i], C.s[i] - 96u);
 }
 
 __device__ __forceinline__ void write_chunks(unsigned char* stage, int p, const ChunkWords& C) {
   unsigned char* base = stage + (p >> 3) * 2048 + (p & 7) * 16;
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
-    const uint32_t byte = chunk_byte(C, i);
-    if (byte == 0xFFu) continue;  // unused chunk: its coefficient rows are zero
-    const uint32_t w = C.w[i];
-    const uint32_t c = w >> 16;
-    const uint32_t v = (c >> 3) == (byte & 0xFu) ? (w & 0xFFFFu) : 0u;
-    const uint32_t val = v << ((c & 1u) * 16u);
-    const uint32_t wd = (c >> 1) & 3u;
-    *reinterpret_cast<uint4*>(base + i * 128) =
-        make_uint4(wd == 0 ? val : 0u, wd == 1 ? val : 0u, wd == 2 ? val : 0u, wd == 3 ? val : 0u);
+    uint4 q;
+    chunk_words(C, i, q.x, q.y, q.z, q.w);
+    *reinterpret_cast<uint4*>(base + i * 128) = q;
   }
 }
 
@@ -220,7 +239,7 @@ __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st
     return false;
   }
   ChunkWords C;
-  read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes), p);
+  read_chunks(C, lb + static_cast<size_t>(b) * kLoadBytes, p);
   // one arrival per warp (the barriers count warps): 128 arrivals on one word per stage
   // serialised on the shared-memory atomics
   __syncwarp();
@@ -245,8 +264,7 @@ __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st
 // produce() for the mult kernel's tensor-memory A operand: the stage's rows go to tensor memory
 // (lane = point, 4 columns per chunk: the chunk's 8 BF16 elements as 4 pairs) with two 32-column
 // stores per thread instead of shared memory, so the tensor cores read A without the
-// shared-memory traffic of writing and reading it. All 16 chunks are written (zeros included),
-// which also overwrites whatever an earlier group left in the columns.
+// shared-memory traffic of writing and reading it.
 __device__ __forceinline__ bool produce_tmem(Sync* sy, int* status, unsigned char* lb, Ring& lr,
                                              int loads, Ring& sr, int stages, uint32_t a_taddr,
                                              int p, int teams) {
@@ -257,7 +275,7 @@ __device__ __forceinline__ bool produce_tmem(Sync* sy, int* status, unsigned cha
     return false;
   }
   ChunkWords C;
-  read_chunks(C, reinterpret_cast<const uint32_t*>(lb + static_cast<size_t>(b) * kLoadBytes), p);
+  read_chunks(C, lb + static_cast<size_t>(b) * kLoadBytes, p);
   __syncwarp();
   if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
   lr.step(teams, loads);
@@ -276,18 +294,7 @@ __device__ __forceinline__ bool produce_tmem(Sync* sy, int* status, unsigned cha
   for (int h = 0; h < 2; ++h) {
     uint32_t r[32];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const uint32_t byte = chunk_byte(C, 8 * h + i);
-      const uint32_t w = C.w[8 * h + i];
-      const uint32_t c = w >> 16;
-      const uint32_t v = byte != 0xFFu && (c >> 3) == (byte & 0xFu) ? (w & 0xFFFFu) : 0u;
-      const uint32_t val = v << ((c & 1u) * 16u);
-      const uint32_t wd = (c >> 1) & 3u;
-      r[4 * i + 0] = wd == 0 ? val : 0u;
-      r[4 * i + 1] = wd == 1 ? val : 0u;
-      r[4 * i + 2] = wd == 2 ? val : 0u;
-      r[4 * i + 3] = wd == 3 ? val : 0u;
-    }
+    for (int i = 0; i < 8; ++i) chunk_words(C, 8 * h + i, r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]);
     tc::tmem_st32(at + 32u * h, r);
   }
   tc::tmem_wait_st();
@@ -304,7 +311,7 @@ __device__ __forceinline__ bool produce_tmem(Sync* sy, int* status, unsigned cha
 __device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, Ring& lr, int loads,
                                      const uint32_t* __restrict__ pc,
                                      const int2* __restrict__ gslots,
-                                     const uint4* __restrict__ gheader, int n_slots, int group,
+                                     const BlockHeader* __restrict__ gheader, int n_slots, int group,
                                      int64_t tile) {
   const int b = lr.idx;
   if (lr.round > 0 && !warp_wait(tc::smem_u32(&sy->lempty[b]), (lr.round - 1u) & 1u)) {
@@ -483,7 +490,7 @@ __device__ __forceinline__ bool multt_window(Sync* sy, int* status, Ring& sr, in
 // columns per stage, instead of in shared memory.
 template <bool TMEM_A>
 __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
-    const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
+    const uint32_t* __restrict__ pc, const BlockHeader* __restrict__ gheader,
     const int2* __restrict__ gslots, const uint16_t* __restrict__ coef, int n_groups, int n_slots, int64_t mpad, int64_t m, int n_tiles,
     int tiles, int gpp, int teams, int stages, int loads, int win, uint32_t tmem_cols, uint16_t* __restrict__ qtiles,
     double* __restrict__ out64, int* __restrict__ status) {
@@ -660,7 +667,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
 // rows (M, strided).
 
 __global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
-    const uint32_t* __restrict__ pc, const uint4* __restrict__ gheader,
+    const uint32_t* __restrict__ pc, const BlockHeader* __restrict__ gheader,
     const int2* __restrict__ gslots, const uint16_t* __restrict__ qtiles, int n_groups, int n_slots, int64_t mpad, int n_tiles, int gpc,
     int streams, int teams, int stages, int loads, int win, uint32_t tmem_cols, int64_t rows,
     double* __restrict__ part, int* __restrict__ status) {
@@ -850,7 +857,7 @@ __global__ void block_pack_kernel(const float4* __restrict__ pmat, const CW* __r
       const float v = lane4 == 0 ? q.x : lane4 == 1 ? q.y : lane4 == 2 ? q.z : q.w;
       const uint32_t cell = (static_cast<uint32_t>(cmat[at]) >> (kBits * lane4)) & ((1u << kBits) - 1u);
       const __nv_bfloat16 b = __float2bfloat16_rn(v);
-      w = static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(&b)) | (cell << 16);
+      w = static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(&b)) | (cell << 20);
     }
     pc[k] = w;
   }
@@ -1063,7 +1070,7 @@ void block_free(BlockPlan* b) {
 bool block_shape_ok(const BlockShape& sh, int smem_cap) {
   return sh.stages >= 2 && sh.stages <= kMaxStages && sh.loads >= 2 && sh.loads <= kMaxLoads &&
          sh.window >= 1 && sh.window <= kMaxWindow && sh.teams >= 1 && sh.teams <= kMaxTeams &&
-         sh.teams <= sh.stages && sh.teams <= sh.loads &&
+         sh.teams <= sh.stages && sh.loads % sh.teams == 0 &&
          sh.mult_tiles >= 1 && sh.mult_tiles <= 16 && mult_tmem_need(sh) <= 512 &&
          sh.mult_groups >= 1 && sh.multt_groups >= 1 && sh.multt_groups <= 16 &&
          mult_smem(sh, mult_groups_fit(sh, smem_cap)) <= static_cast<size_t>(smem_cap) &&
@@ -1119,11 +1126,14 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
   std::vector<int> pos_gp(static_cast<size_t>(sub.total), -1);
   for (int64_t g = 0; g < sub.n; ++g) pos_gp[sub.h_pos[g]] = static_cast<int>(g);
   std::vector<int> row_gp(static_cast<size_t>(rows), -1), gp_row(static_cast<size_t>(sub.n), 0);
-  std::vector<uint4> gheader(static_cast<size_t>(n_groups));
+  std::vector<BlockHeader> gheader(static_cast<size_t>(n_groups));
   std::vector<int2> gslots(static_cast<size_t>(n_groups));
   for (int g = 0; g < n_groups; ++g) {
-    uint8_t bytes[16];
-    std::memset(bytes, 0xFF, sizeof(bytes));
+    BlockHeader& hd = gheader[g];
+    for (int q = 0; q < 16; ++q) {
+      hd.row[q] = 0;  // any row of the group: the shift clears the words
+      hd.base[q] = kUnusedBase;
+    }
     for (int sl = group_first[g]; sl < group_first[g + 1]; ++sl) {
       const int sidx = slot_sub[sl];
       const int co = slot_cn[sl] & 0xFF, nch = slot_cn[sl] >> 8;
@@ -1134,10 +1144,11 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
         row_gp[r] = gp;
         if (gp >= 0) gp_row[gp] = static_cast<int>(r);
       }
-      for (int q = co; q < co + nch; ++q)
-        bytes[q] = static_cast<uint8_t>(((sl - group_first[g]) << 4) | (q - co));
+      for (int q = co; q < co + nch; ++q) {
+        hd.row[q] = static_cast<int32_t>((sl - group_first[g]) * kSlotRow);
+        hd.base[q] = 128 * (q - co);
+      }
     }
-    std::memcpy(&gheader[g], bytes, sizeof(bytes));
     gslots[g] = make_int2(group_first[g], group_first[g + 1] - group_first[g]);
   }
   b->n_groups = n_groups;
@@ -1153,7 +1164,7 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
   };
   bool ok = alloc(&b->row_gp, sizeof(int) * rows) && alloc(&b->gp_row, sizeof(int) * sub.n) &&
-            alloc(&b->gheader, sizeof(uint4) * gheader.size()) &&
+            alloc(&b->gheader, sizeof(BlockHeader) * gheader.size()) &&
             alloc(&b->gslots, sizeof(int2) * gslots.size()) &&
             alloc(&d_slot_sub, sizeof(int) * slot_sub.size()) &&
             alloc(&b->pc, sizeof(uint32_t) * static_cast<size_t>(b->n_slots) * mpad) &&
@@ -1163,7 +1174,7 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
             alloc(&b->status, sizeof(int));
   ok = ok && put(b->row_gp, row_gp.data(), sizeof(int) * rows) &&
        put(b->gp_row, gp_row.data(), sizeof(int) * sub.n) &&
-       put(b->gheader, gheader.data(), sizeof(uint4) * gheader.size()) &&
+       put(b->gheader, gheader.data(), sizeof(BlockHeader) * gheader.size()) &&
        put(b->gslots, gslots.data(), sizeof(int2) * gslots.size()) &&
        put(d_slot_sub, slot_sub.data(), sizeof(int) * slot_sub.size()) &&
        cudaMemsetAsync(b->status, 0, sizeof(int), s) == cudaSuccess;

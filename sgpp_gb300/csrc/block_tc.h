@@ -32,13 +32,21 @@ constexpr int kBlockTile = 128;    // points per tile (MMA M for mult, K extent 
 constexpr int kBlockGroupRows = 128;  // rows per group (MMA M for multT)
 constexpr int kBlockMaxCells = 128;   // largest subspace the block products take
 
+// Per group and chunk q (16 chunks of 8 rows): the byte offset of the chunk's slot row in a
+// stage's load buffer (slot index within the group x 512), and 128 x which of the slot's chunks q
+// is (or a large base for a chunk no slot uses). 128 bytes, copied with the stage's products.
+struct BlockHeader {
+  int32_t row[16];
+  int32_t base[16];
+};
+
 // Tunable launch shapes (picked per operator by the autotuner, sgmev_tune_block)
 struct BlockShape {
   int mult_tiles = 8;      // tiles per mult CTA (their accumulators stay in tensor memory)
   int mult_groups = 32;    // groups whose coefficient rows a mult CTA holds (fewer when shared
                            // memory runs out)
   int multt_groups = 16;   // groups (accumulators) per multT CTA
-  int stages = 3;          // stages of E in flight (shared or tensor memory)
+  int stages = 4;          // stages of E in flight (shared or tensor memory)
   int loads = 6;           // stages of packed products in flight (bulk copies ahead of use)
   int mult_tmem = 1;       // mult keeps its A operand (the stages of E) in tensor memory
   int window = 2;          // stages whose MMAs one issue round interleaves (at most `stages`)
@@ -55,10 +63,10 @@ struct BlockPlan {
   int64_t m = 0;
   int* row_gp = nullptr;      // [rows] grid point of a row, -1 when none
   int* gp_row = nullptr;      // [n] row of a grid point
-  uint4* gheader = nullptr;   // [n_groups] chunk headers: per chunk, its slot in the group << 4 | which
-                              // of the slot's chunks it is (0xFF: unused)
+  BlockHeader* gheader = nullptr;  // [n_groups] chunk headers
   int2* gslots = nullptr;     // [n_groups] first slot and slot count of each group
-  uint32_t* pc = nullptr;     // [mpad / 128][n_slots][128] BF16 product | cell << 16, tile by tile
+  uint32_t* pc = nullptr;     // [mpad / 128][n_slots][128] BF16 product | 16 cell << 16, tile by
+                              // tile
   uint16_t* coef = nullptr;   // [n_groups][4096] coefficient rows, BF16, operand layout
   uint16_t* qtiles = nullptr; // [mpad / 128][4096] Q tiles, BF16, operand layout
   double* part = nullptr;     // [streams][16][rows] partial rows of multT

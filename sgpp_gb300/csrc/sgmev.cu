@@ -1522,7 +1522,7 @@ SGMEV_API int sgmev_set_params(sgmev_op* op, const char* params_json) {
   if (!block_shape_ok(op->blk_shape, cap)) {
     op->blk_shape = before;
     op->blk.shape = before;
-    return fail(SGMEV_ERR_INVALID, "block launch shape does not fit the device's shared memory");
+    return fail(SGMEV_ERR_INVALID, "invalid block launch shape (teams must be at most the stages and divide the loads; window at most 3; the stages and coefficient rows must fit shared and tensor memory)");
   }
   return SGMEV_OK;
 }
@@ -2011,7 +2011,7 @@ static int block_ready(sgmev_op* op) {
   int cap = 0;
   SGMEV_CUDA(cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, op->device));
   if (!block_shape_ok(op->blk_shape, cap))
-    return fail(SGMEV_ERR_INVALID, "block launch shape does not fit the device's shared memory");
+    return fail(SGMEV_ERR_INVALID, "invalid block launch shape (teams must be at most the stages and divide the loads; window at most 3; the stages and coefficient rows must fit shared and tensor memory)");
   if (!op->sub_ok || !mat_ready(op)) {
     op->blk_failed = true;
     op->blk_err = "they stream the materialised subspace products (params \"algo\": \"subspace\", "

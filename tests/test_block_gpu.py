@@ -169,21 +169,33 @@ def test_interleaved_mma_window_gives_the_same_bits(window):
     np.testing.assert_array_equal(out[0][1], out[1][1])
 
 
-@pytest.mark.parametrize("teams", ["1", "3", "4"])
-def test_producer_teams_give_the_same_bits(teams):
+@pytest.mark.parametrize("teams,loads", [("1", "6"), ("3", "6"), ("4", "8")])
+def test_producer_teams_give_the_same_bits(teams, loads):
     """block_teams: teams of 4 producer warps write alternate stages; every stage still holds the
-    same values and the MMAs consume the stages in the same order, so the results are identical."""
+    same values and the MMAs consume the stages in the same order, so the results are identical.
+    d = 9 level 4 with block_mult_groups 4 runs the mult in several passes over the coefficient
+    rows, and 2^15 points give each CTA several hundred stages."""
     rng = np.random.default_rng(62)
-    grid = _grid(6, 4)
-    x = rng.random((20000, 6))
+    grid = _grid(9, 4)
+    x = rng.random((1 << 15, 9))
     a = rng.standard_normal((K, grid.getSize()))
     v = rng.standard_normal((K, x.shape[0]))
     out = []
-    for t in ("2", teams):
+    for t, nl in (("2", "6"), (teams, loads)):
         for where in ("tmem", "smem"):
-            op = _op(grid, x, block_teams=t, block_stages=4, block_mult_a=where)
+            op = _op(grid, x, block_teams=t, block_loads=nl, block_stages=4, block_mult_a=where,
+                     block_mult_groups=4)
             out.append((op.multBlock(a), op.multTransposeBlock(v)))
             op.close()
     for o in out[1:]:
         np.testing.assert_array_equal(out[0][0], o[0])
         np.testing.assert_array_equal(out[0][1], o[1])
+
+
+def test_shapes_whose_load_buffers_would_pass_between_teams_are_refused():
+    rng = np.random.default_rng(63)
+    grid = _grid(3, 3)
+    x = rng.random((300, 3))
+    with pytest.raises(sg.OperationException):
+        _op(grid, x, block_teams=4, block_loads=6, block_stages=4).multBlock(
+            np.zeros((K, grid.getSize())))
