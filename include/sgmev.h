@@ -267,7 +267,7 @@ SGMEV_API int64_t sgmev_kernel_launches(const sgmev_op* op);
  * params "block_inner_tol" (default "1e-3"): inner tolerance of sgmev_fit_block; "block_mult_tiles",
  * "block_mult_groups", "block_multt_groups", "block_stages" (default 4), "block_loads" (default
  * 6): launch shape; "block_window" (1-3, default 2): stages whose MMAs one issue round interleaves;
- * "block_teams" (1-4, default 2, at most block_stages and dividing block_loads): producer teams
+ * "block_teams" (1-4, default 3, at most block_stages and dividing block_loads): producer teams
  * of 4 warps that write alternate stages; and
  * "block_mult_a": "tmem" (default) or "smem", where the mult keeps its A operand (the autotuner's
  * choices, sgpp_gb300.autotune).

@@ -50,7 +50,6 @@ constexpr uint32_t kHeaderAt = 16u * kSlotRow;      // a group has at most 16 sl
 constexpr uint32_t kLoadBytes = kHeaderAt + 128u;   // 128-byte chunk header
 constexpr int32_t kUnusedBase = 0x40000000;         // shift base of a chunk no slot uses
 constexpr uint64_t kWaitNs = 2000000000ull;         // a bounded wait gives up after 2 s
-constexpr uint64_t kPollNs = 4000000000ull;         // the loader's idle polling, after 4 s
 constexpr int kMaxStages = 6;
 constexpr int kMaxLoads = 12;
 constexpr int kMaxWindow = 3;  // stages the MMA thread interleaves
@@ -154,12 +153,11 @@ __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_
 // is one bulk copy (one 512-byte copy per slot kept the copy engine, not the memory, busy).
 // The group's chunk header comes along into the same buffer (a header read from global memory
 // per stage, on the producers' critical path, cost them more than writing the stage).
+// gs: the group's first slot and slot count.
 __device__ __forceinline__ void load_stage(unsigned char* buf, uint32_t mbar,
-                                           const uint32_t* __restrict__ pc,
-                                           const int2* __restrict__ gslots,
+                                           const uint32_t* __restrict__ pc, int2 gs,
                                            const BlockHeader* __restrict__ gheader, int n_slots,
                                            int group, int64_t tile) {
-  const int2 gs = __ldg(gslots + group);
   const uint32_t bytes = static_cast<uint32_t>(gs.y) * kSlotRow;
   bulk_expect(mbar, bytes + static_cast<uint32_t>(sizeof(BlockHeader)));
   bulk_copy(tc::smem_u32(buf), pc + (tile * n_slots + gs.x) * 128, bytes, mbar);
@@ -224,12 +222,100 @@ __device__ __forceinline__ void write_chunks(unsigned char* stage, int p, const 
   }
 }
 
+// The loader warp's copy of gslots for a window of 32 groups, one per lane: a global load of the
+// group's slots per stage, waited for before each copy could be issued, had set the pace of the
+// whole pipeline. The group index is warp-uniform.
+struct GroupSlots {
+  int2 lane_gs = make_int2(0, 0);
+  int window = -1;
+  __device__ __forceinline__ int2 get(const int2* __restrict__ gslots, int n_groups, int group) {
+    const int w0 = group & ~31;
+    if (w0 != window) {
+      window = w0;
+      const int g = w0 + static_cast<int>(threadIdx.x & 31);
+      lane_gs = g < n_groups ? __ldg(gslots + g) : make_int2(0, 0);
+    }
+    return make_int2(__shfl_sync(0xffffffffu, lane_gs.x, group & 31),
+                     __shfl_sync(0xffffffffu, lane_gs.y, group & 31));
+  }
+};
+
+// Where a kernel's stages come from: stage k of the kernel's order is (major, minor) =
+// (k / n_minor, k % n_minor), in the mult (group, tile of the CTA) and in the multT (tile of the
+// stream, group of the pass).
+struct StageSource {
+  const uint32_t* __restrict__ pc;
+  const int2* __restrict__ gslots;
+  const BlockHeader* __restrict__ gheader;
+  int n_slots, n_groups, n_minor;
+  int group0;        // multT: first group of the pass
+  int64_t tile0;     // first tile of the CTA (mult) or of the stream (multT)
+  bool tiles_minor;  // the mult's order
+  int64_t total;     // stages of the CTA
+};
+
+// The copies of one team's stages, issued by the team's first warp: the team's first
+// loads / teams stages up front, then stage k + loads into the buffer of stage k as soon as the
+// team's four warps have read stage k. A team's load buffers are its own, so no other warp takes
+// part (one loader warp issuing every stage's copy after a hand-off per stage had been the
+// slowest link of the pipeline).
+struct TeamLoads {
+  int64_t k = 0;  // next stage to load
+  int major = 0, minor = 0;
+  Ring ring;      // its buffer
+  GroupSlots gsl;
+  __device__ __forceinline__ void init(int team, int n_minor) {
+    k = team;
+    major = team / n_minor;
+    minor = team % n_minor;
+    ring = Ring{team, 0u};
+  }
+  __device__ __forceinline__ void step(int teams, int n_minor, int loads) {
+    k += teams;
+    minor += teams;
+    while (minor >= n_minor) {
+      minor -= n_minor;
+      ++major;
+    }
+    ring.step(teams, loads);
+  }
+  // by the whole warp; the elected lane issues
+  __device__ __forceinline__ void issue(Sync* sy, unsigned char* lb, const StageSource& src) {
+    const int group = src.tiles_minor ? major : src.group0 + minor;
+    const int64_t tile = src.tile0 + (src.tiles_minor ? minor : major);
+    const int2 gs = gsl.get(src.gslots, src.n_groups, group);
+    if (tc::elect_one()) {
+      tc::fence_proxy_async();  // the team's reads of the buffer come before the copy's writes
+      load_stage(lb + static_cast<size_t>(ring.idx) * kLoadBytes,
+                 tc::smem_u32(&sy->lfull[ring.idx]), src.pc, gs, src.gheader, src.n_slots, group,
+                 tile);
+    }
+    __syncwarp();
+  }
+  // before the CTA exits: the last copy into each of the team's buffers has landed (the copies
+  // of an aborted run must not write shared memory after the CTA is gone)
+  __device__ __forceinline__ void drain(Sync* sy, int* status, int teams, int loads, int team) {
+    for (int64_t j = k - teams; j >= team && j >= k - loads; j -= teams) {
+      const int b = static_cast<int>(j % loads);
+      if (!warp_wait(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((j / loads) & 1)) &&
+          (threadIdx.x & 31) == 0)
+        atomicOr(status, 128);
+    }
+  }
+};
+
 // A team's part of its next stage: wait for the packed products, read them, free the load
-// buffer, wait for the E stage to be free, write it, mark it full, step both rings past the
-// other teams' stages. False when a wait ran out.
+// buffer (the team's first warp then loads the team's stage `loads` ahead into it), wait for the
+// E stage to be free, write it, mark it full, step both rings past the other teams' stages.
+// TMEM: the stage's rows go to tensor memory (lane = point, 4 columns per chunk: the chunk's 8
+// BF16 elements as 4 pairs) with two 32-column stores per thread instead of shared memory, so the
+// tensor cores read A without the shared-memory traffic of writing and reading it.
+// False when a wait ran out.
+template <bool TMEM>
 __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st,
                                         unsigned char* lb, Ring& lr, int loads, Ring& sr,
-                                        int stages, int p, int teams) {
+                                        int stages, uint32_t a_taddr, int p, int teams,
+                                        TeamLoads& tl, const StageSource& src, bool issuer) {
   const int b = lr.idx;
   // the warp's lanes decide together (a lane that gave up alone would leave the others waiting
   // at the warp's synchronisation below)
@@ -240,10 +326,17 @@ __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st
   }
   ChunkWords C;
   read_chunks(C, lb + static_cast<size_t>(b) * kLoadBytes, p);
-  // one arrival per warp (the barriers count warps): 128 arrivals on one word per stage
-  // serialised on the shared-memory atomics
+  // one arrival per warp (the barriers count warps)
   __syncwarp();
   if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
+  if (issuer && tl.k < src.total) {
+    if (!warp_wait(tc::smem_u32(&sy->lempty[b]), lr.round & 1u)) {
+      fail_wait(sy, status, 64);
+      return false;
+    }
+    tl.issue(sy, lb, src);
+    tl.step(teams, src.n_minor, loads);
+  }
   lr.step(teams, loads);
   const int sidx = sr.idx;
   const bool free_stage =
@@ -253,88 +346,51 @@ __device__ __forceinline__ bool produce(Sync* sy, int* status, unsigned char* st
     fail_wait(sy, status, 2);
     return false;
   }
-  write_chunks(st + static_cast<size_t>(sidx) * kStageBytes, p, C);
-  tc::fence_proxy_async();
+  if constexpr (TMEM) {
+    // lanes 32 (warp % 4) ...; chunks 8 h .. 8 h + 7 are columns 32 h .. 32 h + 31 of the stage
+    const uint32_t at = a_taddr + (static_cast<uint32_t>((threadIdx.x >> 5) & 3) << 21) +
+                        static_cast<uint32_t>(sidx * 64);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      uint32_t r[32];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        chunk_words(C, 8 * h + i, r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]);
+      tc::tmem_st32(at + 32u * h, r);
+    }
+    tc::tmem_wait_st();
+    tc::fence_before_sync();
+  } else {
+    write_chunks(st + static_cast<size_t>(sidx) * kStageBytes, p, C);
+    tc::fence_proxy_async();
+  }
   __syncwarp();
   if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
   sr.step(teams, stages);
   return true;
 }
 
-// produce() for the mult kernel's tensor-memory A operand: the stage's rows go to tensor memory
-// (lane = point, 4 columns per chunk: the chunk's 8 BF16 elements as 4 pairs) with two 32-column
-// stores per thread instead of shared memory, so the tensor cores read A without the
-// shared-memory traffic of writing and reading it.
-__device__ __forceinline__ bool produce_tmem(Sync* sy, int* status, unsigned char* lb, Ring& lr,
-                                             int loads, Ring& sr, int stages, uint32_t a_taddr,
-                                             int p, int teams) {
-  const int b = lr.idx;
-  if (!__all_sync(0xffffffffu, tc::mbar_wait_ns(tc::smem_u32(&sy->lfull[b]), lr.round & 1u,
-                                                kWaitNs))) {
-    fail_wait(sy, status, 32);
-    return false;
-  }
-  ChunkWords C;
-  read_chunks(C, lb + static_cast<size_t>(b) * kLoadBytes, p);
-  __syncwarp();
-  if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->lempty[b]));
-  lr.step(teams, loads);
-  const int sidx = sr.idx;
-  const bool free_stage =
-      sr.round == 0 ||
-      tc::mbar_wait_ns(tc::smem_u32(&sy->empty[sidx]), (sr.round - 1u) & 1u, kWaitNs);
-  if (!__all_sync(0xffffffffu, free_stage)) {
-    fail_wait(sy, status, 2);
-    return false;
-  }
-  // lanes 32 (warp % 4) ...; chunks 8 h .. 8 h + 7 are columns 32 h .. 32 h + 31 of the stage
-  const uint32_t at = a_taddr + (static_cast<uint32_t>((threadIdx.x >> 5) & 3) << 21) +
-                      static_cast<uint32_t>(sidx * 64);
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    uint32_t r[32];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) chunk_words(C, 8 * h + i, r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]);
-    tc::tmem_st32(at + 32u * h, r);
-  }
-  tc::tmem_wait_st();
-  tc::fence_before_sync();
-  __syncwarp();
-  if ((threadIdx.x & 31) == 0) tc::mbar_arrive(tc::smem_u32(&sy->full[sidx]));
-  sr.step(teams, stages);
-  return true;
-}
-
-// The loader warp's part of a stage: wait for the load buffer to be free, issue the bulk copies
-// from the elected lane (copies issued by a lone thread of a diverged warp had left the loader
-// busy for most of a stage).
-__device__ __forceinline__ bool load(Sync* sy, int* status, unsigned char* lb, Ring& lr, int loads,
-                                     const uint32_t* __restrict__ pc,
-                                     const int2* __restrict__ gslots,
-                                     const BlockHeader* __restrict__ gheader, int n_slots, int group,
-                                     int64_t tile) {
-  const int b = lr.idx;
-  if (lr.round > 0 && !warp_wait(tc::smem_u32(&sy->lempty[b]), (lr.round - 1u) & 1u)) {
-    fail_wait(sy, status, 64);
-    return false;
-  }
-  if (tc::elect_one())
-    load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc, gslots,
-               gheader, n_slots, group, tile);
-  __syncwarp();
-  lr.next(loads);
-  return true;
-}
-
-// The loader's copies still in flight complete before the CTA may exit (the last `loads` stages
-// it issued)
-__device__ __forceinline__ void drain_loads(Sync* sy, int* status, int loads, int64_t issued) {
-  for (int64_t i = issued > loads ? issued - loads : 0; i < issued; ++i) {
-    const int b = static_cast<int>(i % loads);
-    if (!warp_wait(tc::smem_u32(&sy->lfull[b]), static_cast<uint32_t>((i / loads) & 1)) &&
-        (threadIdx.x & 31) == 0)
-      atomicOr(status, 128);
-  }
+// A producer warp's whole run: the team's first warp issues the first copies, every warp
+// produces the team's stages, and the first warp waits for its last copies before the CTA exits.
+template <bool TMEM>
+__device__ __forceinline__ void produce_all(Sync* sy, int* status, unsigned char* st,
+                                            unsigned char* lb, int loads, int stages,
+                                            uint32_t a_taddr, int teams, const StageSource& src) {
+  const int warp = threadIdx.x >> 5, team = warp >> 2, p = threadIdx.x & 127;
+  const bool issuer = (warp & 3) == 0;
+  TeamLoads tl;
+  tl.init(team, src.n_minor);
+  if (issuer)
+    for (int j = 0; j < loads / teams && tl.k < src.total; ++j) {
+      tl.issue(sy, lb, src);
+      tl.step(teams, src.n_minor, loads);
+    }
+  Ring lr{team, 0u}, sr{team, 0u};
+  for (int64_t k = team; k < src.total && !warp_aborted(sy); k += teams)
+    if (!produce<TMEM>(sy, status, st, lb, lr, loads, sr, stages, a_taddr, p, teams, tl, src,
+                       issuer))
+      break;
+  if (issuer) tl.drain(sy, status, teams, loads, team);
 }
 
 // Shared set-up of both kernels: zeroed E stages (rows a group leaves unused must hold finite
@@ -511,13 +567,10 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
   const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, false, false);
 
   if (warp < prod_warps) {
-    // the stages of all passes in order (the passes matter only to the MMA thread and the loader)
-    const int p = tid & 127, team = warp >> 2;
-    Ring lr{team, 0u}, sr{team, 0u};
-    bool ok = true;
-    for (int k = team; k < nt * n_groups && ok && !warp_aborted(sy); k += teams)
-      ok = TMEM_A ? produce_tmem(sy, status, lb, lr, loads, sr, stages, tmem + a_col, p, teams)
-                  : produce(sy, status, st, lb, lr, loads, sr, stages, p, teams);
+    // the stages of all passes in order (the passes matter only to the MMA and loader warps)
+    const StageSource src{pc, gslots, gheader, n_slots, n_groups, nt, 0, t0, true,
+                          static_cast<int64_t>(nt) * n_groups};
+    produce_all<TMEM_A>(sy, status, st, lb, loads, stages, tmem + a_col, teams, src);
   } else if (warp == mma_warp) {
     Ring sr;
     bool ok = true;
@@ -550,11 +603,8 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
       __syncwarp();
     }
   } else if (warp == load_warp) {
-    // The loader warp interleaves two streams of copies without blocking on either: the packed
-    // products of the next stage (as soon as its load buffer is free) and the coefficient rows of
-    // the next pass (as soon as the last pass's MMAs have completed). Waiting for one while the
-    // other is due could stall the MMA warp on coefficients that are never issued. Its lanes run
-    // the loop together; the elected lane issues the copies.
+    // The loader warp copies the coefficient rows of each pass once the MMAs of the pass before
+    // have completed (the producers load their own stages).
     auto issue_coef = [&](int pass) {
       const int g0 = pass * gpp, ng = min(n_groups, g0 + gpp) - g0;
       if (tc::elect_one()) {
@@ -567,54 +617,16 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
       __syncwarp();
     };
     issue_coef(0);
-    int coef_next = 1;
-    int64_t next = 0;                   // stages loaded so far
-    Ring lr;
-    int lpass = 0, lu = 0, lg = 0;      // the next stage's pass, group within the pass and tile
-    int lng = min(n_groups, gpp);       // groups of that pass
-    uint64_t idle_since = 0;
-    while (!warp_aborted(sy) && (lpass < passes || coef_next < passes)) {
-      bool progress = false;
-      if (coef_next < passes &&
-          warp_poll(tc::smem_u32(&sy->pass), static_cast<uint32_t>((coef_next - 1) & 1))) {
-        issue_coef(coef_next++);
-        progress = true;
-      }
-      if (lpass < passes) {
-        const int b = lr.idx;
-        if (lr.round == 0 || warp_poll(tc::smem_u32(&sy->lempty[b]), (lr.round - 1u) & 1u)) {
-          if (tc::elect_one())
-            load_stage(lb + static_cast<size_t>(b) * kLoadBytes, tc::smem_u32(&sy->lfull[b]), pc,
-                       gslots, gheader, n_slots, lpass * gpp + lg, t0 + lu);
-          __syncwarp();
-          lr.next(loads);
-          ++next;
-          if (++lu == nt) {
-            lu = 0;
-            if (++lg == lng) {
-              lg = 0;
-              ++lpass;
-              lng = min(n_groups, (lpass + 1) * gpp) - lpass * gpp;
-            }
-          }
-          progress = true;
-        }
-      }
-      if (progress) {
-        idle_since = 0;
-        continue;
-      }
-      __nanosleep(64);  // leave the issue slots to the producers
-      const uint64_t now = tc::globaltimer_ns();
-      if (idle_since == 0) idle_since = now;
-      if (__shfl_sync(0xffffffffu, now - idle_since > kPollNs, 0)) {
+    int issued = 1;
+    for (int pass = 1; pass < passes && !warp_aborted(sy); ++pass) {
+      if (!warp_wait(tc::smem_u32(&sy->pass), static_cast<uint32_t>((pass - 1) & 1))) {
         fail_wait(sy, status, 64);
         break;
       }
+      issue_coef(pass);
+      issued = pass + 1;
     }
-    drain_loads(sy, status, loads, next);
-    if (!warp_wait(tc::smem_u32(&sy->cfull), static_cast<uint32_t>((coef_next - 1) & 1)) &&
-        lane == 0)
+    if (!warp_wait(tc::smem_u32(&sy->cfull), static_cast<uint32_t>((issued - 1) & 1)) && lane == 0)
       atomicOr(status, 128);
   }
   // every MMA of the CTA has completed once the last commit has
@@ -689,10 +701,8 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
 
   const int nt = tb - ta;
   if (warp < prod_warps && ng > 0) {
-    const int p = tid & 127, team = warp >> 2;
-    Ring lr{team, 0u}, sr{team, 0u};
-    for (int64_t k = team; k < total && !warp_aborted(sy); k += teams)
-      if (!produce(sy, status, st, lb, lr, loads, sr, stages, p, teams)) break;
+    const StageSource src{pc, gslots, gheader, n_slots, n_groups, ng, g0, ta, false, total};
+    produce_all<false>(sy, status, st, lb, loads, stages, 0u, teams, src);
   } else if (warp == mma_warp && ng > 0) {
     // windows of `win` consecutive stages (groups inner: different accumulators), issued
     // round-robin one K-step at a time, as in the mult kernel
@@ -711,13 +721,9 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
       }
     }
   } else if (warp == load_warp && ng > 0) {
-    // Q of tile tl waits only for the MMAs of tile tl - 2, whose stages were loaded before: the
-    // loader may block on either kind of wait without stalling the pipeline for good
-    int64_t issued = 0;
+    // Q of tile tl waits only for the MMAs of tile tl - 2 (the producers load their own stages)
     int q_issued = 0;
-    Ring lr;
-    bool ok = true;
-    for (int tl = 0; tl < nt && ok && !warp_aborted(sy); ++tl) {
+    for (int tl = 0; tl < nt && !warp_aborted(sy); ++tl) {
       const int b = tl & 1, use = tl >> 1;
       if (use > 0 &&
           !warp_wait(tc::smem_u32(&sy->qempty[b]), static_cast<uint32_t>((use - 1) & 1))) {
@@ -732,12 +738,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
       }
       __syncwarp();
       q_issued = tl + 1;
-      for (int gl = 0; gl < ng && ok; ++gl) {
-        ok = load(sy, status, lb, lr, loads, pc, gslots, gheader, n_slots, g0 + gl, ta + tl);
-        if (ok) ++issued;
-      }
     }
-    drain_loads(sy, status, loads, issued);
     for (int tl = q_issued > 2 ? q_issued - 2 : 0; tl < q_issued; ++tl)
       if (!warp_wait(tc::smem_u32(&sy->qfull[tl & 1]), static_cast<uint32_t>((tl >> 1) & 1)) &&
           lane == 0)

@@ -50,7 +50,7 @@ struct BlockShape {
   int loads = 6;           // stages of packed products in flight (bulk copies ahead of use)
   int mult_tmem = 1;       // mult keeps its A operand (the stages of E) in tensor memory
   int window = 2;          // stages whose MMAs one issue round interleaves (at most `stages`)
-  int teams = 2;           // producer teams of 4 warps, each writing every teams-th stage
+  int teams = 3;           // producer teams of 4 warps, each writing every teams-th stage
                            // (at most `stages` and `loads`)
 };
 
