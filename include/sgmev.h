@@ -108,7 +108,9 @@ SGMEV_API int sgmev_device_count(void);
  * exact to the fit's tolerance).
  * "multt_batch": "1" (default), "2" or "4" — points per read-modify-write round of the owner's
  * cell sums in the FP16 multTranspose (the same bits for each; a launch-shape choice of the
- * autotuner, sgpp_gb300.autotune).
+ * autotuner, sgpp_gb300.autotune). "multt_banks": "1" (default) or "2" — banks of cell sums per
+ * owner in the FP16 multTranspose (two independent read-modify-write chains; other last bits
+ * than one bank; an autotuner choice).
  * "basis": "linear" (default) or "modlinear" — the basis of the grid. level_pow2/index stay the
  * (2^l, i) arrays of getLevelIndexArraysForEval for both (a ModLinear grid has the same points).
  * ModLinear functions next to a face extrapolate linearly beyond it, as the reference's mask
@@ -237,10 +239,11 @@ SGMEV_API double sgmev_get_duration(sgmev_op* op);
  * every stream it used. */
 SGMEV_API int sgmev_set_stream(sgmev_op* op, void* stream);
 
-/* Change launch-shape knobs of a live operator: params_json may hold only "multt_batch" and the
- * "block_mult_tiles", "block_mult_groups", "block_multt_groups", "block_stages", "block_loads",
- * "block_window", "block_teams", "block_mult_a" knobs (see
- * sgmev_create); they change no result bits except how the block products are cut into launches.
+/* Change launch-shape knobs of a live operator: params_json may hold only "multt_batch",
+ * "multt_banks" and the "block_mult_tiles", "block_mult_groups", "block_multt_groups",
+ * "block_stages", "block_loads", "block_window", "block_teams", "block_mult_a" knobs (see
+ * sgmev_create); they change no result bits except the order of the FP16 multTranspose's
+ * additions (multt_banks) and how the block products are cut into launches.
  * No counterpart in the reference (whose OpenCL kernels take such parameters from a
  * configuration file written by StaticParameterTuner,
  * datadriven/src/sgpp/datadriven/application/StaticParameterTuner.cpp:297-417); used by the
@@ -258,7 +261,9 @@ SGMEV_API int64_t sgmev_kernel_launches(const sgmev_op* op);
  * The same operator applied to 16 vectors at once, on the 5th-generation tensor cores: per tile of
  * 128 data points and group of 128 grid positions, the products of the materialised subspace
  * products (rounded to BF16, 2^-8 relative) with the 16 vectors (split into BF16 high and low
- * parts, about 2^-16) are tcgen05 MMAs accumulating in FP32. No counterpart in the reference,
+ * parts, about 2^-16) are tcgen05 MMAs accumulating in FP32; with params "block_products": "f16"
+ * the products are FP16 (2^-11) and the vectors FP16 high and low parts (about 2^-22), every
+ * operand scaled by a power of two into FP16's range. No counterpart in the reference,
  * which applies OperationMultipleEval::mult / multTranspose (OperationMultipleEval.hpp:55, :81)
  * to one vector at a time; column k here equals those products of vector k to BF16 accuracy.
  * Needs the subspace algorithm with materialised products (params "algo": "subspace", the default

@@ -11,6 +11,7 @@ themselves with CUDA events (sgmev_profile), and the parameters are set on the l
 
 Tunables:
   multT16   "multt_batch"            points per read-modify-write round of the FP16 multTranspose
+            "multt_banks"            banks of cell sums per owner (2: two independent chains)
   block     "block_window", "block_mult_a", "block_mult_tiles", "block_stages",
             "block_multt_groups"
                                       the tensor-core products with 16 right-hand sides
@@ -48,7 +49,8 @@ class TunableParameter:
 
 
 TUNABLES: Dict[str, List[TunableParameter]] = {
-    "multT16": [TunableParameter("multt_batch", [1, 2, 4])],
+    "multT16": [TunableParameter("multt_batch", [1, 2, 4]),
+                TunableParameter("multt_banks", [1, 2])],
     "block": [TunableParameter("block_window", [1, 2]),
               TunableParameter("block_mult_a", ["tmem", "smem"]),
               TunableParameter("block_mult_tiles", [4, 8]),

@@ -31,7 +31,7 @@ import sgpp_gb300 as sg  # noqa: E402
 from sgpp_gb300.serving import MixGenerator  # noqa: E402
 
 
-def block_pool(probs, lam: float, epsilon: float, workers: int):
+def block_pool(probs, lam: float, epsilon: float, workers: int, params=None):
     """Every problem's 16 right-hand sides as one block fit (sgmev_fit_block: BF16 tensor-core
     inner solves, df64 residuals) on its own operator and stream, `workers` problems at a time.
     A problem the block products do not take (a subspace above 128 cells, or products too large
@@ -56,7 +56,10 @@ def block_pool(probs, lam: float, epsilon: float, workers: int):
                 return
             g, X, Y = probs[k]
             try:
-                op = sg.createOperationMultipleEval(g, X)
+                cfg = sg.OperationMultipleEvalConfiguration(
+                    sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
+                    parameters=dict(params or {}))
+                op = sg.createOperationMultipleEval(g, X, cfg)
                 try:
                     a, its, _ = op.fitBlock(np.ascontiguousarray(Y.T), lam, 100000, epsilon)
                     alphas[k], paths[k], steps[k] = a.T, "block", int(max(its))
@@ -98,6 +101,10 @@ def main() -> int:
                     help="batch: the batch engine (dense kernels, one persistent launch per "
                          "phase); block: per-problem block fits on the tensor cores")
     ap.add_argument("--workers", type=int, default=4, help="block engine: problems in flight")
+    ap.add_argument("--plain", type=int, default=1,
+                    help="block engine: time the plain FP64 path on every problem (0: skip)")
+    ap.add_argument("--param", action="append", default=[], metavar="KEY=VALUE",
+                    help="block engine: operator knob of the block fits (repeatable)")
     args = ap.parse_args()
     if args.engine == "block":
         return main_block(args)
@@ -168,8 +175,9 @@ def main_block(args) -> int:
     probs = [gen.draw(args.rhs) for _ in range(args.problems)]
     if args.rhs != sg.SGMEV_BLOCK_RHS:
         raise SystemExit(f"--engine block takes --rhs {sg.SGMEV_BLOCK_RHS}")
-    block_pool(probs[:2], args.lam, args.epsilon, 1)  # warm-up (library and kernels loaded)
-    sec, alphas, paths, steps = block_pool(probs, args.lam, args.epsilon, args.workers)
+    params = dict(kv.split("=", 1) for kv in args.param)
+    block_pool(probs[:2], args.lam, args.epsilon, 1, params)  # warm-up (library, kernels)
+    sec, alphas, paths, steps = block_pool(probs, args.lam, args.epsilon, args.workers, params)
     errs = []
     for k in range(min(args.check, args.problems)):
         g, X, Y = probs[k]
@@ -191,15 +199,41 @@ def main_block(args) -> int:
     work = np.array([g.getSize() * X.shape[0] * g.getDimension() for g, X, _ in probs], float)
     share = work[: len(seq)].sum() / work.sum()
     solves = args.problems * args.rhs
+    # the plain per-problem FP64 path: every problem's first right-hand side as a plain
+    # FP64-accurate CG fit (the reference's algorithm) on a df64 operator, products built before
+    # the clock starts; its right-hand sides are independent fits of the same cost, so all
+    # problems x all right-hand sides take rhs x the summed time
+    plain = None
+    if args.plain:
+        t_plain = 0.0
+        for g, X, Y in probs:
+            cfg = sg.OperationMultipleEvalConfiguration(
+                sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
+                parameters={"precision": "df64"})
+            op = sg.createOperationMultipleEval(g, X, cfg)
+            y0 = np.ascontiguousarray(Y[:, 0])
+            op.fit(y0, args.lam, 8, args.epsilon, mode=sg.SGMEV_SOLVE_PLAIN)  # builds the products
+            t1 = time.perf_counter()
+            op.fit(y0, args.lam, 100000, args.epsilon, mode=sg.SGMEV_SOLVE_PLAIN)
+            t_plain += time.perf_counter() - t1
+            op.close()
+        plain = {"solves_per_sec": solves / (args.rhs * t_plain),
+                 "seconds_all_problems_one_rhs": t_plain,
+                 "what": "plain FP64-accurate CG (SGMEV_SOLVE_PLAIN) on a df64 operator per "
+                         "problem and right-hand side, one after another; every problem timed "
+                         "on its first right-hand side"}
     line = {
         "metric": "batched_solves_per_sec", "value": solves / sec, "unit": "solves/s",
-        "engine": "block", "problems": args.problems, "rhs": args.rhs, "seconds": sec,
+        "engine": "block", "params": params, "problems": args.problems, "rhs": args.rhs,
+        "seconds": sec,
         "workers": args.workers,
         "paths": {p: paths.count(p) for p in set(paths)},
         "inner_steps": {"min": int(min(steps)), "max": int(max(steps))},
         "alpha_rel_err_vs_fp64": {"max": max(errs) if errs else None, "checked_solves": len(errs)},
         "sequential_single_mixed_solves_per_sec_est": (
             args.problems * share / sum(seq) if seq else None),
+        "plain_fp64_path": plain,
+        "speedup_vs_plain_fp64": (solves / sec) / plain["solves_per_sec"] if plain else None,
         "sequential_note": (f"one right-hand side of the first {len(seq)} problems by the "
                             "single-target mixed fit, rescaled by their share of the N*M*d work"),
         "config": {"mix": "d 2..12, level 3..7, M log-uniform [1e3, 2^20], uniform data",

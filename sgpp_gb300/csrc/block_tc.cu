@@ -16,9 +16,11 @@
 // finishes without further work, after its issued MMAs have completed and its tensor memory is
 // freed.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -126,6 +128,22 @@ __device__ __forceinline__ void split_bf16(float v, uint16_t* hi, uint16_t* lo) 
   const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
   *hi = *reinterpret_cast<const uint16_t*>(&h);
   *lo = *reinterpret_cast<const uint16_t*>(&l);
+}
+
+// FP16 high/low split: v = hi + lo to about 22 significant bits (v already scaled into FP16's range)
+__device__ __forceinline__ void split_f16(float v, uint16_t* hi, uint16_t* lo) {
+  const __half h = __float2half_rn(v);
+  const __half l = __float2half_rn(v - __half2float(h));
+  *hi = *reinterpret_cast<const uint16_t*>(&h);
+  *lo = *reinterpret_cast<const uint16_t*>(&l);
+}
+
+template <bool F16>
+__device__ __forceinline__ void split_pair(float v, uint16_t* hi, uint16_t* lo) {
+  if constexpr (F16)
+    split_f16(v, hi, lo);
+  else
+    split_bf16(v, hi, lo);
 }
 
 // byte offset of element (column n, row r) of a 32-column operand block in the K-major layout
@@ -549,7 +567,8 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
     const uint32_t* __restrict__ pc, const BlockHeader* __restrict__ gheader,
     const int2* __restrict__ gslots, const uint16_t* __restrict__ coef, int n_groups, int n_slots, int64_t mpad, int64_t m, int n_tiles,
     int tiles, int gpp, int teams, int stages, int loads, int win, uint32_t tmem_cols, uint16_t* __restrict__ qtiles,
-    double* __restrict__ out64, int* __restrict__ status) {
+    double* __restrict__ out64, int* __restrict__ status, int f16, const float* __restrict__ scales,
+    float pscale, float qfac) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int smem_stages = TMEM_A ? 0 : stages;
   unsigned char* st = smem;
@@ -564,7 +583,8 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
   block_setup(sy, st, smem_stages, stages, loads, tmem_cols, mma_warp);
   const uint32_t tmem = sy->tmem;
   const uint32_t a_col = static_cast<uint32_t>(tiles * kBlockCols);  // first A column (TMEM_A)
-  const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, false, false);
+  const uint32_t idesc = f16 ? tc::idesc_f16(128, kBlockCols, false, false)
+                             : tc::idesc_bf16(128, kBlockCols, false, false);
 
   if (warp < prod_warps) {
     // the stages of all passes in order (the passes matter only to the MMA and loader warps)
@@ -655,10 +675,18 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
 #pragma unroll
       for (int c = 0; c < kBlockRhs; ++c) {
         const float q = __uint_as_float(r0[c]) + __uint_as_float(r1[c]);
-        if (out64) out64[static_cast<int64_t>(c) * mpad + j] = j < m ? static_cast<double>(q) : 0.0;
+        // FP16: the accumulators hold pscale x scales[c] x Q (powers of two, undone exactly)
+        if (out64) {
+          const double unscale =
+              f16 ? 1.0 / (static_cast<double>(scales[c]) * static_cast<double>(pscale)) : 1.0;
+          out64[static_cast<int64_t>(c) * mpad + j] = j < m ? static_cast<double>(q) * unscale : 0.0;
+        }
         if (qt) {
           uint16_t hi, lo;
-          split_bf16(j < m ? q : 0.0f, &hi, &lo);
+          if (f16)
+            split_f16(j < m ? q * qfac : 0.0f, &hi, &lo);
+          else
+            split_bf16(j < m ? q : 0.0f, &hi, &lo);
           qt[opnd_off(c, p) / 2] = hi;
           qt[opnd_off(c + kBlockRhs, p) / 2] = lo;
         }
@@ -682,7 +710,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
     const uint32_t* __restrict__ pc, const BlockHeader* __restrict__ gheader,
     const int2* __restrict__ gslots, const uint16_t* __restrict__ qtiles, int n_groups, int n_slots, int64_t mpad, int n_tiles, int gpc,
     int streams, int teams, int stages, int loads, int win, uint32_t tmem_cols, int64_t rows,
-    double* __restrict__ part, int* __restrict__ status) {
+    double* __restrict__ part, int* __restrict__ status, int f16) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* st = smem;
   unsigned char* lb = st + static_cast<size_t>(stages) * kStageBytes;
@@ -697,7 +725,8 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
   const int prod_warps = kTeamWarps * teams, mma_warp = prod_warps, load_warp = prod_warps + 1;
   block_setup(sy, st, stages, stages, loads, tmem_cols, mma_warp);
   const uint32_t tmem = sy->tmem;
-  const uint32_t idesc = tc::idesc_bf16(128, kBlockCols, true, false);
+  const uint32_t idesc = f16 ? tc::idesc_f16(128, kBlockCols, true, false)
+                             : tc::idesc_bf16(128, kBlockCols, true, false);
 
   const int nt = tb - ta;
   if (warp < prod_warps && ng > 0) {
@@ -777,40 +806,54 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_multt_kernel(
   if (warp == mma_warp) tc::tmem_dealloc(tmem, tmem_cols);
 }
 
-// out[c][gp] = sum over streams (in order) of the partial rows + scale * add[c][gp]
+// out[c][gp] = sum over streams (in order) of the partial rows / (qscale[c] x pscale)
+// + scale * add[c][gp] (qscale: the Q tiles' FP16 scales, or null; pscale: the products' scale).
+// Threads walk the rows, so that the stream sums read the partial rows coalesced; a row that is
+// no grid point's is skipped, and the padding entries gp in [n, npad) are zero.
 __global__ void block_finish_kernel(const double* __restrict__ part, int streams, int64_t rows,
-                                    const int* __restrict__ gp_row, int64_t n, int64_t npad,
+                                    const int* __restrict__ row_gp, int64_t n, int64_t npad,
                                     double* __restrict__ out, const double* __restrict__ add,
-                                    double scale) {
-  const int64_t total = npad * kBlockRhs;
-  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
-       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const int c = static_cast<int>(k / npad);
-    const int64_t gp = k - static_cast<int64_t>(c) * npad;
-    double v = 0.0;
-    if (gp < n) {
-      const int64_t r = gp_row[gp];
-      for (int sidx = 0; sidx < streams; ++sidx)
-        v += part[(static_cast<int64_t>(sidx) * kBlockRhs + c) * rows + r];
-      if (add) v += scale * add[k];
-    }
-    out[k] = v;
-  }
-}
-
-// coefficient rows: p column-major FP64 [16][npad] in grid order -> BF16 (hi, lo) operand blocks
-__global__ void block_coef_kernel(const double* __restrict__ p, int64_t npad,
-                                  const int* __restrict__ row_gp, int64_t rows,
-                                  uint16_t* __restrict__ coef) {
+                                    double scale, const float* __restrict__ qscale,
+                                    double pscale) {
   const int64_t total = rows * kBlockRhs;
   for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
        k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const int c = static_cast<int>(k / rows);
     const int64_t r = k - static_cast<int64_t>(c) * rows;
     const int gp = row_gp[r];
-    const float v = gp >= 0 ? static_cast<float>(p[static_cast<int64_t>(c) * npad + gp]) : 0.0f;
+    if (gp < 0) continue;
+    double v = 0.0;
+    for (int sidx = 0; sidx < streams; ++sidx)
+      v += part[(static_cast<int64_t>(sidx) * kBlockRhs + c) * rows + r];
+    if (qscale) v /= static_cast<double>(qscale[c]) * pscale;
+    const int64_t o = static_cast<int64_t>(c) * npad + gp;
+    if (add) v += scale * add[o];
+    out[o] = v;
+  }
+  const int64_t pad = npad - n;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+       k < pad * kBlockRhs; k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = static_cast<int>(k / pad);
+    out[static_cast<int64_t>(c) * npad + n + (k - static_cast<int64_t>(c) * pad)] = 0.0;
+  }
+}
+
+// coefficient rows: p column-major FP64 [16][npad] in grid order -> BF16 or FP16 (hi, lo) operand
+// blocks (FP16: scaled by scales[c])
+template <bool F16>
+__global__ void block_coef_kernel(const double* __restrict__ p, int64_t npad,
+                                  const int* __restrict__ row_gp, int64_t rows,
+                                  uint16_t* __restrict__ coef, const float* __restrict__ scales) {
+  const int64_t total = rows * kBlockRhs;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = static_cast<int>(k / rows);
+    const int64_t r = k - static_cast<int64_t>(c) * rows;
+    const int gp = row_gp[r];
+    float v = gp >= 0 ? static_cast<float>(p[static_cast<int64_t>(c) * npad + gp]) : 0.0f;
+    if constexpr (F16) v *= scales[c];
     uint16_t hi, lo;
-    split_bf16(v, &hi, &lo);
+    split_pair<F16>(v, &hi, &lo);
     const int64_t g = r >> 7;
     const int rr = static_cast<int>(r & 127);
     coef[g * 4096 + opnd_off(c, rr) / 2] = hi;
@@ -818,17 +861,20 @@ __global__ void block_coef_kernel(const double* __restrict__ p, int64_t npad,
   }
 }
 
-// Q tiles from a data-side block v column-major FP64 [16][mpad] (zero beyond m)
+// Q tiles from a data-side block v column-major FP64 [16][mpad] (zero beyond m; FP16: scaled by
+// qscale[c])
+template <bool F16>
 __global__ void block_qtile_kernel(const double* __restrict__ v, int64_t mpad, int64_t m,
-                                   uint16_t* __restrict__ qtiles) {
+                                   uint16_t* __restrict__ qtiles, const float* __restrict__ qscale) {
   const int64_t total = mpad * kBlockRhs;
   for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
        k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const int c = static_cast<int>(k / mpad);
     const int64_t j = k - static_cast<int64_t>(c) * mpad;
-    const float x = j < m ? static_cast<float>(v[k]) : 0.0f;
+    float x = j < m ? static_cast<float>(v[k]) : 0.0f;
+    if constexpr (F16) x *= qscale[c];
     uint16_t hi, lo;
-    split_bf16(x, &hi, &lo);
+    split_pair<F16>(x, &hi, &lo);
     const int64_t t = j >> 7;
     const int pp = static_cast<int>(j & 127);
     qtiles[t * 4096 + opnd_off(c, pp) / 2] = hi;
@@ -836,11 +882,13 @@ __global__ void block_qtile_kernel(const double* __restrict__ v, int64_t mpad, i
   }
 }
 
-// packed BF16 products of every slot from the materialised float-float products and cells
-template <typename CW>
+// packed BF16 or FP16 products of every slot from the materialised float-float products and
+// cells; FP16 products are scaled by pscale (a power of two that keeps them out of FP16's
+// subnormal range, where they would lose bits)
+template <typename CW, bool F16>
 __global__ void block_pack_kernel(const float4* __restrict__ pmat, const CW* __restrict__ cmat,
                                   int64_t s_pad, const int* __restrict__ slot_sub, int n_slots,
-                                  int64_t m, int64_t mpad, uint32_t* __restrict__ pc) {
+                                  int64_t m, int64_t mpad, uint32_t* __restrict__ pc, float pscale) {
   constexpr int kBits = sizeof(CW) * 2;
   const int64_t total = static_cast<int64_t>(n_slots) * mpad;
   for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
@@ -857,11 +905,65 @@ __global__ void block_pack_kernel(const float4* __restrict__ pmat, const CW* __r
       const int lane4 = static_cast<int>(j & 3);
       const float v = lane4 == 0 ? q.x : lane4 == 1 ? q.y : lane4 == 2 ? q.z : q.w;
       const uint32_t cell = (static_cast<uint32_t>(cmat[at]) >> (kBits * lane4)) & ((1u << kBits) - 1u);
-      const __nv_bfloat16 b = __float2bfloat16_rn(v);
-      w = static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(&b)) | (cell << 20);
+      uint16_t bits;
+      if constexpr (F16) {
+        const __half h = __float2half_rn(v * pscale);
+        bits = *reinterpret_cast<const uint16_t*>(&h);
+      } else {
+        const __nv_bfloat16 b = __float2bfloat16_rn(v);
+        bits = *reinterpret_cast<const uint16_t*>(&b);
+      }
+      w = static_cast<uint32_t>(bits) | (cell << 20);
     }
     pc[k] = w;
   }
+}
+
+// *out = max(*out, largest |x| of n floats) as float bits
+__global__ void block_absmax_kernel(const float* __restrict__ x, int64_t n,
+                                    unsigned* __restrict__ out) {
+  unsigned big = 0u;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    big = max(big, __float_as_uint(fabsf(x[i])));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) big = max(big, __shfl_xor_sync(0xffffffffu, big, o));
+  if ((threadIdx.x & 31) == 0 && big) atomicMax(out, big);
+}
+
+// colmax[c] = max(colmax[c], largest |v[c][i]| for i < count) as float bits (v column-major with
+// column stride `pad`); grid (blocks, 16)
+__global__ void block_colmax_kernel(const double* __restrict__ v, int64_t pad, int64_t count,
+                                    unsigned* __restrict__ colmax) {
+  const int c = blockIdx.y;
+  const double* col = v + static_cast<int64_t>(c) * pad;
+  double big = 0.0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < count;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    big = fmax(big, fabs(col[i]));
+  unsigned b = __float_as_uint(static_cast<float>(big));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+  if ((threadIdx.x & 31) == 0 && b) atomicMax(colmax + c, b);
+}
+
+// Power-of-two scales from the column maxima: dst[c] maps column c's largest |value| into
+// [2^13, 2^14) (1 for a zero column); with with_q also dst[16 + c] = dst[c] x 2^-shift (the scale
+// of the Q tiles block_mult writes). Resets colmax. One warp.
+__global__ void block_scale_kernel(unsigned* __restrict__ colmax, float* __restrict__ dst,
+                                   int with_q, int shift) {
+  const int c = threadIdx.x;
+  if (c >= kBlockRhs) return;
+  const float big = __uint_as_float(colmax[c]);
+  colmax[c] = 0u;
+  int e = 0;
+  float sc = 1.0f;
+  if (big > 0.0f && isfinite(big)) {
+    (void)frexpf(big, &e);  // big in [2^(e-1), 2^e)
+    sc = ldexpf(1.0f, max(-120, min(120, 14 - e)));
+  }
+  dst[c] = sc;
+  if (with_q) dst[kBlockRhs + c] = ldexpf(sc, -shift);
 }
 
 }  // namespace
@@ -1062,8 +1164,8 @@ unsigned grid_for(int64_t n, int num_sms) {
 }  // namespace
 
 void block_free(BlockPlan* b) {
-  void* ptrs[] = {b->row_gp, b->gp_row, b->gheader, b->gslots, b->pc,
-                  b->coef,   b->qtiles, b->part,  b->status};
+  void* ptrs[] = {b->row_gp, b->gp_row, b->gheader, b->gslots, b->pc,     b->coef,
+                  b->qtiles, b->part,   b->status,  b->scales, b->colmax};
   for (void* q : ptrs) dev_free(q, b->stream);
   *b = BlockPlan{};
 }
@@ -1078,16 +1180,27 @@ bool block_shape_ok(const BlockShape& sh, int smem_cap) {
          multt_smem(sh) <= static_cast<size_t>(smem_cap);
 }
 
-static int multt_streams(const BlockPlan& b, int num_sms) {
-  const int passes = static_cast<int>(cdiv(b.n_groups, b.shape.multt_groups));
+// The multT accumulators (FP32 in tensor memory) take at most about kChainTiles tiles of one
+// stream before they are written out as FP64 partial rows: the tensor cores round the running
+// sums of a long chain of MMAs toward zero, which biased the sums of 546 tiles by -3e-5 on
+// average (and up to -3e-4) in tests against the FP64 products. Streams beyond one CTA per SM
+// run as further waves of CTAs; their partial rows take at most kPartBudget bytes.
+constexpr int64_t kChainTiles = 64;
+constexpr int64_t kPartBudget = int64_t(1) << 30;
+
+static int multt_stream_cap(const BlockPlan& b, int num_sms) {
+  const int64_t n_tiles = b.mpad / kBlockTile;
+  const int64_t by_budget = std::max<int64_t>(1, kPartBudget / (8 * kBlockRhs * std::max<int64_t>(b.rows, 1)));
   return static_cast<int>(std::max<int64_t>(
-      1, std::min<int64_t>(num_sms / std::max(1, passes), b.mpad / kBlockTile)));
+      1, std::min<int64_t>(std::min(n_tiles, by_budget),
+                           std::max<int64_t>(num_sms, 2 * cdiv(n_tiles, kChainTiles)))));
 }
 
-bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cudaStream_t s,
-                 int num_sms, std::string* err) {
+bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, bool f16,
+                 cudaStream_t s, int num_sms, std::string* err) {
   block_free(b);
   b->stream = s;
+  b->f16 = f16;
   if (!sub.pmat || !sub.cmat || sub.h_sub.empty()) {
     *err = "block products need the materialised subspace products";
     return false;
@@ -1158,7 +1271,7 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
   b->n = sub.n;
   b->m = m;
   b->mpad = mpad;
-  b->part_streams = multt_streams(*b, num_sms);
+  b->part_streams = multt_stream_cap(*b, num_sms);
   int* d_slot_sub = nullptr;
   auto alloc = [&](auto** q, size_t bytes) { return dev_malloc(q, bytes, s) == cudaSuccess; };
   auto put = [&](void* dst, const void* src, size_t bytes) {
@@ -1172,23 +1285,60 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
             alloc(&b->coef, kCoefBytes * static_cast<size_t>(n_groups)) &&
             alloc(&b->qtiles, kQBytes * static_cast<size_t>(mpad / kBlockTile)) &&
             alloc(&b->part, sizeof(double) * b->part_streams * kBlockRhs * rows) &&
-            alloc(&b->status, sizeof(int));
+            alloc(&b->status, sizeof(int)) && alloc(&b->scales, sizeof(float) * 2 * kBlockRhs) &&
+            alloc(&b->colmax, sizeof(unsigned) * kBlockRhs);
   ok = ok && put(b->row_gp, row_gp.data(), sizeof(int) * rows) &&
        put(b->gp_row, gp_row.data(), sizeof(int) * sub.n) &&
        put(b->gheader, gheader.data(), sizeof(BlockHeader) * gheader.size()) &&
        put(b->gslots, gslots.data(), sizeof(int2) * gslots.size()) &&
        put(d_slot_sub, slot_sub.data(), sizeof(int) * slot_sub.size()) &&
-       cudaMemsetAsync(b->status, 0, sizeof(int), s) == cudaSuccess;
+       cudaMemsetAsync(b->status, 0, sizeof(int), s) == cudaSuccess &&
+       cudaMemsetAsync(b->colmax, 0, sizeof(unsigned) * kBlockRhs, s) == cudaSuccess;
+  // the largest product: FP16 products are scaled by pe = 2^(14 - e), pmax in [2^(e-1), 2^e), so
+  // that the largest lies in [2^13, 2^14) and products down to 2^-27 of it stay normal; the Q tiles
+  // take qshift: |Q| <= n_slots x the largest product x the largest coefficient
+  unsigned pmax_bits = 0u;
+  ok = ok &&
+       (block_absmax_kernel<<<grid_for(sub.mat_mpad * sub.s_pad, num_sms), 256, 0, s>>>(
+            reinterpret_cast<const float*>(sub.pmat), sub.mat_mpad * sub.s_pad, b->colmax),
+        cudaGetLastError() == cudaSuccess) &&
+       cudaMemcpyAsync(&pmax_bits, b->colmax, sizeof(unsigned), cudaMemcpyDeviceToHost, s) ==
+           cudaSuccess &&
+       cudaStreamSynchronize(s) == cudaSuccess &&
+       cudaMemsetAsync(b->colmax, 0, sizeof(unsigned) * kBlockRhs, s) == cudaSuccess;
+  if (ok) {
+    float pmax;
+    std::memcpy(&pmax, &pmax_bits, sizeof(pmax));
+    int e = 0;
+    if (pmax > 0.0f && std::isfinite(pmax)) (void)std::frexp(pmax, &e);
+    b->pexp = f16 && pmax > 0.0f ? std::max(-60, std::min(60, 14 - e)) : 0;
+    // the accumulators of block_mult reach n_slots x 2^pexp pmax x 2^14; the Q tiles keep 2^14
+    const double bound = static_cast<double>(b->n_slots) *
+                         std::max(1.0, std::ldexp(static_cast<double>(pmax), b->pexp)) * 16384.0;
+    int total = 0;
+    while (total < 120 && std::ldexp(16384.0, total) < bound) ++total;
+    b->qshift = f16 ? total - b->pexp : 0;
+  }
   if (ok) {
     const unsigned blocks = grid_for(static_cast<int64_t>(b->n_slots) * mpad, num_sms);
-    if (sub.cell_bits == 4)
-      block_pack_kernel<uint16_t><<<blocks, 256, 0, s>>>(
-          sub.pmat, static_cast<const uint16_t*>(sub.cmat), sub.s_pad, d_slot_sub, b->n_slots, m,
-          mpad, b->pc);
-    else
-      block_pack_kernel<uint32_t><<<blocks, 256, 0, s>>>(
-          sub.pmat, static_cast<const uint32_t*>(sub.cmat), sub.s_pad, d_slot_sub, b->n_slots, m,
-          mpad, b->pc);
+    const float pscale = std::ldexp(1.0f, b->pexp);
+    if (sub.cell_bits == 4) {
+      const auto* cm = static_cast<const uint16_t*>(sub.cmat);
+      if (f16)
+        block_pack_kernel<uint16_t, true><<<blocks, 256, 0, s>>>(sub.pmat, cm, sub.s_pad, d_slot_sub,
+                                                                 b->n_slots, m, mpad, b->pc, pscale);
+      else
+        block_pack_kernel<uint16_t, false><<<blocks, 256, 0, s>>>(sub.pmat, cm, sub.s_pad, d_slot_sub,
+                                                                  b->n_slots, m, mpad, b->pc, 1.0f);
+    } else {
+      const auto* cm = static_cast<const uint32_t*>(sub.cmat);
+      if (f16)
+        block_pack_kernel<uint32_t, true><<<blocks, 256, 0, s>>>(sub.pmat, cm, sub.s_pad, d_slot_sub,
+                                                                 b->n_slots, m, mpad, b->pc, pscale);
+      else
+        block_pack_kernel<uint32_t, false><<<blocks, 256, 0, s>>>(sub.pmat, cm, sub.s_pad, d_slot_sub,
+                                                                  b->n_slots, m, mpad, b->pc, 1.0f);
+    }
     ok = cudaGetLastError() == cudaSuccess;
   }
   dev_free(d_slot_sub, s);
@@ -1205,8 +1355,18 @@ bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cuda
 cudaError_t block_mult(BlockPlan& b, cudaStream_t s, const double* p, int64_t npad,
                        double* out64, int num_sms) {
   const BlockShape& sh = b.shape;
-  block_coef_kernel<<<grid_for(b.rows * kBlockRhs, num_sms), 256, 0, s>>>(p, npad, b.row_gp,
-                                                                         b.rows, b.coef);
+  if (b.f16) {
+    // per-column scales of the coefficient rows and of the Q tiles this product writes
+    block_colmax_kernel<<<dim3(static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(64, cdiv(b.n, 256)))),
+                               kBlockRhs),
+                          256, 0, s>>>(p, npad, b.n, b.colmax);
+    block_scale_kernel<<<1, 32, 0, s>>>(b.colmax, b.scales, 1, b.qshift);
+    block_coef_kernel<true><<<grid_for(b.rows * kBlockRhs, num_sms), 256, 0, s>>>(
+        p, npad, b.row_gp, b.rows, b.coef, b.scales);
+  } else {
+    block_coef_kernel<false><<<grid_for(b.rows * kBlockRhs, num_sms), 256, 0, s>>>(
+        p, npad, b.row_gp, b.rows, b.coef, nullptr);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const uint32_t cols = tmem_cols_for(cdiv(mult_tmem_need(sh), kBlockCols));
@@ -1221,7 +1381,8 @@ cudaError_t block_mult(BlockPlan& b, cudaStream_t s, const double* p, int64_t np
   const unsigned ctas = static_cast<unsigned>(cdiv(n_tiles, sh.mult_tiles));
   kern<<<ctas, (kTeamWarps * sh.teams + 2) * 32, smem, s>>>(
       b.pc, b.gheader, b.gslots, b.coef, b.n_groups, b.n_slots, b.mpad, b.m, n_tiles, sh.mult_tiles,
-      gpp, sh.teams, sh.stages, sh.loads, std::min(sh.window, sh.stages), cols, b.qtiles, out64, b.status);
+      gpp, sh.teams, sh.stages, sh.loads, std::min(sh.window, sh.stages), cols, b.qtiles, out64, b.status,
+      b.f16 ? 1 : 0, b.scales, std::ldexp(1.0f, b.pexp), std::ldexp(1.0f, -(b.qshift + b.pexp)));
   return cudaGetLastError();
 }
 
@@ -1230,28 +1391,66 @@ cudaError_t block_multt(BlockPlan& b, cudaStream_t s, const double* v, int64_t n
   const BlockShape& sh = b.shape;
   cudaError_t e;
   if (v) {
-    block_qtile_kernel<<<grid_for(b.mpad * kBlockRhs, num_sms), 256, 0, s>>>(v, b.mpad, b.m,
-                                                                             b.qtiles);
+    if (b.f16) {
+      block_colmax_kernel<<<dim3(static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(num_sms, cdiv(b.m, 256)))),
+                                 kBlockRhs),
+                            256, 0, s>>>(v, b.mpad, b.m, b.colmax);
+      block_scale_kernel<<<1, 32, 0, s>>>(b.colmax, b.scales + kBlockRhs, 0, 0);
+      block_qtile_kernel<true><<<grid_for(b.mpad * kBlockRhs, num_sms), 256, 0, s>>>(
+          v, b.mpad, b.m, b.qtiles, b.scales + kBlockRhs);
+    } else {
+      block_qtile_kernel<false><<<grid_for(b.mpad * kBlockRhs, num_sms), 256, 0, s>>>(
+          v, b.mpad, b.m, b.qtiles, nullptr);
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
+  // passes over the groups x streams of tiles: streams of at most about kChainTiles tiles (as
+  // many as the partial rows allow), at least one CTA per SM; of those splits the one whose waves
+  // of CTAs carry the fewest stages (waves x groups per pass x tiles per stream), at most
+  // multt_groups groups per pass and at least kMaxWindow (or all of them): consecutive stages then
+  // feed different accumulators, so the MMA window does not change the order of any
+  // accumulator's additions.
+  const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
+  int gpc = sh.multt_groups, streams = 1;
+  {
+    const int cap = std::max(1, std::min(b.part_streams, std::max(1, n_tiles)));
+    int64_t best = -1;
+    const int p0 = static_cast<int>(cdiv(b.n_groups, sh.multt_groups));
+    for (int p = p0; p <= b.n_groups && p < p0 + 16; ++p) {
+      const int g = static_cast<int>(cdiv(b.n_groups, p));
+      if (cdiv(b.n_groups, g) != p) continue;  // the same split as fewer passes
+      if (g < std::min(kMaxWindow, b.n_groups)) break;
+      const int s_lo = static_cast<int>(std::min<int64_t>(
+          cap, std::max<int64_t>(std::max(1, num_sms / p), cdiv(n_tiles, kChainTiles))));
+      for (int st = s_lo; st <= cap && st < s_lo + 64; ++st) {
+        const int64_t waves = cdiv(static_cast<int64_t>(p) * st, num_sms);
+        const int64_t cost = waves * g * cdiv(n_tiles, st);
+        if (best < 0 || cost < best) {
+          best = cost;
+          gpc = g;
+          streams = st;
+        }
+      }
+    }
+  }
   // with more than half of the tensor memory per CTA, a second CTA on the SM would only wait for
   // the first one's columns: ask for enough shared memory that it is never placed there
-  const uint32_t cols = tmem_cols_for(sh.multt_groups);
+  const uint32_t cols = tmem_cols_for(gpc);
   const size_t smem = cols > 256 ? std::max<size_t>(multt_smem(sh), 120 * 1024) : multt_smem(sh);
   e = set_smem_cap(block_multt_kernel, smem);
   if (e != cudaSuccess) return e;
-  const int passes = static_cast<int>(cdiv(b.n_groups, sh.multt_groups));
-  const int streams = std::min(b.part_streams, multt_streams(b, num_sms));
-  const int n_tiles = static_cast<int>(b.mpad / kBlockTile);
+  const int passes = static_cast<int>(cdiv(b.n_groups, gpc));
   block_multt_kernel<<<static_cast<unsigned>(passes * streams), (kTeamWarps * sh.teams + 2) * 32,
                        smem, s>>>(
-      b.pc, b.gheader, b.gslots, b.qtiles, b.n_groups, b.n_slots, b.mpad, n_tiles, sh.multt_groups,
-      streams, sh.teams, sh.stages, sh.loads, std::min(sh.window, sh.stages), cols, b.rows, b.part, b.status);
+      b.pc, b.gheader, b.gslots, b.qtiles, b.n_groups, b.n_slots, b.mpad, n_tiles, gpc,
+      streams, sh.teams, sh.stages, sh.loads, std::min(sh.window, sh.stages), cols, b.rows, b.part, b.status,
+      b.f16 ? 1 : 0);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  block_finish_kernel<<<grid_for(npad * kBlockRhs, num_sms), 256, 0, s>>>(
-      b.part, streams, b.rows, b.gp_row, b.n, npad, out64, add, scale_add);
+  block_finish_kernel<<<grid_for(b.rows * kBlockRhs, num_sms), 256, 0, s>>>(
+      b.part, streams, b.rows, b.row_gp, b.n, npad, out64, add, scale_add,
+      b.f16 ? b.scales + kBlockRhs : nullptr, std::ldexp(1.0, b.pexp));
   return cudaGetLastError();
 }
 

@@ -72,14 +72,27 @@ struct BlockPlan {
   double* part = nullptr;     // [streams][16][rows] partial rows of multT
   int part_streams = 0;
   int* status = nullptr;      // device error word (a wait that ran out)
+  // FP16 operands instead of BF16 (the products keep 11 significant bits instead of 8). FP16's
+  // range is narrow, so every operand is scaled by a power of two (exact, undone on output): the
+  // products by 2^pexp (the largest into [2^13, 2^14), so that products down to 2^-27 of it stay
+  // out of FP16's subnormals), the coefficient rows and the Q tiles per column (scales[c] and
+  // scales[16 + c]): the largest coefficient of a column maps into [2^13, 2^14), and a Q tile
+  // written by block_mult takes the coefficient scale times 2^-qshift, which bounds the
+  // accumulators (n_slots x the largest scaled product x 2^14) by 2^14.
+  bool f16 = false;
+  int pexp = 0;
+  int qshift = 0;
+  float* scales = nullptr;    // [32]
+  unsigned* colmax = nullptr; // [16] largest |value| per column (float bits), reset after use
   BlockShape shape;
   cudaStream_t stream = nullptr;
 };
 
 // Build the plan and the BF16 products from a materialised subspace plan (its pmat and cmat);
 // false with a message when the grid has a subspace above kBlockMaxCells cells or allocation fails.
-bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, cudaStream_t s,
-                 int num_sms, std::string* err);
+// f16: FP16 products and operands (else BF16).
+bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, bool f16,
+                 cudaStream_t s, int num_sms, std::string* err);
 void block_free(BlockPlan* b);
 
 // Q = B P for 16 columns: P column-major FP64 [16][npad] (grid order). Writes the BF16 Q tiles

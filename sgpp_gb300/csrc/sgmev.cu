@@ -139,7 +139,9 @@ struct sgmev_op {
   std::string blk_err;
   sgmev::BlockShape blk_shape;  // launch shape ("block_*" knobs or the autotuner)
   double block_inner_tol = 1e-3;  // inner tolerance of block fits ("block_inner_tol")
+  bool block_f16 = false;         // FP16 block products ("block_products": "f16") instead of BF16
   int multt_batch = 1;  // points per read-modify-write round of the FP16 multTranspose ("multt_batch")
+  int multt_banks = 1;  // banks of cell sums per owner in the FP16 multTranspose ("multt_banks")
 
   std::vector<double> bb_left, bb_width;
 
@@ -1113,6 +1115,7 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
     if (subspace_build(&op->sub, op->dim, n, level_pow2, index, op->stream, &why)) {
       op->sub.mod = op->mod;
       op->sub.multt_batch = op->multt_batch;
+      op->sub.multt_banks = op->multt_banks;
       const double dense_cost = 3.0 * op->dim * static_cast<double>(n);
       const double sub_cost = 8.0 * static_cast<double>(op->sub.act_work) + 10.0 * op->sub.n_sub;
       op->sub_ok = op->algo == 1 || sub_cost * 1.5 < dense_cost;
@@ -1193,9 +1196,10 @@ static std::string json_string(const char* json, const char* key) {
   return s.substr(p + 1, e - p - 1);
 }
 
-// Launch-shape knobs (the autotuner's choices): "multt_batch" and the "block_*" shape of the
-// tensor-core block products. They change no result (multt_batch) or only how the block products
-// are cut into launches, so they may also change on a live operator (sgmev_set_params).
+// Launch-shape knobs (the autotuner's choices): "multt_batch", "multt_banks" and the "block_*"
+// shape of the tensor-core block products. They change no result (multt_batch), only the order of
+// the FP16 multTranspose's additions (multt_banks), or only how the block products are cut into
+// launches, so they may also change on a live operator (sgmev_set_params).
 static int apply_shape_params(sgmev_op* op, const char* params_json) {
   using namespace sgmev;
   const std::string mb = json_string(params_json, "multt_batch");
@@ -1204,6 +1208,12 @@ static int apply_shape_params(sgmev_op* op, const char* params_json) {
     if (mb != "1" && mb != "2" && mb != "4")
       return fail(SGMEV_ERR_INVALID, "params: multt_batch must be 1, 2 or 4");
     batch = mb[0] - '0';
+  }
+  const std::string mk = json_string(params_json, "multt_banks");
+  int banks = op->multt_banks;
+  if (!mk.empty()) {
+    if (mk != "1" && mk != "2") return fail(SGMEV_ERR_INVALID, "params: multt_banks must be 1 or 2");
+    banks = mk[0] - '0';
   }
   BlockShape sh = op->blk_shape;
   const char* knobs[] = {"block_mult_tiles", "block_mult_groups", "block_multt_groups",
@@ -1227,6 +1237,8 @@ static int apply_shape_params(sgmev_op* op, const char* params_json) {
   }
   op->multt_batch = batch;
   op->sub.multt_batch = batch;
+  op->multt_banks = banks;
+  op->sub.multt_banks = banks;
   op->blk_shape = sh;
   op->blk.shape = sh;
   return SGMEV_OK;
@@ -1353,6 +1365,15 @@ SGMEV_API int sgmev_create(sgmev_op** out, int dim, int64_t n_grid, const double
         return fail(SGMEV_ERR_INVALID, "params: block_inner_tol must be a number in (0, 1)");
       }
       op->block_inner_tol = v;
+    }
+    const std::string bp = json_string(params_json, "block_products");
+    if (!bp.empty()) {
+      if (bp != "bf16" && bp != "f16") {
+        release(op);
+        delete op;
+        return fail(SGMEV_ERR_INVALID, "params: block_products must be \"bf16\" or \"f16\"");
+      }
+      op->block_f16 = bp == "f16";
     }
     const int rc_shape = apply_shape_params(op, params_json);
     if (rc_shape != SGMEV_OK) {
@@ -1497,7 +1518,7 @@ SGMEV_API int sgmev_set_params(sgmev_op* op, const char* params_json) {
   using namespace sgmev;
   SGMEV_TRY(check_op(op));
   if (!params_json) return SGMEV_OK;
-  static const char* allowed[] = {"multt_batch", "block_mult_tiles", "block_mult_groups",
+  static const char* allowed[] = {"multt_batch", "multt_banks", "block_mult_tiles", "block_mult_groups",
                                   "block_multt_groups", "block_stages", "block_loads",
                                   "block_mult_a", "block_window", "block_teams"};
   // every key must be a launch-shape knob
@@ -2019,7 +2040,8 @@ static int block_ready(sgmev_op* op) {
     return fail(SGMEV_ERR_UNSUPPORTED, "block products: " + op->blk_err);
   }
   std::string err;
-  if (!block_build(&op->blk, op->sub, op->m, op->mpad, op->stream, op->num_sms, &err)) {
+  if (!block_build(&op->blk, op->sub, op->m, op->mpad, op->block_f16, op->stream, op->num_sms,
+                   &err)) {
     op->blk_failed = true;
     op->blk_err = err;
     return fail(SGMEV_ERR_UNSUPPORTED, "block products: " + err);

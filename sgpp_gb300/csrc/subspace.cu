@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_mat_build_kernel(
     const int4* __restrict__ desc, const int4* __restrict__ sinfo, int n_sub, int s_pad,
     const float* __restrict__ xh_t, const float* __restrict__ xl_t, int64_t mpad, int64_t m,
     int64_t n_tiles, float4* __restrict__ phi, float4* __restrict__ plo, uint4* __restrict__ p16,
-    uint32_t* __restrict__ cm) {
+    uint32_t* __restrict__ cm, float p16_scale) {
   using Lay = OwnLayout<DIM, true>;
   extern __shared__ __align__(16) unsigned char smem[];
   float* s_pt = reinterpret_cast<float*>(smem);  // [kOwnTile][W]
@@ -684,7 +684,8 @@ __global__ void __launch_bounds__(kOwnMaxThreads, 1) sub_mat_build_kernel(
         const int64_t k = at + static_cast<int64_t>(g) * s_pad;
         phi[k] = make_float4(hv[0], hv[1], hv[2], hv[3]);
         plo[k] = make_float4(lv[0], lv[1], lv[2], lv[3]);
-        const __half2 h01 = __floats2half2_rn(hv[0], hv[1]), h23 = __floats2half2_rn(hv[2], hv[3]);
+        const __half2 h01 = __floats2half2_rn(hv[0] * p16_scale, hv[1] * p16_scale),
+                      h23 = __floats2half2_rn(hv[2] * p16_scale, hv[3] * p16_scale);
         // FP16 copy by pairs of groups: group gg is half gg % 2 of pair gg / 2
         const int64_t gg = tile * kGroupsPerTile + g;
         reinterpret_cast<uint2*>(p16 + (gg >> 1) * s_pad + sid)[gg & 1] =
@@ -710,7 +711,8 @@ cudaError_t launch_mat_build(const SubPlan& p, cudaStream_t s, const float* xh, 
   kern<<<static_cast<unsigned>(blocks), nth, sm, s>>>(p.desc, p.sinfo, p.n_sub,
                                                       static_cast<int>(p.s_pad), xh, xl, mpad, m,
                                                       nt, p.pmat, p.pmat_lo, p.pmat16,
-                                                      static_cast<uint32_t*>(p.cmat));
+                                                      static_cast<uint32_t*>(p.cmat),
+                                                      std::ldexp(1.0f, p16_exp(p)));
   return cudaGetLastError();
 }
 

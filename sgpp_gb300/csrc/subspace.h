@@ -44,6 +44,7 @@ struct SubPlan {
   int4* act = nullptr;    // [n_sub * dim] active dimensions (t, bits(S), bits(L), stride), padded
   int4* sact = nullptr;   // [n_sub] (base over active dimensions, cells, its offset-free part, count)
   int na_max = 0;         // most active dimensions of a subspace
+
   int64_t act_work = 0;   // active dimensions summed over subspaces
   int cmax = 0;           // largest cell count of a subspace
   double* rows = nullptr;  // [row_cap * total] per-CTA partial sums (owner-computes multT)
@@ -72,7 +73,17 @@ struct SubPlan {
   // points per read-modify-write round of the FP16 multTranspose's cell sums (1, 2 or 4; the
   // same bits for each)
   int multt_batch = 1;
+  // banks of cell sums per owner in the FP16 multTranspose (1, or 2: two independent
+  // read-modify-write chains; other bits than one bank)
+  int multt_banks = 1;
 };
+
+// The FP16 copy of the materialised products holds 2^p16_exp(p) x the products, so that they
+// stay out of FP16's subnormal range (a product of many hats is small: in 10 dimensions typically
+// about 2^-14, where FP16 keeps only a few bits); the FP16 kernels multiply their sums by
+// 2^-p16_exp. Products are at most 1 (hats), or 2^(active dimensions) for the modified basis
+// inside the cube; scaled, the largest stays at or below 2^13.
+inline int p16_exp(const SubPlan& p) { return 13 - (p.mod ? (p.na_max < 15 ? p.na_max : 15) : 0); }
 
 // position count up to which alpha is staged in shared memory (and the fixed-point scatter, two
 // 4-byte accumulators per position, can run); larger grids read alpha from global memory

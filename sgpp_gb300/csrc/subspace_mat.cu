@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include "devmem.h"
 #include "kernels.cuh"
@@ -362,7 +363,7 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
     const float* __restrict__ asub, int64_t m, int64_t tile_begin, int64_t n_tiles,
     const uint4* __restrict__ pp, const typename PairCells<CW>::T* __restrict__ cp,
-    float* __restrict__ out32, double* __restrict__ out64) {
+    float* __restrict__ out32, double* __restrict__ out64, float unscale) {
   using PC = PairCells<CW>;
   using CT = typename PC::T;
   constexpr int A = kPairAheadMult;
@@ -461,7 +462,7 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
       float r = 0.0f;
       for (int w = 0; w < wrote; ++w) r += s_part[w * kOwnTile + jj];
       const int64_t j = gt * kOwnTile + jj;
-      const float v = j < m ? r : 0.0f;
+      const float v = j < m ? r * unscale : 0.0f;  // the FP16 products are scaled by 2^p16_exp
       if (out32) out32[j] = v;
       if (out64) out64[j] = static_cast<double>(v);
     }
@@ -483,7 +484,8 @@ template <typename CW, bool SACC, int BATCH>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
     const float* __restrict__ v, int64_t n_tiles, const uint4* __restrict__ pp,
-    const typename PairCells<CW>::T* __restrict__ cp, double* __restrict__ rows, int streams) {
+    const typename PairCells<CW>::T* __restrict__ cp, double* __restrict__ rows, int streams,
+    double unscale) {
   using PC = PairCells<CW>;
   using CT = typename PC::T;
   constexpr int A = kPairAheadMultT;
@@ -583,7 +585,8 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
               }
             } else {
               double* dst = row + offset + c;
-              *dst = first ? static_cast<double>(a) : *dst + static_cast<double>(a);
+              const double au = static_cast<double>(a) * unscale;
+              *dst = first ? au : *dst + au;
             }
             acc[c * nth] = 0.0f;
           }
@@ -597,9 +600,114 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_kernel(
     } else if (SACC) {
       for (int c = 0; c < info.y; ++c) {
         const float2 t = s_sum[c * nth + tid];
-        row[offset + c] = static_cast<double>(t.x) + static_cast<double>(t.y);
+        row[offset + c] = (static_cast<double>(t.x) + static_cast<double>(t.y)) * unscale;
       }
     }
+  }
+}
+
+// mat_multt_half_kernel with two banks of cell sums per owner ("multt_banks" = 2): the points of a
+// group alternate between the banks (points 0 and 2 of four into bank 0, 1 and 3 into bank 1),
+// so each round reads both banks' cells before it writes either. The two read-modify-write
+// chains are independent (the banks are disjoint), so a round waits for one shared-memory
+// latency where the single bank waits for two; the single-bank kernel's warps spend most of their
+// stalls on exactly that wait. The banks are added into one FP32 sum per cell every kFlushTiles
+// tiles (the FP32 terms carry the FP16 products' 2^-11 rounding, far above what the FP32 sums
+// add) and the row gets that sum once, in FP64. The shared memory is the single bank's with its
+// float-float sums: (2 + 1) x 4 bytes per cell and owner. The order of the additions differs
+// from the single-bank kernel, so the results differ in the last bits; they are fixed from run to
+// run.
+template <typename CW>
+__global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_banked_kernel(
+    const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
+    const float* __restrict__ v, int64_t n_tiles, const uint4* __restrict__ pp,
+    const typename PairCells<CW>::T* __restrict__ cp, double* __restrict__ rows, int streams,
+    double unscale) {
+  using PC = PairCells<CW>;
+  using CT = typename PC::T;
+  constexpr int A = kPairAheadMultT;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x, nth = blockDim.x;
+  float* s_sum = reinterpret_cast<float*>(smem);  // [cmax][blockDim]
+  float* s_b0 = s_sum + cmax * nth;               // bank 0, [cmax][blockDim]
+  float* s_b1 = s_b0 + cmax * nth;                // bank 1
+  const int pass = blockIdx.x / streams, stream = blockIdx.x - pass * streams;
+  const int passes = gridDim.x / streams;
+  double* row = rows + static_cast<int64_t>(stream) * total;
+  const float4* v4 = reinterpret_cast<const float4*>(v);
+  for (int s0 = pass * nth; s0 < n_sub; s0 += nth * passes) {
+    const int sid = s0 + tid;
+    if (sid >= n_sub) continue;  // no barriers below: threads run independently
+    const int4 info = sact[sid];
+    const uint32_t offset = static_cast<uint32_t>(info.x) - static_cast<uint32_t>(info.z);
+    float* b0 = s_b0 + tid;
+    float* b1 = s_b1 + tid;
+    float* sum = s_sum + tid;
+    for (int c = 0; c < info.y; ++c) {
+      b0[c * nth] = 0.0f;
+      b1[c * nth] = 0.0f;
+      sum[c * nth] = 0.0f;
+    }
+    const int64_t k_begin = (stream * n_tiles / streams) * kPairs;
+    const int64_t k_end = ((stream + 1) * n_tiles / streams) * kPairs;
+    if (k_begin < k_end) {
+      const uint4* src = pp + k_begin * s_pad + sid;
+      const CT* csrc = cp + k_begin * s_pad + sid;
+      const float4* vt = v4 + 2 * k_begin;
+      uint4 ring[A];
+      CT cring[A];
+#pragma unroll
+      for (int u = 0; u < A; ++u) {
+        ring[u] = ld_stream(src + static_cast<int64_t>(u) * s_pad);
+        cring[u] = ld_stream(csrc + static_cast<int64_t>(u) * s_pad);
+      }
+      src += static_cast<int64_t>(A) * s_pad;
+      csrc += static_cast<int64_t>(A) * s_pad;
+      int since = 0;
+      for (int64_t k0 = k_begin; k0 < k_end; k0 += A) {
+        const bool fetch = k0 + A < k_end;
+#pragma unroll
+        for (int u = 0; u < A; ++u) {
+          const uint4 pw = ring[u];
+          const CT cs = cring[u];
+          if (fetch) {
+            ring[u] = ld_stream(src);
+            cring[u] = ld_stream(csrc);
+            src += s_pad;
+            csrc += s_pad;
+          }
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float4 p = h ? halves4(pw.z, pw.w) : halves4(pw.x, pw.y);
+            const uint32_t w = PC::word(cs, h);
+            const float4 vv = vt[2 * u + h];
+            {
+              const uint32_t c0 = cell_of<CW>(w, 0) * nth, c1 = cell_of<CW>(w, 1) * nth;
+              const float o0 = b0[c0], o1 = b1[c1];
+              b0[c0] = fmaf(vv.x, p.x, o0);
+              b1[c1] = fmaf(vv.y, p.y, o1);
+            }
+            {
+              const uint32_t c2 = cell_of<CW>(w, 2) * nth, c3 = cell_of<CW>(w, 3) * nth;
+              const float o2 = b0[c2], o3 = b1[c3];
+              b0[c2] = fmaf(vv.z, p.z, o2);
+              b1[c3] = fmaf(vv.w, p.w, o3);
+            }
+          }
+        }
+        vt += 2 * A;
+        since += A;
+        if (since == kFlushTiles * kPairs || !fetch) {
+          for (int c = 0; c < info.y; ++c) {
+            sum[c * nth] += b0[c * nth] + b1[c * nth];
+            b0[c * nth] = 0.0f;
+            b1[c * nth] = 0.0f;
+          }
+          since = 0;
+        }
+      }
+    }
+    for (int c = 0; c < info.y; ++c) row[offset + c] = static_cast<double>(sum[c * nth]) * unscale;
   }
 }
 
@@ -1198,7 +1306,7 @@ template <bool HALF, typename CW>
 cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, int64_t m, float* out32,
                             double* out64, int64_t t0, int64_t nt, int num_sms) {
   const size_t sm = mat_mult_smem(p.cmax, p.s_pad);
-  auto go = [&](auto kern, auto pm, auto cm) -> cudaError_t {
+  auto go = [&](auto kern, auto pm, auto cm, auto... extra) -> cudaError_t {
     cudaError_t e = set_smem_cap(kern, sm);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -1208,12 +1316,13 @@ cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, int64_t m, float* 
         1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
     kern<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
         p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub, m, t0, nt, pm, cm, out32,
-        out64);
+        out64, extra...);
     return cudaGetLastError();
   };
   if constexpr (HALF)
     return go(mat_mult_half_kernel<CW>, static_cast<const uint4*>(p.pmat16),
-              static_cast<const typename PairCells<CW>::T*>(p.cpair));
+              static_cast<const typename PairCells<CW>::T*>(p.cpair),
+              std::ldexp(1.0f, -p16_exp(p)));
   else
     return go(mat_mult_kernel<CW>, static_cast<const float4*>(p.pmat),
               static_cast<const CW*>(p.cmat));
@@ -1225,7 +1334,7 @@ cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, int64_t mpad, con
   const size_t sm = mat_multt_smem(p.cmax, p.s_pad);
   const int nth = mat_threads(p.s_pad);
   const bool sacc = mat_multt_sacc(p.cmax, p.s_pad);
-  auto go = [&](auto kern, auto pm, auto cm) -> cudaError_t {
+  auto go = [&](auto kern, auto pm, auto cm, auto... extra) -> cudaError_t {
     cudaError_t e = set_smem_cap(kern, sm);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -1240,22 +1349,25 @@ cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, int64_t mpad, con
     *rows = streams;
     kern<<<static_cast<unsigned>(streams * passes), nth, sm, s>>>(
         p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), v32, nt,
-        pm, cm, p.rows, static_cast<int>(streams));
+        pm, cm, p.rows, static_cast<int>(streams), extra...);
     return cudaGetLastError();
   };
   if constexpr (HALF) {
     const uint4* pm = p.pmat16;
     const auto* cm = static_cast<const typename PairCells<CW>::T*>(p.cpair);
+    const double un = std::ldexp(1.0, -p16_exp(p));
+    // two banks take the shared memory of the single bank with its float-float sums
+    if (p.multt_banks == 2 && sacc) return go(mat_multt_half_banked_kernel<CW>, pm, cm, un);
     switch (p.multt_batch) {
       case 2:
-        return sacc ? go(mat_multt_half_kernel<CW, true, 2>, pm, cm)
-                    : go(mat_multt_half_kernel<CW, false, 2>, pm, cm);
+        return sacc ? go(mat_multt_half_kernel<CW, true, 2>, pm, cm, un)
+                    : go(mat_multt_half_kernel<CW, false, 2>, pm, cm, un);
       case 4:
-        return sacc ? go(mat_multt_half_kernel<CW, true, 4>, pm, cm)
-                    : go(mat_multt_half_kernel<CW, false, 4>, pm, cm);
+        return sacc ? go(mat_multt_half_kernel<CW, true, 4>, pm, cm, un)
+                    : go(mat_multt_half_kernel<CW, false, 4>, pm, cm, un);
       default:
-        return sacc ? go(mat_multt_half_kernel<CW, true, 1>, pm, cm)
-                    : go(mat_multt_half_kernel<CW, false, 1>, pm, cm);
+        return sacc ? go(mat_multt_half_kernel<CW, true, 1>, pm, cm, un)
+                    : go(mat_multt_half_kernel<CW, false, 1>, pm, cm, un);
     }
   } else {
     const float4* pm = p.pmat;

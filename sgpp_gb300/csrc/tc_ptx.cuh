@@ -34,6 +34,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n, bool a_mn, bool 
          ((b_mn ? 1u : 0u) << 16) | (static_cast<uint32_t>(n >> 3) << 17) |
          (static_cast<uint32_t>(m >> 4) << 24);
 }
+// The same with FP16 A and B (type field 0 for both; A and B always share one type)
+__host__ __device__ constexpr uint32_t idesc_f16(int m, int n, bool a_mn, bool b_mn) {
+  return (1u << 4) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+         (static_cast<uint32_t>(n >> 3) << 17) | (static_cast<uint32_t>(m >> 4) << 24);
+}
 
 // ---- tensor memory ------------------------------------------------------------------------
 // allocation and release are warp-wide (one warp, the same one for both)

@@ -54,13 +54,15 @@ class _FakeOp:
 def test_tune_keeps_the_fastest_and_skips_failures(monkeypatch):
     times = {"1": 0.5e-3, "2": 0.4e-3}
     op = _FakeOp(times)
+    # two banks cost 0.05 ms more here, so the single bank with batch 2 wins
     monkeypatch.setattr(autotune, "_evaluate",
-                        lambda o, kernel, m, n, repeats: times[o.params["multt_batch"]])
+                        lambda o, kernel, m, n, repeats: times[o.params["multt_batch"]]
+                        + (0.05e-3 if o.params.get("multt_banks") == "2" else 0.0))
     g = sg.Grid.createLinearGrid(2)
     g.getGenerator().regular(2)
     log = []
     best, t = autotune.tune(op, g, 100, "multT16", log=log.append)
-    assert best == {"multt_batch": "2"} and t == pytest.approx(0.4e-3)
+    assert best == {"multt_batch": "2", "multt_banks": "1"} and t == pytest.approx(0.4e-3)
     assert op.params == best  # left set on the operator
     assert any("error" in rec for rec in log)
 

@@ -199,3 +199,69 @@ def test_shapes_whose_load_buffers_would_pass_between_teams_are_refused():
     with pytest.raises(sg.OperationException):
         _op(grid, x, block_teams=4, block_loads=6, block_stages=4).multBlock(
             np.zeros((K, grid.getSize())))
+
+
+# ---- FP16 operands ("block_products": "f16") ------------------------------------------------
+# The products keep 11 significant bits (at most 2^-11 relative; FP16 subnormals, below 2^-14,
+# keep an absolute 2^-25) and the vectors about 22 (FP16 high and low parts of the column scaled
+# by a power of two), accumulating in FP32: every entry is held to 2^-10 times the oracle's
+# B |a_k| plus, for the subnormal products, 2^-24 times (subspaces x max |a_k|) for mult and
+# 2^-24 times sum |v_k| for multTranspose.
+
+@pytest.mark.parametrize("d,level,m", SHAPES)
+def test_f16_block_products_within_the_fp16_bound(oracle, d, level, m):
+    rng = np.random.default_rng(700 + d * 10 + level)
+    grid = _grid(d, level)
+    n = grid.getSize()
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    x = rng.random((m, d))
+    alpha = rng.standard_normal((K, n))
+    v = rng.standard_normal((K, m))
+    # columns far outside FP16's range and a zero column: the per-column scales bring them in
+    alpha[1] *= 1e30
+    alpha[2] *= 1e-30
+    alpha[3] = 0.0
+    v[1] *= 1e-25
+    v[2] *= 1e25
+    v[3] = 0.0
+    n_sub = len({tuple(r) for r in np.asarray(lp).tolist()})
+    op = _op(grid, x, block_products="f16")
+    got_m = op.multBlock(alpha)
+    got_t = op.multTransposeBlock(v)
+    for k in range(K):
+        ref = oracle.mult_naive(lp, ix, x, alpha[k])
+        absm = oracle.mult_naive(lp, ix, x, np.abs(alpha[k]))
+        bound = 2.0 ** -10 * absm + 2.0 ** -24 * n_sub * np.abs(alpha[k]).max()
+        assert np.all(np.abs(got_m[k] - ref) <= bound), (k, np.max(np.abs(got_m[k] - ref) / np.maximum(bound, 1e-300)))
+        ref_t = oracle.mult_transpose_naive(lp, ix, x, v[k])
+        abst = oracle.mult_transpose_naive(lp, ix, x, np.abs(v[k]))
+        bound_t = 2.0 ** -10 * abst + 2.0 ** -24 * np.abs(v[k]).sum()
+        assert np.all(np.abs(got_t[k] - ref_t) <= bound_t), (k, np.max(np.abs(got_t[k] - ref_t) / np.maximum(bound_t, 1e-300)))
+    op.close()
+
+
+@pytest.mark.parametrize("d,level,m,lam", [(4, 4, 3000, 1e-3), (6, 3, 2500, 1e-4)])
+def test_f16_block_fit_matches_oracle_cg_per_column(oracle, d, level, m, lam):
+    rng = np.random.default_rng(910 + d)
+    grid = _grid(d, level)
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    x = rng.random((m, d))
+    y = np.empty((K, m))
+    y[0] = 10 * np.sin(np.pi * x[:, 0] * x[:, 1]) + 20 * (x[:, 2] - 0.5) ** 2 + 10 * x[:, 3]
+    y[1:] = rng.standard_normal((K - 1, m))
+    y[2] *= 1e6
+    op = _op(grid, x, block_products="f16")
+    alpha, its, res = op.fitBlock(y, lam, 100000, 1e-10)
+    st = oracle.stream(x)
+    for k in range(K):
+        ref, _, _ = st.cg_fit(lp, ix, y[k], lam, 100000, 1e-12)
+        assert rel_err(alpha[k], ref) < 1e-6, (k, rel_err(alpha[k], ref))
+    st.close()
+    op.close()
+
+
+def test_block_products_knob_is_checked():
+    rng = np.random.default_rng(64)
+    grid = _grid(3, 3)
+    with pytest.raises(sg.OperationException, match="block_products"):
+        _op(grid, rng.random((300, 3)), block_products="fp8")
