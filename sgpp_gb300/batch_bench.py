@@ -36,7 +36,7 @@ def block_pool(probs, lam: float, epsilon: float, workers: int, params=None):
     inner solves, df64 residuals) on its own operator and stream, `workers` problems at a time.
     A problem the block products do not take (a subspace above 128 cells, or products too large
     to materialise) runs its right-hand sides as single mixed fits. Returns
-    (seconds, alphas, paths, inner steps per problem)."""
+    (seconds, alphas, paths, inner steps per problem, seconds per problem, why single)."""
     import queue
     import threading
 
@@ -46,6 +46,8 @@ def block_pool(probs, lam: float, epsilon: float, workers: int, params=None):
     alphas = [None] * len(probs)
     paths = [None] * len(probs)
     steps = [0] * len(probs)
+    secs = [0.0] * len(probs)
+    why = [None] * len(probs)
     errors = []
 
     def run():
@@ -55,6 +57,7 @@ def block_pool(probs, lam: float, epsilon: float, workers: int, params=None):
             except queue.Empty:
                 return
             g, X, Y = probs[k]
+            t_k = time.perf_counter()
             try:
                 cfg = sg.OperationMultipleEvalConfiguration(
                     sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
@@ -63,7 +66,8 @@ def block_pool(probs, lam: float, epsilon: float, workers: int, params=None):
                 try:
                     a, its, _ = op.fitBlock(np.ascontiguousarray(Y.T), lam, 100000, epsilon)
                     alphas[k], paths[k], steps[k] = a.T, "block", int(max(its))
-                except sg.OperationException:
+                except sg.OperationException as e:
+                    why[k] = str(e)
                     cols = []
                     for c in range(Y.shape[1]):
                         a, it, _ = op.fit(np.ascontiguousarray(Y[:, c]), lam, 100000, epsilon,
@@ -72,6 +76,7 @@ def block_pool(probs, lam: float, epsilon: float, workers: int, params=None):
                         steps[k] += it
                     alphas[k], paths[k] = np.stack(cols, axis=1), "single"
                 op.close()
+                secs[k] = time.perf_counter() - t_k
             except BaseException as e:  # reported after the run
                 errors.append(e)
 
@@ -84,7 +89,7 @@ def block_pool(probs, lam: float, epsilon: float, workers: int, params=None):
     sec = time.perf_counter() - t0
     if errors:
         raise errors[0]
-    return sec, alphas, paths, steps
+    return sec, alphas, paths, steps, secs, why
 
 
 def main() -> int:
@@ -177,7 +182,8 @@ def main_block(args) -> int:
         raise SystemExit(f"--engine block takes --rhs {sg.SGMEV_BLOCK_RHS}")
     params = dict(kv.split("=", 1) for kv in args.param)
     block_pool(probs[:2], args.lam, args.epsilon, 1, params)  # warm-up (library, kernels)
-    sec, alphas, paths, steps = block_pool(probs, args.lam, args.epsilon, args.workers, params)
+    sec, alphas, paths, steps, secs, why = block_pool(probs, args.lam, args.epsilon, args.workers,
+                                                      params)
     errs = []
     for k in range(min(args.check, args.problems)):
         g, X, Y = probs[k]
@@ -187,26 +193,16 @@ def main_block(args) -> int:
                                mode=sg.SGMEV_SOLVE_MIXED)
             errs.append(float(np.abs(alphas[k][:, c] - ref).max() / np.abs(ref).max()))
         op.close()
-    seq = []
-    for k in range(min(args.sequential, args.problems)):
-        g, X, Y = probs[k]
-        op = sg.createOperationMultipleEval(g, X)
-        t1 = time.perf_counter()
-        op.fit(np.ascontiguousarray(Y[:, 0]), args.lam, 100000, args.epsilon,
-               mode=sg.SGMEV_SOLVE_MIXED)
-        seq.append(time.perf_counter() - t1)
-        op.close()
-    work = np.array([g.getSize() * X.shape[0] * g.getDimension() for g, X, _ in probs], float)
-    share = work[: len(seq)].sum() / work.sum()
     solves = args.problems * args.rhs
     # the plain per-problem FP64 path: every problem's first right-hand side as a plain
     # FP64-accurate CG fit (the reference's algorithm) on a df64 operator, products built before
     # the clock starts; its right-hand sides are independent fits of the same cost, so all
     # problems x all right-hand sides take rhs x the summed time
     plain = None
+    t_plain_k = [None] * len(probs)
     if args.plain:
         t_plain = 0.0
-        for g, X, Y in probs:
+        for k, (g, X, Y) in enumerate(probs):
             cfg = sg.OperationMultipleEvalConfiguration(
                 sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
                 parameters={"precision": "df64"})
@@ -215,7 +211,8 @@ def main_block(args) -> int:
             op.fit(y0, args.lam, 8, args.epsilon, mode=sg.SGMEV_SOLVE_PLAIN)  # builds the products
             t1 = time.perf_counter()
             op.fit(y0, args.lam, 100000, args.epsilon, mode=sg.SGMEV_SOLVE_PLAIN)
-            t_plain += time.perf_counter() - t1
+            t_plain_k[k] = time.perf_counter() - t1
+            t_plain += t_plain_k[k]
             op.close()
         plain = {"solves_per_sec": solves / (args.rhs * t_plain),
                  "seconds_all_problems_one_rhs": t_plain,
@@ -230,12 +227,15 @@ def main_block(args) -> int:
         "paths": {p: paths.count(p) for p in set(paths)},
         "inner_steps": {"min": int(min(steps)), "max": int(max(steps))},
         "alpha_rel_err_vs_fp64": {"max": max(errs) if errs else None, "checked_solves": len(errs)},
-        "sequential_single_mixed_solves_per_sec_est": (
-            args.problems * share / sum(seq) if seq else None),
         "plain_fp64_path": plain,
         "speedup_vs_plain_fp64": (solves / sec) / plain["solves_per_sec"] if plain else None,
-        "sequential_note": (f"one right-hand side of the first {len(seq)} problems by the "
-                            "single-target mixed fit, rescaled by their share of the N*M*d work"),
+        "why_single": sorted({w for w in why if w}),
+        # per problem: d, level, grid points, data points, path, inner steps, seconds in the pool
+        # (workers overlap), seconds of one plain FP64 fit
+        "problems_detail": [[g.getDimension(), int(round(np.log2(max(g.getStorage().getLevelIndexArraysForEval()[0].max(), 2)))),
+                             g.getSize(), X.shape[0], paths[k], int(steps[k]), round(secs[k], 4),
+                             None if t_plain_k[k] is None else round(t_plain_k[k], 4)]
+                            for k, (g, X, _) in enumerate(probs)],
         "config": {"mix": "d 2..12, level 3..7, M log-uniform [1e3, 2^20], uniform data",
                    "max_work_NMd": args.max_work, "epsilon": args.epsilon, "lambda": args.lam},
     }

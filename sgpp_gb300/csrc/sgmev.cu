@@ -127,6 +127,9 @@ struct sgmev_op {
   // at the HBM copy bandwidth, are faster: 1.44 against 1.50 ms on the benchmark workload)
   bool fused_system = false;
   bool mat_failed = false;  // a build was refused or failed for the current grid
+  // the products were built only to pack the block products (the materialised kernels do not take
+  // this grid) and are gone: the other products run on the on-the-fly kernels
+  bool mat_block_only = false;
   bool inner_half = true;   // inner solves of mixed fits use the FP16 products ("inner_products")
   bool use_half = false;    // set while such an inner solve runs
   int algo = 2;          // FP32 products: 0 dense, 1 subspace, 2 auto (params "algo")
@@ -816,6 +819,7 @@ static int64_t multt_tile_pts(const sgmev_op* op, int prec) {
 // device memory and 64 GiB); a failed build falls back to the on-the-fly kernels for this grid.
 static bool mat_ready(sgmev_op* op) {
   using namespace sgmev;
+  if (op->mat_block_only) return false;
   if (op->sub.pmat) return true;
   if (op->mat_mode == 0 || op->mat_failed || !subspace_mat_fits(op->sub, false)) return false;
   // ModLinear products are built for data in the cube (the cell of a boundary-adjacent function
@@ -837,14 +841,7 @@ static bool mat_ready(sgmev_op* op) {
   if (subspace_materialize(&op->sub, op->stream, op->xt32, op->xt32lo, op->mpad, op->m,
                            op->num_sms) != cudaSuccess) {
     (void)cudaGetLastError();
-    dev_free(op->sub.pmat, op->stream);
-    dev_free(op->sub.pmat_lo, op->stream);
-    dev_free(op->sub.pmat16, op->stream);
-    dev_free(op->sub.cmat, op->stream);
-    dev_free(op->sub.cpair, op->stream);
-    op->sub.pmat = op->sub.pmat_lo = nullptr;
-    op->sub.pmat16 = nullptr;
-    op->sub.cmat = op->sub.cpair = nullptr;
+    subspace_mat_release(&op->sub, op->stream);
     op->mat_failed = true;
     return false;
   }
@@ -1106,6 +1103,7 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
   // and ~10 per subspace, against 3 per dimension for every grid point)
   op->sub_ok = false;
   op->mat_failed = false;
+  op->mat_block_only = false;
   block_free(&op->blk);
   op->blk_ok = false;
   op->blk_failed = false;
@@ -2023,6 +2021,32 @@ SGMEV_API int sgmev_profile_read(sgmev_op* op, int kind, int64_t* launches, doub
 }
 
 // ---- 16 right-hand sides: BF16 tensor-core block products and block fits ------------------
+// The materialised products of a grid the materialised kernels do not take, built only to pack
+// the block products from (same memory rule as mat_ready); false when they cannot be built.
+static bool block_materialize(sgmev_op* op) {
+  using namespace sgmev;
+  if (op->mat_mode == 0 || op->mat_block_only || (op->mod && !op->in_cube)) return false;
+  if (op->sub.n_sub <= 0 || op->sub.cmax <= 0 || op->sub.cmax > kBlockMaxCells) return false;
+  const int64_t bytes = subspace_mat_bytes(op->sub, op->mpad);
+  if (op->mat_mode == 1) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return false;
+    }
+    if (static_cast<double>(bytes) > std::min(0.5 * static_cast<double>(free_b), 64.0 * (1ull << 30)))
+      return false;
+  }
+  if (subspace_materialize(&op->sub, op->stream, op->xt32, op->xt32lo, op->mpad, op->m,
+                           op->num_sms) != cudaSuccess) {
+    (void)cudaGetLastError();
+    subspace_mat_release(&op->sub, op->stream);
+    return false;
+  }
+  op->launches += 1;
+  return true;
+}
+
 // The block products need the subspace plan and its materialised products (grids whose subspaces
 // have at most 128 cells); they are built on the first block call and kept until prepare().
 static int block_ready(sgmev_op* op) {
@@ -2033,15 +2057,24 @@ static int block_ready(sgmev_op* op) {
   SGMEV_CUDA(cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, op->device));
   if (!block_shape_ok(op->blk_shape, cap))
     return fail(SGMEV_ERR_INVALID, "invalid block launch shape (teams must be at most the stages and divide the loads; window at most 3; the stages and coefficient rows must fit shared and tensor memory)");
-  if (!op->sub_ok || !mat_ready(op)) {
+  // The block products are packed from the materialised products. Where the materialised
+  // kernels do not take the grid (their coefficients live in shared memory: grids with many
+  // subspaces of many cells), the products are built only for the packing and freed after it.
+  const bool block_only = op->sub_ok && !mat_ready(op) && block_materialize(op);
+  if (!op->sub_ok || (!block_only && !mat_ready(op))) {
     op->blk_failed = true;
     op->blk_err = "they stream the materialised subspace products (params \"algo\": \"subspace\", "
                   "\"materialize\": not \"off\"), which this operator does not have";
     return fail(SGMEV_ERR_UNSUPPORTED, "block products: " + op->blk_err);
   }
   std::string err;
-  if (!block_build(&op->blk, op->sub, op->m, op->mpad, op->block_f16, op->stream, op->num_sms,
-                   &err)) {
+  const bool built = block_build(&op->blk, op->sub, op->m, op->mpad, op->block_f16, op->stream,
+                                 op->num_sms, &err);
+  if (block_only) {
+    subspace_mat_release(&op->sub, op->stream);
+    op->mat_block_only = true;
+  }
+  if (!built) {
     op->blk_failed = true;
     op->blk_err = err;
     return fail(SGMEV_ERR_UNSUPPORTED, "block products: " + err);

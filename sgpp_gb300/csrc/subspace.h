@@ -138,6 +138,8 @@ cudaError_t subspace_mat_build(const SubPlan& p, cudaStream_t s, const float* xh
 // stream them (same contracts as subspace_mult / subspace_multt / subspace_mult_df /
 // subspace_multt_df).
 int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad);
+// free the materialised products of the plan (stream-ordered on s)
+void subspace_mat_release(SubPlan* p, cudaStream_t s);
 bool subspace_mat_fits(const SubPlan& p, bool df);
 cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, const float* xl,
                                  int64_t mpad, int64_t m, int num_sms);

@@ -1135,6 +1135,17 @@ bool subspace_mat_fits(const SubPlan& p, bool df) {
 // nibble cells when every subspace has at most 16 cells
 bool mat_cell4(const SubPlan& p) { return p.cmax <= 16; }
 
+void subspace_mat_release(SubPlan* p, cudaStream_t s) {
+  dev_free(p->pmat, s);
+  dev_free(p->pmat_lo, s);
+  dev_free(p->pmat16, s);
+  dev_free(p->cmat, s);
+  dev_free(p->cpair, s);
+  p->pmat = p->pmat_lo = nullptr;
+  p->pmat16 = nullptr;
+  p->cmat = p->cpair = nullptr;
+}
+
 int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad) {
   // P_hi, P_lo (4 + 4 bytes), the FP16 copy (2) and the cells: byte cells (1) and their pair copy
   // (1), or during the build the byte cells beside the nibbles (0.5) and their pair copy (0.5)

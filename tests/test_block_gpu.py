@@ -265,3 +265,43 @@ def test_block_products_knob_is_checked():
     grid = _grid(3, 3)
     with pytest.raises(sg.OperationException, match="block_products"):
         _op(grid, rng.random((300, 3)), block_products="fp8")
+
+
+def test_block_products_on_a_grid_the_materialised_kernels_do_not_take(oracle):
+    """d = 6 level 7: 924 subspaces of up to 64 cells, whose coefficients (64 x 928 floats) do not
+    fit the materialised kernels' shared memory. The block products still run: the operator builds
+    the materialised products only to pack them, then frees them, and its other products stay on
+    the on-the-fly kernels. Columns within the BF16 bound against the oracle; a block fit matches
+    the plain FP64-accurate fit of each column."""
+    rng = np.random.default_rng(71)
+    d, level, m = 6, 7, 2000
+    grid = _grid(d, level)
+    n = grid.getSize()
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    x = rng.random((m, d))
+    alpha = rng.standard_normal((K, n))
+    v = rng.standard_normal((K, m))
+    op = _op(grid, x)
+    got_m = op.multBlock(alpha)
+    got_t = op.multTransposeBlock(v)
+    for k in (0, K - 1):
+        ref = oracle.mult_naive(lp, ix, x, alpha[k])
+        bound = 2.0 ** -7 * oracle.mult_naive(lp, ix, x, np.abs(alpha[k])) + 1e-12
+        assert np.all(np.abs(got_m[k] - ref) <= bound)
+        ref_t = oracle.mult_transpose_naive(lp, ix, x, v[k])
+        bound_t = 2.0 ** -7 * oracle.mult_transpose_naive(lp, ix, x, np.abs(v[k])) + 1e-12
+        assert np.all(np.abs(got_t[k] - ref_t) <= bound_t)
+    # the single-vector products still work (on-the-fly kernels) and agree with the oracle
+    out = np.zeros(m)
+    op.mult(alpha[0], out)
+    assert rel_err(out, oracle.mult_naive(lp, ix, x, alpha[0])) < 1e-12
+    y = np.empty((K, m))
+    y[0] = np.sin(3 * x[:, 0]) + x[:, 1]
+    y[1:] = rng.standard_normal((K - 1, m))
+    a_blk, its, _ = op.fitBlock(y, 1e-3, 100000, 1e-10)
+    op.close()
+    ref_op = _op(grid, x, precision="df64")
+    for k in (0, 7, K - 1):
+        a1, _, _ = ref_op.fit(y[k], 1e-3, 100000, 1e-10, mode=sg.SGMEV_SOLVE_PLAIN)
+        assert rel_err(a_blk[k], a1) < 1e-6, (k, rel_err(a_blk[k], a1))
+    ref_op.close()
