@@ -11,11 +11,14 @@ requests that arrive while others run overlaps with theirs in the same launches.
 
     python -m sgpp_gb300.serving --rate 200 --duration 20 --max-work 2e10 [--engine pool|batch]
 
-The pool server (default): a request is admitted when a worker is free (first come, first
-served); the worker creates the operator for the request's grid and data (algo and
-materialisation chosen by the library), runs the device-resident mixed-precision fit and frees
-the operator. Workers overlap on the GPU through their streams; the host waits of one fit (its
-CG scalars) are hidden by the other workers' launches. The library call releases the GIL.
+The pool server (default): a request is admitted in arrival order when a worker is free and its
+device-memory footprint (staged data, grid, CG vectors and the materialised products the library
+would build for it) fits what the fits in flight leave of the memory budget (by default 80 % of
+the device memory free when the run starts; a request larger than the whole budget runs alone);
+the worker creates the operator for the request's grid and data (algo and materialisation chosen
+by the library), runs the device-resident mixed-precision fit and frees the operator. Workers
+overlap on the GPU through their streams; the host waits of one fit (its CG scalars) are hidden
+by the other workers' launches. The library call releases the GIL.
 
 prints one JSON line: completed fits/s, offered load, p50/p99 latency, queue depth.
 Synthetic requests follow the batched-fit size mix (d uniform in 2..12, level in 3..7, data size
@@ -55,6 +58,30 @@ class Request:
     alpha: Optional[np.ndarray] = None
     iterations: int = 0
     residual: float = 0.0
+    footprint: int = 0      # device bytes the pool server reserved for the request
+
+
+_SUBSPACES: Dict[tuple, int] = {}  # subspace count per (grid object, size)
+
+
+def request_footprint(grid: "sg.Grid", m: int) -> int:
+    """Device bytes one request's operator and fit hold, as the pool server budgets them: the data
+    staged dim-major in FP64, FP32 and FP32 low parts (points padded to 1024), the grid arrays,
+    the CG vectors, and the materialised subspace products (P_hi, P_lo, the FP16 copy and the
+    cells, 12 bytes per padded point and padded subspace while they are built, at most 64 GiB, the
+    library's own cap)."""
+    d, n = grid.getDimension(), grid.getSize()
+    mpad = -(-max(m, 1) // 1024) * 1024
+    npad = -(-max(n, 1) // 512) * 512
+    key = (id(grid), n)
+    n_sub = _SUBSPACES.get(key)
+    if n_sub is None:
+        lp, _ = grid.getStorage().getLevelIndexArraysForEval()
+        n_sub = len(np.unique(np.asarray(lp), axis=0)) if n else 0
+        _SUBSPACES[key] = n_sub
+    s_pad = -(-n_sub // 32) * 32
+    products = min(mpad * s_pad * 12, 64 << 30)
+    return int(mpad * d * 16 + npad * d * 32 + 12 * npad * 8 + 4 * mpad * 8 + products)
 
 
 class FitServer:
@@ -114,11 +141,26 @@ class FitServer:
 class PoolServer:
     """Worker threads, each fitting one request at a time with its own operator."""
 
-    def __init__(self, workers: int = 8, params: Optional[dict] = None):
+    def __init__(self, workers: int = 8, params: Optional[dict] = None,
+                 memory_budget: Optional[int] = None):
         self.workers = workers
         self.params = dict(params or {})
+        self.memory_budget = memory_budget  # bytes; None: 80 % of the free device memory
         self.queue_depths: List[int] = []
         self.phase_seconds = {"create": 0.0, "fit": 0.0, "close": 0.0}
+        self.peak_reserved = 0
+        self.budget_used: Optional[int] = None  # the budget of the last run
+
+    def footprint(self, r: Request) -> int:
+        return request_footprint(r.grid, r.X.shape[0])
+
+    def _budget(self) -> int:
+        if self.memory_budget is not None:
+            return int(self.memory_budget)
+        import torch
+
+        free, _ = torch.cuda.mem_get_info()
+        return int(0.8 * free)
 
     def close(self) -> None:
         pass
@@ -154,15 +196,44 @@ class PoolServer:
         done: List[Request] = []
         lock = threading.Lock()
         errors: List[BaseException] = []
+        budget = self._budget()
+        self.budget_used = budget
+        # admission in arrival order: ticket k is admitted once tickets 0 .. k-1 are and its
+        # footprint fits next to the fits in flight (alone if it exceeds the whole budget)
+        mem = threading.Condition()
+        state = {"next": 0, "reserved": 0, "running": 0}
         t0 = clock()
+
+        def admit(r: Request, ticket: int) -> None:
+            with mem:
+                mem.wait_for(lambda: state["next"] == ticket and (
+                    state["running"] == 0 or state["reserved"] + r.footprint <= budget))
+                state["next"] += 1
+                state["reserved"] += r.footprint
+                state["running"] += 1
+                self.peak_reserved = max(self.peak_reserved, state["reserved"])
+                mem.notify_all()
+
+        def release(r: Request) -> None:
+            with mem:
+                state["reserved"] -= r.footprint
+                state["running"] -= 1
+                mem.notify_all()
 
         def worker():
             while True:
-                r = work.get()
-                if r is None:
+                item = work.get()
+                if item is None:
                     return
+                ticket, r = item
                 if clock() - t0 > max_seconds:
-                    continue  # past the deadline: drop the rest of the queue
+                    with mem:  # past the deadline: drop it, in its turn
+                        mem.wait_for(lambda: state["next"] == ticket)
+                        state["next"] += 1
+                        mem.notify_all()
+                    continue
+                r.footprint = self.footprint(r)
+                admit(r, ticket)
                 r.admitted = clock() - t0
                 try:
                     self._fit(r, keep_alpha)
@@ -170,6 +241,8 @@ class PoolServer:
                     with lock:
                         errors.append(e)
                     continue
+                finally:
+                    release(r)
                 r.finished = clock() - t0
                 with lock:
                     done.append(r)
@@ -177,11 +250,11 @@ class PoolServer:
         threads = [threading.Thread(target=worker, daemon=True) for _ in range(self.workers)]
         for t in threads:
             t.start()
-        for r in pending:
+        for k, r in enumerate(pending):
             wait = r.arrival - (clock() - t0)
             if wait > 0:
                 time.sleep(wait)
-            work.put(r)
+            work.put((k, r))
             self.queue_depths.append(work.qsize())
         for _ in threads:
             work.put(None)
@@ -299,6 +372,8 @@ def main() -> int:
     }
     if args.engine == "pool":
         line["worker_seconds"] = server.phase_seconds
+        line["memory"] = {"budget_bytes": server.budget_used,
+                          "peak_reserved_bytes": server.peak_reserved}
     print(json.dumps(line))
     server.close()
     return 0

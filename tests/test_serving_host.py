@@ -86,12 +86,15 @@ def test_fit_server_rejects_a_request_that_does_not_fit_an_empty_engine():
 
 class FakePool(serving.PoolServer):
     def __init__(self, workers, fail_rid=None, delay=0.002):
-        super().__init__(workers=workers)
+        super().__init__(workers=workers, memory_budget=1 << 40)
         self.fail_rid = fail_rid
         self.delay = delay
         self.concurrent = 0
         self.peak = 0
         self._lock = threading.Lock()
+
+    def footprint(self, r):
+        return 0
 
     def _fit(self, r, keep_alpha):
         with self._lock:
@@ -138,3 +141,57 @@ def test_percentile():
     assert serving.percentile(v, 0.0) == 1.0
     assert serving.percentile(v, 0.5) == 3.0
     assert serving.percentile(v, 1.0) == 5.0
+
+
+class BudgetPool(FakePool):
+    """FakePool with a fixed footprint per request and a memory budget."""
+
+    def __init__(self, workers, budget, sizes, delay=0.003):
+        super().__init__(workers=workers, delay=delay)
+        self.memory_budget = budget
+        self.sizes = sizes
+        self.order = []
+        self.live = 0
+        self.peak_live = 0
+
+    def footprint(self, r):
+        return self.sizes[r.rid]
+
+    def _fit(self, r, keep_alpha):
+        with self._lock:
+            self.order.append(r.rid)
+            self.live += r.footprint
+            self.peak_live = max(self.peak_live, self.live)
+        try:
+            super()._fit(r, keep_alpha)
+        finally:
+            with self._lock:
+                self.live -= r.footprint
+
+
+def test_pool_server_admits_by_memory_footprint_in_arrival_order():
+    sizes = [6, 6, 6, 3, 3, 6, 12, 1]  # the 12 exceeds the budget: it runs alone
+    srv = BudgetPool(workers=4, budget=10, sizes=sizes)
+    done = srv.run(_requests(len(sizes)))
+    assert sorted(r.rid for r in done) == list(range(len(sizes)))
+    assert srv.order == list(range(len(sizes)))  # admitted in arrival order
+    # never more than the budget in flight, except the oversized request alone
+    assert srv.peak_live <= 12 and srv.peak_reserved <= 12
+    assert all(r.footprint == sizes[r.rid] for r in done)
+    assert srv.budget_used == 10
+
+
+def test_pool_server_runs_side_by_side_what_fits():
+    srv = BudgetPool(workers=4, budget=100, sizes=[10] * 8, delay=0.02)
+    srv.run(_requests(8))
+    assert srv.peak >= 2  # the budget does not serialise requests that fit together
+
+
+def test_request_footprint_counts_the_materialised_products():
+    grid = sg.Grid.createLinearGrid(3)
+    grid.getGenerator().regular(3)
+    small = serving.request_footprint(grid, 1000)
+    big = serving.request_footprint(grid, 100000)
+    n_sub = 10  # level sums 3..5 in 3 dimensions: 1 + 3 + 6
+    assert big - small >= (100352 - 1024) * 32 * 12  # products: 12 bytes per point and subspace
+    assert small > 1024 * 32 * 12 and n_sub <= 32
