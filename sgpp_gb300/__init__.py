@@ -129,7 +129,8 @@ def _vp(a: Optional[np.ndarray]):
 OP_KNOBS = ("precond", "algo", "inner_tol", "materialize", "materialize_multt", "inner_products",
             "system_product", "block_inner_tol", "block_mult_tiles", "block_mult_groups",
             "block_multt_groups", "block_stages", "block_loads", "block_mult_a", "block_window",
-            "block_teams", "multt_batch", "multt_banks", "block_products")
+            "block_teams", "multt_batch", "multt_banks", "multt_ctas",
+            "block_products")
 
 
 def load_library(path: str = LIBRARY_PATH):

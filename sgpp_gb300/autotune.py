@@ -10,8 +10,9 @@ themselves with CUDA events (sgmev_profile), and the parameters are set on the l
 (sgmev_set_params) instead of rebuilding it, so a search costs a few seconds.
 
 Tunables:
-  multT16   "multt_batch"            points per read-modify-write round of the FP16 multTranspose
-            "multt_banks"            banks of cell sums per owner (2: two independent chains)
+  multT16   "multt_banks"            banks of cell sums per owner of the FP16 multTranspose (2: two
+                                     independent read-modify-write chains)
+            "multt_ctas"             its CTAs per SM (3: FP32 cell sums only, two loads in flight)
   block     "block_window", "block_mult_a", "block_mult_tiles", "block_stages",
             "block_multt_groups"
                                       the tensor-core products with 16 right-hand sides
@@ -49,8 +50,8 @@ class TunableParameter:
 
 
 TUNABLES: Dict[str, List[TunableParameter]] = {
-    "multT16": [TunableParameter("multt_batch", [1, 2, 4]),
-                TunableParameter("multt_banks", [1, 2])],
+    "multT16": [TunableParameter("multt_banks", [1, 2]),
+                TunableParameter("multt_ctas", [2, 3])],
     "block": [TunableParameter("block_window", [1, 2]),
               TunableParameter("block_mult_a", ["tmem", "smem"]),
               TunableParameter("block_mult_tiles", [4, 8]),

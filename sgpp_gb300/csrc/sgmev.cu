@@ -145,6 +145,7 @@ struct sgmev_op {
   bool block_f16 = false;         // FP16 block products ("block_products": "f16") instead of BF16
   int multt_batch = 1;  // points per read-modify-write round of the FP16 multTranspose ("multt_batch")
   int multt_banks = 1;  // banks of cell sums per owner in the FP16 multTranspose ("multt_banks")
+  int multt_ctas = 2;   // CTAs per SM of the FP16 multTranspose ("multt_ctas")
 
   std::vector<double> bb_left, bb_width;
 
@@ -1114,6 +1115,7 @@ static int stage_grid(sgmev_op* op, int64_t n, const double* level_pow2, const d
       op->sub.mod = op->mod;
       op->sub.multt_batch = op->multt_batch;
       op->sub.multt_banks = op->multt_banks;
+      op->sub.multt_ctas = op->multt_ctas;
       const double dense_cost = 3.0 * op->dim * static_cast<double>(n);
       const double sub_cost = 8.0 * static_cast<double>(op->sub.act_work) + 10.0 * op->sub.n_sub;
       op->sub_ok = op->algo == 1 || sub_cost * 1.5 < dense_cost;
@@ -1194,10 +1196,10 @@ static std::string json_string(const char* json, const char* key) {
   return s.substr(p + 1, e - p - 1);
 }
 
-// Launch-shape knobs (the autotuner's choices): "multt_batch", "multt_banks" and the "block_*"
-// shape of the tensor-core block products. They change no result (multt_batch), only the order of
-// the FP16 multTranspose's additions (multt_banks), or only how the block products are cut into
-// launches, so they may also change on a live operator (sgmev_set_params).
+// Launch-shape knobs (the autotuner's choices): "multt_batch", "multt_banks", "multt_ctas" and the
+// "block_*" shape of the tensor-core block products. They change no result (multt_batch), only the
+// order of the FP16 multTranspose's additions (multt_banks, multt_ctas), or only how the block
+// products are cut into launches, so they may also change on a live operator (sgmev_set_params).
 static int apply_shape_params(sgmev_op* op, const char* params_json) {
   using namespace sgmev;
   const std::string mb = json_string(params_json, "multt_batch");
@@ -1206,6 +1208,12 @@ static int apply_shape_params(sgmev_op* op, const char* params_json) {
     if (mb != "1" && mb != "2" && mb != "4")
       return fail(SGMEV_ERR_INVALID, "params: multt_batch must be 1, 2 or 4");
     batch = mb[0] - '0';
+  }
+  const std::string mc = json_string(params_json, "multt_ctas");
+  int ctas = op->multt_ctas;
+  if (!mc.empty()) {
+    if (mc != "2" && mc != "3") return fail(SGMEV_ERR_INVALID, "params: multt_ctas must be 2 or 3");
+    ctas = mc[0] - '0';
   }
   const std::string mk = json_string(params_json, "multt_banks");
   int banks = op->multt_banks;
@@ -1237,6 +1245,8 @@ static int apply_shape_params(sgmev_op* op, const char* params_json) {
   op->sub.multt_batch = batch;
   op->multt_banks = banks;
   op->sub.multt_banks = banks;
+  op->multt_ctas = ctas;
+  op->sub.multt_ctas = ctas;
   op->blk_shape = sh;
   op->blk.shape = sh;
   return SGMEV_OK;
@@ -1516,7 +1526,7 @@ SGMEV_API int sgmev_set_params(sgmev_op* op, const char* params_json) {
   using namespace sgmev;
   SGMEV_TRY(check_op(op));
   if (!params_json) return SGMEV_OK;
-  static const char* allowed[] = {"multt_batch", "multt_banks", "block_mult_tiles", "block_mult_groups",
+  static const char* allowed[] = {"multt_batch", "multt_banks", "multt_ctas", "block_mult_tiles", "block_mult_groups",
                                   "block_multt_groups", "block_stages", "block_loads",
                                   "block_mult_a", "block_window", "block_teams"};
   // every key must be a launch-shape knob

@@ -76,6 +76,9 @@ struct SubPlan {
   // banks of cell sums per owner in the FP16 multTranspose (1, or 2: two independent
   // read-modify-write chains; other bits than one bank)
   int multt_banks = 1;
+  // CTAs per SM of the FP16 multTranspose: 2, or 3 (one bank of FP32 cell sums, no flush sums,
+  // fewer loads in flight per thread; other last bits)
+  int multt_ctas = 2;
 };
 
 // The FP16 copy of the materialised products holds 2^p16_exp(p) x the products, so that they

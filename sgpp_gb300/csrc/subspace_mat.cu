@@ -711,6 +711,81 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_multt_half_banked_kernel(
   }
 }
 
+// mat_multt_half_kernel with three CTAs per SM ("multt_ctas" = 3): one bank of FP32 cell sums per
+// owner (16 cells x 512 owners x 4 bytes = 32 KB of shared memory per CTA), added over all of the
+// stream's points and written to the row once, in FP64; two pairs of groups in flight per thread
+// instead of four, so that the thread fits 42 registers. Half as many warps again as the two-CTA
+// kernels hide the latency of the read-modify-write chains. The FP32 sums add up to a few thousand
+// terms that carry the FP16 products' 2^-11 rounding, far above what the FP32 additions lose.
+template <typename CW>
+__global__ void __launch_bounds__(kMatThreads, 3) mat_multt_half_lean_kernel(
+    const int4* __restrict__ sact, int n_sub, int s_pad, int cmax, int total,
+    const float* __restrict__ v, int64_t n_tiles, const uint4* __restrict__ pp,
+    const typename PairCells<CW>::T* __restrict__ cp, double* __restrict__ rows, int streams,
+    double unscale) {
+  using PC = PairCells<CW>;
+  using CT = typename PC::T;
+  constexpr int A = 2;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x, nth = blockDim.x;
+  float* s_acc = reinterpret_cast<float*>(smem);  // [cmax][blockDim]
+  const int pass = blockIdx.x / streams, stream = blockIdx.x - pass * streams;
+  const int passes = gridDim.x / streams;
+  double* row = rows + static_cast<int64_t>(stream) * total;
+  const float4* v4 = reinterpret_cast<const float4*>(v);
+  for (int s0 = pass * nth; s0 < n_sub; s0 += nth * passes) {
+    const int sid = s0 + tid;
+    if (sid >= n_sub) continue;  // no barriers below: threads run independently
+    const int4 info = sact[sid];
+    const uint32_t offset = static_cast<uint32_t>(info.x) - static_cast<uint32_t>(info.z);
+    float* acc = s_acc + tid;
+    for (int c = 0; c < info.y; ++c) acc[c * nth] = 0.0f;
+    const int64_t k_begin = (stream * n_tiles / streams) * kPairs;
+    const int64_t k_end = ((stream + 1) * n_tiles / streams) * kPairs;
+    if (k_begin < k_end) {
+      const uint4* src = pp + k_begin * s_pad + sid;
+      const CT* csrc = cp + k_begin * s_pad + sid;
+      const float4* vt = v4 + 2 * k_begin;
+      uint4 ring[A];
+      CT cring[A];
+#pragma unroll
+      for (int u = 0; u < A; ++u) {
+        ring[u] = ld_stream(src + static_cast<int64_t>(u) * s_pad);
+        cring[u] = ld_stream(csrc + static_cast<int64_t>(u) * s_pad);
+      }
+      src += static_cast<int64_t>(A) * s_pad;
+      csrc += static_cast<int64_t>(A) * s_pad;
+      for (int64_t k0 = k_begin; k0 < k_end; k0 += A) {
+        const bool fetch = k0 + A < k_end;
+#pragma unroll
+        for (int u = 0; u < A; ++u) {
+          const uint4 pw = ring[u];
+          const CT cs = cring[u];
+          if (fetch) {
+            ring[u] = ld_stream(src);
+            cring[u] = ld_stream(csrc);
+            src += s_pad;
+            csrc += s_pad;
+          }
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float4 p = h ? halves4(pw.z, pw.w) : halves4(pw.x, pw.y);
+            const uint32_t w = PC::word(cs, h);
+            const float4 vv = vt[2 * u + h];
+            acc[cell_of<CW>(w, 0) * nth] += vv.x * p.x;
+            acc[cell_of<CW>(w, 1) * nth] += vv.y * p.y;
+            acc[cell_of<CW>(w, 2) * nth] += vv.z * p.z;
+            acc[cell_of<CW>(w, 3) * nth] += vv.w * p.w;
+          }
+        }
+        vt += 2 * A;
+      }
+    }
+    for (int c = 0; c < info.y; ++c)
+      row[offset + c] = static_cast<double>(acc[c * nth]) * unscale;
+  }
+}
+
 // ---- float-float (FP64-accurate) variants -------------------------------------------------
 __device__ __forceinline__ ff shfl_ff(ff v, int mask) {
   return ff{__shfl_xor_sync(0xffffffffu, v.h, mask), __shfl_xor_sync(0xffffffffu, v.l, mask)};
@@ -1363,11 +1438,31 @@ cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, int64_t mpad, con
         pm, cm, p.rows, static_cast<int>(streams), extra...);
     return cudaGetLastError();
   };
+  // the three-CTA kernel: FP32 cell sums only (4 bytes per cell and owner)
+  auto go_lean = [&](auto kern, auto pm, auto cm, auto... extra) -> cudaError_t {
+    const size_t sml = sizeof(float) * static_cast<size_t>(p.cmax) * nth;
+    cudaError_t e = set_smem_cap(kern, sml);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nth, sml);
+    if (e != cudaSuccess) return e;
+    const int64_t nt = mpad / kOwnTile;
+    const int64_t passes = (p.n_sub + nth - 1) / nth;
+    const int64_t streams = std::max<int64_t>(
+        1, std::min<int64_t>(std::max(1, per_sm) * static_cast<int64_t>(num_sms) / passes,
+                             std::min<int64_t>(p.row_cap, std::max<int64_t>(nt, 1))));
+    *rows = streams;
+    kern<<<static_cast<unsigned>(streams * passes), nth, sml, s>>>(
+        p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, static_cast<int>(p.total), v32, nt,
+        pm, cm, p.rows, static_cast<int>(streams), extra...);
+    return cudaGetLastError();
+  };
   if constexpr (HALF) {
     const uint4* pm = p.pmat16;
     const auto* cm = static_cast<const typename PairCells<CW>::T*>(p.cpair);
     const double un = std::ldexp(1.0, -p16_exp(p));
     // two banks take the shared memory of the single bank with its float-float sums
+    if (p.multt_ctas == 3) return go_lean(mat_multt_half_lean_kernel<CW>, pm, cm, un);
     if (p.multt_banks == 2 && sacc) return go(mat_multt_half_banked_kernel<CW>, pm, cm, un);
     switch (p.multt_batch) {
       case 2:

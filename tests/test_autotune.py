@@ -46,23 +46,23 @@ class _FakeOp:
         self.params = {}
 
     def setParams(self, p):
-        if p.get("multt_batch") == "4":
+        if p.get("multt_banks") == "2" and p.get("multt_ctas") == "3":
             raise sg.OperationException("does not fit")
         self.params = dict(p)
 
 
 def test_tune_keeps_the_fastest_and_skips_failures(monkeypatch):
-    times = {"1": 0.5e-3, "2": 0.4e-3}
+    times = {"2": 0.5e-3, "3": 0.4e-3}
     op = _FakeOp(times)
-    # two banks cost 0.05 ms more here, so the single bank with batch 2 wins
+    # two banks cost 0.05 ms more here, so one bank with three CTAs per SM wins
     monkeypatch.setattr(autotune, "_evaluate",
-                        lambda o, kernel, m, n, repeats: times[o.params["multt_batch"]]
+                        lambda o, kernel, m, n, repeats: times[o.params["multt_ctas"]]
                         + (0.05e-3 if o.params.get("multt_banks") == "2" else 0.0))
     g = sg.Grid.createLinearGrid(2)
     g.getGenerator().regular(2)
     log = []
     best, t = autotune.tune(op, g, 100, "multT16", log=log.append)
-    assert best == {"multt_batch": "2", "multt_banks": "1"} and t == pytest.approx(0.4e-3)
+    assert best == {"multt_banks": "1", "multt_ctas": "3"} and t == pytest.approx(0.4e-3)
     assert op.params == best  # left set on the operator
     assert any("error" in rec for rec in log)
 

@@ -132,12 +132,14 @@ def test_multt_batch_gives_the_same_bits(batch):
     assert out[0][1] == out[1][1]
 
 
+@pytest.mark.parametrize("knob,value", [("multt_banks", "2"), ("multt_ctas", "3")])
 @pytest.mark.parametrize("d,level,m,pin", [(6, 4, 30000, True), (9, 5, 20000, False)])
-def test_multt_banks_reach_the_fp64_solution(oracle, d, level, m, pin):
-    """Two banks of cell sums in the FP16 multTranspose (multt_banks = 2) add the terms in another
-    order: the mixed fit still reaches the FP64 solution (the oracle's, d = 6 level 4; the single
-    bank's to 1e-6, d = 9 level 5 with 715 subspaces of 16 cells and 512 owners per CTA),
-    within two inner iterations of the single bank, with the same bits from run to run."""
+def test_multt_variants_reach_the_fp64_solution(oracle, knob, value, d, level, m, pin):
+    """The FP16 multTranspose's variants add the terms in another order: two banks of cell sums
+    (multt_banks = 2) and three CTAs per SM with FP32 cell sums only (multt_ctas = 3). The mixed
+    fit still reaches the FP64 solution (the oracle's, d = 6 level 4; the default kernel's to 1e-6,
+    d = 9 level 5 with 715 subspaces of 16 cells and 512 owners per CTA), within two inner
+    iterations of the default kernel, with the same bits from run to run."""
     rng = np.random.default_rng(37)
     grid = sg.Grid.createLinearGrid(d)
     grid.getGenerator().regular(level)
@@ -148,17 +150,20 @@ def test_multt_banks_reach_the_fp64_solution(oracle, d, level, m, pin):
         lp, ix = grid.getStorage().getLevelIndexArraysForEval()
         ref, _, _ = oracle.stream(x).cg_fit(lp, ix, y, 1e-4, 20000, 1e-12)
     out = {}
-    for banks in ("1", "2", "2"):
+    for v in (None, value, value):
+        params = {"algo": "subspace", "materialize": "on"}
+        if v is not None:
+            params[knob] = v
         cfg = sg.OperationMultipleEvalConfiguration(
             sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
-            parameters={"algo": "subspace", "materialize": "on", "multt_banks": banks})
+            parameters=params)
         op = sg.createOperationMultipleEval(grid, x, cfg)
         a, it, _ = op.fit(y, 1e-4, 10000, 1e-10, mode=sg.SGMEV_SOLVE_MIXED)
         op.close()
         if ref is not None:
             assert rel_err(a, ref) < 1e-6
-        if banks in out:
-            np.testing.assert_array_equal(a, out[banks][0])
-        out[banks] = (a, it)
-    assert rel_err(out["2"][0], out["1"][0]) < 1e-6
-    assert abs(out["1"][1] - out["2"][1]) <= 2
+        if v in out:
+            np.testing.assert_array_equal(a, out[v][0])
+        out[v] = (a, it)
+    assert rel_err(out[value][0], out[None][0]) < 1e-6
+    assert abs(out[None][1] - out[value][1]) <= 2
