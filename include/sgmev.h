@@ -110,7 +110,9 @@ SGMEV_API int sgmev_device_count(void);
  * cell sums in the FP16 multTranspose (the same bits for each; a launch-shape choice of the
  * autotuner, sgpp_gb300.autotune). "multt_banks": "1" (default) or "2" — banks of cell sums per
  * owner in the FP16 multTranspose (two independent read-modify-write chains; other last bits
- * than one bank; an autotuner choice).
+ * than one bank; an autotuner choice). "multt_ctas": "2" (default) or "3" — CTAs per SM of the
+ * FP16 multTranspose (three: FP32 cell sums only, fewer loads in flight per thread; other last
+ * bits; an autotuner choice).
  * "basis": "linear" (default) or "modlinear" — the basis of the grid. level_pow2/index stay the
  * (2^l, i) arrays of getLevelIndexArraysForEval for both (a ModLinear grid has the same points).
  * ModLinear functions next to a face extrapolate linearly beyond it, as the reference's mask
@@ -240,10 +242,10 @@ SGMEV_API double sgmev_get_duration(sgmev_op* op);
 SGMEV_API int sgmev_set_stream(sgmev_op* op, void* stream);
 
 /* Change launch-shape knobs of a live operator: params_json may hold only "multt_batch",
- * "multt_banks" and the "block_mult_tiles", "block_mult_groups", "block_multt_groups",
+ * "multt_banks", "multt_ctas" and the "block_mult_tiles", "block_mult_groups", "block_multt_groups",
  * "block_stages", "block_loads", "block_window", "block_teams", "block_mult_a" knobs (see
  * sgmev_create); they change no result bits except the order of the FP16 multTranspose's
- * additions (multt_banks) and how the block products are cut into launches.
+ * additions (multt_banks, multt_ctas) and how the block products are cut into launches.
  * No counterpart in the reference (whose OpenCL kernels take such parameters from a
  * configuration file written by StaticParameterTuner,
  * datadriven/src/sgpp/datadriven/application/StaticParameterTuner.cpp:297-417); used by the
