@@ -64,6 +64,11 @@ class Request:
 _SUBSPACES: Dict[tuple, int] = {}  # subspace count per (grid object, size)
 
 
+def _keep(keep_alpha, r: "Request") -> bool:
+    """keep_alpha: True / False for every request, or a predicate of the request."""
+    return bool(keep_alpha(r)) if callable(keep_alpha) else bool(keep_alpha)
+
+
 def request_footprint(grid: "sg.Grid", m: int) -> int:
     """Device bytes one request's operator and fit hold, as the pool server budgets them: the data
     staged dim-major in FP64, FP32 and FP32 low parts (points padded to 1024), the grid arrays,
@@ -131,7 +136,7 @@ class FitServer:
                 if phases[slot] == sg.BatchEngine.PHASE_DONE:
                     r = resident.pop(slot)
                     alpha, r.iterations, r.residual, _ = self.engine.result(slot)
-                    r.alpha = alpha if keep_alpha else None
+                    r.alpha = alpha if _keep(keep_alpha, r) else None
                     r.finished = clock() - t0
                     self.engine.remove(slot)
                     done.append(r)
@@ -183,7 +188,7 @@ class PoolServer:
         self.phase_seconds["create"] += t1 - t0  # (unsynchronised sums: a rough split)
         self.phase_seconds["fit"] += t2 - t1
         self.phase_seconds["close"] += t3 - t2
-        r.alpha = alpha if keep_alpha else None
+        r.alpha = alpha if _keep(keep_alpha, r) else None
 
     def run(self, requests: List[Request], clock: Callable[[], float] = time.perf_counter,
             keep_alpha: bool = True, max_seconds: float = 1e9) -> List[Request]:
@@ -335,6 +340,9 @@ def main() -> int:
     ap.add_argument("--drain-seconds", type=float, default=60.0)
     ap.add_argument("--engine", choices=["pool", "batch"], default="pool")
     ap.add_argument("--workers", type=int, default=8, help="pool server: concurrent fits")
+    ap.add_argument("--check-every", type=int, default=500,
+                    help="keep alpha of every n-th request for the FP64 check")
+    ap.add_argument("--checks", type=int, default=6, help="served requests checked against FP64")
     ap.add_argument("--pinned", action="store_true",
                     help="request data in page-locked host memory (receive buffers)")
     args = ap.parse_args()
@@ -354,14 +362,25 @@ def main() -> int:
         server = FitServer(max_slots=args.max_slots, grid_capacity=1 << 25,
                            data_capacity=1 << 27)
     t0 = time.perf_counter()
-    done = server.run(reqs, keep_alpha=False, max_seconds=args.duration + args.drain_seconds)
+    # alpha is kept for every check_every-th request only (checked against FP64 afterwards)
+    done = server.run(reqs, keep_alpha=lambda r: r.rid % args.check_every == 0,
+                      max_seconds=args.duration + args.drain_seconds)
     wall = time.perf_counter() - t0
+    # the served alphas against FP64 solutions of the same requests (df64-refined fits to 1e-12)
+    errs = []
+    for r in sorted((r for r in done if r.alpha is not None), key=lambda r: r.rid)[:args.checks]:
+        op = sg.createOperationMultipleEval(r.grid, r.X)
+        ref, _, _ = op.fit(np.ascontiguousarray(r.Y[:, 0]), r.lam, 100000, 1e-12,
+                           mode=sg.SGMEV_SOLVE_MIXED)
+        op.close()
+        errs.append(float(np.abs(r.alpha - ref).max() / max(np.abs(ref).max(), 1e-300)))
     lat = [r.finished - r.arrival for r in done]
     line = {
         "metric": "served_fits_per_sec", "value": len(done) / wall, "unit": "fits/s",
         "offered_rate": args.rate, "requests": len(reqs), "completed": len(done),
         "wall_s": wall, "latency_ms": {"p50": 1e3 * percentile(lat, 0.5),
                                         "p99": 1e3 * percentile(lat, 0.99)},
+        "alpha_rel_err_vs_fp64": {"max": max(errs) if errs else None, "checked": len(errs)},
         "queue_depth": {"max": max(server.queue_depths or [0]),
                         "mean": float(np.mean(server.queue_depths or [0]))},
         "config": {"mix": "d in 2..12, level 3..7, M log-uniform [1e3, 2^20], uniform data",
