@@ -32,6 +32,9 @@ plain_fp64_path  whole plain FP64-accurate CG fits (the reference's algorithm) o
         operator, and the mixed fits' speed-up over them
 cpu_baseline  the oracle port of the reference's STREAMING FP64 path on the host cores: one
         B^T(B a) on all points (median of 3), times the operator applications of one CG fit
+batched  one run of the batched configuration (96 problems of the size mix, 16 targets each,
+        as block fits on the tensor cores) against the plain per-problem FP64 path: solves/s of
+        both and their ratio (sgpp_gb300.batch_bench --engine block; --batched-probe 0 skips it)
 
 --impl reference prints the same line for the reference's CPU implementation of the path
 (the oracle port: the compiled reference needs its sources, which do not travel); its steps are
@@ -440,6 +443,29 @@ def plain_fp64_fit(args, grid, x, d_y, stream, mixed_fits_per_sec, local_rank):
             "speedup_mixed_vs_plain_fp64": mixed_fits_per_sec * t}
 
 
+def batched_probe(args):
+    """One run of the batched configuration: 96 problems of the size mix (d uniform in 2..12,
+    level in 3..7, M log-uniform in [1e3, 2^20], N*M*d <= 1e12), 16 targets each, as block fits
+    on the tensor cores with 4 problems in flight, against the plain per-problem FP64 path
+    (sgpp_gb300.batch_bench --engine block); a summary of its line."""
+    import types
+
+    from sgpp_gb300 import batch_bench
+
+    a = types.SimpleNamespace(problems=96, rhs=16, max_work=1e12, epsilon=args.epsilon, lam=1e-4,
+                              check=2, seed=11, workers=4, plain=1, param=[])
+    line = batch_bench.measure_block(a)
+    return {"metric": "batched_solves_per_sec", "value": line["value"], "unit": "solves/s",
+            "seconds": line["seconds"], "problems": a.problems, "rhs": a.rhs,
+            "plain_fp64_solves_per_sec": line["plain_fp64_path"]["solves_per_sec"],
+            "speedup_vs_plain_fp64": line["speedup_vs_plain_fp64"], "paths": line["paths"],
+            "alpha_rel_err_vs_fp64": line["alpha_rel_err_vs_fp64"],
+            "workload": "96 problems, d uniform in 2..12, level in 3..7, M log-uniform in "
+                        "[1e3, 2^20], uniform data, N*M*d <= 1e12, 16 targets each; block fits "
+                        "on the tensor cores, 4 problems in flight; plain FP64 = "
+                        "SGMEV_SOLVE_PLAIN on a df64 operator per problem and target"}
+
+
 def op_config(args):
     """Operator configuration: the CUDA subtype with its default knobs, plus --inner-tol."""
     import sgpp_gb300 as sg
@@ -630,6 +656,10 @@ def run_ours(args):
     plain = plain_fp64_fit(args, grid, x, d_y, stream, value / world, local_rank) \
         if args.plain_fp64_probe else None
 
+    # the batched configuration (96 problems x 16 targets on the tensor cores against the plain
+    # per-problem FP64 path), one run on one GPU, outside the timed region
+    batched = batched_probe(args) if args.batched_probe and world == 1 else None
+
     if rank == 0:
         lat = sorted(step_ms)
         p = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
@@ -655,6 +685,7 @@ def run_ours(args):
             "roofline": roofline, "clocks": clocks, "gpu_launches": int(launches),
             "launch_shape": tuned,
             "e2e": e2e, "cpu_baseline": cpu, "plain_fp64_path": plain,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     op.close()
@@ -795,6 +826,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-fp64-probe", type=int, default=2,
                     help="timed plain FP64-accurate fits on a df64 operator (0: skip)")
+    ap.add_argument("--batched-probe", type=int, default=1,
+                    help="one run of the batched configuration beside the line (0: skip)")
     ap.add_argument("--dense-probe", type=int, default=1,
                     help="timed launches of the dense FP32 and FP64 mult kernels (0: skip)")
     ap.add_argument("--inner-tol", type=float, default=None,

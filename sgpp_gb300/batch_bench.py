@@ -176,6 +176,12 @@ def main() -> int:
 
 
 def main_block(args) -> int:
+    print(json.dumps(measure_block(args)))
+    return 0
+
+
+def measure_block(args) -> dict:
+    """The block engine on the mix (see main): returns the JSON line as a dict."""
     gen = MixGenerator(args.seed, args.max_work, pool=4)
     probs = [gen.draw(args.rhs) for _ in range(args.problems)]
     if args.rhs != sg.SGMEV_BLOCK_RHS:
@@ -239,8 +245,7 @@ def main_block(args) -> int:
         "config": {"mix": "d 2..12, level 3..7, M log-uniform [1e3, 2^20], uniform data",
                    "max_work_NMd": args.max_work, "epsilon": args.epsilon, "lambda": args.lam},
     }
-    print(json.dumps(line))
-    return 0
+    return line
 
 
 if __name__ == "__main__":
