@@ -7,7 +7,7 @@ ctypes bindings for
     ``oracle/ref.mk`` (only where the reference sources exist; absent on hosts without them).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may
-import this package, and only as the checker or the timed CPU baseline. The product
+import this package, and only as the reference results of the tests or the timed CPU baseline. The product
 (``sgpp_gb300``) never imports it.
 """
 from __future__ import annotations
@@ -35,7 +35,8 @@ def _ptr(a: np.ndarray):
 def reference_source() -> str | None:
     """The reference checkout that the build recipe (oracle/ref.mk) and the fixture scripts read:
     $SGPP_REFERENCE_SRC when set, else the build container's checkout; None when the sources are
-    not there (the GPU host has none, and nothing run there needs them)."""
+    not there (a machine without the reference checkout; nothing the GPU tests or the benchmark
+    run needs them)."""
     path = os.environ.get("SGPP_REFERENCE_SRC") or "/root/reference"
     return path if os.path.isdir(os.path.join(path, "base", "src")) else None
 

@@ -4,8 +4,8 @@
  * A plain-C, FP64 restatement of SG++'s multi-evaluation path for the piecewise-linear hat
  * basis on Linear (no-boundary) sparse grids, and for the modified linear basis on ModLinear
  * grids (the same grid points; boundary-adjacent functions extrapolate to the cube faces). Only tests/, __graft_entry__.smoke() and the
- * cpu_baseline leg of bench.py may load this library, and only as the checker (or the timed
- * CPU baseline). The shipped CUDA path never calls into it.
+ * cpu_baseline leg of bench.py may load this library, and only as the reference results of the
+ * tests (or the timed CPU baseline). The shipped CUDA path never calls into it.
  *
  * Parity pin: tests/test_oracle_golden.py checks every function here against fixtures that
  * tests/golden/make_golden.py produced from the reference's own compiled code (oracle/ref.mk
