@@ -1462,7 +1462,9 @@ cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, int64_t mpad, con
     const auto* cm = static_cast<const typename PairCells<CW>::T*>(p.cpair);
     const double un = std::ldexp(1.0, -p16_exp(p));
     // two banks take the shared memory of the single bank with its float-float sums
-    if (p.multt_ctas == 3) return go_lean(mat_multt_half_lean_kernel<CW>, pm, cm, un);
+    // three CTAs per SM while their FP32 cell sums leave room for three (else the kernels above)
+    if (p.multt_ctas == 3 && sizeof(float) * static_cast<size_t>(p.cmax) * nth <= 72 * 1024)
+      return go_lean(mat_multt_half_lean_kernel<CW>, pm, cm, un);
     if (p.multt_banks == 2 && sacc) return go(mat_multt_half_banked_kernel<CW>, pm, cm, un);
     switch (p.multt_batch) {
       case 2:
