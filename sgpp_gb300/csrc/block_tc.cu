@@ -115,12 +115,6 @@ __device__ __forceinline__ bool warp_wait(uint32_t mbar, uint32_t parity) {
 __device__ __forceinline__ bool warp_aborted(const Sync* sy) {
   return __shfl_sync(0xffffffffu, sy->abort, 0) != 0;
 }
-// lane 0's non-blocking test, for the whole warp
-__device__ __forceinline__ bool warp_poll(uint32_t mbar, uint32_t parity) {
-  bool done = false;
-  if ((threadIdx.x & 31) == 0) done = tc::mbar_poll(mbar, parity);
-  return __shfl_sync(0xffffffffu, done, 0);
-}
 
 // BF16 high/low split: v = hi + lo to about 16 significant bits
 __device__ __forceinline__ void split_bf16(float v, uint16_t* hi, uint16_t* lo) {
