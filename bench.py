@@ -696,13 +696,14 @@ def run_ours(args):
 
 def run_block(args):
     """16 regression fits sharing the benchmark's grid and data (targets y and y + N(0, 1) noise)
-    through sgmev_fit_block: BF16 tensor-core inner solves over the 16 columns, df64 outer
+    through sgmev_fit_block: tensor-core inner solves over the 16 columns, df64 outer
     residuals. value = fits/s (16 per step); compared with 16 single-target mixed fits."""
     import torch
 
     import sgpp_gb300 as sg
     from sgpp_gb300 import autotune
 
+    blk = dict(kv.split("=", 1) for kv in args.param).get("block_products", "f16")
     torch.cuda.set_device(0)
     x, y = make_workload(args.seed)
     grid, lp, ix = grid_arrays(args.basis)
@@ -770,9 +771,10 @@ def run_block(args):
         "config": {"workload": f"16 regression fits sharing one grid and data set: "
                                f"{bench_config(args.basis, n, m, args.epsilon, 1)['workload']}; "
                                "targets y and y + N(0, 1)"},
-        "dtype": "bf16 (tensor cores, FP32 accumulation) + df64",
-        "precision": "inner block CG on BF16 tcgen05 products (products rounded to BF16, vectors "
-                     "as BF16 high + low parts, FP32 accumulation in tensor memory), FP64 vectors; "
+        "dtype": f"{blk} (tensor cores, FP32 accumulation) + df64",
+        "precision": f"inner block CG on {blk.upper()} tcgen05 products (products rounded to "
+                     f"{blk.upper()}, vectors as {blk.upper()} high + low parts, FP32 accumulation "
+                     "in tensor memory), FP64 vectors; "
                      "outer residuals with FP64-accurate float-float products per column",
         "inner_cg_steps_per_column": [int(v) for v in its],
         "alpha_rel_err_vs_fp64_column0": err0, "alpha_rel_err_source": note,

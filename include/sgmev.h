@@ -262,16 +262,18 @@ SGMEV_API int64_t sgmev_kernel_launches(const sgmev_op* op);
 /*
  * The same operator applied to 16 vectors at once, on the 5th-generation tensor cores: per tile of
  * 128 data points and group of 128 grid positions, the products of the materialised subspace
- * products (rounded to BF16, 2^-8 relative) with the 16 vectors (split into BF16 high and low
- * parts, about 2^-16) are tcgen05 MMAs accumulating in FP32; with params "block_products": "f16"
- * the products are FP16 (2^-11) and the vectors FP16 high and low parts (about 2^-22), every
- * operand scaled by a power of two into FP16's range. No counterpart in the reference,
+ * products (rounded to FP16, 2^-11 relative) with the 16 vectors (split into FP16 high and low
+ * parts, about 2^-22; every operand scaled by a power of two into FP16's range) are tcgen05 MMAs
+ * accumulating in FP32; with params "block_products": "bf16" the products are rounded to BF16
+ * (2^-8) and the vectors split into BF16 parts (about 2^-16). No counterpart in the reference,
  * which applies OperationMultipleEval::mult / multTranspose (OperationMultipleEval.hpp:55, :81)
- * to one vector at a time; column k here equals those products of vector k to BF16 accuracy.
+ * to one vector at a time; column k here equals those products of vector k to FP16 (or BF16)
+ * accuracy.
  * Needs the subspace algorithm with materialised products (params "algo": "subspace", the default
  * where it pays) and subspaces of at most 128 cells; otherwise SGMEV_ERR_UNSUPPORTED.
  * Vectors are column-major: vector k of length n at offset k * n. Host buffers; blocks.
- * params "block_inner_tol" (default "1e-3"): inner tolerance of sgmev_fit_block; "block_mult_tiles",
+ * params "block_products": "f16" (default) or "bf16"; "block_inner_tol" (default "1e-4" with
+ * FP16 products, "1e-3" with BF16 ones): inner tolerance of sgmev_fit_block; "block_mult_tiles",
  * "block_mult_groups", "block_multt_groups", "block_stages" (default 4), "block_loads" (default
  * 6): launch shape; "block_window" (1-3, default 2): stages whose MMAs one issue round interleaves;
  * "block_teams" (1-4, default 3, at most block_stages and dividing block_loads): producer teams

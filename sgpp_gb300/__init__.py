@@ -661,8 +661,9 @@ class OperationMultiEvalCuda:
         return a
 
     def multBlock(self, alpha):
-        """[16 x n_data] = the mult of each of the 16 rows of alpha [16 x n_grid] (BF16 tensor
-        cores: products rounded to BF16, vectors to about 2^-16, FP32 accumulation)."""
+        """[16 x n_data] = the mult of each of the 16 rows of alpha [16 x n_grid] (tensor cores:
+        products rounded to FP16, vectors to about 2^-22, FP32 accumulation; with params
+        "block_products": "bf16" products rounded to BF16, vectors to about 2^-16)."""
         a = self._block(alpha, self._n, "alpha")
         out = np.zeros((SGMEV_BLOCK_RHS, self._m))
         _check(load_library().sgmev_mult_block(self._h, _vp(a), _vp(out)))

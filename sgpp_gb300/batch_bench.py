@@ -32,7 +32,7 @@ from sgpp_gb300.serving import MixGenerator  # noqa: E402
 
 
 def block_pool(probs, lam: float, epsilon: float, workers: int, params=None):
-    """Every problem's 16 right-hand sides as one block fit (sgmev_fit_block: BF16 tensor-core
+    """Every problem's 16 right-hand sides as one block fit (sgmev_fit_block: tensor-core
     inner solves, df64 residuals) on its own operator and stream, `workers` problems at a time.
     A problem the block products do not take (a subspace above 128 cells, or products too large
     to materialise) runs its right-hand sides as single mixed fits. Returns

@@ -1,11 +1,12 @@
-// Products with 16 right-hand sides on the tensor cores: BF16 tcgen05 MMAs over weighted one-hot
-// tiles of the materialised subspace products (the scheme is described in block_tc.h).
+// Products with 16 right-hand sides on the tensor cores: FP16 or BF16 tcgen05 MMAs over weighted
+// one-hot tiles of the materialised subspace products (the scheme is described in block_tc.h).
 //
-// Both kernels run one CTA per SM: eight producer warps and one MMA warp.
-//   producers  read the packed BF16 products (2 bytes + the cell index per point and subspace,
-//              one 32-bit load) of a tile of 128 points and a group of 16 chunks and write the
-//              tile's rows of E into a shared-memory stage: 16 bytes per point and chunk, one
-//              non-zero BF16 per point and subspace (thread = point and half a group);
+// Both kernels run one CTA per SM: producer teams of four warps (three teams by default), one MMA
+// warp and one loader warp.
+//   producers  read the packed FP16 / BF16 products (2 bytes + the cell index per point and
+//              subspace, one 32-bit word) of a tile of 128 points and a group of 16 chunks and
+//              write the tile's rows of E into a stage (shared or tensor memory): 16 bytes per
+//              point and chunk, one non-zero per point and subspace (thread = point);
 //   MMA warp   one thread waits for a full stage and issues its eight 128 x 32 x 16 MMAs, then
 //              commits them to the stage's "empty" barrier, which frees the stage for the
 //              producers once the tensor cores have read it.
@@ -45,8 +46,8 @@ constexpr int kTeamWarps = 4;
 constexpr int kMaxTeams = 4;
 constexpr int kMaxThreads = (kTeamWarps * kMaxTeams + 2) * 32;
 constexpr uint32_t kStageBytes = 128u * 16u * 16u;  // 128 points x 16 chunks x 16 bytes
-constexpr uint32_t kCoefBytes = 4096u * 2u;         // 128 rows x 32 columns of BF16
-constexpr uint32_t kQBytes = 4096u * 2u;            // 128 points x 32 columns of BF16
+constexpr uint32_t kCoefBytes = 4096u * 2u;         // 128 rows x 32 columns of 16-bit values
+constexpr uint32_t kQBytes = 4096u * 2u;            // 128 points x 32 columns of 16-bit values
 constexpr uint32_t kSlotRow = 128u * 4u;            // one slot's packed words of a tile
 constexpr uint32_t kHeaderAt = 16u * kSlotRow;      // a group has at most 16 slots, then its
 constexpr uint32_t kLoadBytes = kHeaderAt + 128u;   // 128-byte chunk header
@@ -177,7 +178,7 @@ __device__ __forceinline__ void load_stage(unsigned char* buf, uint32_t mbar,
 }
 
 // ---- producer: one stage of E ----------------------------------------------------------------
-// A packed word holds a point's BF16 product in one subspace (low half) and 16 x its cell c in
+// A packed word holds a point's 16-bit product in one subspace (low half) and 16 x its cell c in
 // that subspace (high half). Each group carries a header (BlockHeader): for chunk q, the byte
 // offset of its slot's row in the load buffer and the shift base 128 x (which of the slot's
 // chunks q is), or kUnusedBase for a chunk no slot uses. The chunk holds the point's product at
@@ -320,7 +321,7 @@ struct TeamLoads {
 // buffer (the team's first warp then loads the team's stage `loads` ahead into it), wait for the
 // E stage to be free, write it, mark it full, step both rings past the other teams' stages.
 // TMEM: the stage's rows go to tensor memory (lane = point, 4 columns per chunk: the chunk's 8
-// BF16 elements as 4 pairs) with two 32-column stores per thread instead of shared memory, so the
+// 16-bit elements as 4 pairs) with two 32-column stores per thread instead of shared memory, so the
 // tensor cores read A without the shared-memory traffic of writing and reading it.
 // False when a wait ran out.
 template <bool TMEM>
@@ -442,7 +443,7 @@ __device__ __forceinline__ void block_setup(Sync* sy, unsigned char* st, int sme
 // ---- mult: Q[tile] = sum over groups of E[tile][group] C[group] -------------------------------
 // A CTA owns `tiles` consecutive tiles, whose accumulators (128 x 32 FP32 each) stay in tensor
 // memory, and walks the groups in passes of `gpp` groups whose coefficient rows the loader copies
-// into shared memory once the previous pass's MMAs have completed. Output: the BF16 Q tiles
+// into shared memory once the previous pass's MMAs have completed. Output: the Q tiles
 // (operand layout of block_multt) and optionally Q in FP64.
 // The MMA warp's issue of W consecutive stages: wait for each to be full, then issue their
 // K-steps round-robin (neighbouring stages feed different accumulators), then free each stage.
@@ -694,7 +695,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) block_mult_kernel(
 
 // ---- multT: R[group] = sum over tiles of E[tile][group]^T Q[tile] -----------------------------
 // CTA b takes the groups of pass b / streams (up to `gpc` accumulators of 128 rows x 32 FP32 in
-// tensor memory) and the tiles of stream b % streams; the loader copies each tile's Q (BF16,
+// tensor memory) and the tiles of stream b % streams; the loader copies each tile's Q (16-bit,
 // operand layout) into one of two buffers ahead of its first stage. The accumulators go out as
 // FP64 partial rows of the stream, summed over the streams in order by block_finish_kernel.
 // Operand A (E^T, MN-major) core-matrix offsets: along the points (K, leading) and along the

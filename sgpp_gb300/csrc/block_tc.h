@@ -3,13 +3,14 @@
 // For K = 16 coefficient vectors (or data-side vectors) at once, B P and B^T Q become
 // contractions: per tile of 128 points and per group of 128 "rows" (cells of subspaces), the
 // weighted one-hot matrix E[point][row] = p_s(x) where row = the cell of subspace s that x lies in,
-// 0 elsewhere, is formed in shared memory from the materialised products (BF16) and contracted
-// on the tensor cores (tcgen05.mma kind::f16, BF16 operands, FP32 accumulators in tensor memory):
+// 0 elsewhere, is formed in shared memory from the materialised products (FP16, or BF16) and
+// contracted on the tensor cores (tcgen05.mma kind::f16, FP16 or BF16 operands, FP32 accumulators
+// in tensor memory):
 //   mult:  Q[tile][32] += E[tile][group] * C[group][32]    (C: the coefficient rows)
 //   multT: R[group][32] += E[tile][group]^T * Q[tile][32]
-// The 32 columns are the 16 right-hand sides split into BF16 high and low parts (x = hi + lo,
-// about 16 significant bits), so that only the products are rounded to BF16 (2^-8); the two
-// halves are added in FP32 when the accumulators are read.
+// The 32 columns are the 16 right-hand sides split into high and low parts (x = hi + lo, about 22
+// significant bits in FP16, 16 in BF16), so that only the products are rounded (2^-11 in FP16,
+// 2^-8 in BF16); the two halves are added in FP32 when the accumulators are read.
 //
 // Rows: every subspace with C cells takes max(1, C / 8) chunks of 8 rows; subspaces are packed,
 // largest first, into groups of 16 chunks (a subspace never spans two groups, so C <= 128); a
@@ -27,7 +28,7 @@
 namespace sgmev {
 
 constexpr int kBlockRhs = 16;      // right-hand sides per block product
-constexpr int kBlockCols = 32;     // MMA columns: high and low BF16 parts
+constexpr int kBlockCols = 32;     // MMA columns: high and low parts
 constexpr int kBlockTile = 128;    // points per tile (MMA M for mult, K extent for multT)
 constexpr int kBlockGroupRows = 128;  // rows per group (MMA M for multT)
 constexpr int kBlockMaxCells = 128;   // largest subspace the block products take
@@ -65,10 +66,10 @@ struct BlockPlan {
   int* gp_row = nullptr;      // [n] row of a grid point
   BlockHeader* gheader = nullptr;  // [n_groups] chunk headers
   int2* gslots = nullptr;     // [n_groups] first slot and slot count of each group
-  uint32_t* pc = nullptr;     // [mpad / 128][n_slots][128] BF16 product | 16 cell << 16, tile by
-                              // tile
-  uint16_t* coef = nullptr;   // [n_groups][4096] coefficient rows, BF16, operand layout
-  uint16_t* qtiles = nullptr; // [mpad / 128][4096] Q tiles, BF16, operand layout
+  uint32_t* pc = nullptr;     // [mpad / 128][n_slots][128] FP16 / BF16 product | 16 cell << 16,
+                              // tile by tile
+  uint16_t* coef = nullptr;   // [n_groups][4096] coefficient rows, FP16 / BF16, operand layout
+  uint16_t* qtiles = nullptr; // [mpad / 128][4096] Q tiles, FP16 / BF16, operand layout
   double* part = nullptr;     // [streams][16][rows] partial rows of multT
   int part_streams = 0;
   int* status = nullptr;      // device error word (a wait that ran out)
@@ -88,14 +89,14 @@ struct BlockPlan {
   cudaStream_t stream = nullptr;
 };
 
-// Build the plan and the BF16 products from a materialised subspace plan (its pmat and cmat);
+// Build the plan and the packed products from a materialised subspace plan (its pmat and cmat);
 // false with a message when the grid has a subspace above kBlockMaxCells cells or allocation fails.
 // f16: FP16 products and operands (else BF16).
 bool block_build(BlockPlan* b, const SubPlan& sub, int64_t m, int64_t mpad, bool f16,
                  cudaStream_t s, int num_sms, std::string* err);
 void block_free(BlockPlan* b);
 
-// Q = B P for 16 columns: P column-major FP64 [16][npad] (grid order). Writes the BF16 Q tiles
+// Q = B P for 16 columns: P column-major FP64 [16][npad] (grid order). Writes the Q tiles
 // (input of block_multt) and, when out64 is given, Q column-major FP64 [16][mpad].
 cudaError_t block_mult(BlockPlan& b, cudaStream_t s, const double* p, int64_t npad,
                        double* out64, int num_sms);

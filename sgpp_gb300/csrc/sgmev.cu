@@ -141,8 +141,10 @@ struct sgmev_op {
   bool blk_failed = false;
   std::string blk_err;
   sgmev::BlockShape blk_shape;  // launch shape ("block_*" knobs or the autotuner)
-  double block_inner_tol = 1e-3;  // inner tolerance of block fits ("block_inner_tol")
-  bool block_f16 = false;         // FP16 block products ("block_products": "f16") instead of BF16
+  // inner tolerance of block fits ("block_inner_tol"); 0: the operand type's default (1e-4 for
+  // FP16 products, 1e-3 for BF16 ones, whose 2^-8 rounding limits what a tighter solve gains)
+  double block_inner_tol = 0.0;
+  bool block_f16 = true;          // FP16 block products ("block_products": "f16", default) or BF16
   int multt_batch = 1;  // points per read-modify-write round of the FP16 multTranspose ("multt_batch")
   int multt_banks = 1;  // banks of cell sums per owner in the FP16 multTranspose ("multt_banks")
   int multt_ctas = 2;   // CTAs per SM of the FP16 multTranspose ("multt_ctas")
@@ -2242,7 +2244,9 @@ static int fit_block_common(sgmev_op* op, const double* y, bool y_dev, double la
     for (int k = 0; k < K; ++k) {
       done[k] = done[k] || rho[k] <= epsilon * epsilon * rho0[k] || rho[k] == 0.0;
       all_done = all_done && done[k];
-      const double want = std::min(0.5, std::max(op->block_inner_tol,
+      const double inner_tol =
+          op->block_inner_tol > 0.0 ? op->block_inner_tol : (op->block_f16 ? 1e-4 : 1e-3);
+      const double want = std::min(0.5, std::max(inner_tol,
                                                  epsilon * std::sqrt(rho0[k] / std::max(rho[k], 1e-300)) * 0.5));
       tol2[k] = done[k] ? HUGE_VAL : want * want;
     }

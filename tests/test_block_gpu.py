@@ -1,12 +1,13 @@
 """16 right-hand sides on the tensor cores (sgmev_mult_block, sgmev_mult_transpose_block,
 sgmev_fit_block) through the C ABI.
 
-The block products round the materialised subspace products to BF16 (8 significant bits: at most
-2^-8 relative) and split the 16 vectors into BF16 high and low parts (about 2^-16), accumulating
-in FP32, so column k of B [a_1 .. a_16] may differ from the FP64 product B a_k by at most about
-2^-8 times sum_s |p_s(x_j)| |a_k[c_s(x_j)]|: the tests hold every entry to 2^-7 times that sum,
-which the oracle computes exactly as B |a_k| (hats are non-negative). The block fits refine with FP64-accurate
-residuals, so each column's alpha must match the oracle's FP64 CG solution to 1e-6.
+With params "block_products": "bf16" the block products round the materialised subspace products
+to BF16 (8 significant bits: at most 2^-8 relative) and split the 16 vectors into BF16 high and
+low parts (about 2^-16), accumulating in FP32, so column k of B [a_1 .. a_16] may differ from the
+FP64 product B a_k by at most about 2^-8 times sum_s |p_s(x_j)| |a_k[c_s(x_j)]|: those tests hold
+every entry to 2^-7 times that sum, which the oracle computes exactly as B |a_k| (hats are
+non-negative). The default, FP16 operands, has its own bound (below). The block fits refine with
+FP64-accurate residuals, so each column's alpha must match the oracle's FP64 CG solution to 1e-6.
 """
 import os
 
@@ -55,7 +56,7 @@ def test_block_products_within_the_bf16_bound(oracle, d, level, m):
     x = rng.random((m, d))
     alpha = rng.standard_normal((K, n))
     v = rng.standard_normal((K, m))
-    op = _op(grid, x)
+    op = _op(grid, x, block_products="bf16")
     got_m = op.multBlock(alpha)
     got_t = op.multTransposeBlock(v)
     for k in range(K):
@@ -93,7 +94,7 @@ def test_block_fit_matches_oracle_cg_per_column(oracle, d, level, m, lam):
     y = np.empty((K, m))
     y[0] = 10 * np.sin(np.pi * x[:, 0] * x[:, 1]) + 20 * (x[:, 2] - 0.5) ** 2 + 10 * x[:, 3]
     y[1:] = rng.standard_normal((K - 1, m))
-    op = _op(grid, x)
+    op = _op(grid, x, block_products="bf16")
     alpha, its, res = op.fitBlock(y, lam, 100000, 1e-10)
     st = oracle.stream(x)
     for k in range(K):
@@ -271,8 +272,8 @@ def test_block_products_on_a_grid_the_materialised_kernels_do_not_take(oracle):
     """d = 6 level 7: 924 subspaces of up to 64 cells, whose coefficients (64 x 928 floats) do not
     fit the materialised kernels' shared memory. The block products still run: the operator builds
     the materialised products only to pack them, then frees them, and its other products stay on
-    the on-the-fly kernels. Columns within the BF16 bound against the oracle; a block fit matches
-    the plain FP64-accurate fit of each column."""
+    the on-the-fly kernels. Columns within the BF16 bound against the oracle; a block fit (FP16,
+    the default) matches the plain FP64-accurate fit of each column."""
     rng = np.random.default_rng(71)
     d, level, m = 6, 7, 2000
     grid = _grid(d, level)
@@ -281,7 +282,7 @@ def test_block_products_on_a_grid_the_materialised_kernels_do_not_take(oracle):
     x = rng.random((m, d))
     alpha = rng.standard_normal((K, n))
     v = rng.standard_normal((K, m))
-    op = _op(grid, x)
+    op = _op(grid, x, block_products="bf16")
     got_m = op.multBlock(alpha)
     got_t = op.multTransposeBlock(v)
     for k in (0, K - 1):
@@ -298,6 +299,8 @@ def test_block_products_on_a_grid_the_materialised_kernels_do_not_take(oracle):
     y = np.empty((K, m))
     y[0] = np.sin(3 * x[:, 0]) + x[:, 1]
     y[1:] = rng.standard_normal((K - 1, m))
+    op.close()
+    op = _op(grid, x)
     a_blk, its, _ = op.fitBlock(y, 1e-3, 100000, 1e-10)
     op.close()
     ref_op = _op(grid, x, precision="df64")
