@@ -462,7 +462,7 @@ def batched_probe(args):
             "alpha_rel_err_vs_fp64": line["alpha_rel_err_vs_fp64"],
             "workload": "96 problems, d uniform in 2..12, level in 3..7, M log-uniform in "
                         "[1e3, 2^20], uniform data, N*M*d <= 1e12, 16 targets each; block fits "
-                        "on the tensor cores, 4 problems in flight; plain FP64 = "
+                        "on the tensor cores (FP16 products), 4 problems in flight; plain FP64 = "
                         "SGMEV_SOLVE_PLAIN on a df64 operator per problem and target"}
 
 
