@@ -144,6 +144,9 @@ int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad);
 // free the materialised products of the plan (stream-ordered on s)
 void subspace_mat_release(SubPlan* p, cudaStream_t s);
 bool subspace_mat_fits(const SubPlan& p, bool df);
+// whether the FP16 kernels of mixed fits take the grid (the mult in windows of subspaces where
+// all coefficients do not fit shared memory at once)
+bool subspace_mat_half_fits(const SubPlan& p);
 cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, const float* xl,
                                  int64_t mpad, int64_t m, int num_sms);
 // fused FP32 system product out64 = B^T (B alpha) (+ scale_add * add), one pass over the

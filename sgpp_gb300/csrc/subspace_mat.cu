@@ -358,12 +358,18 @@ static_assert(kPairs % kPairAheadMult == 0 && kPairs % kPairAheadMultT == 0,
 // ring slot. A CTA takes a contiguous range of tiles, and with one pass over the subspaces its
 // ring runs from one tile into the next instead of starting again at each tile (a ring restart
 // waits a full memory latency, about 2.5 us at this load, against ~30 us of work per tile).
+// Windows: the kernel can take a window of the subspaces (sact, pp and cp advanced to its first
+// subspace, n_sub and s_pad its count and padded count) while s_stride stays the product rows'
+// length; with accumulate the window's sums are added to the outputs (the windows run as
+// successive launches, in subspace order), so grids whose coefficients do not fit shared memory
+// at once take several windows.
 template <typename CW>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
     const float* __restrict__ asub, int64_t m, int64_t tile_begin, int64_t n_tiles,
     const uint4* __restrict__ pp, const typename PairCells<CW>::T* __restrict__ cp,
-    float* __restrict__ out32, double* __restrict__ out64, float unscale) {
+    float* __restrict__ out32, double* __restrict__ out64, float unscale, int s_stride,
+    int accumulate) {
   using PC = PairCells<CW>;
   using CT = typename PC::T;
   constexpr int A = kPairAheadMult;
@@ -406,16 +412,16 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
       const bool first = s0 == 0;
       const int off2 = two ? 32 : 0;
       if (!one_pass || tile == t_first) {
-        const int64_t at = gt * kPairs * static_cast<int64_t>(s_pad) + sid;
+        const int64_t at = gt * kPairs * static_cast<int64_t>(s_stride) + sid;
 #pragma unroll
         for (int u = 0; u < A; ++u) {
-          ring[u] = ld_stream(pp + at + static_cast<int64_t>(u) * s_pad);
-          cring[u] = ld_stream(cp + at + static_cast<int64_t>(u) * s_pad);
-          ring2[u] = ld_stream(pp + at + off2 + static_cast<int64_t>(u) * s_pad);
-          cring2[u] = ld_stream(cp + at + off2 + static_cast<int64_t>(u) * s_pad);
+          ring[u] = ld_stream(pp + at + static_cast<int64_t>(u) * s_stride);
+          cring[u] = ld_stream(cp + at + static_cast<int64_t>(u) * s_stride);
+          ring2[u] = ld_stream(pp + at + off2 + static_cast<int64_t>(u) * s_stride);
+          cring2[u] = ld_stream(cp + at + off2 + static_cast<int64_t>(u) * s_stride);
         }
-        nsrc = pp + at + static_cast<int64_t>(A) * s_pad;
-        ncsrc = cp + at + static_cast<int64_t>(A) * s_pad;
+        nsrc = pp + at + static_cast<int64_t>(A) * s_stride;
+        ncsrc = cp + at + static_cast<int64_t>(A) * s_stride;
       }
       // refills run into the next tile when the ring continues there
       const bool more = one_pass && tile + 1 < t_last;
@@ -431,8 +437,8 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
             cring[u] = ld_stream(ncsrc);
             ring2[u] = ld_stream(nsrc + off2);
             cring2[u] = ld_stream(ncsrc + off2);
-            nsrc += s_pad;
-            ncsrc += s_pad;
+            nsrc += s_stride;
+            ncsrc += s_stride;
           }
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
@@ -463,8 +469,8 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_half_kernel(
       for (int w = 0; w < wrote; ++w) r += s_part[w * kOwnTile + jj];
       const int64_t j = gt * kOwnTile + jj;
       const float v = j < m ? r * unscale : 0.0f;  // the FP16 products are scaled by 2^p16_exp
-      if (out32) out32[j] = v;
-      if (out64) out64[j] = static_cast<double>(v);
+      if (out32) out32[j] = accumulate ? out32[j] + v : v;
+      if (out64) out64[j] = accumulate ? out64[j] + static_cast<double>(v) : static_cast<double>(v);
     }
     __syncthreads();  // the partials are read before the next tile overwrites them
   }
@@ -1195,6 +1201,16 @@ size_t mat_multt_df_smem(int cmax, int64_t s_pad) {
 
 constexpr size_t kMatSmemBudget = 200 * 1024;
 
+// subspaces per window of the FP16 mult: all of them when their coefficients fit the shared
+// memory budget, else the largest multiple of kMultBlock that does (0 if none)
+int mat_mult_half_window(int cmax, int64_t s_pad) {
+  if (mat_mult_smem(cmax, s_pad) <= kMatSmemBudget) return static_cast<int>(s_pad);
+  int w = 0;
+  while (w + kMultBlock < s_pad && mat_mult_smem(cmax, w + kMultBlock) <= kMatSmemBudget)
+    w += kMultBlock;
+  return w;
+}
+
 }  // namespace
 
 bool subspace_mat_fits(const SubPlan& p, bool df) {
@@ -1205,6 +1221,14 @@ bool subspace_mat_fits(const SubPlan& p, bool df) {
            mat_multt_df_smem(p.cmax, s_pad) <= kMatSmemBudget;
   return mat_mult_smem(p.cmax, s_pad) <= kMatSmemBudget &&
          mat_multt_smem(p.cmax, s_pad) <= kMatSmemBudget;
+}
+
+// the FP16 kernels of the inner solves: the multTranspose's cell sums fit shared memory, and the
+// mult's coefficients do at least for a window of its subspaces
+bool subspace_mat_half_fits(const SubPlan& p) {
+  const int64_t s_pad = (p.n_sub + 31) / 32 * 32;
+  if (!(p.n_sub > 0 && p.cmax > 0 && p.cmax <= kMatMaxCells && p.rows != nullptr)) return false;
+  return mat_multt_smem(p.cmax, s_pad) <= kMatSmemBudget && mat_mult_half_window(p.cmax, s_pad) > 0;
 }
 
 // nibble cells when every subspace has at most 16 cells
@@ -1405,11 +1429,36 @@ cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, int64_t m, float* 
         out64, extra...);
     return cudaGetLastError();
   };
-  if constexpr (HALF)
-    return go(mat_mult_half_kernel<CW>, static_cast<const uint4*>(p.pmat16),
-              static_cast<const typename PairCells<CW>::T*>(p.cpair),
-              std::ldexp(1.0f, -p16_exp(p)));
-  else
+  if constexpr (HALF) {
+    const auto* cpair = static_cast<const typename PairCells<CW>::T*>(p.cpair);
+    const float un = std::ldexp(1.0f, -p16_exp(p));
+    const int w = mat_mult_half_window(p.cmax, p.s_pad);
+    if (w >= p.s_pad)
+      return go(mat_mult_half_kernel<CW>, static_cast<const uint4*>(p.pmat16), cpair, un,
+                static_cast<int>(p.s_pad), 0);
+    if (w <= 0) return cudaErrorInvalidConfiguration;
+    // windows of w subspaces in subspace order, each adding its sums to the outputs
+    auto kern = mat_mult_half_kernel<CW>;
+    const size_t smw = mat_mult_smem(p.cmax, w);
+    cudaError_t e = set_smem_cap(kern, smw);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMatThreads, smw);
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = std::max<int64_t>(
+        1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
+    for (int sb = 0; sb < p.n_sub; sb += w) {
+      const int cnt = std::min(w, p.n_sub - sb);
+      const int cnt_pad = (cnt + 31) / 32 * 32;  // within the padded rows: sb is a multiple of 64
+      kern<<<static_cast<unsigned>(blocks), kMatThreads, mat_mult_smem(p.cmax, cnt_pad), s>>>(
+          p.sact + sb, cnt, cnt_pad, p.cmax, p.asub, m, t0, nt,
+          static_cast<const uint4*>(p.pmat16) + sb, cpair + sb, out32, out64, un,
+          static_cast<int>(p.s_pad), sb > 0 ? 1 : 0);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  } else
     return go(mat_mult_kernel<CW>, static_cast<const float4*>(p.pmat),
               static_cast<const CW*>(p.cmat));
 }

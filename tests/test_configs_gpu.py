@@ -167,3 +167,36 @@ def test_multt_variants_reach_the_fp64_solution(oracle, knob, value, d, level, m
         out[v] = (a, it)
     assert rel_err(out[value][0], out[None][0]) < 1e-6
     assert abs(out[None][1] - out[value][1]) <= 2
+
+
+def test_mixed_fit_on_a_grid_whose_coefficients_take_mult_windows():
+    """d = 6 level 7: 924 subspaces of up to 64 cells, whose FP32 coefficients (64 x 960) exceed
+    the FP16 mult's shared memory; the mult then walks the subspaces in windows (704 + 220 here),
+    each launch adding its sums to the output. The mixed fit streams the FP16 products through
+    those windows and reaches the plain FP64-accurate fit's solution."""
+    rng = np.random.default_rng(43)
+    d, level, m = 6, 7, 20000
+    grid = sg.Grid.createLinearGrid(d)
+    grid.getGenerator().regular(level)
+    x = rng.random((m, d))
+    y = np.sin(3 * x[:, 0]) + x[:, 1] ** 2 + 0.1 * rng.standard_normal(m)
+    cfg = sg.OperationMultipleEvalConfiguration(
+        sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
+        parameters={"algo": "subspace", "materialize": "on"})
+    op = sg.createOperationMultipleEval(grid, x, cfg)
+    op.profile(True)
+    a, it, _ = op.fit(y, 1e-3, 20000, 1e-10, mode=sg.SGMEV_SOLVE_MIXED)
+    launches, _ = op.profileRead(sg.SGMEV_KERNEL_MULT_MAT16)
+    op.profile(False)
+    again, it2, _ = op.fit(y, 1e-3, 20000, 1e-10, mode=sg.SGMEV_SOLVE_MIXED)
+    op.close()
+    assert launches > 0  # the inner solves ran the FP16 materialised mult
+    np.testing.assert_array_equal(a, again)
+    assert it == it2
+    cfg64 = sg.OperationMultipleEvalConfiguration(
+        sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
+        parameters={"precision": "df64"})
+    ref_op = sg.createOperationMultipleEval(grid, x, cfg64)
+    ref, _, _ = ref_op.fit(y, 1e-3, 20000, 1e-10, mode=sg.SGMEV_SOLVE_PLAIN)
+    ref_op.close()
+    assert rel_err(a, ref) < 1e-6, rel_err(a, ref)
