@@ -237,7 +237,12 @@ class PoolServer:
                         state["next"] += 1
                         mem.notify_all()
                     continue
-                r.footprint = self.footprint(r)
+                try:
+                    r.footprint = self.footprint(r)
+                except BaseException as e:  # reported after the run; the ticket still passes
+                    with lock:
+                        errors.append(e)
+                    r.footprint = 0
                 admit(r, ticket)
                 r.admitted = clock() - t0
                 try:

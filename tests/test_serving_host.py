@@ -195,3 +195,16 @@ def test_request_footprint_counts_the_materialised_products():
     n_sub = 10  # level sums 3..5 in 3 dimensions: 1 + 3 + 6
     assert big - small >= (100352 - 1024) * 32 * 12  # products: 12 bytes per point and subspace
     assert small > 1024 * 32 * 12 and n_sub <= 32
+
+
+def test_pool_server_keeps_admitting_after_a_footprint_error():
+    class BadFootprint(BudgetPool):
+        def footprint(self, r):
+            if r.rid == 2:
+                raise ValueError("no footprint for request 2")
+            return super().footprint(r)
+
+    srv = BadFootprint(workers=3, budget=10, sizes=[4] * 6)
+    with pytest.raises(ValueError, match="request 2"):
+        srv.run(_requests(6))
+    assert sorted(srv.order) == list(range(6))  # every request still ran, in order
