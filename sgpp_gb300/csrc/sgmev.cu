@@ -824,11 +824,7 @@ static bool mat_ready(sgmev_op* op) {
   using namespace sgmev;
   if (op->mat_block_only) return false;
   if (op->sub.pmat) return true;
-  if (op->mat_mode == 0 || op->mat_failed) return false;
-  // the FP32 kernels need every coefficient in shared memory; the FP16 ones of the inner solves
-  // can take the mult in windows of subspaces
-  if (!subspace_mat_fits(op->sub, false) && !(op->inner_half && subspace_mat_half_fits(op->sub)))
-    return false;
+  if (op->mat_mode == 0 || op->mat_failed || !subspace_mat_fits(op->sub, false)) return false;
   // ModLinear products are built for data in the cube (the cell of a boundary-adjacent function
   // is clamped there); data outside it stays on the dense kernels, which extrapolate
   if (op->mod && !op->in_cube) return false;
@@ -886,7 +882,7 @@ static int dev_mult(sgmev_op* op, int prec, const double* a64, const float* a32,
     SGMEV_TRY(run_mult_df(op, a32, a32lo, j_begin, j_end, &p));
     if (out64) SGMEV_TRY((run_reduce<float2, double>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out64, nullptr, 0.0)));
     if (out32) SGMEV_TRY((run_reduce<float2, float>(op, (int)p.nsplit, op->mpad, j_begin, valid, total, out32, nullptr, 0.0)));
-  } else if (op->sub_ok && mat_ready(op) && (op->use_half || subspace_mat_fits(op->sub, false))) {
+  } else if (op->sub_ok && mat_ready(op)) {
     const long ev = prof_begin(op, op->use_half ? KIND_MULT_MAT16 : KIND_MULT_MAT32);
     SGMEV_CUDA(subspace_mult_mat(op->sub, op->stream, op->xt32, op->mpad, op->m, a32, out32, out64,
                                  j_begin, j_end, op->num_sms, op->use_half));

@@ -143,10 +143,10 @@ cudaError_t subspace_mat_build(const SubPlan& p, cudaStream_t s, const float* xh
 int64_t subspace_mat_bytes(const SubPlan& p, int64_t mpad);
 // free the materialised products of the plan (stream-ordered on s)
 void subspace_mat_release(SubPlan* p, cudaStream_t s);
+// whether the materialised kernels take the grid (FP32 / FP16 ones, or with df the float-float
+// ones); the FP32 / FP16 mult takes its subspaces in windows where all coefficients do not fit
+// shared memory at once
 bool subspace_mat_fits(const SubPlan& p, bool df);
-// whether the FP16 kernels of mixed fits take the grid (the mult in windows of subspaces where
-// all coefficients do not fit shared memory at once)
-bool subspace_mat_half_fits(const SubPlan& p);
 cudaError_t subspace_materialize(SubPlan* p, cudaStream_t s, const float* xh, const float* xl,
                                  int64_t mpad, int64_t m, int num_sms);
 // fused FP32 system product out64 = B^T (B alpha) (+ scale_add * add), one pass over the

@@ -131,12 +131,13 @@ __host__ __device__ constexpr int mult_at_pad(int s_pad) {
   return (s_pad + kMultBlock - 1) / kMultBlock * kMultBlock;
 }
 
+// s_stride / accumulate: windows of the subspaces, as in mat_mult_half_kernel below.
 template <typename CW>
 __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
     const int4* __restrict__ sact, int n_sub, int s_pad, int cmax,
     const float* __restrict__ asub, int64_t m, int64_t tile_begin, int64_t n_tiles,
     const float4* __restrict__ pm, const CW* __restrict__ cm, float* __restrict__ out32,
-    double* __restrict__ out64) {
+    double* __restrict__ out64, int s_stride, int accumulate) {
   using PT = float4;
   constexpr int A = kAhead2;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -179,16 +180,16 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
       float* part = s_part + warp * kOwnTile;
       const bool first = s0 == 0;
       if (!one_pass || tile == t_first) {
-        const int64_t at = gt * kGroups * static_cast<int64_t>(s_pad) + sid;
+        const int64_t at = gt * kGroups * static_cast<int64_t>(s_stride) + sid;
 #pragma unroll
         for (int u = 0; u < A; ++u) {
-          ring[u] = ld_stream(pm + at + static_cast<int64_t>(u) * s_pad);
-          cring[u] = ld_stream(cm + at + static_cast<int64_t>(u) * s_pad);
-          ring2[u] = ld_stream(pm + at + off2 + static_cast<int64_t>(u) * s_pad);
-          cring2[u] = ld_stream(cm + at + off2 + static_cast<int64_t>(u) * s_pad);
+          ring[u] = ld_stream(pm + at + static_cast<int64_t>(u) * s_stride);
+          cring[u] = ld_stream(cm + at + static_cast<int64_t>(u) * s_stride);
+          ring2[u] = ld_stream(pm + at + off2 + static_cast<int64_t>(u) * s_stride);
+          cring2[u] = ld_stream(cm + at + off2 + static_cast<int64_t>(u) * s_stride);
         }
-        nsrc = pm + at + static_cast<int64_t>(A) * s_pad;
-        ncsrc = cm + at + static_cast<int64_t>(A) * s_pad;
+        nsrc = pm + at + static_cast<int64_t>(A) * s_stride;
+        ncsrc = cm + at + static_cast<int64_t>(A) * s_stride;
       }
       // refills run into the next tile when the ring continues there
       const bool more = one_pass && tile + 1 < t_last;
@@ -205,8 +206,8 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
             cring[u] = ld_stream(ncsrc);
             ring2[u] = ld_stream(nsrc + off2);
             cring2[u] = ld_stream(ncsrc + off2);
-            nsrc += s_pad;
-            ncsrc += s_pad;
+            nsrc += s_stride;
+            ncsrc += s_stride;
           }
           // cells are below cmax by construction (the build writes c < cells of s <= cmax)
           float v0 = a_col[cell_of<CW>(cs, 0) * sp] * p.x;
@@ -233,8 +234,8 @@ __global__ void __launch_bounds__(kMatThreads, 2) mat_mult_kernel(
       for (int w = 0; w < wrote; ++w) r += s_part[w * kOwnTile + jj];
       const int64_t j = gt * kOwnTile + jj;
       const float v = j < m ? r : 0.0f;
-      if (out32) out32[j] = v;
-      if (out64) out64[j] = static_cast<double>(v);
+      if (out32) out32[j] = accumulate ? out32[j] + v : v;
+      if (out64) out64[j] = accumulate ? out64[j] + static_cast<double>(v) : static_cast<double>(v);
     }
     __syncthreads();  // the partials are read before the next tile overwrites them
   }
@@ -1201,9 +1202,9 @@ size_t mat_multt_df_smem(int cmax, int64_t s_pad) {
 
 constexpr size_t kMatSmemBudget = 200 * 1024;
 
-// subspaces per window of the FP16 mult: all of them when their coefficients fit the shared
-// memory budget, else the largest multiple of kMultBlock that does (0 if none)
-int mat_mult_half_window(int cmax, int64_t s_pad) {
+// subspaces per window of the materialised mult: all of them when their coefficients fit the
+// shared memory budget, else the largest multiple of kMultBlock that does (0 if none)
+int mat_mult_window(int cmax, int64_t s_pad) {
   if (mat_mult_smem(cmax, s_pad) <= kMatSmemBudget) return static_cast<int>(s_pad);
   int w = 0;
   while (w + kMultBlock < s_pad && mat_mult_smem(cmax, w + kMultBlock) <= kMatSmemBudget)
@@ -1219,16 +1220,8 @@ bool subspace_mat_fits(const SubPlan& p, bool df) {
   if (df)
     return mat_mult_df_smem(p.cmax, s_pad) <= kMatSmemBudget &&
            mat_multt_df_smem(p.cmax, s_pad) <= kMatSmemBudget;
-  return mat_mult_smem(p.cmax, s_pad) <= kMatSmemBudget &&
-         mat_multt_smem(p.cmax, s_pad) <= kMatSmemBudget;
-}
-
-// the FP16 kernels of the inner solves: the multTranspose's cell sums fit shared memory, and the
-// mult's coefficients do at least for a window of its subspaces
-bool subspace_mat_half_fits(const SubPlan& p) {
-  const int64_t s_pad = (p.n_sub + 31) / 32 * 32;
-  if (!(p.n_sub > 0 && p.cmax > 0 && p.cmax <= kMatMaxCells && p.rows != nullptr)) return false;
-  return mat_multt_smem(p.cmax, s_pad) <= kMatSmemBudget && mat_mult_half_window(p.cmax, s_pad) > 0;
+  // the mult takes its subspaces in windows where all coefficients do not fit at once
+  return mat_mult_window(p.cmax, s_pad) > 0 && mat_multt_smem(p.cmax, s_pad) <= kMatSmemBudget;
 }
 
 // nibble cells when every subspace has at most 16 cells
@@ -1415,31 +1408,12 @@ cudaError_t launch_multt_df(const SubPlan& p, cudaStream_t s, int64_t mpad, cons
 template <bool HALF, typename CW>
 cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, int64_t m, float* out32,
                             double* out64, int64_t t0, int64_t nt, int num_sms) {
-  const size_t sm = mat_mult_smem(p.cmax, p.s_pad);
-  auto go = [&](auto kern, auto pm, auto cm, auto... extra) -> cudaError_t {
-    cudaError_t e = set_smem_cap(kern, sm);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMatThreads, sm);
-    if (e != cudaSuccess) return e;
-    const int64_t blocks = std::max<int64_t>(
-        1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
-    kern<<<static_cast<unsigned>(blocks), kMatThreads, sm, s>>>(
-        p.sact, p.n_sub, static_cast<int>(p.s_pad), p.cmax, p.asub, m, t0, nt, pm, cm, out32,
-        out64, extra...);
-    return cudaGetLastError();
-  };
-  if constexpr (HALF) {
-    const auto* cpair = static_cast<const typename PairCells<CW>::T*>(p.cpair);
-    const float un = std::ldexp(1.0f, -p16_exp(p));
-    const int w = mat_mult_half_window(p.cmax, p.s_pad);
-    if (w >= p.s_pad)
-      return go(mat_mult_half_kernel<CW>, static_cast<const uint4*>(p.pmat16), cpair, un,
-                static_cast<int>(p.s_pad), 0);
-    if (w <= 0) return cudaErrorInvalidConfiguration;
-    // windows of w subspaces in subspace order, each adding its sums to the outputs
-    auto kern = mat_mult_half_kernel<CW>;
-    const size_t smw = mat_mult_smem(p.cmax, w);
+  // all subspaces in one launch when their coefficients fit shared memory, else windows of w
+  // subspaces in subspace order, each launch adding its sums to the outputs
+  const int w = mat_mult_window(p.cmax, p.s_pad);
+  if (w <= 0) return cudaErrorInvalidConfiguration;
+  auto run = [&](auto kern, auto pm, auto cm, auto... extra) -> cudaError_t {
+    const size_t smw = mat_mult_smem(p.cmax, std::min<int64_t>(w, p.s_pad));
     cudaError_t e = set_smem_cap(kern, smw);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -1449,20 +1423,24 @@ cudaError_t launch_mat_mult(const SubPlan& p, cudaStream_t s, int64_t m, float* 
         1, std::min<int64_t>(nt, static_cast<int64_t>(std::max(1, per_sm)) * num_sms));
     for (int sb = 0; sb < p.n_sub; sb += w) {
       const int cnt = std::min(w, p.n_sub - sb);
-      const int cnt_pad = (cnt + 31) / 32 * 32;  // within the padded rows: sb is a multiple of 64
+      // the window's padded count stays within the padded rows: sb is a multiple of 64
+      const int cnt_pad = w >= p.s_pad ? static_cast<int>(p.s_pad) : (cnt + 31) / 32 * 32;
       kern<<<static_cast<unsigned>(blocks), kMatThreads, mat_mult_smem(p.cmax, cnt_pad), s>>>(
-          p.sact + sb, cnt, cnt_pad, p.cmax, p.asub, m, t0, nt,
-          static_cast<const uint4*>(p.pmat16) + sb, cpair + sb, out32, out64, un,
-          static_cast<int>(p.s_pad), sb > 0 ? 1 : 0);
+          p.sact + sb, cnt, cnt_pad, p.cmax, p.asub, m, t0, nt, pm + sb, cm + sb, out32, out64,
+          extra..., static_cast<int>(p.s_pad), sb > 0 ? 1 : 0);
       e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
-  } else
-    return go(mat_mult_kernel<CW>, static_cast<const float4*>(p.pmat),
-              static_cast<const CW*>(p.cmat));
+  };
+  if constexpr (HALF)
+    return run(mat_mult_half_kernel<CW>, static_cast<const uint4*>(p.pmat16),
+               static_cast<const typename PairCells<CW>::T*>(p.cpair),
+               std::ldexp(1.0f, -p16_exp(p)));
+  else
+    return run(mat_mult_kernel<CW>, static_cast<const float4*>(p.pmat),
+               static_cast<const CW*>(p.cmat));
 }
-
 template <bool HALF, typename CW>
 cudaError_t launch_mat_multt(const SubPlan& p, cudaStream_t s, int64_t mpad, const float* v32,
                              int num_sms, int64_t* rows) {

@@ -200,3 +200,29 @@ def test_mixed_fit_on_a_grid_whose_coefficients_take_mult_windows():
     ref, _, _ = ref_op.fit(y, 1e-3, 20000, 1e-10, mode=sg.SGMEV_SOLVE_PLAIN)
     ref_op.close()
     assert rel_err(a, ref) < 1e-6, rel_err(a, ref)
+
+
+def test_fp32_products_on_a_grid_whose_coefficients_take_mult_windows(oracle):
+    """The FP32 materialised mult takes the same windows: on the d = 6 level 7 grid its products
+    match the oracle to the FP32 tolerance of the other parity tests, and they ran on the
+    materialised kernels."""
+    rng = np.random.default_rng(44)
+    d, level, m = 6, 7, 5000
+    grid = sg.Grid.createLinearGrid(d)
+    grid.getGenerator().regular(level)
+    n = grid.getSize()
+    lp, ix = grid.getStorage().getLevelIndexArraysForEval()
+    x = rng.random((m, d))
+    alpha = rng.standard_normal(n)
+    cfg = sg.OperationMultipleEvalConfiguration(
+        sg.OperationMultipleEvalType.STREAMING, sg.OperationMultipleEvalSubType.CUDA,
+        parameters={"precision": "float", "algo": "subspace", "materialize": "on"})
+    op = sg.createOperationMultipleEval(grid, x, cfg)
+    op.profile(True)
+    out = np.zeros(m)
+    op.mult(alpha, out)
+    launches, _ = op.profileRead(sg.SGMEV_KERNEL_MULT_MAT32)
+    op.profile(False)
+    op.close()
+    assert launches > 0
+    assert rel_err(out, oracle.mult_naive(lp, ix, x, alpha)) < 1e-4
