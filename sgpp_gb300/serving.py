@@ -32,6 +32,7 @@ import json
 import os
 import sys
 import time
+import weakref
 from typing import Callable, Dict, List, Optional
 
 import numpy as np
@@ -61,7 +62,8 @@ class Request:
     footprint: int = 0      # device bytes the pool server reserved for the request
 
 
-_SUBSPACES: Dict[tuple, int] = {}  # subspace count per (grid object, size)
+# subspace count per live grid object (with the size it was counted at: grids can grow)
+_SUBSPACES: "weakref.WeakKeyDictionary" = weakref.WeakKeyDictionary()
 
 
 def _keep(keep_alpha, r: "Request") -> bool:
@@ -78,12 +80,19 @@ def request_footprint(grid: "sg.Grid", m: int) -> int:
     d, n = grid.getDimension(), grid.getSize()
     mpad = -(-max(m, 1) // 1024) * 1024
     npad = -(-max(n, 1) // 512) * 512
-    key = (id(grid), n)
-    n_sub = _SUBSPACES.get(key)
-    if n_sub is None:
+    try:
+        cached = _SUBSPACES.get(grid)
+    except TypeError:  # an object without weak references: count every time
+        cached = None
+    if cached is not None and cached[0] == n:
+        n_sub = cached[1]
+    else:
         lp, _ = grid.getStorage().getLevelIndexArraysForEval()
         n_sub = len(np.unique(np.asarray(lp), axis=0)) if n else 0
-        _SUBSPACES[key] = n_sub
+        try:
+            _SUBSPACES[grid] = (n, n_sub)
+        except TypeError:
+            pass
     s_pad = -(-n_sub // 32) * 32
     products = min(mpad * s_pad * 12, 64 << 30)
     return int(mpad * d * 16 + npad * d * 32 + 12 * npad * 8 + 4 * mpad * 8 + products)
