@@ -208,3 +208,17 @@ def test_pool_server_keeps_admitting_after_a_footprint_error():
     with pytest.raises(ValueError, match="request 2"):
         srv.run(_requests(6))
     assert sorted(srv.order) == list(range(6))  # every request still ran, in order
+
+
+def test_request_footprint_recounts_a_grid_that_grew():
+    grid = sg.Grid.createLinearGrid(2)
+    grid.getGenerator().regular(2)
+    before = serving.request_footprint(grid, 5000)
+    n_sub_before = serving._SUBSPACES[grid][1]
+    for _ in range(3):  # the same object, more points and subspaces
+        alpha = np.ones(grid.getSize())
+        grid.getGenerator().refine(sg.SurplusRefinementFunctor(alpha, grid.getSize(), 0.0))
+    after = serving.request_footprint(grid, 5000)
+    assert serving._SUBSPACES[grid] == (grid.getSize(), serving._SUBSPACES[grid][1])
+    # the count was redone (3 -> 15 subspaces; both pad to 32, so the bytes may stay the same)
+    assert serving._SUBSPACES[grid][1] > n_sub_before and after >= before
